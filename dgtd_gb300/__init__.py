@@ -1,0 +1,316 @@
+"""dgtd_gb300 — GB300-native DG time-domain Maxwell step (Python binding).
+
+The product is the CUDA shared library ``libdgtd_gb300.so`` built from
+``dgtd_gb300/csrc`` (C ABI in ``include/dgtd_gb300.h``). This module is a thin
+ctypes binding over it, used by the tests and the benchmark; there is no
+Python or CPU compute path. Loading fails loudly when the library is missing.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass, field
+from pathlib import Path
+from typing import Optional, Sequence
+
+import numpy as np
+
+_PKG = Path(__file__).resolve().parent
+LIB_PATH = _PKG / "libdgtd_gb300.so"
+
+DGTD_OK = 0
+BC_OPEN, BC_PEC, BC_PMC, BC_SMA = 0, 1, 2, 3
+FP64, FP32_3XTF32 = 0, 1
+RK4, LSERK4 = 0, 1
+
+
+class DgtdError(RuntimeError):
+    pass
+
+
+class MeshDesc(C.Structure):
+    _fields_ = [
+        ("dim", C.c_int32),
+        ("n_vertices", C.c_int64), ("vertices", C.POINTER(C.c_double)),
+        ("n_elements", C.c_int64), ("elements", C.POINTER(C.c_int32)),
+        ("eps_r", C.POINTER(C.c_double)), ("mu_r", C.POINTER(C.c_double)), ("sigma", C.POINTER(C.c_double)),
+        ("n_bdr_faces", C.c_int64), ("bdr_faces", C.POINTER(C.c_int32)), ("bdr_codes", C.POINTER(C.c_int32)),
+        ("n_tfsf_faces", C.c_int64), ("tfsf_faces", C.POINTER(C.c_int32)),
+        ("n_int_faces", C.c_int64), ("int_faces", C.POINTER(C.c_int32)), ("int_codes", C.POINTER(C.c_int32)),
+    ]
+
+
+class OpOpts(C.Structure):
+    _fields_ = [("order", C.c_int32), ("alpha", C.c_double), ("precision", C.c_int32), ("batch", C.c_int32)]
+
+
+class PlaneWave(C.Structure):
+    _fields_ = [("propagation", C.c_double * 3), ("polarization", C.c_double * 3), ("spread", C.c_double),
+                ("mean", C.c_double), ("frequency", C.c_double), ("batch", C.c_int32)]
+
+
+class OpInfo(C.Structure):
+    _fields_ = [("n_elements", C.c_int64), ("order", C.c_int32), ("np", C.c_int32), ("nfp", C.c_int32),
+                ("batch", C.c_int32), ("precision", C.c_int32), ("ndofs", C.c_int64), ("state_len", C.c_int64),
+                ("n_tfsf_faces", C.c_int64), ("min_edge", C.c_double), ("dt_scale_min", C.c_double),
+                ("device_bytes", C.c_int64)]
+
+
+class BoxSpec(C.Structure):
+    _fields_ = [("n", C.c_int32 * 3), ("lo", C.c_double * 3), ("hi", C.c_double * 3),
+                ("hole_lo", C.c_int32 * 3), ("hole_hi", C.c_int32 * 3),
+                ("tf_lo", C.c_int32 * 3), ("tf_hi", C.c_int32 * 3),
+                ("outer_bc", C.c_int32), ("hole_bc", C.c_int32)]
+
+
+_lib_handle: Optional[C.CDLL] = None
+
+# Every symbol the C ABI declares, with (restype, argtypes).
+_P = C.c_void_p
+_D = C.POINTER(C.c_double)
+_I32 = C.POINTER(C.c_int32)
+_I64 = C.POINTER(C.c_int64)
+SIGNATURES = {
+    "dgtd_last_error": (C.c_char_p, []),
+    "dgtd_op_create": (C.c_int, [C.POINTER(MeshDesc), C.POINTER(OpOpts), C.POINTER(_P)]),
+    "dgtd_op_destroy": (None, [_P]),
+    "dgtd_op_get_info": (C.c_int, [_P, C.POINTER(OpInfo)]),
+    "dgtd_op_node_coords": (C.c_int, [_P, _D]),
+    "dgtd_op_set_planewaves": (C.c_int, [_P, C.POINTER(PlaneWave), C.c_int32]),
+    "dgtd_op_mult": (C.c_int, [_P, _P, _P, C.c_double, _P]),
+    "dgtd_op_mult_host": (C.c_int, [_P, _D, _D, C.c_double]),
+    "dgtd_op_step": (C.c_int, [_P, _P, C.c_double, C.c_double, C.c_int32, C.c_int32, _P]),
+    "dgtd_op_run_host": (C.c_int, [_P, _D, C.c_double, C.c_double, C.c_double, C.c_int32, _I64]),
+    "dgtd_op_norm2": (C.c_int, [_P, _P, _D, _P]),
+    "dgtd_op_estimate_dt": (C.c_int, [_P, C.c_double, _D]),
+    "dgtd_box_mesh_size": (C.c_int, [C.POINTER(BoxSpec), _I64, _I64, _I64, _I64]),
+    "dgtd_box_mesh_fill": (C.c_int, [C.POINTER(BoxSpec), _D, _I32, _I32, _I32, _I32]),
+    "dgtd_ref_tet": (C.c_int, [C.c_int32, _D, _D, _D, _D, _D, _D, _D, _D, _I32]),
+    "dgtd_mesh_validate": (C.c_int, [C.POINTER(MeshDesc), C.POINTER(OpOpts), C.POINTER(OpInfo)]),
+}
+
+
+def lib() -> C.CDLL:
+    """Load the CUDA library (raises if it was not built)."""
+    global _lib_handle
+    if _lib_handle is None:
+        if not LIB_PATH.exists():
+            raise ImportError(f"{LIB_PATH} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`")
+        h = C.CDLL(str(LIB_PATH))
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(h, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib_handle = h
+    return _lib_handle
+
+
+def _check(rc: int, what: str) -> None:
+    if rc != DGTD_OK:
+        msg = lib().dgtd_last_error().decode(errors="replace")
+        raise DgtdError(f"{what} failed ({rc}): {msg}")
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(_D)
+
+
+def _ip(a: np.ndarray):
+    return a.ctypes.data_as(_I32)
+
+
+@dataclass
+class Mesh:
+    """Flat mesh tables (vertices [nv,3], tets [ne,4], boundary/TF-SF faces)."""
+    vertices: np.ndarray
+    elements: np.ndarray
+    bdr_faces: np.ndarray = field(default_factory=lambda: np.zeros((0, 3), np.int32))
+    bdr_codes: np.ndarray = field(default_factory=lambda: np.zeros((0,), np.int32))
+    tfsf_faces: np.ndarray = field(default_factory=lambda: np.zeros((0, 3), np.int32))
+    int_faces: np.ndarray = field(default_factory=lambda: np.zeros((0, 3), np.int32))
+    int_codes: np.ndarray = field(default_factory=lambda: np.zeros((0,), np.int32))
+    eps: Optional[np.ndarray] = None
+    mu: Optional[np.ndarray] = None
+    sigma: Optional[np.ndarray] = None
+    dim: int = 3
+
+    @property
+    def n_elements(self) -> int:
+        return int(self.elements.shape[0])
+
+    def normalized(self) -> "Mesh":
+        f64 = lambda a: None if a is None else np.ascontiguousarray(a, dtype=np.float64)
+        i32 = lambda a: np.ascontiguousarray(a, dtype=np.int32)
+        return Mesh(f64(self.vertices), i32(self.elements), i32(self.bdr_faces).reshape(-1, 3),
+                    i32(self.bdr_codes).reshape(-1), i32(self.tfsf_faces).reshape(-1, 3),
+                    i32(self.int_faces).reshape(-1, 3), i32(self.int_codes).reshape(-1),
+                    f64(self.eps), f64(self.mu), f64(self.sigma), self.dim)
+
+
+def box_mesh(n: Sequence[int], lo=(0.0, 0.0, 0.0), hi=(1.0, 1.0, 1.0), hole=None, tfsf=None,
+             outer_bc: int = BC_PEC, hole_bc: int = BC_PEC) -> Mesh:
+    """Structured box of n[0] x n[1] x n[2] hexes, each split into 6 tets.
+
+    hole / tfsf: ((i0, j0, k0), (i1, j1, k1)) cell-index ranges (half open).
+    """
+    s = BoxSpec()
+    for d in range(3):
+        s.n[d] = int(n[d]); s.lo[d] = float(lo[d]); s.hi[d] = float(hi[d])
+        if hole is not None:
+            s.hole_lo[d] = int(hole[0][d]); s.hole_hi[d] = int(hole[1][d])
+        if tfsf is not None:
+            s.tf_lo[d] = int(tfsf[0][d]); s.tf_hi[d] = int(tfsf[1][d])
+    s.outer_bc = outer_bc; s.hole_bc = hole_bc
+    nv, ne, nb, nt = C.c_int64(), C.c_int64(), C.c_int64(), C.c_int64()
+    L = lib()
+    _check(L.dgtd_box_mesh_size(C.byref(s), C.byref(nv), C.byref(ne), C.byref(nb), C.byref(nt)), "box_mesh_size")
+    V = np.zeros((nv.value, 3)); E = np.zeros((ne.value, 4), np.int32)
+    BF = np.zeros((nb.value, 3), np.int32); BC = np.zeros((nb.value,), np.int32)
+    TF = np.zeros((nt.value, 3), np.int32)
+    _check(L.dgtd_box_mesh_fill(C.byref(s), _dp(V), _ip(E), _ip(BF), _ip(BC), _ip(TF)), "box_mesh_fill")
+    return Mesh(V, E, BF, BC, TF)
+
+
+def ref_tet(order: int) -> dict:
+    """The product's reference-element tables (host), for known-answer tests."""
+    np_ = (order + 1) * (order + 2) * (order + 3) // 6
+    nfp = (order + 1) * (order + 2) // 2
+    out = {k: np.zeros(np_) for k in ("r", "s", "t")}
+    for k in ("Dr", "Ds", "Dt", "Minv"):
+        out[k] = np.zeros((np_, np_))
+    out["LIFT"] = np.zeros((np_, 4 * nfp))
+    out["Fmask"] = np.zeros((4, nfp), np.int32)
+    _check(lib().dgtd_ref_tet(order, *(_dp(out[k]) for k in ("r", "s", "t", "Dr", "Ds", "Dt", "Minv", "LIFT")),
+                              _ip(out["Fmask"])), "ref_tet")
+    return out
+
+
+def _ptr(x) -> int:
+    """Device pointer of a torch tensor or a raw integer address."""
+    if isinstance(x, int):
+        return x
+    if hasattr(x, "data_ptr"):
+        return int(x.data_ptr())
+    raise TypeError("expected a torch CUDA tensor or a device address")
+
+
+def _stream(s) -> Optional[int]:
+    if s is None:
+        return None
+    if isinstance(s, int):
+        return s
+    return int(s.cuda_stream) if hasattr(s, "cuda_stream") else int(s)
+
+
+def _mesh_desc(m: Mesh) -> MeshDesc:
+    d = MeshDesc()
+    d.dim = 3
+    d.n_vertices = m.vertices.shape[0]; d.vertices = _dp(m.vertices)
+    d.n_elements = m.elements.shape[0]; d.elements = _ip(m.elements)
+    null_d = C.POINTER(C.c_double)()
+    d.eps_r = _dp(m.eps) if m.eps is not None else null_d
+    d.mu_r = _dp(m.mu) if m.mu is not None else null_d
+    d.sigma = _dp(m.sigma) if m.sigma is not None else null_d
+    d.n_bdr_faces = m.bdr_codes.shape[0]; d.bdr_faces = _ip(m.bdr_faces); d.bdr_codes = _ip(m.bdr_codes)
+    d.n_tfsf_faces = m.tfsf_faces.shape[0]; d.tfsf_faces = _ip(m.tfsf_faces)
+    d.n_int_faces = m.int_codes.shape[0]; d.int_faces = _ip(m.int_faces); d.int_codes = _ip(m.int_codes)
+    return d
+
+
+def validate_mesh(mesh: Mesh, order: int = 3, batch: int = 1) -> dict:
+    """Build the mesh tables on the host only (no GPU) and return the op info."""
+    m = mesh.normalized()
+    d = _mesh_desc(m)
+    o = OpOpts(order=order, alpha=1.0, precision=FP64, batch=batch)
+    inf = OpInfo()
+    _check(lib().dgtd_mesh_validate(C.byref(d), C.byref(o), C.byref(inf)), "dgtd_mesh_validate")
+    return {k: getattr(inf, k) for k, _ in OpInfo._fields_}
+
+
+class Operator:
+    """DG Maxwell evolution operator on the GPU (the reference's
+    ``GlobalEvolution : mfem::TimeDependentOperator``, GlobalEvolution.h:14-111).
+
+    ``mult(x, y, t)`` is ``Mult`` with ``SetTime(t)``; ``step`` fuses the RK
+    stages; all compute runs in the CUDA library.
+    """
+
+    def __init__(self, mesh: Mesh, order: int = 3, alpha: float = 1.0, precision: int = FP64, batch: int = 1):
+        m = mesh.normalized()
+        self._keep = m
+        d = _mesh_desc(m)
+        o = OpOpts(order=order, alpha=alpha, precision=precision, batch=batch)
+        h = C.c_void_p()
+        _check(lib().dgtd_op_create(C.byref(d), C.byref(o), C.byref(h)), "dgtd_op_create")
+        self._h = h
+        inf = OpInfo()
+        _check(lib().dgtd_op_get_info(self._h, C.byref(inf)), "get_info")
+        self.info = {k: getattr(inf, k) for k, _ in OpInfo._fields_}
+        self.order = order
+        self.batch = batch
+        self.precision = precision
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) and self._h.value:
+            lib().dgtd_op_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def state_len(self) -> int:
+        return int(self.info["state_len"])
+
+    @property
+    def ndofs(self) -> int:
+        return int(self.info["ndofs"])
+
+    def node_coords(self) -> np.ndarray:
+        xyz = np.zeros((3, self.ndofs))
+        _check(lib().dgtd_op_node_coords(self._h, _dp(xyz)), "node_coords")
+        return xyz
+
+    def set_planewaves(self, waves: Sequence[dict]) -> None:
+        arr = (PlaneWave * max(1, len(waves)))()
+        for i, w in enumerate(waves):
+            arr[i].propagation[:] = list(map(float, w["propagation"]))
+            arr[i].polarization[:] = list(map(float, w["polarization"]))
+            arr[i].spread = float(w["spread"]); arr[i].mean = float(w["mean"])
+            arr[i].frequency = float(w.get("frequency", 0.0)); arr[i].batch = int(w.get("batch", 0))
+        _check(lib().dgtd_op_set_planewaves(self._h, arr, len(waves)), "set_planewaves")
+
+    def estimate_dt(self, cfl: float = 1.0) -> float:
+        v = C.c_double()
+        _check(lib().dgtd_op_estimate_dt(self._h, cfl, C.byref(v)), "estimate_dt")
+        return v.value
+
+    # -- device API (torch tensors or raw device addresses)
+    def mult(self, x, y, t: float = 0.0, stream=None) -> None:
+        _check(lib().dgtd_op_mult(self._h, _ptr(x), _ptr(y), float(t), _stream(stream)), "dgtd_op_mult")
+
+    def step(self, state, t0: float, dt: float, nsteps: int, integrator: int = RK4, stream=None) -> None:
+        _check(lib().dgtd_op_step(self._h, _ptr(state), float(t0), float(dt), int(nsteps), int(integrator),
+                                  _stream(stream)), "dgtd_op_step")
+
+    def norm2(self, state, stream=None) -> np.ndarray:
+        out = np.zeros(self.batch)
+        _check(lib().dgtd_op_norm2(self._h, _ptr(state), _dp(out), _stream(stream)), "dgtd_op_norm2")
+        return out
+
+    # -- host API
+    def mult_host(self, x: np.ndarray, t: float = 0.0) -> np.ndarray:
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        y = np.zeros_like(x)
+        _check(lib().dgtd_op_mult_host(self._h, _dp(x), _dp(y), float(t)), "dgtd_op_mult_host")
+        return y
+
+    def run_host(self, x: np.ndarray, t0: float, dt: float, final_time: float, integrator: int = RK4):
+        x = np.array(x, dtype=np.float64, copy=True)
+        n = C.c_int64()
+        _check(lib().dgtd_op_run_host(self._h, _dp(x), float(t0), float(dt), float(final_time), int(integrator),
+                                      C.byref(n)), "dgtd_op_run_host")
+        return x, int(n.value)

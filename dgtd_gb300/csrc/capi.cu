@@ -1,0 +1,557 @@
+// C ABI of the DG Maxwell step: operator life cycle, Mult, fused stepping.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/dgtd_gb300.h"
+#include "batched.hpp"
+#include "kernels.hpp"
+#include "mesh.hpp"
+#include "refelem.hpp"
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg)
+{
+    g_err = msg;
+    return code;
+}
+
+struct CudaError : std::runtime_error {
+    using std::runtime_error::runtime_error;
+};
+
+void ck(cudaError_t e, const char* what)
+{
+    if (e != cudaSuccess) throw CudaError(std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+template <typename T>
+T* upload(const std::vector<T>& v, int64_t& bytes)
+{
+    if (v.empty()) return nullptr;
+    T* d = nullptr;
+    ck(cudaMalloc(&d, v.size() * sizeof(T)), "cudaMalloc");
+    ck(cudaMemcpy(d, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice), "cudaMemcpy H2D");
+    bytes += static_cast<int64_t>(v.size() * sizeof(T));
+    return d;
+}
+
+// LSERK4 coefficients (Carpenter & Kennedy 1994, 5-stage, 4th order, 2N storage).
+const double kRk4a[5] = {0.0, -567301805773.0 / 1357537059087.0, -2404267990393.0 / 2016746695238.0,
+                         -3550918686646.0 / 2091501179385.0, -1275806237668.0 / 842570457699.0};
+const double kRk4b[5] = {1432997174477.0 / 9575080441755.0, 5161836677717.0 / 13612068292357.0,
+                         1720146321549.0 / 2090206949498.0, 3134564353537.0 / 4481467310338.0,
+                         2277821191437.0 / 14882151754819.0};
+const double kRk4c[5] = {0.0, 1432997174477.0 / 9575080441755.0, 2526269341429.0 / 6820363962896.0,
+                         2006345519317.0 / 3224310063776.0, 2802321613138.0 / 2924317926251.0};
+
+}  // namespace
+
+struct dgtd_op {
+    dgtd::RefTet ref;
+    dgtd::MeshTables mesh;
+    dgtd::TablesDev dev{};
+    int batch = 1;
+    int precision = DGTD_FP64;
+    double alpha = 1.0;
+    int64_t device_bytes = 0;
+    int64_t state_len = 0;
+    int64_t n_tfsf_faces = 0;
+    std::vector<void*> allocs;
+    // sources
+    std::vector<dgtd::PlaneWaveDev> pw_host;
+    dgtd::PlaneWaveDev* pw_dev = nullptr;
+    int pw_cap = 0;
+    int* skip_dev = nullptr;
+    double* norm_dev = nullptr;
+    // RK scratch (allocated on first dgtd_op_step)
+    double* ws = nullptr;
+    int64_t ws_len = 0;
+    // batched FP32 form
+    std::unique_ptr<dgtd::BatchedOp> batched;
+
+    ~dgtd_op()
+    {
+        for (void* p : allocs) cudaFree(p);
+        if (pw_dev) cudaFree(pw_dev);
+        if (skip_dev) cudaFree(skip_dev);
+        if (norm_dev) cudaFree(norm_dev);
+        if (ws) cudaFree(ws);
+    }
+    template <typename T>
+    T* up(const std::vector<T>& v)
+    {
+        T* d = upload(v, device_bytes);
+        if (d) allocs.push_back(d);
+        return d;
+    }
+};
+
+namespace {
+
+dgtd::MeshInput to_input(const dgtd_mesh_desc* m)
+{
+    if (!m) throw std::invalid_argument("mesh descriptor is NULL");
+    if (m->dim != 3) throw std::invalid_argument("only dim = 3 tetrahedral meshes are supported");
+    if (m->n_vertices <= 0 || !m->vertices) throw std::invalid_argument("mesh has no vertices");
+    if (m->n_elements <= 0 || !m->elements) throw std::invalid_argument("mesh has no elements");
+    dgtd::MeshInput in;
+    in.dim = 3;
+    in.vertices.assign(m->vertices, m->vertices + 3 * m->n_vertices);
+    in.elements.assign(m->elements, m->elements + 4 * m->n_elements);
+    if (m->eps_r) in.eps.assign(m->eps_r, m->eps_r + m->n_elements);
+    if (m->mu_r) in.mu.assign(m->mu_r, m->mu_r + m->n_elements);
+    if (m->sigma) in.sigma.assign(m->sigma, m->sigma + m->n_elements);
+    if (m->n_bdr_faces > 0) {
+        if (!m->bdr_faces || !m->bdr_codes) throw std::invalid_argument("boundary faces without arrays");
+        in.bdr_faces.assign(m->bdr_faces, m->bdr_faces + 3 * m->n_bdr_faces);
+        in.bdr_codes.assign(m->bdr_codes, m->bdr_codes + m->n_bdr_faces);
+    }
+    if (m->n_tfsf_faces > 0) {
+        if (!m->tfsf_faces) throw std::invalid_argument("TF/SF faces without array");
+        in.tfsf_faces.assign(m->tfsf_faces, m->tfsf_faces + 3 * m->n_tfsf_faces);
+    }
+    if (m->n_int_faces > 0) {
+        if (!m->int_faces || !m->int_codes) throw std::invalid_argument("interior faces without arrays");
+        in.int_faces.assign(m->int_faces, m->int_faces + 3 * m->n_int_faces);
+        in.int_codes.assign(m->int_codes, m->int_codes + m->n_int_faces);
+    }
+    return in;
+}
+
+std::vector<double> transpose(const std::vector<double>& a, int rows, int cols)
+{
+    std::vector<double> t(a.size());
+    for (int i = 0; i < rows; ++i)
+        for (int j = 0; j < cols; ++j) t[static_cast<size_t>(j) * rows + i] = a[static_cast<size_t>(i) * cols + j];
+    return t;
+}
+
+void ensure_sources(dgtd_op* op)
+{
+    int n = static_cast<int>(op->pw_host.size());
+    if (n > op->pw_cap) {
+        if (op->pw_dev) cudaFree(op->pw_dev);
+        op->pw_dev = nullptr;
+        ck(cudaMalloc(&op->pw_dev, n * sizeof(dgtd::PlaneWaveDev)), "cudaMalloc sources");
+        op->pw_cap = n;
+    }
+    if (n > 0)
+        ck(cudaMemcpy(op->pw_dev, op->pw_host.data(), n * sizeof(dgtd::PlaneWaveDev), cudaMemcpyHostToDevice),
+           "cudaMemcpy sources");
+}
+
+bool has_sources(const dgtd_op* op) { return op->mesh.tfsf_elems.size() > 0 && !op->pw_host.empty(); }
+
+// One fused stage on the plain FP64 form.
+void run_stage(dgtd_op* op, dgtd::StageArgs A, double t, cudaStream_t s)
+{
+    A.t = t;
+    A.batch = op->batch;
+    if (has_sources(op)) {
+        ck(dgtd::launch_tfsf_skip(op->dev, op->pw_dev, static_cast<int>(op->pw_host.size()), op->batch, t,
+                                  op->skip_dev, s),
+           "tfsf skip kernel");
+        A.pw = op->pw_dev;
+        A.n_pw = static_cast<int>(op->pw_host.size());
+        A.skip = op->skip_dev;
+    } else {
+        A.pw = nullptr;
+        A.n_pw = 0;
+        A.skip = nullptr;
+    }
+    ck(dgtd::launch_stage_fp64(op->dev, A, s), "stage kernel");
+}
+
+void ensure_ws(dgtd_op* op)
+{
+    int64_t need = 3 * op->state_len;
+    if (op->ws_len >= need) return;
+    if (op->ws) cudaFree(op->ws);
+    op->ws = nullptr;
+    op->ws_len = 0;
+    ck(cudaMalloc(&op->ws, need * sizeof(double)), "cudaMalloc RK scratch");
+    op->ws_len = need;
+}
+
+// One RK step of size dt at time t on d_x (device) using the op's scratch.
+void rk_step(dgtd_op* op, double* d_x, double t, double dt, int integrator, double* lsrk_other, double*& cur,
+             cudaStream_t s)
+{
+    const int64_t L = op->state_len;
+    if (integrator == DGTD_RK4) {
+        double* y0 = op->ws;
+        double* y1 = op->ws + L;
+        double* z = op->ws + 2 * L;
+        dgtd::StageArgs A{};
+        A.dt = dt;
+        A.x = d_x;
+        A.z = z;
+        A.mode = dgtd::MODE_RK4_1; A.in = d_x; A.yout = y0; run_stage(op, A, t, s);
+        A.mode = dgtd::MODE_RK4_2; A.in = y0; A.yout = y1; run_stage(op, A, t + dt / 2, s);
+        A.mode = dgtd::MODE_RK4_3; A.in = y1; A.yout = y0; run_stage(op, A, t + dt / 2, s);
+        A.mode = dgtd::MODE_RK4_4; A.in = y0; A.yout = nullptr; run_stage(op, A, t + dt, s);
+    } else {
+        double* res = op->ws + 2 * L;
+        for (int st = 0; st < 5; ++st) {
+            double* nxt = (cur == d_x) ? lsrk_other : d_x;
+            dgtd::StageArgs A{};
+            A.dt = dt;
+            A.mode = dgtd::MODE_LSRK;
+            A.in = cur;
+            A.yout = nxt;
+            A.res = res;
+            A.a = kRk4a[st];
+            A.b = kRk4b[st];
+            run_stage(op, A, t + kRk4c[st] * dt, s);
+            cur = nxt;
+        }
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* dgtd_last_error(void) { return g_err.c_str(); }
+
+int dgtd_op_create(const dgtd_mesh_desc* mesh, const dgtd_op_opts* opts, dgtd_op** out)
+{
+    if (!out) return fail(DGTD_ERR_INVALID, "out pointer is NULL");
+    *out = nullptr;
+    if (!opts) return fail(DGTD_ERR_INVALID, "options are NULL");
+    if (opts->order < 1 || opts->order > 6) return fail(DGTD_ERR_UNSUPPORTED, "order must be in [1, 6]");
+    if (opts->batch < 1) return fail(DGTD_ERR_INVALID, "batch must be >= 1");
+    if (opts->precision != DGTD_FP64 && opts->precision != DGTD_FP32_3XTF32)
+        return fail(DGTD_ERR_INVALID, "unknown precision form");
+    if (!(opts->alpha >= 0.0)) return fail(DGTD_ERR_INVALID, "alpha must be >= 0");
+    std::unique_ptr<dgtd_op> op;
+    try {
+        op = std::make_unique<dgtd_op>();
+        op->ref = dgtd::build_ref_tet(opts->order);
+        op->mesh = dgtd::build_tables(to_input(mesh), op->ref);
+        op->batch = opts->batch;
+        op->precision = opts->precision;
+        op->alpha = opts->alpha;
+        const int Np = op->ref.Np, Nfp = op->ref.Nfp;
+        op->state_len = 6 * op->mesh.K * Np * static_cast<int64_t>(op->batch);
+        for (auto c : op->mesh.fcode)
+            if (c == dgtd::FACE_TFSF_TF || c == dgtd::FACE_TFSF_SF) ++op->n_tfsf_faces;
+
+        dgtd::TablesDev& T = op->dev;
+        T.p = opts->order; T.Np = Np; T.Nfp = Nfp; T.K = op->mesh.K; T.N = op->mesh.K * Np;
+        T.alpha = opts->alpha;
+        T.DrT = op->up(transpose(op->ref.Dr, Np, Np));
+        T.DsT = op->up(transpose(op->ref.Ds, Np, Np));
+        T.DtT = op->up(transpose(op->ref.Dt, Np, Np));
+        T.LIFTT = op->up(transpose(op->ref.LIFT, Np, 4 * Nfp));
+        T.Fmask = op->up(op->ref.Fmask);
+        T.geo = op->up(op->mesh.geo);
+        T.fgeo = op->up(op->mesh.fgeo);
+        T.mat = op->up(op->mesh.mat);
+        T.vmapP = op->up(op->mesh.vmapP);
+        T.fcode = op->up(op->mesh.fcode);
+        std::vector<double> xyz;
+        xyz.reserve(3 * T.N);
+        xyz.insert(xyz.end(), op->mesh.x.begin(), op->mesh.x.end());
+        xyz.insert(xyz.end(), op->mesh.y.begin(), op->mesh.y.end());
+        xyz.insert(xyz.end(), op->mesh.z.begin(), op->mesh.z.end());
+        T.xyz = op->up(xyz);
+        T.tfsf_elems = op->up(op->mesh.tfsf_elems);
+        T.n_tfsf_elems = static_cast<int64_t>(op->mesh.tfsf_elems.size());
+        ck(cudaMalloc(&op->skip_dev, op->batch * sizeof(int)), "cudaMalloc skip");
+        ck(cudaMalloc(&op->norm_dev, op->batch * sizeof(double)), "cudaMalloc norm");
+        if (op->precision == DGTD_FP32_3XTF32) op->batched = dgtd::BatchedOp::create(op->ref, op->mesh, op->dev, op->batch);
+    } catch (const CudaError& e) {
+        return fail(DGTD_ERR_CUDA, e.what());
+    } catch (const std::bad_alloc&) {
+        return fail(DGTD_ERR_NOMEM, "host allocation failed");
+    } catch (const std::exception& e) {
+        return fail(DGTD_ERR_INVALID, e.what());
+    }
+    *out = op.release();
+    return DGTD_OK;
+}
+
+void dgtd_op_destroy(dgtd_op* op) { delete op; }
+
+int dgtd_op_get_info(const dgtd_op* op, dgtd_op_info* info)
+{
+    if (!op || !info) return fail(DGTD_ERR_INVALID, "NULL argument");
+    info->n_elements = op->mesh.K;
+    info->order = op->ref.p;
+    info->np = op->ref.Np;
+    info->nfp = op->ref.Nfp;
+    info->batch = op->batch;
+    info->precision = op->precision;
+    info->ndofs = op->mesh.K * op->ref.Np;
+    info->state_len = op->state_len;
+    info->n_tfsf_faces = op->n_tfsf_faces;
+    info->min_edge = op->mesh.min_edge;
+    info->dt_scale_min = op->mesh.dt_scale_min;
+    info->device_bytes = op->device_bytes + (op->batched ? op->batched->device_bytes() : 0);
+    return DGTD_OK;
+}
+
+int dgtd_op_node_coords(const dgtd_op* op, double* h_xyz)
+{
+    if (!op || !h_xyz) return fail(DGTD_ERR_INVALID, "NULL argument");
+    const int64_t N = op->mesh.K * op->ref.Np;
+    std::memcpy(h_xyz, op->mesh.x.data(), N * sizeof(double));
+    std::memcpy(h_xyz + N, op->mesh.y.data(), N * sizeof(double));
+    std::memcpy(h_xyz + 2 * N, op->mesh.z.data(), N * sizeof(double));
+    return DGTD_OK;
+}
+
+int dgtd_op_set_planewaves(dgtd_op* op, const dgtd_planewave* pw, int32_t n)
+{
+    if (!op) return fail(DGTD_ERR_INVALID, "NULL operator");
+    if (n < 0 || (n > 0 && !pw)) return fail(DGTD_ERR_INVALID, "bad source array");
+    std::vector<dgtd::PlaneWaveDev> v;
+    for (int i = 0; i < n; ++i) {
+        const dgtd_planewave& s = pw[i];
+        if (s.batch < 0 || s.batch >= op->batch) return fail(DGTD_ERR_INVALID, "source batch index out of range");
+        if (!(s.spread > 0.0)) return fail(DGTD_ERR_INVALID, "source spread must be positive");
+        double kn = std::sqrt(s.propagation[0] * s.propagation[0] + s.propagation[1] * s.propagation[1] +
+                              s.propagation[2] * s.propagation[2]);
+        double pn = std::sqrt(s.polarization[0] * s.polarization[0] + s.polarization[1] * s.polarization[1] +
+                              s.polarization[2] * s.polarization[2]);
+        if (!(kn > 0.0) || !(pn > 0.0)) return fail(DGTD_ERR_INVALID, "zero propagation or polarization");
+        dgtd::PlaneWaveDev d{};
+        for (int c = 0; c < 3; ++c) { d.k[c] = s.propagation[c] / kn; d.pol[c] = s.polarization[c] / pn; }
+        d.kxp[0] = d.k[1] * d.pol[2] - d.k[2] * d.pol[1];
+        d.kxp[1] = d.k[2] * d.pol[0] - d.k[0] * d.pol[2];
+        d.kxp[2] = d.k[0] * d.pol[1] - d.k[1] * d.pol[0];
+        d.spread = s.spread;
+        d.mean = s.mean;
+        d.freq = s.frequency;
+        d.batch = s.batch;
+        v.push_back(d);
+    }
+    try {
+        op->pw_host = v;
+        ensure_sources(op);
+        if (op->batched) op->batched->set_sources(op->pw_host);
+    } catch (const std::exception& e) {
+        return fail(DGTD_ERR_CUDA, e.what());
+    }
+    return DGTD_OK;
+}
+
+int dgtd_op_mult(dgtd_op* op, const double* d_x, double* d_y, double t, void* stream)
+{
+    if (!op || !d_x || !d_y) return fail(DGTD_ERR_INVALID, "NULL argument");
+    if (d_x == d_y) return fail(DGTD_ERR_INVALID, "x and y must not alias");
+    if (op->precision != DGTD_FP64) return fail(DGTD_ERR_UNSUPPORTED, "dgtd_op_mult is the FP64 form; use the batched API");
+    try {
+        dgtd::StageArgs A{};
+        A.mode = dgtd::MODE_MULT;
+        A.in = d_x;
+        A.out = d_y;
+        run_stage(op, A, t, static_cast<cudaStream_t>(stream));
+    } catch (const std::exception& e) {
+        return fail(DGTD_ERR_CUDA, e.what());
+    }
+    return DGTD_OK;
+}
+
+int dgtd_op_mult_host(dgtd_op* op, const double* h_x, double* h_y, double t)
+{
+    if (!op || !h_x || !h_y) return fail(DGTD_ERR_INVALID, "NULL argument");
+    double *dx = nullptr, *dy = nullptr;
+    const size_t bytes = op->state_len * sizeof(double);
+    int rc = DGTD_OK;
+    try {
+        ck(cudaMalloc(&dx, bytes), "cudaMalloc");
+        ck(cudaMalloc(&dy, bytes), "cudaMalloc");
+        ck(cudaMemcpy(dx, h_x, bytes, cudaMemcpyHostToDevice), "H2D");
+        rc = dgtd_op_mult(op, dx, dy, t, nullptr);
+        if (rc == DGTD_OK) {
+            ck(cudaMemcpy(h_y, dy, bytes, cudaMemcpyDeviceToHost), "D2H");
+        }
+    } catch (const std::exception& e) {
+        rc = fail(DGTD_ERR_CUDA, e.what());
+    }
+    if (dx) cudaFree(dx);
+    if (dy) cudaFree(dy);
+    return rc;
+}
+
+int dgtd_op_step(dgtd_op* op, double* d_state, double t0, double dt, int32_t nsteps, int32_t integrator, void* stream)
+{
+    if (!op || !d_state) return fail(DGTD_ERR_INVALID, "NULL argument");
+    if (nsteps < 0) return fail(DGTD_ERR_INVALID, "nsteps must be >= 0");
+    if (integrator != DGTD_RK4 && integrator != DGTD_LSERK4) return fail(DGTD_ERR_INVALID, "unknown integrator");
+    if (op->precision != DGTD_FP64) return fail(DGTD_ERR_UNSUPPORTED, "dgtd_op_step is the FP64 form; use the batched API");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    try {
+        ensure_ws(op);
+        double* other = op->ws;   // LSERK4 second state buffer
+        double* cur = d_state;
+        if (integrator == DGTD_LSERK4)
+            ck(cudaMemsetAsync(op->ws + 2 * op->state_len, 0, op->state_len * sizeof(double), s), "memset");
+        double t = t0;
+        for (int i = 0; i < nsteps; ++i) {
+            rk_step(op, d_state, t, dt, integrator, other, cur, s);
+            t += dt;
+        }
+        if (integrator == DGTD_LSERK4 && cur != d_state)
+            ck(cudaMemcpyAsync(d_state, cur, op->state_len * sizeof(double), cudaMemcpyDeviceToDevice, s), "copy");
+    } catch (const std::exception& e) {
+        return fail(DGTD_ERR_CUDA, e.what());
+    }
+    return DGTD_OK;
+}
+
+int dgtd_op_run_host(dgtd_op* op, double* h_state, double t0, double dt, double final_time, int32_t integrator,
+                     int64_t* steps_out)
+{
+    if (!op || !h_state) return fail(DGTD_ERR_INVALID, "NULL argument");
+    if (!(dt > 0.0)) return fail(DGTD_ERR_INVALID, "dt must be positive");
+    if (op->precision != DGTD_FP64) return fail(DGTD_ERR_UNSUPPORTED, "dgtd_op_run_host is the FP64 form");
+    double* d = nullptr;
+    const size_t bytes = op->state_len * sizeof(double);
+    int rc = DGTD_OK;
+    int64_t steps = 0;
+    try {
+        ck(cudaMalloc(&d, bytes), "cudaMalloc");
+        ck(cudaMemcpy(d, h_state, bytes, cudaMemcpyHostToDevice), "H2D");
+        double t = t0;
+        while (t <= final_time - 1e-8 * dt) {
+            double truedt = std::min(dt, final_time - t);
+            rc = dgtd_op_step(op, d, t, truedt, 1, integrator, nullptr);
+            if (rc != DGTD_OK) break;
+            t += truedt;
+            ++steps;
+        }
+        if (rc == DGTD_OK) {
+            ck(cudaMemcpy(h_state, d, bytes, cudaMemcpyDeviceToHost), "D2H");
+        }
+    } catch (const std::exception& e) {
+        rc = fail(DGTD_ERR_CUDA, e.what());
+    }
+    if (d) cudaFree(d);
+    if (steps_out) *steps_out = steps;
+    return rc;
+}
+
+int dgtd_op_norm2(dgtd_op* op, const double* d_state, double* h_out, void* stream)
+{
+    if (!op || !d_state || !h_out) return fail(DGTD_ERR_INVALID, "NULL argument");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    try {
+        ck(dgtd::launch_norm2(d_state, op->state_len / op->batch, op->batch, op->norm_dev, s), "norm kernel");
+        ck(cudaMemcpyAsync(h_out, op->norm_dev, op->batch * sizeof(double), cudaMemcpyDeviceToHost, s), "D2H");
+        ck(cudaStreamSynchronize(s), "sync");
+    } catch (const std::exception& e) {
+        return fail(DGTD_ERR_CUDA, e.what());
+    }
+    return DGTD_OK;
+}
+
+int dgtd_op_estimate_dt(const dgtd_op* op, double cfl, double* dt_out)
+{
+    if (!op || !dt_out) return fail(DGTD_ERR_INVALID, "NULL argument");
+    if (!(cfl > 0.0)) return fail(DGTD_ERR_INVALID, "cfl must be positive");
+    auto g = dgtd::gauss_lobatto(op->ref.p);
+    const double rmin = std::fabs(g[1] - g[0]);   // GLL spacing on a segment of length 2
+    double dt = op->mesh.dt_scale_min * rmin * 2.0 / 3.0 * 0.75 * cfl;
+    *dt_out = dt / 0.8;
+    return DGTD_OK;
+}
+
+int dgtd_mesh_validate(const dgtd_mesh_desc* mesh, const dgtd_op_opts* opts, dgtd_op_info* info)
+{
+    if (!opts || !info) return fail(DGTD_ERR_INVALID, "NULL argument");
+    if (opts->order < 1 || opts->order > 6) return fail(DGTD_ERR_UNSUPPORTED, "order must be in [1, 6]");
+    try {
+        auto ref = dgtd::build_ref_tet(opts->order);
+        auto tab = dgtd::build_tables(to_input(mesh), ref);
+        std::memset(info, 0, sizeof(*info));
+        info->n_elements = tab.K;
+        info->order = ref.p; info->np = ref.Np; info->nfp = ref.Nfp;
+        info->batch = opts->batch; info->precision = opts->precision;
+        info->ndofs = tab.K * ref.Np;
+        info->state_len = 6 * tab.K * ref.Np * static_cast<int64_t>(std::max(1, opts->batch));
+        for (auto c : tab.fcode)
+            if (c == dgtd::FACE_TFSF_TF || c == dgtd::FACE_TFSF_SF) ++info->n_tfsf_faces;
+        info->min_edge = tab.min_edge;
+        info->dt_scale_min = tab.dt_scale_min;
+    } catch (const std::exception& e) {
+        return fail(DGTD_ERR_INVALID, e.what());
+    }
+    return DGTD_OK;
+}
+
+int dgtd_box_mesh_size(const dgtd_box_spec* spec, int64_t* nv, int64_t* ne, int64_t* nb, int64_t* nt)
+{
+    if (!spec) return fail(DGTD_ERR_INVALID, "NULL spec");
+    try {
+        dgtd::BoxSpec b;
+        for (int d = 0; d < 3; ++d) {
+            b.n[d] = spec->n[d]; b.lo[d] = spec->lo[d]; b.hi[d] = spec->hi[d];
+            b.hole_lo[d] = spec->hole_lo[d]; b.hole_hi[d] = spec->hole_hi[d];
+            b.tf_lo[d] = spec->tf_lo[d]; b.tf_hi[d] = spec->tf_hi[d];
+        }
+        b.outer_bc = spec->outer_bc; b.hole_bc = spec->hole_bc;
+        auto m = dgtd::make_box(b);
+        if (nv) *nv = static_cast<int64_t>(m.vertices.size() / 3);
+        if (ne) *ne = static_cast<int64_t>(m.elements.size() / 4);
+        if (nb) *nb = static_cast<int64_t>(m.bdr_codes.size());
+        if (nt) *nt = static_cast<int64_t>(m.tfsf_faces.size() / 3);
+    } catch (const std::exception& e) {
+        return fail(DGTD_ERR_INVALID, e.what());
+    }
+    return DGTD_OK;
+}
+
+int dgtd_box_mesh_fill(const dgtd_box_spec* spec, double* vertices, int32_t* elements, int32_t* bdr_faces,
+                       int32_t* bdr_codes, int32_t* tfsf_faces)
+{
+    if (!spec) return fail(DGTD_ERR_INVALID, "NULL spec");
+    try {
+        dgtd::BoxSpec b;
+        for (int d = 0; d < 3; ++d) {
+            b.n[d] = spec->n[d]; b.lo[d] = spec->lo[d]; b.hi[d] = spec->hi[d];
+            b.hole_lo[d] = spec->hole_lo[d]; b.hole_hi[d] = spec->hole_hi[d];
+            b.tf_lo[d] = spec->tf_lo[d]; b.tf_hi[d] = spec->tf_hi[d];
+        }
+        b.outer_bc = spec->outer_bc; b.hole_bc = spec->hole_bc;
+        auto m = dgtd::make_box(b);
+        if (vertices) std::memcpy(vertices, m.vertices.data(), m.vertices.size() * sizeof(double));
+        if (elements) std::memcpy(elements, m.elements.data(), m.elements.size() * sizeof(int32_t));
+        if (bdr_faces) std::memcpy(bdr_faces, m.bdr_faces.data(), m.bdr_faces.size() * sizeof(int32_t));
+        if (bdr_codes) std::memcpy(bdr_codes, m.bdr_codes.data(), m.bdr_codes.size() * sizeof(int32_t));
+        if (tfsf_faces) std::memcpy(tfsf_faces, m.tfsf_faces.data(), m.tfsf_faces.size() * sizeof(int32_t));
+    } catch (const std::exception& e) {
+        return fail(DGTD_ERR_INVALID, e.what());
+    }
+    return DGTD_OK;
+}
+
+int dgtd_ref_tet(int32_t order, double* r, double* s, double* t, double* Dr, double* Ds, double* Dt, double* Minv,
+                 double* lift, int32_t* fmask)
+{
+    try {
+        auto T = dgtd::build_ref_tet(order);
+        auto cp = [](double* dst, const std::vector<double>& v) {
+            if (dst) std::memcpy(dst, v.data(), v.size() * sizeof(double));
+        };
+        cp(r, T.r); cp(s, T.s); cp(t, T.t); cp(Dr, T.Dr); cp(Ds, T.Ds); cp(Dt, T.Dt); cp(Minv, T.Minv); cp(lift, T.LIFT);
+        if (fmask) for (size_t i = 0; i < T.Fmask.size(); ++i) fmask[i] = T.Fmask[i];
+    } catch (const std::exception& e) {
+        return fail(DGTD_ERR_INVALID, e.what());
+    }
+    return DGTD_OK;
+}
+
+}  // extern "C"

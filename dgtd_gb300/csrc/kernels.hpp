@@ -1,0 +1,81 @@
+// Device-side data structures and kernel launchers of the DG Maxwell step.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace dgtd {
+
+// One plane-wave source (reference: Planewave + Gaussian/ModulatedGaussian,
+// src/math/Function.h:45-143, 329-416; built by driver.cpp:483-519).
+// E = g(x.k - t) pol,  H = g(x.k - t) (k x pol),  g(s) = exp(-(s-mean)^2/(2 spread^2))
+// [* cos(2 pi freq (s - mean)) when freq != 0].
+struct PlaneWaveDev {
+    double k[3];
+    double pol[3];
+    double kxp[3];
+    double spread;
+    double mean;
+    double freq;
+    int batch;      // incidence index the source belongs to
+    int pad;
+};
+
+// Epilogue of the fused RHS kernel.
+enum StageMode : int {
+    MODE_MULT = 0,     // out = L(in)
+    MODE_RK4_1 = 1,    // y_out = x + dt/2 k ; z = x + dt/6 k           (in = x)
+    MODE_RK4_2 = 2,    // y_out = x + dt/2 k ; z += dt/3 k              (in = y)
+    MODE_RK4_3 = 3,    // y_out = x + dt k   ; z += dt/3 k              (in = y)
+    MODE_RK4_4 = 4,    // x = z + dt/6 k                                 (in = y)
+    MODE_LSRK = 5,     // res = a res + dt k ; u_out = u_in + b res      (in = u_in)
+};
+
+struct TablesDev {
+    int p, Np, Nfp;
+    int64_t K;
+    int64_t N;                 // K * Np
+    const double* DrT;         // [Np][Np] transposed
+    const double* DsT;
+    const double* DtT;
+    const double* LIFTT;       // [4 Nfp][Np] transposed
+    const int* Fmask;          // [4][Nfp]
+    const double* geo;         // [K][9]
+    const double* fgeo;        // [K][16]
+    const double* mat;         // [K][3]
+    const int32_t* vmapP;      // [K][4][Nfp]
+    const int32_t* fcode;      // [K][4]
+    const double* xyz;         // [3][N]
+    const int32_t* tfsf_elems; // [n_tfsf_elems]
+    int64_t n_tfsf_elems;
+    double alpha;
+};
+
+struct StageArgs {
+    const double* in;    // [B][6][N]
+    double* out;         // MULT output
+    double* x;           // RK4 base state
+    double* yout;        // RK4 stage output
+    double* z;           // RK4 accumulator
+    double* res;         // LSRK residual
+    double t;            // stage time
+    double dt;
+    double a, b;         // LSRK coefficients
+    int mode;
+    int batch;           // B
+    const PlaneWaveDev* pw;
+    int n_pw;
+    const int* skip;     // [B] TF/SF skip flags (nullptr: never skip)
+};
+
+// Launch the fused FP64 RHS + stage-update kernel for one stage.
+cudaError_t launch_stage_fp64(const TablesDev& T, const StageArgs& A, cudaStream_t s);
+
+// Per-incidence TF/SF skip decision (reference GlobalEvolution.cpp:587-598):
+// skip[b] = (sum over TF/SF-submesh nodes and components of (0.5 pw)^2 < 1e-16).
+cudaError_t launch_tfsf_skip(const TablesDev& T, const PlaneWaveDev* pw, int n_pw, int batch,
+                             double t, int* skip, cudaStream_t s);
+
+// Squared L2 norm of each incidence's state: out[b] = sum_i in[b][i]^2.
+cudaError_t launch_norm2(const double* in, int64_t n_per_batch, int batch, double* out, cudaStream_t s);
+
+}  // namespace dgtd

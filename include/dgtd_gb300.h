@@ -1,0 +1,194 @@
+/*
+ * dgtd_gb300 — C ABI of the GB300-native DG time-domain Maxwell step.
+ *
+ * This is the boundary that replaces the reference's evolution operator
+ * (class maxwell::GlobalEvolution : mfem::TimeDependentOperator,
+ * src/evolution/GlobalEvolution.h:14-111) and the time loop that drives it
+ * (maxwell::Solver::run/step, src/solver/Solver.cpp:483-551).
+ *
+ * Conventions
+ *  - Every call returns DGTD_OK (0) or a negative error code; no exception
+ *    crosses the ABI. dgtd_last_error() returns a thread-local message.
+ *  - State vectors use the reference layout (src/evolution/Fields.h:48-65):
+ *    [Ex | Ey | Ez | Hx | Hy | Hz], each block K*Np doubles, element-major,
+ *    nodes in the order of L2_FECollection(p, 3, GaussLobatto). A batched
+ *    operator (batch B > 1) stacks B such vectors back to back.
+ *  - Pointers named d_* are device pointers; h_* are host pointers.
+ *  - `stream` is a cudaStream_t (NULL = legacy default stream).
+ *  - One operator per stream at a time: calls on one operator are not
+ *    re-entrant (the reference's Mult mutates work vectors, GlobalEvolution.h:82-110).
+ */
+#ifndef DGTD_GB300_H
+#define DGTD_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DGTD_OK 0
+#define DGTD_ERR_INVALID (-1)
+#define DGTD_ERR_CUDA (-2)
+#define DGTD_ERR_UNSUPPORTED (-3)
+#define DGTD_ERR_NOMEM (-4)
+#define DGTD_ERR_TIMEOUT (-5)
+
+/* Boundary codes (reference BdrCond, src/components/Types.h:47-55). */
+#define DGTD_BC_OPEN 0
+#define DGTD_BC_PEC 1
+#define DGTD_BC_PMC 2
+#define DGTD_BC_SMA 3
+
+/* Precision forms. */
+#define DGTD_FP64 0        /* plain form: FP64 state and arithmetic */
+#define DGTD_FP32_3XTF32 1 /* batched form: FP32 state, 3xTF32 tensor-core contractions */
+
+/* Time integrators. */
+#define DGTD_RK4 0    /* classical RK4, mfem::RK4Solver semantics (reference default, Solver.cpp:45-47) */
+#define DGTD_LSERK4 1 /* 5-stage low-storage RK4 (Carpenter & Kennedy 1994) */
+
+/*
+ * Mesh description (replaces the MFEM ParMesh + Model of the reference:
+ * element attributes -> per-element eps/mu/sigma, Model.cpp:145-161;
+ * boundary attributes -> codes, driver.cpp:870-887; TF/SF interior faces,
+ * SubMesher.cpp:359-775).
+ */
+typedef struct dgtd_mesh_desc {
+    int32_t dim;                /* 3 (tetrahedra) */
+    int64_t n_vertices;
+    const double* vertices;     /* [n_vertices][3] */
+    int64_t n_elements;
+    const int32_t* elements;    /* [n_elements][4], positively oriented */
+    const double* eps_r;        /* [n_elements] or NULL (1) */
+    const double* mu_r;         /* [n_elements] or NULL (1) */
+    const double* sigma;        /* [n_elements] or NULL (0) */
+    int64_t n_bdr_faces;
+    const int32_t* bdr_faces;   /* [n_bdr_faces][3] vertex ids */
+    const int32_t* bdr_codes;   /* [n_bdr_faces] DGTD_BC_* */
+    int64_t n_tfsf_faces;
+    const int32_t* tfsf_faces;  /* [n][3], winding normal points into the total-field side */
+    int64_t n_int_faces;
+    const int32_t* int_faces;   /* [n][3] interior PEC/PMC/SMA sheets */
+    const int32_t* int_codes;   /* [n] DGTD_BC_PEC/PMC/SMA */
+} dgtd_mesh_desc;
+
+typedef struct dgtd_op_opts {
+    int32_t order;      /* polynomial order p, 1..6 (reference solver_options.order) */
+    double alpha;       /* upwind coefficient (reference solver_options.upwind_alpha) */
+    int32_t precision;  /* DGTD_FP64 or DGTD_FP32_3XTF32 */
+    int32_t batch;      /* B incidences sharing the mesh (>= 1) */
+} dgtd_op_opts;
+
+/* Gaussian / modulated-Gaussian plane wave (reference Planewave, Function.h:329-416,
+ * built by driver.cpp:483-519; mean is the 1D Gaussian mean along the propagation). */
+typedef struct dgtd_planewave {
+    double propagation[3]; /* normalised by the library */
+    double polarization[3];/* normalised by the library */
+    double spread;
+    double mean;
+    double frequency;      /* 0: plain Gaussian; else carrier (normalised units) */
+    int32_t batch;         /* incidence index in [0, B) */
+} dgtd_planewave;
+
+typedef struct dgtd_op_info {
+    int64_t n_elements;
+    int32_t order, np, nfp;
+    int32_t batch;
+    int32_t precision;
+    int64_t ndofs;          /* K*Np (per field component) */
+    int64_t state_len;      /* 6*K*Np*B entries of the reference-layout state */
+    int64_t n_tfsf_faces;   /* element faces flagged TF/SF (counted per side) */
+    double min_edge;
+    double dt_scale_min;    /* min over elements of vol / (sum of face areas / 2) */
+    int64_t device_bytes;   /* bytes of device tables held by the operator */
+} dgtd_op_info;
+
+typedef struct dgtd_op dgtd_op;
+
+/* Thread-local description of the last error. */
+const char* dgtd_last_error(void);
+
+/* Operator life cycle (reference GlobalEvolution ctor, GlobalEvolution.cpp:32-364:
+ * here the once-per-mesh work is the geometric-factor / LIFT / node-map build). */
+int dgtd_op_create(const dgtd_mesh_desc* mesh, const dgtd_op_opts* opts, dgtd_op** out);
+void dgtd_op_destroy(dgtd_op* op);
+int dgtd_op_get_info(const dgtd_op* op, dgtd_op_info* info);
+
+/* Physical coordinates of every DOF node: h_xyz is [3][K*Np]
+ * (reference buildDoFPositions, HesthavenEvolutionMethods.cpp:77-91). */
+int dgtd_op_node_coords(const dgtd_op* op, double* h_xyz);
+
+/* Replace the plane-wave sources (reference TotalField sources handled by
+ * GlobalEvolution::applyTFSFSourceToVector, GlobalEvolution.cpp:551-626). */
+int dgtd_op_set_planewaves(dgtd_op* op, const dgtd_planewave* pw, int32_t n);
+
+/* y = dU/dt(x, t): exact TimeDependentOperator::Mult semantics
+ * (reference GlobalEvolution::Mult, GlobalEvolution.cpp:628-1088), FP64 form.
+ * d_x, d_y: device, state_len doubles each, must not alias. */
+int dgtd_op_mult(dgtd_op* op, const double* d_x, double* d_y, double t, void* stream);
+
+/* Same as dgtd_op_mult with host buffers: copies in, applies, copies out
+ * (synchronous). */
+int dgtd_op_mult_host(dgtd_op* op, const double* h_x, double* h_y, double t);
+
+/* Advance d_state (device, reference layout) by nsteps steps of size dt from t0
+ * with the fused stage kernels (reference Solver::step + mfem RK4Solver::Step,
+ * Solver.cpp:535-551). The operator keeps its RK registers in device scratch it
+ * allocates on first use. */
+int dgtd_op_step(dgtd_op* op, double* d_state, double t0, double dt, int32_t nsteps, int32_t integrator,
+                 void* stream);
+
+/* Run to final_time from t0 following the reference loop (Solver::run,
+ * Solver.cpp:483-551: while t <= T - 1e-8 dt, last step truncated to T - t).
+ * h_state: host, in/out. Returns the number of steps taken in *steps_out. */
+int dgtd_op_run_host(dgtd_op* op, double* h_state, double t0, double dt, double final_time, int32_t integrator,
+                     int64_t* steps_out);
+
+/* Squared L2 norm per incidence: h_out[b] (host) for d_state (device). */
+int dgtd_op_norm2(dgtd_op* op, const double* d_state, double* h_out, void* stream);
+
+/* Automatic time step of the reference's 3D Global operator
+ * (estimateTimeStep, Solver.cpp:289-300, 349-351) at the given cfl. */
+int dgtd_op_estimate_dt(const dgtd_op* op, double cfl, double* dt_out);
+
+/* ---- host-only mesh helpers (no GPU needed) ---------------------------------- */
+
+/* Build the reference-element and mesh tables on the host only (the
+ * once-per-mesh part of dgtd_op_create, no device allocation) and report them
+ * in *info: validates a mesh description (connectivity, orientation, boundary
+ * and TF/SF faces) without a GPU. */
+int dgtd_mesh_validate(const dgtd_mesh_desc* mesh, const dgtd_op_opts* opts, dgtd_op_info* info);
+
+/* Structured box mesh: n[3] cells on [lo,hi], each hex split into 6 tetrahedra
+ * around its (0,0,0)-(1,1,1) diagonal (the split the reference's tests get from
+ * Mesh::MakeCartesian3D(..., TETRAHEDRON), Solver3DTest.cpp:36). Cells in
+ * [hole_lo, hole_hi) are removed (their surface gets hole_bc); cells in
+ * [tf_lo, tf_hi) form the total-field region (its surface becomes TF/SF faces). */
+typedef struct dgtd_box_spec {
+    int32_t n[3];
+    double lo[3], hi[3];
+    int32_t hole_lo[3], hole_hi[3];
+    int32_t tf_lo[3], tf_hi[3];
+    int32_t outer_bc, hole_bc;
+} dgtd_box_spec;
+
+int dgtd_box_mesh_size(const dgtd_box_spec* spec, int64_t* n_vertices, int64_t* n_elements,
+                       int64_t* n_bdr_faces, int64_t* n_tfsf_faces);
+int dgtd_box_mesh_fill(const dgtd_box_spec* spec, double* vertices, int32_t* elements, int32_t* bdr_faces,
+                       int32_t* bdr_codes, int32_t* tfsf_faces);
+
+/* Reference-element tables of the product (host only), for known-answer
+ * tests against the reference's element-matrix tests
+ * (test/hesthavenComparison/Hesthaven3DTest.cpp:77-152, 232-265).
+ * Arrays: r,s,t [Np]; Dr,Ds,Dt,Minv [Np*Np]; lift [Np*4*Nfp]; fmask [4*Nfp]
+ * (row-major, Hesthaven (-1,1) reference tetrahedron). Any pointer may be NULL. */
+int dgtd_ref_tet(int32_t order, double* r, double* s, double* t, double* Dr, double* Ds, double* Dt,
+                 double* Minv, double* lift, int32_t* fmask);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DGTD_GB300_H */

@@ -1,0 +1,1289 @@
+// CPU oracle for the DG Maxwell step — TEST INFRASTRUCTURE ONLY.
+//
+// This file restates, on the CPU in FP64, the algorithm of the reference's
+// evolution operator so that the GPU path can be checked against it. It is
+// never part of the product: only tests/, __graft_entry__.smoke() and the
+// cpu_baseline leg of bench.py load it.
+//
+// Two independent restatements are provided:
+//  (A) "global": the assembled sparse operator of GlobalEvolution
+//      (src/evolution/GlobalEvolution.cpp:628-826) built like
+//      DGOperatorFactory::buildGlobalOperator (src/components/DGOperatorFactory.h:1428-1602):
+//      weak-form element matrices by exact quadrature (mass, strong-form
+//      derivative ∫ v du/dx, the zero/one/two-normal face "jump" integrators of
+//      src/mfemExtension/BilinearIntegrators.cpp:9-149 and the interior-boundary
+//      integrator :356-412), multiplied by the piecewise-eps/mu inverse mass
+//      (DGOperatorFactory.h:413-424) and placed with the signs of
+//      DGOperatorFactory.h:1061-1208; TF/SF through a second face operator
+//      applied to the +-0.5 masked plane wave (GlobalEvolution.cpp:551-626,
+//      SourcesManager.cpp:129-231) with the ||pw|| < 1e-8 skip.
+//  (B) "nodal": the matrix-free nodal form of HesthavenEvolution::Mult
+//      (src/evolution/HesthavenEvolution.cpp:450-541): node jumps, boundary
+//      rules, TF/SF, upwind flux, per-element derivative and lift matrices,
+//      with the boundary coefficients of (A).
+// Time integration: classical RK4 with mfem::RK4Solver's register sequence
+// (used by src/solver/Solver.cpp:45-47, 535-551) and the run loop of
+// Solver::run (Solver.cpp:483-533); optionally the 5-stage low-storage RK4.
+//
+// Element basis: Lagrange polynomials on the node set of
+// L2_FECollection(p, dim, GaussLobatto) (barycentric blend of Gauss-Lobatto
+// points), represented through the Bernstein basis; quadrature: collapsed
+// (Duffy) Gauss-Legendre products, exact for the polynomial integrands of
+// affine elements. Nothing here is shared with the product's code.
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace orc {
+
+using std::vector;
+
+// ---------------------------------------------------------------- 1D rules
+static void gauss_legendre01(int n, vector<double>& x, vector<double>& w)
+{
+    x.resize(n); w.resize(n);
+    for (int i = 0; i < n; ++i) {
+        double z = std::cos(M_PI * (i + 0.75) / (n + 0.5));
+        double dp = 0.0;
+        for (int it = 0; it < 200; ++it) {
+            double p0 = 1.0, p1 = z;
+            for (int k = 2; k <= n; ++k) { double pk = ((2 * k - 1) * z * p1 - (k - 1) * p0) / k; p0 = p1; p1 = pk; }
+            double pn = (n == 1) ? z : p1, pm = (n == 1) ? 1.0 : p0;
+            dp = n * (z * pn - pm) / (z * z - 1.0);
+            double dz = pn / dp;
+            z -= dz;
+            if (std::fabs(dz) < 1e-16) break;
+        }
+        x[i] = 0.5 * (1.0 - z);
+        w[i] = 1.0 / ((1.0 - z * z) * dp * dp);   // 2/((1-z^2)P'^2) scaled by 1/2 for [0,1]
+    }
+}
+
+// Gauss-Lobatto points on [0,1]: ends plus the extrema of P_p, found by
+// bisection-refined Newton on the derivative of the Legendre recurrence.
+static vector<double> lobatto01(int p)
+{
+    vector<double> g(p + 1);
+    if (p == 0) { g[0] = 0.5; return g; }
+    g[0] = 0.0; g[p] = 1.0;
+    auto dleg = [p](double z, double& d1, double& d2) {
+        // P_p'(z) and P_p''(z) by the recurrence for (P, P', P'')
+        double P0 = 1, P1 = z, D0 = 0, D1 = 1, S0 = 0, S1 = 0;
+        for (int k = 2; k <= p; ++k) {
+            double Pk = ((2 * k - 1) * z * P1 - (k - 1) * P0) / k;
+            double Dk = ((2 * k - 1) * (P1 + z * D1) - (k - 1) * D0) / k;
+            double Sk = ((2 * k - 1) * (2 * D1 + z * S1) - (k - 1) * S0) / k;
+            P0 = P1; P1 = Pk; D0 = D1; D1 = Dk; S0 = S1; S1 = Sk;
+        }
+        if (p == 1) { d1 = 1.0; d2 = 0.0; } else { d1 = D1; d2 = S1; }
+    };
+    for (int i = 1; i < p; ++i) {
+        double z = -std::cos(M_PI * i / p);
+        for (int it = 0; it < 200; ++it) {
+            double d1, d2; dleg(z, d1, d2);
+            double dz = d1 / d2;
+            z -= dz;
+            if (std::fabs(dz) < 1e-16) break;
+        }
+        g[i] = 0.5 * (1.0 + z);
+    }
+    for (int i = 0; i <= p / 2; ++i) { double v = 0.5 * (g[i] + 1.0 - g[p - i]); g[i] = v; g[p - i] = 1.0 - v; }
+    return g;
+}
+
+// ---------------------------------------------------------------- dense LU
+struct LU {
+    int n = 0; vector<double> a; vector<int> piv;
+    explicit LU(const vector<double>& m, int n_) : n(n_), a(m), piv(n_)
+    {
+        for (int k = 0; k < n; ++k) {
+            int p = k;
+            for (int i = k + 1; i < n; ++i) if (std::fabs(a[i * n + k]) > std::fabs(a[p * n + k])) p = i;
+            piv[k] = p;
+            if (p != k) for (int j = 0; j < n; ++j) std::swap(a[k * n + j], a[p * n + j]);
+            if (a[k * n + k] == 0.0) throw std::runtime_error("oracle: singular matrix");
+            for (int i = k + 1; i < n; ++i) {
+                double f = a[i * n + k] /= a[k * n + k];
+                for (int j = k + 1; j < n; ++j) a[i * n + j] -= f * a[k * n + j];
+            }
+        }
+    }
+    void solve(double* b) const
+    {
+        // rows were swapped as whole rows during factorisation (PA = LU): permute b first
+        for (int k = 0; k < n; ++k) std::swap(b[k], b[piv[k]]);
+        for (int k = 0; k < n; ++k) for (int i = k + 1; i < n; ++i) b[i] -= a[i * n + k] * b[k];
+        for (int k = n - 1; k >= 0; --k) { for (int j = k + 1; j < n; ++j) b[k] -= a[k * n + j] * b[j]; b[k] /= a[k * n + k]; }
+    }
+    vector<double> inverse() const
+    {
+        vector<double> inv(n * n), col(n);
+        for (int j = 0; j < n; ++j) {
+            std::fill(col.begin(), col.end(), 0.0); col[j] = 1.0; solve(col.data());
+            for (int i = 0; i < n; ++i) inv[i * n + j] = col[i];
+        }
+        return inv;
+    }
+};
+
+// ---------------------------------------------------------------- element basis
+// Lagrange basis on the GaussLobatto node set of the reference simplex
+// (dim 1: [0,1]; dim 3: tet (0,0,0),(1,0,0),(0,1,0),(0,0,1)), through Bernstein polynomials.
+struct Basis {
+    // Evaluated in extended precision: the Bernstein-to-Lagrange change of
+    // basis is moderately ill-conditioned at p = 6.
+    typedef long double R;
+    int dim = 3, p = 1, Np = 0;
+    vector<double> nodes;                 // [Np][dim] reference coordinates
+    vector<std::array<int, 4>> bidx;      // Bernstein multi-indices (l0, l1, l2, l3)
+    vector<R> C;                          // [Np][Np]: phi_i = sum_m B_m C[m][i]
+    vector<R> fact;
+
+    R bern(const std::array<int, 4>& a, const R* lam, int deg) const
+    {
+        R v = fact[deg];
+        for (int q = 0; q <= dim; ++q) {
+            R pw = 1; for (int e = 0; e < a[q]; ++e) pw *= lam[q];
+            v *= pw / fact[a[q]];
+        }
+        return v;
+    }
+    void lam_of(const double* xi, double* lam) const
+    {
+        double s = 0;
+        for (int d = 0; d < dim; ++d) { lam[d + 1] = xi[d]; s += xi[d]; }
+        lam[0] = 1.0 - s;
+    }
+    void lamR(const double* xi, R* lam) const
+    {
+        R s = 0;
+        for (int d = 0; d < dim; ++d) { lam[d + 1] = xi[d]; s += xi[d]; }
+        lam[0] = 1 - s;
+    }
+    void init(int dim_, int p_)
+    {
+        dim = dim_; p = p_;
+        fact.resize(p + 2); fact[0] = 1; for (int i = 1; i < p + 2; ++i) fact[i] = fact[i - 1] * i;
+        auto g = lobatto01(p);
+        nodes.clear(); bidx.clear();
+        if (dim == 1) {
+            Np = p + 1;
+            for (int i = 0; i <= p; ++i) nodes.push_back(g[i]);
+            for (int i = 0; i <= p; ++i) bidx.push_back({p - i, i, 0, 0});
+        } else {
+            for (int k = 0; k <= p; ++k)
+                for (int j = 0; j + k <= p; ++j)
+                    for (int i = 0; i + j + k <= p; ++i) {
+                        int l = p - i - j - k;
+                        double w = g[i] + g[j] + g[k] + g[l];
+                        nodes.push_back(g[i] / w); nodes.push_back(g[j] / w); nodes.push_back(g[k] / w);
+                        bidx.push_back({l, i, j, k});
+                    }
+            Np = static_cast<int>(bidx.size());
+        }
+        // Gauss-Jordan inverse of the Bernstein Vandermonde in extended precision
+        vector<R> V(Np * Np), I(Np * Np, 0);
+        for (int n = 0; n < Np; ++n) {
+            R lam[4] = {0, 0, 0, 0};
+            lamR(&nodes[n * dim], lam);
+            for (int m = 0; m < Np; ++m) V[n * Np + m] = bern(bidx[m], lam, p);
+            I[n * Np + n] = 1;
+        }
+        for (int c = 0; c < Np; ++c) {
+            int best = c;
+            for (int r = c + 1; r < Np; ++r) if (fabsl(V[r * Np + c]) > fabsl(V[best * Np + c])) best = r;
+            if (V[best * Np + c] == 0) throw std::runtime_error("oracle: singular Bernstein Vandermonde");
+            for (int k = 0; k < Np; ++k) { std::swap(V[c * Np + k], V[best * Np + k]); std::swap(I[c * Np + k], I[best * Np + k]); }
+            R d = 1 / V[c * Np + c];
+            for (int k = 0; k < Np; ++k) { V[c * Np + k] *= d; I[c * Np + k] *= d; }
+            for (int r = 0; r < Np; ++r) {
+                if (r == c) continue;
+                R f = V[r * Np + c];
+                if (f == 0) continue;
+                for (int k = 0; k < Np; ++k) { V[r * Np + k] -= f * V[c * Np + k]; I[r * Np + k] -= f * I[c * Np + k]; }
+            }
+        }
+        C = I;
+    }
+    void shapeR(const double* xi, R* phi) const
+    {
+        R lam[4] = {0, 0, 0, 0}; lamR(xi, lam);
+        vector<R> b(Np);
+        for (int m = 0; m < Np; ++m) b[m] = bern(bidx[m], lam, p);
+        for (int i = 0; i < Np; ++i) { R s = 0; for (int m = 0; m < Np; ++m) s += b[m] * C[m * Np + i]; phi[i] = s; }
+    }
+    void dshapeR(const double* xi, R* dphi) const
+    {
+        R lam[4] = {0, 0, 0, 0}; lamR(xi, lam);
+        vector<R> db(Np * dim, 0);
+        for (int m = 0; m < Np; ++m) {
+            R dl[4] = {0, 0, 0, 0};
+            for (int q = 0; q <= dim; ++q) {
+                if (bidx[m][q] == 0) continue;
+                auto a = bidx[m]; a[q] -= 1;
+                dl[q] = static_cast<R>(p) * bern(a, lam, p - 1);
+            }
+            for (int d = 0; d < dim; ++d) db[m * dim + d] = dl[d + 1] - dl[0];
+        }
+        for (int i = 0; i < Np; ++i)
+            for (int d = 0; d < dim; ++d) {
+                R s = 0; for (int m = 0; m < Np; ++m) s += db[m * dim + d] * C[m * Np + i];
+                dphi[i * dim + d] = s;
+            }
+    }
+    void shape(const double* xi, double* phi) const
+    {
+        R lam[4] = {0, 0, 0, 0}; lamR(xi, lam);
+        vector<R> b(Np);
+        for (int m = 0; m < Np; ++m) b[m] = bern(bidx[m], lam, p);
+        for (int i = 0; i < Np; ++i) { R s = 0; for (int m = 0; m < Np; ++m) s += b[m] * C[m * Np + i]; phi[i] = static_cast<double>(s); }
+    }
+    // dphi[i*dim + d] = d phi_i / d xi_d
+    void dshape(const double* xi, double* dphi) const
+    {
+        R lam[4] = {0, 0, 0, 0}; lamR(xi, lam);
+        vector<R> db(Np * dim, 0);
+        for (int m = 0; m < Np; ++m) {
+            R dl[4] = {0, 0, 0, 0};
+            for (int q = 0; q <= dim; ++q) {
+                if (bidx[m][q] == 0) continue;
+                auto a = bidx[m]; a[q] -= 1;
+                // d/d lam_q of p!/a! prod lam^a  =  p * B^{p-1}_{a - e_q}
+                dl[q] = static_cast<R>(p) * bern(a, lam, p - 1);
+            }
+            for (int d = 0; d < dim; ++d) db[m * dim + d] = dl[d + 1] - dl[0];
+        }
+        for (int i = 0; i < Np; ++i)
+            for (int d = 0; d < dim; ++d) {
+                R s = 0; for (int m = 0; m < Np; ++m) s += db[m * dim + d] * C[m * Np + i];
+                dphi[i * dim + d] = static_cast<double>(s);
+            }
+    }
+};
+
+// Quadrature on the reference simplex (weights sum to its measure).
+struct Quad { vector<double> x; vector<double> w; };
+
+static Quad tet_quad(int n)
+{
+    vector<double> g, gw; gauss_legendre01(n, g, gw);
+    Quad q;
+    for (int a = 0; a < n; ++a) for (int b = 0; b < n; ++b) for (int c = 0; c < n; ++c) {
+        double u = g[a], v = g[b], w = g[c];
+        q.x.push_back(u * (1 - v) * (1 - w)); q.x.push_back(v * (1 - w)); q.x.push_back(w);
+        q.w.push_back(gw[a] * gw[b] * gw[c] * (1 - v) * (1 - w) * (1 - w));
+    }
+    return q;
+}
+static Quad tri_quad(int n)
+{
+    vector<double> g, gw; gauss_legendre01(n, g, gw);
+    Quad q;
+    for (int a = 0; a < n; ++a) for (int b = 0; b < n; ++b) {
+        double u = g[a], v = g[b];
+        q.x.push_back(u * (1 - v)); q.x.push_back(v);
+        q.w.push_back(gw[a] * gw[b] * (1 - v));
+    }
+    return q;
+}
+
+// ---------------------------------------------------------------- CSR builder
+struct CSR {
+    int64_t rows = 0, cols = 0;
+    vector<int64_t> rp; vector<int32_t> ci; vector<double> v;
+    void spmv(const double* x, double* y, double scale, bool accumulate) const
+    {
+#pragma omp parallel for schedule(static)
+        for (int64_t r = 0; r < rows; ++r) {
+            double s = 0;
+            for (int64_t k = rp[r]; k < rp[r + 1]; ++k) s += v[k] * x[ci[k]];
+            y[r] = accumulate ? y[r] + scale * s : scale * s;
+        }
+    }
+};
+
+// Row-wise triplet accumulation (rows are owned by one element block, so each
+// element's rows are built independently and merged).
+
+enum { BC_OPEN = 0, BC_PEC = 1, BC_PMC = 2, BC_SMA = 3 };
+
+struct Face {
+    int64_t e1, e2;      // e2 = -1 on the boundary
+    int f1, f2;
+    int kind;            // 0 interior, 1 boundary, 2 TF/SF (interior), 3 interior PEC/PMC/SMA sheet
+    int bc;              // BC code for kinds 1 and 3
+    double n[3];         // unit normal, outward from e1
+    double jac;          // face Jacobian |J_f| w.r.t. the reference face (MFEM measure: tri 1/2, point 1)
+    int tf_side;         // kind 2: +1 if e1 is in the total field, -1 otherwise
+};
+
+struct PW { double k[3], pol[3], kxp[3], spread, mean, freq; };
+
+struct Oracle {
+    int dim = 3, p = 1, Np = 0, Nfp = 0, nfaces = 4;
+    double alpha = 1.0;
+    int64_t K = 0, N = 0;
+    Basis B;
+    vector<double> verts; vector<int32_t> elems;
+    vector<double> eps, mu, sig;
+    vector<double> A;      // per element affine map: x = v0 + A xi, A [3][dim]
+    vector<double> Ainv;   // [dim][3]
+    vector<double> detJ;
+    vector<double> X;      // [3][N] node coordinates
+    vector<Face> faces;
+    vector<int64_t> elem_face;   // [K][nfaces] -> face index
+    vector<int> fnodes;          // [nfaces][Nfp] reference nodes on each local face
+    vector<int32_t> tfsf_elems;
+    vector<PW> pws;
+    // (A) global
+    bool have_csr = false; CSR Aglob, Ttfsf;
+    // (B) nodal
+    bool have_nodal = false;
+    vector<double> Dx;            // per shape class: [3][Np][Np] physical derivative M^-1 S_d
+    vector<double> Lf;            // per shape class: [nfaces][Np][Nfp] M^-1 * face mass (face nodes)
+    vector<int> shape_of;         // element -> shape class
+    vector<int64_t> vmapP;        // [K][nfaces][Nfp]
+
+    // ---- geometry
+    void ref_to_phys(int64_t e, const double* xi, double* x) const
+    {
+        const double* v0 = &verts[3 * elems[e * (dim + 1)]];
+        for (int r = 0; r < 3; ++r) { x[r] = v0[r]; for (int d = 0; d < dim; ++d) x[r] += A[e * 3 * dim + r * dim + d] * xi[d]; }
+    }
+    void phys_to_ref(int64_t e, const double* x, double* xi) const
+    {
+        const double* v0 = &verts[3 * elems[e * (dim + 1)]];
+        for (int d = 0; d < dim; ++d) { xi[d] = 0; for (int r = 0; r < 3; ++r) xi[d] += Ainv[e * 3 * dim + d * 3 + r] * (x[r] - v0[r]); }
+    }
+};
+
+static void cross(const double* a, const double* b, double* c)
+{
+    c[0] = a[1] * b[2] - a[2] * b[1]; c[1] = a[2] * b[0] - a[0] * b[2]; c[2] = a[0] * b[1] - a[1] * b[0];
+}
+
+// Reference boundary coefficient table (DGOperatorFactory.h:21-35): c[bc][field]
+static double bc_coeff(int bc, int field)
+{
+    switch (bc) {
+    case BC_PEC: return field == 0 ? 2.0 : 0.0;
+    case BC_PMC: return field == 0 ? 0.0 : 2.0;
+    case BC_SMA: return 1.0;
+    default: return 0.0;
+    }
+}
+
+static void build_geometry(Oracle& O)
+{
+    const int dim = O.dim, nv = dim + 1;
+    O.A.assign(O.K * 3 * dim, 0.0); O.Ainv.assign(O.K * 3 * dim, 0.0); O.detJ.resize(O.K);
+    for (int64_t e = 0; e < O.K; ++e) {
+        const double* v0 = &O.verts[3 * O.elems[e * nv]];
+        double* Ae = &O.A[e * 3 * dim];
+        for (int d = 0; d < dim; ++d) {
+            const double* vd = &O.verts[3 * O.elems[e * nv + d + 1]];
+            for (int r = 0; r < 3; ++r) Ae[r * dim + d] = vd[r] - v0[r];
+        }
+        if (dim == 1) {
+            double h = Ae[0];
+            if (!(h > 0)) throw std::runtime_error("oracle: 1D segment with non-positive length");
+            O.detJ[e] = h; O.Ainv[e * 3 + 0] = 1.0 / h;
+        } else {
+            double c0[3] = {Ae[0], Ae[3], Ae[6]}, c1[3] = {Ae[1], Ae[4], Ae[7]}, c2[3] = {Ae[2], Ae[5], Ae[8]};
+            double x12[3]; cross(c1, c2, x12);
+            double det = c0[0] * x12[0] + c0[1] * x12[1] + c0[2] * x12[2];
+            if (!(det > 0)) throw std::runtime_error("oracle: tetrahedron with non-positive Jacobian");
+            O.detJ[e] = det;
+            double x20[3], x01[3]; cross(c2, c0, x20); cross(c0, c1, x01);
+            double* Ai = &O.Ainv[e * 9];
+            for (int r = 0; r < 3; ++r) { Ai[0 * 3 + r] = x12[r] / det; Ai[1 * 3 + r] = x20[r] / det; Ai[2 * 3 + r] = x01[r] / det; }
+        }
+    }
+    O.N = O.K * O.Np;
+    O.X.assign(3 * O.N, 0.0);
+    for (int64_t e = 0; e < O.K; ++e)
+        for (int n = 0; n < O.Np; ++n) {
+            double x[3]; O.ref_to_phys(e, &O.B.nodes[n * dim], x);
+            for (int r = 0; r < 3; ++r) O.X[r * O.N + e * O.Np + n] = x[r];
+        }
+}
+
+// local face f of the reference simplex: the face opposite vertex f
+static void local_face_nodes(Oracle& O)
+{
+    const int dim = O.dim;
+    O.nfaces = dim + 1;
+    O.Nfp = (dim == 1) ? 1 : (O.p + 1) * (O.p + 2) / 2;
+    O.fnodes.assign(O.nfaces * O.Nfp, -1);
+    for (int f = 0; f < O.nfaces; ++f) {
+        int c = 0;
+        for (int n = 0; n < O.Np; ++n) {
+            double lam[4] = {0, 0, 0, 0}; O.B.lam_of(&O.B.nodes[n * dim], lam);
+            if (std::fabs(lam[f]) < 1e-12) O.fnodes[f * O.Nfp + c++] = n;
+        }
+        if (c != O.Nfp) throw std::runtime_error("oracle: face node count");
+    }
+}
+
+static std::array<int32_t, 3> face_key(const Oracle& O, int64_t e, int f)
+{
+    const int nv = O.dim + 1;
+    std::array<int32_t, 3> k = {-1, -1, -1};
+    int c = 0;
+    for (int q = 0; q < nv; ++q) if (q != f) k[c++] = O.elems[e * nv + q];
+    std::sort(k.begin(), k.begin() + c);
+    return k;
+}
+
+static void face_normal(const Oracle& O, int64_t e, int f, double* n, double& jac)
+{
+    if (O.dim == 1) {
+        // MFEM 1D face "normal" 2x-1 at the element-local face point (IntegratorFunctions.cpp:56-63)
+        n[0] = (f == 1) ? -1.0 : 1.0;   // face 0 is opposite vertex 0 -> the x = 1 end
+        n[1] = n[2] = 0.0; jac = 1.0;
+        return;
+    }
+    const int nv = 4;
+    const double* P[3]; int c = 0;
+    for (int q = 0; q < nv; ++q) if (q != f) P[c++] = &O.verts[3 * O.elems[e * nv + q]];
+    double a[3], b[3], cr[3];
+    for (int r = 0; r < 3; ++r) { a[r] = P[1][r] - P[0][r]; b[r] = P[2][r] - P[0][r]; }
+    cross(a, b, cr);
+    double len = std::sqrt(cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2]);
+    // orient outward: away from the opposite vertex
+    const double* vf = &O.verts[3 * O.elems[e * nv + f]];
+    double d = 0; for (int r = 0; r < 3; ++r) d += cr[r] * (P[0][r] - vf[r]);
+    double s = d > 0 ? 1.0 : -1.0;
+    for (int r = 0; r < 3; ++r) n[r] = s * cr[r] / len;
+    jac = len;   // |J_f| = 2 area = |cross|, reference triangle measure 1/2
+}
+
+static void build_faces(Oracle& O, int64_t nb, const int32_t* bf, const int32_t* bc, int64_t nt, const int32_t* tf,
+                        int64_t ni, const int32_t* ifc, const int32_t* icodes)
+{
+    const int dim = O.dim, nf = O.nfaces;
+    std::map<std::array<int32_t, 3>, std::pair<int64_t, int>> open;
+    O.elem_face.assign(O.K * nf, -1);
+    for (int64_t e = 0; e < O.K; ++e)
+        for (int f = 0; f < nf; ++f) {
+            auto k = face_key(O, e, f);
+            auto it = open.find(k);
+            if (it == open.end()) { open[k] = {e, f}; continue; }
+            Face F{};
+            F.e1 = it->second.first; F.f1 = it->second.second; F.e2 = e; F.f2 = f; F.kind = 0; F.bc = 0;
+            face_normal(O, F.e1, F.f1, F.n, F.jac);
+            O.elem_face[F.e1 * nf + F.f1] = static_cast<int64_t>(O.faces.size());
+            O.elem_face[F.e2 * nf + F.f2] = static_cast<int64_t>(O.faces.size());
+            O.faces.push_back(F);
+            open.erase(it);
+        }
+    std::map<std::array<int32_t, 3>, int64_t> key_to_face;
+    for (auto& kv : open) {
+        Face F{};
+        F.e1 = kv.second.first; F.f1 = kv.second.second; F.e2 = -1; F.f2 = -1; F.kind = 1; F.bc = BC_OPEN;
+        face_normal(O, F.e1, F.f1, F.n, F.jac);
+        O.elem_face[F.e1 * nf + F.f1] = static_cast<int64_t>(O.faces.size());
+        O.faces.push_back(F);
+    }
+    for (size_t i = 0; i < O.faces.size(); ++i) key_to_face[face_key(O, O.faces[i].e1, O.faces[i].f1)] = i;
+    const int fv = (dim == 1) ? 1 : 3;
+    auto lookup = [&](const int32_t* v) {
+        std::array<int32_t, 3> k = {-1, -1, -1};
+        for (int q = 0; q < fv; ++q) k[q] = v[q];
+        std::sort(k.begin(), k.begin() + fv);
+        auto it = key_to_face.find(k);
+        if (it == key_to_face.end()) throw std::runtime_error("oracle: face not found");
+        return it->second;
+    };
+    for (int64_t b = 0; b < nb; ++b) {
+        int64_t fi = lookup(&bf[b * fv]);
+        if (O.faces[fi].kind != 1) throw std::runtime_error("oracle: boundary code on interior face");
+        O.faces[fi].bc = bc[b];
+    }
+    for (int64_t b = 0; b < ni; ++b) {
+        int64_t fi = lookup(&ifc[b * fv]);
+        if (O.faces[fi].kind != 0) throw std::runtime_error("oracle: interior sheet on boundary face");
+        O.faces[fi].kind = 3; O.faces[fi].bc = icodes[b];
+    }
+    vector<char> mark(O.K, 0);
+    for (int64_t b = 0; b < nt; ++b) {
+        const int32_t* v = &tf[b * (dim == 1 ? 2 : 3)];
+        int64_t fi = lookup(v);
+        Face& F = O.faces[fi];
+        if (F.kind != 0) throw std::runtime_error("oracle: TF/SF face must be interior");
+        F.kind = 2;
+        // orientation of the given face: 3D winding normal / 1D given direction
+        double gn[3] = {0, 0, 0};
+        if (dim == 1) gn[0] = (v[1] >= 0) ? 1.0 : -1.0;
+        else {
+            const double* P0 = &O.verts[3 * v[0]]; const double* P1 = &O.verts[3 * v[1]]; const double* P2 = &O.verts[3 * v[2]];
+            double a[3], bb[3]; for (int r = 0; r < 3; ++r) { a[r] = P1[r] - P0[r]; bb[r] = P2[r] - P0[r]; }
+            cross(a, bb, gn);
+        }
+        // the given normal points into the TF side; F.n points from e1 to e2
+        double d = F.n[0] * gn[0] + F.n[1] * gn[1] + F.n[2] * gn[2];
+        F.tf_side = (d > 0) ? -1 : +1;   // e2 is TF when the normals agree -> e1 is SF
+        mark[F.e1] = 1; mark[F.e2] = 1;
+    }
+    for (int64_t e = 0; e < O.K; ++e) if (mark[e]) O.tfsf_elems.push_back(static_cast<int32_t>(e));
+}
+
+// ---------------------------------------------------------------- (A) global
+// Element matrices: mass M, its inverse, strong-form derivative S_d = int phi_i dphi_j/dx_d
+// and the physical derivative D_d = M^-1 S_d, accumulated and inverted in extended
+// precision (the mass matrix of the p = 6 node set has condition number ~2e3).
+struct ElemMats { vector<double> M, Minv, S[3], D[3]; };
+
+static ElemMats elem_mats(const Oracle& O, int64_t e, const Quad& q)
+{
+    typedef long double R;
+    const int Np = O.Np, dim = O.dim;
+    vector<R> M(Np * Np, 0), S[3];
+    for (int d = 0; d < 3; ++d) S[d].assign(Np * Np, 0);
+    vector<R> phi(Np), dphi(Np * dim), g(Np);
+    const size_t nq = q.w.size();
+    for (size_t k = 0; k < nq; ++k) {
+        const double* xi = &q.x[k * dim];
+        O.B.shapeR(xi, phi.data()); O.B.dshapeR(xi, dphi.data());
+        R w = static_cast<R>(q.w[k]) * O.detJ[e];
+        for (int i = 0; i < Np; ++i) for (int j = 0; j < Np; ++j) M[i * Np + j] += w * phi[i] * phi[j];
+        for (int d = 0; d < dim; ++d) {
+            // d phi_j / d x_d = sum_r dphi_j/dxi_r * Ainv[r][d]
+            for (int j = 0; j < Np; ++j) {
+                R gg = 0; for (int r = 0; r < dim; ++r) gg += dphi[j * dim + r] * O.Ainv[e * 3 * dim + r * 3 + d];
+                g[j] = gg;
+            }
+            for (int i = 0; i < Np; ++i) for (int j = 0; j < Np; ++j) S[d][i * Np + j] += w * phi[i] * g[j];
+        }
+    }
+    // Gauss-Jordan inverse of M in extended precision
+    vector<R> A = M, I(Np * Np, 0);
+    for (int i = 0; i < Np; ++i) I[i * Np + i] = 1;
+    for (int c = 0; c < Np; ++c) {
+        int best = c;
+        for (int r = c + 1; r < Np; ++r) if (fabsl(A[r * Np + c]) > fabsl(A[best * Np + c])) best = r;
+        for (int k = 0; k < Np; ++k) { std::swap(A[c * Np + k], A[best * Np + k]); std::swap(I[c * Np + k], I[best * Np + k]); }
+        R dv = 1 / A[c * Np + c];
+        for (int k = 0; k < Np; ++k) { A[c * Np + k] *= dv; I[c * Np + k] *= dv; }
+        for (int r = 0; r < Np; ++r) {
+            if (r == c) continue;
+            R f = A[r * Np + c];
+            if (f == 0) continue;
+            for (int k = 0; k < Np; ++k) { A[r * Np + k] -= f * A[c * Np + k]; I[r * Np + k] -= f * I[c * Np + k]; }
+        }
+    }
+    ElemMats m;
+    m.M.resize(Np * Np); m.Minv.resize(Np * Np);
+    for (int q2 = 0; q2 < Np * Np; ++q2) { m.M[q2] = static_cast<double>(M[q2]); m.Minv[q2] = static_cast<double>(I[q2]); }
+    for (int d = 0; d < 3; ++d) {
+        m.S[d].resize(Np * Np); m.D[d].assign(Np * Np, 0.0);
+        for (int q2 = 0; q2 < Np * Np; ++q2) m.S[d][q2] = static_cast<double>(S[d][q2]);
+        if (d >= dim) continue;
+        for (int i = 0; i < Np; ++i) for (int j = 0; j < Np; ++j) {
+            R acc = 0; for (int l = 0; l < Np; ++l) acc += I[i * Np + l] * S[d][l * Np + j];
+            m.D[d][i * Np + j] = static_cast<double>(acc);
+        }
+    }
+    return m;
+}
+
+// Elements sharing one affine map matrix share element matrices.
+static void shape_classes(Oracle& O, vector<int64_t>& rep)
+{
+    const int dim = O.dim;
+    std::map<vector<double>, int> cls;
+    O.shape_of.resize(O.K);
+    rep.clear();
+    for (int64_t e = 0; e < O.K; ++e) {
+        vector<double> key(O.A.begin() + e * 3 * dim, O.A.begin() + (e + 1) * 3 * dim);
+        for (auto& v : key) v = std::round(v * 1e12) / 1e12;
+        auto it = cls.find(key);
+        if (it == cls.end()) { int id = static_cast<int>(rep.size()); cls[key] = id; rep.push_back(e); O.shape_of[e] = id; }
+        else O.shape_of[e] = it->second;
+    }
+}
+
+// Face quadrature: physical points and weights (MFEM measure: ip.weight * |J_f|).
+static void face_points(const Oracle& O, const Face& F, vector<double>& xq, vector<double>& wq)
+{
+    xq.clear(); wq.clear();
+    if (O.dim == 1) {
+        double xi = (F.f1 == 0) ? 1.0 : 0.0, x[3];
+        O.ref_to_phys(F.e1, &xi, x);
+        xq.insert(xq.end(), x, x + 3); wq.push_back(1.0);
+        return;
+    }
+    Quad tq = tri_quad(O.p + 2);
+    const int nv = 4; const double* P[3]; int c = 0;
+    for (int q = 0; q < nv; ++q) if (q != F.f1) P[c++] = &O.verts[3 * O.elems[F.e1 * nv + q]];
+    for (size_t k = 0; k < tq.w.size(); ++k) {
+        double u = tq.x[2 * k], v = tq.x[2 * k + 1];
+        for (int r = 0; r < 3; ++r) xq.push_back(P[0][r] + u * (P[1][r] - P[0][r]) + v * (P[2][r] - P[0][r]));
+        wq.push_back(tq.w[k]);   // reference weight; |J_f| applied by the caller
+    }
+}
+
+// Rows of element `side` (1 = F.e1, 2 = F.e2) of one face integrator:
+// own block (rows and columns of that element) and coupling block (columns of
+// the other element). mode 0: zero-normal (w = beta/2 wq |J|), 1: one-normal
+// dir d (w = beta/2 wq n_d |J|, un-normalised normal), 2: two-normal (d, d2)
+// (w = beta/2 wq n_d n_d2 / |J| with the un-normalised normal).
+static void face_rows(const Oracle& O, const Face& F, int side, int mode, int d, int d2, double beta, bool decoupled,
+                      double* own, double* coup)
+{
+    const int Np = O.Np;
+    vector<double> xq, wq; face_points(O, F, xq, wq);
+    double nn = 1.0;
+    if (mode == 0) nn = F.jac;
+    if (mode == 1) nn = F.n[d] * F.jac;
+    if (mode == 2) nn = F.n[d] * F.n[d2] * F.jac;
+    const bool has2 = F.e2 >= 0;
+    std::fill(own, own + Np * Np, 0.0);
+    std::fill(coup, coup + Np * Np, 0.0);
+    vector<double> p1(Np), p2(Np);
+    for (size_t k = 0; k < wq.size(); ++k) {
+        double xi1[3], xi2[3];
+        O.phys_to_ref(F.e1, &xq[3 * k], xi1); O.B.shape(xi1, p1.data());
+        if (has2) { O.phys_to_ref(F.e2, &xq[3 * k], xi2); O.B.shape(xi2, p2.data()); }
+        const double w = 0.5 * beta * wq[k] * nn;
+        if (side == 1) {
+            // TL: +w p1 p1 ; TR: -w p1 p2 (buildFaceMatrix off-diagonal sign, IntegratorFunctions.cpp:85-98)
+            for (int i = 0; i < Np; ++i) for (int j = 0; j < Np; ++j) {
+                own[i * Np + j] += w * p1[i] * p1[j];
+                if (has2 && !decoupled) coup[i * Np + j] -= w * p1[i] * p2[j];
+            }
+        } else {
+            // element-2 rows: the one-normal integrator passes -w (BilinearIntegrators.cpp:83-90),
+            // the zero/two-normal ones +w; the interior-boundary integrator keeps only BR (:356-412).
+            const double s2 = (mode == 1) ? -1.0 : 1.0;
+            for (int i = 0; i < Np; ++i) for (int j = 0; j < Np; ++j) {
+                own[i * Np + j] += s2 * w * p2[i] * p2[j];
+                if (!decoupled) coup[i * Np + j] -= s2 * w * p2[i] * p1[j];
+            }
+        }
+    }
+}
+
+static void build_global(Oracle& O)
+{
+    const int Np = O.Np, dim = O.dim, nf = O.nfaces, R = 6 * Np, S = (1 + nf);
+    const int64_t N = O.N;
+    Quad vq;
+    if (dim == 3) vq = tet_quad(O.p + 3);
+    else { vector<double> g, gw; gauss_legendre01(O.p + 2, g, gw); vq.x = g; vq.w = gw; }
+
+    vector<int64_t> rep;
+    shape_classes(O, rep);
+    vector<ElemMats> cls_mats(rep.size());
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int64_t c = 0; c < static_cast<int64_t>(rep.size()); ++c) cls_mats[c] = elem_mats(O, rep[c], vq);
+
+    // per element: dense local rows [R][S slots][6][Np] -> compressed rows
+    vector<vector<int32_t>> colsA(O.K), colsT(O.K);
+    vector<vector<double>> valsA(O.K), valsT(O.K);
+    vector<vector<int32_t>> cntA(O.K), cntT(O.K);
+#pragma omp parallel
+    {
+        vector<double> LA(static_cast<size_t>(R) * S * R), LT(static_cast<size_t>(R) * S * R);
+        vector<double> own(Np * Np), coup(Np * Np), tmp(Np * Np);
+#pragma omp for schedule(dynamic, 8)
+        for (int64_t e = 0; e < O.K; ++e) {
+            std::fill(LA.begin(), LA.end(), 0.0);
+            std::fill(LT.begin(), LT.end(), 0.0);
+            const ElemMats& m = cls_mats[O.shape_of[e]];
+            int64_t slot_elem[5] = {e, -1, -1, -1, -1};
+            // add sign * scale * (Minv * blk | blk) at rows (field, rc), slot s cols (gfield, cc)
+            auto place_m = [&](vector<double>& L, int field, int rc, int gfield, int cc, int s, const double* bm, double sign,
+                               bool premultiplied) {
+                const double sc = sign * (field == 0 ? 1.0 / O.eps[e] : 1.0 / O.mu[e]);
+                for (int i = 0; i < Np; ++i)
+                    for (int j = 0; j < Np; ++j) {
+                        double acc;
+                        if (premultiplied) acc = bm[i * Np + j];
+                        else { acc = 0; for (int l = 0; l < Np; ++l) acc += m.Minv[i * Np + l] * bm[l * Np + j]; }
+                        L[(static_cast<size_t>((3 * field + rc) * Np + i) * S + s) * R + (3 * gfield + cc) * Np + j] += sc * acc;
+                    }
+            };
+            auto place = [&](vector<double>& L, int field, int rc, int gfield, int cc, int s, const double* bm, double sign) {
+                place_m(L, field, rc, gfield, cc, s, bm, sign, false);
+            };
+            // volume: directional operators MInv_f D_x (DGOperatorFactory.h:1061-1086)
+            for (int f = 0; f < 2; ++f)
+                for (int x = 0; x < dim; ++x) {
+                    int y = (x + 1) % 3, z = (x + 2) % 3;
+                    double sg = 1.0 - 2.0 * f;
+                    place_m(LA, f, z, 1 - f, y, 0, m.D[x].data(), sg, true);
+                    place_m(LA, f, y, 1 - f, z, 0, m.D[x].data(), -sg, true);
+                }
+            // conductivity (DGOperatorFactory.h:1194-1208): -MInv_E (sigma M) = -(sigma/eps) I
+            if (O.sig[e] != 0.0) {
+                std::fill(tmp.begin(), tmp.end(), 0.0);
+                for (int q = 0; q < Np; ++q) tmp[q * Np + q] = O.sig[e];
+                for (int d = 0; d < 3; ++d) place_m(LA, 0, d, 0, d, 0, tmp.data(), -1.0, true);
+            }
+            for (int lf = 0; lf < nf; ++lf) {
+                const Face& F = O.faces[O.elem_face[e * nf + lf]];
+                const int side = (F.e1 == e && F.f1 == lf) ? 1 : 2;
+                const int s = 1 + lf;
+                slot_elem[s] = (side == 1) ? F.e2 : F.e1;
+                if (F.kind == 1 && F.bc == BC_OPEN) continue;
+                const bool interior = (F.kind == 0 || F.kind == 2);
+                const bool sheet = (F.kind == 3);
+                for (int f = 0; f < 2; ++f) {
+                    const int g = 1 - f;
+                    // coefficients (DGOperatorFactory.h:469-573, 577-675): zero/two-normal
+                    // c[bc][f]*alpha (SMA: 1), one-normal c[bc][alt f] (SMA: 1); interior alpha / 1.
+                    double beta0, beta1;
+                    if (interior) { beta0 = O.alpha; beta1 = 1.0; }
+                    else if (F.bc == BC_SMA) { beta0 = 1.0; beta1 = 1.0; }
+                    else { beta0 = bc_coeff(F.bc, f) * O.alpha; beta1 = bc_coeff(F.bc, g); }
+                    auto both = [&](auto&& fn) { fn(LA); if (F.kind == 2) fn(LT); };
+                    if (beta0 != 0.0) {
+                        face_rows(O, F, side, 0, 0, 0, beta0, sheet, own.data(), coup.data());
+                        both([&](vector<double>& L) {
+                            for (int d = 0; d < 3; ++d) {
+                                place(L, f, d, f, d, 0, own.data(), -1.0);
+                                if (slot_elem[s] >= 0 && !sheet) place(L, f, d, f, d, s, coup.data(), -1.0);
+                            }
+                        });
+                        for (int d = 0; d < dim; ++d)
+                            for (int d2 = 0; d2 < dim; ++d2) {
+                                face_rows(O, F, side, 2, d, d2, beta0, sheet, own.data(), coup.data());
+                                both([&](vector<double>& L) {
+                                    place(L, f, d, f, d2, 0, own.data(), 1.0);
+                                    if (slot_elem[s] >= 0 && !sheet) place(L, f, d, f, d2, s, coup.data(), 1.0);
+                                });
+                            }
+                    }
+                    if (beta1 != 0.0)
+                        for (int x = 0; x < dim; ++x) {
+                            int y = (x + 1) % 3, z = (x + 2) % 3;
+                            double sg = 1.0 - 2.0 * f;
+                            face_rows(O, F, side, 1, x, 0, beta1, sheet, own.data(), coup.data());
+                            both([&](vector<double>& L) {
+                                place(L, f, y, g, z, 0, own.data(), sg);
+                                place(L, f, z, g, y, 0, own.data(), -sg);
+                                if (slot_elem[s] >= 0 && !sheet) {
+                                    place(L, f, y, g, z, s, coup.data(), sg);
+                                    place(L, f, z, g, y, s, coup.data(), -sg);
+                                }
+                            });
+                        }
+                }
+            }
+            // compress (Threshold(1e-20), DGOperatorFactory.h:1569-1570)
+            auto compress = [&](const vector<double>& L, vector<int32_t>& cols, vector<double>& vals, vector<int32_t>& cnt) {
+                cnt.assign(R, 0);
+                for (int r = 0; r < R; ++r)
+                    for (int s = 0; s < S; ++s) {
+                        if (slot_elem[s] < 0) continue;
+                        for (int c = 0; c < R; ++c) {
+                            double v = L[(static_cast<size_t>(r) * S + s) * R + c];
+                            if (std::fabs(v) <= 1e-20) continue;
+                            cols.push_back(static_cast<int32_t>((c / Np) * N + slot_elem[s] * Np + (c % Np)));
+                            vals.push_back(v);
+                            ++cnt[r];
+                        }
+                    }
+            };
+            compress(LA, colsA[e], valsA[e], cntA[e]);
+            compress(LT, colsT[e], valsT[e], cntT[e]);
+        }
+    }
+    auto finalize = [&](vector<vector<int32_t>>& cols, vector<vector<double>>& vals, vector<vector<int32_t>>& cnt, CSR& M) {
+        M.rows = 6 * N; M.cols = 6 * N;
+        M.rp.assign(6 * N + 1, 0);
+        for (int64_t e = 0; e < O.K; ++e)
+            for (int r = 0; r < R; ++r) M.rp[(r / Np) * N + e * Np + (r % Np) + 1] = cnt[e][r];
+        for (int64_t r = 0; r < 6 * N; ++r) M.rp[r + 1] += M.rp[r];
+        M.ci.resize(M.rp[6 * N]); M.v.resize(M.rp[6 * N]);
+#pragma omp parallel for schedule(dynamic, 64)
+        for (int64_t e = 0; e < O.K; ++e) {
+            size_t off = 0;
+            for (int r = 0; r < R; ++r) {
+                int64_t k = M.rp[(r / Np) * N + e * Np + (r % Np)];
+                for (int q = 0; q < cnt[e][r]; ++q) { M.ci[k + q] = cols[e][off + q]; M.v[k + q] = vals[e][off + q]; }
+                off += cnt[e][r];
+            }
+            vector<int32_t>().swap(cols[e]); vector<double>().swap(vals[e]);
+        }
+    };
+    finalize(colsA, valsA, cntA, O.Aglob);
+    finalize(colsT, valsT, cntT, O.Ttfsf);
+    O.have_csr = true;
+}
+
+// ---------------------------------------------------------------- sources
+static double profile(const PW& w, double s)
+{
+    double a = s - w.mean;
+    double g = std::exp(-a * a / (2.0 * w.spread * w.spread));
+    if (w.freq != 0.0) g *= std::cos(2.0 * M_PI * w.freq * a);
+    return g;
+}
+static void pw_at(const Oracle& O, const double* x, double t, double* e, double* h)
+{
+    for (int c = 0; c < 3; ++c) e[c] = h[c] = 0.0;
+    for (const PW& w : O.pws) {
+        double s = x[0] * w.k[0] + x[1] * w.k[1] + x[2] * w.k[2] - t;
+        double g = profile(w, s);
+        for (int c = 0; c < 3; ++c) { e[c] += g * w.pol[c]; h[c] += g * w.kxp[c]; }
+    }
+}
+
+// ||0.5 pw||^2 over all nodes of the TF/SF-adjacent elements (GlobalEvolution.cpp:587-598)
+static bool tfsf_skip(const Oracle& O, double t)
+{
+    if (O.pws.empty() || O.tfsf_elems.empty()) return true;
+    double acc = 0.0;
+    for (int32_t e : O.tfsf_elems)
+        for (int n = 0; n < O.Np; ++n) {
+            int64_t gi = static_cast<int64_t>(e) * O.Np + n;
+            double x[3] = {O.X[gi], O.X[O.N + gi], O.X[2 * O.N + gi]}, pe[3], ph[3];
+            pw_at(O, x, t, pe, ph);
+            for (int c = 0; c < 3; ++c) acc += 0.25 * (pe[c] * pe[c] + ph[c] * ph[c]);
+        }
+    return acc < 1e-16;
+}
+
+static void mult_global(Oracle& O, const double* x, double* y, double t)
+{
+    if (!O.have_csr) build_global(O);
+    O.Aglob.spmv(x, y, 1.0, false);
+    if (O.tfsf_elems.empty() || tfsf_skip(O, t)) return;
+    // w = +-0.5 pw on every DOF of the TF/SF-adjacent elements; out -= T w
+    vector<double> w(6 * O.N, 0.0);
+    vector<int> side(O.K, 0);
+    for (const Face& F : O.faces)
+        if (F.kind == 2) { side[F.e1] = F.tf_side; side[F.e2] = -F.tf_side; }
+    for (int32_t e : O.tfsf_elems) {
+        double sg = 0.5 * side[e];
+        for (int n = 0; n < O.Np; ++n) {
+            int64_t gi = static_cast<int64_t>(e) * O.Np + n;
+            double xx[3] = {O.X[gi], O.X[O.N + gi], O.X[2 * O.N + gi]}, pe[3], ph[3];
+            pw_at(O, xx, t, pe, ph);
+            for (int c = 0; c < 3; ++c) { w[c * O.N + gi] = sg * pe[c]; w[(3 + c) * O.N + gi] = sg * ph[c]; }
+        }
+    }
+    O.Ttfsf.spmv(w.data(), y, -1.0, true);
+}
+
+// ---------------------------------------------------------------- (B) nodal
+static void build_nodal(Oracle& O)
+{
+    const int Np = O.Np, Nfp = O.Nfp, dim = O.dim, nf = O.nfaces;
+    Quad vq;
+    if (dim == 3) vq = tet_quad(O.p + 3);
+    else { vector<double> g, gw; gauss_legendre01(O.p + 2, g, gw); vq.x = g; vq.w = gw; }
+    vector<int64_t> rep;
+    shape_classes(O, rep);
+    const int nc = static_cast<int>(rep.size());
+    O.Dx.assign(static_cast<size_t>(nc) * 3 * Np * Np, 0.0);
+    O.Lf.assign(static_cast<size_t>(nc) * nf * Np * Nfp, 0.0);
+    for (int c = 0; c < nc; ++c) {
+        int64_t e = rep[c];
+        ElemMats m = elem_mats(O, e, vq);
+        for (int d = 0; d < dim; ++d)
+            for (int q = 0; q < Np * Np; ++q) O.Dx[(static_cast<size_t>(c) * 3 + d) * Np * Np + q] = m.D[d][q];
+        // face mass of each local face, restricted to its nodes, premultiplied by M^-1
+        for (int f = 0; f < nf; ++f) {
+            Face tmp{}; tmp.e1 = e; tmp.f1 = f; tmp.e2 = -1;
+            double nrm[3]; double jac; face_normal(O, e, f, nrm, jac);
+            vector<double> xq, wq; face_points(O, tmp, xq, wq);
+            vector<double> Mf(Np * Nfp, 0.0), phi(Np);
+            for (size_t k = 0; k < wq.size(); ++k) {
+                double xi[3]; O.phys_to_ref(e, &xq[3 * k], xi); O.B.shape(xi, phi.data());
+                double w = wq[k] * jac;
+                for (int i = 0; i < Np; ++i)
+                    for (int a = 0; a < Nfp; ++a) Mf[i * Nfp + a] += w * phi[i] * phi[O.fnodes[f * Nfp + a]];
+            }
+            for (int i = 0; i < Np; ++i) for (int a = 0; a < Nfp; ++a) {
+                double s = 0; for (int l = 0; l < Np; ++l) s += m.Minv[i * Np + l] * Mf[l * Nfp + a];
+                O.Lf[((static_cast<size_t>(c) * nf + f) * Np + i) * Nfp + a] = s;
+            }
+        }
+    }
+    // node maps by coordinate matching
+    O.vmapP.assign(O.K * nf * Nfp, -1);
+    for (int64_t e = 0; e < O.K; ++e)
+        for (int f = 0; f < nf; ++f) {
+            const Face& F = O.faces[O.elem_face[e * nf + f]];
+            int64_t en = (F.e1 == e) ? F.e2 : F.e1;
+            int fn = (F.e1 == e) ? F.f2 : F.f1;
+            for (int a = 0; a < Nfp; ++a) {
+                int64_t gm = e * Np + O.fnodes[f * Nfp + a];
+                if (en < 0) { O.vmapP[(e * nf + f) * Nfp + a] = gm; continue; }
+                double best = 1e300; int64_t bi = -1;
+                for (int b = 0; b < Nfp; ++b) {
+                    int64_t gp = en * Np + O.fnodes[fn * Nfp + b];
+                    double d = 0; for (int r = 0; r < 3; ++r) { double q = O.X[r * O.N + gm] - O.X[r * O.N + gp]; d += q * q; }
+                    if (d < best) { best = d; bi = gp; }
+                }
+                O.vmapP[(e * nf + f) * Nfp + a] = bi;
+            }
+        }
+    O.have_nodal = true;
+}
+
+static void mult_nodal(Oracle& O, const double* u, double* out, double t)
+{
+    if (!O.have_nodal) build_nodal(O);
+    const int Np = O.Np, Nfp = O.Nfp, nf = O.nfaces, dim = O.dim;
+    const int64_t N = O.N;
+    const bool skip = O.tfsf_elems.empty() || tfsf_skip(O, t);
+#pragma omp parallel for schedule(static)
+    for (int64_t e = 0; e < O.K; ++e) {
+        const int c = O.shape_of[e];
+        vector<double> flux(6 * nf * Nfp);
+        for (int f = 0; f < nf; ++f) {
+            const Face& F = O.faces[O.elem_face[e * nf + f]];
+            double n[3] = {F.n[0], F.n[1], F.n[2]};
+            if (F.e1 != e) for (int r = 0; r < 3; ++r) n[r] = -n[r];
+            for (int a = 0; a < Nfp; ++a) {
+                int64_t gm = e * Np + O.fnodes[f * Nfp + a];
+                int64_t gp = O.vmapP[(e * nf + f) * Nfp + a];
+                double dE[3], dH[3], aE = O.alpha, aH = O.alpha;
+                for (int q = 0; q < 3; ++q) { dE[q] = u[q * N + gp] - u[q * N + gm]; dH[q] = u[(3 + q) * N + gp] - u[(3 + q) * N + gm]; }
+                int bc = -1;
+                if (F.kind == 1 || F.kind == 3) bc = F.bc;
+                if (bc >= 0) {
+                    // image rules equivalent to the assembled boundary coefficients
+                    double cE = bc_coeff(bc, 0), cH = bc_coeff(bc, 1);
+                    if (bc == BC_OPEN) { cE = 0; cH = 0; }
+                    for (int q = 0; q < 3; ++q) { dE[q] = -cE * u[q * N + gm]; dH[q] = -cH * u[(3 + q) * N + gm]; }
+                    if (bc == BC_SMA) { aE = 1.0; aH = 1.0; }
+                }
+                if (F.kind == 2 && !skip) {
+                    int side = (F.e1 == e) ? F.tf_side : -F.tf_side;
+                    double xx[3] = {O.X[gm], O.X[N + gm], O.X[2 * N + gm]}, pe[3], ph[3];
+                    pw_at(O, xx, t, pe, ph);
+                    for (int q = 0; q < 3; ++q) { dE[q] += side * pe[q]; dH[q] += side * ph[q]; }
+                }
+                double ndE = n[0] * dE[0] + n[1] * dE[1] + n[2] * dE[2];
+                double ndH = n[0] * dH[0] + n[1] * dH[1] + n[2] * dH[2];
+                double fe[3], fh[3];
+                fe[0] = (n[1] * dH[2] - n[2] * dH[1]) + aE * (dE[0] - ndE * n[0]);
+                fe[1] = (n[2] * dH[0] - n[0] * dH[2]) + aE * (dE[1] - ndE * n[1]);
+                fe[2] = (n[0] * dH[1] - n[1] * dH[0]) + aE * (dE[2] - ndE * n[2]);
+                fh[0] = -(n[1] * dE[2] - n[2] * dE[1]) + aH * (dH[0] - ndH * n[0]);
+                fh[1] = -(n[2] * dE[0] - n[0] * dE[2]) + aH * (dH[1] - ndH * n[1]);
+                fh[2] = -(n[0] * dE[1] - n[1] * dE[0]) + aH * (dH[2] - ndH * n[2]);
+                for (int q = 0; q < 3; ++q) {
+                    flux[(q * nf + f) * Nfp + a] = 0.5 * fe[q];
+                    flux[((3 + q) * nf + f) * Nfp + a] = 0.5 * fh[q];
+                }
+            }
+        }
+        const double ie = 1.0 / O.eps[e], im = 1.0 / O.mu[e], se = O.sig[e] / O.eps[e];
+        for (int i = 0; i < Np; ++i) {
+            double d[6][3] = {};
+            for (int dd = 0; dd < dim; ++dd) {
+                const double* Drow = &O.Dx[((static_cast<size_t>(c) * 3 + dd) * Np + i) * Np];
+                for (int q = 0; q < 6; ++q) {
+                    double s = 0; for (int j = 0; j < Np; ++j) s += Drow[j] * u[q * N + e * Np + j];
+                    d[q][dd] = s;
+                }
+            }
+            double lf[6] = {};
+            for (int f = 0; f < nf; ++f) {
+                const double* L = &O.Lf[((static_cast<size_t>(c) * nf + f) * Np + i) * Nfp];
+                for (int q = 0; q < 6; ++q) {
+                    double s = 0; for (int a = 0; a < Nfp; ++a) s += L[a] * flux[(q * nf + f) * Nfp + a];
+                    lf[q] += s;
+                }
+            }
+            // curl: (curl F)_x = dF_z/dy - dF_y/dz ...
+            double cH[3] = {d[5][1] - d[4][2], d[3][2] - d[5][0], d[4][0] - d[3][1]};
+            double cE[3] = {d[2][1] - d[1][2], d[0][2] - d[2][0], d[1][0] - d[0][1]};
+            int64_t gi = e * Np + i;
+            for (int q = 0; q < 3; ++q) {
+                out[q * N + gi] = ie * (cH[q] + lf[q]) - se * u[q * N + gi];
+                out[(3 + q) * N + gi] = im * (-cE[q] + lf[3 + q]);
+            }
+        }
+    }
+}
+
+static void mult(Oracle& O, int form, const double* x, double* y, double t)
+{
+    if (form == 0) mult_global(O, x, y, t);
+    else mult_nodal(O, x, y, t);
+}
+
+// mfem::RK4Solver::Step register sequence.
+static void rk4_step(Oracle& O, int form, double* x, double t, double dt, vector<double>& k, vector<double>& y,
+                     vector<double>& z)
+{
+    const int64_t L = 6 * O.N;
+    mult(O, form, x, k.data(), t);
+    for (int64_t i = 0; i < L; ++i) { y[i] = x[i] + dt / 2 * k[i]; z[i] = x[i] + dt / 6 * k[i]; }
+    mult(O, form, y.data(), k.data(), t + dt / 2);
+    for (int64_t i = 0; i < L; ++i) { y[i] = x[i] + dt / 2 * k[i]; z[i] += dt / 3 * k[i]; }
+    mult(O, form, y.data(), k.data(), t + dt / 2);
+    for (int64_t i = 0; i < L; ++i) { y[i] = x[i] + dt * k[i]; z[i] += dt / 3 * k[i]; }
+    mult(O, form, y.data(), k.data(), t + dt);
+    for (int64_t i = 0; i < L; ++i) x[i] = z[i] + dt / 6 * k[i];
+}
+
+static const double LSA[5] = {0.0, -567301805773.0 / 1357537059087.0, -2404267990393.0 / 2016746695238.0,
+                              -3550918686646.0 / 2091501179385.0, -1275806237668.0 / 842570457699.0};
+static const double LSB[5] = {1432997174477.0 / 9575080441755.0, 5161836677717.0 / 13612068292357.0,
+                              1720146321549.0 / 2090206949498.0, 3134564353537.0 / 4481467310338.0,
+                              2277821191437.0 / 14882151754819.0};
+static const double LSC[5] = {0.0, 1432997174477.0 / 9575080441755.0, 2526269341429.0 / 6820363962896.0,
+                              2006345519317.0 / 3224310063776.0, 2802321613138.0 / 2924317926251.0};
+
+static void lserk_step(Oracle& O, int form, double* x, double t, double dt, vector<double>& k, vector<double>& res)
+{
+    const int64_t L = 6 * O.N;
+    for (int s = 0; s < 5; ++s) {
+        mult(O, form, x, k.data(), t + LSC[s] * dt);
+        for (int64_t i = 0; i < L; ++i) { res[i] = LSA[s] * res[i] + dt * k[i]; x[i] += LSB[s] * res[i]; }
+    }
+}
+
+}  // namespace orc
+
+// ================================================================ C API
+extern "C" {
+
+static thread_local std::string g_orc_err;
+const char* orc_last_error(void) { return g_orc_err.c_str(); }
+
+void* orc_create(int dim, int order, double alpha, int64_t nv, const double* verts, int64_t ne, const int32_t* elems,
+                 const double* eps, const double* mu, const double* sigma, int64_t nb, const int32_t* bfaces,
+                 const int32_t* bcodes, int64_t nt, const int32_t* tfaces, int64_t ni, const int32_t* ifaces,
+                 const int32_t* icodes)
+{
+    try {
+        if (dim != 1 && dim != 3) throw std::runtime_error("oracle: dim must be 1 or 3");
+        auto O = std::make_unique<orc::Oracle>();
+        O->dim = dim; O->p = order; O->alpha = alpha; O->K = ne;
+        O->B.init(dim, order);
+        O->Np = O->B.Np;
+        O->verts.assign(verts, verts + 3 * nv);
+        O->elems.assign(elems, elems + (dim + 1) * ne);
+        O->eps.assign(ne, 1.0); O->mu.assign(ne, 1.0); O->sig.assign(ne, 0.0);
+        if (eps) O->eps.assign(eps, eps + ne);
+        if (mu) O->mu.assign(mu, mu + ne);
+        if (sigma) O->sig.assign(sigma, sigma + ne);
+        orc::build_geometry(*O);
+        orc::local_face_nodes(*O);
+        orc::build_faces(*O, nb, bfaces, bcodes, nt, tfaces, ni, ifaces, icodes);
+        return O.release();
+    } catch (const std::exception& e) {
+        g_orc_err = e.what();
+        return nullptr;
+    }
+}
+
+void orc_destroy(void* h) { delete static_cast<orc::Oracle*>(h); }
+int64_t orc_ndofs(void* h) { return static_cast<orc::Oracle*>(h)->N; }
+int orc_np(void* h) { return static_cast<orc::Oracle*>(h)->Np; }
+void orc_nodes(void* h, double* xyz)
+{
+    auto* O = static_cast<orc::Oracle*>(h);
+    std::memcpy(xyz, O->X.data(), O->X.size() * sizeof(double));
+}
+
+// params: [n][11] = k(3), pol(3), spread, mean, freq, unused, unused
+void orc_set_planewaves(void* h, int n, const double* prm)
+{
+    auto* O = static_cast<orc::Oracle*>(h);
+    O->pws.clear();
+    for (int i = 0; i < n; ++i) {
+        const double* q = prm + 11 * i;
+        orc::PW w{};
+        double kn = std::sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2]);
+        double pn = std::sqrt(q[3] * q[3] + q[4] * q[4] + q[5] * q[5]);
+        for (int c = 0; c < 3; ++c) { w.k[c] = q[c] / kn; w.pol[c] = q[3 + c] / pn; }
+        orc::cross(w.k, w.pol, w.kxp);
+        w.spread = q[6]; w.mean = q[7]; w.freq = q[8];
+        O->pws.push_back(w);
+    }
+}
+
+int orc_mult(void* h, int form, const double* x, double* y, double t)
+{
+    try { orc::mult(*static_cast<orc::Oracle*>(h), form, x, y, t); }
+    catch (const std::exception& e) { g_orc_err = e.what(); return -1; }
+    return 0;
+}
+
+int orc_step(void* h, int form, double* x, double t0, double dt, int nsteps, int integrator)
+{
+    try {
+        auto& O = *static_cast<orc::Oracle*>(h);
+        const int64_t L = 6 * O.N;
+        std::vector<double> k(L), y(L), z(L, 0.0);
+        double t = t0;
+        for (int s = 0; s < nsteps; ++s) {
+            if (integrator == 0) orc::rk4_step(O, form, x, t, dt, k, y, z);
+            else orc::lserk_step(O, form, x, t, dt, k, z);
+            t += dt;
+        }
+    } catch (const std::exception& e) { g_orc_err = e.what(); return -1; }
+    return 0;
+}
+
+// Reference run loop (Solver::run, Solver.cpp:483-551)
+int orc_run(void* h, int form, double* x, double t0, double dt, double T, int integrator, int64_t* steps)
+{
+    try {
+        auto& O = *static_cast<orc::Oracle*>(h);
+        const int64_t L = 6 * O.N;
+        std::vector<double> k(L), y(L), z(L, 0.0);
+        double t = t0; int64_t n = 0;
+        while (t <= T - 1e-8 * dt) {
+            double h2 = std::min(dt, T - t);
+            if (integrator == 0) orc::rk4_step(O, form, x, t, h2, k, y, z);
+            else orc::lserk_step(O, form, x, t, h2, k, z);
+            t += h2; ++n;
+        }
+        if (steps) *steps = n;
+    } catch (const std::exception& e) { g_orc_err = e.what(); return -1; }
+    return 0;
+}
+
+int64_t orc_nnz(void* h)
+{
+    auto& O = *static_cast<orc::Oracle*>(h);
+    if (!O.have_csr) orc::build_global(O);
+    return static_cast<int64_t>(O.Aglob.v.size());
+}
+
+// Element matrices on one element with the given vertices (for known-answer tests):
+// M, Minv, D_x, D_y, D_z (each Np x Np); D_d = M^-1 S_d, S_d = int phi_i dphi_j/dx_d.
+int orc_element_matrices(int dim, int order, const double* verts, double* M, double* Minv, double* Sx, double* Sy,
+                         double* Sz)
+{
+    try {
+        int32_t el[4] = {0, 1, 2, 3};
+        void* h = orc_create(dim, order, 1.0, dim + 1, verts, 1, el, nullptr, nullptr, nullptr, 0, nullptr, nullptr, 0,
+                             nullptr, 0, nullptr, nullptr);
+        if (!h) return -1;
+        auto& O = *static_cast<orc::Oracle*>(h);
+        orc::Quad vq;
+        if (dim == 3) vq = orc::tet_quad(order + 3);
+        else { std::vector<double> g, gw; orc::gauss_legendre01(order + 2, g, gw); vq.x = g; vq.w = gw; }
+        auto m = orc::elem_mats(O, 0, vq);
+        const size_t n2 = static_cast<size_t>(O.Np) * O.Np;
+        if (M) std::memcpy(M, m.M.data(), n2 * sizeof(double));
+        if (Minv) std::memcpy(Minv, m.Minv.data(), n2 * sizeof(double));
+        if (Sx) std::memcpy(Sx, m.D[0].data(), n2 * sizeof(double));
+        if (Sy) std::memcpy(Sy, m.D[1].data(), n2 * sizeof(double));
+        if (Sz) std::memcpy(Sz, m.D[2].data(), n2 * sizeof(double));
+        orc_destroy(h);
+    } catch (const std::exception& e) { g_orc_err = e.what(); return -1; }
+    return 0;
+}
+
+// One scalar sub-operator as a dense [N x N] matrix (N = K Np), for known-answer
+// tests of the integrators (reference test/hesthavenComparison/Hesthaven1DTest.cpp):
+// out = (M^-1 / minv_coef) * F with F one of
+//   kind 0: zero-normal jump form, 1: one-normal (dir d), 2: two-normal (d, d2),
+//   3: strong derivative S_d = int phi_i dphi_j/dx_d (no faces),
+// assembled with beta_int on interior faces and beta_bdr on every boundary face.
+int orc_subop(void* h, int kind, int d, int d2, double beta_int, double beta_bdr, double minv_coef, double* out)
+{
+    try {
+        auto& O = *static_cast<orc::Oracle*>(h);
+        const int Np = O.Np, nf = O.nfaces;
+        const int64_t N = O.N;
+        std::memset(out, 0, sizeof(double) * N * N);
+        orc::Quad vq;
+        if (O.dim == 3) vq = orc::tet_quad(O.p + 3);
+        else { std::vector<double> g, gw; orc::gauss_legendre01(O.p + 2, g, gw); vq.x = g; vq.w = gw; }
+        std::vector<double> own(Np * Np), coup(Np * Np);
+        for (int64_t e = 0; e < O.K; ++e) {
+            orc::ElemMats m = orc::elem_mats(O, e, vq);
+            std::vector<double> rows(static_cast<size_t>(Np) * N, 0.0);
+            if (kind == 3) {
+                // D = M^-1 S  -> S = M D
+                for (int i = 0; i < Np; ++i) for (int j = 0; j < Np; ++j) {
+                    double acc = 0; for (int l = 0; l < Np; ++l) acc += m.M[i * Np + l] * m.D[d][l * Np + j];
+                    rows[static_cast<size_t>(i) * N + e * Np + j] = acc;
+                }
+            } else {
+                for (int lf = 0; lf < nf; ++lf) {
+                    const orc::Face& F = O.faces[O.elem_face[e * nf + lf]];
+                    const int side = (F.e1 == e && F.f1 == lf) ? 1 : 2;
+                    const double beta = (F.e2 >= 0) ? beta_int : beta_bdr;
+                    orc::face_rows(O, F, side, kind, d, d2, beta, false, own.data(), coup.data());
+                    int64_t other = (side == 1) ? F.e2 : F.e1;
+                    for (int i = 0; i < Np; ++i) for (int j = 0; j < Np; ++j) {
+                        rows[static_cast<size_t>(i) * N + e * Np + j] += own[i * Np + j];
+                        if (other >= 0) rows[static_cast<size_t>(i) * N + other * Np + j] += coup[i * Np + j];
+                    }
+                }
+            }
+            for (int i = 0; i < Np; ++i)
+                for (int64_t c = 0; c < N; ++c) {
+                    double acc = 0; for (int l = 0; l < Np; ++l) acc += m.Minv[i * Np + l] * rows[static_cast<size_t>(l) * N + c];
+                    out[(e * Np + i) * N + c] = acc / minv_coef;
+                }
+        }
+    } catch (const std::exception& ex) { g_orc_err = ex.what(); return -1; }
+    return 0;
+}
+
+// Emat of the reference's Hesthaven reference tetrahedron ((0,0,0),(2,0,0),(0,2,0),(0,0,2)),
+// as assembled by assembleHesthavenRefElemEmat (HesthavenEvolution.cpp:53-81): for each
+// face f, the face mass of the element basis (weight 2 * ip.weight, no face Jacobian),
+// columns restricted to the face's nodes in ascending order, times 2 for tetrahedra.
+int orc_ref_emat(int order, double* emat)
+{
+    try {
+        orc::Basis B; B.init(3, order);
+        const int Np = B.Np, Nfp = (order + 1) * (order + 2) / 2;
+        orc::Quad tq = orc::tri_quad(order + 2);
+        std::memset(emat, 0, sizeof(double) * Np * 4 * Nfp);
+        // MFEM reference-tet face vertex sets, face f opposite vertex f
+        const double V[4][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+        std::vector<double> phi(Np);
+        for (int f = 0; f < 4; ++f) {
+            int vv[3], c = 0; for (int q = 0; q < 4; ++q) if (q != f) vv[c++] = q;
+            std::vector<int> fn;
+            for (int n = 0; n < Np; ++n) { double lam[4]; B.lam_of(&B.nodes[3 * n], lam); if (std::fabs(lam[f]) < 1e-12) fn.push_back(n); }
+            for (size_t k = 0; k < tq.w.size(); ++k) {
+                double u = tq.x[2 * k], v = tq.x[2 * k + 1], xi[3];
+                for (int r = 0; r < 3; ++r) xi[r] = V[vv[0]][r] + u * (V[vv[1]][r] - V[vv[0]][r]) + v * (V[vv[2]][r] - V[vv[0]][r]);
+                B.shape(xi, phi.data());
+                double w = 2.0 * tq.w[k] * 2.0;
+                for (int i = 0; i < Np; ++i)
+                    for (int a = 0; a < Nfp; ++a) emat[i * 4 * Nfp + f * Nfp + a] += w * phi[i] * phi[fn[a]];
+            }
+        }
+    } catch (const std::exception& e) { g_orc_err = e.what(); return -1; }
+    return 0;
+}
+
+// Gauss-Lobatto points on [0,1] (the 1D node set), for tests.
+int orc_lobatto(int p, double* out)
+{
+    auto g = orc::lobatto01(p);
+    std::memcpy(out, g.data(), g.size() * sizeof(double));
+    return 0;
+}
+
+int orc_threads(void)
+{
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+}  // extern "C"

@@ -1,0 +1,38 @@
+"""Shared test setup: the `gpu` marker, library builds, common fixtures."""
+import os
+import sys
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parent.parent
+if str(ROOT) not in sys.path:
+    sys.path.insert(0, str(ROOT))
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
+
+
+def _ensure_built():
+    from dgtd_gb300 import build as pkg_build
+    from oracle import pyoracle
+    pkg_build.build()
+    pyoracle.build()
+
+
+_ensure_built()
+
+
+@pytest.fixture(scope="session")
+def torch_cuda():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return torch
+
+
+def rel_l2(a, b):
+    import numpy as np
+    nb = np.linalg.norm(b)
+    return float(np.linalg.norm(a - b) / (nb if nb > 0 else 1.0))

@@ -1,0 +1,346 @@
+"""Benchmark of the DG Maxwell time step (DOF-updates/s) on GB300.
+
+Contract: ``python bench.py --gpus N --steps K --warmup W [--impl ours|reference]``
+prints ONE JSON line on rank 0.
+
+A "step" is one full RK4 time step (all stages) of the workload over its mesh.
+``value`` is the device-timed rate with inputs resident in HBM; ``e2e`` is the
+same metric through the C ABI with host buffers (host->device copy of the
+state, the step, device->host read of the state) inside the timed region.
+
+N > 1: the path is replicas only (independent solves, no collective); every
+rank runs its own copy of the workload on its GPU and ``value`` sums them.
+
+``--impl reference`` times the reference algorithm's CPU implementation on the
+host cores: the reference cannot be built here (its MFEM fork is not vendored),
+so this is the CPU restatement in oracle/ (assembled CSR + RK4, OpenMP),
+stepped on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "DOF-updates/s"
+UNIT = "DOF-updates/s"
+
+
+# ----------------------------------------------------------------------------- workloads
+def te110_state(xyz: np.ndarray) -> np.ndarray:
+    x, y = xyz[0], xyz[1]
+    z = np.zeros_like(x)
+    return np.concatenate([z, z, np.sin(np.pi * x) * np.sin(np.pi * y), z, z, z])
+
+
+WORKLOADS = {
+    "cubic_resonator_fp64": dict(
+        desc="3D PEC cubic resonator: unit cube 8^3 hexes x 6 tets (3,072), p=3 (Np=20), eps=mu=1, "
+             "upwind, TE110 initial mode, classical RK4, dt=1e-3; plain FP64 form",
+        cells=(8, 8, 8), lo=(0, 0, 0), hi=(1, 1, 1), order=3, batch=1, dt=1e-3, precision="fp64",
+        outer_bc="PEC", init="te110", dtype="f64"),
+}
+DEFAULT_WORKLOAD = "cubic_resonator_fp64"
+
+
+def build_mesh(w: dict):
+    import dgtd_gb300 as dg
+    bc = {"PEC": dg.BC_PEC, "SMA": dg.BC_SMA, "PMC": dg.BC_PMC}[w["outer_bc"]]
+    return dg.box_mesh(w["cells"], lo=w["lo"], hi=w["hi"], hole=w.get("hole"), tfsf=w.get("tfsf"), outer_bc=bc)
+
+
+def initial_state(w: dict, xyz: np.ndarray) -> np.ndarray:
+    if w["init"] == "te110":
+        return te110_state(xyz)
+    raise ValueError(w["init"])
+
+
+# ----------------------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi clocks/throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        if self.proc is None or self.path is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in Path(self.path).read_text().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1])); mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+# ----------------------------------------------------------------------------- helpers
+def measured_peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return {"hbm_gbs": d.get("hbm_gbs", 6800.0), "bf16_tflops": d.get("bf16_tflops", 1900.0), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "source": "fallback"}
+
+
+def profile_traffic(kernel: str, workload: str):
+    """Per-launch DRAM bytes of the dominant kernel from the committed ncu summary, if present."""
+    f = ROOT / "profiles" / f"{kernel}__{workload}.json"
+    if f.exists():
+        return json.loads(f.read_text()).get("dram_bytes_per_launch")
+    return None
+
+
+def dist_init(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if args.impl == "ours" else "gloo"
+        dist.init_process_group(backend=backend)
+    return world, rank, local
+
+
+def max_over_ranks(v: float, world: int, device=None) -> float:
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world: int):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+# ----------------------------------------------------------------------------- CPU side
+def cpu_rate(w: dict, budget_s: float, max_steps: int | None = None) -> dict:
+    """Time the oracle's assembled-CSR RK4 (the reference's default algorithm) on a sample."""
+    from oracle import pyoracle as po
+    mesh = build_mesh(w)
+    orc = po.Oracle.from_mesh(mesh, w["order"])
+    x = initial_state(w, orc.nodes())
+    t_build0 = time.perf_counter()
+    orc.nnz()                                    # assemble outside the timed sample
+    t_build = time.perf_counter() - t_build0
+    orc.step(x, 0.0, w["dt"], 1)                 # warm-up (page-in)
+    steps, t0 = 0, time.perf_counter()
+    t = 0.0
+    while True:
+        x = orc.step(x, t, w["dt"], 1)
+        t += w["dt"]; steps += 1
+        el = time.perf_counter() - t0
+        if el >= budget_s or (max_steps is not None and steps >= max_steps):
+            break
+    dofs = 6 * orc.ndofs
+    return {"value": dofs * steps / el, "seconds": el, "steps": steps, "dofs": dofs, "cores": po.threads(),
+            "assembly_s": t_build, "nnz": orc.nnz()}
+
+
+# ----------------------------------------------------------------------------- GPU side
+def run_ours(args, world, rank, local):
+    import torch
+    import dgtd_gb300 as dg
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    w = WORKLOADS[args.workload]
+    mesh = build_mesh(w)
+    prec = dg.FP64 if w["precision"] == "fp64" else dg.FP32_3XTF32
+    t_setup0 = time.perf_counter()
+    op = dg.Operator(mesh, order=w["order"], alpha=1.0, precision=prec, batch=w["batch"])
+    setup_s = time.perf_counter() - t_setup0
+    xyz = op.node_coords()
+    x0 = np.tile(initial_state(w, xyz), w["batch"])
+    state = torch.from_numpy(x0).to(dev)
+    stream = torch.cuda.current_stream(dev)
+    dt = w["dt"]
+    dofs = 6 * op.ndofs * w["batch"]
+    flush = torch.empty(int(256 * 2 ** 20) // 4, dtype=torch.float32, device=dev)   # 256 MB > 129 MB L2
+
+    t = 0.0
+    for _ in range(args.warmup):
+        op.step(state, t, dt, 1, stream=stream); t += dt
+    torch.cuda.synchronize(dev)
+
+    n_launch0 = dg.kernel_launches()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    barrier(world)
+    torch.cuda.synchronize(dev)
+    with ClockSampler(local) as clk:
+        for k in range(args.steps):
+            flush.zero_()                                 # L2 flush between timed steps (not timed)
+            ev[k][0].record(stream)
+            op.step(state, t, dt, 1, stream=stream)
+            ev[k][1].record(stream)
+            t += dt
+        torch.cuda.synchronize(dev)
+    barrier(world)
+    launches = dg.kernel_launches() - n_launch0
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    total_s = sum(step_ms) / 1e3
+    total_s = max_over_ranks(total_s, world, dev)
+    value = world * dofs * args.steps / total_s
+    ms_per_step = total_s * 1e3 / args.steps
+    if not np.all(np.isfinite(state.cpu().numpy())):
+        raise RuntimeError("non-finite state after the timed steps")
+
+    # --- end to end through the C ABI with host buffers (pinned), copies inside the timed region
+    host = torch.from_numpy(x0.copy()).pin_memory()
+    out = torch.empty_like(host).pin_memory()
+    dstate = torch.empty_like(state)
+    e2e_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    t2 = 0.0
+    torch.cuda.synchronize(dev)
+    for k in range(args.steps):
+        flush.zero_()
+        e2e_ev[k][0].record(stream)
+        dstate.copy_(host, non_blocking=True)
+        op.step(dstate, t2, dt, 1, stream=stream)
+        out.copy_(dstate, non_blocking=True)
+        e2e_ev[k][1].record(stream)
+        t2 += dt
+    torch.cuda.synchronize(dev)
+    e2e_s = max_over_ranks(sum(a.elapsed_time(b) for a, b in e2e_ev) / 1e3, world, dev)
+    state_bytes = int(x0.nbytes)
+
+    # --- roofline of the dominant kernel (the fused stage kernel; RK4 = 4 launches per step)
+    peaks = measured_peaks()
+    launches_per_step = launches / args.steps
+    stage_launches = 4
+    avg_launch_s = (total_s / args.steps) / stage_launches
+    word = 8 if prec == dg.FP64 else 4
+    K, Np = op.info["n_elements"], op.info["np"]
+    nfp = op.info["nfp"]
+    # algorithmic bytes per DOF per RK4 step: 16 words (x, y, z registers: 3+5+5+3)
+    alg_bytes_launch = 16 * word * dofs / stage_launches
+    achieved_gbs = alg_bytes_launch / avg_launch_s / 1e9
+    flops_per_dof_step = 4 * (6 * Np + 8 * nfp)          # contraction terms, FMA = 2
+    achieved_tflops = flops_per_dof_step * dofs / (total_s / args.steps) / 1e12
+    traffic = profile_traffic("stage_fp64", args.workload)
+    roofline = {"bound": "hbm", "achieved": round(achieved_gbs, 2), "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                "frac": round(achieved_gbs / peaks["hbm_gbs"], 4), "traffic": traffic,
+                "peak_source": peaks["source"], "kernel": "stage_fp64",
+                "algorithmic_bytes_per_launch": alg_bytes_launch, "avg_launch_ms": avg_launch_s * 1e3,
+                "fp64_pipe": {"achieved_tflops": round(achieved_tflops, 4), "nominal_peak_tflops": 1.25,
+                              "frac_of_nominal": round(achieved_tflops / 1.25, 4),
+                              "note": "plain FP64 form is FP64-issue bound; FP64 peak is the nominal GB300 figure, not measured"}}
+    return dict(value=value, ms_per_step=ms_per_step, e2e_value=world * dofs * args.steps / e2e_s,
+                state_bytes=state_bytes, launches=launches, clocks=clk.summary(), roofline=roofline,
+                setup_s=setup_s, w=w, dofs=dofs, K=K, Np=Np)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default=DEFAULT_WORKLOAD)
+    ap.add_argument("--cpu-budget", type=float, default=15.0, help="seconds of CPU baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    world, rank, local = dist_init(args)
+    w = WORKLOADS[args.workload]
+    config = {"workload": args.workload, "description": w["desc"], "elements": None, "order": w["order"],
+              "incidences": w["batch"], "dt": w["dt"], "integrator": "RK4",
+              "l2": "flushed between timed steps (256 MB write)", "parallelism": f"replicas x{world}"}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        n_steps = max(1, args.steps)
+        # bounded: each step is one RK4 step of the workload on the host cores
+        for _ in range(min(args.warmup, 1)):
+            pass
+        r = cpu_rate(w, budget_s=min(args.cpu_budget * 4, 120.0), max_steps=n_steps)
+        config["elements"] = None
+        line = {"metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": args.gpus, "steps": r["steps"],
+                "warmup": 1, "ms_per_step": r["seconds"] * 1e3 / r["steps"], "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+                "config": config,
+                "cpu_baseline": {"value": r["value"], "unit": UNIT, "cores": r["cores"], "kind": "port",
+                                 "sample": f"{r['steps']} RK4 steps of the workload with the oracle's assembled CSR "
+                                           f"operator ({r['nnz']} nnz), assembly ({r['assembly_s']:.1f} s) excluded"},
+                "e2e": {"value": r["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+
+    r = run_ours(args, world, rank, local)
+    config["elements"] = r["K"]
+    config["dofs_per_step"] = r["dofs"]
+    if rank != 0:
+        return
+    cpu = None
+    if not args.no_cpu_baseline and world == 1:
+        c = cpu_rate(w, budget_s=args.cpu_budget)
+        cpu = {"value": c["value"], "unit": UNIT, "cores": c["cores"], "kind": "port",
+               "sample": f"{c['steps']} RK4 steps ({c['seconds']:.1f} s) of the same mesh with the oracle's "
+                         f"assembled CSR operator (GlobalEvolution restatement, {c['nnz']} nnz), OpenMP"}
+    line = {"metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": r["w"]["dtype"], "data": "synthetic", "config": config,
+            "e2e": {"value": r["e2e_value"], "unit": UNIT, "h2d_bytes_per_step": r["state_bytes"],
+                    "d2h_bytes_per_step": r["state_bytes"]},
+            "gpu_launches": r["launches"], "clocks": r["clocks"], "roofline": r["roofline"],
+            "cpu_baseline": cpu, "setup_s": r["setup_s"]}
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

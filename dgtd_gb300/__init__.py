@@ -72,6 +72,7 @@ _I32 = C.POINTER(C.c_int32)
 _I64 = C.POINTER(C.c_int64)
 SIGNATURES = {
     "dgtd_last_error": (C.c_char_p, []),
+    "dgtd_kernel_launches": (C.c_uint64, []),
     "dgtd_op_create": (C.c_int, [C.POINTER(MeshDesc), C.POINTER(OpOpts), C.POINTER(_P)]),
     "dgtd_op_destroy": (None, [_P]),
     "dgtd_op_get_info": (C.c_int, [_P, C.POINTER(OpInfo)]),
@@ -103,6 +104,11 @@ def lib() -> C.CDLL:
             fn.argtypes = args
         _lib_handle = h
     return _lib_handle
+
+
+def kernel_launches() -> int:
+    """Kernels launched by the CUDA library in this process so far."""
+    return int(lib().dgtd_kernel_launches())
 
 
 def _check(rc: int, what: str) -> None:

@@ -2,6 +2,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <memory>
@@ -18,6 +19,7 @@
 namespace {
 
 thread_local std::string g_err;
+std::atomic<uint64_t> g_launches{0};   // kernels launched by this library (all threads)
 
 int fail(int code, const std::string& msg)
 {
@@ -161,6 +163,7 @@ void run_stage(dgtd_op* op, dgtd::StageArgs A, double t, cudaStream_t s)
         ck(dgtd::launch_tfsf_skip(op->dev, op->pw_dev, static_cast<int>(op->pw_host.size()), op->batch, t,
                                   op->skip_dev, s),
            "tfsf skip kernel");
+        g_launches.fetch_add(1, std::memory_order_relaxed);
         A.pw = op->pw_dev;
         A.n_pw = static_cast<int>(op->pw_host.size());
         A.skip = op->skip_dev;
@@ -170,6 +173,7 @@ void run_stage(dgtd_op* op, dgtd::StageArgs A, double t, cudaStream_t s)
         A.skip = nullptr;
     }
     ck(dgtd::launch_stage_fp64(op->dev, A, s), "stage kernel");
+    g_launches.fetch_add(1, std::memory_order_relaxed);
 }
 
 void ensure_ws(dgtd_op* op)
@@ -223,6 +227,8 @@ void rk_step(dgtd_op* op, double* d_x, double t, double dt, int integrator, doub
 extern "C" {
 
 const char* dgtd_last_error(void) { return g_err.c_str(); }
+
+uint64_t dgtd_kernel_launches(void) { return g_launches.load(std::memory_order_relaxed); }
 
 int dgtd_op_create(const dgtd_mesh_desc* mesh, const dgtd_op_opts* opts, dgtd_op** out)
 {
@@ -450,6 +456,7 @@ int dgtd_op_norm2(dgtd_op* op, const double* d_state, double* h_out, void* strea
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     try {
         ck(dgtd::launch_norm2(d_state, op->state_len / op->batch, op->batch, op->norm_dev, s), "norm kernel");
+        g_launches.fetch_add(1, std::memory_order_relaxed);
         ck(cudaMemcpyAsync(h_out, op->norm_dev, op->batch * sizeof(double), cudaMemcpyDeviceToHost, s), "D2H");
         ck(cudaStreamSynchronize(s), "sync");
     } catch (const std::exception& e) {

@@ -110,6 +110,9 @@ typedef struct dgtd_op dgtd_op;
 /* Thread-local description of the last error. */
 const char* dgtd_last_error(void);
 
+/* Number of CUDA kernels this library has launched in the process so far. */
+uint64_t dgtd_kernel_launches(void);
+
 /* Operator life cycle (reference GlobalEvolution ctor, GlobalEvolution.cpp:32-364:
  * here the once-per-mesh work is the geometric-factor / LIFT / node-map build). */
 int dgtd_op_create(const dgtd_mesh_desc* mesh, const dgtd_op_opts* opts, dgtd_op** out);

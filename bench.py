@@ -133,9 +133,12 @@ def measured_peaks() -> dict:
 
 def profile_traffic(kernel: str, workload: str):
     """Per-launch DRAM bytes of the dominant kernel from the committed ncu summary, if present."""
-    f = ROOT / "profiles" / f"{kernel}__{workload}.json"
+    f = ROOT / "profiles" / f"{kernel}__{workload}.md"
     if f.exists():
-        return json.loads(f.read_text()).get("dram_bytes_per_launch")
+        import re
+        m = re.search(r"^dram_bytes_per_launch:\s*([0-9.eE+]+)", f.read_text(), flags=re.M)
+        if m:
+            return float(m.group(1))
     return None
 
 
@@ -286,8 +289,8 @@ def run_ours(args, world, rank, local):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=50)
-    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default=DEFAULT_WORKLOAD)
     ap.add_argument("--cpu-budget", type=float, default=15.0, help="seconds of CPU baseline sample")

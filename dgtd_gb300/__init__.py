@@ -53,7 +53,8 @@ class OpInfo(C.Structure):
     _fields_ = [("n_elements", C.c_int64), ("order", C.c_int32), ("np", C.c_int32), ("nfp", C.c_int32),
                 ("batch", C.c_int32), ("precision", C.c_int32), ("ndofs", C.c_int64), ("state_len", C.c_int64),
                 ("n_tfsf_faces", C.c_int64), ("min_edge", C.c_double), ("dt_scale_min", C.c_double),
-                ("device_bytes", C.c_int64)]
+                ("device_bytes", C.c_int64), ("work_len", C.c_int64), ("work_word_bytes", C.c_int32),
+                ("batch_padded", C.c_int32)]
 
 
 class BoxSpec(C.Structure):
@@ -80,6 +81,8 @@ SIGNATURES = {
     "dgtd_op_set_planewaves": (C.c_int, [_P, C.POINTER(PlaneWave), C.c_int32]),
     "dgtd_op_mult": (C.c_int, [_P, _P, _P, C.c_double, _P]),
     "dgtd_op_mult_host": (C.c_int, [_P, _D, _D, C.c_double]),
+    "dgtd_op_pack": (C.c_int, [_P, _P, _P, _P]),
+    "dgtd_op_unpack": (C.c_int, [_P, _P, _P, _P]),
     "dgtd_op_step": (C.c_int, [_P, _P, C.c_double, C.c_double, C.c_int32, C.c_int32, _P]),
     "dgtd_op_run_host": (C.c_int, [_P, _D, C.c_double, C.c_double, C.c_double, C.c_int32, _I64]),
     "dgtd_op_norm2": (C.c_int, [_P, _P, _D, _P]),
@@ -269,7 +272,28 @@ class Operator:
 
     @property
     def state_len(self) -> int:
+        """Entries of the reference-layout state (6 K Np B)."""
         return int(self.info["state_len"])
+
+    @property
+    def work_len(self) -> int:
+        """Entries of the working state used by mult/step (FP64: reference layout; FP32: internal)."""
+        return int(self.info["work_len"])
+
+    def work_dtype(self):
+        import torch
+        return torch.float64 if int(self.info["work_word_bytes"]) == 8 else torch.float32
+
+    def new_work(self, device="cuda"):
+        import torch
+        return torch.zeros(self.work_len, dtype=self.work_dtype(), device=device)
+
+    def pack(self, ref, work, stream=None) -> None:
+        """Reference-layout FP64 device state -> working state."""
+        _check(lib().dgtd_op_pack(self._h, _ptr(ref), _ptr(work), _stream(stream)), "dgtd_op_pack")
+
+    def unpack(self, work, ref, stream=None) -> None:
+        _check(lib().dgtd_op_unpack(self._h, _ptr(work), _ptr(ref), _stream(stream)), "dgtd_op_unpack")
 
     @property
     def ndofs(self) -> int:

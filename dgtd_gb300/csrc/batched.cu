@@ -1,13 +1,524 @@
-// Batched FP32 + 3xTF32 form (placeholder until the tensor-core kernels land).
+// Batched FP32 form of the DG Maxwell step (B incidences on one mesh).
+//
+// Same operator as the plain FP64 form (see plain_fp64.cu for the equations and
+// the reference citations) evaluated in FP32 on an incidence-fastest layout.
+// One block handles one element and a chunk of 32 incidences: lanes are
+// incidences, so every load and store of the element's fields, its face
+// traces and its neighbours' traces is a coalesced 128-byte row.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
 #include <stdexcept>
+#include <string>
 
 #include "batched.hpp"
 
 namespace dgtd {
 
-std::unique_ptr<BatchedOp> BatchedOp::create(const RefTet&, const MeshTables&, const TablesDev&, int)
+namespace {
+
+void ckb(cudaError_t e, const char* what)
 {
-    throw std::runtime_error("the FP32 3xTF32 batched form is not available in this build");
+    if (e != cudaSuccess) throw std::runtime_error(std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+constexpr int kWarps = 4;
+constexpr int kLanes = 32;
+
+__device__ __forceinline__ void pw_eval_f32(const PlaneWaveF32* pw, int n_pw, int b, float px, float py, float pz,
+                                            float t, float* e, float* h)
+{
+    e[0] = e[1] = e[2] = h[0] = h[1] = h[2] = 0.0f;
+    for (int q = 0; q < n_pw; ++q) {
+        const PlaneWaveF32& w = pw[q];
+        if (w.batch != b) continue;
+        const float s = px * w.k[0] + py * w.k[1] + pz * w.k[2] - t;
+        const float a = s - w.mean;
+        float g = expf(-a * a / (2.0f * w.spread * w.spread));
+        if (w.freq != 0.0f) g *= cosf(6.283185307179586f * w.freq * a);
+        e[0] += g * w.pol[0]; e[1] += g * w.pol[1]; e[2] += g * w.pol[2];
+        h[0] += g * w.kxp[0]; h[1] += g * w.kxp[1]; h[2] += g * w.kxp[2];
+    }
+}
+
+template <int P>
+struct OrdB {
+    static constexpr int Np = (P + 1) * (P + 2) * (P + 3) / 6;
+    static constexpr int Nfp = (P + 1) * (P + 2) / 2;
+    static constexpr int NF = 4 * Nfp;
+    static constexpr size_t smem = sizeof(float) * 6 * (Np + NF) * kLanes;
+};
+
+template <int P>
+__global__ void __launch_bounds__(kWarps * kLanes) stage_f32(BatchedTables T, BatchedStageArgs A)
+{
+    using O = OrdB<P>;
+    constexpr int Np = O::Np, Nfp = O::Nfp, NF = O::NF;
+    extern __shared__ float sm[];
+    float* s_u = sm;                       // [6][Np][32]
+    float* s_f = sm + 6 * Np * kLanes;     // [6][NF][32]
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t e = blockIdx.x;
+    const int b = blockIdx.y * kLanes + lane;
+    const int64_t Bp = T.Bpad;
+    const int64_t col = static_cast<int64_t>(blockIdx.y) * kLanes + lane;
+    const float* __restrict__ in = A.in;
+
+    for (int r = warp; r < 6 * Np; r += kWarps) s_u[r * kLanes + lane] = in[(e * 6 * Np + r) * Bp + col];
+    __syncthreads();
+
+    // ---- face fluxes (lane = incidence) ------------------------------------------
+    const bool skip_src = (A.skip == nullptr) || A.skip[b];
+    for (int fn = warp; fn < NF; fn += kWarps) {
+        const int f = fn / Nfp, a = fn - f * Nfp;
+        const int vm = T.Fmask[fn];
+        const int code = T.fcode[e * 4 + f];
+        const float* fg = T.fgeo + e * 16 + f * 4;
+        const float nx = fg[0], ny = fg[1], nz = fg[2], fs = fg[3];
+        float uM[6], dE[3], dH[3];
+#pragma unroll
+        for (int c = 0; c < 6; ++c) uM[c] = s_u[(c * Np + vm) * kLanes + lane];
+        float aE = T.alpha, aH = T.alpha;
+        if (code == 0 || code == 4 || code == 5) {
+            const int32_t gp = T.vmapP[(e * 4 + f) * Nfp + a];
+            const int64_t en = gp / Np, node = gp - en * Np;
+            const float* nb = in + ((en * 6) * Np + node) * Bp + col;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                dE[c] = __ldg(nb + c * Np * Bp) - uM[c];
+                dH[c] = __ldg(nb + (c + 3) * Np * Bp) - uM[c + 3];
+            }
+            if (code != 0 && !skip_src) {
+                const float* xq = T.fxyz + ((e * 4 + f) * Nfp + a) * 3;
+                float pe[3], ph[3];
+                pw_eval_f32(A.pw, A.n_pw, b, xq[0], xq[1], xq[2], A.t, pe, ph);
+                const float sg = (code == 4) ? 1.0f : -1.0f;
+#pragma unroll
+                for (int c = 0; c < 3; ++c) { dE[c] += sg * pe[c]; dH[c] += sg * ph[c]; }
+            }
+        } else if (code == 1 || code == 6) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) { dE[c] = -2.0f * uM[c]; dH[c] = 0.0f; }
+        } else if (code == 2 || code == 7) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) { dE[c] = 0.0f; dH[c] = -2.0f * uM[c + 3]; }
+        } else if (code == 3 || code == 8) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) { dE[c] = -uM[c]; dH[c] = -uM[c + 3]; }
+            aE = 1.0f; aH = 1.0f;
+        } else {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) { dE[c] = 0.0f; dH[c] = 0.0f; }
+        }
+        const float ndE = nx * dE[0] + ny * dE[1] + nz * dE[2];
+        const float ndH = nx * dH[0] + ny * dH[1] + nz * dH[2];
+        const float h = 0.5f * fs;
+        s_f[(0 * NF + fn) * kLanes + lane] = h * ((ny * dH[2] - nz * dH[1]) + aE * (dE[0] - ndE * nx));
+        s_f[(1 * NF + fn) * kLanes + lane] = h * ((nz * dH[0] - nx * dH[2]) + aE * (dE[1] - ndE * ny));
+        s_f[(2 * NF + fn) * kLanes + lane] = h * ((nx * dH[1] - ny * dH[0]) + aE * (dE[2] - ndE * nz));
+        s_f[(3 * NF + fn) * kLanes + lane] = h * (-(ny * dE[2] - nz * dE[1]) + aH * (dH[0] - ndH * nx));
+        s_f[(4 * NF + fn) * kLanes + lane] = h * (-(nz * dE[0] - nx * dE[2]) + aH * (dH[1] - ndH * ny));
+        s_f[(5 * NF + fn) * kLanes + lane] = h * (-(nx * dE[1] - ny * dE[0]) + aH * (dH[2] - ndH * nz));
+    }
+    __syncthreads();
+
+    // ---- volume + lift + epilogue: a warp owns nodes warp, warp+4, ...; two at a time ----
+    const float* g = T.geo + e * 9;
+    const float rx = g[0], ry = g[1], rz = g[2], sx = g[3], sy = g[4], sz = g[5], tx = g[6], ty = g[7], tz = g[8];
+    const float ie = T.mat[e * 3 + 0], im = T.mat[e * 3 + 1], se = T.mat[e * 3 + 2];
+    const float* __restrict__ Dr = T.D;
+    const float* __restrict__ Ds = T.D + Np * Np;
+    const float* __restrict__ Dt = T.D + 2 * Np * Np;
+    for (int i0 = warp; i0 < Np; i0 += 2 * kWarps) {
+        const int i1 = i0 + kWarps;
+        const bool two = i1 < Np;
+        float ar0[6], as0[6], at0[6], ar1[6], as1[6], at1[6];
+#pragma unroll
+        for (int c = 0; c < 6; ++c) { ar0[c] = as0[c] = at0[c] = ar1[c] = as1[c] = at1[c] = 0.0f; }
+        for (int j = 0; j < Np; ++j) {
+            float u[6];
+#pragma unroll
+            for (int c = 0; c < 6; ++c) u[c] = s_u[(c * Np + j) * kLanes + lane];
+            const float dr0 = __ldg(Dr + i0 * Np + j), ds0 = __ldg(Ds + i0 * Np + j), dt0 = __ldg(Dt + i0 * Np + j);
+            const int i1c = two ? i1 : i0;
+            const float dr1 = __ldg(Dr + i1c * Np + j), ds1 = __ldg(Ds + i1c * Np + j), dt1 = __ldg(Dt + i1c * Np + j);
+#pragma unroll
+            for (int c = 0; c < 6; ++c) {
+                ar0[c] = fmaf(dr0, u[c], ar0[c]); as0[c] = fmaf(ds0, u[c], as0[c]); at0[c] = fmaf(dt0, u[c], at0[c]);
+                ar1[c] = fmaf(dr1, u[c], ar1[c]); as1[c] = fmaf(ds1, u[c], as1[c]); at1[c] = fmaf(dt1, u[c], at1[c]);
+            }
+        }
+        float lf0[6], lf1[6];
+#pragma unroll
+        for (int c = 0; c < 6; ++c) { lf0[c] = 0.0f; lf1[c] = 0.0f; }
+        const int i1c = two ? i1 : i0;
+        for (int m = 0; m < NF; ++m) {
+            const float L0 = __ldg(T.LIFT + i0 * NF + m), L1 = __ldg(T.LIFT + i1c * NF + m);
+#pragma unroll
+            for (int c = 0; c < 6; ++c) {
+                const float fv = s_f[(c * NF + m) * kLanes + lane];
+                lf0[c] = fmaf(L0, fv, lf0[c]);
+                lf1[c] = fmaf(L1, fv, lf1[c]);
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            if (q == 1 && !two) break;
+            const int i = q == 0 ? i0 : i1;
+            const float* ar = q == 0 ? ar0 : ar1;
+            const float* as = q == 0 ? as0 : as1;
+            const float* at = q == 0 ? at0 : at1;
+            const float* lf = q == 0 ? lf0 : lf1;
+            auto dx = [&](int c) { return rx * ar[c] + sx * as[c] + tx * at[c]; };
+            auto dy = [&](int c) { return ry * ar[c] + sy * as[c] + ty * at[c]; };
+            auto dz = [&](int c) { return rz * ar[c] + sz * as[c] + tz * at[c]; };
+            float k[6];
+            k[0] = ie * ((dy(5) - dz(4)) + lf[0]) - se * s_u[(0 * Np + i) * kLanes + lane];
+            k[1] = ie * ((dz(3) - dx(5)) + lf[1]) - se * s_u[(1 * Np + i) * kLanes + lane];
+            k[2] = ie * ((dx(4) - dy(3)) + lf[2]) - se * s_u[(2 * Np + i) * kLanes + lane];
+            k[3] = im * (-(dy(2) - dz(1)) + lf[3]);
+            k[4] = im * (-(dz(0) - dx(2)) + lf[4]);
+            k[5] = im * (-(dx(1) - dy(0)) + lf[5]);
+            const float dt = A.dt;
+#pragma unroll
+            for (int c = 0; c < 6; ++c) {
+                const int64_t idx = ((e * 6 + c) * Np + i) * Bp + col;
+                const float uc = s_u[(c * Np + i) * kLanes + lane];
+                switch (A.mode) {
+                case MODE_MULT: A.out[idx] = k[c]; break;
+                case MODE_RK4_1: A.yout[idx] = uc + 0.5f * dt * k[c]; A.z[idx] = uc + (dt / 6.0f) * k[c]; break;
+                case MODE_RK4_2: A.yout[idx] = A.x[idx] + 0.5f * dt * k[c]; A.z[idx] += (dt / 3.0f) * k[c]; break;
+                case MODE_RK4_3: A.yout[idx] = A.x[idx] + dt * k[c]; A.z[idx] += (dt / 3.0f) * k[c]; break;
+                case MODE_RK4_4: A.x[idx] = A.z[idx] + (dt / 6.0f) * k[c]; break;
+                case MODE_LSRK: {
+                    const float r = A.a * A.res[idx] + dt * k[c];
+                    A.res[idx] = r;
+                    A.yout[idx] = uc + A.b * r;
+                    break;
+                }
+                default: break;
+                }
+            }
+        }
+    }
+}
+
+__global__ void tfsf_skip_f32(BatchedTables T, const PlaneWaveF32* pw, int n_pw, float t, int* skip)
+{
+    const int b = blockIdx.x;
+    double acc = 0.0;
+    for (int64_t w = threadIdx.x; w < T.n_tfsf_nodes; w += blockDim.x) {
+        float pe[3], ph[3];
+        pw_eval_f32(pw, n_pw, b, T.nxyz[w], T.nxyz[T.n_tfsf_nodes + w], T.nxyz[2 * T.n_tfsf_nodes + w], t, pe, ph);
+        float s = 0.0f;
+        for (int c = 0; c < 3; ++c) s += pe[c] * pe[c] + ph[c] * ph[c];
+        acc += 0.25 * static_cast<double>(s);
+    }
+    __shared__ double red[256];
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) skip[b] = (red[0] < 1e-16) ? 1 : 0;
+}
+
+// reference [b][c][e*Np+i] (FP64) -> internal [e'][c][i][b] (FP32)
+__global__ void pack_kernel(const double* __restrict__ ref, float* __restrict__ st, const int32_t* __restrict__ perm,
+                            int64_t K, int Np, int B, int Bp)
+{
+    const int64_t total = K * 6 * Np;
+    for (int64_t r = blockIdx.x; r < total; r += gridDim.x) {
+        const int64_t ei = r / (6 * Np);
+        const int rem = static_cast<int>(r - ei * 6 * Np), c = rem / Np, i = rem - c * Np;
+        const int64_t er = perm[ei];
+        const int64_t N = K * Np;
+        for (int b = threadIdx.x; b < Bp; b += blockDim.x)
+            st[r * Bp + b] = (b < B) ? static_cast<float>(ref[(static_cast<int64_t>(b) * 6 + c) * N + er * Np + i]) : 0.0f;
+    }
+}
+
+__global__ void unpack_kernel(const float* __restrict__ st, double* __restrict__ ref, const int32_t* __restrict__ perm,
+                              int64_t K, int Np, int B, int Bp)
+{
+    const int64_t total = K * 6 * Np;
+    for (int64_t r = blockIdx.x; r < total; r += gridDim.x) {
+        const int64_t ei = r / (6 * Np);
+        const int rem = static_cast<int>(r - ei * 6 * Np), c = rem / Np, i = rem - c * Np;
+        const int64_t er = perm[ei];
+        const int64_t N = K * Np;
+        for (int b = threadIdx.x; b < B; b += blockDim.x)
+            ref[(static_cast<int64_t>(b) * 6 + c) * N + er * Np + i] = st[r * Bp + b];
+    }
+}
+
+// out[b] += sum over rows of st[row][b]^2 (lane = incidence)
+__global__ void norm2_f32(const float* __restrict__ st, int64_t rows, int Bp, double* out)
+{
+    const int b = blockIdx.y * 32 + threadIdx.x;
+    double acc = 0.0;
+    for (int64_t r = blockIdx.x * blockDim.y + threadIdx.y; r < rows; r += static_cast<int64_t>(gridDim.x) * blockDim.y) {
+        const float v = st[r * Bp + b];
+        acc += static_cast<double>(v) * v;
+    }
+    atomicAdd(out + b, acc);
+}
+
+uint64_t morton3(uint32_t x, uint32_t y, uint32_t z)
+{
+    auto spread = [](uint64_t v) {
+        v &= 0x1fffff;
+        v = (v | v << 32) & 0x1f00000000ffffULL;
+        v = (v | v << 16) & 0x1f0000ff0000ffULL;
+        v = (v | v << 8) & 0x100f00f00f00f00fULL;
+        v = (v | v << 4) & 0x10c30c30c30c30c3ULL;
+        v = (v | v << 2) & 0x1249249249249249ULL;
+        return v;
+    };
+    return spread(x) | (spread(y) << 1) | (spread(z) << 2);
+}
+
+template <int P>
+void launch_stage(const BatchedTables& T, const BatchedStageArgs& A, cudaStream_t s)
+{
+    using O = OrdB<P>;
+    static bool attr = false;
+    if (!attr) {
+        ckb(cudaFuncSetAttribute(stage_f32<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(O::smem)),
+            "smem attribute");
+        attr = true;
+    }
+    dim3 grid(static_cast<unsigned>(T.K), static_cast<unsigned>(T.Bpad / kLanes));
+    stage_f32<P><<<grid, kWarps * kLanes, O::smem, s>>>(T, A);
+    ckb(cudaGetLastError(), "batched stage kernel");
+}
+
+// LSERK4 coefficients (Carpenter & Kennedy 1994)
+const double kA[5] = {0.0, -567301805773.0 / 1357537059087.0, -2404267990393.0 / 2016746695238.0,
+                      -3550918686646.0 / 2091501179385.0, -1275806237668.0 / 842570457699.0};
+const double kB[5] = {1432997174477.0 / 9575080441755.0, 5161836677717.0 / 13612068292357.0,
+                      1720146321549.0 / 2090206949498.0, 3134564353537.0 / 4481467310338.0,
+                      2277821191437.0 / 14882151754819.0};
+const double kC[5] = {0.0, 1432997174477.0 / 9575080441755.0, 2526269341429.0 / 6820363962896.0,
+                      2006345519317.0 / 3224310063776.0, 2802321613138.0 / 2924317926251.0};
+
+}  // namespace
+
+std::unique_ptr<BatchedOp> BatchedOp::create(const RefTet& ref, const MeshTables& mesh, const TablesDev& dev, int batch)
+{
+    std::unique_ptr<BatchedOp> op(new BatchedOp());
+    const int Np = ref.Np, Nfp = ref.Nfp;
+    const int64_t K = mesh.K;
+    op->K_ = K; op->Np_ = Np; op->B_ = batch; op->Bpad_ = ((batch + 31) / 32) * 32;
+    op->state_len_ = K * 6 * Np * static_cast<int64_t>(op->Bpad_);
+
+    // Morton order of element centroids
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    std::vector<double> cen(3 * K);
+    for (int64_t e = 0; e < K; ++e) {
+        double c[3] = {0, 0, 0};
+        for (int i = 0; i < Np; ++i) { c[0] += mesh.x[e * Np + i]; c[1] += mesh.y[e * Np + i]; c[2] += mesh.z[e * Np + i]; }
+        for (int d = 0; d < 3; ++d) { cen[3 * e + d] = c[d] / Np; lo[d] = std::min(lo[d], c[d] / Np); hi[d] = std::max(hi[d], c[d] / Np); }
+    }
+    std::vector<uint64_t> code(K);
+    for (int64_t e = 0; e < K; ++e) {
+        uint32_t q[3];
+        for (int d = 0; d < 3; ++d) {
+            double span = hi[d] - lo[d];
+            double u = span > 0 ? (cen[3 * e + d] - lo[d]) / span : 0.0;
+            q[d] = static_cast<uint32_t>(std::min(2097151.0, std::max(0.0, u * 2097151.0)));
+        }
+        code[e] = morton3(q[0], q[1], q[2]);
+    }
+    std::vector<int32_t> perm(K), inv(K);
+    std::iota(perm.begin(), perm.end(), 0);
+    std::stable_sort(perm.begin(), perm.end(), [&](int32_t a, int32_t b) { return code[a] < code[b]; });
+    for (int64_t i = 0; i < K; ++i) inv[perm[i]] = static_cast<int32_t>(i);
+
+    // FP32 tables in internal order (built in FP64 on the host, rounded once)
+    std::vector<float> D(3 * Np * Np), L(Np * 4 * Nfp), geo(K * 9), fgeo(K * 16), mat(K * 3);
+    for (int q = 0; q < Np * Np; ++q) { D[q] = ref.Dr[q]; D[Np * Np + q] = ref.Ds[q]; D[2 * Np * Np + q] = ref.Dt[q]; }
+    for (size_t q = 0; q < L.size(); ++q) L[q] = static_cast<float>(ref.LIFT[q]);
+    std::vector<int32_t> vmapP(K * 4 * Nfp), fcode(K * 4);
+    std::vector<float> fxyz(K * 4 * Nfp * 3, 0.0f);
+    bool has_tfsf = false;
+    for (int64_t ei = 0; ei < K; ++ei) {
+        const int64_t er = perm[ei];
+        for (int q = 0; q < 9; ++q) geo[ei * 9 + q] = static_cast<float>(mesh.geo[er * 9 + q]);
+        for (int q = 0; q < 16; ++q) fgeo[ei * 16 + q] = static_cast<float>(mesh.fgeo[er * 16 + q]);
+        for (int q = 0; q < 3; ++q) mat[ei * 3 + q] = static_cast<float>(mesh.mat[er * 3 + q]);
+        for (int f = 0; f < 4; ++f) {
+            const int fc = mesh.fcode[er * 4 + f];
+            fcode[ei * 4 + f] = fc;
+            if (fc == FACE_TFSF_TF || fc == FACE_TFSF_SF) has_tfsf = true;
+            for (int a = 0; a < Nfp; ++a) {
+                const int32_t g = mesh.vmapP[(er * 4 + f) * Nfp + a];
+                const int64_t en = g / Np, node = g - en * Np;
+                vmapP[(ei * 4 + f) * Nfp + a] = static_cast<int32_t>(inv[en] * Np + node);
+                const int64_t gm = er * Np + ref.Fmask[f * Nfp + a];
+                float* xq = &fxyz[((ei * 4 + f) * Nfp + a) * 3];
+                xq[0] = static_cast<float>(mesh.x[gm]); xq[1] = static_cast<float>(mesh.y[gm]); xq[2] = static_cast<float>(mesh.z[gm]);
+            }
+        }
+    }
+    const int64_t nt = static_cast<int64_t>(mesh.tfsf_elems.size()) * Np;
+    std::vector<float> nxyz(3 * std::max<int64_t>(nt, 1), 0.0f);
+    for (size_t q = 0; q < mesh.tfsf_elems.size(); ++q)
+        for (int i = 0; i < Np; ++i) {
+            const int64_t gm = static_cast<int64_t>(mesh.tfsf_elems[q]) * Np + i, w = static_cast<int64_t>(q) * Np + i;
+            nxyz[w] = static_cast<float>(mesh.x[gm]);
+            nxyz[nt + w] = static_cast<float>(mesh.y[gm]);
+            nxyz[2 * nt + w] = static_cast<float>(mesh.z[gm]);
+        }
+    op->has_tfsf_ = has_tfsf;
+
+    auto up = [&](const auto& v) {
+        using T = typename std::decay_t<decltype(v)>::value_type;
+        T* d = nullptr;
+        ckb(cudaMalloc(&d, v.size() * sizeof(T)), "cudaMalloc");
+        op->allocs_.push_back(d);
+        ckb(cudaMemcpy(d, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice), "H2D");
+        op->device_bytes_ += static_cast<int64_t>(v.size() * sizeof(T));
+        return static_cast<const T*>(d);
+    };
+    BatchedTables& T = op->T_;
+    T.p = ref.p; T.Np = Np; T.Nfp = Nfp; T.B = batch; T.Bpad = op->Bpad_; T.K = K;
+    T.alpha = static_cast<float>(dev.alpha);
+    T.D = up(D); T.LIFT = up(L); T.Fmask = up(ref.Fmask);
+    T.geo = up(geo); T.fgeo = up(fgeo); T.mat = up(mat);
+    T.vmapP = up(vmapP); T.fcode = up(fcode); T.fxyz = up(fxyz);
+    T.nxyz = up(nxyz); T.n_tfsf_nodes = nt;
+    op->perm_ = const_cast<int32_t*>(up(perm));
+    ckb(cudaMalloc(&op->skip_, op->Bpad_ * sizeof(int)), "cudaMalloc skip");
+    op->allocs_.push_back(op->skip_);
+    return op;
+}
+
+BatchedOp::~BatchedOp()
+{
+    for (void* p : allocs_) cudaFree(p);
+    if (pw_dev_) cudaFree(pw_dev_);
+    if (ws_) cudaFree(ws_);
+}
+
+void BatchedOp::set_sources(const std::vector<PlaneWaveDev>& pw)
+{
+    std::vector<PlaneWaveF32> v;
+    for (const auto& w : pw) {
+        PlaneWaveF32 f{};
+        for (int c = 0; c < 3; ++c) { f.k[c] = float(w.k[c]); f.pol[c] = float(w.pol[c]); f.kxp[c] = float(w.kxp[c]); }
+        f.spread = float(w.spread); f.mean = float(w.mean); f.freq = float(w.freq); f.batch = w.batch;
+        v.push_back(f);
+    }
+    n_pw_ = static_cast<int>(v.size());
+    if (n_pw_ > pw_cap_) {
+        if (pw_dev_) cudaFree(pw_dev_);
+        pw_dev_ = nullptr;
+        ckb(cudaMalloc(&pw_dev_, n_pw_ * sizeof(PlaneWaveF32)), "cudaMalloc sources");
+        pw_cap_ = n_pw_;
+    }
+    if (n_pw_) ckb(cudaMemcpy(pw_dev_, v.data(), n_pw_ * sizeof(PlaneWaveF32), cudaMemcpyHostToDevice), "H2D sources");
+}
+
+void BatchedOp::stage(BatchedStageArgs A, double t, cudaStream_t s)
+{
+    A.t = static_cast<float>(t);
+    if (has_tfsf_ && n_pw_ > 0) {
+        tfsf_skip_f32<<<Bpad_, 256, 0, s>>>(T_, pw_dev_, n_pw_, static_cast<float>(t), skip_);
+        ckb(cudaGetLastError(), "tfsf skip kernel");
+        ++launches_;
+        A.pw = pw_dev_; A.n_pw = n_pw_; A.skip = skip_;
+    } else {
+        A.pw = nullptr; A.n_pw = 0; A.skip = nullptr;
+    }
+    switch (T_.p) {
+    case 1: launch_stage<1>(T_, A, s); break;
+    case 2: launch_stage<2>(T_, A, s); break;
+    case 3: launch_stage<3>(T_, A, s); break;
+    case 4: launch_stage<4>(T_, A, s); break;
+    case 5: launch_stage<5>(T_, A, s); break;
+    case 6: launch_stage<6>(T_, A, s); break;
+    default: throw std::runtime_error("unsupported order");
+    }
+    ++launches_;
+}
+
+void BatchedOp::ensure_ws()
+{
+    if (ws_) return;
+    ckb(cudaMalloc(&ws_, 3 * state_len_ * sizeof(float)), "cudaMalloc RK scratch");
+}
+
+void BatchedOp::pack(const double* d_ref, float* d_state, cudaStream_t s)
+{
+    pack_kernel<<<std::min<int64_t>(K_ * 6 * Np_, 1 << 20), 64, 0, s>>>(d_ref, d_state, perm_, K_, Np_, B_, Bpad_);
+    ckb(cudaGetLastError(), "pack kernel");
+    ++launches_;
+}
+
+void BatchedOp::unpack(const float* d_state, double* d_ref, cudaStream_t s)
+{
+    unpack_kernel<<<std::min<int64_t>(K_ * 6 * Np_, 1 << 20), 64, 0, s>>>(d_state, d_ref, perm_, K_, Np_, B_, Bpad_);
+    ckb(cudaGetLastError(), "unpack kernel");
+    ++launches_;
+}
+
+void BatchedOp::mult(const float* d_in, float* d_out, double t, cudaStream_t s)
+{
+    BatchedStageArgs A{};
+    A.mode = MODE_MULT; A.in = d_in; A.out = d_out;
+    stage(A, t, s);
+}
+
+void BatchedOp::step(float* d_x, double t0, double dt, int nsteps, int integrator, cudaStream_t s)
+{
+    ensure_ws();
+    const int64_t L = state_len_;
+    float* y0 = ws_;
+    float* y1 = ws_ + L;
+    float* z = ws_ + 2 * L;
+    double t = t0;
+    if (integrator == 0) {
+        for (int n = 0; n < nsteps; ++n) {
+            BatchedStageArgs A{};
+            A.dt = static_cast<float>(dt); A.x = d_x; A.z = z;
+            A.mode = MODE_RK4_1; A.in = d_x; A.yout = y0; stage(A, t, s);
+            A.mode = MODE_RK4_2; A.in = y0; A.yout = y1; stage(A, t + dt / 2, s);
+            A.mode = MODE_RK4_3; A.in = y1; A.yout = y0; stage(A, t + dt / 2, s);
+            A.mode = MODE_RK4_4; A.in = y0; A.yout = nullptr; stage(A, t + dt, s);
+            t += dt;
+        }
+    } else {
+        float* res = z;
+        float* other = y0;
+        ckb(cudaMemsetAsync(res, 0, L * sizeof(float), s), "memset");
+        float* cur = d_x;
+        for (int n = 0; n < nsteps; ++n) {
+            for (int st = 0; st < 5; ++st) {
+                float* nxt = (cur == d_x) ? other : d_x;
+                BatchedStageArgs A{};
+                A.dt = static_cast<float>(dt); A.mode = MODE_LSRK; A.in = cur; A.yout = nxt; A.res = res;
+                A.a = static_cast<float>(kA[st]); A.b = static_cast<float>(kB[st]);
+                stage(A, t + kC[st] * dt, s);
+                cur = nxt;
+            }
+            t += dt;
+        }
+        if (cur != d_x) ckb(cudaMemcpyAsync(d_x, cur, L * sizeof(float), cudaMemcpyDeviceToDevice, s), "copy");
+    }
+}
+
+void BatchedOp::norm2(const float* d_state, double* d_out_dev, cudaStream_t s)
+{
+    ckb(cudaMemsetAsync(d_out_dev, 0, Bpad_ * sizeof(double), s), "memset");
+    const int64_t rows = K_ * 6 * Np_;
+    dim3 block(32, 8);
+    dim3 grid(static_cast<unsigned>(std::min<int64_t>((rows + 7) / 8, 4096)), static_cast<unsigned>(Bpad_ / 32));
+    norm2_f32<<<grid, block, 0, s>>>(d_state, rows, Bpad_, d_out_dev);
+    ckb(cudaGetLastError(), "norm kernel");
+    ++launches_;
 }
 
 }  // namespace dgtd

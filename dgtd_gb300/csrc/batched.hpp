@@ -1,8 +1,16 @@
-// Batched FP32 + 3xTF32 form of the DG Maxwell step (B incidences per mesh).
+// Batched FP32 form of the DG Maxwell step: B incidences share one mesh.
+//
+// Internal layout (private to this form): state[e'][c][i][b] in FP32 with the
+// incidence index b fastest (B padded to a multiple of 32), elements e' in a
+// space-filling-curve (Morton) order of their centroids so that face
+// neighbours are processed close in time and their traces stay in L2.
+// dgtd_op_pack / dgtd_op_unpack convert to and from the reference layout.
 #pragma once
 #include <cstdint>
 #include <memory>
 #include <vector>
+
+#include <cuda_runtime.h>
 
 #include "kernels.hpp"
 #include "mesh.hpp"
@@ -10,12 +18,76 @@
 
 namespace dgtd {
 
+struct PlaneWaveF32 {
+    float k[3], pol[3], kxp[3];
+    float spread, mean, freq;
+    int batch, pad;
+};
+
+struct BatchedTables {
+    int p, Np, Nfp, B, Bpad;
+    int64_t K;
+    const float* D;        // [3][Np][Np]   Dr, Ds, Dt (row i, column j)
+    const float* LIFT;     // [Np][4 Nfp]
+    const int* Fmask;      // [4][Nfp]
+    const float* geo;      // [K][9]
+    const float* fgeo;     // [K][16]
+    const float* mat;      // [K][3]
+    const int32_t* vmapP;  // [K][4][Nfp]  neighbour (element' * Np + node), internal numbering
+    const int32_t* fcode;  // [K][4]
+    const float* fxyz;     // [K][4][Nfp][3] face-node coordinates (TF/SF source evaluation)
+    const float* nxyz;     // [3][n_tfsf_nodes] coordinates of the TF/SF-submesh nodes (skip test)
+    int64_t n_tfsf_nodes;
+    float alpha;
+};
+
+struct BatchedStageArgs {
+    const float* in;
+    float* out;
+    float* x;
+    float* yout;
+    float* z;
+    float* res;
+    float t, dt, a, b;
+    int mode;
+    const PlaneWaveF32* pw;
+    int n_pw;
+    const int* skip;       // [Bpad]
+};
+
 class BatchedOp {
 public:
     static std::unique_ptr<BatchedOp> create(const RefTet& ref, const MeshTables& mesh, const TablesDev& dev, int batch);
-    virtual ~BatchedOp() = default;
-    virtual void set_sources(const std::vector<PlaneWaveDev>& pw) = 0;
-    virtual int64_t device_bytes() const = 0;
+    ~BatchedOp();
+    void set_sources(const std::vector<PlaneWaveDev>& pw);
+    int64_t device_bytes() const { return device_bytes_; }
+    int64_t state_len() const { return state_len_; }       // floats of one internal state
+    int64_t kernel_launches() const { return launches_; }
+
+    // reference layout (FP64, [b][c][e*Np+i]) <-> internal FP32
+    void pack(const double* d_ref, float* d_state, cudaStream_t s);
+    void unpack(const float* d_state, double* d_ref, cudaStream_t s);
+    void mult(const float* d_in, float* d_out, double t, cudaStream_t s);
+    void step(float* d_state, double t0, double dt, int nsteps, int integrator, cudaStream_t s);
+    void norm2(const float* d_state, double* d_out_dev, cudaStream_t s);
+
+private:
+    void stage(BatchedStageArgs A, double t, cudaStream_t s);
+    void ensure_ws();
+
+    BatchedTables T_{};
+    int64_t K_ = 0;
+    int Np_ = 0, B_ = 0, Bpad_ = 0;
+    int64_t state_len_ = 0;
+    int64_t device_bytes_ = 0;
+    int64_t launches_ = 0;
+    std::vector<void*> allocs_;
+    int32_t* perm_ = nullptr;   // internal element -> reference element
+    PlaneWaveF32* pw_dev_ = nullptr;
+    int n_pw_ = 0, pw_cap_ = 0;
+    int* skip_ = nullptr;
+    float* ws_ = nullptr;
+    bool has_tfsf_ = false;
 };
 
 }  // namespace dgtd

@@ -100,6 +100,14 @@ struct dgtd_op {
 
 namespace {
 
+// Adds the batched form's kernel launches to the library-wide counter.
+struct BatchedCount {
+    dgtd_op* op;
+    int64_t before;
+    explicit BatchedCount(dgtd_op* o) : op(o), before(o->batched->kernel_launches()) {}
+    ~BatchedCount() { g_launches.fetch_add(op->batched->kernel_launches() - before, std::memory_order_relaxed); }
+};
+
 dgtd::MeshInput to_input(const dgtd_mesh_desc* m)
 {
     if (!m) throw std::invalid_argument("mesh descriptor is NULL");
@@ -275,7 +283,7 @@ int dgtd_op_create(const dgtd_mesh_desc* mesh, const dgtd_op_opts* opts, dgtd_op
         T.tfsf_elems = op->up(op->mesh.tfsf_elems);
         T.n_tfsf_elems = static_cast<int64_t>(op->mesh.tfsf_elems.size());
         ck(cudaMalloc(&op->skip_dev, op->batch * sizeof(int)), "cudaMalloc skip");
-        ck(cudaMalloc(&op->norm_dev, op->batch * sizeof(double)), "cudaMalloc norm");
+        ck(cudaMalloc(&op->norm_dev, (op->batch + 32) * sizeof(double)), "cudaMalloc norm");
         if (op->precision == DGTD_FP32_3XTF32) op->batched = dgtd::BatchedOp::create(op->ref, op->mesh, op->dev, op->batch);
     } catch (const CudaError& e) {
         return fail(DGTD_ERR_CUDA, e.what());
@@ -305,6 +313,10 @@ int dgtd_op_get_info(const dgtd_op* op, dgtd_op_info* info)
     info->min_edge = op->mesh.min_edge;
     info->dt_scale_min = op->mesh.dt_scale_min;
     info->device_bytes = op->device_bytes + (op->batched ? op->batched->device_bytes() : 0);
+    info->work_len = op->batched ? op->batched->state_len() : op->state_len;
+    info->work_word_bytes = op->batched ? 4 : 8;
+    info->batch_padded = op->batched ? static_cast<int32_t>(op->batched->state_len() / (op->mesh.K * 6 * op->ref.Np))
+                                     : op->batch;
     return DGTD_OK;
 }
 
@@ -353,17 +365,55 @@ int dgtd_op_set_planewaves(dgtd_op* op, const dgtd_planewave* pw, int32_t n)
     return DGTD_OK;
 }
 
-int dgtd_op_mult(dgtd_op* op, const double* d_x, double* d_y, double t, void* stream)
+int dgtd_op_mult(dgtd_op* op, const void* d_x, void* d_y, double t, void* stream)
 {
     if (!op || !d_x || !d_y) return fail(DGTD_ERR_INVALID, "NULL argument");
     if (d_x == d_y) return fail(DGTD_ERR_INVALID, "x and y must not alias");
-    if (op->precision != DGTD_FP64) return fail(DGTD_ERR_UNSUPPORTED, "dgtd_op_mult is the FP64 form; use the batched API");
     try {
+        if (op->batched) {
+            BatchedCount bc(op);
+            op->batched->mult(static_cast<const float*>(d_x), static_cast<float*>(d_y), t, static_cast<cudaStream_t>(stream));
+            return DGTD_OK;
+        }
         dgtd::StageArgs A{};
         A.mode = dgtd::MODE_MULT;
-        A.in = d_x;
-        A.out = d_y;
+        A.in = static_cast<const double*>(d_x);
+        A.out = static_cast<double*>(d_y);
         run_stage(op, A, t, static_cast<cudaStream_t>(stream));
+    } catch (const std::exception& e) {
+        return fail(DGTD_ERR_CUDA, e.what());
+    }
+    return DGTD_OK;
+}
+
+int dgtd_op_pack(dgtd_op* op, const double* d_ref, void* d_work, void* stream)
+{
+    if (!op || !d_ref || !d_work) return fail(DGTD_ERR_INVALID, "NULL argument");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    try {
+        if (op->batched) {
+            BatchedCount bc(op);
+            op->batched->pack(d_ref, static_cast<float*>(d_work), s);
+        } else if (static_cast<const void*>(d_ref) != d_work) {
+            ck(cudaMemcpyAsync(d_work, d_ref, op->state_len * sizeof(double), cudaMemcpyDeviceToDevice, s), "copy");
+        }
+    } catch (const std::exception& e) {
+        return fail(DGTD_ERR_CUDA, e.what());
+    }
+    return DGTD_OK;
+}
+
+int dgtd_op_unpack(dgtd_op* op, const void* d_work, double* d_ref, void* stream)
+{
+    if (!op || !d_ref || !d_work) return fail(DGTD_ERR_INVALID, "NULL argument");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    try {
+        if (op->batched) {
+            BatchedCount bc(op);
+            op->batched->unpack(static_cast<const float*>(d_work), d_ref, s);
+        } else if (d_work != static_cast<const void*>(d_ref)) {
+            ck(cudaMemcpyAsync(d_ref, d_work, op->state_len * sizeof(double), cudaMemcpyDeviceToDevice, s), "copy");
+        }
     } catch (const std::exception& e) {
         return fail(DGTD_ERR_CUDA, e.what());
     }
@@ -374,32 +424,47 @@ int dgtd_op_mult_host(dgtd_op* op, const double* h_x, double* h_y, double t)
 {
     if (!op || !h_x || !h_y) return fail(DGTD_ERR_INVALID, "NULL argument");
     double *dx = nullptr, *dy = nullptr;
+    void *wx = nullptr, *wy = nullptr;
     const size_t bytes = op->state_len * sizeof(double);
     int rc = DGTD_OK;
     try {
         ck(cudaMalloc(&dx, bytes), "cudaMalloc");
         ck(cudaMalloc(&dy, bytes), "cudaMalloc");
         ck(cudaMemcpy(dx, h_x, bytes, cudaMemcpyHostToDevice), "H2D");
-        rc = dgtd_op_mult(op, dx, dy, t, nullptr);
-        if (rc == DGTD_OK) {
-            ck(cudaMemcpy(h_y, dy, bytes, cudaMemcpyDeviceToHost), "D2H");
+        if (op->batched) {
+            const size_t wb = op->batched->state_len() * sizeof(float);
+            ck(cudaMalloc(&wx, wb), "cudaMalloc");
+            ck(cudaMalloc(&wy, wb), "cudaMalloc");
+            rc = dgtd_op_pack(op, dx, wx, nullptr);
+            if (rc == DGTD_OK) rc = dgtd_op_mult(op, wx, wy, t, nullptr);
+            if (rc == DGTD_OK) rc = dgtd_op_unpack(op, wy, dy, nullptr);
+        } else {
+            rc = dgtd_op_mult(op, dx, dy, t, nullptr);
         }
+        if (rc == DGTD_OK) ck(cudaMemcpy(h_y, dy, bytes, cudaMemcpyDeviceToHost), "D2H");
     } catch (const std::exception& e) {
         rc = fail(DGTD_ERR_CUDA, e.what());
     }
     if (dx) cudaFree(dx);
     if (dy) cudaFree(dy);
+    if (wx) cudaFree(wx);
+    if (wy) cudaFree(wy);
     return rc;
 }
 
-int dgtd_op_step(dgtd_op* op, double* d_state, double t0, double dt, int32_t nsteps, int32_t integrator, void* stream)
+int dgtd_op_step(dgtd_op* op, void* d_work, double t0, double dt, int32_t nsteps, int32_t integrator, void* stream)
 {
-    if (!op || !d_state) return fail(DGTD_ERR_INVALID, "NULL argument");
+    if (!op || !d_work) return fail(DGTD_ERR_INVALID, "NULL argument");
     if (nsteps < 0) return fail(DGTD_ERR_INVALID, "nsteps must be >= 0");
     if (integrator != DGTD_RK4 && integrator != DGTD_LSERK4) return fail(DGTD_ERR_INVALID, "unknown integrator");
-    if (op->precision != DGTD_FP64) return fail(DGTD_ERR_UNSUPPORTED, "dgtd_op_step is the FP64 form; use the batched API");
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     try {
+        if (op->batched) {
+            BatchedCount bc(op);
+            op->batched->step(static_cast<float*>(d_work), t0, dt, nsteps, integrator, s);
+            return DGTD_OK;
+        }
+        double* d_state = static_cast<double*>(d_work);
         ensure_ws(op);
         double* other = op->ws;   // LSERK4 second state buffer
         double* cur = d_state;
@@ -423,40 +488,52 @@ int dgtd_op_run_host(dgtd_op* op, double* h_state, double t0, double dt, double 
 {
     if (!op || !h_state) return fail(DGTD_ERR_INVALID, "NULL argument");
     if (!(dt > 0.0)) return fail(DGTD_ERR_INVALID, "dt must be positive");
-    if (op->precision != DGTD_FP64) return fail(DGTD_ERR_UNSUPPORTED, "dgtd_op_run_host is the FP64 form");
     double* d = nullptr;
+    void* w = nullptr;
     const size_t bytes = op->state_len * sizeof(double);
     int rc = DGTD_OK;
     int64_t steps = 0;
     try {
         ck(cudaMalloc(&d, bytes), "cudaMalloc");
         ck(cudaMemcpy(d, h_state, bytes, cudaMemcpyHostToDevice), "H2D");
+        if (op->batched) {
+            ck(cudaMalloc(&w, op->batched->state_len() * sizeof(float)), "cudaMalloc");
+            rc = dgtd_op_pack(op, d, w, nullptr);
+        } else {
+            w = d;
+        }
         double t = t0;
-        while (t <= final_time - 1e-8 * dt) {
+        while (rc == DGTD_OK && t <= final_time - 1e-8 * dt) {
             double truedt = std::min(dt, final_time - t);
-            rc = dgtd_op_step(op, d, t, truedt, 1, integrator, nullptr);
+            rc = dgtd_op_step(op, w, t, truedt, 1, integrator, nullptr);
             if (rc != DGTD_OK) break;
             t += truedt;
             ++steps;
         }
-        if (rc == DGTD_OK) {
-            ck(cudaMemcpy(h_state, d, bytes, cudaMemcpyDeviceToHost), "D2H");
-        }
+        if (rc == DGTD_OK && op->batched) rc = dgtd_op_unpack(op, w, d, nullptr);
+        if (rc == DGTD_OK) ck(cudaMemcpy(h_state, d, bytes, cudaMemcpyDeviceToHost), "D2H");
     } catch (const std::exception& e) {
         rc = fail(DGTD_ERR_CUDA, e.what());
     }
+    if (w && w != d) cudaFree(w);
     if (d) cudaFree(d);
     if (steps_out) *steps_out = steps;
     return rc;
 }
 
-int dgtd_op_norm2(dgtd_op* op, const double* d_state, double* h_out, void* stream)
+int dgtd_op_norm2(dgtd_op* op, const void* d_state, double* h_out, void* stream)
 {
     if (!op || !d_state || !h_out) return fail(DGTD_ERR_INVALID, "NULL argument");
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     try {
-        ck(dgtd::launch_norm2(d_state, op->state_len / op->batch, op->batch, op->norm_dev, s), "norm kernel");
-        g_launches.fetch_add(1, std::memory_order_relaxed);
+        if (op->batched) {
+            BatchedCount bc(op);
+            op->batched->norm2(static_cast<const float*>(d_state), op->norm_dev, s);
+        } else {
+            ck(dgtd::launch_norm2(static_cast<const double*>(d_state), op->state_len / op->batch, op->batch,
+                                  op->norm_dev, s), "norm kernel");
+            g_launches.fetch_add(1, std::memory_order_relaxed);
+        }
         ck(cudaMemcpyAsync(h_out, op->norm_dev, op->batch * sizeof(double), cudaMemcpyDeviceToHost, s), "D2H");
         ck(cudaStreamSynchronize(s), "sync");
     } catch (const std::exception& e) {

@@ -103,6 +103,11 @@ typedef struct dgtd_op_info {
     double min_edge;
     double dt_scale_min;    /* min over elements of vol / (sum of face areas / 2) */
     int64_t device_bytes;   /* bytes of device tables held by the operator */
+    int64_t work_len;       /* entries of the operator's working state (dgtd_op_step / dgtd_op_mult):
+                               FP64 form: = state_len (reference layout);
+                               FP32 form: K*6*Np*Bpad floats, element-blocked, incidence fastest */
+    int32_t work_word_bytes;/* 8 (FP64 form) or 4 (FP32 form) */
+    int32_t batch_padded;   /* B rounded up to the incidence chunk (FP32 form), else B */
 } dgtd_op_info;
 
 typedef struct dgtd_op dgtd_op;
@@ -128,19 +133,25 @@ int dgtd_op_node_coords(const dgtd_op* op, double* h_xyz);
 int dgtd_op_set_planewaves(dgtd_op* op, const dgtd_planewave* pw, int32_t n);
 
 /* y = dU/dt(x, t): exact TimeDependentOperator::Mult semantics
- * (reference GlobalEvolution::Mult, GlobalEvolution.cpp:628-1088), FP64 form.
- * d_x, d_y: device, state_len doubles each, must not alias. */
-int dgtd_op_mult(dgtd_op* op, const double* d_x, double* d_y, double t, void* stream);
+ * (reference GlobalEvolution::Mult, GlobalEvolution.cpp:628-1088).
+ * d_x, d_y: device working states (work_len entries of work_word_bytes each;
+ * the reference layout for the FP64 form), must not alias. */
+int dgtd_op_mult(dgtd_op* op, const void* d_x, void* d_y, double t, void* stream);
+
+/* Convert between the reference layout (FP64, [b][c][e*Np+i], device) and the
+ * operator's working state (device). Identity copy for the FP64 form. */
+int dgtd_op_pack(dgtd_op* op, const double* d_ref, void* d_work, void* stream);
+int dgtd_op_unpack(dgtd_op* op, const void* d_work, double* d_ref, void* stream);
 
 /* Same as dgtd_op_mult with host buffers: copies in, applies, copies out
  * (synchronous). */
 int dgtd_op_mult_host(dgtd_op* op, const double* h_x, double* h_y, double t);
 
-/* Advance d_state (device, reference layout) by nsteps steps of size dt from t0
+/* Advance d_state (device working state) by nsteps steps of size dt from t0
  * with the fused stage kernels (reference Solver::step + mfem RK4Solver::Step,
  * Solver.cpp:535-551). The operator keeps its RK registers in device scratch it
  * allocates on first use. */
-int dgtd_op_step(dgtd_op* op, double* d_state, double t0, double dt, int32_t nsteps, int32_t integrator,
+int dgtd_op_step(dgtd_op* op, void* d_state, double t0, double dt, int32_t nsteps, int32_t integrator,
                  void* stream);
 
 /* Run to final_time from t0 following the reference loop (Solver::run,
@@ -149,8 +160,8 @@ int dgtd_op_step(dgtd_op* op, double* d_state, double t0, double dt, int32_t nst
 int dgtd_op_run_host(dgtd_op* op, double* h_state, double t0, double dt, double final_time, int32_t integrator,
                      int64_t* steps_out);
 
-/* Squared L2 norm per incidence: h_out[b] (host) for d_state (device). */
-int dgtd_op_norm2(dgtd_op* op, const double* d_state, double* h_out, void* stream);
+/* Squared L2 norm per incidence: h_out[b] (host, B entries) of a working state (device). */
+int dgtd_op_norm2(dgtd_op* op, const void* d_state, double* h_out, void* stream);
 
 /* Automatic time step of the reference's 3D Global operator
  * (estimateTimeStep, Solver.cpp:289-300, 349-351) at the given cfl. */

@@ -71,6 +71,7 @@ _P = C.c_void_p
 _D = C.POINTER(C.c_double)
 _I32 = C.POINTER(C.c_int32)
 _I64 = C.POINTER(C.c_int64)
+_D_F = C.POINTER(C.c_float)
 SIGNATURES = {
     "dgtd_last_error": (C.c_char_p, []),
     "dgtd_kernel_launches": (C.c_uint64, []),
@@ -86,11 +87,15 @@ SIGNATURES = {
     "dgtd_op_step": (C.c_int, [_P, _P, C.c_double, C.c_double, C.c_int32, C.c_int32, _P]),
     "dgtd_op_run_host": (C.c_int, [_P, _D, C.c_double, C.c_double, C.c_double, C.c_int32, _I64]),
     "dgtd_op_norm2": (C.c_int, [_P, _P, _D, _P]),
+    "dgtd_op_set_contraction": (C.c_int, [_P, C.c_int32]),
+    "dgtd_op_uses_tensor_cores": (C.c_int, [_P]),
+    "dgtd_op_check": (C.c_int, [_P, _P]),
     "dgtd_op_estimate_dt": (C.c_int, [_P, C.c_double, _D]),
     "dgtd_box_mesh_size": (C.c_int, [C.POINTER(BoxSpec), _I64, _I64, _I64, _I64]),
     "dgtd_box_mesh_fill": (C.c_int, [C.POINTER(BoxSpec), _D, _I32, _I32, _I32, _I32]),
     "dgtd_ref_tet": (C.c_int, [C.c_int32, _D, _D, _D, _D, _D, _D, _D, _D, _I32]),
     "dgtd_mesh_validate": (C.c_int, [C.POINTER(MeshDesc), C.POINTER(OpOpts), C.POINTER(OpInfo)]),
+    "dgtd_tc_selftest": (C.c_int, [_D_F, _D_F, _D_F, C.c_int32, _I32]),
 }
 
 
@@ -192,6 +197,18 @@ def ref_tet(order: int) -> dict:
     _check(lib().dgtd_ref_tet(order, *(_dp(out[k]) for k in ("r", "s", "t", "Dr", "Ds", "Dt", "Minv", "LIFT")),
                               _ip(out["Fmask"])), "ref_tet")
     return out
+
+
+def tc_selftest(a: np.ndarray, b: np.ndarray):
+    """Run the device tensor-core self-check: returns (D = A B^T in 3xTF32, status)."""
+    a = np.ascontiguousarray(a, dtype=np.float32); b = np.ascontiguousarray(b, dtype=np.float32)
+    assert a.shape[0] == 128 and b.shape[0] == 48 and a.shape[1] == b.shape[1]
+    d = np.zeros((128, 48), np.float32)
+    st = C.c_int32()
+    fp = C.POINTER(C.c_float)
+    _check(lib().dgtd_tc_selftest(a.ctypes.data_as(fp), b.ctypes.data_as(fp), d.ctypes.data_as(fp),
+                                  a.shape[1], C.byref(st)), "dgtd_tc_selftest")
+    return d, int(st.value)
 
 
 def _ptr(x) -> int:
@@ -325,6 +342,18 @@ class Operator:
     def step(self, state, t0: float, dt: float, nsteps: int, integrator: int = RK4, stream=None) -> None:
         _check(lib().dgtd_op_step(self._h, _ptr(state), float(t0), float(dt), int(nsteps), int(integrator),
                                   _stream(stream)), "dgtd_op_step")
+
+    def set_contraction(self, mode: int) -> None:
+        """FP32 batched form: 0 = tensor cores (tcgen05 3xTF32) where supported, 1 = FP32 SIMT."""
+        _check(lib().dgtd_op_set_contraction(self._h, int(mode)), "dgtd_op_set_contraction")
+
+    @property
+    def uses_tensor_cores(self) -> bool:
+        return bool(lib().dgtd_op_uses_tensor_cores(self._h))
+
+    def check(self, stream=None) -> None:
+        """Synchronise and raise if a kernel reported a timed-out device wait."""
+        _check(lib().dgtd_op_check(self._h, _stream(stream)), "dgtd_op_check")
 
     def norm2(self, state, stream=None) -> np.ndarray:
         out = np.zeros(self.batch)

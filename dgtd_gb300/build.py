@@ -22,7 +22,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3",
               "--expt-relaxed-constexpr", "-I", str(ROOT / "include")]
 
-SOURCES = ["refelem.cpp", "mesh.cpp", "plain_fp64.cu", "batched.cu", "capi.cu"]
+SOURCES = ["refelem.cpp", "mesh.cpp", "plain_fp64.cu", "batched.cu", "batched_tc.cu", "tc_selftest.cu", "capi.cu"]
 
 
 def nvcc() -> str:

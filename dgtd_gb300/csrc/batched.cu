@@ -23,7 +23,7 @@ void ckb(cudaError_t e, const char* what)
     if (e != cudaSuccess) throw std::runtime_error(std::string(what) + ": " + cudaGetErrorString(e));
 }
 
-constexpr int kWarps = 4;
+constexpr int kWarps = 8;
 constexpr int kLanes = 32;
 
 __device__ __forceinline__ void pw_eval_f32(const PlaneWaveF32* pw, int n_pw, int b, float px, float py, float pz,
@@ -123,7 +123,7 @@ __global__ void __launch_bounds__(kWarps * kLanes) stage_f32(BatchedTables T, Ba
     }
     __syncthreads();
 
-    // ---- volume + lift + epilogue: a warp owns nodes warp, warp+4, ...; two at a time ----
+    // ---- volume + lift + epilogue: a warp owns nodes warp, warp+kWarps, ...; two at a time ----
     const float* g = T.geo + e * 9;
     const float rx = g[0], ry = g[1], rz = g[2], sx = g[3], sy = g[4], sz = g[5], tx = g[6], ty = g[7], tz = g[8];
     const float ie = T.mat[e * 3 + 0], im = T.mat[e * 3 + 1], se = T.mat[e * 3 + 2];
@@ -136,6 +136,7 @@ __global__ void __launch_bounds__(kWarps * kLanes) stage_f32(BatchedTables T, Ba
         float ar0[6], as0[6], at0[6], ar1[6], as1[6], at1[6];
 #pragma unroll
         for (int c = 0; c < 6; ++c) { ar0[c] = as0[c] = at0[c] = ar1[c] = as1[c] = at1[c] = 0.0f; }
+#pragma unroll 5
         for (int j = 0; j < Np; ++j) {
             float u[6];
 #pragma unroll
@@ -153,6 +154,7 @@ __global__ void __launch_bounds__(kWarps * kLanes) stage_f32(BatchedTables T, Ba
 #pragma unroll
         for (int c = 0; c < 6; ++c) { lf0[c] = 0.0f; lf1[c] = 0.0f; }
         const int i1c = two ? i1 : i0;
+#pragma unroll 4
         for (int m = 0; m < NF; ++m) {
             const float L0 = __ldg(T.LIFT + i0 * NF + m), L1 = __ldg(T.LIFT + i1c * NF + m);
 #pragma unroll
@@ -391,6 +393,13 @@ std::unique_ptr<BatchedOp> BatchedOp::create(const RefTet& ref, const MeshTables
     T.vmapP = up(vmapP); T.fcode = up(fcode); T.fxyz = up(fxyz);
     T.nxyz = up(nxyz); T.n_tfsf_nodes = nt;
     op->perm_ = const_cast<int32_t*>(up(perm));
+    op->op_img_ = up(tc_operator_image(ref));
+    ckb(cudaMalloc(&op->status_, sizeof(int)), "cudaMalloc status");
+    op->allocs_.push_back(op->status_);
+    ckb(cudaMemset(op->status_, 0, sizeof(int)), "memset status");
+    int dev_id = 0;
+    ckb(cudaGetDevice(&dev_id), "cudaGetDevice");
+    ckb(cudaDeviceGetAttribute(&op->n_sm_, cudaDevAttrMultiProcessorCount, dev_id), "SM count");
     ckb(cudaMalloc(&op->skip_, op->Bpad_ * sizeof(int)), "cudaMalloc skip");
     op->allocs_.push_back(op->skip_);
     return op;
@@ -433,6 +442,11 @@ void BatchedOp::stage(BatchedStageArgs A, double t, cudaStream_t s)
     } else {
         A.pw = nullptr; A.n_pw = 0; A.skip = nullptr;
     }
+    if (uses_tensor_cores()) {
+        launch_stage_tc(T_, A, op_img_, status_, n_sm_, s);
+        ++launches_;
+        return;
+    }
     switch (T_.p) {
     case 1: launch_stage<1>(T_, A, s); break;
     case 2: launch_stage<2>(T_, A, s); break;
@@ -443,6 +457,15 @@ void BatchedOp::stage(BatchedStageArgs A, double t, cudaStream_t s)
     default: throw std::runtime_error("unsupported order");
     }
     ++launches_;
+}
+
+int BatchedOp::take_status(cudaStream_t s)
+{
+    int h = 0;
+    ckb(cudaMemcpyAsync(&h, status_, sizeof(int), cudaMemcpyDeviceToHost, s), "status D2H");
+    ckb(cudaStreamSynchronize(s), "sync");
+    if (h) ckb(cudaMemsetAsync(status_, 0, sizeof(int), s), "status reset");
+    return h;
 }
 
 void BatchedOp::ensure_ws()

@@ -55,6 +55,12 @@ struct BatchedStageArgs {
     const int* skip;       // [Bpad]
 };
 
+// Tensor-core stage kernel (batched_tc.cu).
+bool tc_supported(int p, int Bpad);
+std::vector<uint32_t> tc_operator_image(const RefTet& ref);
+void launch_stage_tc(const BatchedTables& T, const BatchedStageArgs& A, const uint32_t* op_img, int* status, int n_sm,
+                     cudaStream_t s);
+
 class BatchedOp {
 public:
     static std::unique_ptr<BatchedOp> create(const RefTet& ref, const MeshTables& mesh, const TablesDev& dev, int batch);
@@ -70,6 +76,11 @@ public:
     void mult(const float* d_in, float* d_out, double t, cudaStream_t s);
     void step(float* d_state, double t0, double dt, int nsteps, int integrator, cudaStream_t s);
     void norm2(const float* d_state, double* d_out_dev, cudaStream_t s);
+    // contraction path: 0 = tensor cores (tcgen05, 3xTF32) when supported, 1 = FP32 SIMT
+    void set_contraction(int mode) { contraction_ = mode; }
+    bool uses_tensor_cores() const { return contraction_ == 0 && tc_supported(T_.p, Bpad_); }
+    // reads and clears the device error flag (synchronises the stream)
+    int take_status(cudaStream_t s);
 
 private:
     void stage(BatchedStageArgs A, double t, cudaStream_t s);
@@ -88,6 +99,10 @@ private:
     int* skip_ = nullptr;
     float* ws_ = nullptr;
     bool has_tfsf_ = false;
+    int contraction_ = 0;
+    const uint32_t* op_img_ = nullptr;
+    int* status_ = nullptr;
+    int n_sm_ = 152;
 };
 
 }  // namespace dgtd

@@ -542,6 +542,30 @@ int dgtd_op_norm2(dgtd_op* op, const void* d_state, double* h_out, void* stream)
     return DGTD_OK;
 }
 
+int dgtd_op_set_contraction(dgtd_op* op, int32_t mode)
+{
+    if (!op) return fail(DGTD_ERR_INVALID, "NULL operator");
+    if (mode != 0 && mode != 1) return fail(DGTD_ERR_INVALID, "contraction mode must be 0 or 1");
+    if (op->batched) op->batched->set_contraction(mode);
+    return DGTD_OK;
+}
+
+int dgtd_op_uses_tensor_cores(const dgtd_op* op) { return (op && op->batched && op->batched->uses_tensor_cores()) ? 1 : 0; }
+
+int dgtd_op_check(dgtd_op* op, void* stream)
+{
+    if (!op) return fail(DGTD_ERR_INVALID, "NULL operator");
+    try {
+        cudaStream_t s = static_cast<cudaStream_t>(stream);
+        ck(cudaStreamSynchronize(s), "sync");
+        if (op->batched && op->batched->take_status(s))
+            return fail(DGTD_ERR_TIMEOUT, "a tensor-core completion wait inside the stage kernel timed out");
+    } catch (const std::exception& e) {
+        return fail(DGTD_ERR_CUDA, e.what());
+    }
+    return DGTD_OK;
+}
+
 int dgtd_op_estimate_dt(const dgtd_op* op, double cfl, double* dt_out)
 {
     if (!op || !dt_out) return fail(DGTD_ERR_INVALID, "NULL argument");

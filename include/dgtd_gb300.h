@@ -160,6 +160,17 @@ int dgtd_op_step(dgtd_op* op, void* d_state, double t0, double dt, int32_t nstep
 int dgtd_op_run_host(dgtd_op* op, double* h_state, double t0, double dt, double final_time, int32_t integrator,
                      int64_t* steps_out);
 
+/* Contraction path of the FP32 batched form: 0 = tensor cores (tcgen05, 3xTF32) where
+ * supported (orders 1..4, B padded to a multiple of 64), else FP32 SIMT; 1 = FP32 SIMT. */
+int dgtd_op_set_contraction(dgtd_op* op, int32_t mode);
+
+/* 1 when the FP32 batched form runs its contractions on the tensor cores, else 0. */
+int dgtd_op_uses_tensor_cores(const dgtd_op* op);
+
+/* Synchronise the stream and report device-side failures of earlier calls
+ * (a bounded wait inside a kernel that gave up): DGTD_OK or DGTD_ERR_TIMEOUT. */
+int dgtd_op_check(dgtd_op* op, void* stream);
+
 /* Squared L2 norm per incidence: h_out[b] (host, B entries) of a working state (device). */
 int dgtd_op_norm2(dgtd_op* op, const void* d_state, double* h_out, void* stream);
 
@@ -200,6 +211,12 @@ int dgtd_box_mesh_fill(const dgtd_box_spec* spec, double* vertices, int32_t* ele
  * (row-major, Hesthaven (-1,1) reference tetrahedron). Any pointer may be NULL. */
 int dgtd_ref_tet(int32_t order, double* r, double* s, double* t, double* Dr, double* Ds, double* Dt,
                  double* Minv, double* lift, int32_t* fmask);
+
+/* Device self-check of the tensor-core (tcgen05, kind::tf32) building blocks the
+ * batched form uses: D[128 x 48] = A[128 x k] * B[48 x k]^T in 3xTF32 on one CTA.
+ * h_a [128*k], h_b [48*k], h_d [128*48] host, row-major; k a multiple of 8, <= 96.
+ * *status: 0 ok, 2 the tensor-core completion wait timed out. */
+int dgtd_tc_selftest(const float* h_a, const float* h_b, float* h_d, int32_t k, int32_t* status);
 
 #ifdef __cplusplus
 }

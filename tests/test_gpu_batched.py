@@ -140,3 +140,70 @@ def test_batched_norm_and_launch_count(torch_cuda):
     op.step(w, 0.0, 1e-3, 2)
     torch.cuda.synchronize()
     assert dg.kernel_launches() - before == 8          # 4 stage kernels per RK4 step, no sources
+
+
+# ---------------------------------------------------------------- tensor-core path (tcgen05, 3xTF32)
+
+@pytest.mark.parametrize("order", [1, 2, 3, 4])
+def test_tensor_core_mult_vs_oracle(torch_cuda, order):
+    """B = 64 incidences (one 64-wide chunk): the stage runs on tcgen05; check against the oracle."""
+    torch = torch_cuda
+    m = scatter_mesh(6) if order <= 2 else dg.box_mesh((3, 3, 3), lo=(-1, -1, -1), hi=(1, 1, 1),
+                                                       tfsf=((1,) * 3, (2,) * 3), outer_bc=dg.BC_SMA)
+    B = 64
+    waves = waves_for(B, spread=0.3, mean=-0.2)
+    op = dg.Operator(m, order=order, precision=dg.FP32_3XTF32, batch=B)
+    assert op.uses_tensor_cores
+    op.set_planewaves(waves)
+    x = RNG.standard_normal(op.state_len)
+    xd = torch.from_numpy(x).cuda()
+    w = op.new_work(); y = op.new_work()
+    op.pack(xd, w)
+    op.mult(w, y, 0.25)
+    op.check()
+    yd = torch.zeros_like(xd)
+    op.unpack(y, yd)
+    torch.cuda.synchronize()
+    yv = yd.cpu().numpy()
+    L = op.state_len // B
+    for b in (0, 17, 63):
+        orc = po.Oracle.from_mesh(m, order)
+        orc.set_planewaves([waves[b]])
+        xb = x[b * L:(b + 1) * L].astype(np.float32).astype(np.float64)
+        err = rel_l2(yv[b * L:(b + 1) * L], orc.mult(xb, 0.25))
+        assert err < 2e-6, (b, err)
+
+
+def test_tensor_core_matches_simt_and_fp64(torch_cuda):
+    """Scattering case, B = 64, p = 3, 300 RK4 steps: tensor-core path vs FP32 SIMT path vs FP64 form."""
+    torch = torch_cuda
+    m = scatter_mesh(6)
+    B, order = 64, 3
+    waves = waves_for(B)
+    op64 = dg.Operator(m, order=order, batch=B)
+    tc = dg.Operator(m, order=order, precision=dg.FP32_3XTF32, batch=B)
+    simt = dg.Operator(m, order=order, precision=dg.FP32_3XTF32, batch=B)
+    simt.set_contraction(1)
+    assert tc.uses_tensor_cores and not simt.uses_tensor_cores
+    for o in (op64, tc, simt):
+        o.set_planewaves(waves)
+    dt = op64.estimate_dt(1.0)
+    x0 = torch.zeros(op64.state_len, dtype=torch.float64, device="cuda")
+    x64 = x0.clone()
+    wt = tc.new_work(); tc.pack(x0, wt)
+    ws = simt.new_work(); simt.pack(x0, ws)
+    nsteps = 300
+    op64.step(x64, 0.0, dt, nsteps)
+    tc.step(wt, 0.0, dt, nsteps)
+    simt.step(ws, 0.0, dt, nsteps)
+    tc.check()
+    xt = torch.zeros_like(x0); tc.unpack(wt, xt)
+    xs = torch.zeros_like(x0); simt.unpack(ws, xs)
+    torch.cuda.synchronize()
+    a, s_, r = xt.cpu().numpy(), xs.cpu().numpy(), x64.cpu().numpy()
+    L = op64.state_len // B
+    e_tc = [rel_l2(a[b * L:(b + 1) * L], r[b * L:(b + 1) * L]) for b in range(B)]
+    e_st = [rel_l2(a[b * L:(b + 1) * L], s_[b * L:(b + 1) * L]) for b in range(B)]
+    assert np.linalg.norm(r) > 1.0
+    assert max(e_tc) <= 1e-5, max(e_tc)
+    assert max(e_st) <= 1e-5, max(e_st)

@@ -26,13 +26,13 @@ void ckb(cudaError_t e, const char* what)
 constexpr int kWarps = 8;
 constexpr int kLanes = 32;
 
-__device__ __forceinline__ void pw_eval_f32(const PlaneWaveF32* pw, int n_pw, int b, float px, float py, float pz,
+__device__ __forceinline__ void pw_eval_f32(const PlaneWaveF32* pw, const int* pw_off, int b, float px, float py, float pz,
                                             float t, float* e, float* h)
 {
     e[0] = e[1] = e[2] = h[0] = h[1] = h[2] = 0.0f;
-    for (int q = 0; q < n_pw; ++q) {
+    const int q1 = pw_off[b + 1];
+    for (int q = pw_off[b]; q < q1; ++q) {
         const PlaneWaveF32& w = pw[q];
-        if (w.batch != b) continue;
         const float s = px * w.k[0] + py * w.k[1] + pz * w.k[2] - t;
         const float a = s - w.mean;
         float g = expf(-a * a / (2.0f * w.spread * w.spread));
@@ -92,7 +92,7 @@ __global__ void __launch_bounds__(kWarps * kLanes) stage_f32(BatchedTables T, Ba
             if (code != 0 && !skip_src) {
                 const float* xq = T.fxyz + ((e * 4 + f) * Nfp + a) * 3;
                 float pe[3], ph[3];
-                pw_eval_f32(A.pw, A.n_pw, b, xq[0], xq[1], xq[2], A.t, pe, ph);
+                pw_eval_f32(A.pw, A.pw_off, b, xq[0], xq[1], xq[2], A.t, pe, ph);
                 const float sg = (code == 4) ? 1.0f : -1.0f;
 #pragma unroll
                 for (int c = 0; c < 3; ++c) { dE[c] += sg * pe[c]; dH[c] += sg * ph[c]; }
@@ -206,13 +206,13 @@ __global__ void __launch_bounds__(kWarps * kLanes) stage_f32(BatchedTables T, Ba
     }
 }
 
-__global__ void tfsf_skip_f32(BatchedTables T, const PlaneWaveF32* pw, int n_pw, float t, int* skip)
+__global__ void tfsf_skip_f32(BatchedTables T, const PlaneWaveF32* pw, const int* pw_off, float t, int* skip)
 {
     const int b = blockIdx.x;
     double acc = 0.0;
     for (int64_t w = threadIdx.x; w < T.n_tfsf_nodes; w += blockDim.x) {
         float pe[3], ph[3];
-        pw_eval_f32(pw, n_pw, b, T.nxyz[w], T.nxyz[T.n_tfsf_nodes + w], T.nxyz[2 * T.n_tfsf_nodes + w], t, pe, ph);
+        pw_eval_f32(pw, pw_off, b, T.nxyz[w], T.nxyz[T.n_tfsf_nodes + w], T.nxyz[2 * T.n_tfsf_nodes + w], t, pe, ph);
         float s = 0.0f;
         for (int c = 0; c < 3; ++c) s += pe[c] * pe[c] + ph[c] * ph[c];
         acc += 0.25 * static_cast<double>(s);
@@ -409,18 +409,26 @@ BatchedOp::~BatchedOp()
 {
     for (void* p : allocs_) cudaFree(p);
     if (pw_dev_) cudaFree(pw_dev_);
+    if (pw_off_) cudaFree(pw_off_);
     if (ws_) cudaFree(ws_);
 }
 
 void BatchedOp::set_sources(const std::vector<PlaneWaveDev>& pw)
 {
+    // sorted by incidence with an offset table, so a kernel visits only its incidence's sources
     std::vector<PlaneWaveF32> v;
-    for (const auto& w : pw) {
-        PlaneWaveF32 f{};
-        for (int c = 0; c < 3; ++c) { f.k[c] = float(w.k[c]); f.pol[c] = float(w.pol[c]); f.kxp[c] = float(w.kxp[c]); }
-        f.spread = float(w.spread); f.mean = float(w.mean); f.freq = float(w.freq); f.batch = w.batch;
-        v.push_back(f);
+    std::vector<int> off(Bpad_ + 1, 0);
+    for (int b = 0; b < Bpad_; ++b) {
+        off[b] = static_cast<int>(v.size());
+        for (const auto& w : pw) {
+            if (w.batch != b) continue;
+            PlaneWaveF32 f{};
+            for (int c = 0; c < 3; ++c) { f.k[c] = float(w.k[c]); f.pol[c] = float(w.pol[c]); f.kxp[c] = float(w.kxp[c]); }
+            f.spread = float(w.spread); f.mean = float(w.mean); f.freq = float(w.freq); f.batch = w.batch;
+            v.push_back(f);
+        }
     }
+    off[Bpad_] = static_cast<int>(v.size());
     n_pw_ = static_cast<int>(v.size());
     if (n_pw_ > pw_cap_) {
         if (pw_dev_) cudaFree(pw_dev_);
@@ -428,19 +436,21 @@ void BatchedOp::set_sources(const std::vector<PlaneWaveDev>& pw)
         ckb(cudaMalloc(&pw_dev_, n_pw_ * sizeof(PlaneWaveF32)), "cudaMalloc sources");
         pw_cap_ = n_pw_;
     }
+    if (!pw_off_) ckb(cudaMalloc(&pw_off_, (Bpad_ + 1) * sizeof(int)), "cudaMalloc source offsets");
     if (n_pw_) ckb(cudaMemcpy(pw_dev_, v.data(), n_pw_ * sizeof(PlaneWaveF32), cudaMemcpyHostToDevice), "H2D sources");
+    ckb(cudaMemcpy(pw_off_, off.data(), (Bpad_ + 1) * sizeof(int), cudaMemcpyHostToDevice), "H2D source offsets");
 }
 
 void BatchedOp::stage(BatchedStageArgs A, double t, cudaStream_t s)
 {
     A.t = static_cast<float>(t);
     if (has_tfsf_ && n_pw_ > 0) {
-        tfsf_skip_f32<<<Bpad_, 256, 0, s>>>(T_, pw_dev_, n_pw_, static_cast<float>(t), skip_);
+        tfsf_skip_f32<<<Bpad_, 256, 0, s>>>(T_, pw_dev_, pw_off_, static_cast<float>(t), skip_);
         ckb(cudaGetLastError(), "tfsf skip kernel");
         ++launches_;
-        A.pw = pw_dev_; A.n_pw = n_pw_; A.skip = skip_;
+        A.pw = pw_dev_; A.pw_off = pw_off_; A.skip = skip_;
     } else {
-        A.pw = nullptr; A.n_pw = 0; A.skip = nullptr;
+        A.pw = nullptr; A.pw_off = nullptr; A.skip = nullptr;
     }
     if (uses_tensor_cores()) {
         launch_stage_tc(T_, A, op_img_, status_, n_sm_, s);

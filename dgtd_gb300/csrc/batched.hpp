@@ -50,9 +50,9 @@ struct BatchedStageArgs {
     float* res;
     float t, dt, a, b;
     int mode;
-    const PlaneWaveF32* pw;
-    int n_pw;
-    const int* skip;       // [Bpad]
+    const PlaneWaveF32* pw;  // sources sorted by incidence
+    const int* pw_off;       // [Bpad + 1]: sources of incidence b are pw[pw_off[b] .. pw_off[b+1])
+    const int* skip;         // [Bpad]
 };
 
 // Tensor-core stage kernel (batched_tc.cu).
@@ -95,6 +95,7 @@ private:
     std::vector<void*> allocs_;
     int32_t* perm_ = nullptr;   // internal element -> reference element
     PlaneWaveF32* pw_dev_ = nullptr;
+    int* pw_off_ = nullptr;
     int n_pw_ = 0, pw_cap_ = 0;
     int* skip_ = nullptr;
     float* ws_ = nullptr;

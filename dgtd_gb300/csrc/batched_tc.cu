@@ -56,13 +56,13 @@ struct TcOrd {
     static constexpr size_t smem = 2 * static_cast<size_t>(OpBytes) + 2 * 2 * SlotBytes;
 };
 
-__device__ __forceinline__ void pw_eval(const PlaneWaveF32* pw, int n_pw, int b, float px, float py, float pz, float t,
+__device__ __forceinline__ void pw_eval(const PlaneWaveF32* pw, const int* pw_off, int b, float px, float py, float pz, float t,
                                         float* e, float* h)
 {
     e[0] = e[1] = e[2] = h[0] = h[1] = h[2] = 0.0f;
-    for (int q = 0; q < n_pw; ++q) {
+    const int q1 = pw_off[b + 1];
+    for (int q = pw_off[b]; q < q1; ++q) {
         const PlaneWaveF32& w = pw[q];
-        if (w.batch != b) continue;
         const float s = px * w.k[0] + py * w.k[1] + pz * w.k[2] - t;
         const float a = s - w.mean;
         float g = expf(-a * a / (2.0f * w.spread * w.spread));
@@ -99,10 +99,12 @@ __global__ void __launch_bounds__(kThreads, 2) stage_tc(BatchedTables T, Batched
     __shared__ int s_err;
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    // producer mapping: incidence bl, k-quad, component half
-    const int bl = tid & 63, quad = (tid >> 6) & 1, half = tid >> 7;
+    // producer mapping: incidence bl and a pair of K columns (kq); all six target components
+    const int bl = tid & 63, kq = tid >> 6;
     const int64_t Bp = T.Bpad;
     const int nchunk = static_cast<int>(Bp / kChunk);
+    const int CB = Np * static_cast<int>(Bp);          // stride of one component inside an element block
+    const int64_t EB = 6 * static_cast<int64_t>(CB);   // stride of one element block
 
     // ---- prologue: operator image, face mask, barriers, tensor memory
     {
@@ -128,14 +130,14 @@ __global__ void __launch_bounds__(kThreads, 2) stage_tc(BatchedTables T, Batched
     const uint32_t taddr = tbase;
     const uint32_t idesc = tc::idesc_tf32(128, N);
     uint32_t ncommit0 = 0, ncommit1 = 0;     // commits issued per ring slot (uniform in all threads)
-    const float* __restrict__ in = A.in;
     const float dtf = A.dt;
 
     for (int64_t w = blockIdx.x; w < n_work; w += gridDim.x) {
         const int64_t e = w / nchunk;
         const int g = static_cast<int>(w - e * nchunk);
-        const int64_t colb = static_cast<int64_t>(g) * kChunk + bl;      // incidence column
-        const int b = static_cast<int>(colb);
+        const int b = g * kChunk + bl;                   // incidence of this thread's row
+        const int64_t eoff = e * EB + static_cast<int64_t>(g) * kChunk;
+        const float* __restrict__ ue = A.in + eoff;      // element block of the stage input
         const float* gg = T.geo + e * 9;
         const float g0 = __ldg(gg + 0), g1 = __ldg(gg + 1), g2 = __ldg(gg + 2), g3 = __ldg(gg + 3),
                     g4 = __ldg(gg + 4), g5 = __ldg(gg + 5), g6 = __ldg(gg + 6), g7 = __ldg(gg + 7), g8 = __ldg(gg + 8);
@@ -147,48 +149,52 @@ __global__ void __launch_bounds__(kThreads, 2) stage_tc(BatchedTables T, Batched
                 const uint32_t nc = slot ? ncommit1 : ncommit0;
                 if (!tc::mbar_wait(&bars[slot], (nc - 1) & 1u)) s_err = 1;
             }
-            // ---- produce K-step q: 4 consecutive k for 3 target components
-            float v[3][4];
+            // ---- produce K-step q: columns k0, k0+1 for all six target components
+            float v[6][2];
 #pragma unroll
-            for (int kk = 0; kk < 4; ++kk) {
-                const int k = q * 8 + quad * 4 + kk;
+            for (int kk = 0; kk < 2; ++kk) {
+                const int k = q * 8 + kq * 2 + kk;
                 if (k < 3 * Np) {
                     const int type = k / Np, j = k - type * Np;
-                    // partner field at node j: H for E targets (half 0), E for H targets (half 1)
-                    const int64_t base = ((e * 6 + (half ? 0 : 3)) * Np + j) * Bp + colb;
-                    const float Fx = __ldg(in + base), Fy = __ldg(in + base + Np * Bp), Fz = __ldg(in + base + 2 * Np * Bp);
-                    const float sg = half ? -1.0f : 1.0f;
                     const float gx = type == 0 ? g0 : (type == 1 ? g3 : g6);
                     const float gy = type == 0 ? g1 : (type == 1 ? g4 : g7);
                     const float gz = type == 0 ? g2 : (type == 1 ? g5 : g8);
-                    v[0][kk] = sg * (gy * Fz - gz * Fy);
-                    v[1][kk] = sg * (gz * Fx - gx * Fz);
-                    v[2][kk] = sg * (gx * Fy - gy * Fx);
+                    const int o = j * static_cast<int>(Bp) + bl;
+                    const float Ex = __ldg(ue + o), Ey = __ldg(ue + o + CB), Ez = __ldg(ue + o + 2 * CB);
+                    const float Hx = __ldg(ue + o + 3 * CB), Hy = __ldg(ue + o + 4 * CB), Hz = __ldg(ue + o + 5 * CB);
+                    // E targets: g x H (curl H); H targets: -(g x E) (-curl E)
+                    v[0][kk] = gy * Hz - gz * Hy;
+                    v[1][kk] = gz * Hx - gx * Hz;
+                    v[2][kk] = gx * Hy - gy * Hx;
+                    v[3][kk] = gz * Ey - gy * Ez;
+                    v[4][kk] = gx * Ez - gz * Ex;
+                    v[5][kk] = gy * Ex - gx * Ey;
                 } else if (k < 3 * Np + NF) {
                     const int m = k - 3 * Np, f = m / Nfp, a = m - f * Nfp;
                     const int vm = s_fmask[m];
                     const int code = __ldg(T.fcode + e * 4 + f);
                     const float* fg = T.fgeo + e * 16 + f * 4;
                     const float nx = __ldg(fg), ny = __ldg(fg + 1), nz = __ldg(fg + 2), fs = __ldg(fg + 3);
-                    const int64_t ob = ((e * 6) * Np + vm) * Bp + colb;
+                    const int o = vm * static_cast<int>(Bp) + bl;
                     float uM[6];
 #pragma unroll
-                    for (int c = 0; c < 6; ++c) uM[c] = __ldg(in + ob + c * Np * Bp);
+                    for (int c = 0; c < 6; ++c) uM[c] = __ldg(ue + o + c * CB);
                     float dE[3], dH[3];
                     float aE = T.alpha, aH = T.alpha;
                     if (code == 0 || code == 4 || code == 5) {
                         const int32_t gp = __ldg(T.vmapP + (e * 4 + f) * Nfp + a);
-                        const int64_t en = gp / Np, node = gp - en * Np;
-                        const int64_t nb = ((en * 6) * Np + node) * Bp + colb;
+                        const int32_t en = gp / Np, node = gp - en * Np;
+                        const float* __restrict__ un = A.in + static_cast<int64_t>(en) * EB +
+                                                       static_cast<int64_t>(g) * kChunk + node * static_cast<int>(Bp) + bl;
 #pragma unroll
                         for (int c = 0; c < 3; ++c) {
-                            dE[c] = __ldg(in + nb + c * Np * Bp) - uM[c];
-                            dH[c] = __ldg(in + nb + (c + 3) * Np * Bp) - uM[c + 3];
+                            dE[c] = __ldg(un + c * CB) - uM[c];
+                            dH[c] = __ldg(un + (c + 3) * CB) - uM[c + 3];
                         }
                         if (code != 0 && !skip_src) {
                             const float* xq = T.fxyz + ((e * 4 + f) * Nfp + a) * 3;
                             float pe[3], ph[3];
-                            pw_eval(A.pw, A.n_pw, b, __ldg(xq), __ldg(xq + 1), __ldg(xq + 2), A.t, pe, ph);
+                            pw_eval(A.pw, A.pw_off, b, __ldg(xq), __ldg(xq + 1), __ldg(xq + 2), A.t, pe, ph);
                             const float s2 = (code == 4) ? 1.0f : -1.0f;
 #pragma unroll
                             for (int c = 0; c < 3; ++c) { dE[c] += s2 * pe[c]; dH[c] += s2 * ph[c]; }
@@ -208,34 +214,30 @@ __global__ void __launch_bounds__(kThreads, 2) stage_tc(BatchedTables T, Batched
                         for (int c = 0; c < 3; ++c) { dE[c] = 0.0f; dH[c] = 0.0f; }
                     }
                     const float hf = 0.5f * fs;
-                    if (half == 0) {
-                        const float ndE = nx * dE[0] + ny * dE[1] + nz * dE[2];
-                        v[0][kk] = hf * ((ny * dH[2] - nz * dH[1]) + aE * (dE[0] - ndE * nx));
-                        v[1][kk] = hf * ((nz * dH[0] - nx * dH[2]) + aE * (dE[1] - ndE * ny));
-                        v[2][kk] = hf * ((nx * dH[1] - ny * dH[0]) + aE * (dE[2] - ndE * nz));
-                    } else {
-                        const float ndH = nx * dH[0] + ny * dH[1] + nz * dH[2];
-                        v[0][kk] = hf * (-(ny * dE[2] - nz * dE[1]) + aH * (dH[0] - ndH * nx));
-                        v[1][kk] = hf * (-(nz * dE[0] - nx * dE[2]) + aH * (dH[1] - ndH * ny));
-                        v[2][kk] = hf * (-(nx * dE[1] - ny * dE[0]) + aH * (dH[2] - ndH * nz));
-                    }
+                    const float ndE = nx * dE[0] + ny * dE[1] + nz * dE[2];
+                    const float ndH = nx * dH[0] + ny * dH[1] + nz * dH[2];
+                    v[0][kk] = hf * ((ny * dH[2] - nz * dH[1]) + aE * (dE[0] - ndE * nx));
+                    v[1][kk] = hf * ((nz * dH[0] - nx * dH[2]) + aE * (dE[1] - ndE * ny));
+                    v[2][kk] = hf * ((nx * dH[1] - ny * dH[0]) + aE * (dE[2] - ndE * nz));
+                    v[3][kk] = hf * (-(ny * dE[2] - nz * dE[1]) + aH * (dH[0] - ndH * nx));
+                    v[4][kk] = hf * (-(nz * dE[0] - nx * dE[2]) + aH * (dH[1] - ndH * ny));
+                    v[5][kk] = hf * (-(nx * dE[1] - ny * dE[0]) + aH * (dH[2] - ndH * nz));
                 } else {
-                    v[0][kk] = v[1][kk] = v[2][kk] = 0.0f;
+#pragma unroll
+                    for (int c = 0; c < 6; ++c) v[c][kk] = 0.0f;
                 }
             }
             unsigned char* shi = ring + slot * 2 * O::SlotBytes;
             unsigned char* slo = shi + O::SlotBytes;
 #pragma unroll
-            for (int cl = 0; cl < 3; ++cl) {
-                const int c = 3 * half + cl, t = c >> 1, r = (c & 1) * 64 + bl;
-                const uint32_t off = t * kTileBytes + tc::tile_offset(r, quad * 4);
-                float4 h4, l4;
-                h4.x = tc::to_tf32(v[cl][0]); l4.x = tc::to_tf32(v[cl][0] - h4.x);
-                h4.y = tc::to_tf32(v[cl][1]); l4.y = tc::to_tf32(v[cl][1] - h4.y);
-                h4.z = tc::to_tf32(v[cl][2]); l4.z = tc::to_tf32(v[cl][2] - h4.z);
-                h4.w = tc::to_tf32(v[cl][3]); l4.w = tc::to_tf32(v[cl][3] - h4.w);
-                *reinterpret_cast<float4*>(shi + off) = h4;
-                *reinterpret_cast<float4*>(slo + off) = l4;
+            for (int c = 0; c < 6; ++c) {
+                const int t = c >> 1, r = (c & 1) * 64 + bl;
+                const uint32_t off = t * kTileBytes + tc::tile_offset(r, kq * 2);
+                float2 h2, l2;
+                h2.x = tc::to_tf32(v[c][0]); l2.x = tc::to_tf32(v[c][0] - h2.x);
+                h2.y = tc::to_tf32(v[c][1]); l2.y = tc::to_tf32(v[c][1] - h2.y);
+                *reinterpret_cast<float2*>(shi + off) = h2;
+                *reinterpret_cast<float2*>(slo + off) = l2;
             }
             tc::fence_proxy_async();
             tc::fence_before_sync();
@@ -264,14 +266,15 @@ __global__ void __launch_bounds__(kThreads, 2) stage_tc(BatchedTables T, Batched
         if (!tc::mbar_wait(&bars[NKS & 1], (((NKS & 1) ? ncommit1 : ncommit0) - 1) & 1u)) s_err = 1;
         tc::fence_after_sync();
         if (!__syncthreads_or(s_err)) {
-            // ---- epilogue: warp (lane group lg, column half ch)
+            // ---- epilogue: warp (lane group lg, column half ch); rows of the tile are (c, incidence)
             const int lg = warp & 3, ch = warp >> 2;
             const int r = lg * 32 + lane;
             const float ie = __ldg(T.mat + e * 3 + 0), im = __ldg(T.mat + e * 3 + 1), se = __ldg(T.mat + e * 3 + 2);
+            const int blr = r & 63;
 #pragma unroll 1
             for (int t = 0; t < 3; ++t) {
-                const int c = 2 * t + (r >> 6), blr = r & 63;
-                const int64_t rowbase = ((e * 6 + c) * Np) * Bp + static_cast<int64_t>(g) * kChunk + blr;
+                const int c = 2 * t + (r >> 6);
+                const int rowoff = c * CB + blr;
 #pragma unroll 1
                 for (int c0 = ch * (N / 2); c0 < (ch + 1) * (N / 2); c0 += 8) {
                     float dv[8];
@@ -281,8 +284,8 @@ __global__ void __launch_bounds__(kThreads, 2) stage_tc(BatchedTables T, Batched
                     for (int u = 0; u < 8; ++u) {
                         const int i = c0 + u;
                         if (i >= Np) break;
-                        const int64_t idx = rowbase + static_cast<int64_t>(i) * Bp;
-                        const float uc = in[idx];
+                        const int64_t idx = eoff + rowoff + i * static_cast<int>(Bp);
+                        const float uc = ue[rowoff + i * static_cast<int>(Bp)];
                         const float k = (c < 3) ? (ie * dv[u] - se * uc) : (im * dv[u]);
                         switch (A.mode) {
                         case MODE_MULT: A.out[idx] = k; break;

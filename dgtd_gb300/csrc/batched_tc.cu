@@ -19,11 +19,12 @@
 // accumulators live in tensor memory; the epilogue applies 1/eps, 1/mu, the
 // conductivity term and the RK stage update.
 //
-// Per CTA (persistent, two per SM): the element's field block staged in shared
-// memory once per work item; a 2-slot ring holding one K-step of W (written by
-// all threads) and of Op (a 1D bulk async copy from L2 into the slot, completing
-// on an mbarrier); tcgen05.commit -> mbarrier releases a slot once the tensor
-// core has consumed it.
+// Per CTA (persistent, one per SM, 512 threads): Op hi/lo resident in shared
+// memory; the element's field block and face tables of the next work item
+// prefetched by 1D bulk async copies into a second buffer (mbarrier
+// completion) while the current item is processed; a 2-slot ring of W K-steps
+// written by all threads; tcgen05.commit -> mbarrier releases a slot once the
+// tensor core has consumed it.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -40,9 +41,10 @@ namespace dgtd {
 
 namespace {
 
-constexpr int kThreads = 256;
+constexpr int kThreads = 512;
 constexpr int kChunk = 64;          // incidences per work item
-constexpr int kTileBytes = 4096;    // 128 rows x 8 tf32
+constexpr int kWsbo = 288;                 // W operand: bytes between 8-row groups (bank-conflict-free stores)
+constexpr int kTileBytes = 16 * kWsbo;      // W tile: 128 rows x 8 tf32
 
 template <int P>
 struct TcOrd {
@@ -54,11 +56,15 @@ struct TcOrd {
     static constexpr int NKS = KKp / 8;
     static constexpr int N = (Np + 15) / 16 * 16;
     static constexpr int OpStep = N * 32;                   // bytes of one K-step of Op (N rows x 8 tf32)
+    static constexpr int OpBytes = NKS * OpStep;            // per hi / lo
     static constexpr int WBytes = 3 * kTileBytes;           // one K-step of W (3 M-tiles), per hi / lo
-    static constexpr int SlotBytes = 2 * WBytes + 2 * OpStep;
     static constexpr int UBytes = 6 * Np * kChunk * 4;      // staged element block
+    static constexpr int NbrBytes = (4 * NF + 15) / 16 * 16;
+    // U | neighbour table | face geometry (16 floats) | face codes (4 ints)
+    static constexpr int UBufBytes = (UBytes + NbrBytes + 64 + 16 + 127) / 128 * 128;
     static constexpr int TmemCols = 256;
-    static constexpr size_t smem = static_cast<size_t>(UBytes) + 2 * static_cast<size_t>(SlotBytes);
+    static constexpr size_t smem = 2 * static_cast<size_t>(OpBytes) + 2 * static_cast<size_t>(UBufBytes) +
+                                   2 * 2 * static_cast<size_t>(WBytes);
 };
 
 __device__ __forceinline__ void pw_eval(const PlaneWaveF32* pw, const int* pw_off, int b, float px, float py, float pz,
@@ -77,14 +83,14 @@ __device__ __forceinline__ void pw_eval(const PlaneWaveF32* pw, const int* pw_of
     }
 }
 
-__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* v)
+__device__ __forceinline__ void tmem_ld4(uint32_t taddr, float* v)
 {
-    uint32_t r[8];
-    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+    uint32_t r[4];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
                  : "r"(taddr));
 #pragma unroll
-    for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
+    for (int i = 0; i < 4; ++i) v[i] = __uint_as_float(r[i]);
 }
 
 __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes)
@@ -109,184 +115,290 @@ __device__ __forceinline__ void split_tf32(float v, float& hi, float& lo)
     lo = v - hi;
 }
 
+// Stage update of QC nodes (stride Bp) of one row of an element block: loads of the
+// RK registers first, then the stores. `nv` = valid nodes (<= QC).
+template <int QC>
+__device__ __forceinline__ void epilogue_store(const BatchedStageArgs& A, int64_t base, int Bp, int nv, const float* kv,
+                                               const float* uc, float dtf)
+{
+    float* __restrict__ out = A.out;
+    float* __restrict__ x = A.x;
+    float* __restrict__ y = A.yout;
+    float* __restrict__ z = A.z;
+    float* __restrict__ res = A.res;
+    float a[QC], b[QC];
+    switch (A.mode) {
+    case MODE_MULT:
+#pragma unroll
+        for (int j = 0; j < QC; ++j)
+            if (j < nv) out[base + j * Bp] = kv[j];
+        break;
+    case MODE_RK4_1:
+#pragma unroll
+        for (int j = 0; j < QC; ++j)
+            if (j < nv) {
+                y[base + j * Bp] = uc[j] + 0.5f * dtf * kv[j];
+                z[base + j * Bp] = uc[j] + (dtf / 6.0f) * kv[j];
+            }
+        break;
+    case MODE_RK4_2:
+    case MODE_RK4_3: {
+        const float cy = (A.mode == MODE_RK4_2) ? 0.5f * dtf : dtf;
+#pragma unroll
+        for (int j = 0; j < QC; ++j)
+            if (j < nv) { a[j] = x[base + j * Bp]; b[j] = z[base + j * Bp]; }
+#pragma unroll
+        for (int j = 0; j < QC; ++j)
+            if (j < nv) {
+                y[base + j * Bp] = a[j] + cy * kv[j];
+                z[base + j * Bp] = b[j] + (dtf / 3.0f) * kv[j];
+            }
+        break;
+    }
+    case MODE_RK4_4:
+#pragma unroll
+        for (int j = 0; j < QC; ++j)
+            if (j < nv) b[j] = z[base + j * Bp];
+#pragma unroll
+        for (int j = 0; j < QC; ++j)
+            if (j < nv) x[base + j * Bp] = b[j] + (dtf / 6.0f) * kv[j];
+        break;
+    case MODE_LSRK:
+#pragma unroll
+        for (int j = 0; j < QC; ++j)
+            if (j < nv) a[j] = res[base + j * Bp];
+#pragma unroll
+        for (int j = 0; j < QC; ++j)
+            if (j < nv) {
+                const float rr = A.a * a[j] + dtf * kv[j];
+                res[base + j * Bp] = rr;
+                y[base + j * Bp] = uc[j] + A.b * rr;
+            }
+        break;
+    default: break;
+    }
+}
+
+// Issue the bulk copies of one work item's element block and face tables (one thread).
 template <int P>
-__global__ void __launch_bounds__(kThreads, 2) stage_tc(BatchedTables T, BatchedStageArgs A, const uint32_t* __restrict__ op_img,
+__device__ __forceinline__ void prefetch_item(const BatchedTables& T, const float* in, int64_t w, int nchunk, int Bp,
+                                              unsigned char* buf, uint64_t* bar)
+{
+    using O = TcOrd<P>;
+    constexpr int Np = O::Np, NF = O::NF;
+    const int64_t e = w / nchunk;
+    const int g = static_cast<int>(w - e * nchunk);
+    const int64_t EB = 6 * static_cast<int64_t>(Np) * Bp;
+    const float* src = in + e * EB + static_cast<int64_t>(g) * kChunk;
+    mbar_expect_tx(bar, O::UBytes + 4 * NF + 64 + 16);
+    if (Bp == kChunk) {
+        bulk_g2s(buf, src, O::UBytes, bar);
+    } else {
+        for (int r = 0; r < 6 * Np; ++r)
+            bulk_g2s(buf + r * kChunk * 4, src + static_cast<int64_t>(r) * Bp, kChunk * 4, bar);
+    }
+    bulk_g2s(buf + O::UBytes, T.vmapP + e * NF, 4 * NF, bar);
+    bulk_g2s(buf + O::UBytes + O::NbrBytes, T.fgeo + e * 16, 64, bar);
+    bulk_g2s(buf + O::UBytes + O::NbrBytes + 64, T.fcode + e * 4, 16, bar);
+}
+
+template <int P>
+__global__ void __launch_bounds__(kThreads, 1) stage_tc(BatchedTables T, BatchedStageArgs A, const uint32_t* __restrict__ op_img,
                                                      int64_t n_work, int* status)
 {
     using O = TcOrd<P>;
     constexpr int Np = O::Np, Nfp = O::Nfp, NF = O::NF, NKS = O::NKS, N = O::N;
     extern __shared__ __align__(128) unsigned char sm[];
-    float* s_u = reinterpret_cast<float*>(sm);                // [6][Np][64]
-    unsigned char* ring = sm + O::UBytes;                     // [slot]{W hi, W lo, Op hi, Op lo}
-    __shared__ uint64_t mma_bar[2], op_bar[2];
+    unsigned char* op_hi = sm;
+    unsigned char* op_lo = sm + O::OpBytes;
+    unsigned char* ubuf0 = sm + 2 * O::OpBytes;
+    unsigned char* ring = ubuf0 + 2 * O::UBufBytes;           // [slot]{W hi, W lo}
+    __shared__ uint64_t mma_bar[2], u_bar[2];
     __shared__ uint32_t tbase;
     __shared__ int s_fmask[NF];
-    __shared__ int32_t s_nbr[NF];        // neighbour (element * Np + node) of each face node, internal numbering
-    __shared__ float s_fg[16];            // nx ny nz Fscale per face
-    __shared__ int s_code[4];
-    __shared__ int s_err;
+    __shared__ int s_tj[3 * Np];          // combo column -> (type << 8) | node
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int bl = tid & 63, kq = tid >> 6;      // producer: incidence and a pair of K columns
+    const int bl = tid & 63, kc8 = tid >> 6;     // producer: incidence and one K column of each K-step
     const int Bp = static_cast<int>(T.Bpad);
     const int nchunk = Bp / kChunk;
     const int CB = Np * Bp;                      // component stride inside an element block (global)
     const int64_t EB = 6 * static_cast<int64_t>(CB);
 
+    // ---- prologue: resident operator, lookup tables, barriers, tensor memory, first item
+    {
+        const uint4* src = reinterpret_cast<const uint4*>(op_img);
+        uint4* dst = reinterpret_cast<uint4*>(op_hi);
+        for (int i = tid; i < 2 * O::OpBytes / 16; i += kThreads) dst[i] = __ldg(src + i);
+    }
     for (int i = tid; i < NF; i += kThreads) s_fmask[i] = T.Fmask[i];
+    for (int i = tid; i < 3 * Np; i += kThreads) s_tj[i] = ((i / Np) << 8) | (i % Np);
     if (tid == 0) {
-        for (int s = 0; s < 2; ++s) { tc::mbar_init(&mma_bar[s], 1); tc::mbar_init(&op_bar[s], 1); }
+        for (int s = 0; s < 2; ++s) { tc::mbar_init(&mma_bar[s], 1); tc::mbar_init(&u_bar[s], 1); }
         tc::mbar_fence_init();
-        s_err = 0;
     }
     if (warp == 0) {
         tc::tmem_alloc(&tbase, O::TmemCols);
         tc::tmem_relinquish();
     }
+    tc::fence_proxy_async();
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
+    if (tid == 0 && static_cast<int64_t>(blockIdx.x) < n_work)
+        prefetch_item<P>(T, A.in, blockIdx.x, nchunk, Bp, ubuf0, &u_bar[0]);
     const uint32_t taddr = tbase;
     const uint32_t idesc = tc::idesc_tf32(128, N);
-    uint32_t nmma0 = 0u, nmma1 = 0u, nop0 = 0u, nop1 = 0u;   // completions issued per ring slot (uniform)
+    // phases per barrier: MMA commits, item copies issued and consumed (uniform in all threads)
+    uint32_t nmma0 = 0u, nmma1 = 0u, nu0 = 0u, nu1 = 0u, ni0 = 0u, ni1 = 0u;
+    int err = 0;   // a bounded wait ran out; made uniform at the next barrier
+    if (static_cast<int64_t>(blockIdx.x) < n_work) ++ni0;
     const float dtf = A.dt;
+    // per-thread store offsets of the producer (row = (c & 1) * 64 + bl of tile c / 2, column kc8)
+    uint32_t soff[6];
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+        const int r = (c & 1) * 64 + bl;
+        soff[c] = (c >> 1) * kTileBytes + (r >> 3) * kWsbo + ((kc8 & 7) >> 2) * tc::kLBO + (r & 7) * 16 + (kc8 & 3) * 4;
+    }
 
-    for (int64_t w = blockIdx.x; w < n_work; w += gridDim.x) {
+    int it = 0;
+    for (int64_t w = blockIdx.x; w < n_work; w += gridDim.x, ++it) {
+        const int ub = it & 1;
+        unsigned char* buf = ubuf0 + ub * O::UBufBytes;
+        const float* s_u = reinterpret_cast<const float*>(buf);          // [6][Np][64]
+        const int32_t* s_nbr = reinterpret_cast<const int32_t*>(buf + O::UBytes);
+        const float* s_fg = reinterpret_cast<const float*>(buf + O::UBytes + O::NbrBytes);
+        const int* s_code = reinterpret_cast<const int*>(buf + O::UBytes + O::NbrBytes + 64);
+        if (!tc::mbar_wait(&u_bar[ub], ((ub ? nu1 : nu0)) & 1u)) err = 1;
+        if (ub) ++nu1; else ++nu0;
+        // prefetch the next item into the other buffer (its previous user finished last iteration)
+        if (w + gridDim.x < n_work) {
+            if (tid == 0)
+                prefetch_item<P>(T, A.in, w + gridDim.x, nchunk, Bp, ubuf0 + (ub ^ 1) * O::UBufBytes, &u_bar[ub ^ 1]);
+            if (ub) ++ni0; else ++ni1;
+        }
+
         const int64_t e = w / nchunk;
         const int g = static_cast<int>(w - e * nchunk);
         const int b = g * kChunk + bl;
         const int64_t eoff = e * EB + static_cast<int64_t>(g) * kChunk;
-        // ---- stage the element block (6 Np rows of 64 incidences) and its face tables
-        {
-            const float* __restrict__ src = A.in + eoff;
-            for (int idx = tid; idx < 6 * Np * 16; idx += kThreads) {
-                const int row = idx >> 4, q4 = idx & 15;
-                reinterpret_cast<float4*>(s_u)[idx] =
-                    __ldg(reinterpret_cast<const float4*>(src + static_cast<int64_t>(row) * Bp) + q4);
-            }
-            for (int i = tid; i < NF; i += kThreads) s_nbr[i] = __ldg(T.vmapP + e * NF + i);
-            if (tid < 16) s_fg[tid] = __ldg(T.fgeo + e * 16 + tid);
-            if (tid < 4) s_code[tid] = __ldg(T.fcode + e * 4 + tid);
-        }
         const float* gg = T.geo + e * 9;
         const float g0 = __ldg(gg + 0), g1 = __ldg(gg + 1), g2 = __ldg(gg + 2), g3 = __ldg(gg + 3),
                     g4 = __ldg(gg + 4), g5 = __ldg(gg + 5), g6 = __ldg(gg + 6), g7 = __ldg(gg + 7), g8 = __ldg(gg + 8);
         const bool skip_src = (A.skip == nullptr) || A.skip[b];
-        __syncthreads();
+        // neighbour traces of this thread's flux column, loaded one K-step ahead
+        auto load_nbr = [&](int k, float* dst) {
+            if (k < NF) {
+                const int code = s_code[k / Nfp];
+                if (code == 0 || code == 4 || code == 5) {
+                    const int32_t gp = s_nbr[k];
+                    const int32_t en = gp / Np, node = gp - en * Np;
+                    const float* __restrict__ un =
+                        A.in + static_cast<int64_t>(en) * EB + static_cast<int64_t>(g) * kChunk + node * Bp + bl;
+#pragma unroll
+                    for (int c = 0; c < 6; ++c) dst[c] = __ldg(un + c * CB);
+                }
+            }
+        };
+        float nb[6], nbn[6];
+        load_nbr(kc8, nb);
 
         for (int q = 0; q < NKS; ++q) {
+            load_nbr((q + 1) * 8 + kc8, nbn);
             const int slot = q & 1;
-            unsigned char* sw = ring + slot * O::SlotBytes;
-            unsigned char* w_hi = sw;
-            unsigned char* w_lo = sw + O::WBytes;
-            unsigned char* o_hi = sw + 2 * O::WBytes;
-            if (q >= 2 && !tc::mbar_wait(&mma_bar[slot], ((slot ? nmma1 : nmma0) - 1) & 1u)) s_err = 1;
-            if (tid == 0) {
-                // Op K-step q (hi and lo contiguous) into the slot
-                mbar_expect_tx(&op_bar[slot], 2 * O::OpStep);
-                bulk_g2s(o_hi, op_img + static_cast<size_t>(q) * (2 * O::OpStep / 4), 2 * O::OpStep, &op_bar[slot]);
-            }
-            if (slot) ++nop1; else ++nop0;
-            // ---- produce K-step q of W: columns k0, k0 + 1 for all six target components
-            float v[6][2];
+            unsigned char* w_hi = ring + slot * 2 * O::WBytes;
+            unsigned char* w_lo = w_hi + O::WBytes;
+            if (q >= 2 && !tc::mbar_wait(&mma_bar[slot], ((slot ? nmma1 : nmma0) - 1) & 1u)) err = 1;
+            // ---- produce column k of K-step q for all six target components
+            float v[6];
+            const int k = q * 8 + kc8;
+            if (k < NF) {
+                const int m = k, f = m / Nfp;
+                const int vm = s_fmask[m];
+                const int code = s_code[f];
+                const float nx = s_fg[f * 4], ny = s_fg[f * 4 + 1], nz = s_fg[f * 4 + 2], fs = s_fg[f * 4 + 3];
+                float uM[6];
 #pragma unroll
-            for (int kk = 0; kk < 2; ++kk) {
-                const int k = q * 8 + kq * 2 + kk;
-                if (k < NF) {
-                    const int m = k, f = m / Nfp;
-                    const int vm = s_fmask[m];
-                    const int code = s_code[f];
-                    const float nx = s_fg[f * 4], ny = s_fg[f * 4 + 1], nz = s_fg[f * 4 + 2], fs = s_fg[f * 4 + 3];
-                    float uM[6];
+                for (int c = 0; c < 6; ++c) uM[c] = s_u[(c * Np + vm) * kChunk + bl];
+                float dE[3], dH[3];
+                float aE = T.alpha, aH = T.alpha;
+                if (code == 0 || code == 4 || code == 5) {
 #pragma unroll
-                    for (int c = 0; c < 6; ++c) uM[c] = s_u[(c * Np + vm) * kChunk + bl];
-                    float dE[3], dH[3];
-                    float aE = T.alpha, aH = T.alpha;
-                    if (code == 0 || code == 4 || code == 5) {
-                        const int32_t gp = s_nbr[m];
-                        const int32_t en = gp / Np, node = gp - en * Np;
-                        const float* __restrict__ un =
-                            A.in + static_cast<int64_t>(en) * EB + static_cast<int64_t>(g) * kChunk + node * Bp + bl;
-#pragma unroll
-                        for (int c = 0; c < 3; ++c) {
-                            dE[c] = __ldg(un + c * CB) - uM[c];
-                            dH[c] = __ldg(un + (c + 3) * CB) - uM[c + 3];
-                        }
-                        if (code != 0 && !skip_src) {
-                            const float* xq = T.fxyz + (e * NF + m) * 3;
-                            float pe[3], ph[3];
-                            pw_eval(A.pw, A.pw_off, b, __ldg(xq), __ldg(xq + 1), __ldg(xq + 2), A.t, pe, ph);
-                            const float s2 = (code == 4) ? 1.0f : -1.0f;
-#pragma unroll
-                            for (int c = 0; c < 3; ++c) { dE[c] += s2 * pe[c]; dH[c] += s2 * ph[c]; }
-                        }
-                    } else if (code == 1 || code == 6) {
-#pragma unroll
-                        for (int c = 0; c < 3; ++c) { dE[c] = -2.0f * uM[c]; dH[c] = 0.0f; }
-                    } else if (code == 2 || code == 7) {
-#pragma unroll
-                        for (int c = 0; c < 3; ++c) { dE[c] = 0.0f; dH[c] = -2.0f * uM[c + 3]; }
-                    } else if (code == 3 || code == 8) {
-#pragma unroll
-                        for (int c = 0; c < 3; ++c) { dE[c] = -uM[c]; dH[c] = -uM[c + 3]; }
-                        aE = 1.0f; aH = 1.0f;
-                    } else {
-#pragma unroll
-                        for (int c = 0; c < 3; ++c) { dE[c] = 0.0f; dH[c] = 0.0f; }
+                    for (int c = 0; c < 3; ++c) {
+                        dE[c] = nb[c] - uM[c];
+                        dH[c] = nb[c + 3] - uM[c + 3];
                     }
-                    const float hf = 0.5f * fs;
-                    const float ndE = nx * dE[0] + ny * dE[1] + nz * dE[2];
-                    const float ndH = nx * dH[0] + ny * dH[1] + nz * dH[2];
-                    v[0][kk] = hf * ((ny * dH[2] - nz * dH[1]) + aE * (dE[0] - ndE * nx));
-                    v[1][kk] = hf * ((nz * dH[0] - nx * dH[2]) + aE * (dE[1] - ndE * ny));
-                    v[2][kk] = hf * ((nx * dH[1] - ny * dH[0]) + aE * (dE[2] - ndE * nz));
-                    v[3][kk] = hf * (-(ny * dE[2] - nz * dE[1]) + aH * (dH[0] - ndH * nx));
-                    v[4][kk] = hf * (-(nz * dE[0] - nx * dE[2]) + aH * (dH[1] - ndH * ny));
-                    v[5][kk] = hf * (-(nx * dE[1] - ny * dE[0]) + aH * (dH[2] - ndH * nz));
-                } else if (k < NF + 3 * Np) {
-                    const int kc = k - NF, type = kc / Np, j = kc - type * Np;
-                    const float gx = type == 0 ? g0 : (type == 1 ? g3 : g6);
-                    const float gy = type == 0 ? g1 : (type == 1 ? g4 : g7);
-                    const float gz = type == 0 ? g2 : (type == 1 ? g5 : g8);
-                    const float* uj = s_u + j * kChunk + bl;
-                    const float Ex = uj[0], Ey = uj[Np * kChunk], Ez = uj[2 * Np * kChunk];
-                    const float Hx = uj[3 * Np * kChunk], Hy = uj[4 * Np * kChunk], Hz = uj[5 * Np * kChunk];
-                    // E targets: g x H (curl H); H targets: -(g x E) (-curl E)
-                    v[0][kk] = gy * Hz - gz * Hy;
-                    v[1][kk] = gz * Hx - gx * Hz;
-                    v[2][kk] = gx * Hy - gy * Hx;
-                    v[3][kk] = gz * Ey - gy * Ez;
-                    v[4][kk] = gx * Ez - gz * Ex;
-                    v[5][kk] = gy * Ex - gx * Ey;
+                    if (code != 0 && !skip_src) {
+                        const float* xq = T.fxyz + (e * NF + m) * 3;
+                        float pe[3], ph[3];
+                        pw_eval(A.pw, A.pw_off, b, __ldg(xq), __ldg(xq + 1), __ldg(xq + 2), A.t, pe, ph);
+                        const float s2 = (code == 4) ? 1.0f : -1.0f;
+#pragma unroll
+                        for (int c = 0; c < 3; ++c) { dE[c] += s2 * pe[c]; dH[c] += s2 * ph[c]; }
+                    }
+                } else if (code == 1 || code == 6) {
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) { dE[c] = -2.0f * uM[c]; dH[c] = 0.0f; }
+                } else if (code == 2 || code == 7) {
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) { dE[c] = 0.0f; dH[c] = -2.0f * uM[c + 3]; }
+                } else if (code == 3 || code == 8) {
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) { dE[c] = -uM[c]; dH[c] = -uM[c + 3]; }
+                    aE = 1.0f; aH = 1.0f;
                 } else {
 #pragma unroll
-                    for (int c = 0; c < 6; ++c) v[c][kk] = 0.0f;
+                    for (int c = 0; c < 3; ++c) { dE[c] = 0.0f; dH[c] = 0.0f; }
                 }
+                const float hf = 0.5f * fs;
+                const float ndE = nx * dE[0] + ny * dE[1] + nz * dE[2];
+                const float ndH = nx * dH[0] + ny * dH[1] + nz * dH[2];
+                v[0] = hf * ((ny * dH[2] - nz * dH[1]) + aE * (dE[0] - ndE * nx));
+                v[1] = hf * ((nz * dH[0] - nx * dH[2]) + aE * (dE[1] - ndE * ny));
+                v[2] = hf * ((nx * dH[1] - ny * dH[0]) + aE * (dE[2] - ndE * nz));
+                v[3] = hf * (-(ny * dE[2] - nz * dE[1]) + aH * (dH[0] - ndH * nx));
+                v[4] = hf * (-(nz * dE[0] - nx * dE[2]) + aH * (dH[1] - ndH * ny));
+                v[5] = hf * (-(nx * dE[1] - ny * dE[0]) + aH * (dH[2] - ndH * nz));
+            } else if (k < NF + 3 * Np) {
+                const int tj = s_tj[k - NF], type = tj >> 8, j = tj & 255;
+                const float gx = type == 0 ? g0 : (type == 1 ? g3 : g6);
+                const float gy = type == 0 ? g1 : (type == 1 ? g4 : g7);
+                const float gz = type == 0 ? g2 : (type == 1 ? g5 : g8);
+                const float* uj = s_u + j * kChunk + bl;
+                const float Ex = uj[0], Ey = uj[Np * kChunk], Ez = uj[2 * Np * kChunk];
+                const float Hx = uj[3 * Np * kChunk], Hy = uj[4 * Np * kChunk], Hz = uj[5 * Np * kChunk];
+                // E targets: g x H (curl H); H targets: -(g x E) (-curl E)
+                v[0] = gy * Hz - gz * Hy;
+                v[1] = gz * Hx - gx * Hz;
+                v[2] = gx * Hy - gy * Hx;
+                v[3] = gz * Ey - gy * Ez;
+                v[4] = gx * Ez - gz * Ex;
+                v[5] = gy * Ex - gx * Ey;
+            } else {
+#pragma unroll
+                for (int c = 0; c < 6; ++c) v[c] = 0.0f;
             }
 #pragma unroll
             for (int c = 0; c < 6; ++c) {
-                const int t = c >> 1, r = (c & 1) * 64 + bl;
-                const uint32_t off = t * kTileBytes + tc::tile_offset(r, kq * 2);
-                float2 h2, l2;
-                split_tf32(v[c][0], h2.x, l2.x);
-                split_tf32(v[c][1], h2.y, l2.y);
-                *reinterpret_cast<float2*>(w_hi + off) = h2;
-                *reinterpret_cast<float2*>(w_lo + off) = l2;
+                float h, l;
+                split_tf32(v[c], h, l);
+                *reinterpret_cast<float*>(w_hi + soff[c]) = h;
+                *reinterpret_cast<float*>(w_lo + soff[c]) = l;
             }
             tc::fence_proxy_async();
             tc::fence_before_sync();
-            __syncthreads();
-            if (s_err) break;
-            if (tid == 0 && !tc::mbar_wait(&op_bar[slot], ((slot ? nop1 : nop0) - 1) & 1u)) s_err = 1;
-            if (tid == 0 && !s_err) {
+            if (__syncthreads_or(err)) { err = 1; break; }
+            if (tid == 0) {
                 tc::fence_after_sync();
                 const uint32_t ah0 = tc::smem_u32(w_hi), al0 = tc::smem_u32(w_lo);
-                const uint64_t bh = tc::smem_desc(tc::smem_u32(o_hi));
-                const uint64_t blo = tc::smem_desc(tc::smem_u32(o_hi + O::OpStep));
+                const uint64_t bh = tc::smem_desc(tc::smem_u32(op_hi + q * O::OpStep));
+                const uint64_t blo = tc::smem_desc(tc::smem_u32(op_lo + q * O::OpStep));
 #pragma unroll
                 for (int t = 0; t < 3; ++t) {
                     const uint32_t d = taddr + t * N;
-                    const uint64_t ah = tc::smem_desc(ah0 + t * kTileBytes), al = tc::smem_desc(al0 + t * kTileBytes);
+                    const uint64_t ah = tc::smem_desc_sbo(ah0 + t * kTileBytes, kWsbo);
+                    const uint64_t al = tc::smem_desc_sbo(al0 + t * kTileBytes, kWsbo);
                     tc::mma_tf32(d, ah, bh, idesc, q > 0);
                     tc::mma_tf32(d, al, bh, idesc, true);
                     tc::mma_tf32(d, ah, blo, idesc, true);
@@ -294,57 +406,58 @@ __global__ void __launch_bounds__(kThreads, 2) stage_tc(BatchedTables T, Batched
                 tc::mma_commit(&mma_bar[slot]);
             }
             if (slot) ++nmma1; else ++nmma0;
+#pragma unroll
+            for (int c = 0; c < 6; ++c) nb[c] = nbn[c];
         }
-        if (s_err) break;
+        if (err) break;
         // ---- all MMAs of this work item done
-        if (!tc::mbar_wait(&mma_bar[0], (nmma0 - 1) & 1u)) s_err = 1;
-        if (!tc::mbar_wait(&mma_bar[1], (nmma1 - 1) & 1u)) s_err = 1;
+        if (!tc::mbar_wait(&mma_bar[0], (nmma0 - 1) & 1u)) err = 1;
+        if (!tc::mbar_wait(&mma_bar[1], (nmma1 - 1) & 1u)) err = 1;
         tc::fence_after_sync();
-        if (!__syncthreads_or(s_err)) {
-            // ---- epilogue: warp (lane group lg, column half ch); tile rows are (c, incidence)
-            const int lg = warp & 3, ch = warp >> 2;
+        if (__syncthreads_or(err)) { err = 1; break; }
+        {
+            // ---- epilogue: warp = (lane group lg, column quarter cq); tile rows are (c, incidence).
+            // All operand loads of a tile are issued before its stores so that each thread
+            // waits for one memory round trip per tile, not one per output.
+            constexpr int QC = N / 4;
+            const int lg = warp & 3, cq = warp >> 2;
             const int r = lg * 32 + lane;
             const float ie = __ldg(T.mat + e * 3 + 0), im = __ldg(T.mat + e * 3 + 1), se = __ldg(T.mat + e * 3 + 2);
             const int blr = r & 63;
+            const int cb = cq * QC;
 #pragma unroll 1
             for (int t = 0; t < 3; ++t) {
                 const int c = 2 * t + (r >> 6);
-                const int rowoff = c * CB + blr;
-                const float* su = s_u + c * Np * kChunk + blr;
-#pragma unroll 1
-                for (int c0 = ch * (N / 2); c0 < (ch + 1) * (N / 2); c0 += 8) {
-                    float dv[8];
-                    tmem_ld8(taddr + (static_cast<uint32_t>(lg * 32) << 16) + t * N + c0, dv);
-                    tc::tmem_ld_wait();
+                const int64_t base = eoff + c * CB + blr + static_cast<int64_t>(cb) * Bp;
+                const float* su = s_u + (c * Np + cb) * kChunk + blr;
+                float kv[QC], uc[QC];
 #pragma unroll
-                    for (int u = 0; u < 8; ++u) {
-                        const int i = c0 + u;
-                        if (i >= Np) break;
-                        const int64_t idx = eoff + rowoff + i * Bp;
-                        const float uc = su[i * kChunk];
-                        const float k = (c < 3) ? (ie * dv[u] - se * uc) : (im * dv[u]);
-                        switch (A.mode) {
-                        case MODE_MULT: A.out[idx] = k; break;
-                        case MODE_RK4_1: A.yout[idx] = uc + 0.5f * dtf * k; A.z[idx] = uc + (dtf / 6.0f) * k; break;
-                        case MODE_RK4_2: A.yout[idx] = A.x[idx] + 0.5f * dtf * k; A.z[idx] += (dtf / 3.0f) * k; break;
-                        case MODE_RK4_3: A.yout[idx] = A.x[idx] + dtf * k; A.z[idx] += (dtf / 3.0f) * k; break;
-                        case MODE_RK4_4: A.x[idx] = A.z[idx] + (dtf / 6.0f) * k; break;
-                        case MODE_LSRK: {
-                            const float rr = A.a * A.res[idx] + dtf * k;
-                            A.res[idx] = rr;
-                            A.yout[idx] = uc + A.b * rr;
-                            break;
-                        }
-                        default: break;
-                        }
-                    }
+                for (int j = 0; j < QC; j += 4)
+                    tmem_ld4(taddr + (static_cast<uint32_t>(lg * 32) << 16) + t * N + cb + j, kv + j);
+                tc::tmem_ld_wait();
+                const float fe = (c < 3) ? ie : im, fs = (c < 3) ? se : 0.0f;
+#pragma unroll
+                for (int j = 0; j < QC; ++j) {
+                    uc[j] = (cb + j < Np) ? su[j * kChunk] : 0.0f;
+                    kv[j] = fe * kv[j] - fs * uc[j];
                 }
+                epilogue_store<QC>(A, base, Bp, Np - cb, kv, uc, dtf);
             }
         }
         tc::fence_before_sync();
-        if (__syncthreads_or(s_err)) break;
+        __syncthreads();
     }
-    if (s_err && tid == 0) atomicExch(status, 1);
+    if (err) {
+        // drain: wait (bounded) for this CTA's copies and MMAs still in flight before
+        // the tensor memory and the shared buffers are released
+        if (tid == 0) {
+            atomicExch(status, 1);
+            if (nmma0) tc::mbar_wait(&mma_bar[0], (nmma0 - 1) & 1u);
+            if (nmma1) tc::mbar_wait(&mma_bar[1], (nmma1 - 1) & 1u);
+            if (ni0) tc::mbar_wait(&u_bar[0], (ni0 - 1) & 1u);
+            if (ni1) tc::mbar_wait(&u_bar[1], (ni1 - 1) & 1u);
+        }
+    }
     tc::fence_before_sync();
     __syncthreads();
     if (warp == 0) tc::tmem_dealloc(taddr, O::TmemCols);
@@ -371,13 +484,13 @@ float bits_to_float(uint32_t u)
 bool tc_supported(int p, int Bpad) { return p >= 1 && p <= 4 && Bpad % kChunk == 0; }
 
 // Host image of Op = [LIFT | Dr | Ds | Dt]^T as the kernel's K-major B operand:
-// per K-step q, N rows x 8 tf32 high parts followed by the N x 8 low parts.
+// all K-steps of the tf32 high parts (N rows x 8 columns each), then all low parts.
 std::vector<uint32_t> tc_operator_image(const RefTet& ref)
 {
     const int Np = ref.Np, Nfp = ref.Nfp, NF = 4 * Nfp, KK = NF + 3 * Np, KKp = (KK + 7) / 8 * 8, NKS = KKp / 8;
     const int N = (Np + 15) / 16 * 16;
-    const size_t step_words = static_cast<size_t>(N) * 8;        // one K-step, hi or lo
-    std::vector<uint32_t> img(2 * step_words * NKS, 0u);
+    const size_t words = static_cast<size_t>(NKS) * N * 8;        // one operator part (hi or lo)
+    std::vector<uint32_t> img(2 * words, 0u);
     for (int i = 0; i < Np; ++i)
         for (int k = 0; k < KK; ++k) {
             double v;
@@ -391,10 +504,9 @@ std::vector<uint32_t> tc_operator_image(const RefTet& ref)
             const uint32_t hb = tf32_bits_rna(f);
             const float lo = static_cast<float>(v - static_cast<double>(bits_to_float(hb)));
             const uint32_t lb = tf32_bits_rna(lo);
-            const size_t base = static_cast<size_t>(k / 8) * 2 * step_words;
-            const size_t off = tc::tile_offset(i, k) / 4;
-            img[base + off] = hb;
-            img[base + step_words + off] = lb;
+            const size_t off = (static_cast<size_t>(k / 8) * N * 32 + tc::tile_offset(i, k)) / 4;
+            img[off] = hb;
+            img[words + off] = lb;
         }
     return img;
 }
@@ -403,6 +515,8 @@ void launch_stage_tc(const BatchedTables& T, const BatchedStageArgs& A, const ui
                      cudaStream_t s)
 {
     const int64_t n_work = T.K * (T.Bpad / kChunk);
+    if (reinterpret_cast<uintptr_t>(A.in) % 16 != 0)
+        throw std::runtime_error("tensor-core stage: the input state must be 16-byte aligned (bulk async copies)");
     auto go = [&](auto kernel, size_t smem) {
         static bool attr[8] = {};
         if (!attr[T.p]) {
@@ -410,8 +524,7 @@ void launch_stage_tc(const BatchedTables& T, const BatchedStageArgs& A, const ui
             if (e != cudaSuccess) throw std::runtime_error(std::string("tc smem attribute: ") + cudaGetErrorString(e));
             attr[T.p] = true;
         }
-        const int per_sm = (2 * (smem + 2048) <= 228 * 1024) ? 2 : 1;
-        const int64_t grid = std::min<int64_t>(n_work, static_cast<int64_t>(n_sm) * per_sm);
+        const int64_t grid = std::min<int64_t>(n_work, static_cast<int64_t>(n_sm));
         kernel<<<static_cast<unsigned>(grid), kThreads, smem, s>>>(T, A, op_img, n_work, status);
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) throw std::runtime_error(std::string("tc stage kernel: ") + cudaGetErrorString(e));

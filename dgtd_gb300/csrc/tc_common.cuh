@@ -40,6 +40,19 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr)
     return d;
 }
 
+// Same with an explicit stride-byte offset (multiple of 16 bytes): a stride that is
+// 32 bytes past a multiple of 128 puts the four 8-row groups touched by 32
+// consecutive rows of one K column on 32 distinct shared-memory banks.
+__device__ __forceinline__ uint64_t smem_desc_sbo(uint32_t saddr, uint32_t sbo)
+{
+    uint64_t d = 0;
+    d |= static_cast<uint64_t>((saddr >> 4) & 0x3FFFu);
+    d |= static_cast<uint64_t>((kLBO >> 4) & 0x3FFFu) << 16;
+    d |= static_cast<uint64_t>((sbo >> 4) & 0x3FFFu) << 32;
+    d |= static_cast<uint64_t>(1u) << 46;
+    return d;
+}
+
 // Instruction descriptor for kind::tf32: D = F32, A = B = TF32, both K-major.
 // bits [4,6) D format (1 = F32), [7,10) A format (2 = TF32), [10,13) B format,
 // [15] A major (0 = K), [16] B major, [17,23) N >> 3, [24,29) M >> 4.

@@ -86,6 +86,8 @@ SIGNATURES = {
     "dgtd_op_unpack": (C.c_int, [_P, _P, _P, _P]),
     "dgtd_op_step": (C.c_int, [_P, _P, C.c_double, C.c_double, C.c_int32, C.c_int32, _P]),
     "dgtd_op_run_host": (C.c_int, [_P, _D, C.c_double, C.c_double, C.c_double, C.c_int32, _I64]),
+    "dgtd_op_step_noalloc": (C.c_int, [_P, _P, C.c_double, C.c_double, C.c_int32, C.c_int32, _P]),
+    "dgtd_noalloc_max_state": (C.c_int64, []),
     "dgtd_op_norm2": (C.c_int, [_P, _P, _D, _P]),
     "dgtd_op_set_contraction": (C.c_int, [_P, C.c_int32]),
     "dgtd_op_uses_tensor_cores": (C.c_int, [_P]),
@@ -117,6 +119,11 @@ def lib() -> C.CDLL:
 def kernel_launches() -> int:
     """Kernels launched by the CUDA library in this process so far."""
     return int(lib().dgtd_kernel_launches())
+
+
+def noalloc_max_state() -> int:
+    """Largest reference-layout state (6*K*Np*B entries) Operator.step_noalloc accepts."""
+    return int(lib().dgtd_noalloc_max_state())
 
 
 def _check(rc: int, what: str) -> None:
@@ -342,6 +349,12 @@ class Operator:
     def step(self, state, t0: float, dt: float, nsteps: int, integrator: int = RK4, stream=None) -> None:
         _check(lib().dgtd_op_step(self._h, _ptr(state), float(t0), float(dt), int(nsteps), int(integrator),
                                   _stream(stream)), "dgtd_op_step")
+
+    def step_noalloc(self, state, t0: float, dt: float, nsteps: int, integrator: int = RK4, stream=None) -> None:
+        """FP64 form: dgtd_op_step with the RK registers in the library's fixed device
+        scratch (no device allocation; calls overlapping on the GPU race)."""
+        _check(lib().dgtd_op_step_noalloc(self._h, _ptr(state), float(t0), float(dt), int(nsteps), int(integrator),
+                                          _stream(stream)), "dgtd_op_step_noalloc")
 
     def set_contraction(self, mode: int) -> None:
         """FP32 batched form: 0 = tensor cores (tcgen05 3xTF32) where supported, 1 = FP32 SIMT."""

@@ -6,6 +6,7 @@
 #include <cmath>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -658,6 +659,124 @@ int dgtd_ref_tet(int32_t order, double* r, double* s, double* t, double* Dr, dou
         if (fmask) for (size_t i = 0; i < T.Fmask.size(); ++i) fmask[i] = T.Fmask[i];
     } catch (const std::exception& e) {
         return fail(DGTD_ERR_INVALID, e.what());
+    }
+    return DGTD_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Stepping without device allocation.
+//
+// dgtd_op_step allocates its three RK registers with cudaMalloc on first use.
+// Some callers cannot allow that: a host that has reserved all device memory
+// up front for its own pool, or a caller on a path where a cudaMalloc would
+// synchronise the device and stall other streams. dgtd_op_step_noalloc runs the
+// same fused stage kernels with the registers in one file-scope device array
+// of fixed size instead, so the call itself allocates nothing.
+//
+// The array is shared by every operator and every call in the process and
+// keeps the last call's contents; the parts that must start at zero (the
+// LSERK4 residual) are cleared by each call. Calls that overlap on the GPU
+// (two streams, or two host threads) use the same registers and race.
+namespace {
+
+// Largest reference-layout state (6 * K * Np * B entries) the scratch holds.
+constexpr int64_t kNoAllocMaxState = int64_t(1) << 20;
+// Three RK registers of FP64 state: 24 MiB.
+static __device__ __align__(256) double g_noalloc_scratch[3 * kNoAllocMaxState];
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+double* g_noalloc_ptr[kNoAllocMaxDevices] = {};
+
+// Address of the scratch array on the current device; looked up once per device
+// (the first call on each device does this set-up).
+double* noalloc_scratch()
+{
+    int dev = -1;
+    ck(cudaGetDevice(&dev), "cudaGetDevice");
+    if (dev < 0 || dev >= kNoAllocMaxDevices) throw CudaError("device ordinal out of range for the no-allocation scratch");
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_ptr[dev]) {
+        double* ptr = nullptr;
+        ck(cudaGetSymbolAddress(reinterpret_cast<void**>(&ptr), g_noalloc_scratch), "cudaGetSymbolAddress");
+        g_noalloc_ptr[dev] = ptr;
+    }
+    return g_noalloc_ptr[dev];
+}
+
+// One RK step with the registers at ws (3 * state_len doubles); the same stage
+// sequence as rk_step.
+void rk_step_at(dgtd_op* op, double* ws, double* d_x, double t, double dt, int integrator, double* lsrk_other,
+                double*& cur, cudaStream_t s)
+{
+    const int64_t L = op->state_len;
+    if (integrator == DGTD_RK4) {
+        double* y0 = ws;
+        double* y1 = ws + L;
+        double* z = ws + 2 * L;
+        dgtd::StageArgs A{};
+        A.dt = dt;
+        A.x = d_x;
+        A.z = z;
+        A.mode = dgtd::MODE_RK4_1; A.in = d_x; A.yout = y0; run_stage(op, A, t, s);
+        A.mode = dgtd::MODE_RK4_2; A.in = y0; A.yout = y1; run_stage(op, A, t + dt / 2, s);
+        A.mode = dgtd::MODE_RK4_3; A.in = y1; A.yout = y0; run_stage(op, A, t + dt / 2, s);
+        A.mode = dgtd::MODE_RK4_4; A.in = y0; A.yout = nullptr; run_stage(op, A, t + dt, s);
+    } else {
+        double* res = ws + 2 * L;
+        for (int st = 0; st < 5; ++st) {
+            double* nxt = (cur == d_x) ? lsrk_other : d_x;
+            dgtd::StageArgs A{};
+            A.dt = dt;
+            A.mode = dgtd::MODE_LSRK;
+            A.in = cur;
+            A.yout = nxt;
+            A.res = res;
+            A.a = kRk4a[st];
+            A.b = kRk4b[st];
+            run_stage(op, A, t + kRk4c[st] * dt, s);
+            cur = nxt;
+        }
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int64_t dgtd_noalloc_max_state(void) { return kNoAllocMaxState; }
+
+int dgtd_op_step_noalloc(dgtd_op* op, void* d_state, double t0, double dt, int32_t nsteps, int32_t integrator,
+                         void* stream)
+{
+    if (!op || !d_state) return fail(DGTD_ERR_INVALID, "NULL argument");
+    if (nsteps < 0) return fail(DGTD_ERR_INVALID, "nsteps must be >= 0");
+    if (integrator != DGTD_RK4 && integrator != DGTD_LSERK4) return fail(DGTD_ERR_INVALID, "unknown integrator");
+    if (op->batched)
+        return fail(DGTD_ERR_UNSUPPORTED, "dgtd_op_step_noalloc supports the FP64 form only");
+    if (op->state_len > kNoAllocMaxState)
+        return fail(DGTD_ERR_INVALID, "dgtd_op_step_noalloc: state of " + std::to_string(op->state_len) +
+                                          " entries exceeds the fixed scratch limit of " +
+                                          std::to_string(kNoAllocMaxState) + " entries (6*K*Np*B)");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    try {
+        double* ws = noalloc_scratch();
+        double* state = static_cast<double*>(d_state);
+        double* other = ws;   // LSERK4 second state buffer
+        double* cur = state;
+        if (integrator == DGTD_LSERK4)
+            ck(cudaMemsetAsync(ws + 2 * op->state_len, 0, op->state_len * sizeof(double), s), "memset");
+        double t = t0;
+        for (int i = 0; i < nsteps; ++i) {
+            rk_step_at(op, ws, state, t, dt, integrator, other, cur, s);
+            t += dt;
+        }
+        if (integrator == DGTD_LSERK4 && cur != state)
+            ck(cudaMemcpyAsync(state, cur, op->state_len * sizeof(double), cudaMemcpyDeviceToDevice, s), "copy");
+    } catch (const std::exception& e) {
+        return fail(DGTD_ERR_CUDA, e.what());
     }
     return DGTD_OK;
 }

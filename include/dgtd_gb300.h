@@ -160,6 +160,20 @@ int dgtd_op_step(dgtd_op* op, void* d_state, double t0, double dt, int32_t nstep
 int dgtd_op_run_host(dgtd_op* op, double* h_state, double t0, double dt, double final_time, int32_t integrator,
                      int64_t* steps_out);
 
+/* Same as dgtd_op_step on the FP64 form, but allocating nothing: the three RK
+ * registers live in one fixed file-scope device array of 3 * dgtd_noalloc_max_state()
+ * doubles (24 MiB), shared by all operators and calls in the process. No counterpart
+ * in the reference; it serves callers that cannot allow a device allocation during
+ * stepping. The first call on each device looks up the array's address (set-up: make
+ * that call before any stream capture). Errors: DGTD_ERR_INVALID when state_len
+ * exceeds dgtd_noalloc_max_state(), DGTD_ERR_UNSUPPORTED for the FP32 batched form.
+ * The array keeps the last call's contents; calls that overlap on the GPU race. */
+int dgtd_op_step_noalloc(dgtd_op* op, void* d_state, double t0, double dt, int32_t nsteps, int32_t integrator,
+                         void* stream);
+
+/* Largest state_len (reference-layout entries) dgtd_op_step_noalloc accepts. */
+int64_t dgtd_noalloc_max_state(void);
+
 /* Contraction path of the FP32 batched form: 0 = tensor cores (tcgen05, 3xTF32) where
  * supported (orders 1..4, B padded to a multiple of 64), else FP32 SIMT; 1 = FP32 SIMT. */
 int dgtd_op_set_contraction(dgtd_op* op, int32_t mode);

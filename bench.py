@@ -375,7 +375,7 @@ def run_ours(args, world, rank, local):
     achieved_gbs = alg_bytes_launch / avg_launch_s / 1e9
     flops_per_dof_step = 4 * (6 * Np + 8 * nfp)          # contraction terms, FMA = 2
     achieved_tflops = flops_per_dof_step * dofs / (total_s / args.steps) / 1e12
-    kname = "stage_fp64" if prec == dg.FP64 else "stage_f32"
+    kname = "stage_fp64" if prec == dg.FP64 else ("stage_tc" if op.uses_tensor_cores else "stage_f32")
     traffic = profile_traffic(kname, args.workload)
     roofline = {"bound": "hbm", "achieved": round(achieved_gbs, 2), "peak": peaks["hbm_gbs"], "unit": "GB/s",
                 "frac": round(achieved_gbs / peaks["hbm_gbs"], 4), "traffic": traffic,
@@ -409,6 +409,104 @@ def run_ours(args, world, rank, local):
     return res
 
 
+# ----------------------------------------------------------------------------- serving
+SERVING_DESC = ("Serving stream (reduced C5): Poisson arrivals; each request a box [-1,1]^3 of n^3 hexes x 6 tets, "
+                "n ~ U{4..12}, central PEC cube of round(n/6) hexes (n >= 5), SMA outer boundary, TF/SF box one cell "
+                "in, order p ~ U{2..5}, one Gaussian plane wave (spread 0.1, delay 0.5) with random direction and "
+                "orthogonal polarisation, final time T ~ U[0.5, 1.5], dt from the reference 3D estimator at cfl=1; "
+                "plain FP64 operator, classical RK4; seed 20261206")
+
+
+def serving_requests(n_req: int, rate: float, seed: int = 20261206):
+    import dgtd_gb300 as dg
+    rng = np.random.default_rng(seed)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, n_req))
+    reqs = []
+    for _ in range(n_req):
+        n = int(rng.integers(4, 13))
+        p = int(rng.integers(2, 6))
+        T = float(rng.uniform(0.5, 1.5))
+        k = rng.standard_normal(3); k /= np.linalg.norm(k)
+        g = rng.standard_normal(3); pol = g - g.dot(k) * k; pol /= np.linalg.norm(pol)
+        hole = None
+        if n >= 5:
+            c = max(1, int(np.floor(n / 6 + 0.5)))
+            lo = (n - c) // 2
+            hole = ((lo,) * 3, (lo + c,) * 3)
+        m = dg.box_mesh((n, n, n), lo=(-1, -1, -1), hi=(1, 1, 1), hole=hole, tfsf=((1,) * 3, (n - 1,) * 3),
+                        outer_bc=dg.BC_SMA, hole_bc=dg.BC_PEC)
+        reqs.append(dict(mesh=m, order=p, final_time=T, n=n,
+                         waves=[dict(propagation=k, polarization=pol, spread=0.1, mean=-0.5)]))
+    return reqs, arrivals
+
+
+def run_serving(n_req: int, rate: float, serial_sample: int, device: int) -> dict:
+    """Continuous-batching run of a request stream through dgtd_server_*, with time-to-solution
+    per request (submit -> result on the host), and a serial sample of the same requests through
+    the single-operator path for comparison."""
+    import dgtd_gb300 as dg
+    reqs, arrivals = serving_requests(n_req, rate)
+    free, total = 0, 0
+    try:
+        import torch
+        free, total = torch.cuda.mem_get_info(device)
+    except Exception:
+        pass
+    budget = int(min(24 << 30, max(1 << 30, free // 4)))
+    with dg.Server(memory_budget=budget, max_active=64, steps_per_round=4, device=device) as srv:
+        w = srv.submit(reqs[0]["mesh"], reqs[0]["order"], 0.05, waves=reqs[0]["waves"], cfl=1.0)   # warm-up
+        srv.wait(w, timeout=600, want_state=False)
+        base = srv.stats()
+        ids = [None] * n_req
+        t0 = time.perf_counter()
+
+        def feeder():
+            for i, r in enumerate(reqs):
+                d = t0 + arrivals[i] - time.perf_counter()
+                if d > 0:
+                    time.sleep(d)
+                ids[i] = srv.submit(r["mesh"], r["order"], r["final_time"], waves=r["waves"], cfl=1.0)
+
+        th = threading.Thread(target=feeder)
+        th.start()
+        th.join()
+        stats = []
+        for i in range(n_req):
+            _, st = srv.wait(ids[i], timeout=3600, want_state=False)
+            stats.append(st)
+        wall = time.perf_counter() - t0
+        end = srv.stats()
+    tts = np.array([s["t_done"] - s["t_submit"] for s in stats])
+    first = min(s["t_submit"] for s in stats)
+    last = max(s["t_done"] for s in stats)
+    span = last - first
+    dof = end["dof_updates"] - base["dof_updates"]
+    launches = end["stage_launches"] - base["stage_launches"]
+    packed = end["slot_stage_updates"] - base["slot_stage_updates"]
+    out = {"requests": n_req, "arrival_rate_per_s": rate, "solves_per_s": n_req / span,
+           "p50_time_to_solution_s": float(np.percentile(tts, 50)), "p99_time_to_solution_s": float(np.percentile(tts, 99)),
+           "mean_time_to_solution_s": float(tts.mean()), "makespan_s": span, "wall_s": wall,
+           "dof_updates_per_s": dof / span, "stage_launches": launches,
+           "requests_per_stage_launch": packed / max(1, launches), "max_active": end["max_active_seen"],
+           "peak_device_bytes": end["peak_bytes_in_use"], "memory_budget": budget, "failed": end["failed"] - base["failed"],
+           "precision": "fp64 (plain form; bit-identical alone and in the mix, tests/test_gpu_serve.py)",
+           "workload": SERVING_DESC}
+    if serial_sample > 0:
+        # the same first requests one at a time through the single-operator path (one solve per call)
+        t1 = time.perf_counter()
+        for r in reqs[:serial_sample]:
+            op = dg.Operator(r["mesh"], order=r["order"])
+            op.set_planewaves(r["waves"])
+            op.run_host(np.zeros(op.state_len), 0.0, op.estimate_dt(1.0), r["final_time"])
+            op.close()
+        ser = time.perf_counter() - t1
+        mix_sample = sum(s["t_done"] - s["t_submit"] for s in stats[:serial_sample])
+        out["serial_sample"] = {"requests": serial_sample, "seconds": ser, "solves_per_s": serial_sample / ser,
+                                "path": "dgtd_op_run_host, one request at a time"}
+        del mix_sample
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -420,6 +518,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64-compare", action="store_true")
     ap.add_argument("--fp64-steps", type=int, default=3)
+    ap.add_argument("--serving-requests", type=int, default=64, help="requests of the serving stream (0: skip)")
+    ap.add_argument("--serving-rate", type=float, default=4.0, help="Poisson arrival rate of the serving stream (1/s)")
+    ap.add_argument("--serving-serial", type=int, default=8, help="requests also run one at a time for comparison")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -472,6 +573,8 @@ def main():
         line["plain_fp64"] = r["plain_fp64"]
     if "accuracy" in r:
         line["accuracy"] = r["accuracy"]
+    if args.serving_requests > 0 and world == 1:
+        line["serving"] = run_serving(args.serving_requests, args.serving_rate, args.serving_serial, local)
     print(json.dumps(line), flush=True)
 
 

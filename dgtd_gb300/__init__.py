@@ -25,7 +25,11 @@ RK4, LSERK4 = 0, 1
 
 
 class DgtdError(RuntimeError):
-    pass
+    """A C-ABI call returned an error status (``code``: the DGTD_ERR_* value)."""
+
+    def __init__(self, msg: str, code: int = 0):
+        super().__init__(msg)
+        self.code = code
 
 
 class MeshDesc(C.Structure):
@@ -64,6 +68,34 @@ class BoxSpec(C.Structure):
                 ("outer_bc", C.c_int32), ("hole_bc", C.c_int32)]
 
 
+class ServerOpts(C.Structure):
+    _fields_ = [("memory_budget", C.c_int64), ("max_active", C.c_int32), ("steps_per_round", C.c_int32),
+                ("device", C.c_int32)]
+
+
+class Request(C.Structure):
+    _fields_ = [("mesh", C.POINTER(MeshDesc)), ("order", C.c_int32), ("alpha", C.c_double),
+                ("waves", C.POINTER(PlaneWave)), ("n_waves", C.c_int32), ("h_init", C.POINTER(C.c_double)),
+                ("t0", C.c_double), ("final_time", C.c_double), ("dt", C.c_double), ("cfl", C.c_double)]
+
+
+class RequestStats(C.Structure):
+    _fields_ = [("status", C.c_int32), ("order", C.c_int32), ("n_elements", C.c_int64), ("state_len", C.c_int64),
+                ("steps", C.c_int64), ("region_bytes", C.c_int64), ("dt", C.c_double), ("t_submit", C.c_double),
+                ("t_admit", C.c_double), ("t_first_launch", C.c_double), ("t_done", C.c_double)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_int64), ("completed", C.c_int64), ("failed", C.c_int64), ("active", C.c_int64),
+                ("queued", C.c_int64), ("stage_launches", C.c_int64), ("slot_stage_updates", C.c_int64),
+                ("max_active_seen", C.c_int64), ("bytes_in_use", C.c_int64), ("peak_bytes_in_use", C.c_int64),
+                ("memory_budget", C.c_int64), ("dof_updates", C.c_int64)]
+
+
+REQ_QUEUED, REQ_ACTIVE, REQ_DONE, REQ_FAILED = 0, 1, 2, 3
+SERVER_MAX_ACTIVE = 128
+DGTD_ERR_TIMEOUT = -5
+
 _lib_handle: Optional[C.CDLL] = None
 
 # Every symbol the C ABI declares, with (restype, argtypes).
@@ -98,6 +130,17 @@ SIGNATURES = {
     "dgtd_ref_tet": (C.c_int, [C.c_int32, _D, _D, _D, _D, _D, _D, _D, _D, _I32]),
     "dgtd_mesh_validate": (C.c_int, [C.POINTER(MeshDesc), C.POINTER(OpOpts), C.POINTER(OpInfo)]),
     "dgtd_tc_selftest": (C.c_int, [_D_F, _D_F, _D_F, C.c_int32, _I32]),
+    "dgtd_server_create": (C.c_int, [C.POINTER(ServerOpts), C.POINTER(_P)]),
+    "dgtd_server_destroy": (None, [_P]),
+    "dgtd_server_submit": (C.c_int, [_P, C.POINTER(Request), _I64]),
+    "dgtd_server_wait": (C.c_int, [_P, C.c_int64, C.c_double, _D, C.POINTER(RequestStats)]),
+    "dgtd_server_query": (C.c_int, [_P, C.c_int64, C.POINTER(RequestStats)]),
+    "dgtd_server_get_stats": (C.c_int, [_P, C.POINTER(ServerStats)]),
+    "dgtd_arena_create": (C.c_int, [C.c_int64, C.c_int64, C.POINTER(_P)]),
+    "dgtd_arena_destroy": (None, [_P]),
+    "dgtd_arena_alloc": (C.c_int64, [_P, C.c_int64]),
+    "dgtd_arena_release": (C.c_int, [_P, C.c_int64]),
+    "dgtd_arena_usage": (C.c_int, [_P, _I64, _I64, _I64]),
 }
 
 
@@ -129,7 +172,17 @@ def noalloc_max_state() -> int:
 def _check(rc: int, what: str) -> None:
     if rc != DGTD_OK:
         msg = lib().dgtd_last_error().decode(errors="replace")
-        raise DgtdError(f"{what} failed ({rc}): {msg}")
+        raise DgtdError(f"{what} failed ({rc}): {msg}", rc)
+
+
+def _waves_array(waves: Sequence[dict]):
+    arr = (PlaneWave * max(1, len(waves)))()
+    for i, w in enumerate(waves):
+        arr[i].propagation[:] = list(map(float, w["propagation"]))
+        arr[i].polarization[:] = list(map(float, w["polarization"]))
+        arr[i].spread = float(w["spread"]); arr[i].mean = float(w["mean"])
+        arr[i].frequency = float(w.get("frequency", 0.0)); arr[i].batch = int(w.get("batch", 0))
+    return arr
 
 
 def _dp(a: np.ndarray):
@@ -329,13 +382,7 @@ class Operator:
         return xyz
 
     def set_planewaves(self, waves: Sequence[dict]) -> None:
-        arr = (PlaneWave * max(1, len(waves)))()
-        for i, w in enumerate(waves):
-            arr[i].propagation[:] = list(map(float, w["propagation"]))
-            arr[i].polarization[:] = list(map(float, w["polarization"]))
-            arr[i].spread = float(w["spread"]); arr[i].mean = float(w["mean"])
-            arr[i].frequency = float(w.get("frequency", 0.0)); arr[i].batch = int(w.get("batch", 0))
-        _check(lib().dgtd_op_set_planewaves(self._h, arr, len(waves)), "set_planewaves")
+        _check(lib().dgtd_op_set_planewaves(self._h, _waves_array(waves), len(waves)), "set_planewaves")
 
     def estimate_dt(self, cfl: float = 1.0) -> float:
         v = C.c_double()
@@ -386,3 +433,104 @@ class Operator:
         _check(lib().dgtd_op_run_host(self._h, _dp(x), float(t0), float(dt), float(final_time), int(integrator),
                                       C.byref(n)), "dgtd_op_run_host")
         return x, int(n.value)
+
+
+class Server:
+    """Continuous-batching server of independent solves (C ABI ``dgtd_server_*``).
+
+    Each request is one ``Solver::run`` of its own mesh, order, plane waves and
+    final time (plain FP64 operator, classical RK4). ``submit`` returns at once;
+    ``wait`` returns the final state (reference layout) and the request's timing.
+    """
+
+    def __init__(self, memory_budget: int = 4 << 30, max_active: int = 64, steps_per_round: int = 4, device: int = 0):
+        o = ServerOpts(memory_budget=int(memory_budget), max_active=int(max_active),
+                       steps_per_round=int(steps_per_round), device=int(device))
+        h = C.c_void_p()
+        _check(lib().dgtd_server_create(C.byref(o), C.byref(h)), "dgtd_server_create")
+        self._h = h
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) and self._h.value:
+            lib().dgtd_server_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, mesh: Mesh, order: int, final_time: float, waves: Sequence[dict] = (), init=None,
+               dt: float = 0.0, cfl: float = 1.0, alpha: float = 1.0, t0: float = 0.0) -> int:
+        m = mesh.normalized()
+        d = _mesh_desc(m)
+        arr = _waves_array(waves)
+        q = Request()
+        q.mesh = C.pointer(d)
+        q.order = int(order); q.alpha = float(alpha)
+        q.waves = arr; q.n_waves = len(waves)
+        keep = None
+        if init is not None:
+            keep = np.ascontiguousarray(init, dtype=np.float64)
+            q.h_init = _dp(keep)
+        q.t0 = float(t0); q.final_time = float(final_time); q.dt = float(dt); q.cfl = float(cfl)
+        rid = C.c_int64()
+        _check(lib().dgtd_server_submit(self._h, C.byref(q), C.byref(rid)), "dgtd_server_submit")
+        return int(rid.value)
+
+    def wait(self, rid: int, timeout: float = -1.0, want_state: bool = True):
+        """(final state in the reference layout or None, stats dict) of a request, which is then
+        released. Raises DgtdError (code -5 when the timeout expires, the request stays pending)."""
+        st = RequestStats()
+        out = None
+        if want_state:
+            _check(lib().dgtd_server_query(self._h, int(rid), C.byref(st)), "dgtd_server_query")
+            out = np.zeros(int(st.state_len))
+        _check(lib().dgtd_server_wait(self._h, int(rid), float(timeout), _dp(out) if out is not None else None,
+                                      C.byref(st)), "dgtd_server_wait")
+        return out, {k: getattr(st, k) for k, _ in RequestStats._fields_}
+
+    def query(self, rid: int) -> dict:
+        st = RequestStats()
+        _check(lib().dgtd_server_query(self._h, int(rid), C.byref(st)), "dgtd_server_query")
+        return {k: getattr(st, k) for k, _ in RequestStats._fields_}
+
+    def stats(self) -> dict:
+        st = ServerStats()
+        _check(lib().dgtd_server_get_stats(self._h, C.byref(st)), "dgtd_server_get_stats")
+        return {k: getattr(st, k) for k, _ in ServerStats._fields_}
+
+
+class Arena:
+    """Host-side first-fit range allocator the server uses for its device budget."""
+
+    def __init__(self, capacity: int, align: int = 256):
+        h = C.c_void_p()
+        _check(lib().dgtd_arena_create(int(capacity), int(align), C.byref(h)), "dgtd_arena_create")
+        self._h = h
+
+    def alloc(self, nbytes: int) -> int:
+        return int(lib().dgtd_arena_alloc(self._h, int(nbytes)))
+
+    def release(self, off: int) -> None:
+        _check(lib().dgtd_arena_release(self._h, int(off)), "dgtd_arena_release")
+
+    def usage(self) -> dict:
+        a, b, c = C.c_int64(), C.c_int64(), C.c_int64()
+        _check(lib().dgtd_arena_usage(self._h, C.byref(a), C.byref(b), C.byref(c)), "dgtd_arena_usage")
+        return {"in_use": a.value, "largest_free": b.value, "n_free_ranges": c.value}
+
+    def __del__(self):
+        try:
+            if self._h.value:
+                lib().dgtd_arena_destroy(self._h)
+                self._h = C.c_void_p()
+        except Exception:
+            pass

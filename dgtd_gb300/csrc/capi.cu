@@ -28,6 +28,15 @@ int fail(int code, const std::string& msg)
     return code;
 }
 
+}  // namespace
+
+namespace dgtd {
+// Records the thread-local message dgtd_last_error() returns (also used by serve.cu).
+int set_last_error(int code, const std::string& msg) { return fail(code, msg); }
+}  // namespace dgtd
+
+namespace {
+
 struct CudaError : std::runtime_error {
     using std::runtime_error::runtime_error;
 };

@@ -1,263 +1,27 @@
-// Plain FP64 form of the DG Maxwell step: one fused kernel per RK stage.
-//
-// Computes, per element (reference HesthavenEvolution::Mult,
-// src/evolution/HesthavenEvolution.cpp:450-541, with the material scaling and
-// boundary coefficients of the assembled operator, src/components/DGOperatorFactory.h:21-45,
-// 413-424, 1061-1208):
-//   dE/dt = (1/eps) [ curl H + LIFT (Fscale/2 * fluxE) ] - (sigma/eps) E
-//   dH/dt = (1/mu)  [-curl E + LIFT (Fscale/2 * fluxH) ]
-//   fluxE = n x dH + aE (dE - n (n.dE)),  fluxH = -n x dE + aH (dH - n (n.dH)),
-// with d = u(neighbour) - u(own) and the boundary / TF-SF rules applied to d.
-// The epilogue fuses the classical RK4 register updates of mfem::RK4Solver
-// (called from src/solver/Solver.cpp:544) or a low-storage RK stage.
-//
-// Layout in HBM (reference src/evolution/Fields.h:48-65): state[b][c][e*Np+i],
-// c = Ex,Ey,Ez,Hx,Hy,Hz; elements contiguous inside each component, so a block
-// of consecutive elements reads six contiguous runs.
-//
-// The GB300 FP64 pipe is ~1.25 TFLOP/s, so this form is FP64-issue bound
-// (arithmetic intensity ~6 flop/B >> ridge): the kernel is organised to keep
-// the FP64 pipe fed (shared-memory broadcast of the element's fields,
-// coalesced transposed operator rows from L1/L2) rather than to save bytes.
-#include <cmath>
-
-#include "kernels.hpp"
+// Plain FP64 form of the DG Maxwell step: one fused kernel per RK stage over
+// one operator's mesh (grid: element blocks x incidences), plus the TF/SF
+// skip test and the per-incidence norm. The stage arithmetic (reference
+// HesthavenEvolution::Mult, src/evolution/HesthavenEvolution.cpp:450-541, with
+// the RK4 register updates of mfem::RK4Solver, src/solver/Solver.cpp:544) is
+// in fp64_stage.cuh.
+#include "fp64_stage.cuh"
 
 namespace dgtd {
 
 namespace {
 
-constexpr int kBlock = 256;
-
-template <int P>
-struct Ord {
-    static constexpr int Np = (P + 1) * (P + 2) * (P + 3) / 6;
-    static constexpr int Nfp = (P + 1) * (P + 2) / 2;
-    static constexpr int NF = 4 * Nfp;
-    // elements per block: fill 256 threads, capped so static shared memory stays below 48 KB
-    static constexpr int EPB0 = kBlock / Np > 0 ? kBlock / Np : 1;
-    static constexpr int EPB = EPB0 > 32 ? 32 : EPB0;
-};
-
-__device__ __forceinline__ double pw_profile(const PlaneWaveDev& w, double s)
-{
-    double a = s - w.mean;
-    double g = exp(-a * a / (2.0 * w.spread * w.spread));
-    if (w.freq != 0.0) g *= cos(2.0 * M_PI * w.freq * a);
-    return g;
-}
-
-// Sum of the plane waves of incidence b at point x and time t.
-__device__ __forceinline__ void eval_pw(const PlaneWaveDev* pw, int n_pw, int b, double px, double py, double pz,
-                                        double t, double* e, double* h)
-{
-    e[0] = e[1] = e[2] = h[0] = h[1] = h[2] = 0.0;
-    for (int q = 0; q < n_pw; ++q) {
-        const PlaneWaveDev& w = pw[q];
-        if (w.batch != b) continue;
-        double s = px * w.k[0] + py * w.k[1] + pz * w.k[2] - t;
-        double g = pw_profile(w, s);
-        e[0] += g * w.pol[0]; e[1] += g * w.pol[1]; e[2] += g * w.pol[2];
-        h[0] += g * w.kxp[0]; h[1] += g * w.kxp[1]; h[2] += g * w.kxp[2];
-    }
-}
+using fp64::Ord;
+using fp64::kBlock;
 
 template <int P>
 __global__ void __launch_bounds__(kBlock) stage_fp64(TablesDev T, StageArgs A)
 {
-    using O = Ord<P>;
-    constexpr int Np = O::Np, Nfp = O::Nfp, NF = O::NF, EPB = O::EPB;
-    __shared__ double s_u[6][EPB * Np];
-    __shared__ double s_f[6][EPB * NF];
-    __shared__ int s_fmask[4 * Nfp];
-
-    const int tid = threadIdx.x;
-    const int b = blockIdx.y;
-    const int64_t e0 = static_cast<int64_t>(blockIdx.x) * EPB;
-    const int64_t N = T.N;
-    const double* __restrict__ in = A.in + static_cast<int64_t>(b) * 6 * N;
-    const int nel = (T.K - e0) < EPB ? static_cast<int>(T.K - e0) : EPB;
-
-    for (int i = tid; i < 4 * Nfp; i += blockDim.x) s_fmask[i] = T.Fmask[i];
-    // coalesced load of the block's fields
-    for (int c = 0; c < 6; ++c)
-        for (int i = tid; i < nel * Np; i += blockDim.x) s_u[c][i] = in[c * N + e0 * Np + i];
-    __syncthreads();
-
-    // ---- face fluxes -----------------------------------------------------------
-    const bool skip_src = (A.skip != nullptr) && A.skip[b];
-    for (int w = tid; w < nel * NF; w += blockDim.x) {
-        const int el = w / NF, fn = w - el * NF, f = fn / Nfp, a = fn - f * Nfp;
-        const int64_t e = e0 + el;
-        const int vm = s_fmask[f * Nfp + a];
-        const int code = T.fcode[e * 4 + f];
-        const double* fg = T.fgeo + e * 16 + f * 4;
-        const double nx = fg[0], ny = fg[1], nz = fg[2], fs = fg[3];
-        double uM[6], dE[3], dH[3];
-#pragma unroll
-        for (int c = 0; c < 6; ++c) uM[c] = s_u[c][el * Np + vm];
-        double aE = T.alpha, aH = T.alpha;
-        if (code == 0 || code == 4 || code == 5) {
-            const int64_t gp = T.vmapP[(e * 4 + f) * Nfp + a];
-#pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                dE[c] = __ldg(in + c * N + gp) - uM[c];
-                dH[c] = __ldg(in + (c + 3) * N + gp) - uM[c + 3];
-            }
-            if (code != 0 && !skip_src) {
-                const int64_t gm = e * Np + vm;
-                double pe[3], ph[3];
-                eval_pw(A.pw, A.n_pw, b, T.xyz[gm], T.xyz[N + gm], T.xyz[2 * N + gm], A.t, pe, ph);
-                const double sg = (code == 4) ? 1.0 : -1.0;
-#pragma unroll
-                for (int c = 0; c < 3; ++c) { dE[c] += sg * pe[c]; dH[c] += sg * ph[c]; }
-            }
-        } else if (code == 1 || code == 6) {           // PEC
-#pragma unroll
-            for (int c = 0; c < 3; ++c) { dE[c] = -2.0 * uM[c]; dH[c] = 0.0; }
-        } else if (code == 2 || code == 7) {           // PMC
-#pragma unroll
-            for (int c = 0; c < 3; ++c) { dE[c] = 0.0; dH[c] = -2.0 * uM[c + 3]; }
-        } else if (code == 3 || code == 8) {           // SMA: penalty 1 regardless of alpha
-#pragma unroll
-            for (int c = 0; c < 3; ++c) { dE[c] = -uM[c]; dH[c] = -uM[c + 3]; }
-            aE = 1.0; aH = 1.0;
-        } else {                                        // open: zero jump
-#pragma unroll
-            for (int c = 0; c < 3; ++c) { dE[c] = 0.0; dH[c] = 0.0; }
-        }
-        const double ndE = nx * dE[0] + ny * dE[1] + nz * dE[2];
-        const double ndH = nx * dH[0] + ny * dH[1] + nz * dH[2];
-        const double h = 0.5 * fs;
-        const int o = el * NF + fn;
-        s_f[0][o] = h * ((ny * dH[2] - nz * dH[1]) + aE * (dE[0] - ndE * nx));
-        s_f[1][o] = h * ((nz * dH[0] - nx * dH[2]) + aE * (dE[1] - ndE * ny));
-        s_f[2][o] = h * ((nx * dH[1] - ny * dH[0]) + aE * (dE[2] - ndE * nz));
-        s_f[3][o] = h * (-(ny * dE[2] - nz * dE[1]) + aH * (dH[0] - ndH * nx));
-        s_f[4][o] = h * (-(nz * dE[0] - nx * dE[2]) + aH * (dH[1] - ndH * ny));
-        s_f[5][o] = h * (-(nx * dE[1] - ny * dE[0]) + aH * (dH[2] - ndH * nz));
-    }
-    __syncthreads();
-
-    // ---- volume terms + LIFT + epilogue ----------------------------------------
-    if (tid >= nel * Np) return;
-    const int el = tid / Np, i = tid - el * Np;
-    const int64_t e = e0 + el;
-    double ar[6], as[6], at[6];
-#pragma unroll
-    for (int c = 0; c < 6; ++c) { ar[c] = 0.0; as[c] = 0.0; at[c] = 0.0; }
-    const double* __restrict__ DrT = T.DrT;
-    const double* __restrict__ DsT = T.DsT;
-    const double* __restrict__ DtT = T.DtT;
-#pragma unroll 4
-    for (int j = 0; j < Np; ++j) {
-        const double dr = __ldg(DrT + j * Np + i), ds = __ldg(DsT + j * Np + i), dt = __ldg(DtT + j * Np + i);
-#pragma unroll
-        for (int c = 0; c < 6; ++c) {
-            const double u = s_u[c][el * Np + j];
-            ar[c] = fma(dr, u, ar[c]);
-            as[c] = fma(ds, u, as[c]);
-            at[c] = fma(dt, u, at[c]);
-        }
-    }
-    double lf[6];
-#pragma unroll
-    for (int c = 0; c < 6; ++c) lf[c] = 0.0;
-    const double* __restrict__ LT = T.LIFTT;
-#pragma unroll 4
-    for (int m = 0; m < NF; ++m) {
-        const double L = __ldg(LT + m * Np + i);
-#pragma unroll
-        for (int c = 0; c < 6; ++c) lf[c] = fma(L, s_f[c][el * NF + m], lf[c]);
-    }
-    const double* g = T.geo + e * 9;
-    const double rx = g[0], ry = g[1], rz = g[2], sx = g[3], sy = g[4], sz = g[5], tx = g[6], ty = g[7], tz = g[8];
-    auto dx = [&](int c) { return rx * ar[c] + sx * as[c] + tx * at[c]; };
-    auto dy = [&](int c) { return ry * ar[c] + sy * as[c] + ty * at[c]; };
-    auto dz = [&](int c) { return rz * ar[c] + sz * as[c] + tz * at[c]; };
-    const double curlHx = dy(5) - dz(4), curlHy = dz(3) - dx(5), curlHz = dx(4) - dy(3);
-    const double curlEx = dy(2) - dz(1), curlEy = dz(0) - dx(2), curlEz = dx(1) - dy(0);
-    const double* mt = T.mat + e * 3;
-    const double ie = mt[0], im = mt[1], se = mt[2];
-    double k[6];
-    k[0] = ie * (curlHx + lf[0]) - se * s_u[0][tid];
-    k[1] = ie * (curlHy + lf[1]) - se * s_u[1][tid];
-    k[2] = ie * (curlHz + lf[2]) - se * s_u[2][tid];
-    k[3] = im * (-curlEx + lf[3]);
-    k[4] = im * (-curlEy + lf[4]);
-    k[5] = im * (-curlEz + lf[5]);
-
-    const int64_t base = static_cast<int64_t>(b) * 6 * N + e * Np + i;
-    const double dt = A.dt;
-    switch (A.mode) {
-    case MODE_MULT:
-#pragma unroll
-        for (int c = 0; c < 6; ++c) A.out[base + c * N] = k[c];
-        break;
-    case MODE_RK4_1:
-#pragma unroll
-        for (int c = 0; c < 6; ++c) {
-            const double xv = s_u[c][tid];
-            A.yout[base + c * N] = xv + 0.5 * dt * k[c];
-            A.z[base + c * N] = xv + (dt / 6.0) * k[c];
-        }
-        break;
-    case MODE_RK4_2:
-#pragma unroll
-        for (int c = 0; c < 6; ++c) {
-            const double xv = A.x[base + c * N];
-            A.yout[base + c * N] = xv + 0.5 * dt * k[c];
-            A.z[base + c * N] += (dt / 3.0) * k[c];
-        }
-        break;
-    case MODE_RK4_3:
-#pragma unroll
-        for (int c = 0; c < 6; ++c) {
-            const double xv = A.x[base + c * N];
-            A.yout[base + c * N] = xv + dt * k[c];
-            A.z[base + c * N] += (dt / 3.0) * k[c];
-        }
-        break;
-    case MODE_RK4_4:
-#pragma unroll
-        for (int c = 0; c < 6; ++c) A.x[base + c * N] = A.z[base + c * N] + (dt / 6.0) * k[c];
-        break;
-    case MODE_LSRK:
-#pragma unroll
-        for (int c = 0; c < 6; ++c) {
-            const double r = A.a * A.res[base + c * N] + dt * k[c];
-            A.res[base + c * N] = r;
-            A.yout[base + c * N] = s_u[c][tid] + A.b * r;
-        }
-        break;
-    default:
-        break;
-    }
+    fp64::stage_body<P>(T, A, static_cast<int64_t>(blockIdx.x) * Ord<P>::EPB, static_cast<int>(blockIdx.y));
 }
 
 __global__ void tfsf_skip_kernel(TablesDev T, const PlaneWaveDev* pw, int n_pw, double t, int* skip)
 {
-    const int b = blockIdx.x;
-    const int64_t total = T.n_tfsf_elems * T.Np;
-    double acc = 0.0;
-    for (int64_t w = threadIdx.x; w < total; w += blockDim.x) {
-        const int64_t e = T.tfsf_elems[w / T.Np];
-        const int64_t gm = e * T.Np + (w % T.Np);
-        double pe[3], ph[3];
-        eval_pw(pw, n_pw, b, T.xyz[gm], T.xyz[T.N + gm], T.xyz[2 * T.N + gm], t, pe, ph);
-        for (int c = 0; c < 3; ++c) {
-            const double a = 0.5 * pe[c], h = 0.5 * ph[c];
-            acc += a * a + h * h;
-        }
-    }
-    __shared__ double red[256];
-    red[threadIdx.x] = acc;
-    __syncthreads();
-    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-        if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) skip[b] = (red[0] < 1e-16) ? 1 : 0;
+    fp64::tfsf_skip_body(T, pw, n_pw, static_cast<int>(blockIdx.x), t, skip + blockIdx.x);
 }
 
 __global__ void norm2_kernel(const double* in, int64_t n, double* out)

@@ -192,6 +192,100 @@ int dgtd_op_norm2(dgtd_op* op, const void* d_state, double* h_out, void* stream)
  * (estimateTimeStep, Solver.cpp:289-300, 349-351) at the given cfl. */
 int dgtd_op_estimate_dt(const dgtd_op* op, double cfl, double* dt_out);
 
+/* ---- serving: continuous batching of independent solves ------------------------
+ *
+ * The reference runs one case per process (driver::buildSolverJson +
+ * Solver::run, src/driver/driver.cpp:1545, src/solver/Solver.cpp:483-533). The
+ * server runs many such solves at once on one GPU: each request is one
+ * Solver::run of its own mesh, order, plane wave and final time, with the
+ * plain FP64 operator and classical RK4 (the same arithmetic as dgtd_op_step,
+ * so a result is bit-identical alone and in the mix). Requests are admitted as
+ * device memory (a fixed budget, allocated once when the server starts) and
+ * slots free up; every active request of one order advances in the same
+ * kernel launches. Three host threads: admission (mesh tables, memory
+ * reservation, upload), engine (launches), retirement (result download). */
+
+#define DGTD_SERVER_MAX_ACTIVE 128
+
+#define DGTD_REQ_QUEUED 0   /* submitted, waiting for memory */
+#define DGTD_REQ_ACTIVE 1   /* uploaded / stepping */
+#define DGTD_REQ_DONE 2
+#define DGTD_REQ_FAILED 3
+
+typedef struct dgtd_server dgtd_server;
+
+typedef struct dgtd_server_opts {
+    int64_t memory_budget;    /* device bytes for request regions, allocated at create (> 0) */
+    int32_t max_active;       /* requests stepping at once, 1..DGTD_SERVER_MAX_ACTIVE */
+    int32_t steps_per_round;  /* steps per active request between admission checks (>= 1) */
+    int32_t device;           /* CUDA device ordinal */
+} dgtd_server_opts;
+
+typedef struct dgtd_request {
+    const dgtd_mesh_desc* mesh;     /* copied by dgtd_server_submit */
+    int32_t order;                  /* 1..6 */
+    double alpha;                   /* upwind coefficient */
+    const dgtd_planewave* waves;    /* batch index must be 0; may be NULL with n_waves = 0 */
+    int32_t n_waves;                /* <= 8 */
+    const double* h_init;           /* initial state, reference layout (6*K*Np); NULL = zero fields */
+    double t0;
+    double final_time;
+    double dt;                      /* > 0: step size; <= 0: dgtd_op_estimate_dt at cfl */
+    double cfl;
+} dgtd_request;
+
+typedef struct dgtd_request_stats {
+    int32_t status;        /* DGTD_REQ_* */
+    int32_t order;
+    int64_t n_elements;
+    int64_t state_len;     /* 6*K*Np */
+    int64_t steps;         /* RK4 steps taken */
+    int64_t region_bytes;  /* device bytes the request held */
+    double dt;
+    double t_submit;       /* seconds on the server clock (since create) */
+    double t_admit;        /* region reserved and uploaded */
+    double t_first_launch;
+    double t_done;         /* result on the host */
+} dgtd_request_stats;
+
+typedef struct dgtd_server_stats {
+    int64_t submitted, completed, failed;
+    int64_t active, queued;
+    int64_t stage_launches;        /* stage kernels launched */
+    int64_t slot_stage_updates;    /* sum over stage launches of the requests they advanced */
+    int64_t max_active_seen;
+    int64_t bytes_in_use, peak_bytes_in_use, memory_budget;
+    int64_t dof_updates;           /* sum over requests of 6*K*Np per step taken */
+} dgtd_server_stats;
+
+/* Start a server (allocates the memory budget on the device, starts its threads). */
+int dgtd_server_create(const dgtd_server_opts* opts, dgtd_server** out);
+/* Stop the threads, fail requests not yet done, release all memory. */
+void dgtd_server_destroy(dgtd_server* s);
+/* Queue a request (inputs are copied; returns at once). DGTD_ERR_INVALID for a
+ * malformed request; a request larger than the whole budget fails later with
+ * DGTD_REQ_FAILED. */
+int dgtd_server_submit(dgtd_server* s, const dgtd_request* req, int64_t* id_out);
+/* Wait up to timeout_s seconds (< 0: forever) for request `id`. On DGTD_OK the
+ * final state is copied to h_state (if not NULL; 6*K*Np doubles), *stats is
+ * filled (if not NULL) and the request is released. DGTD_ERR_TIMEOUT leaves it
+ * pending; a failed request returns DGTD_ERR_CUDA or DGTD_ERR_NOMEM with its
+ * message in dgtd_last_error() and is released. */
+int dgtd_server_wait(dgtd_server* s, int64_t id, double timeout_s, double* h_state, dgtd_request_stats* stats);
+/* Status of a request without waiting (stats->status). */
+int dgtd_server_query(dgtd_server* s, int64_t id, dgtd_request_stats* stats);
+int dgtd_server_get_stats(dgtd_server* s, dgtd_server_stats* out);
+
+/* Host-side range allocator the server carves request regions from (first fit,
+ * neighbours merged on release); exported so its bookkeeping can be tested
+ * without a GPU. */
+typedef struct dgtd_arena dgtd_arena;
+int dgtd_arena_create(int64_t capacity, int64_t align, dgtd_arena** out);
+void dgtd_arena_destroy(dgtd_arena* a);
+int64_t dgtd_arena_alloc(dgtd_arena* a, int64_t bytes);     /* offset, or -1 if no range fits */
+int dgtd_arena_release(dgtd_arena* a, int64_t offset);      /* DGTD_OK or DGTD_ERR_INVALID */
+int dgtd_arena_usage(const dgtd_arena* a, int64_t* in_use, int64_t* largest_free, int64_t* n_free_ranges);
+
 /* ---- host-only mesh helpers (no GPU needed) ---------------------------------- */
 
 /* Build the reference-element and mesh tables on the host only (the

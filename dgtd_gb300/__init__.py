@@ -68,6 +68,29 @@ class BoxSpec(C.Structure):
                 ("outer_bc", C.c_int32), ("hole_bc", C.c_int32)]
 
 
+class ProbeSpec(C.Structure):
+    _fields_ = [("n_points", C.c_int32), ("points", C.POINTER(C.c_double)), ("n_surface_faces", C.c_int64),
+                ("surface_faces", C.POINTER(C.c_int32)), ("n_freqs", C.c_int32), ("freqs", C.POINTER(C.c_double)),
+                ("every", C.c_int32), ("max_records", C.c_int32)]
+
+
+class CaseInfo(C.Structure):
+    _fields_ = [("order", C.c_int32), ("integrator", C.c_int32), ("alpha", C.c_double), ("time_step", C.c_double),
+                ("final_time", C.c_double), ("cfl", C.c_double), ("n_waves", C.c_int32),
+                ("n_initial_fields", C.c_int32), ("n_point_probes", C.c_int32), ("n_surfaces", C.c_int32),
+                ("n_elements", C.c_int64), ("n_vertices", C.c_int64)]
+
+
+class CaseRunOpts(C.Structure):
+    _fields_ = [("precision", C.c_int32), ("freqs", C.POINTER(C.c_double)), ("n_freqs", C.c_int32),
+                ("out_dir", C.c_char_p)]
+
+
+class CaseResult(C.Structure):
+    _fields_ = [("steps", C.c_int64), ("dt", C.c_double), ("final_time", C.c_double), ("n_records", C.c_int64),
+                ("seconds", C.c_double)]
+
+
 class ServerOpts(C.Structure):
     _fields_ = [("memory_budget", C.c_int64), ("max_active", C.c_int32), ("steps_per_round", C.c_int32),
                 ("device", C.c_int32)]
@@ -130,6 +153,22 @@ SIGNATURES = {
     "dgtd_ref_tet": (C.c_int, [C.c_int32, _D, _D, _D, _D, _D, _D, _D, _D, _I32]),
     "dgtd_mesh_validate": (C.c_int, [C.POINTER(MeshDesc), C.POINTER(OpOpts), C.POINTER(OpInfo)]),
     "dgtd_tc_selftest": (C.c_int, [_D_F, _D_F, _D_F, C.c_int32, _I32]),
+    "dgtd_op_set_probes": (C.c_int, [_P, C.POINTER(ProbeSpec)]),
+    "dgtd_op_clear_probes": (C.c_int, [_P]),
+    "dgtd_op_probe_reset": (C.c_int, [_P, _P]),
+    "dgtd_op_probe_info": (C.c_int, [_P, _I64, _I64, _I64]),
+    "dgtd_op_probe_surface": (C.c_int, [_P, _D, _D, _D]),
+    "dgtd_op_probe_sample": (C.c_int, [_P, _P, C.c_double, _P]),
+    "dgtd_op_probe_read": (C.c_int, [_P, _D, _D, _D, _D, _P]),
+    "dgtd_case_load": (C.c_int, [C.c_char_p, C.POINTER(_P)]),
+    "dgtd_case_destroy": (None, [_P]),
+    "dgtd_case_get_info": (C.c_int, [_P, C.POINTER(CaseInfo)]),
+    "dgtd_case_mesh": (C.c_int, [_P, C.POINTER(MeshDesc)]),
+    "dgtd_case_planewaves": (C.c_int, [_P, C.POINTER(PlaneWave), C.c_int32]),
+    "dgtd_case_point_probes": (C.c_int, [_P, _D]),
+    "dgtd_case_surface": (C.c_int, [_P, C.c_int32, _I32, _I64]),
+    "dgtd_case_initial_state": (C.c_int, [_P, _D, C.c_int64, _D]),
+    "dgtd_case_run": (C.c_int, [_P, C.POINTER(CaseRunOpts), _D, C.POINTER(CaseResult)]),
     "dgtd_server_create": (C.c_int, [C.POINTER(ServerOpts), C.POINTER(_P)]),
     "dgtd_server_destroy": (None, [_P]),
     "dgtd_server_submit": (C.c_int, [_P, C.POINTER(Request), _I64]),
@@ -420,6 +459,52 @@ class Operator:
         _check(lib().dgtd_op_norm2(self._h, _ptr(state), _dp(out), _stream(stream)), "dgtd_op_norm2")
         return out
 
+    # -- probes (point probes, near-to-far surface, running FP64 DFT sums)
+    def set_probes(self, points=None, surface_faces=None, freqs=(), every: int = 1, max_records: int = 0) -> None:
+        pts = np.ascontiguousarray(np.zeros((0, 3)) if points is None else points, dtype=np.float64).reshape(-1, 3)
+        fcs = np.ascontiguousarray(np.zeros((0, 3)) if surface_faces is None else surface_faces,
+                                   dtype=np.int32).reshape(-1, 3)
+        fr = np.ascontiguousarray(freqs, dtype=np.float64).reshape(-1)
+        self._probe_keep = (pts, fcs, fr)
+        sp = ProbeSpec(n_points=pts.shape[0], points=_dp(pts), n_surface_faces=fcs.shape[0], surface_faces=_ip(fcs),
+                       n_freqs=fr.shape[0], freqs=_dp(fr), every=int(every), max_records=int(max_records))
+        _check(lib().dgtd_op_set_probes(self._h, C.byref(sp)), "dgtd_op_set_probes")
+        self._probe_shape = (pts.shape[0], fr.shape[0], int(max_records))
+
+    def clear_probes(self) -> None:
+        _check(lib().dgtd_op_clear_probes(self._h), "dgtd_op_clear_probes")
+
+    def probe_reset(self, stream=None) -> None:
+        _check(lib().dgtd_op_probe_reset(self._h, _stream(stream)), "dgtd_op_probe_reset")
+
+    def probe_sample(self, state, t: float, stream=None) -> None:
+        _check(lib().dgtd_op_probe_sample(self._h, _ptr(state), float(t), _stream(stream)), "dgtd_op_probe_sample")
+
+    def probe_info(self) -> dict:
+        a, b, c = C.c_int64(), C.c_int64(), C.c_int64()
+        _check(lib().dgtd_op_probe_info(self._h, C.byref(a), C.byref(b), C.byref(c)), "dgtd_op_probe_info")
+        return {"n_surface_nodes": a.value, "n_samples": b.value, "n_records": c.value}
+
+    def probe_surface(self):
+        n = self.probe_info()["n_surface_nodes"]
+        xyz, nrm, w = np.zeros((n, 3)), np.zeros((n, 3)), np.zeros(n)
+        _check(lib().dgtd_op_probe_surface(self._h, _dp(xyz), _dp(nrm), _dp(w)), "dgtd_op_probe_surface")
+        return xyz, nrm, w
+
+    def probe_read(self, stream=None) -> dict:
+        """Raw DFT sums as complex arrays: points [B, n_points, 6, nf], surface [B, n_surf, 6, nf];
+        series [n_records, B, n_points, 6] and its times."""
+        npts, nf, _ = self._probe_shape
+        info = self.probe_info()
+        ns, nr = info["n_surface_nodes"], info["n_records"]
+        B = self.batch
+        pd = np.zeros((B, npts, 6, nf, 2)); sd = np.zeros((B, ns, 6, nf, 2))
+        se = np.zeros((nr, B, npts, 6)); st = np.zeros(nr)
+        _check(lib().dgtd_op_probe_read(self._h, _dp(pd), _dp(sd), _dp(se), _dp(st), _stream(stream)),
+               "dgtd_op_probe_read")
+        return {"points": pd[..., 0] + 1j * pd[..., 1], "surface": sd[..., 0] + 1j * sd[..., 1], "series": se,
+                "times": st, "n_samples": info["n_samples"]}
+
     # -- host API
     def mult_host(self, x: np.ndarray, t: float = 0.0) -> np.ndarray:
         x = np.ascontiguousarray(x, dtype=np.float64)
@@ -534,3 +619,74 @@ class Arena:
                 self._h = C.c_void_p()
         except Exception:
             pass
+
+
+class Case:
+    """A reference JSON case (``driver::buildSolverJson`` input) and its gmsh 2.2 mesh."""
+
+    def __init__(self, json_path):
+        h = C.c_void_p()
+        _check(lib().dgtd_case_load(str(json_path).encode(), C.byref(h)), "dgtd_case_load")
+        self._h = h
+        inf = CaseInfo()
+        _check(lib().dgtd_case_get_info(self._h, C.byref(inf)), "dgtd_case_get_info")
+        self.info = {k: getattr(inf, k) for k, _ in CaseInfo._fields_}
+
+    def __del__(self):
+        try:
+            if self._h.value:
+                lib().dgtd_case_destroy(self._h)
+                self._h = C.c_void_p()
+        except Exception:
+            pass
+
+    def mesh(self) -> Mesh:
+        d = MeshDesc()
+        _check(lib().dgtd_case_mesh(self._h, C.byref(d)), "dgtd_case_mesh")
+        nv, ne, nb, nt, ni = d.n_vertices, d.n_elements, d.n_bdr_faces, d.n_tfsf_faces, d.n_int_faces
+        arr = lambda p, n, dt: np.ctypeslib.as_array(p, shape=(n,)).astype(dt).copy() if n > 0 else np.zeros(0, dt)
+        return Mesh(arr(d.vertices, 3 * nv, np.float64).reshape(-1, 3), arr(d.elements, 4 * ne, np.int32).reshape(-1, 4),
+                    arr(d.bdr_faces, 3 * nb, np.int32).reshape(-1, 3), arr(d.bdr_codes, nb, np.int32),
+                    arr(d.tfsf_faces, 3 * nt, np.int32).reshape(-1, 3), arr(d.int_faces, 3 * ni, np.int32).reshape(-1, 3),
+                    arr(d.int_codes, ni, np.int32), arr(d.eps_r, ne, np.float64), arr(d.mu_r, ne, np.float64),
+                    arr(d.sigma, ne, np.float64))
+
+    def planewaves(self) -> list:
+        n = self.info["n_waves"]
+        a = (PlaneWave * max(1, n))()
+        _check(lib().dgtd_case_planewaves(self._h, a, n), "dgtd_case_planewaves")
+        return [dict(propagation=list(a[i].propagation), polarization=list(a[i].polarization), spread=a[i].spread,
+                     mean=a[i].mean, frequency=a[i].frequency, batch=a[i].batch) for i in range(n)]
+
+    def point_probes(self) -> np.ndarray:
+        p = np.zeros((self.info["n_point_probes"], 3))
+        if p.size:
+            _check(lib().dgtd_case_point_probes(self._h, _dp(p)), "dgtd_case_point_probes")
+        return p
+
+    def surface(self, s: int) -> np.ndarray:
+        n = C.c_int64()
+        _check(lib().dgtd_case_surface(self._h, int(s), None, C.byref(n)), "dgtd_case_surface")
+        f = np.zeros((n.value, 3), np.int32)
+        _check(lib().dgtd_case_surface(self._h, int(s), _ip(f), C.byref(n)), "dgtd_case_surface")
+        return f
+
+    def initial_state(self, xyz: np.ndarray) -> np.ndarray:
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+        n = xyz.shape[1]
+        out = np.zeros(6 * n)
+        _check(lib().dgtd_case_initial_state(self._h, _dp(xyz), n, _dp(out)), "dgtd_case_initial_state")
+        return out
+
+    def run(self, freqs=(), out_dir=None, want_state: bool = True):
+        fr = np.ascontiguousarray(freqs, dtype=np.float64).reshape(-1)
+        o = CaseRunOpts(precision=FP64, freqs=_dp(fr) if fr.size else None, n_freqs=fr.size,
+                        out_dir=str(out_dir).encode() if out_dir else None)
+        r = CaseResult()
+        state = None
+        if want_state:
+            Np = (self.info["order"] + 1) * (self.info["order"] + 2) * (self.info["order"] + 3) // 6
+            state = np.zeros(6 * self.info["n_elements"] * Np)
+        _check(lib().dgtd_case_run(self._h, C.byref(o), _dp(state) if state is not None else None, C.byref(r)),
+               "dgtd_case_run")
+        return state, {k: getattr(r, k) for k, _ in CaseResult._fields_}

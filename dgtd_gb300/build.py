@@ -23,7 +23,7 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompil
               "--expt-relaxed-constexpr", "-I", str(ROOT / "include")]
 
 SOURCES = ["refelem.cpp", "mesh.cpp", "plain_fp64.cu", "batched.cu", "batched_tc.cu", "tc_selftest.cu", "capi.cu",
-           "serve.cu"]
+           "serve.cu", "probes.cu", "jsoncase.cpp", "case_api.cu"]
 
 
 def nvcc() -> str:

@@ -206,25 +206,49 @@ __global__ void __launch_bounds__(kWarps * kLanes) stage_f32(BatchedTables T, Ba
     }
 }
 
-__global__ void tfsf_skip_f32(BatchedTables T, const PlaneWaveF32* pw, const int* pw_off, float t, int* skip)
+// TF/SF skip flags (reference GlobalEvolution.cpp:587-598: the source is skipped while
+// ||0.5 pw||^2 over the TF/SF-submesh nodes is below 1e-16). Grid (Bpad, kSkipParts):
+// block (b, part) sums a fixed slice of the nodes; the last block of incidence b
+// to finish (ticket counter) adds the partial sums in slice order, so the decision
+// does not depend on block scheduling.
+constexpr int kSkipParts = 16;
+
+__global__ void __launch_bounds__(256) tfsf_skip_f32(BatchedTables T, const PlaneWaveF32* pw, const int* pw_off, float t,
+                                                     double* partial, unsigned int* ticket, int* skip)
 {
-    const int b = blockIdx.x;
+    const int b = blockIdx.x, part = blockIdx.y, nparts = gridDim.y;
+    const int64_t n = T.n_tfsf_nodes;
+    const int64_t lo = n * part / nparts, hi = n * (part + 1) / nparts;
     double acc = 0.0;
-    for (int64_t w = threadIdx.x; w < T.n_tfsf_nodes; w += blockDim.x) {
+    for (int64_t w = lo + threadIdx.x; w < hi; w += blockDim.x) {
         float pe[3], ph[3];
-        pw_eval_f32(pw, pw_off, b, T.nxyz[w], T.nxyz[T.n_tfsf_nodes + w], T.nxyz[2 * T.n_tfsf_nodes + w], t, pe, ph);
+        pw_eval_f32(pw, pw_off, b, T.nxyz[w], T.nxyz[n + w], T.nxyz[2 * n + w], t, pe, ph);
         float s = 0.0f;
         for (int c = 0; c < 3; ++c) s += pe[c] * pe[c] + ph[c] * ph[c];
         acc += 0.25 * static_cast<double>(s);
     }
     __shared__ double red[256];
+    __shared__ bool last;
     red[threadIdx.x] = acc;
     __syncthreads();
     for (int s = blockDim.x / 2; s > 0; s >>= 1) {
         if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
         __syncthreads();
     }
-    if (threadIdx.x == 0) skip[b] = (red[0] < 1e-16) ? 1 : 0;
+    if (threadIdx.x == 0) {
+        partial[b * nparts + part] = red[0];
+        __threadfence();
+        last = atomicAdd(&ticket[b], 1u) == static_cast<unsigned int>(nparts - 1);
+    }
+    __syncthreads();
+    if (last && threadIdx.x == 0) {
+        __threadfence();
+        double sum = 0.0;
+        const volatile double* pv = partial + b * nparts;
+        for (int q = 0; q < nparts; ++q) sum += pv[q];
+        skip[b] = (sum < 1e-16) ? 1 : 0;
+        ticket[b] = 0u;
+    }
 }
 
 // reference [b][c][e*Np+i] (FP64) -> internal [e'][c][i][b] (FP32)
@@ -338,6 +362,7 @@ std::unique_ptr<BatchedOp> BatchedOp::create(const RefTet& ref, const MeshTables
     std::iota(perm.begin(), perm.end(), 0);
     std::stable_sort(perm.begin(), perm.end(), [&](int32_t a, int32_t b) { return code[a] < code[b]; });
     for (int64_t i = 0; i < K; ++i) inv[perm[i]] = static_cast<int32_t>(i);
+    op->inv_perm_host_ = inv;
 
     // FP32 tables in internal order (built in FP64 on the host, rounded once)
     std::vector<float> D(3 * Np * Np), L(Np * 4 * Nfp), geo(K * 9), fgeo(K * 16), mat(K * 3);
@@ -402,6 +427,11 @@ std::unique_ptr<BatchedOp> BatchedOp::create(const RefTet& ref, const MeshTables
     ckb(cudaDeviceGetAttribute(&op->n_sm_, cudaDevAttrMultiProcessorCount, dev_id), "SM count");
     ckb(cudaMalloc(&op->skip_, op->Bpad_ * sizeof(int)), "cudaMalloc skip");
     op->allocs_.push_back(op->skip_);
+    ckb(cudaMalloc(&op->skip_partial_, op->Bpad_ * kSkipParts * sizeof(double)), "cudaMalloc skip partials");
+    op->allocs_.push_back(op->skip_partial_);
+    ckb(cudaMalloc(&op->skip_ticket_, op->Bpad_ * sizeof(unsigned int)), "cudaMalloc skip tickets");
+    op->allocs_.push_back(op->skip_ticket_);
+    ckb(cudaMemset(op->skip_ticket_, 0, op->Bpad_ * sizeof(unsigned int)), "memset skip tickets");
     return op;
 }
 
@@ -445,7 +475,8 @@ void BatchedOp::stage(BatchedStageArgs A, double t, cudaStream_t s)
 {
     A.t = static_cast<float>(t);
     if (has_tfsf_ && n_pw_ > 0) {
-        tfsf_skip_f32<<<Bpad_, 256, 0, s>>>(T_, pw_dev_, pw_off_, static_cast<float>(t), skip_);
+        tfsf_skip_f32<<<dim3(Bpad_, kSkipParts), 256, 0, s>>>(T_, pw_dev_, pw_off_, static_cast<float>(t),
+                                                             skip_partial_, skip_ticket_, skip_);
         ckb(cudaGetLastError(), "tfsf skip kernel");
         ++launches_;
         A.pw = pw_dev_; A.pw_off = pw_off_; A.skip = skip_;

@@ -69,6 +69,9 @@ public:
     int64_t device_bytes() const { return device_bytes_; }
     int64_t state_len() const { return state_len_; }       // floats of one internal state
     int64_t kernel_launches() const { return launches_; }
+    int batch_padded() const { return Bpad_; }
+    // internal (Morton) index of each reference element, host copy
+    const std::vector<int32_t>& inv_perm() const { return inv_perm_host_; }
 
     // reference layout (FP64, [b][c][e*Np+i]) <-> internal FP32
     void pack(const double* d_ref, float* d_state, cudaStream_t s);
@@ -94,10 +97,13 @@ private:
     int64_t launches_ = 0;
     std::vector<void*> allocs_;
     int32_t* perm_ = nullptr;   // internal element -> reference element
+    std::vector<int32_t> inv_perm_host_;
     PlaneWaveF32* pw_dev_ = nullptr;
     int* pw_off_ = nullptr;
     int n_pw_ = 0, pw_cap_ = 0;
     int* skip_ = nullptr;
+    double* skip_partial_ = nullptr;      // [Bpad][parts] partial sums of the skip test
+    unsigned int* skip_ticket_ = nullptr; // [Bpad] blocks finished per incidence
     float* ws_ = nullptr;
     bool has_tfsf_ = false;
     int contraction_ = 0;

@@ -3,15 +3,16 @@
 // For one element e and one chunk of 64 incidences the right-hand side of all
 // six field components is a single tall-skinny product
 //
-//   RHS^T[(c,b), i] = sum_k W[(c,b), k] * Op[k, i],  Op = [LIFT | Dr | Ds | Dt]^T,
+//   RHS^T[(c,b), i] = sum_k W[(c,b), k] * Op[k, i],  Op = [Dr | Ds | Dt | LIFT]^T,
 //
 // with W the per-element operand built on the fly:
-//   k in [0, 4Nfp)          : Fscale/2 * upwind flux at face node k
-//                             (reference HesthavenEvolution.cpp:509-520);
-//   k in [4Nfp, 4Nfp + 3Np) : (g_r x F, g_s x F, g_t x F) at node (k - 4Nfp) mod Np, where F is
-//                             the partner field (H for E targets, -E for H targets) and g_r, g_s,
+//   k in [0, 3Np)           : (g_r x F, g_s x F, g_t x F) at node k mod Np, where F is the
+//                             partner field (H for E targets, -E for H targets) and g_r, g_s,
 //                             g_t the element's geometric factors (rows of d(r,s,t)/dx), so the
-//                             product is the curl (:522-534).
+//                             product is the curl (reference HesthavenEvolution.cpp:522-534);
+//   k in [3Np, 3Np + 4Nfp)  : Fscale/2 * upwind flux at face node k - 3Np (:509-520).
+// The volume columns come first so that the neighbour traces the flux columns
+// need are loaded while the volume columns are being built.
 // Rows (c, b) are 6 components x 64 incidences = 3 M-tiles of 128; N = Np padded
 // to 16; K padded to 8. W is split into a tf32 high part (mantissa truncated) and
 // the FP32 remainder, the constant Op into round-to-nearest hi/lo parts, giving
@@ -19,12 +20,22 @@
 // accumulators live in tensor memory; the epilogue applies 1/eps, 1/mu, the
 // conductivity term and the RK stage update.
 //
-// Per CTA (persistent, one per SM, 512 threads): Op hi/lo resident in shared
-// memory; the element's field block and face tables of the next work item
-// prefetched by 1D bulk async copies into a second buffer (mbarrier
-// completion) while the current item is processed; a 2-slot ring of W K-steps
-// written by all threads; tcgen05.commit -> mbarrier releases a slot once the
-// tensor core has consumed it.
+// One persistent CTA per SM, warp-specialised, no CTA-wide barrier in the
+// steady state (all hand-offs are mbarriers, every wait bounded):
+//   warps 0-7  producers, two groups of 128 threads: group g builds the K-steps
+//              q = g, g + 2, ... of each work item into ring slot g. A thread
+//              owns one incidence and 4 consecutive columns of its K-step and
+//              computes all 6 component rows, stored as 16-byte vectors
+//              (conflict-free in the K-major core-matrix layout);
+//   warps 8-11 epilogue: drain a double-buffered tensor-memory accumulator
+//              (tcgen05.ld) and apply the stage update, with the global
+//              RK-register loads of the next 8 nodes in flight;
+//   warp 12    tensor-memory owner and MMA issuer (one thread);
+//   warp 13    copy issuer (one thread): 1D bulk async copies of the next work
+//              item's element block and face tables into the free staging
+//              buffer (mbarrier transaction counts).
+// Op hi/lo stays resident in shared memory for the whole launch. The RK stage
+// mode is a template parameter, so each instantiation carries one epilogue.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -41,10 +52,18 @@ namespace dgtd {
 
 namespace {
 
-constexpr int kThreads = 512;
-constexpr int kChunk = 64;          // incidences per work item
-constexpr int kWsbo = 288;                 // W operand: bytes between 8-row groups (bank-conflict-free stores)
-constexpr int kTileBytes = 16 * kWsbo;      // W tile: 128 rows x 8 tf32
+constexpr int kThreads = 448;
+constexpr int kProducerThreads = 256;   // warps 0-7
+constexpr int kEpiWarp0 = 8;            // warps 8-11 (TMEM lane quarters 0-3)
+constexpr int kEpiThreads = 128;
+constexpr int kMmaWarp = 12;
+constexpr int kCopyWarp = 13;        // the last warp: copy issuer
+constexpr int kChunk = 64;              // incidences per work item
+constexpr int kTile = 4096;             // one W tile: 128 rows x 8 tf32, SBO 256, LBO 128
+constexpr int kWStep = 3 * kTile;       // one K-step of W (3 M-tiles), hi or lo
+constexpr int kSlot = 2 * kWStep;       // hi + lo
+constexpr uint32_t kAccStride = 256;    // TMEM columns between the two accumulator buffers
+constexpr uint32_t kTmemCols = 512;
 
 template <int P>
 struct TcOrd {
@@ -55,17 +74,22 @@ struct TcOrd {
     static constexpr int KKp = (KK + 7) / 8 * 8;
     static constexpr int NKS = KKp / 8;
     static constexpr int N = (Np + 15) / 16 * 16;
+    static constexpr int NCH = (Np + 7) / 8;               // 8-column epilogue chunks per tile
     static constexpr int OpStep = N * 32;                   // bytes of one K-step of Op (N rows x 8 tf32)
     static constexpr int OpBytes = NKS * OpStep;            // per hi / lo
-    static constexpr int WBytes = 3 * kTileBytes;           // one K-step of W (3 M-tiles), per hi / lo
     static constexpr int UBytes = 6 * Np * kChunk * 4;      // staged element block
     static constexpr int NbrBytes = (4 * NF + 15) / 16 * 16;
     // U | neighbour table | face geometry (16 floats) | face codes (4 ints)
     static constexpr int UBufBytes = (UBytes + NbrBytes + 64 + 16 + 127) / 128 * 128;
-    static constexpr int TmemCols = 256;
     static constexpr size_t smem = 2 * static_cast<size_t>(OpBytes) + 2 * static_cast<size_t>(UBufBytes) +
-                                   2 * 2 * static_cast<size_t>(WBytes);
+                                   2 * static_cast<size_t>(kSlot);
+    static_assert(3 * N <= static_cast<int>(kAccStride), "accumulator buffer too narrow");
 };
+
+// Column metadata: kind in bits 28-29 (0 flux, 1 volume, 2 padding);
+// flux: face node m in bits 16-27, its volume node in bits 0-15;
+// volume: derivative direction (0 r, 1 s, 2 t) in bits 16-23, node in bits 0-15.
+constexpr int kColFlux = 0, kColVol = 1, kColPad = 2;
 
 __device__ __forceinline__ void pw_eval(const PlaneWaveF32* pw, const int* pw_off, int b, float px, float py, float pz,
                                         float t, float* e, float* h)
@@ -83,16 +107,6 @@ __device__ __forceinline__ void pw_eval(const PlaneWaveF32* pw, const int* pw_of
     }
 }
 
-__device__ __forceinline__ void tmem_ld4(uint32_t taddr, float* v)
-{
-    uint32_t r[4];
-    asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
-                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
-                 : "r"(taddr));
-#pragma unroll
-    for (int i = 0; i < 4; ++i) v[i] = __uint_as_float(r[i]);
-}
-
 __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes)
 {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(tc::smem_u32(bar)), "r"(bytes)
@@ -108,6 +122,17 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
                  : "memory");
 }
 
+// Bring `bytes` (multiple of 16, 16-byte aligned) of global memory into L2 ahead of use.
+__device__ __forceinline__ void prefetch_l2(const void* src, uint32_t bytes)
+{
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void st_shared_v4(uint32_t addr, float a, float b, float c, float d)
+{
+    asm volatile("st.shared.v4.f32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "f"(a), "f"(b), "f"(c), "f"(d) : "memory");
+}
+
 // tf32 high part by mantissa truncation, and the FP32 remainder
 __device__ __forceinline__ void split_tf32(float v, float& hi, float& lo)
 {
@@ -115,69 +140,7 @@ __device__ __forceinline__ void split_tf32(float v, float& hi, float& lo)
     lo = v - hi;
 }
 
-// Stage update of QC nodes (stride Bp) of one row of an element block: loads of the
-// RK registers first, then the stores. `nv` = valid nodes (<= QC).
-template <int QC>
-__device__ __forceinline__ void epilogue_store(const BatchedStageArgs& A, int64_t base, int Bp, int nv, const float* kv,
-                                               const float* uc, float dtf)
-{
-    float* __restrict__ out = A.out;
-    float* __restrict__ x = A.x;
-    float* __restrict__ y = A.yout;
-    float* __restrict__ z = A.z;
-    float* __restrict__ res = A.res;
-    float a[QC], b[QC];
-    switch (A.mode) {
-    case MODE_MULT:
-#pragma unroll
-        for (int j = 0; j < QC; ++j)
-            if (j < nv) out[base + j * Bp] = kv[j];
-        break;
-    case MODE_RK4_1:
-#pragma unroll
-        for (int j = 0; j < QC; ++j)
-            if (j < nv) {
-                y[base + j * Bp] = uc[j] + 0.5f * dtf * kv[j];
-                z[base + j * Bp] = uc[j] + (dtf / 6.0f) * kv[j];
-            }
-        break;
-    case MODE_RK4_2:
-    case MODE_RK4_3: {
-        const float cy = (A.mode == MODE_RK4_2) ? 0.5f * dtf : dtf;
-#pragma unroll
-        for (int j = 0; j < QC; ++j)
-            if (j < nv) { a[j] = x[base + j * Bp]; b[j] = z[base + j * Bp]; }
-#pragma unroll
-        for (int j = 0; j < QC; ++j)
-            if (j < nv) {
-                y[base + j * Bp] = a[j] + cy * kv[j];
-                z[base + j * Bp] = b[j] + (dtf / 3.0f) * kv[j];
-            }
-        break;
-    }
-    case MODE_RK4_4:
-#pragma unroll
-        for (int j = 0; j < QC; ++j)
-            if (j < nv) b[j] = z[base + j * Bp];
-#pragma unroll
-        for (int j = 0; j < QC; ++j)
-            if (j < nv) x[base + j * Bp] = b[j] + (dtf / 6.0f) * kv[j];
-        break;
-    case MODE_LSRK:
-#pragma unroll
-        for (int j = 0; j < QC; ++j)
-            if (j < nv) a[j] = res[base + j * Bp];
-#pragma unroll
-        for (int j = 0; j < QC; ++j)
-            if (j < nv) {
-                const float rr = A.a * a[j] + dtf * kv[j];
-                res[base + j * Bp] = rr;
-                y[base + j * Bp] = uc[j] + A.b * rr;
-            }
-        break;
-    default: break;
-    }
-}
+__device__ __forceinline__ bool flag_set(const int* f) { return *reinterpret_cast<const volatile int*>(f) != 0; }
 
 // Issue the bulk copies of one work item's element block and face tables (one thread).
 template <int P>
@@ -202,9 +165,79 @@ __device__ __forceinline__ void prefetch_item(const BatchedTables& T, const floa
     bulk_g2s(buf + O::UBytes + O::NbrBytes + 64, T.fcode + e * 4, 16, bar);
 }
 
-template <int P>
-__global__ void __launch_bounds__(kThreads, 1) stage_tc(BatchedTables T, BatchedStageArgs A, const uint32_t* __restrict__ op_img,
-                                                     int64_t n_work, int* status)
+// Epilogue operand loads of one chunk of kEpiNodes nodes (global, stride Bp between nodes).
+constexpr int kEpiNodes = 8;
+struct EpiOps {
+    float a[kEpiNodes];   // x (RK4_2/3) or res (LSRK)
+    float z[kEpiNodes];   // z (RK4_2/3/4)
+    float u[kEpiNodes];   // stage input (RK4_1, LSRK, conductivity)
+};
+
+template <int MODE>
+__device__ __forceinline__ void epi_load(const BatchedStageArgs& A, int64_t base, int Bp, int nv, bool need_u, EpiOps& o)
+{
+    constexpr bool need_a = (MODE == MODE_RK4_2 || MODE == MODE_RK4_3 || MODE == MODE_LSRK);
+    constexpr bool need_z = (MODE == MODE_RK4_2 || MODE == MODE_RK4_3 || MODE == MODE_RK4_4);
+    const float* __restrict__ px = (MODE == MODE_LSRK ? A.res : A.x) + base;
+    const float* __restrict__ pz = A.z + base;
+    const float* __restrict__ pu = A.in + base;
+#pragma unroll
+    for (int j = 0; j < kEpiNodes; ++j) {
+        if (j < nv) {
+            if (need_a) o.a[j] = px[j * Bp];
+            if (need_z) o.z[j] = pz[j * Bp];
+            if (need_u) o.u[j] = __ldg(pu + j * Bp);
+        }
+    }
+}
+
+// Stage update of one chunk: k = fe * acc - fs * u, then the RK register writes.
+template <int MODE>
+__device__ __forceinline__ void epi_store(const BatchedStageArgs& A, int64_t base, int Bp, int nv, bool need_u,
+                                          const float* kv, float fe, float fs, float dtf, const EpiOps& o)
+{
+#pragma unroll
+    for (int j = 0; j < kEpiNodes; ++j) {
+        if (j < nv) {
+            const float uc = need_u ? o.u[j] : 0.0f;
+            const float k = fe * kv[j] - fs * uc;
+            const int64_t ix = base + static_cast<int64_t>(j) * Bp;
+            if (MODE == MODE_MULT) {
+                A.out[ix] = k;
+            } else if (MODE == MODE_RK4_1) {
+                A.yout[ix] = uc + 0.5f * dtf * k;
+                A.z[ix] = uc + (dtf / 6.0f) * k;
+            } else if (MODE == MODE_RK4_2) {
+                A.yout[ix] = o.a[j] + 0.5f * dtf * k;
+                A.z[ix] = o.z[j] + (dtf / 3.0f) * k;
+            } else if (MODE == MODE_RK4_3) {
+                A.yout[ix] = o.a[j] + dtf * k;
+                A.z[ix] = o.z[j] + (dtf / 3.0f) * k;
+            } else if (MODE == MODE_RK4_4) {
+                A.x[ix] = o.z[j] + (dtf / 6.0f) * k;
+            } else {   // MODE_LSRK
+                const float rr = A.a * o.a[j] + dtf * k;
+                A.res[ix] = rr;
+                A.yout[ix] = uc + A.b * rr;
+            }
+        }
+    }
+}
+
+// Jumps (neighbour minus own, with the boundary rules and the TF/SF source) at one
+// face node and the resulting Fscale/2-scaled upwind flux of all six components.
+__device__ __forceinline__ void tfsf_source(const BatchedStageArgs& A, const float* xq, int b, int code, float* dE, float* dH)
+{
+    float pe[3], ph[3];
+    pw_eval(A.pw, A.pw_off, b, __ldg(xq), __ldg(xq + 1), __ldg(xq + 2), A.t, pe, ph);
+    const float s2 = (code == 4) ? 1.0f : -1.0f;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) { dE[c] += s2 * pe[c]; dH[c] += s2 * ph[c]; }
+}
+
+template <int P, int MODE>
+__global__ void __launch_bounds__(kThreads, 1)
+    stage_tc(BatchedTables T, BatchedStageArgs A, const uint32_t* __restrict__ op_img, int64_t n_work, int* status)
 {
     using O = TcOrd<P>;
     constexpr int Np = O::Np, Nfp = O::Nfp, NF = O::NF, NKS = O::NKS, N = O::N;
@@ -212,255 +245,334 @@ __global__ void __launch_bounds__(kThreads, 1) stage_tc(BatchedTables T, Batched
     unsigned char* op_hi = sm;
     unsigned char* op_lo = sm + O::OpBytes;
     unsigned char* ubuf0 = sm + 2 * O::OpBytes;
-    unsigned char* ring = ubuf0 + 2 * O::UBufBytes;           // [slot]{W hi, W lo}
-    __shared__ uint64_t mma_bar[2], u_bar[2];
+    unsigned char* ring = ubuf0 + 2 * O::UBufBytes;
+    __shared__ uint64_t u_full[2], u_empty[2], w_full[2], w_empty[2], acc_full[2], acc_empty[2], drain_bar;
     __shared__ uint32_t tbase;
-    __shared__ int s_fmask[NF];
-    __shared__ int s_tj[3 * Np];          // combo column -> (type << 8) | node
+    __shared__ int s_col[O::KKp];
+    __shared__ int s_err;
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int bl = tid & 63, kc8 = tid >> 6;     // producer: incidence and one K column of each K-step
     const int Bp = static_cast<int>(T.Bpad);
     const int nchunk = Bp / kChunk;
     const int CB = Np * Bp;                      // component stride inside an element block (global)
     const int64_t EB = 6 * static_cast<int64_t>(CB);
 
-    // ---- prologue: resident operator, lookup tables, barriers, tensor memory, first item
+    // ---- prologue: resident operator, column table, barriers, tensor memory
     {
         const uint4* src = reinterpret_cast<const uint4*>(op_img);
         uint4* dst = reinterpret_cast<uint4*>(op_hi);
         for (int i = tid; i < 2 * O::OpBytes / 16; i += kThreads) dst[i] = __ldg(src + i);
     }
-    for (int i = tid; i < NF; i += kThreads) s_fmask[i] = T.Fmask[i];
-    for (int i = tid; i < 3 * Np; i += kThreads) s_tj[i] = ((i / Np) << 8) | (i % Np);
+    for (int k = tid; k < O::KKp; k += kThreads) {
+        int v;
+        if (k < 3 * Np) v = (kColVol << 28) | ((k / Np) << 16) | (k % Np);
+        else if (k < O::KK) v = (kColFlux << 28) | ((k - 3 * Np) << 16) | T.Fmask[k - 3 * Np];
+        else v = kColPad << 28;
+        s_col[k] = v;
+    }
     if (tid == 0) {
-        for (int s = 0; s < 2; ++s) { tc::mbar_init(&mma_bar[s], 1); tc::mbar_init(&u_bar[s], 1); }
+        for (int s = 0; s < 2; ++s) {
+            tc::mbar_init(&u_full[s], 1);
+            tc::mbar_init(&u_empty[s], kProducerThreads);
+            tc::mbar_init(&w_full[s], kProducerThreads / 2);
+            tc::mbar_init(&w_empty[s], 1);
+            tc::mbar_init(&acc_full[s], 1);
+            tc::mbar_init(&acc_empty[s], kEpiThreads);
+        }
+        tc::mbar_init(&drain_bar, 1);
+        s_err = 0;
         tc::mbar_fence_init();
     }
-    if (warp == 0) {
-        tc::tmem_alloc(&tbase, O::TmemCols);
+    if (warp == kMmaWarp) {
+        tc::tmem_alloc(&tbase, kTmemCols);
         tc::tmem_relinquish();
     }
     tc::fence_proxy_async();
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
-    if (tid == 0 && static_cast<int64_t>(blockIdx.x) < n_work)
-        prefetch_item<P>(T, A.in, blockIdx.x, nchunk, Bp, ubuf0, &u_bar[0]);
-    const uint32_t taddr = tbase;
-    const uint32_t idesc = tc::idesc_tf32(128, N);
-    // phases per barrier: MMA commits, item copies issued and consumed (uniform in all threads)
-    uint32_t nmma0 = 0u, nmma1 = 0u, nu0 = 0u, nu1 = 0u, ni0 = 0u, ni1 = 0u;
-    int err = 0;   // a bounded wait ran out; made uniform at the next barrier
-    if (static_cast<int64_t>(blockIdx.x) < n_work) ++ni0;
-    const float dtf = A.dt;
-    // per-thread store offsets of the producer (row = (c & 1) * 64 + bl of tile c / 2, column kc8)
-    uint32_t soff[6];
+    const uint32_t tmem = tbase;
+    bool err = false;
+
+    if (warp < kEpiWarp0) {
+        // ================================================================ producers
+        const int pb = tid & 63;             // incidence within the chunk
+        const int kh = (tid >> 6) & 1;       // which 4 columns of the K-step
+        const int grp = tid >> 7;            // K-steps grp, grp + 2, ... -> ring slot grp
+        uint32_t soff[6];
 #pragma unroll
-    for (int c = 0; c < 6; ++c) {
-        const int r = (c & 1) * 64 + bl;
-        soff[c] = (c >> 1) * kTileBytes + (r >> 3) * kWsbo + ((kc8 & 7) >> 2) * tc::kLBO + (r & 7) * 16 + (kc8 & 3) * 4;
+        for (int c = 0; c < 6; ++c) {
+            const int row = (c & 1) * 64 + pb;
+            soff[c] = tc::smem_u32(ring) + grp * kSlot + (c >> 1) * kTile + (row >> 3) * 256 + kh * 128 +
+                      (row & 7) * 16;
+        }
+        int it = 0;
+        int uses = 0;                        // uses of this group's ring slot so far
+        for (int64_t w = blockIdx.x; w < n_work; w += gridDim.x, ++it) {
+            const int ub = it & 1;
+            const unsigned char* buf = ubuf0 + ub * O::UBufBytes;
+            const float* s_u = reinterpret_cast<const float*>(buf);          // [6][Np][64]
+            const int32_t* s_nbr = reinterpret_cast<const int32_t*>(buf + O::UBytes);
+            const float* s_fg = reinterpret_cast<const float*>(buf + O::UBytes + O::NbrBytes);
+            const int* s_code = reinterpret_cast<const int*>(buf + O::UBytes + O::NbrBytes + 64);
+            if (flag_set(&s_err) || !tc::mbar_wait(&u_full[ub], (it >> 1) & 1)) { err = true; break; }
+            const int64_t e = w / nchunk;
+            const int g = static_cast<int>(w - e * nchunk);
+            const int b = g * kChunk + pb;
+            const float* gg = T.geo + e * 9;
+            float geo[9];
+#pragma unroll
+            for (int q = 0; q < 9; ++q) geo[q] = __ldg(gg + q);
+            const bool skip_src = (A.skip == nullptr) || A.skip[b];
+            const float* __restrict__ nin = A.in + static_cast<int64_t>(g) * kChunk + pb;
+            // neighbour traces of this thread's 4 columns of a K-step (flux columns of interior faces),
+            // loaded one K-step of this group ahead
+            float nb[4][6], nbn[4][6];
+#define DGTD_LOAD_NBR(QQ, DST)                                                                          \
+    _Pragma("unroll") for (int jj = 0; jj < 4; ++jj)                                                    \
+    {                                                                                                   \
+        const int m_ = (QQ) * 8 + kh * 4 + jj - 3 * Np;                                                 \
+        if (m_ >= 0 && m_ < NF) {                                                                       \
+            const int code_ = s_code[m_ / Nfp];                                                         \
+            if (code_ == 0 || code_ == 4 || code_ == 5) {                                               \
+                const int32_t gp_ = s_nbr[m_];                                                          \
+                const int32_t en_ = gp_ / Np, node_ = gp_ - en_ * Np;                                   \
+                const float* __restrict__ un_ = nin + static_cast<int64_t>(en_) * EB + node_ * Bp;      \
+                _Pragma("unroll") for (int c = 0; c < 6; ++c) DST[jj][c] = __ldg(un_ + c * CB);         \
+            }                                                                                           \
+        }                                                                                               \
     }
-
-    int it = 0;
-    for (int64_t w = blockIdx.x; w < n_work; w += gridDim.x, ++it) {
-        const int ub = it & 1;
-        unsigned char* buf = ubuf0 + ub * O::UBufBytes;
-        const float* s_u = reinterpret_cast<const float*>(buf);          // [6][Np][64]
-        const int32_t* s_nbr = reinterpret_cast<const int32_t*>(buf + O::UBytes);
-        const float* s_fg = reinterpret_cast<const float*>(buf + O::UBytes + O::NbrBytes);
-        const int* s_code = reinterpret_cast<const int*>(buf + O::UBytes + O::NbrBytes + 64);
-        if (!tc::mbar_wait(&u_bar[ub], ((ub ? nu1 : nu0)) & 1u)) err = 1;
-        if (ub) ++nu1; else ++nu0;
-        // prefetch the next item into the other buffer (its previous user finished last iteration)
-        if (w + gridDim.x < n_work) {
-            if (tid == 0)
-                prefetch_item<P>(T, A.in, w + gridDim.x, nchunk, Bp, ubuf0 + (ub ^ 1) * O::UBufBytes, &u_bar[ub ^ 1]);
-            if (ub) ++ni0; else ++ni1;
-        }
-
-        const int64_t e = w / nchunk;
-        const int g = static_cast<int>(w - e * nchunk);
-        const int b = g * kChunk + bl;
-        const int64_t eoff = e * EB + static_cast<int64_t>(g) * kChunk;
-        const float* gg = T.geo + e * 9;
-        const float g0 = __ldg(gg + 0), g1 = __ldg(gg + 1), g2 = __ldg(gg + 2), g3 = __ldg(gg + 3),
-                    g4 = __ldg(gg + 4), g5 = __ldg(gg + 5), g6 = __ldg(gg + 6), g7 = __ldg(gg + 7), g8 = __ldg(gg + 8);
-        const bool skip_src = (A.skip == nullptr) || A.skip[b];
-        // neighbour traces of this thread's flux column, loaded one K-step ahead
-        auto load_nbr = [&](int k, float* dst) {
-            if (k < NF) {
-                const int code = s_code[k / Nfp];
-                if (code == 0 || code == 4 || code == 5) {
-                    const int32_t gp = s_nbr[k];
-                    const int32_t en = gp / Np, node = gp - en * Np;
-                    const float* __restrict__ un =
-                        A.in + static_cast<int64_t>(en) * EB + static_cast<int64_t>(g) * kChunk + node * Bp + bl;
+            // a K-step holds flux columns when it reaches past the 3Np volume columns
+            if (grp * 8 + 7 >= 3 * Np) { DGTD_LOAD_NBR(grp, nb) }
+            for (int q = grp; q < NKS; q += 2) {
+                if (q + 2 < NKS && (q + 2) * 8 + 7 >= 3 * Np) { DGTD_LOAD_NBR(q + 2, nbn) }
+                float v[6][4];
 #pragma unroll
-                    for (int c = 0; c < 6; ++c) dst[c] = __ldg(un + c * CB);
-                }
-            }
-        };
-        float nb[6], nbn[6];
-        load_nbr(kc8, nb);
-
-        for (int q = 0; q < NKS; ++q) {
-            load_nbr((q + 1) * 8 + kc8, nbn);
-            const int slot = q & 1;
-            unsigned char* w_hi = ring + slot * 2 * O::WBytes;
-            unsigned char* w_lo = w_hi + O::WBytes;
-            if (q >= 2 && !tc::mbar_wait(&mma_bar[slot], ((slot ? nmma1 : nmma0) - 1) & 1u)) err = 1;
-            // ---- produce column k of K-step q for all six target components
-            float v[6];
-            const int k = q * 8 + kc8;
-            if (k < NF) {
-                const int m = k, f = m / Nfp;
-                const int vm = s_fmask[m];
-                const int code = s_code[f];
-                const float nx = s_fg[f * 4], ny = s_fg[f * 4 + 1], nz = s_fg[f * 4 + 2], fs = s_fg[f * 4 + 3];
-                float uM[6];
+                for (int jj = 0; jj < 4; ++jj) {
+                    const int k = q * 8 + kh * 4 + jj;
+                    const int ci = s_col[k];
+                    const int kind = ci >> 28;
+                    if (kind == kColFlux) {
+                        const int m = (ci >> 16) & 0xfff, vm = ci & 0xffff, f = m / Nfp;
+                        const int code = s_code[f];
+                        const float nx = s_fg[f * 4], ny = s_fg[f * 4 + 1], nz = s_fg[f * 4 + 2];
+                        const float hf = 0.5f * s_fg[f * 4 + 3];
+                        float uM[6];
 #pragma unroll
-                for (int c = 0; c < 6; ++c) uM[c] = s_u[(c * Np + vm) * kChunk + bl];
-                float dE[3], dH[3];
-                float aE = T.alpha, aH = T.alpha;
-                if (code == 0 || code == 4 || code == 5) {
+                        for (int c = 0; c < 6; ++c) uM[c] = s_u[(c * Np + vm) * kChunk + pb];
+                        float dE[3], dH[3];
+                        float aE = T.alpha, aH = T.alpha;
+                        if (code == 0 || code == 4 || code == 5) {
 #pragma unroll
-                    for (int c = 0; c < 3; ++c) {
-                        dE[c] = nb[c] - uM[c];
-                        dH[c] = nb[c + 3] - uM[c + 3];
+                            for (int c = 0; c < 3; ++c) {
+                                dE[c] = nb[jj][c] - uM[c];
+                                dH[c] = nb[jj][c + 3] - uM[c + 3];
+                            }
+                            if (code != 0 && !skip_src) tfsf_source(A, T.fxyz + (e * NF + m) * 3, b, code, dE, dH);
+                        } else if (code == 1 || code == 6) {
+#pragma unroll
+                            for (int c = 0; c < 3; ++c) { dE[c] = -2.0f * uM[c]; dH[c] = 0.0f; }
+                        } else if (code == 2 || code == 7) {
+#pragma unroll
+                            for (int c = 0; c < 3; ++c) { dE[c] = 0.0f; dH[c] = -2.0f * uM[c + 3]; }
+                        } else if (code == 3 || code == 8) {
+#pragma unroll
+                            for (int c = 0; c < 3; ++c) { dE[c] = -uM[c]; dH[c] = -uM[c + 3]; }
+                            aE = 1.0f; aH = 1.0f;
+                        } else {
+#pragma unroll
+                            for (int c = 0; c < 3; ++c) { dE[c] = 0.0f; dH[c] = 0.0f; }
+                        }
+                        const float ndE = nx * dE[0] + ny * dE[1] + nz * dE[2];
+                        const float ndH = nx * dH[0] + ny * dH[1] + nz * dH[2];
+                        v[0][jj] = hf * ((ny * dH[2] - nz * dH[1]) + aE * (dE[0] - ndE * nx));
+                        v[1][jj] = hf * ((nz * dH[0] - nx * dH[2]) + aE * (dE[1] - ndE * ny));
+                        v[2][jj] = hf * ((nx * dH[1] - ny * dH[0]) + aE * (dE[2] - ndE * nz));
+                        v[3][jj] = hf * (-(ny * dE[2] - nz * dE[1]) + aH * (dH[0] - ndH * nx));
+                        v[4][jj] = hf * (-(nz * dE[0] - nx * dE[2]) + aH * (dH[1] - ndH * ny));
+                        v[5][jj] = hf * (-(nx * dE[1] - ny * dE[0]) + aH * (dH[2] - ndH * nz));
+                    } else if (kind == kColVol) {
+                        const int d = (ci >> 16) & 0xff, j = ci & 0xffff;
+                        const float gx = d == 0 ? geo[0] : (d == 1 ? geo[3] : geo[6]);
+                        const float gy = d == 0 ? geo[1] : (d == 1 ? geo[4] : geo[7]);
+                        const float gz = d == 0 ? geo[2] : (d == 1 ? geo[5] : geo[8]);
+                        const float* uj = s_u + j * kChunk + pb;
+                        const float Ex = uj[0], Ey = uj[Np * kChunk], Ez = uj[2 * Np * kChunk];
+                        const float Hx = uj[3 * Np * kChunk], Hy = uj[4 * Np * kChunk], Hz = uj[5 * Np * kChunk];
+                        // E rows: g x H (curl H); H rows: -(g x E) (-curl E)
+                        v[0][jj] = gy * Hz - gz * Hy;
+                        v[1][jj] = gz * Hx - gx * Hz;
+                        v[2][jj] = gx * Hy - gy * Hx;
+                        v[3][jj] = gz * Ey - gy * Ez;
+                        v[4][jj] = gx * Ez - gz * Ex;
+                        v[5][jj] = gy * Ex - gx * Ey;
+                    } else {
+#pragma unroll
+                        for (int c = 0; c < 6; ++c) v[c][jj] = 0.0f;
                     }
-                    if (code != 0 && !skip_src) {
-                        const float* xq = T.fxyz + (e * NF + m) * 3;
-                        float pe[3], ph[3];
-                        pw_eval(A.pw, A.pw_off, b, __ldg(xq), __ldg(xq + 1), __ldg(xq + 2), A.t, pe, ph);
-                        const float s2 = (code == 4) ? 1.0f : -1.0f;
-#pragma unroll
-                        for (int c = 0; c < 3; ++c) { dE[c] += s2 * pe[c]; dH[c] += s2 * ph[c]; }
-                    }
-                } else if (code == 1 || code == 6) {
-#pragma unroll
-                    for (int c = 0; c < 3; ++c) { dE[c] = -2.0f * uM[c]; dH[c] = 0.0f; }
-                } else if (code == 2 || code == 7) {
-#pragma unroll
-                    for (int c = 0; c < 3; ++c) { dE[c] = 0.0f; dH[c] = -2.0f * uM[c + 3]; }
-                } else if (code == 3 || code == 8) {
-#pragma unroll
-                    for (int c = 0; c < 3; ++c) { dE[c] = -uM[c]; dH[c] = -uM[c + 3]; }
-                    aE = 1.0f; aH = 1.0f;
-                } else {
-#pragma unroll
-                    for (int c = 0; c < 3; ++c) { dE[c] = 0.0f; dH[c] = 0.0f; }
                 }
-                const float hf = 0.5f * fs;
-                const float ndE = nx * dE[0] + ny * dE[1] + nz * dE[2];
-                const float ndH = nx * dH[0] + ny * dH[1] + nz * dH[2];
-                v[0] = hf * ((ny * dH[2] - nz * dH[1]) + aE * (dE[0] - ndE * nx));
-                v[1] = hf * ((nz * dH[0] - nx * dH[2]) + aE * (dE[1] - ndE * ny));
-                v[2] = hf * ((nx * dH[1] - ny * dH[0]) + aE * (dE[2] - ndE * nz));
-                v[3] = hf * (-(ny * dE[2] - nz * dE[1]) + aH * (dH[0] - ndH * nx));
-                v[4] = hf * (-(nz * dE[0] - nx * dE[2]) + aH * (dH[1] - ndH * ny));
-                v[5] = hf * (-(nx * dE[1] - ny * dE[0]) + aH * (dH[2] - ndH * nz));
-            } else if (k < NF + 3 * Np) {
-                const int tj = s_tj[k - NF], type = tj >> 8, j = tj & 255;
-                const float gx = type == 0 ? g0 : (type == 1 ? g3 : g6);
-                const float gy = type == 0 ? g1 : (type == 1 ? g4 : g7);
-                const float gz = type == 0 ? g2 : (type == 1 ? g5 : g8);
-                const float* uj = s_u + j * kChunk + bl;
-                const float Ex = uj[0], Ey = uj[Np * kChunk], Ez = uj[2 * Np * kChunk];
-                const float Hx = uj[3 * Np * kChunk], Hy = uj[4 * Np * kChunk], Hz = uj[5 * Np * kChunk];
-                // E targets: g x H (curl H); H targets: -(g x E) (-curl E)
-                v[0] = gy * Hz - gz * Hy;
-                v[1] = gz * Hx - gx * Hz;
-                v[2] = gx * Hy - gy * Hx;
-                v[3] = gz * Ey - gy * Ez;
-                v[4] = gx * Ez - gz * Ex;
-                v[5] = gy * Ex - gx * Ey;
-            } else {
-#pragma unroll
-                for (int c = 0; c < 6; ++c) v[c] = 0.0f;
-            }
-#pragma unroll
-            for (int c = 0; c < 6; ++c) {
-                float h, l;
-                split_tf32(v[c], h, l);
-                *reinterpret_cast<float*>(w_hi + soff[c]) = h;
-                *reinterpret_cast<float*>(w_lo + soff[c]) = l;
-            }
-            tc::fence_proxy_async();
-            tc::fence_before_sync();
-            if (__syncthreads_or(err)) { err = 1; break; }
-            if (tid == 0) {
-                tc::fence_after_sync();
-                const uint32_t ah0 = tc::smem_u32(w_hi), al0 = tc::smem_u32(w_lo);
-                const uint64_t bh = tc::smem_desc(tc::smem_u32(op_hi + q * O::OpStep));
-                const uint64_t blo = tc::smem_desc(tc::smem_u32(op_lo + q * O::OpStep));
-#pragma unroll
-                for (int t = 0; t < 3; ++t) {
-                    const uint32_t d = taddr + t * N;
-                    const uint64_t ah = tc::smem_desc_sbo(ah0 + t * kTileBytes, kWsbo);
-                    const uint64_t al = tc::smem_desc_sbo(al0 + t * kTileBytes, kWsbo);
-                    tc::mma_tf32(d, ah, bh, idesc, q > 0);
-                    tc::mma_tf32(d, al, bh, idesc, true);
-                    tc::mma_tf32(d, ah, blo, idesc, true);
+                // ---- hand the K-step to the tensor core through this group's ring slot
+                if (uses >= 1 && (flag_set(&s_err) || !tc::mbar_wait(&w_empty[grp], (uses - 1) & 1))) {
+                    err = true;
+                    break;
                 }
-                tc::mma_commit(&mma_bar[slot]);
-            }
-            if (slot) ++nmma1; else ++nmma0;
 #pragma unroll
-            for (int c = 0; c < 6; ++c) nb[c] = nbn[c];
+                for (int c = 0; c < 6; ++c) {
+                    float h[4], l[4];
+#pragma unroll
+                    for (int jj = 0; jj < 4; ++jj) split_tf32(v[c][jj], h[jj], l[jj]);
+                    st_shared_v4(soff[c], h[0], h[1], h[2], h[3]);
+                    st_shared_v4(soff[c] + kWStep, l[0], l[1], l[2], l[3]);
+                }
+                tc::fence_proxy_async();
+                tc::mbar_arrive(&w_full[grp]);
+                ++uses;
+#pragma unroll
+                for (int jj = 0; jj < 4; ++jj)
+#pragma unroll
+                    for (int c = 0; c < 6; ++c) nb[jj][c] = nbn[jj][c];
+            }
+#undef DGTD_LOAD_NBR
+            if (err) break;
+            tc::mbar_arrive(&u_empty[ub]);        // this thread is done with the staged block
         }
-        if (err) break;
-        // ---- all MMAs of this work item done
-        if (!tc::mbar_wait(&mma_bar[0], (nmma0 - 1) & 1u)) err = 1;
-        if (!tc::mbar_wait(&mma_bar[1], (nmma1 - 1) & 1u)) err = 1;
-        tc::fence_after_sync();
-        if (__syncthreads_or(err)) { err = 1; break; }
-        {
-            // ---- epilogue: warp = (lane group lg, column quarter cq); tile rows are (c, incidence).
-            // All operand loads of a tile are issued before its stores so that each thread
-            // waits for one memory round trip per tile, not one per output.
-            constexpr int QC = N / 4;
-            const int lg = warp & 3, cq = warp >> 2;
-            const int r = lg * 32 + lane;
+    } else if (warp < kEpiWarp0 + 4) {
+        // ================================================================ epilogue
+        const int lq = warp & 3;                  // TMEM lane quarter of this warp
+        const int r = lq * 32 + lane;             // accumulator row within each tile
+        const int blr = r & 63;
+        const float dtf = A.dt;
+        constexpr int NCHT = 3 * O::NCH;          // 8-node chunks per item (3 tiles)
+        int it = 0;
+        for (int64_t w = blockIdx.x; w < n_work; w += gridDim.x, ++it) {
+            const int64_t e = w / nchunk;
+            const int g = static_cast<int>(w - e * nchunk);
+            const int abuf = it & 1;
             const float ie = __ldg(T.mat + e * 3 + 0), im = __ldg(T.mat + e * 3 + 1), se = __ldg(T.mat + e * 3 + 2);
-            const int blr = r & 63;
-            const int cb = cq * QC;
-#pragma unroll 1
-            for (int t = 0; t < 3; ++t) {
-                const int c = 2 * t + (r >> 6);
-                const int64_t base = eoff + c * CB + blr + static_cast<int64_t>(cb) * Bp;
-                const float* su = s_u + (c * Np + cb) * kChunk + blr;
-                float kv[QC], uc[QC];
-#pragma unroll
-                for (int j = 0; j < QC; j += 4)
-                    tmem_ld4(taddr + (static_cast<uint32_t>(lg * 32) << 16) + t * N + cb + j, kv + j);
+            const bool need_u = (MODE == MODE_RK4_1) || (MODE == MODE_LSRK) || (se != 0.0f);
+            const int64_t eoff = e * EB + static_cast<int64_t>(g) * kChunk + blr;
+            const uint32_t tacc = tmem + abuf * kAccStride + (static_cast<uint32_t>(lq * 32) << 16);
+            auto chunk_base = [&](int n) {
+                const int t = n / O::NCH, cb = (n % O::NCH) * kEpiNodes;
+                return eoff + static_cast<int64_t>(2 * t + (r >> 6)) * CB + static_cast<int64_t>(cb) * Bp;
+            };
+            auto chunk_nv = [&](int n) { return min(kEpiNodes, Np - (n % O::NCH) * kEpiNodes); };
+            // one chunk: accumulator columns -> registers, release the buffer after the last one, update
+            auto process = [&](int n, const EpiOps& o) {
+                const int t = n / O::NCH, cb = (n % O::NCH) * kEpiNodes;
+                float kv[kEpiNodes];
+                tc::tmem_ld8(tacc + t * N + cb, kv);
                 tc::tmem_ld_wait();
-                const float fe = (c < 3) ? ie : im, fs = (c < 3) ? se : 0.0f;
-#pragma unroll
-                for (int j = 0; j < QC; ++j) {
-                    uc[j] = (cb + j < Np) ? su[j * kChunk] : 0.0f;
-                    kv[j] = fe * kv[j] - fs * uc[j];
+                if (n == NCHT - 1) {
+                    tc::fence_before_sync();
+                    tc::mbar_arrive(&acc_empty[abuf]);
                 }
-                epilogue_store<QC>(A, base, Bp, Np - cb, kv, uc, dtf);
+                const int c = 2 * t + (r >> 6);
+                const float fe = (c < 3) ? ie : im, fs = (c < 3) ? se : 0.0f;
+                epi_store<MODE>(A, chunk_base(n), Bp, chunk_nv(n), need_u, kv, fe, fs, dtf, o);
+            };
+            EpiOps o0, o1;
+            epi_load<MODE>(A, chunk_base(0), Bp, chunk_nv(0), need_u, o0);
+            if (flag_set(&s_err) || !tc::mbar_wait(&acc_full[abuf], (it >> 1) & 1)) { err = true; break; }
+            tc::fence_after_sync();
+#pragma unroll 1
+            for (int n = 0; n < NCHT; n += 2) {
+                if (n + 1 < NCHT) epi_load<MODE>(A, chunk_base(n + 1), Bp, chunk_nv(n + 1), need_u, o1);
+                process(n, o0);
+                if (n + 1 < NCHT) {
+                    if (n + 2 < NCHT) epi_load<MODE>(A, chunk_base(n + 2), Bp, chunk_nv(n + 2), need_u, o0);
+                    process(n + 1, o1);
+                }
             }
         }
-        tc::fence_before_sync();
-        __syncthreads();
-    }
-    if (err) {
-        // drain: wait (bounded) for this CTA's copies and MMAs still in flight before
-        // the tensor memory and the shared buffers are released
-        if (tid == 0) {
-            atomicExch(status, 1);
-            if (nmma0) tc::mbar_wait(&mma_bar[0], (nmma0 - 1) & 1u);
-            if (nmma1) tc::mbar_wait(&mma_bar[1], (nmma1 - 1) & 1u);
-            if (ni0) tc::mbar_wait(&u_bar[0], (ni0 - 1) & 1u);
-            if (ni1) tc::mbar_wait(&u_bar[1], (ni1 - 1) & 1u);
+    } else if (warp == kMmaWarp) {
+        // ================================================================ MMA issuer
+        if (lane == 0) {
+            const uint32_t idesc = tc::idesc_tf32(128, N);
+            const uint32_t ring_u32 = tc::smem_u32(ring);
+            int it = 0;
+            int uses0 = 0, uses1 = 0;        // consumed K-steps per ring slot
+            for (int64_t w = blockIdx.x; w < n_work; w += gridDim.x, ++it) {
+                const int abuf = it & 1, ause = it >> 1;
+                if (ause >= 1 && (flag_set(&s_err) || !tc::mbar_wait(&acc_empty[abuf], (ause - 1) & 1))) {
+                    err = true;
+                    break;
+                }
+                tc::fence_after_sync();
+                const uint32_t dacc = tmem + abuf * kAccStride;
+                for (int q = 0; q < NKS; ++q) {
+                    const int slot = q & 1;
+                    const int use = slot ? uses1 : uses0;
+                    if (flag_set(&s_err) || !tc::mbar_wait(&w_full[slot], use & 1)) { err = true; break; }
+                    if (slot) ++uses1; else ++uses0;
+                    tc::fence_after_sync();
+                    const uint32_t ah0 = ring_u32 + slot * kSlot, al0 = ah0 + kWStep;
+                    const uint64_t bh = tc::smem_desc(tc::smem_u32(op_hi + q * O::OpStep));
+                    const uint64_t blo = tc::smem_desc(tc::smem_u32(op_lo + q * O::OpStep));
+#pragma unroll
+                    for (int t = 0; t < 3; ++t) {
+                        const uint32_t d = dacc + t * N;
+                        const uint64_t ah = tc::smem_desc(ah0 + t * kTile);
+                        const uint64_t al = tc::smem_desc(al0 + t * kTile);
+                        tc::mma_tf32(d, ah, bh, idesc, q > 0);
+                        tc::mma_tf32(d, al, bh, idesc, true);
+                        tc::mma_tf32(d, ah, blo, idesc, true);
+                    }
+                    tc::mma_commit(&w_empty[slot]);
+                }
+                if (err) break;
+                tc::mma_commit(&acc_full[abuf]);
+            }
+            if (err) {
+                // wait (bounded) for the MMAs already issued before the tensor memory is freed
+                tc::mma_commit(&drain_bar);
+                tc::mbar_wait(&drain_bar, 0);
+            }
+        }
+    } else if (warp == kCopyWarp) {
+        // ================================================================ copy issuer
+        if (lane == 0) {
+            int it = 0;
+            int issued0 = 0, issued1 = 0;     // copies issued per staging buffer
+            for (int64_t w = blockIdx.x; w < n_work; w += gridDim.x, ++it) {
+                const int ub = it & 1, use = it >> 1;
+                if (use >= 1 && (flag_set(&s_err) || !tc::mbar_wait(&u_empty[ub], (use - 1) & 1))) {
+                    err = true;
+                    break;
+                }
+                prefetch_item<P>(T, A.in, w, nchunk, Bp, ubuf0 + ub * O::UBufBytes, &u_full[ub]);
+                if (ub) ++issued1; else ++issued0;
+                // the RK registers the epilogue of this item reads: into L2 now, so that its
+                // loads wait for L2 rather than HBM (whole element block once per element)
+                const int64_t e = w / nchunk;
+                if (w - e * nchunk == 0) {
+                    const uint32_t eb = static_cast<uint32_t>(EB * sizeof(float));
+                    if (MODE == MODE_RK4_2 || MODE == MODE_RK4_3) {
+                        prefetch_l2(A.x + e * EB, eb);
+                        prefetch_l2(A.z + e * EB, eb);
+                    } else if (MODE == MODE_RK4_4) {
+                        prefetch_l2(A.z + e * EB, eb);
+                    } else if (MODE == MODE_LSRK) {
+                        prefetch_l2(A.res + e * EB, eb);
+                    }
+                }
+            }
+            if (err) {
+                // wait (bounded) for this CTA's copies still in flight
+                if (issued0) tc::mbar_wait(&u_full[0], (issued0 - 1) & 1);
+                if (issued1) tc::mbar_wait(&u_full[1], (issued1 - 1) & 1);
+            }
         }
     }
+
+    if (err) atomicExch(&s_err, 1);
     tc::fence_before_sync();
     __syncthreads();
-    if (warp == 0) tc::tmem_dealloc(taddr, O::TmemCols);
+    if (tid == 0 && s_err) atomicExch(status, 1);
+    if (warp == kMmaWarp) {
+        tc::fence_after_sync();
+        tc::tmem_dealloc(tmem, kTmemCols);
+    }
 }
 
 uint32_t tf32_bits_rna(float x)
@@ -483,7 +595,7 @@ float bits_to_float(uint32_t u)
 
 bool tc_supported(int p, int Bpad) { return p >= 1 && p <= 4 && Bpad % kChunk == 0; }
 
-// Host image of Op = [LIFT | Dr | Ds | Dt]^T as the kernel's K-major B operand:
+// Host image of Op = [Dr | Ds | Dt | LIFT]^T as the kernel's K-major B operand:
 // all K-steps of the tf32 high parts (N rows x 8 columns each), then all low parts.
 std::vector<uint32_t> tc_operator_image(const RefTet& ref)
 {
@@ -494,9 +606,9 @@ std::vector<uint32_t> tc_operator_image(const RefTet& ref)
     for (int i = 0; i < Np; ++i)
         for (int k = 0; k < KK; ++k) {
             double v;
-            if (k < NF) v = ref.LIFT[static_cast<size_t>(i) * NF + k];
+            if (k >= 3 * Np) v = ref.LIFT[static_cast<size_t>(i) * NF + (k - 3 * Np)];
             else {
-                const int kc = k - NF, type = kc / Np, j = kc - type * Np;
+                const int type = k / Np, j = k - type * Np;
                 const std::vector<double>& D = type == 0 ? ref.Dr : (type == 1 ? ref.Ds : ref.Dt);
                 v = D[static_cast<size_t>(i) * Np + j];
             }
@@ -511,29 +623,53 @@ std::vector<uint32_t> tc_operator_image(const RefTet& ref)
     return img;
 }
 
+namespace {
+
+template <int P, int MODE>
+void launch_tc_instance(const BatchedTables& T, const BatchedStageArgs& A, const uint32_t* op_img, int* status,
+                        int64_t grid, int64_t n_work, cudaStream_t s)
+{
+    static bool attr = false;
+    if (!attr) {
+        cudaError_t e = cudaFuncSetAttribute(stage_tc<P, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             static_cast<int>(TcOrd<P>::smem));
+        if (e != cudaSuccess) throw std::runtime_error(std::string("tc smem attribute: ") + cudaGetErrorString(e));
+        attr = true;
+    }
+    stage_tc<P, MODE><<<static_cast<unsigned>(grid), kThreads, TcOrd<P>::smem, s>>>(T, A, op_img, n_work, status);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) throw std::runtime_error(std::string("tc stage kernel: ") + cudaGetErrorString(e));
+}
+
+template <int P>
+void launch_tc_order(const BatchedTables& T, const BatchedStageArgs& A, const uint32_t* op_img, int* status,
+                     int64_t grid, int64_t n_work, cudaStream_t s)
+{
+    switch (A.mode) {
+    case MODE_MULT: launch_tc_instance<P, MODE_MULT>(T, A, op_img, status, grid, n_work, s); break;
+    case MODE_RK4_1: launch_tc_instance<P, MODE_RK4_1>(T, A, op_img, status, grid, n_work, s); break;
+    case MODE_RK4_2: launch_tc_instance<P, MODE_RK4_2>(T, A, op_img, status, grid, n_work, s); break;
+    case MODE_RK4_3: launch_tc_instance<P, MODE_RK4_3>(T, A, op_img, status, grid, n_work, s); break;
+    case MODE_RK4_4: launch_tc_instance<P, MODE_RK4_4>(T, A, op_img, status, grid, n_work, s); break;
+    case MODE_LSRK: launch_tc_instance<P, MODE_LSRK>(T, A, op_img, status, grid, n_work, s); break;
+    default: throw std::runtime_error("tensor-core stage: unknown stage mode");
+    }
+}
+
+}  // namespace
+
 void launch_stage_tc(const BatchedTables& T, const BatchedStageArgs& A, const uint32_t* op_img, int* status, int n_sm,
                      cudaStream_t s)
 {
     const int64_t n_work = T.K * (T.Bpad / kChunk);
     if (reinterpret_cast<uintptr_t>(A.in) % 16 != 0)
         throw std::runtime_error("tensor-core stage: the input state must be 16-byte aligned (bulk async copies)");
-    auto go = [&](auto kernel, size_t smem) {
-        static bool attr[8] = {};
-        if (!attr[T.p]) {
-            cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-            if (e != cudaSuccess) throw std::runtime_error(std::string("tc smem attribute: ") + cudaGetErrorString(e));
-            attr[T.p] = true;
-        }
-        const int64_t grid = std::min<int64_t>(n_work, static_cast<int64_t>(n_sm));
-        kernel<<<static_cast<unsigned>(grid), kThreads, smem, s>>>(T, A, op_img, n_work, status);
-        cudaError_t e = cudaGetLastError();
-        if (e != cudaSuccess) throw std::runtime_error(std::string("tc stage kernel: ") + cudaGetErrorString(e));
-    };
+    const int64_t grid = std::min<int64_t>(n_work, static_cast<int64_t>(n_sm));
     switch (T.p) {
-    case 1: go(stage_tc<1>, TcOrd<1>::smem); break;
-    case 2: go(stage_tc<2>, TcOrd<2>::smem); break;
-    case 3: go(stage_tc<3>, TcOrd<3>::smem); break;
-    case 4: go(stage_tc<4>, TcOrd<4>::smem); break;
+    case 1: launch_tc_order<1>(T, A, op_img, status, grid, n_work, s); break;
+    case 2: launch_tc_order<2>(T, A, op_img, status, grid, n_work, s); break;
+    case 3: launch_tc_order<3>(T, A, op_img, status, grid, n_work, s); break;
+    case 4: launch_tc_order<4>(T, A, op_img, status, grid, n_work, s); break;
     default: throw std::runtime_error("tensor-core stage kernel supports orders 1..4");
     }
 }

@@ -15,6 +15,7 @@
 #include "batched.hpp"
 #include "kernels.hpp"
 #include "mesh.hpp"
+#include "probes.hpp"
 #include "refelem.hpp"
 
 namespace {
@@ -90,6 +91,9 @@ struct dgtd_op {
     int64_t ws_len = 0;
     // batched FP32 form
     std::unique_ptr<dgtd::BatchedOp> batched;
+    // point probes / DFT accumulators, sampled by dgtd_op_step every probes->every() steps
+    std::unique_ptr<dgtd::ProbeSet> probes;
+    int64_t probe_steps = 0;
 
     ~dgtd_op()
     {
@@ -469,9 +473,22 @@ int dgtd_op_step(dgtd_op* op, void* d_work, double t0, double dt, int32_t nsteps
     if (integrator != DGTD_RK4 && integrator != DGTD_LSERK4) return fail(DGTD_ERR_INVALID, "unknown integrator");
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     try {
+        dgtd::ProbeSet* pr = op->probes.get();
         if (op->batched) {
             BatchedCount bc(op);
-            op->batched->step(static_cast<float*>(d_work), t0, dt, nsteps, integrator, s);
+            if (!pr) {
+                op->batched->step(static_cast<float*>(d_work), t0, dt, nsteps, integrator, s);
+                return DGTD_OK;
+            }
+            double t = t0;
+            for (int i = 0; i < nsteps; ++i) {
+                op->batched->step(static_cast<float*>(d_work), t, dt, 1, integrator, s);
+                t += dt;
+                if (++op->probe_steps % pr->every() == 0) {
+                    pr->sample(d_work, t, s);
+                    g_launches.fetch_add(1, std::memory_order_relaxed);
+                }
+            }
             return DGTD_OK;
         }
         double* d_state = static_cast<double*>(d_work);
@@ -484,6 +501,10 @@ int dgtd_op_step(dgtd_op* op, void* d_work, double t0, double dt, int32_t nsteps
         for (int i = 0; i < nsteps; ++i) {
             rk_step(op, d_state, t, dt, integrator, other, cur, s);
             t += dt;
+            if (pr && ++op->probe_steps % pr->every() == 0) {
+                pr->sample(cur, t, s);
+                g_launches.fetch_add(1, std::memory_order_relaxed);
+            }
         }
         if (integrator == DGTD_LSERK4 && cur != d_state)
             ck(cudaMemcpyAsync(d_state, cur, op->state_len * sizeof(double), cudaMemcpyDeviceToDevice, s), "copy");
@@ -584,6 +605,109 @@ int dgtd_op_estimate_dt(const dgtd_op* op, double cfl, double* dt_out)
     const double rmin = std::fabs(g[1] - g[0]);   // GLL spacing on a segment of length 2
     double dt = op->mesh.dt_scale_min * rmin * 2.0 / 3.0 * 0.75 * cfl;
     *dt_out = dt / 0.8;
+    return DGTD_OK;
+}
+
+int dgtd_op_set_probes(dgtd_op* op, const dgtd_probe_spec* spec)
+{
+    if (!op || !spec) return fail(DGTD_ERR_INVALID, "NULL argument");
+    if (spec->n_points < 0 || spec->n_surface_faces < 0 || spec->n_freqs < 0)
+        return fail(DGTD_ERR_INVALID, "negative probe counts");
+    if ((spec->n_points > 0 && !spec->points) || (spec->n_surface_faces > 0 && !spec->surface_faces) ||
+        (spec->n_freqs > 0 && !spec->freqs))
+        return fail(DGTD_ERR_INVALID, "probe arrays missing");
+    try {
+        dgtd::ProbeSpec ps;
+        ps.points.assign(spec->points, spec->points + 3 * static_cast<int64_t>(spec->n_points));
+        ps.surface_faces.assign(spec->surface_faces, spec->surface_faces + 3 * spec->n_surface_faces);
+        ps.freqs.assign(spec->freqs, spec->freqs + spec->n_freqs);
+        ps.every = spec->every;
+        ps.max_records = spec->max_records;
+        dgtd::ProbeStateLayout lay;
+        lay.Np = op->ref.Np;
+        lay.N = op->mesh.K * op->ref.Np;
+        lay.B = op->batch;
+        if (op->batched) {
+            lay.fp32 = true;
+            lay.Bp = op->batched->batch_padded();
+            lay.inv_perm = op->batched->inv_perm().data();
+        }
+        op->probes.reset();
+        op->probes = dgtd::ProbeSet::create(op->ref, op->mesh, ps, lay);
+        op->probe_steps = 0;
+    } catch (const std::invalid_argument& e) {
+        return fail(DGTD_ERR_INVALID, e.what());
+    } catch (const std::exception& e) {
+        return fail(DGTD_ERR_CUDA, e.what());
+    }
+    return DGTD_OK;
+}
+
+int dgtd_op_clear_probes(dgtd_op* op)
+{
+    if (!op) return fail(DGTD_ERR_INVALID, "NULL operator");
+    op->probes.reset();
+    op->probe_steps = 0;
+    return DGTD_OK;
+}
+
+int dgtd_op_probe_reset(dgtd_op* op, void* stream)
+{
+    if (!op) return fail(DGTD_ERR_INVALID, "NULL operator");
+    if (!op->probes) return fail(DGTD_ERR_INVALID, "no probes installed");
+    try {
+        op->probes->reset(static_cast<cudaStream_t>(stream));
+        op->probe_steps = 0;
+    } catch (const std::exception& e) {
+        return fail(DGTD_ERR_CUDA, e.what());
+    }
+    return DGTD_OK;
+}
+
+int dgtd_op_probe_info(const dgtd_op* op, int64_t* n_surface_nodes, int64_t* n_samples, int64_t* n_records)
+{
+    if (!op) return fail(DGTD_ERR_INVALID, "NULL operator");
+    if (!op->probes) return fail(DGTD_ERR_INVALID, "no probes installed");
+    if (n_surface_nodes) *n_surface_nodes = op->probes->n_surface_nodes();
+    if (n_samples) *n_samples = op->probes->n_samples();
+    if (n_records) *n_records = op->probes->n_records();
+    return DGTD_OK;
+}
+
+int dgtd_op_probe_surface(const dgtd_op* op, double* h_xyz, double* h_normal, double* h_weight)
+{
+    if (!op) return fail(DGTD_ERR_INVALID, "NULL operator");
+    if (!op->probes) return fail(DGTD_ERR_INVALID, "no probes installed");
+    const auto& P = *op->probes;
+    if (h_xyz) std::copy(P.surface_xyz().begin(), P.surface_xyz().end(), h_xyz);
+    if (h_normal) std::copy(P.surface_normal().begin(), P.surface_normal().end(), h_normal);
+    if (h_weight) std::copy(P.surface_weight().begin(), P.surface_weight().end(), h_weight);
+    return DGTD_OK;
+}
+
+int dgtd_op_probe_sample(dgtd_op* op, const void* d_state, double t, void* stream)
+{
+    if (!op || !d_state) return fail(DGTD_ERR_INVALID, "NULL argument");
+    if (!op->probes) return fail(DGTD_ERR_INVALID, "no probes installed");
+    try {
+        op->probes->sample(d_state, t, static_cast<cudaStream_t>(stream));
+        g_launches.fetch_add(1, std::memory_order_relaxed);
+    } catch (const std::exception& e) {
+        return fail(DGTD_ERR_CUDA, e.what());
+    }
+    return DGTD_OK;
+}
+
+int dgtd_op_probe_read(dgtd_op* op, double* h_point_dft, double* h_surface_dft, double* h_series, double* h_series_t,
+                       void* stream)
+{
+    if (!op) return fail(DGTD_ERR_INVALID, "NULL operator");
+    if (!op->probes) return fail(DGTD_ERR_INVALID, "no probes installed");
+    try {
+        op->probes->read(h_point_dft, h_surface_dft, h_series, h_series_t, static_cast<cudaStream_t>(stream));
+    } catch (const std::exception& e) {
+        return fail(DGTD_ERR_CUDA, e.what());
+    }
     return DGTD_OK;
 }
 

@@ -1,0 +1,236 @@
+// C ABI of the JSON-case front end: load a reference case file and run it on the GPU.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cstdio>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/dgtd_gb300.h"
+#include "jsoncase.hpp"
+
+namespace dgtd {
+int set_last_error(int code, const std::string& msg);   // capi.cu
+}
+
+struct dgtd_case {
+    dgtd::Case c;
+};
+
+namespace {
+
+int cfail(int code, const std::string& msg) { return dgtd::set_last_error(code, msg); }
+
+bool unsupported(const std::string& m)
+{
+    return m.find("not supported") != std::string::npos;
+}
+
+// Raises with the library's last error message on a non-OK status.
+void ok(int rc, const char* what)
+{
+    if (rc != DGTD_OK) throw std::runtime_error(std::string(what) + ": " + dgtd_last_error());
+}
+
+}  // namespace
+
+extern "C" {
+
+int dgtd_case_load(const char* json_path, dgtd_case** out)
+{
+    if (!json_path || !out) return cfail(DGTD_ERR_INVALID, "NULL argument");
+    *out = nullptr;
+    try {
+        auto c = std::make_unique<dgtd_case>();
+        c->c = dgtd::load_case(json_path);
+        *out = c.release();
+    } catch (const std::exception& e) {
+        return cfail(unsupported(e.what()) ? DGTD_ERR_UNSUPPORTED : DGTD_ERR_INVALID, e.what());
+    }
+    return DGTD_OK;
+}
+
+void dgtd_case_destroy(dgtd_case* c) { delete c; }
+
+int dgtd_case_get_info(const dgtd_case* cs, dgtd_case_info* info)
+{
+    if (!cs || !info) return cfail(DGTD_ERR_INVALID, "NULL argument");
+    const dgtd::Case& c = cs->c;
+    info->order = c.order;
+    info->integrator = c.integrator;
+    info->alpha = c.alpha;
+    info->time_step = c.dt;
+    info->final_time = c.final_time;
+    info->cfl = c.cfl;
+    info->n_waves = static_cast<int32_t>(c.waves.size());
+    info->n_initial_fields = static_cast<int32_t>(c.initial.size());
+    info->n_point_probes = static_cast<int32_t>(c.point_pos.size() / 3);
+    info->n_surfaces = static_cast<int32_t>(c.surfaces.size());
+    info->n_elements = static_cast<int64_t>(c.elements.size() / 4);
+    info->n_vertices = static_cast<int64_t>(c.vertices.size() / 3);
+    return DGTD_OK;
+}
+
+int dgtd_case_mesh(const dgtd_case* cs, dgtd_mesh_desc* m)
+{
+    if (!cs || !m) return cfail(DGTD_ERR_INVALID, "NULL argument");
+    const dgtd::Case& c = cs->c;
+    *m = dgtd_mesh_desc{};
+    m->dim = 3;
+    m->n_vertices = static_cast<int64_t>(c.vertices.size() / 3);
+    m->vertices = c.vertices.data();
+    m->n_elements = static_cast<int64_t>(c.elements.size() / 4);
+    m->elements = c.elements.data();
+    m->eps_r = c.eps.data();
+    m->mu_r = c.mu.data();
+    m->sigma = c.sigma.data();
+    m->n_bdr_faces = static_cast<int64_t>(c.bdr_codes.size());
+    m->bdr_faces = c.bdr_faces.data();
+    m->bdr_codes = c.bdr_codes.data();
+    m->n_tfsf_faces = static_cast<int64_t>(c.tfsf_faces.size() / 3);
+    m->tfsf_faces = c.tfsf_faces.data();
+    m->n_int_faces = static_cast<int64_t>(c.int_codes.size());
+    m->int_faces = c.int_faces.data();
+    m->int_codes = c.int_codes.data();
+    return DGTD_OK;
+}
+
+int dgtd_case_planewaves(const dgtd_case* cs, dgtd_planewave* out, int32_t capacity)
+{
+    if (!cs || (!out && capacity > 0)) return cfail(DGTD_ERR_INVALID, "NULL argument");
+    const auto& w = cs->c.waves;
+    if (capacity < static_cast<int32_t>(w.size())) return cfail(DGTD_ERR_INVALID, "capacity below the number of plane waves");
+    std::copy(w.begin(), w.end(), out);
+    return DGTD_OK;
+}
+
+int dgtd_case_point_probes(const dgtd_case* cs, double* h_points)
+{
+    if (!cs || !h_points) return cfail(DGTD_ERR_INVALID, "NULL argument");
+    std::copy(cs->c.point_pos.begin(), cs->c.point_pos.end(), h_points);
+    return DGTD_OK;
+}
+
+int dgtd_case_surface(const dgtd_case* cs, int32_t s, int32_t* faces, int64_t* n_faces)
+{
+    if (!cs) return cfail(DGTD_ERR_INVALID, "NULL argument");
+    if (s < 0 || s >= static_cast<int32_t>(cs->c.surfaces.size())) return cfail(DGTD_ERR_INVALID, "no such surface");
+    const auto& f = cs->c.surfaces[s].faces;
+    if (n_faces) *n_faces = static_cast<int64_t>(f.size() / 3);
+    if (faces) std::copy(f.begin(), f.end(), faces);
+    return DGTD_OK;
+}
+
+int dgtd_case_initial_state(const dgtd_case* cs, const double* h_xyz, int64_t n, double* h_state)
+{
+    if (!cs || !h_xyz || !h_state || n < 0) return cfail(DGTD_ERR_INVALID, "bad argument");
+    auto u = dgtd::case_initial_state(cs->c, h_xyz, n);
+    std::copy(u.begin(), u.end(), h_state);
+    return DGTD_OK;
+}
+
+int dgtd_case_run(const dgtd_case* cs, const dgtd_case_run_opts* ro, double* h_state, dgtd_case_result* res)
+{
+    if (!cs) return cfail(DGTD_ERR_INVALID, "NULL case");
+    const dgtd::Case& c = cs->c;
+    if (ro && ro->precision != DGTD_FP64) return cfail(DGTD_ERR_UNSUPPORTED, "cases run on the plain FP64 form");
+    if (ro && ro->n_freqs > 0 && !ro->freqs) return cfail(DGTD_ERR_INVALID, "frequency array missing");
+    if (!(c.final_time >= 0.0)) return cfail(DGTD_ERR_INVALID, "final_time must be >= 0");
+    dgtd_op* op = nullptr;
+    double* d = nullptr;
+    int rc = DGTD_OK;
+    try {
+        dgtd_mesh_desc m;
+        ok(dgtd_case_mesh(cs, &m), "case mesh");
+        dgtd_op_opts o{};
+        o.order = c.order;
+        o.alpha = c.alpha;
+        o.precision = DGTD_FP64;
+        o.batch = 1;
+        ok(dgtd_op_create(&m, &o, &op), "dgtd_op_create");
+        if (!c.waves.empty())
+            ok(dgtd_op_set_planewaves(op, c.waves.data(), static_cast<int32_t>(c.waves.size())), "set_planewaves");
+        double dt = c.dt;
+        if (!(dt > 0.0)) ok(dgtd_op_estimate_dt(op, c.cfl, &dt), "estimate_dt");
+        dgtd_op_info info;
+        ok(dgtd_op_get_info(op, &info), "get_info");
+        const int64_t N = info.ndofs;
+        std::vector<double> xyz(3 * N);
+        ok(dgtd_op_node_coords(op, xyz.data()), "node_coords");
+        std::vector<double> u = dgtd::case_initial_state(c, xyz.data(), N);
+
+        // probes: points at the smallest requested interval, all surfaces in one set
+        const int32_t npts = static_cast<int32_t>(c.point_pos.size() / 3);
+        std::vector<int32_t> faces;
+        for (const auto& s : c.surfaces) faces.insert(faces.end(), s.faces.begin(), s.faces.end());
+        int every = 1;
+        if (npts > 0) every = *std::min_element(c.point_interval.begin(), c.point_interval.end());
+        const int64_t est_steps = dt > 0.0 ? static_cast<int64_t>(c.final_time / dt) + 2 : 2;
+        const bool probes = npts > 0 || !faces.empty();
+        if (probes) {
+            dgtd_probe_spec ps{};
+            ps.n_points = npts;
+            ps.points = c.point_pos.data();
+            ps.n_surface_faces = static_cast<int64_t>(faces.size() / 3);
+            ps.surface_faces = faces.data();
+            ps.n_freqs = ro ? ro->n_freqs : 0;
+            ps.freqs = ro ? ro->freqs : nullptr;
+            ps.every = every;
+            ps.max_records = npts > 0 ? static_cast<int32_t>(std::min<int64_t>(est_steps / every + 2, 1 << 24)) : 0;
+            ok(dgtd_op_set_probes(op, &ps), "set_probes");
+        }
+        const size_t bytes = u.size() * sizeof(double);
+        if (cudaMalloc(&d, bytes) != cudaSuccess) throw std::runtime_error("cudaMalloc of the case state failed");
+        if (cudaMemcpy(d, u.data(), bytes, cudaMemcpyHostToDevice) != cudaSuccess) throw std::runtime_error("H2D failed");
+        const auto t0 = std::chrono::steady_clock::now();
+        double t = 0.0;
+        int64_t steps = 0;
+        while (t <= c.final_time - 1e-8 * dt) {
+            const double h = std::min(dt, c.final_time - t);
+            ok(dgtd_op_step(op, d, t, h, 1, c.integrator, nullptr), "dgtd_op_step");
+            t += h;
+            ++steps;
+        }
+        if (probes && npts > 0 && steps % every != 0) ok(dgtd_op_probe_sample(op, d, t, nullptr), "final probe sample");
+        if (cudaDeviceSynchronize() != cudaSuccess) throw std::runtime_error("device synchronisation failed");
+        const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        if (h_state && cudaMemcpy(h_state, d, bytes, cudaMemcpyDeviceToHost) != cudaSuccess)
+            throw std::runtime_error("D2H failed");
+        int64_t nrec = 0;
+        if (probes) {
+            ok(dgtd_op_probe_info(op, nullptr, nullptr, &nrec), "probe_info");
+            if (ro && ro->out_dir && npts > 0) {
+                std::vector<double> series(static_cast<size_t>(nrec) * npts * 6), times(nrec);
+                ok(dgtd_op_probe_read(op, nullptr, nullptr, series.data(), times.data(), nullptr), "probe_read");
+                for (int32_t k = 0; k < npts; ++k) {
+                    const std::string path = std::string(ro->out_dir) + "/PointProbe" + std::to_string(k) + ".dat";
+                    FILE* f = std::fopen(path.c_str(), "w");
+                    if (!f) throw std::runtime_error("cannot write " + path);
+                    for (int64_t r = 0; r < nrec; ++r) {
+                        const double* v = &series[(static_cast<size_t>(r) * npts + k) * 6];
+                        std::fprintf(f, "%.10e %.10e %.10e %.10e %.10e %.10e %.10e\n", times[r], v[0], v[1], v[2], v[3],
+                                     v[4], v[5]);
+                    }
+                    std::fclose(f);
+                }
+            }
+        }
+        if (res) {
+            res->steps = steps;
+            res->dt = dt;
+            res->final_time = t;
+            res->n_records = nrec;
+            res->seconds = secs;
+        }
+    } catch (const std::exception& e) {
+        rc = cfail(DGTD_ERR_CUDA, e.what());
+    }
+    if (d) cudaFree(d);
+    if (op) dgtd_op_destroy(op);
+    return rc;
+}
+
+}  // extern "C"

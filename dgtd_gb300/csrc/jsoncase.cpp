@@ -1,0 +1,607 @@
+// JSON-case front end (see jsoncase.hpp).
+#include "jsoncase.hpp"
+
+#include <algorithm>
+#include <array>
+#include <cctype>
+#include <cmath>
+#include <cstdlib>
+#include <fstream>
+#include <set>
+#include <sstream>
+#include <stdexcept>
+
+namespace dgtd {
+
+// ============================================================================ JSON
+const Json* Json::find(const std::string& key) const
+{
+    if (type != Object) return nullptr;
+    for (const auto& kv : obj)
+        if (kv.first == key) return &kv.second;
+    return nullptr;
+}
+
+const Json& Json::at(const std::string& key) const
+{
+    const Json* j = find(key);
+    if (!j) throw std::runtime_error("JSON: missing key '" + key + "'");
+    return *j;
+}
+
+double Json::number() const
+{
+    if (type != Number) throw std::runtime_error("JSON: number expected");
+    return num;
+}
+
+int Json::integer() const { return static_cast<int>(std::lround(number())); }
+
+const std::string& Json::string() const
+{
+    if (type != String) throw std::runtime_error("JSON: string expected");
+    return str;
+}
+
+std::vector<double> Json::numbers() const
+{
+    if (type != Array) throw std::runtime_error("JSON: array expected");
+    std::vector<double> v;
+    for (const auto& e : arr) v.push_back(e.number());
+    return v;
+}
+
+namespace {
+
+struct JsonParser {
+    const std::string& s;
+    size_t i = 0;
+    explicit JsonParser(const std::string& t) : s(t) {}
+
+    [[noreturn]] void fail(const std::string& what)
+    {
+        throw std::runtime_error("JSON parse error at offset " + std::to_string(i) + ": " + what);
+    }
+    void ws()
+    {
+        while (i < s.size() && std::isspace(static_cast<unsigned char>(s[i]))) ++i;
+    }
+    bool lit(const char* w)
+    {
+        size_t n = std::char_traits<char>::length(w);
+        if (s.compare(i, n, w) == 0) { i += n; return true; }
+        return false;
+    }
+    Json value()
+    {
+        ws();
+        if (i >= s.size()) fail("unexpected end");
+        Json j;
+        const char c = s[i];
+        if (c == '{') {
+            j.type = Json::Object;
+            ++i; ws();
+            if (i < s.size() && s[i] == '}') { ++i; return j; }
+            for (;;) {
+                ws();
+                if (i >= s.size() || s[i] != '"') fail("object key expected");
+                std::string k = string();
+                ws();
+                if (i >= s.size() || s[i] != ':') fail("':' expected");
+                ++i;
+                j.obj.emplace_back(k, value());
+                ws();
+                if (i < s.size() && s[i] == ',') { ++i; continue; }
+                if (i < s.size() && s[i] == '}') { ++i; return j; }
+                fail("',' or '}' expected");
+            }
+        }
+        if (c == '[') {
+            j.type = Json::Array;
+            ++i; ws();
+            if (i < s.size() && s[i] == ']') { ++i; return j; }
+            for (;;) {
+                j.arr.push_back(value());
+                ws();
+                if (i < s.size() && s[i] == ',') { ++i; continue; }
+                if (i < s.size() && s[i] == ']') { ++i; return j; }
+                fail("',' or ']' expected");
+            }
+        }
+        if (c == '"') { j.type = Json::String; j.str = string(); return j; }
+        if (lit("true")) { j.type = Json::Bool; j.b = true; return j; }
+        if (lit("false")) { j.type = Json::Bool; j.b = false; return j; }
+        if (lit("null")) return j;
+        // number
+        const char* begin = s.c_str() + i;
+        char* end = nullptr;
+        const double v = std::strtod(begin, &end);
+        if (end == begin) fail("value expected");
+        i += static_cast<size_t>(end - begin);
+        j.type = Json::Number;
+        j.num = v;
+        return j;
+    }
+    std::string string()
+    {
+        std::string out;
+        ++i;   // opening quote
+        while (i < s.size() && s[i] != '"') {
+            if (s[i] == '\\') {
+                if (++i >= s.size()) fail("bad escape");
+                const char e = s[i];
+                switch (e) {
+                case 'n': out += '\n'; break;
+                case 't': out += '\t'; break;
+                case 'r': out += '\r'; break;
+                case 'b': out += '\b'; break;
+                case 'f': out += '\f'; break;
+                case 'u': {
+                    if (i + 4 >= s.size()) fail("bad \\u escape");
+                    const int cp = std::stoi(s.substr(i + 1, 4), nullptr, 16);
+                    out += cp < 128 ? static_cast<char>(cp) : '?';
+                    i += 4;
+                    break;
+                }
+                default: out += e; break;
+                }
+                ++i;
+            } else {
+                out += s[i++];
+            }
+        }
+        if (i >= s.size()) fail("unterminated string");
+        ++i;
+        return out;
+    }
+};
+
+}  // namespace
+
+Json parse_json(const std::string& text)
+{
+    JsonParser p(text);
+    Json j = p.value();
+    p.ws();
+    if (p.i != text.size()) p.fail("trailing characters");
+    return j;
+}
+
+// ============================================================================ gmsh 2.2
+GmshMesh read_gmsh22(const std::string& path)
+{
+    std::ifstream f(path);
+    if (!f) throw std::runtime_error("cannot open mesh file " + path);
+    GmshMesh m;
+    std::map<long, int32_t> node_index;
+    std::string line;
+    bool have_format = false, have_nodes = false;
+    while (std::getline(f, line)) {
+        if (line.rfind("$MeshFormat", 0) == 0) {
+            std::getline(f, line);
+            std::istringstream is(line);
+            double ver = 0; int ftype = 0, dsize = 0;
+            is >> ver >> ftype >> dsize;
+            if (std::floor(ver) != 2.0) throw std::runtime_error(path + ": gmsh format " + line + " (2.2 ASCII expected)");
+            if (ftype != 0) throw std::runtime_error(path + ": binary gmsh files are not supported");
+            have_format = true;
+        } else if (line.rfind("$Nodes", 0) == 0) {
+            std::getline(f, line);
+            const long n = std::stol(line);
+            m.xyz.reserve(3 * n);
+            for (long k = 0; k < n; ++k) {
+                std::getline(f, line);
+                std::istringstream is(line);
+                long id; double x, y, z;
+                if (!(is >> id >> x >> y >> z)) throw std::runtime_error(path + ": bad node line: " + line);
+                node_index[id] = static_cast<int32_t>(m.xyz.size() / 3);
+                m.xyz.insert(m.xyz.end(), {x, y, z});
+            }
+            have_nodes = true;
+        } else if (line.rfind("$Elements", 0) == 0) {
+            if (!have_nodes) throw std::runtime_error(path + ": $Elements before $Nodes");
+            std::getline(f, line);
+            const long n = std::stol(line);
+            for (long k = 0; k < n; ++k) {
+                std::getline(f, line);
+                std::istringstream is(line);
+                long id; int type, ntags;
+                if (!(is >> id >> type >> ntags)) throw std::runtime_error(path + ": bad element line: " + line);
+                std::vector<long> tags(ntags);
+                for (auto& t : tags) is >> t;
+                const int phys = ntags > 0 ? static_cast<int>(tags[0]) : 0;
+                auto nodes = [&](int cnt) {
+                    std::vector<int32_t> v(cnt);
+                    for (int q = 0; q < cnt; ++q) {
+                        long nid;
+                        if (!(is >> nid)) throw std::runtime_error(path + ": short element line: " + line);
+                        auto it = node_index.find(nid);
+                        if (it == node_index.end()) throw std::runtime_error(path + ": element references a missing node");
+                        v[q] = it->second;
+                    }
+                    return v;
+                };
+                if (type == 4) {
+                    auto v = nodes(4);
+                    m.tets.insert(m.tets.end(), v.begin(), v.end());
+                    m.tet_tag.push_back(phys);
+                } else if (type == 2) {
+                    auto v = nodes(3);
+                    m.tris.insert(m.tris.end(), v.begin(), v.end());
+                    m.tri_tag.push_back(phys);
+                } else if (type == 11 || type == 29 || type == 9 || type == 20 || type == 21) {
+                    throw std::runtime_error(path + ": curved (high-order) elements are not supported");
+                } else if (type == 15 || type == 1 || type == 8 || type == 26 || type == 27 || type == 28) {
+                    // points and lines: not part of a tetrahedral model
+                } else {
+                    throw std::runtime_error(path + ": unsupported gmsh element type " + std::to_string(type));
+                }
+            }
+        }
+    }
+    if (!have_format) throw std::runtime_error(path + ": no $MeshFormat section");
+    if (m.tets.empty()) throw std::runtime_error(path + ": no tetrahedra (only 3D meshes are supported)");
+    return m;
+}
+
+void refine_uniform(GmshMesh& m)
+{
+    std::map<std::pair<int32_t, int32_t>, int32_t> mid;
+    auto midpoint = [&](int32_t a, int32_t b) {
+        auto key = std::make_pair(std::min(a, b), std::max(a, b));
+        auto it = mid.find(key);
+        if (it != mid.end()) return it->second;
+        const int32_t id = static_cast<int32_t>(m.xyz.size() / 3);
+        for (int d = 0; d < 3; ++d) m.xyz.push_back(0.5 * (m.xyz[3 * a + d] + m.xyz[3 * b + d]));
+        mid[key] = id;
+        return id;
+    };
+    std::vector<int32_t> tets, ttag, tris, rtag;
+    const size_t ne = m.tet_tag.size();
+    for (size_t e = 0; e < ne; ++e) {
+        const int32_t v0 = m.tets[4 * e], v1 = m.tets[4 * e + 1], v2 = m.tets[4 * e + 2], v3 = m.tets[4 * e + 3];
+        const int32_t m01 = midpoint(v0, v1), m02 = midpoint(v0, v2), m03 = midpoint(v0, v3);
+        const int32_t m12 = midpoint(v1, v2), m13 = midpoint(v1, v3), m23 = midpoint(v2, v3);
+        const int32_t kids[8][4] = {{v0, m01, m02, m03}, {m01, v1, m12, m13}, {m02, m12, v2, m23}, {m03, m13, m23, v3},
+                                    // the inner octahedron split along the m02-m13 diagonal
+                                    {m01, m02, m03, m13}, {m01, m02, m12, m13}, {m02, m03, m13, m23},
+                                    {m02, m12, m13, m23}};
+        for (const auto& k : kids) {
+            tets.insert(tets.end(), k, k + 4);
+            ttag.push_back(m.tet_tag[e]);
+        }
+    }
+    const size_t nt = m.tri_tag.size();
+    for (size_t t = 0; t < nt; ++t) {
+        const int32_t a = m.tris[3 * t], b = m.tris[3 * t + 1], c = m.tris[3 * t + 2];
+        const int32_t ab = midpoint(a, b), bc = midpoint(b, c), ca = midpoint(c, a);
+        const int32_t kids[4][3] = {{a, ab, ca}, {ab, b, bc}, {ca, bc, c}, {ab, bc, ca}};
+        for (const auto& k : kids) {
+            tris.insert(tris.end(), k, k + 3);
+            rtag.push_back(m.tri_tag[t]);
+        }
+    }
+    m.tets.swap(tets);
+    m.tet_tag.swap(ttag);
+    m.tris.swap(tris);
+    m.tri_tag.swap(rtag);
+}
+
+// ============================================================================ case
+namespace {
+
+constexpr double kFreeSpaceImpedance = 376.730313668;   // ohm; bulk conductivity S/m -> normalised units
+constexpr double kSpeedOfLight = 299792458.0;           // m/s; modulation frequency Hz -> normalised units
+constexpr double kAutoDelaySigmas = 5.0;                 // automatic plane-wave delay (pulse this many sigmas upstream)
+
+std::string dirname(const std::string& p)
+{
+    const size_t k = p.find_last_of('/');
+    return k == std::string::npos ? std::string(".") : p.substr(0, k);
+}
+
+std::string stem(const std::string& p)
+{
+    size_t a = p.find_last_of('/');
+    a = (a == std::string::npos) ? 0 : a + 1;
+    size_t b = p.find_last_of('.');
+    if (b == std::string::npos || b < a) b = p.size();
+    return p.substr(a, b - a);
+}
+
+std::vector<int> int_list(const Json& j)
+{
+    std::vector<int> v;
+    for (double x : j.numbers()) v.push_back(static_cast<int>(std::lround(x)));
+    return v;
+}
+
+void vec3(const Json& j, double* out)
+{
+    auto v = j.numbers();
+    out[0] = out[1] = out[2] = 0.0;
+    for (size_t d = 0; d < v.size() && d < 3; ++d) out[d] = v[d];
+}
+
+double orient(const double* a, const double* b, const double* c, const double* d)
+{
+    const double u[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]};
+    const double v[3] = {c[0] - a[0], c[1] - a[1], c[2] - a[2]};
+    const double w[3] = {d[0] - a[0], d[1] - a[1], d[2] - a[2]};
+    return u[0] * (v[1] * w[2] - v[2] * w[1]) - u[1] * (v[0] * w[2] - v[2] * w[0]) + u[2] * (v[0] * w[1] - v[1] * w[0]);
+}
+
+}  // namespace
+
+Case load_case(const std::string& json_path)
+{
+    std::ifstream jf(json_path);
+    if (!jf) throw std::runtime_error("cannot open case file " + json_path);
+    std::stringstream buf;
+    buf << jf.rdbuf();
+    const Json J = parse_json(buf.str());
+    Case c;
+    c.dir = dirname(json_path);
+    c.name = stem(json_path);
+
+    // ---- solver options (driver.cpp:644-705)
+    if (const Json* so = J.find("solver_options")) {
+        if (const Json* v = so->find("upwind_alpha")) c.alpha = v->number();
+        if (const Json* v = so->find("time_step")) c.dt = v->number();
+        if (const Json* v = so->find("final_time")) c.final_time = v->number();
+        if (const Json* v = so->find("cfl")) c.cfl = v->number();
+        if (const Json* v = so->find("order")) c.order = v->integer();
+        if (const Json* v = so->find("evolution_operator")) c.evolution_operator = v->string();
+        if (const Json* v = so->find("ode_type")) {
+            const std::string& o = v->string();
+            if (o == "RK4" || o == "rk4") c.integrator = DGTD_RK4;
+            else if (o == "LSERK4" || o == "lserk4") c.integrator = DGTD_LSERK4;
+            else throw std::runtime_error("ode_type '" + o + "' is not supported (RK4, LSERK4)");
+        }
+    }
+    if (c.order < 1 || c.order > 6) throw std::runtime_error("order must be in [1, 6]");
+
+    // ---- mesh (driver.cpp:1063-1188, 1242-1479)
+    const Json& model = J.at("model");
+    GmshMesh g = read_gmsh22(c.dir + "/" + model.at("filename").string());
+    if (const Json* r = model.find("refinement"))
+        for (int k = 0; k < r->integer(); ++k) refine_uniform(g);
+    const int64_t K = static_cast<int64_t>(g.tet_tag.size());
+    c.vertices = g.xyz;
+    c.elements = g.tets;
+    for (int64_t e = 0; e < K; ++e) {
+        int32_t* v = &c.elements[4 * e];
+        const double* X = c.vertices.data();
+        if (orient(X + 3 * v[0], X + 3 * v[1], X + 3 * v[2], X + 3 * v[3]) < 0.0) std::swap(v[2], v[3]);
+    }
+
+    // ---- materials by volume tag (driver.cpp:946-982)
+    std::map<int, std::array<double, 3>> mat;
+    for (const Json& mj : model.at("materials").arr) {
+        std::array<double, 3> em = {1.0, 1.0, 0.0};
+        if (const Json* v = mj.find("relative_permittivity")) em[0] = v->number();
+        if (const Json* v = mj.find("relative_permeability")) em[1] = v->number();
+        if (const Json* v = mj.find("bulk_conductivity")) em[2] = v->number() * kFreeSpaceImpedance;
+        for (int t : int_list(mj.at("tags"))) mat[t] = em;
+    }
+    c.eps.resize(K); c.mu.resize(K); c.sigma.resize(K);
+    for (int64_t e = 0; e < K; ++e) {
+        auto it = mat.find(g.tet_tag[e]);
+        if (it == mat.end())
+            throw std::runtime_error("element attribute " + std::to_string(g.tet_tag[e]) + " has no material in the case");
+        c.eps[e] = it->second[0]; c.mu[e] = it->second[1]; c.sigma[e] = it->second[2];
+    }
+
+    // ---- face -> elements map of the tagged triangles
+    using Key = std::array<int32_t, 3>;
+    auto key_of = [](int32_t a, int32_t b, int32_t d) { Key k{a, b, d}; std::sort(k.begin(), k.end()); return k; };
+    std::map<Key, std::vector<int64_t>> face_elems;
+    for (size_t t = 0; t < g.tri_tag.size(); ++t) face_elems[key_of(g.tris[3 * t], g.tris[3 * t + 1], g.tris[3 * t + 2])];
+    for (int64_t e = 0; e < K; ++e)
+        for (int f = 0; f < 4; ++f) {
+            int32_t v[3]; int q = 0;
+            for (int k = 0; k < 4; ++k) if (k != f) v[q++] = c.elements[4 * e + k];
+            auto it = face_elems.find(key_of(v[0], v[1], v[2]));
+            if (it != face_elems.end()) it->second.push_back(e);
+        }
+    auto barycentre = [&](int64_t e, double* out) {
+        out[0] = out[1] = out[2] = 0.0;
+        for (int k = 0; k < 4; ++k)
+            for (int d = 0; d < 3; ++d) out[d] += 0.25 * c.vertices[3 * c.elements[4 * e + k] + d];
+    };
+
+    // ---- plane waves (driver.cpp:565-609) and their TF/SF surfaces (SubMesher.cpp:677-775)
+    std::set<int> tfsf_tags;
+    if (const Json* srcs = J.find("sources")) {
+        for (const Json& s : srcs->arr) {
+            const std::string& type = s.at("type").string();
+            if (type == "planewave") {
+                const Json& mag = s.at("magnitude");
+                dgtd_planewave w{};
+                vec3(s.at("propagation"), w.propagation);
+                vec3(s.at("polarization"), w.polarization);
+                w.spread = mag.at("spread").number();
+                const double kn = std::sqrt(w.propagation[0] * w.propagation[0] + w.propagation[1] * w.propagation[1] +
+                                            w.propagation[2] * w.propagation[2]);
+                if (!(kn > 0.0)) throw std::runtime_error("plane wave with zero propagation");
+                const double kh[3] = {w.propagation[0] / kn, w.propagation[1] / kn, w.propagation[2] / kn};
+                std::vector<int> tags = s.has("tags") ? int_list(s.at("tags")) : std::vector<int>();
+                if (const Json* m = mag.find("mean")) {
+                    double mv[3];
+                    vec3(*m, mv);
+                    w.mean = mv[0] * kh[0] + mv[1] * kh[1] + mv[2] * kh[2];
+                } else {
+                    // automatic delay: the pulse peak kAutoDelaySigmas sqrt(2) spreads upstream of
+                    // the earliest TF/SF surface element centroid (driver.cpp:455-472, 576-589)
+                    double min_phase = 1e300;
+                    for (size_t t = 0; t < g.tri_tag.size(); ++t) {
+                        if (std::find(tags.begin(), tags.end(), g.tri_tag[t]) == tags.end()) continue;
+                        double ph = 0.0;
+                        for (int d = 0; d < 3; ++d) {
+                            double x = 0.0;
+                            for (int k = 0; k < 3; ++k) x += g.xyz[3 * g.tris[3 * t + k] + d] / 3.0;
+                            ph += x * kh[d];
+                        }
+                        min_phase = std::min(min_phase, ph);
+                    }
+                    if (min_phase == 1e300) min_phase = 0.0;
+                    w.mean = min_phase - kAutoDelaySigmas * w.spread * std::sqrt(2.0);
+                }
+                if (const Json* fr = mag.find("frequency")) w.frequency = fr->number() / kSpeedOfLight;
+                w.batch = 0;
+                c.waves.push_back(w);
+                for (int t : tags) tfsf_tags.insert(t);
+            } else if (type == "initial") {
+                CaseInitialField f;
+                const std::string& ft = s.at("field_type").string();
+                if (ft == "electric") f.field = 0;
+                else if (ft == "magnetic") f.field = 1;
+                else throw std::runtime_error("initial field_type must be electric or magnetic");
+                vec3(s.at("polarization"), f.pol);
+                const Json& mag = s.at("magnitude");
+                const std::string& mt = mag.at("type").string();
+                if (mt == "gaussian") {
+                    f.kind = 0;
+                    f.spread = mag.at("spread").number();
+                    vec3(s.at("center"), f.center);
+                    f.dimension = s.has("dimension") ? s.at("dimension").integer() : 1;
+                    if (f.dimension < 1 || f.dimension > 3) throw std::runtime_error("gaussian dimension must be 1..3");
+                } else if (mt == "resonant") {
+                    f.kind = 1;
+                    f.modes = int_list(mag.at("modes"));
+                } else {
+                    throw std::runtime_error("initial field magnitude '" + mt + "' is not supported (gaussian, resonant)");
+                }
+                c.initial.push_back(f);
+            } else {
+                throw std::runtime_error("source type '" + type + "' is not supported (initial, planewave)");
+            }
+        }
+    }
+    if (!tfsf_tags.empty()) {
+        // total-field side: the element whose barycentre is closer to the centroid of the
+        // TF/SF surface vertices; the winding normal of each face points into it
+        double cen[3] = {0, 0, 0};
+        std::set<int32_t> verts;
+        for (size_t t = 0; t < g.tri_tag.size(); ++t)
+            if (tfsf_tags.count(g.tri_tag[t]))
+                for (int k = 0; k < 3; ++k) verts.insert(g.tris[3 * t + k]);
+        for (int32_t v : verts)
+            for (int d = 0; d < 3; ++d) cen[d] += g.xyz[3 * v + d] / static_cast<double>(verts.size());
+        for (size_t t = 0; t < g.tri_tag.size(); ++t) {
+            if (!tfsf_tags.count(g.tri_tag[t])) continue;
+            int32_t a = g.tris[3 * t], b = g.tris[3 * t + 1], d = g.tris[3 * t + 2];
+            const auto& el = face_elems[key_of(a, b, d)];
+            if (el.size() != 2) throw std::runtime_error("TF/SF surface faces must lie between two elements");
+            double b0[3], b1[3];
+            barycentre(el[0], b0);
+            barycentre(el[1], b1);
+            double d0 = 0, d1 = 0;
+            for (int q = 0; q < 3; ++q) { d0 += (b0[q] - cen[q]) * (b0[q] - cen[q]); d1 += (b1[q] - cen[q]) * (b1[q] - cen[q]); }
+            const double* tf = d0 < d1 ? b0 : b1;
+            const double* A = &c.vertices[3 * a];
+            const double* B = &c.vertices[3 * b];
+            const double* D = &c.vertices[3 * d];
+            if (orient(A, B, D, tf) < 0.0) std::swap(b, d);
+            c.tfsf_faces.insert(c.tfsf_faces.end(), {a, b, d});
+        }
+    }
+
+    // ---- boundaries by surface tag (driver.cpp:1005-1049)
+    std::map<int, int> bc_of_tag;
+    if (const Json* bs = model.find("boundaries")) {
+        for (const Json& bj : bs->arr) {
+            const std::string& type = bj.at("type").string();
+            int code;
+            if (type == "PEC") code = DGTD_BC_PEC;
+            else if (type == "PMC") code = DGTD_BC_PMC;
+            else if (type == "SMA") code = DGTD_BC_SMA;
+            else throw std::runtime_error("boundary type '" + type + "' is not supported (PEC, PMC, SMA)");
+            for (int t : int_list(bj.at("tags"))) bc_of_tag[t] = code;
+        }
+    }
+    for (size_t t = 0; t < g.tri_tag.size(); ++t) {
+        const int tag = g.tri_tag[t];
+        auto it = bc_of_tag.find(tag);
+        if (it == bc_of_tag.end()) continue;
+        const int32_t a = g.tris[3 * t], b = g.tris[3 * t + 1], d = g.tris[3 * t + 2];
+        const auto& el = face_elems[key_of(a, b, d)];
+        if (el.size() == 1) {
+            c.bdr_faces.insert(c.bdr_faces.end(), {a, b, d});
+            c.bdr_codes.push_back(it->second);
+        } else if (el.size() == 2) {
+            c.int_faces.insert(c.int_faces.end(), {a, b, d});
+            c.int_codes.push_back(it->second);
+        } else {
+            throw std::runtime_error("tagged surface triangle is not a face of the tetrahedral mesh");
+        }
+    }
+
+    // ---- probes (driver.cpp:707-868)
+    auto interval_of = [&](const Json& pj) {
+        if (const Json* st = pj.find("steps")) return std::max(1, st->integer());
+        if (const Json* sv = pj.find("saves")) {
+            // a number of saves over the run: interval = steps / saves (driver.cpp:718-733)
+            const double dt = c.dt > 0.0 ? c.dt : 1.0;
+            const long steps = std::lround(c.final_time / dt);
+            return std::max<int>(1, static_cast<int>(steps / std::max(1, sv->integer())));
+        }
+        return 1;
+    };
+    if (const Json* pr = J.find("probes")) {
+        if (const Json* pts = pr->find("point"))
+            for (const Json& pj : pts->arr) {
+                double x[3];
+                vec3(pj.at("position"), x);
+                c.point_pos.insert(c.point_pos.end(), {x[0], x[1], x[2]});
+                c.point_interval.push_back(interval_of(pj));
+            }
+        for (const char* kind : {"rcssurface", "farfield"})
+            if (const Json* surf = pr->find(kind))
+                for (const Json& sj : surf->arr) {
+                    CaseSurface s;
+                    s.name = sj.has("name") ? sj.at("name").string() : std::string(kind);
+                    s.interval = interval_of(sj);
+                    if (sj.has("tags")) s.tags = int_list(sj.at("tags"));
+                    // orient each face away from the centroid of the surface's vertices
+                    double cen[3] = {0, 0, 0};
+                    std::set<int32_t> verts;
+                    for (size_t t = 0; t < g.tri_tag.size(); ++t)
+                        if (std::find(s.tags.begin(), s.tags.end(), g.tri_tag[t]) != s.tags.end())
+                            for (int k = 0; k < 3; ++k) verts.insert(g.tris[3 * t + k]);
+                    for (int32_t v : verts)
+                        for (int d = 0; d < 3; ++d) cen[d] += g.xyz[3 * v + d] / static_cast<double>(verts.size());
+                    for (size_t t = 0; t < g.tri_tag.size(); ++t) {
+                        if (std::find(s.tags.begin(), s.tags.end(), g.tri_tag[t]) == s.tags.end()) continue;
+                        int32_t a = g.tris[3 * t], b = g.tris[3 * t + 1], d = g.tris[3 * t + 2];
+                        if (orient(&c.vertices[3 * a], &c.vertices[3 * b], &c.vertices[3 * d], cen) > 0.0) std::swap(b, d);
+                        s.faces.insert(s.faces.end(), {a, b, d});
+                    }
+                    c.surfaces.push_back(s);
+                }
+    }
+    return c;
+}
+
+std::vector<double> case_initial_state(const Case& c, const double* xyz, int64_t n)
+{
+    std::vector<double> u(6 * static_cast<size_t>(n), 0.0);
+    for (const auto& f : c.initial) {
+        for (int64_t i = 0; i < n; ++i) {
+            const double p[3] = {xyz[i], xyz[n + i], xyz[2 * n + i]};
+            double v;
+            if (f.kind == 0) {
+                double r2 = 0.0;
+                for (int d = 0; d < f.dimension; ++d) r2 += (p[d] - f.center[d]) * (p[d] - f.center[d]);
+                v = std::exp(-r2 / (2.0 * f.spread * f.spread));
+            } else {
+                v = 1.0;
+                for (size_t d = 0; d < f.modes.size() && d < 3; ++d) v *= std::sin(f.modes[d] * M_PI * p[d]);
+            }
+            for (int k = 0; k < 3; ++k) u[(3 * f.field + k) * static_cast<size_t>(n) + i] += v * f.pol[k];
+        }
+    }
+    return u;
+}
+
+}  // namespace dgtd

@@ -1,0 +1,105 @@
+// JSON-case front end: the reference's case files (src/driver/driver.cpp,
+// buildSolverJson :1545 and the parsers it calls, :531-705, :707-868, :946-1060)
+// read into the flat mesh / options / sources / probes tables of this library.
+//
+// Supported: gmsh 2.2 ASCII meshes with first-order tetrahedra (physical tags
+// as attributes), uniform refinement, materials by volume tag (relative
+// permittivity / permeability / bulk conductivity in S/m), PEC / PMC / SMA
+// boundaries by surface tag (interior when the tagged faces lie between two
+// elements), Gaussian and resonant-mode initial fields, Gaussian and modulated
+// Gaussian plane waves on a tagged TF/SF surface (explicit or automatic delay),
+// point probes and near-to-far ("rcssurface" / "farfield") surfaces by tag.
+// Rejected with a clear error: SGBC boundaries, dipole and Bessel sources,
+// curved (second-order) elements, 1D/2D meshes.
+#pragma once
+#include <cstdint>
+#include <map>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "../../include/dgtd_gb300.h"
+
+namespace dgtd {
+
+// Minimal JSON value (objects keep insertion order).
+struct Json {
+    enum Type { Null, Bool, Number, String, Array, Object } type = Null;
+    bool b = false;
+    double num = 0.0;
+    std::string str;
+    std::vector<Json> arr;
+    std::vector<std::pair<std::string, Json>> obj;
+
+    const Json* find(const std::string& key) const;
+    bool has(const std::string& key) const { return find(key) != nullptr; }
+    const Json& at(const std::string& key) const;   // throws if missing
+    double number() const;
+    int integer() const;
+    const std::string& string() const;
+    std::vector<double> numbers() const;             // array of numbers
+};
+
+Json parse_json(const std::string& text);
+
+struct GmshMesh {
+    std::vector<double> xyz;           // [nv][3]
+    std::vector<int32_t> tets;         // [ne][4] vertex indices
+    std::vector<int32_t> tet_tag;      // physical tag per tet
+    std::vector<int32_t> tris;         // [nt][3]
+    std::vector<int32_t> tri_tag;
+};
+
+GmshMesh read_gmsh22(const std::string& path);
+// One level of uniform refinement: every tetrahedron into 8 (edge midpoints), every
+// tagged triangle into 4, tags inherited.
+void refine_uniform(GmshMesh& m);
+
+struct CaseInitialField {
+    int field = 0;                  // 0 electric, 1 magnetic
+    int kind = 0;                   // 0 gaussian, 1 resonant mode
+    double spread = 0.1;
+    double center[3] = {0, 0, 0};
+    double pol[3] = {0, 0, 1};
+    int dimension = 1;
+    std::vector<int> modes;
+};
+
+struct CaseSurface {
+    std::string name;
+    std::vector<int> tags;
+    int interval = 1;
+    std::vector<int32_t> faces;     // [n][3], winding normal pointing away from the region the surface encloses
+};
+
+struct Case {
+    std::string dir, name;
+    int order = 3;
+    double alpha = 1.0;
+    double dt = 0.0;                // 0: estimate from cfl
+    double final_time = 0.0;
+    double cfl = 1.0;
+    int integrator = DGTD_RK4;
+    std::string evolution_operator = "global";
+    // mesh
+    std::vector<double> vertices;
+    std::vector<int32_t> elements;
+    std::vector<double> eps, mu, sigma;
+    std::vector<int32_t> bdr_faces, bdr_codes, tfsf_faces, int_faces, int_codes;
+    // sources
+    std::vector<dgtd_planewave> waves;
+    std::vector<CaseInitialField> initial;
+    // probes
+    std::vector<double> point_pos;  // [n][3]
+    std::vector<int> point_interval;
+    std::vector<CaseSurface> surfaces;
+};
+
+Case load_case(const std::string& json_path);
+
+// Initial field at the nodes (reference SourcesManager::setInitialFields,
+// src/solver/SourcesManager.cpp:16-36: nodal projection of InitialField::eval,
+// src/components/Sources.cpp:37-57). xyz is [3][n]; returns [6][n].
+std::vector<double> case_initial_state(const Case& c, const double* xyz, int64_t n);
+
+}  // namespace dgtd

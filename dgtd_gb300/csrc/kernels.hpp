@@ -30,42 +30,52 @@ enum StageMode : int {
     MODE_LSRK = 5,     // res = a res + dt k ; u_out = u_in + b res      (in = u_in)
 };
 
-struct TablesDev {
+// Per-mesh device tables of the plain (thread-per-node) form, in the arithmetic
+// type R of that form: double for the FP64 form, float for the single-instance
+// FP32 form.
+template <typename R>
+struct TablesT {
     int p, Np, Nfp;
     int64_t K;
     int64_t N;                 // K * Np
-    const double* DrT;         // [Np][Np] transposed
-    const double* DsT;
-    const double* DtT;
-    const double* LIFTT;       // [4 Nfp][Np] transposed
+    const R* DrT;              // [Np][Np] transposed
+    const R* DsT;
+    const R* DtT;
+    const R* LIFTT;            // [4 Nfp][Np] transposed
     const int* Fmask;          // [4][Nfp]
-    const double* geo;         // [K][9]
-    const double* fgeo;        // [K][16]
-    const double* mat;         // [K][3]
+    const R* geo;              // [K][9]
+    const R* fgeo;             // [K][16]
+    const R* mat;              // [K][3]
     const int32_t* vmapP;      // [K][4][Nfp]
     const int32_t* fcode;      // [K][4]
-    const double* xyz;         // [3][N]
+    const R* xyz;              // [3][N]
     const int32_t* tfsf_elems; // [n_tfsf_elems]
     int64_t n_tfsf_elems;
-    double alpha;
+    R alpha;
 };
 
-struct StageArgs {
-    const double* in;    // [B][6][N]
-    double* out;         // MULT output
-    double* x;           // RK4 base state
-    double* yout;        // RK4 stage output
-    double* z;           // RK4 accumulator
-    double* res;         // LSRK residual
+template <typename R>
+struct StageArgsT {
+    const R* in;         // [B][6][N]
+    R* out;              // MULT output
+    R* x;                // RK4 base state
+    R* yout;             // RK4 stage output
+    R* z;                // RK4 accumulator
+    R* res;              // LSRK residual
     double t;            // stage time
-    double dt;
-    double a, b;         // LSRK coefficients
+    R dt;
+    R a, b;              // LSRK coefficients
     int mode;
     int batch;           // B
     const PlaneWaveDev* pw;
     int n_pw;
     const int* skip;     // [B] TF/SF skip flags (nullptr: never skip)
 };
+
+using TablesDev = TablesT<double>;
+using StageArgs = StageArgsT<double>;
+using TablesF32 = TablesT<float>;
+using StageArgsF32 = StageArgsT<float>;
 
 // Launch the fused FP64 RHS + stage-update kernel for one stage.
 cudaError_t launch_stage_fp64(const TablesDev& T, const StageArgs& A, cudaStream_t s);
@@ -77,5 +87,14 @@ cudaError_t launch_tfsf_skip(const TablesDev& T, const PlaneWaveDev* pw, int n_p
 
 // Squared L2 norm of each incidence's state: out[b] = sum_i in[b][i]^2.
 cudaError_t launch_norm2(const double* in, int64_t n_per_batch, int batch, double* out, cudaStream_t s);
+
+// Single-instance FP32 form (single_f32.cu): the same fused stage in FP32 on the
+// reference layout, one thread per node.
+cudaError_t launch_stage_f32s(const TablesF32& T, const StageArgsF32& A, cudaStream_t s);
+cudaError_t launch_tfsf_skip_f32s(const TablesF32& T, const PlaneWaveDev* pw, int n_pw, int batch, double t, int* skip,
+                                  cudaStream_t s);
+cudaError_t launch_norm2_f32s(const float* in, int64_t n_per_batch, int batch, double* out, cudaStream_t s);
+cudaError_t launch_convert_f64_to_f32(const double* in, float* out, int64_t n, cudaStream_t s);
+cudaError_t launch_convert_f32_to_f64(const float* in, double* out, int64_t n, cudaStream_t s);
 
 }  // namespace dgtd

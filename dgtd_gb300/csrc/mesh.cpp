@@ -243,6 +243,8 @@ MeshTables build_tables(const MeshInput& in, const RefTet& ref)
                 out[a] = static_cast<int32_t>(en * Np + ref.Fmask[fn * Nfp + best]);
             }
         }
+    T.elem_vertices = in.elements;
+    T.vertices = in.vertices;
     return T;
 }
 

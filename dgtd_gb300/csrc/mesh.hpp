@@ -54,6 +54,8 @@ struct MeshTables {
     std::vector<int32_t> fcode;         // [K][Nfaces]
     std::vector<int32_t> nbr;           // [K][Nfaces] neighbour element or -1
     std::vector<int32_t> tfsf_elems;    // elements adjacent to a TF/SF face (unique, ascending)
+    std::vector<int32_t> elem_vertices; // [K][4] vertex ids (input order)
+    std::vector<double> vertices;       // [nv][3]
     double min_edge = 0.0;              // smallest edge length
     double dt_scale_min = 0.0;          // min over elements of vol / (sum of face areas / 2)
 };

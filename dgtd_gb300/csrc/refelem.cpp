@@ -226,6 +226,7 @@ RefTet build_ref_tet(int p)
             }
     std::vector<double> Vinv = V;
     if (!invert_matrix(Vinv, Np)) throw std::runtime_error("singular tet Vandermonde");
+    T.Vinv = Vinv;
     T.Dr.resize(Np * Np); T.Ds.resize(Np * Np); T.Dt.resize(Np * Np);
     matmul(Vr.data(), Vinv.data(), T.Dr.data(), Np, Np, Np);
     matmul(Vs.data(), Vinv.data(), T.Ds.data(), Np, Np, Np);
@@ -254,6 +255,7 @@ RefTet build_ref_tet(int p)
 
     // Emat: reference-triangle (area 2) mass of each face's nodal basis.
     std::vector<double> Emat(static_cast<size_t>(Np) * 4 * Nfp, 0.0);
+    T.face_w.assign(4 * Nfp, 0.0);
     for (int f = 0; f < 4; ++f) {
         int verts[3], c = 0;
         for (int v = 0; v < 4; ++v) if (v != f) verts[c++] = v;
@@ -275,12 +277,29 @@ RefTet build_ref_tet(int p)
             }
         if (!invert_matrix(VVt, Nfp)) throw std::runtime_error("singular face Vandermonde");
         for (int a = 0; a < Nfp; ++a)
-            for (int b = 0; b < Nfp; ++b)
+            for (int b = 0; b < Nfp; ++b) {
                 Emat[static_cast<size_t>(T.Fmask[f * Nfp + a]) * 4 * Nfp + f * Nfp + b] = VVt[a * Nfp + b];
+                T.face_w[f * Nfp + a] += VVt[a * Nfp + b];   // row sum of the face mass = quadrature weight
+            }
     }
     T.LIFT.resize(static_cast<size_t>(Np) * 4 * Nfp);
     matmul(T.Minv.data(), Emat.data(), T.LIFT.data(), Np, Np, 4 * Nfp);
     return T;
+}
+
+void nodal_basis_at(const RefTet& T, double r, double s, double t, double* phi)
+{
+    const int p = T.p, Np = T.Np;
+    std::vector<double> psi(Np);
+    int m = 0;
+    for (int i = 0; i <= p; ++i)
+        for (int j = 0; i + j <= p; ++j)
+            for (int k = 0; i + j + k <= p; ++k) psi[m++] = simplex3d(r, s, t, i, j, k);
+    for (int n = 0; n < Np; ++n) {
+        double acc = 0.0;
+        for (int q = 0; q < Np; ++q) acc += T.Vinv[static_cast<size_t>(q) * Np + n] * psi[q];
+        phi[n] = acc;
+    }
 }
 
 RefSeg build_ref_seg(int p)

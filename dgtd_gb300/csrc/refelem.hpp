@@ -38,6 +38,8 @@ struct RefTet {
     std::vector<double> Minv;             // [Np][Np] inverse mass on the (-1,1) tet
     std::vector<double> LIFT;             // [Np][4*Nfp]
     std::vector<int> Fmask;               // [4][Nfp] volume node of each face node
+    std::vector<double> Vinv;             // [Np][Np] inverse Vandermonde (modal <- nodal)
+    std::vector<double> face_w;           // [4][Nfp] face-node quadrature weights on a reference face of area 2
 };
 
 struct RefSeg {
@@ -48,6 +50,10 @@ struct RefSeg {
 };
 
 RefTet build_ref_tet(int p);
+
+// Values of the Np nodal basis functions at reference point (r, s, t) (Hesthaven
+// coordinates): phi_n = sum_m Vinv[m][n] psi_m(r, s, t).
+void nodal_basis_at(const RefTet& T, double r, double s, double t, double* phi);
 RefSeg build_ref_seg(int p);
 
 inline int tet_np(int p) { return (p + 1) * (p + 2) * (p + 3) / 6; }

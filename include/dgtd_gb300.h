@@ -192,6 +192,100 @@ int dgtd_op_norm2(dgtd_op* op, const void* d_state, double* h_out, void* stream)
  * (estimateTimeStep, Solver.cpp:289-300, 349-351) at the given cfl. */
 int dgtd_op_estimate_dt(const dgtd_op* op, double cfl, double* dt_out);
 
+/* ---- probes: point probes and running FP64 DFT accumulators ---------------------
+ *
+ * Replace the reference's point probes (PointProbe, src/components/Probes.h:132-160;
+ * ProbesManager::updateProbe, src/solver/ProbesManager.cpp:380-405) and the DFT of
+ * exported surface snapshots done by the near-to-far post-processor
+ * (RCSSurfacePostProcessor.cpp:274-300). Sums are accumulated on the device in
+ * FP64 after every `every`-th step of dgtd_op_step, or by dgtd_op_probe_sample:
+ *   S(f) = sum_n u(t_n) exp(-i 2 pi f t_n)      (the reference divides by the sample count)
+ * for every field component of every point probe and surface node. */
+typedef struct dgtd_probe_spec {
+    int32_t n_points;
+    const double* points;          /* [n_points][3]; each must lie in the mesh */
+    int64_t n_surface_faces;
+    const int32_t* surface_faces;  /* [n][3] vertex ids of mesh faces (near-to-far surface);
+                                      winding normal points out of the enclosed region */
+    int32_t n_freqs;               /* 0..64 */
+    const double* freqs;           /* cycles per unit time */
+    int32_t every;                 /* dgtd_op_step samples after every `every`-th step (>= 1) */
+    int32_t max_records;           /* point time-series capacity in samples (0: no series) */
+} dgtd_probe_spec;
+
+/* Install probes (replaces earlier ones; sums start at zero; the step counter restarts). */
+int dgtd_op_set_probes(dgtd_op* op, const dgtd_probe_spec* spec);
+int dgtd_op_clear_probes(dgtd_op* op);
+/* Zero the sums and the time series. */
+int dgtd_op_probe_reset(dgtd_op* op, void* stream);
+int dgtd_op_probe_info(const dgtd_op* op, int64_t* n_surface_nodes, int64_t* n_samples, int64_t* n_records);
+/* Surface nodes: coordinates [n][3], unit outward normals [n][3], quadrature weights [n]
+ * (sum of the weights = surface area). Any pointer may be NULL. */
+int dgtd_op_probe_surface(const dgtd_op* op, double* h_xyz, double* h_normal, double* h_weight);
+/* Add one sample of a working state (device) at time t. */
+int dgtd_op_probe_sample(dgtd_op* op, const void* d_state, double t, void* stream);
+/* Read (synchronising `stream`): point sums [B][n_points][6][n_freqs][2] (re, im),
+ * surface sums [B][n_surface_nodes][6][n_freqs][2], point series [n_records][B][n_points][6]
+ * and its times [n_records]. Any pointer may be NULL. */
+int dgtd_op_probe_read(dgtd_op* op, double* h_point_dft, double* h_surface_dft, double* h_series, double* h_series_t,
+                       void* stream);
+
+/* ---- JSON cases --------------------------------------------------------------
+ *
+ * The reference's case files (driver::buildSolverJson, src/driver/driver.cpp:1545:
+ * solver_options, model {filename (gmsh 2.2 ASCII), refinement, materials,
+ * boundaries}, sources {initial, planewave}, probes {point, rcssurface, farfield})
+ * loaded into this library's tables. Unsupported features (SGBC, dipoles,
+ * curved elements, 1D/2D meshes) are rejected with DGTD_ERR_UNSUPPORTED. */
+typedef struct dgtd_case dgtd_case;
+
+typedef struct dgtd_case_info {
+    int32_t order;
+    int32_t integrator;          /* DGTD_RK4 / DGTD_LSERK4 (solver_options.ode_type) */
+    double alpha;
+    double time_step;            /* 0: estimated from cfl */
+    double final_time;
+    double cfl;
+    int32_t n_waves;
+    int32_t n_initial_fields;
+    int32_t n_point_probes;
+    int32_t n_surfaces;
+    int64_t n_elements;
+    int64_t n_vertices;
+} dgtd_case_info;
+
+typedef struct dgtd_case_run_opts {
+    int32_t precision;           /* DGTD_FP64 (the plain form) */
+    const double* freqs;         /* DFT frequencies of the point probes and surfaces (may be NULL) */
+    int32_t n_freqs;
+    const char* out_dir;         /* if not NULL: PointProbe<k>.dat files (t Ex Ey Ez Hx Hy Hz) */
+} dgtd_case_run_opts;
+
+typedef struct dgtd_case_result {
+    int64_t steps;
+    double dt;
+    double final_time;
+    int64_t n_records;           /* point-probe samples recorded */
+    double seconds;              /* wall time of the time loop */
+} dgtd_case_result;
+
+/* Read a case file and its mesh. */
+int dgtd_case_load(const char* json_path, dgtd_case** out);
+void dgtd_case_destroy(dgtd_case* c);
+int dgtd_case_get_info(const dgtd_case* c, dgtd_case_info* info);
+/* Views into the case's tables (valid while the case lives). */
+int dgtd_case_mesh(const dgtd_case* c, dgtd_mesh_desc* mesh);
+int dgtd_case_planewaves(const dgtd_case* c, dgtd_planewave* out, int32_t capacity);
+int dgtd_case_point_probes(const dgtd_case* c, double* h_points);
+/* Surface s: its faces [n][3] (winding normal outwards); *n_faces gets the count (faces may be NULL). */
+int dgtd_case_surface(const dgtd_case* c, int32_t s, int32_t* faces, int64_t* n_faces);
+/* Initial fields at given nodes: h_xyz [3][n] -> h_state [6][n] (nodal projection). */
+int dgtd_case_initial_state(const dgtd_case* c, const double* h_xyz, int64_t n, double* h_state);
+/* Run the case to its final time on the GPU (reference Solver::run loop) with
+ * point probes recorded at their intervals; h_state (may be NULL) gets the final
+ * state (reference layout). */
+int dgtd_case_run(const dgtd_case* c, const dgtd_case_run_opts* opts, double* h_state, dgtd_case_result* result);
+
 /* ---- serving: continuous batching of independent solves ------------------------
  *
  * The reference runs one case per process (driver::buildSolverJson +

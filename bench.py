@@ -409,6 +409,85 @@ def run_ours(args, world, rank, local):
     return res
 
 
+# ----------------------------------------------------------------------------- high order (single instance)
+HIGH_ORDER_DESC = ("High-order heterogeneous dielectric: unit cube 32^3 hexes x 6 tets (196,608), p=6 (Np=84), "
+                   "eps_r ~ U[1,4] per element (seed 20261204), mu=1, PEC walls, E = sum of 8 Fourier modes "
+                   "a_m sin(k_m.x + phi_m) with a ~ N(0,1)^3, k_m in pi*{1..3}^3, phi_m ~ U[0,2pi) (seed 20261205), "
+                   "H=0, dt=2e-4, classical RK4; single-instance FP32 form (FP32 SIMT contractions)")
+
+
+def high_order_mesh(n: int):
+    import dgtd_gb300 as dg
+    m = dg.box_mesh((n, n, n))
+    m.eps = np.random.default_rng(20261204).uniform(1.0, 4.0, m.n_elements)
+    return m
+
+
+def high_order_state(xyz: np.ndarray) -> np.ndarray:
+    rng = np.random.default_rng(20261205)
+    E = np.zeros((3, xyz.shape[1]))
+    for _ in range(8):
+        k = np.pi * rng.integers(1, 4, 3)
+        a = rng.standard_normal(3)
+        ph = rng.uniform(0.0, 2.0 * np.pi)
+        E += np.outer(a, np.sin(k @ xyz + ph))
+    return np.concatenate([E.ravel(), np.zeros(3 * xyz.shape[1])])
+
+
+def run_high_order(steps: int, dev) -> dict:
+    """C4 on the single-instance FP32 form: rate, the FP64 form's rate on the same mesh, and the
+    FP32-vs-FP64 error of a reduced mesh (8^3 hexes) over 500 steps."""
+    import torch
+    import dgtd_gb300 as dg
+    dt = 2e-4
+    m = high_order_mesh(32)
+    op = dg.Operator(m, order=6, precision=dg.FP32)
+    x0 = torch.from_numpy(high_order_state(op.node_coords())).to(dev)
+    w = op.new_work(dev)
+    op.pack(x0, w)
+    stream = torch.cuda.current_stream(dev)
+    flush = torch.empty(int(256 * 2 ** 20) // 4, dtype=torch.float32, device=dev)
+    op.step(w, 0.0, dt, 3, stream=stream)
+    torch.cuda.synchronize(dev)
+    n0 = dg.kernel_launches()
+    ms, _ = time_steps(op, w, dt, 3 * dt, steps, stream, flush, dev)
+    launches = dg.kernel_launches() - n0
+    dofs = 6 * op.ndofs
+    step_s = sum(ms) / 1e3 / steps
+    Np, Nfp = op.info["np"], op.info["nfp"]
+    flops = 4 * (6 * Np + 8 * Nfp) * dofs / step_s
+    out = {"workload": HIGH_ORDER_DESC, "elements": m.n_elements, "dofs_per_step": dofs, "steps": steps,
+           "value": dofs / step_s, "unit": UNIT, "ms_per_step": step_s * 1e3, "gpu_launches": launches,
+           "contraction_tflops": flops / 1e12,
+           "hbm_gbs_algorithmic": 16 * 4 * dofs / step_s / 1e9}
+    del w, x0, op
+    torch.cuda.empty_cache()
+    op64 = dg.Operator(m, order=6)
+    x64 = torch.from_numpy(high_order_state(op64.node_coords())).to(dev)
+    op64.step(x64, 0.0, dt, 1, stream=stream)
+    torch.cuda.synchronize(dev)
+    ms64, _ = time_steps(op64, x64, dt, dt, 2, stream, flush, dev)
+    out["plain_fp64"] = {"value": dofs * 2 / (sum(ms64) / 1e3), "ms_per_step": sum(ms64) / 2, "steps": 2}
+    out["speedup_vs_fp64"] = out["value"] / out["plain_fp64"]["value"]
+    del x64, op64
+    torch.cuda.empty_cache()
+    ms_ = high_order_mesh(8)
+    a64 = dg.Operator(ms_, order=6)
+    a32 = dg.Operator(ms_, order=6, precision=dg.FP32)
+    xa = torch.from_numpy(high_order_state(a64.node_coords())).to(dev)
+    wa = a32.new_work(dev)
+    a32.pack(xa, wa)
+    a64.step(xa, 0.0, dt, 500, stream=stream)
+    a32.step(wa, 0.0, dt, 500, stream=stream)
+    back = torch.zeros_like(xa)
+    a32.unpack(wa, back)
+    torch.cuda.synchronize(dev)
+    r, b = xa.cpu().numpy(), back.cpu().numpy()
+    out["accuracy"] = {"rel_l2_vs_fp64": float(np.linalg.norm(b - r) / np.linalg.norm(r)), "steps": 500,
+                       "case": "8^3 hexes x 6 tets, same order, materials and initial field"}
+    return out
+
+
 # ----------------------------------------------------------------------------- serving
 SERVING_DESC = ("Serving stream (reduced C5): Poisson arrivals; each request a box [-1,1]^3 of n^3 hexes x 6 tets, "
                 "n ~ U{4..12}, central PEC cube of round(n/6) hexes (n >= 5), SMA outer boundary, TF/SF box one cell "
@@ -519,6 +598,7 @@ def main():
     ap.add_argument("--no-fp64-compare", action="store_true")
     ap.add_argument("--fp64-steps", type=int, default=3)
     ap.add_argument("--serving-requests", type=int, default=64, help="requests of the serving stream (0: skip)")
+    ap.add_argument("--high-order-steps", type=int, default=10, help="timed steps of the p=6 dielectric (0: skip)")
     ap.add_argument("--serving-rate", type=float, default=4.0, help="Poisson arrival rate of the serving stream (1/s)")
     ap.add_argument("--serving-serial", type=int, default=8, help="requests also run one at a time for comparison")
     args = ap.parse_args()
@@ -573,6 +653,9 @@ def main():
         line["plain_fp64"] = r["plain_fp64"]
     if "accuracy" in r:
         line["accuracy"] = r["accuracy"]
+    if args.high_order_steps > 0 and world == 1:
+        import torch
+        line["high_order"] = run_high_order(args.high_order_steps, torch.device("cuda", local))
     if args.serving_requests > 0 and world == 1:
         line["serving"] = run_serving(args.serving_requests, args.serving_rate, args.serving_serial, local)
     print(json.dumps(line), flush=True)

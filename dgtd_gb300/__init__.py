@@ -20,7 +20,7 @@ LIB_PATH = _PKG / "libdgtd_gb300.so"
 
 DGTD_OK = 0
 BC_OPEN, BC_PEC, BC_PMC, BC_SMA = 0, 1, 2, 3
-FP64, FP32_3XTF32 = 0, 1
+FP64, FP32_3XTF32, FP32 = 0, 1, 2
 RK4, LSERK4 = 0, 1
 
 
@@ -146,6 +146,7 @@ SIGNATURES = {
     "dgtd_op_norm2": (C.c_int, [_P, _P, _D, _P]),
     "dgtd_op_set_contraction": (C.c_int, [_P, C.c_int32]),
     "dgtd_op_uses_tensor_cores": (C.c_int, [_P]),
+    "dgtd_op_set_graph_steps": (C.c_int, [_P, C.c_int32]),
     "dgtd_op_check": (C.c_int, [_P, _P]),
     "dgtd_op_estimate_dt": (C.c_int, [_P, C.c_double, _D]),
     "dgtd_box_mesh_size": (C.c_int, [C.POINTER(BoxSpec), _I64, _I64, _I64, _I64]),
@@ -445,6 +446,10 @@ class Operator:
     def set_contraction(self, mode: int) -> None:
         """FP32 batched form: 0 = tensor cores (tcgen05 3xTF32) where supported, 1 = FP32 SIMT."""
         _check(lib().dgtd_op_set_contraction(self._h, int(mode)), "dgtd_op_set_contraction")
+
+    def set_graph_steps(self, steps: int) -> None:
+        """Batched FP32 form: replay blocks of `steps` RK4 steps from one captured CUDA graph (0: off)."""
+        _check(lib().dgtd_op_set_graph_steps(self._h, int(steps)), "dgtd_op_set_graph_steps")
 
     @property
     def uses_tensor_cores(self) -> bool:

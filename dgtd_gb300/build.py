@@ -23,7 +23,8 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompil
               "--expt-relaxed-constexpr", "-I", str(ROOT / "include")]
 
 SOURCES = ["refelem.cpp", "mesh.cpp", "plain_fp64.cu", "batched.cu", "batched_tc.cu", "tc_selftest.cu", "capi.cu",
-           "serve.cu", "probes.cu", "jsoncase.cpp", "case_api.cu"]
+           "serve.cu", "probes.cu", "jsoncase.cpp", "case_api.cu",
+           "single_f32.cu"]
 
 
 def nvcc() -> str:

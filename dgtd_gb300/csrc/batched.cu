@@ -92,7 +92,8 @@ __global__ void __launch_bounds__(kWarps * kLanes) stage_f32(BatchedTables T, Ba
             if (code != 0 && !skip_src) {
                 const float* xq = T.fxyz + ((e * 4 + f) * Nfp + a) * 3;
                 float pe[3], ph[3];
-                pw_eval_f32(A.pw, A.pw_off, b, xq[0], xq[1], xq[2], A.t, pe, ph);
+                const float ts = A.t_base ? static_cast<float>(*A.t_base + static_cast<double>(A.t)) : A.t;
+                pw_eval_f32(A.pw, A.pw_off, b, xq[0], xq[1], xq[2], ts, pe, ph);
                 const float sg = (code == 4) ? 1.0f : -1.0f;
 #pragma unroll
                 for (int c = 0; c < 3; ++c) { dE[c] += sg * pe[c]; dH[c] += sg * ph[c]; }
@@ -214,8 +215,10 @@ __global__ void __launch_bounds__(kWarps * kLanes) stage_f32(BatchedTables T, Ba
 constexpr int kSkipParts = 16;
 
 __global__ void __launch_bounds__(256) tfsf_skip_f32(BatchedTables T, const PlaneWaveF32* pw, const int* pw_off, float t,
-                                                     double* partial, unsigned int* ticket, int* skip)
+                                                     const double* t_base, double* partial, unsigned int* ticket,
+                                                     int* skip)
 {
+    if (t_base) t = static_cast<float>(*t_base + static_cast<double>(t));
     const int b = blockIdx.x, part = blockIdx.y, nparts = gridDim.y;
     const int64_t n = T.n_tfsf_nodes;
     const int64_t lo = n * part / nparts, hi = n * (part + 1) / nparts;
@@ -291,6 +294,11 @@ __global__ void norm2_f32(const float* __restrict__ st, int64_t rows, int Bp, do
     }
     atomicAdd(out + b, acc);
 }
+
+// Device block start time of a graph replay: set before the first replay, advanced by
+// the last node of each replay.
+__global__ void set_time(double* t_dev, double t) { *t_dev = t; }
+__global__ void advance_time(double* t_dev, double dt_block) { *t_dev += dt_block; }
 
 uint64_t morton3(uint32_t x, uint32_t y, uint32_t z)
 {
@@ -437,6 +445,8 @@ std::unique_ptr<BatchedOp> BatchedOp::create(const RefTet& ref, const MeshTables
 
 BatchedOp::~BatchedOp()
 {
+    drop_graph();
+    if (t_dev_) cudaFree(t_dev_);
     for (void* p : allocs_) cudaFree(p);
     if (pw_dev_) cudaFree(pw_dev_);
     if (pw_off_) cudaFree(pw_off_);
@@ -473,10 +483,10 @@ void BatchedOp::set_sources(const std::vector<PlaneWaveDev>& pw)
 
 void BatchedOp::stage(BatchedStageArgs A, double t, cudaStream_t s)
 {
-    A.t = static_cast<float>(t);
+    if (A.t_base == nullptr) A.t = static_cast<float>(t);   // else t is the offset set by the caller
     if (has_tfsf_ && n_pw_ > 0) {
-        tfsf_skip_f32<<<dim3(Bpad_, kSkipParts), 256, 0, s>>>(T_, pw_dev_, pw_off_, static_cast<float>(t),
-                                                             skip_partial_, skip_ticket_, skip_);
+        tfsf_skip_f32<<<dim3(Bpad_, kSkipParts), 256, 0, s>>>(T_, pw_dev_, pw_off_, A.t, A.t_base, skip_partial_,
+                                                             skip_ticket_, skip_);
         ckb(cudaGetLastError(), "tfsf skip kernel");
         ++launches_;
         A.pw = pw_dev_; A.pw_off = pw_off_; A.skip = skip_;
@@ -536,24 +546,90 @@ void BatchedOp::mult(const float* d_in, float* d_out, double t, cudaStream_t s)
     stage(A, t, s);
 }
 
+void BatchedOp::rk4_steps_direct(float* d_x, double t, double dt, int nsteps, cudaStream_t s)
+{
+    const int64_t L = state_len_;
+    float* y0 = ws_;
+    float* y1 = ws_ + L;
+    float* z = ws_ + 2 * L;
+    for (int n = 0; n < nsteps; ++n) {
+        BatchedStageArgs A{};
+        A.dt = static_cast<float>(dt); A.x = d_x; A.z = z;
+        A.mode = MODE_RK4_1; A.in = d_x; A.yout = y0; stage(A, t, s);
+        A.mode = MODE_RK4_2; A.in = y0; A.yout = y1; stage(A, t + dt / 2, s);
+        A.mode = MODE_RK4_3; A.in = y1; A.yout = y0; stage(A, t + dt / 2, s);
+        A.mode = MODE_RK4_4; A.in = y0; A.yout = nullptr; stage(A, t + dt, s);
+        t += dt;
+    }
+}
+
+void BatchedOp::set_graph_steps(int g)
+{
+    if (g < 0) throw std::runtime_error("graph steps must be >= 0");
+    drop_graph();
+    graph_steps_ = g;
+}
+
+void BatchedOp::drop_graph()
+{
+    if (gexec_) cudaGraphExecDestroy(gexec_);
+    gexec_ = nullptr;
+    g_x_ = nullptr;
+}
+
 void BatchedOp::step(float* d_x, double t0, double dt, int nsteps, int integrator, cudaStream_t s)
 {
     ensure_ws();
     const int64_t L = state_len_;
     float* y0 = ws_;
-    float* y1 = ws_ + L;
     float* z = ws_ + 2 * L;
     double t = t0;
     if (integrator == 0) {
-        for (int n = 0; n < nsteps; ++n) {
-            BatchedStageArgs A{};
-            A.dt = static_cast<float>(dt); A.x = d_x; A.z = z;
-            A.mode = MODE_RK4_1; A.in = d_x; A.yout = y0; stage(A, t, s);
-            A.mode = MODE_RK4_2; A.in = y0; A.yout = y1; stage(A, t + dt / 2, s);
-            A.mode = MODE_RK4_3; A.in = y1; A.yout = y0; stage(A, t + dt / 2, s);
-            A.mode = MODE_RK4_4; A.in = y0; A.yout = nullptr; stage(A, t + dt, s);
-            t += dt;
+        const int G = graph_steps_;
+        // blocks of G steps replayed from one captured graph (not on the legacy default stream,
+        // which cannot be captured); the stage times are offsets from the device scalar t_dev_
+        if (G > 0 && s != nullptr && nsteps >= G) {
+            if (gexec_ && (g_x_ != d_x || g_dt_ != dt || g_stream_ != s || g_contraction_ != contraction_)) drop_graph();
+            if (!gexec_) {
+                if (!t_dev_) ckb(cudaMalloc(&t_dev_, sizeof(double)), "cudaMalloc graph time");
+                // one direct step first so that every kernel attribute is set outside the capture
+                rk4_steps_direct(d_x, t, dt, 1, s);
+                t += dt;
+                nsteps -= 1;
+                cudaGraph_t graph = nullptr;
+                ckb(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "graph capture");
+                const int64_t before = launches_;
+                float* y1 = ws_ + L;
+                for (int n = 0; n < G; ++n) {
+                    BatchedStageArgs A{};
+                    A.dt = static_cast<float>(dt); A.x = d_x; A.z = z; A.t_base = t_dev_;
+                    const double tn = n * dt;
+                    A.mode = MODE_RK4_1; A.in = d_x; A.yout = y0; A.t = static_cast<float>(tn); stage(A, 0.0, s);
+                    A.mode = MODE_RK4_2; A.in = y0; A.yout = y1; A.t = static_cast<float>(tn + dt / 2); stage(A, 0.0, s);
+                    A.mode = MODE_RK4_3; A.in = y1; A.yout = y0; A.t = static_cast<float>(tn + dt / 2); stage(A, 0.0, s);
+                    A.mode = MODE_RK4_4; A.in = y0; A.yout = nullptr; A.t = static_cast<float>(tn + dt); stage(A, 0.0, s);
+                }
+                advance_time<<<1, 1, 0, s>>>(t_dev_, G * dt);
+                cudaError_t ce = cudaStreamEndCapture(s, &graph);
+                if (ce != cudaSuccess) throw std::runtime_error(std::string("graph capture: ") + cudaGetErrorString(ce));
+                ce = cudaGraphInstantiate(&gexec_, graph, 0);
+                cudaGraphDestroy(graph);
+                if (ce != cudaSuccess) { gexec_ = nullptr; throw std::runtime_error(std::string("graph instantiate: ") + cudaGetErrorString(ce)); }
+                g_graph_launches_ = launches_ - before + 1;
+                launches_ = before;
+                g_x_ = d_x; g_dt_ = dt; g_stream_ = s; g_contraction_ = contraction_;
+            }
+            set_time<<<1, 1, 0, s>>>(t_dev_, t);
+            ckb(cudaGetLastError(), "set time");
+            ++launches_;
+            while (nsteps >= G) {
+                ckb(cudaGraphLaunch(gexec_, s), "graph launch");
+                launches_ += g_graph_launches_;
+                t += G * dt;
+                nsteps -= G;
+            }
         }
+        rk4_steps_direct(d_x, t, dt, nsteps, s);
     } else {
         float* res = z;
         float* other = y0;

@@ -48,7 +48,8 @@ struct BatchedStageArgs {
     float* yout;
     float* z;
     float* res;
-    float t, dt, a, b;
+    float t, dt, a, b;       // stage time: t, or *t_base + t when t_base is set (CUDA-graph replay)
+    const double* t_base;    // device block start time (graph replay), else nullptr
     int mode;
     const PlaneWaveF32* pw;  // sources sorted by incidence
     const int* pw_off;       // [Bpad + 1]: sources of incidence b are pw[pw_off[b] .. pw_off[b+1])
@@ -81,6 +82,8 @@ public:
     void norm2(const float* d_state, double* d_out_dev, cudaStream_t s);
     // contraction path: 0 = tensor cores (tcgen05, 3xTF32) when supported, 1 = FP32 SIMT
     void set_contraction(int mode) { contraction_ = mode; }
+    // RK4 steps per captured CUDA graph (0: launch every stage directly)
+    void set_graph_steps(int g);
     bool uses_tensor_cores() const { return contraction_ == 0 && tc_supported(T_.p, Bpad_); }
     // reads and clears the device error flag (synchronises the stream)
     int take_status(cudaStream_t s);
@@ -88,6 +91,8 @@ public:
 private:
     void stage(BatchedStageArgs A, double t, cudaStream_t s);
     void ensure_ws();
+    void rk4_steps_direct(float* d_x, double t, double dt, int nsteps, cudaStream_t s);
+    void drop_graph();
 
     BatchedTables T_{};
     int64_t K_ = 0;
@@ -107,6 +112,15 @@ private:
     float* ws_ = nullptr;
     bool has_tfsf_ = false;
     int contraction_ = 0;
+    // CUDA graph of graph_steps_ RK4 steps (stage times relative to the device scalar t_dev_)
+    int graph_steps_ = 0;
+    double* t_dev_ = nullptr;
+    cudaGraphExec_t gexec_ = nullptr;
+    float* g_x_ = nullptr;
+    double g_dt_ = 0.0;
+    cudaStream_t g_stream_ = nullptr;
+    int g_contraction_ = -1;
+    int64_t g_graph_launches_ = 0;   // kernels in one replay
     const uint32_t* op_img_ = nullptr;
     int* status_ = nullptr;
     int n_sm_ = 152;

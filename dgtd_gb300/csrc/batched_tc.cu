@@ -165,6 +165,26 @@ __device__ __forceinline__ void prefetch_item(const BatchedTables& T, const floa
     bulk_g2s(buf + O::UBytes + O::NbrBytes + 64, T.fcode + e * 4, 16, bar);
 }
 
+// The RK registers the epilogue of work item w reads, brought into L2 ahead of
+// use so that its loads wait for L2 rather than HBM (the whole element block,
+// once per element). Issued one item ahead: earlier, the lines are evicted by
+// the other SMs' streams before they are read.
+template <int MODE>
+__device__ __forceinline__ void prefetch_rk_registers(const BatchedStageArgs& A, int64_t w, int nchunk, int64_t EB)
+{
+    const int64_t e = w / nchunk;
+    if (w - e * nchunk != 0) return;
+    const uint32_t eb = static_cast<uint32_t>(EB * sizeof(float));
+    if (MODE == MODE_RK4_2 || MODE == MODE_RK4_3) {
+        prefetch_l2(A.x + e * EB, eb);
+        prefetch_l2(A.z + e * EB, eb);
+    } else if (MODE == MODE_RK4_4) {
+        prefetch_l2(A.z + e * EB, eb);
+    } else if (MODE == MODE_LSRK) {
+        prefetch_l2(A.res + e * EB, eb);
+    }
+}
+
 // Epilogue operand loads of one chunk of kEpiNodes nodes (global, stride Bp between nodes).
 constexpr int kEpiNodes = 8;
 struct EpiOps {
@@ -229,7 +249,8 @@ __device__ __forceinline__ void epi_store(const BatchedStageArgs& A, int64_t bas
 __device__ __forceinline__ void tfsf_source(const BatchedStageArgs& A, const float* xq, int b, int code, float* dE, float* dH)
 {
     float pe[3], ph[3];
-    pw_eval(A.pw, A.pw_off, b, __ldg(xq), __ldg(xq + 1), __ldg(xq + 2), A.t, pe, ph);
+    const float ts = A.t_base ? static_cast<float>(*A.t_base + static_cast<double>(A.t)) : A.t;
+    pw_eval(A.pw, A.pw_off, b, __ldg(xq), __ldg(xq + 1), __ldg(xq + 2), ts, pe, ph);
     const float s2 = (code == 4) ? 1.0f : -1.0f;
 #pragma unroll
     for (int c = 0; c < 3; ++c) { dE[c] += s2 * pe[c]; dH[c] += s2 * ph[c]; }
@@ -471,6 +492,8 @@ __global__ void __launch_bounds__(kThreads, 1)
                 const float fe = (c < 3) ? ie : im, fs = (c < 3) ? se : 0.0f;
                 epi_store<MODE>(A, chunk_base(n), Bp, chunk_nv(n), need_u, kv, fe, fs, dtf, o);
             };
+            if (warp == kEpiWarp0 && lane == 0 && w + gridDim.x < n_work)
+                prefetch_rk_registers<MODE>(A, w + gridDim.x, nchunk, EB);
             EpiOps o0, o1;
             epi_load<MODE>(A, chunk_base(0), Bp, chunk_nv(0), need_u, o0);
             if (flag_set(&s_err) || !tc::mbar_wait(&acc_full[abuf], (it >> 1) & 1)) { err = true; break; }
@@ -542,20 +565,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                 }
                 prefetch_item<P>(T, A.in, w, nchunk, Bp, ubuf0 + ub * O::UBufBytes, &u_full[ub]);
                 if (ub) ++issued1; else ++issued0;
-                // the RK registers the epilogue of this item reads: into L2 now, so that its
-                // loads wait for L2 rather than HBM (whole element block once per element)
-                const int64_t e = w / nchunk;
-                if (w - e * nchunk == 0) {
-                    const uint32_t eb = static_cast<uint32_t>(EB * sizeof(float));
-                    if (MODE == MODE_RK4_2 || MODE == MODE_RK4_3) {
-                        prefetch_l2(A.x + e * EB, eb);
-                        prefetch_l2(A.z + e * EB, eb);
-                    } else if (MODE == MODE_RK4_4) {
-                        prefetch_l2(A.z + e * EB, eb);
-                    } else if (MODE == MODE_LSRK) {
-                        prefetch_l2(A.res + e * EB, eb);
-                    }
-                }
+                if (it == 0) prefetch_rk_registers<MODE>(A, w, nchunk, EB);   // later items: the epilogue
             }
             if (err) {
                 // wait (bounded) for this CTA's copies still in flight

@@ -89,6 +89,9 @@ struct dgtd_op {
     // RK scratch (allocated on first dgtd_op_step)
     double* ws = nullptr;
     int64_t ws_len = 0;
+    // single-instance FP32 form: FP32 copies of the tables, RK scratch
+    dgtd::TablesF32 dev32{};
+    float* ws32 = nullptr;
     // batched FP32 form
     std::unique_ptr<dgtd::BatchedOp> batched;
     // point probes / DFT accumulators, sampled by dgtd_op_step every probes->every() steps
@@ -102,6 +105,7 @@ struct dgtd_op {
         if (skip_dev) cudaFree(skip_dev);
         if (norm_dev) cudaFree(norm_dev);
         if (ws) cudaFree(ws);
+        if (ws32) cudaFree(ws32);
     }
     template <typename T>
     T* up(const std::vector<T>& v)
@@ -244,6 +248,71 @@ void rk_step(dgtd_op* op, double* d_x, double t, double dt, int integrator, doub
     }
 }
 
+// ---- single-instance FP32 form: the same stage sequence on FP32 registers
+void run_stage32(dgtd_op* op, dgtd::StageArgsF32 A, double t, cudaStream_t s)
+{
+    A.t = t;
+    A.batch = op->batch;
+    if (has_sources(op)) {
+        ck(dgtd::launch_tfsf_skip_f32s(op->dev32, op->pw_dev, static_cast<int>(op->pw_host.size()), op->batch, t,
+                                       op->skip_dev, s),
+           "tfsf skip kernel");
+        g_launches.fetch_add(1, std::memory_order_relaxed);
+        A.pw = op->pw_dev;
+        A.n_pw = static_cast<int>(op->pw_host.size());
+        A.skip = op->skip_dev;
+    } else {
+        A.pw = nullptr;
+        A.n_pw = 0;
+        A.skip = nullptr;
+    }
+    ck(dgtd::launch_stage_f32s(op->dev32, A, s), "FP32 stage kernel");
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+}
+
+void ensure_ws32(dgtd_op* op)
+{
+    if (op->ws32) return;
+    ck(cudaMalloc(&op->ws32, 3 * op->state_len * sizeof(float)), "cudaMalloc RK scratch");
+}
+
+void rk_step32(dgtd_op* op, float* d_x, double t, double dt, int integrator, float* lsrk_other, float*& cur,
+               cudaStream_t s)
+{
+    const int64_t L = op->state_len;
+    const float dtf = static_cast<float>(dt);
+    if (integrator == DGTD_RK4) {
+        float* y0 = op->ws32;
+        float* y1 = op->ws32 + L;
+        float* z = op->ws32 + 2 * L;
+        dgtd::StageArgsF32 A{};
+        A.dt = dtf;
+        A.x = d_x;
+        A.z = z;
+        A.mode = dgtd::MODE_RK4_1; A.in = d_x; A.yout = y0; run_stage32(op, A, t, s);
+        A.mode = dgtd::MODE_RK4_2; A.in = y0; A.yout = y1; run_stage32(op, A, t + dt / 2, s);
+        A.mode = dgtd::MODE_RK4_3; A.in = y1; A.yout = y0; run_stage32(op, A, t + dt / 2, s);
+        A.mode = dgtd::MODE_RK4_4; A.in = y0; A.yout = nullptr; run_stage32(op, A, t + dt, s);
+    } else {
+        float* res = op->ws32 + 2 * L;
+        for (int st = 0; st < 5; ++st) {
+            float* nxt = (cur == d_x) ? lsrk_other : d_x;
+            dgtd::StageArgsF32 A{};
+            A.dt = dtf;
+            A.mode = dgtd::MODE_LSRK;
+            A.in = cur;
+            A.yout = nxt;
+            A.res = res;
+            A.a = static_cast<float>(kRk4a[st]);
+            A.b = static_cast<float>(kRk4b[st]);
+            run_stage32(op, A, t + kRk4c[st] * dt, s);
+            cur = nxt;
+        }
+    }
+}
+
+bool ref_layout_fp64(const dgtd_op* op) { return op->precision == DGTD_FP64; }
+
 }  // namespace
 
 extern "C" {
@@ -259,7 +328,7 @@ int dgtd_op_create(const dgtd_mesh_desc* mesh, const dgtd_op_opts* opts, dgtd_op
     if (!opts) return fail(DGTD_ERR_INVALID, "options are NULL");
     if (opts->order < 1 || opts->order > 6) return fail(DGTD_ERR_UNSUPPORTED, "order must be in [1, 6]");
     if (opts->batch < 1) return fail(DGTD_ERR_INVALID, "batch must be >= 1");
-    if (opts->precision != DGTD_FP64 && opts->precision != DGTD_FP32_3XTF32)
+    if (opts->precision != DGTD_FP64 && opts->precision != DGTD_FP32_3XTF32 && opts->precision != DGTD_FP32)
         return fail(DGTD_ERR_INVALID, "unknown precision form");
     if (!(opts->alpha >= 0.0)) return fail(DGTD_ERR_INVALID, "alpha must be >= 0");
     std::unique_ptr<dgtd_op> op;
@@ -299,6 +368,25 @@ int dgtd_op_create(const dgtd_mesh_desc* mesh, const dgtd_op_opts* opts, dgtd_op
         ck(cudaMalloc(&op->skip_dev, op->batch * sizeof(int)), "cudaMalloc skip");
         ck(cudaMalloc(&op->norm_dev, (op->batch + 32) * sizeof(double)), "cudaMalloc norm");
         if (op->precision == DGTD_FP32_3XTF32) op->batched = dgtd::BatchedOp::create(op->ref, op->mesh, op->dev, op->batch);
+        if (op->precision == DGTD_FP32) {
+            auto f32 = [](const std::vector<double>& v) { return std::vector<float>(v.begin(), v.end()); };
+            dgtd::TablesF32& F = op->dev32;
+            F.p = T.p; F.Np = T.Np; F.Nfp = T.Nfp; F.K = T.K; F.N = T.N;
+            F.alpha = static_cast<float>(T.alpha);
+            F.DrT = op->up(f32(transpose(op->ref.Dr, Np, Np)));
+            F.DsT = op->up(f32(transpose(op->ref.Ds, Np, Np)));
+            F.DtT = op->up(f32(transpose(op->ref.Dt, Np, Np)));
+            F.LIFTT = op->up(f32(transpose(op->ref.LIFT, Np, 4 * Nfp)));
+            F.Fmask = T.Fmask;
+            F.geo = op->up(f32(op->mesh.geo));
+            F.fgeo = op->up(f32(op->mesh.fgeo));
+            F.mat = op->up(f32(op->mesh.mat));
+            F.vmapP = T.vmapP;
+            F.fcode = T.fcode;
+            F.xyz = op->up(f32(xyz));
+            F.tfsf_elems = T.tfsf_elems;
+            F.n_tfsf_elems = T.n_tfsf_elems;
+        }
     } catch (const CudaError& e) {
         return fail(DGTD_ERR_CUDA, e.what());
     } catch (const std::bad_alloc&) {
@@ -328,7 +416,7 @@ int dgtd_op_get_info(const dgtd_op* op, dgtd_op_info* info)
     info->dt_scale_min = op->mesh.dt_scale_min;
     info->device_bytes = op->device_bytes + (op->batched ? op->batched->device_bytes() : 0);
     info->work_len = op->batched ? op->batched->state_len() : op->state_len;
-    info->work_word_bytes = op->batched ? 4 : 8;
+    info->work_word_bytes = op->precision == DGTD_FP64 ? 8 : 4;
     info->batch_padded = op->batched ? static_cast<int32_t>(op->batched->state_len() / (op->mesh.K * 6 * op->ref.Np))
                                      : op->batch;
     return DGTD_OK;
@@ -389,6 +477,14 @@ int dgtd_op_mult(dgtd_op* op, const void* d_x, void* d_y, double t, void* stream
             op->batched->mult(static_cast<const float*>(d_x), static_cast<float*>(d_y), t, static_cast<cudaStream_t>(stream));
             return DGTD_OK;
         }
+        if (op->precision == DGTD_FP32) {
+            dgtd::StageArgsF32 A{};
+            A.mode = dgtd::MODE_MULT;
+            A.in = static_cast<const float*>(d_x);
+            A.out = static_cast<float*>(d_y);
+            run_stage32(op, A, t, static_cast<cudaStream_t>(stream));
+            return DGTD_OK;
+        }
         dgtd::StageArgs A{};
         A.mode = dgtd::MODE_MULT;
         A.in = static_cast<const double*>(d_x);
@@ -408,6 +504,9 @@ int dgtd_op_pack(dgtd_op* op, const double* d_ref, void* d_work, void* stream)
         if (op->batched) {
             BatchedCount bc(op);
             op->batched->pack(d_ref, static_cast<float*>(d_work), s);
+        } else if (op->precision == DGTD_FP32) {
+            ck(dgtd::launch_convert_f64_to_f32(d_ref, static_cast<float*>(d_work), op->state_len, s), "pack kernel");
+            g_launches.fetch_add(1, std::memory_order_relaxed);
         } else if (static_cast<const void*>(d_ref) != d_work) {
             ck(cudaMemcpyAsync(d_work, d_ref, op->state_len * sizeof(double), cudaMemcpyDeviceToDevice, s), "copy");
         }
@@ -425,6 +524,9 @@ int dgtd_op_unpack(dgtd_op* op, const void* d_work, double* d_ref, void* stream)
         if (op->batched) {
             BatchedCount bc(op);
             op->batched->unpack(static_cast<const float*>(d_work), d_ref, s);
+        } else if (op->precision == DGTD_FP32) {
+            ck(dgtd::launch_convert_f32_to_f64(static_cast<const float*>(d_work), d_ref, op->state_len, s), "unpack kernel");
+            g_launches.fetch_add(1, std::memory_order_relaxed);
         } else if (d_work != static_cast<const void*>(d_ref)) {
             ck(cudaMemcpyAsync(d_ref, d_work, op->state_len * sizeof(double), cudaMemcpyDeviceToDevice, s), "copy");
         }
@@ -445,8 +547,8 @@ int dgtd_op_mult_host(dgtd_op* op, const double* h_x, double* h_y, double t)
         ck(cudaMalloc(&dx, bytes), "cudaMalloc");
         ck(cudaMalloc(&dy, bytes), "cudaMalloc");
         ck(cudaMemcpy(dx, h_x, bytes, cudaMemcpyHostToDevice), "H2D");
-        if (op->batched) {
-            const size_t wb = op->batched->state_len() * sizeof(float);
+        if (op->precision != DGTD_FP64) {
+            const size_t wb = (op->batched ? op->batched->state_len() : op->state_len) * sizeof(float);
             ck(cudaMalloc(&wx, wb), "cudaMalloc");
             ck(cudaMalloc(&wy, wb), "cudaMalloc");
             rc = dgtd_op_pack(op, dx, wx, nullptr);
@@ -491,6 +593,26 @@ int dgtd_op_step(dgtd_op* op, void* d_work, double t0, double dt, int32_t nsteps
             }
             return DGTD_OK;
         }
+        if (op->precision == DGTD_FP32) {
+            float* d_state = static_cast<float*>(d_work);
+            ensure_ws32(op);
+            float* other = op->ws32;   // LSERK4 second state buffer
+            float* cur = d_state;
+            if (integrator == DGTD_LSERK4)
+                ck(cudaMemsetAsync(op->ws32 + 2 * op->state_len, 0, op->state_len * sizeof(float), s), "memset");
+            double t = t0;
+            for (int i = 0; i < nsteps; ++i) {
+                rk_step32(op, d_state, t, dt, integrator, other, cur, s);
+                t += dt;
+                if (pr && ++op->probe_steps % pr->every() == 0) {
+                    pr->sample(cur, t, s);
+                    g_launches.fetch_add(1, std::memory_order_relaxed);
+                }
+            }
+            if (integrator == DGTD_LSERK4 && cur != d_state)
+                ck(cudaMemcpyAsync(d_state, cur, op->state_len * sizeof(float), cudaMemcpyDeviceToDevice, s), "copy");
+            return DGTD_OK;
+        }
         double* d_state = static_cast<double*>(d_work);
         ensure_ws(op);
         double* other = op->ws;   // LSERK4 second state buffer
@@ -527,8 +649,8 @@ int dgtd_op_run_host(dgtd_op* op, double* h_state, double t0, double dt, double 
     try {
         ck(cudaMalloc(&d, bytes), "cudaMalloc");
         ck(cudaMemcpy(d, h_state, bytes, cudaMemcpyHostToDevice), "H2D");
-        if (op->batched) {
-            ck(cudaMalloc(&w, op->batched->state_len() * sizeof(float)), "cudaMalloc");
+        if (op->precision != DGTD_FP64) {
+            ck(cudaMalloc(&w, (op->batched ? op->batched->state_len() : op->state_len) * sizeof(float)), "cudaMalloc");
             rc = dgtd_op_pack(op, d, w, nullptr);
         } else {
             w = d;
@@ -541,7 +663,7 @@ int dgtd_op_run_host(dgtd_op* op, double* h_state, double t0, double dt, double 
             t += truedt;
             ++steps;
         }
-        if (rc == DGTD_OK && op->batched) rc = dgtd_op_unpack(op, w, d, nullptr);
+        if (rc == DGTD_OK && op->precision != DGTD_FP64) rc = dgtd_op_unpack(op, w, d, nullptr);
         if (rc == DGTD_OK) ck(cudaMemcpy(h_state, d, bytes, cudaMemcpyDeviceToHost), "D2H");
     } catch (const std::exception& e) {
         rc = fail(DGTD_ERR_CUDA, e.what());
@@ -560,6 +682,10 @@ int dgtd_op_norm2(dgtd_op* op, const void* d_state, double* h_out, void* stream)
         if (op->batched) {
             BatchedCount bc(op);
             op->batched->norm2(static_cast<const float*>(d_state), op->norm_dev, s);
+        } else if (op->precision == DGTD_FP32) {
+            ck(dgtd::launch_norm2_f32s(static_cast<const float*>(d_state), op->state_len / op->batch, op->batch,
+                                       op->norm_dev, s), "norm kernel");
+            g_launches.fetch_add(1, std::memory_order_relaxed);
         } else {
             ck(dgtd::launch_norm2(static_cast<const double*>(d_state), op->state_len / op->batch, op->batch,
                                   op->norm_dev, s), "norm kernel");
@@ -578,6 +704,19 @@ int dgtd_op_set_contraction(dgtd_op* op, int32_t mode)
     if (!op) return fail(DGTD_ERR_INVALID, "NULL operator");
     if (mode != 0 && mode != 1) return fail(DGTD_ERR_INVALID, "contraction mode must be 0 or 1");
     if (op->batched) op->batched->set_contraction(mode);
+    return DGTD_OK;
+}
+
+int dgtd_op_set_graph_steps(dgtd_op* op, int32_t steps)
+{
+    if (!op) return fail(DGTD_ERR_INVALID, "NULL operator");
+    if (steps < 0) return fail(DGTD_ERR_INVALID, "graph steps must be >= 0");
+    if (!op->batched) return fail(DGTD_ERR_UNSUPPORTED, "CUDA-graph stepping is implemented for the batched FP32 form");
+    try {
+        op->batched->set_graph_steps(steps);
+    } catch (const std::exception& e) {
+        return fail(DGTD_ERR_CUDA, e.what());
+    }
     return DGTD_OK;
 }
 
@@ -631,6 +770,8 @@ int dgtd_op_set_probes(dgtd_op* op, const dgtd_probe_spec* spec)
             lay.fp32 = true;
             lay.Bp = op->batched->batch_padded();
             lay.inv_perm = op->batched->inv_perm().data();
+        } else if (op->precision == DGTD_FP32) {
+            lay.f32_ref = true;
         }
         op->probes.reset();
         op->probes = dgtd::ProbeSet::create(op->ref, op->mesh, ps, lay);
@@ -887,7 +1028,7 @@ int dgtd_op_step_noalloc(dgtd_op* op, void* d_state, double t0, double dt, int32
     if (!op || !d_state) return fail(DGTD_ERR_INVALID, "NULL argument");
     if (nsteps < 0) return fail(DGTD_ERR_INVALID, "nsteps must be >= 0");
     if (integrator != DGTD_RK4 && integrator != DGTD_LSERK4) return fail(DGTD_ERR_INVALID, "unknown integrator");
-    if (op->batched)
+    if (op->precision != DGTD_FP64)
         return fail(DGTD_ERR_UNSUPPORTED, "dgtd_op_step_noalloc supports the FP64 form only");
     if (op->state_len > kNoAllocMaxState)
         return fail(DGTD_ERR_INVALID, "dgtd_op_step_noalloc: state of " + std::to_string(op->state_len) +

@@ -43,41 +43,46 @@ struct Ord {
     static constexpr int EPB = EPB0 > 32 ? 32 : EPB0;
 };
 
-__device__ __forceinline__ double pw_profile(const PlaneWaveDev& w, double s)
+// The body is written for an arithmetic type R: double (the FP64 form) or float
+// (the single-instance FP32 form). Source parameters are stored in double and
+// evaluated in R.
+template <typename R>
+__device__ __forceinline__ R pw_profile(const PlaneWaveDev& w, R s)
 {
-    double a = s - w.mean;
-    double g = exp(-a * a / (2.0 * w.spread * w.spread));
-    if (w.freq != 0.0) g *= cos(2.0 * M_PI * w.freq * a);
+    R a = s - static_cast<R>(w.mean);
+    const R sp = static_cast<R>(w.spread);
+    R g = exp(-a * a / (R(2) * sp * sp));
+    if (w.freq != 0.0) g *= cos(R(2) * static_cast<R>(M_PI) * static_cast<R>(w.freq) * a);
     return g;
 }
 
 // Sum of the plane waves of incidence b at point x and time t.
-__device__ __forceinline__ void eval_pw(const PlaneWaveDev* pw, int n_pw, int b, double px, double py, double pz,
-                                        double t, double* e, double* h)
+template <typename R>
+__device__ __forceinline__ void eval_pw(const PlaneWaveDev* pw, int n_pw, int b, R px, R py, R pz, R t, R* e, R* h)
 {
-    e[0] = e[1] = e[2] = h[0] = h[1] = h[2] = 0.0;
+    e[0] = e[1] = e[2] = h[0] = h[1] = h[2] = R(0);
     for (int q = 0; q < n_pw; ++q) {
         const PlaneWaveDev& w = pw[q];
         if (w.batch != b) continue;
-        double s = px * w.k[0] + py * w.k[1] + pz * w.k[2] - t;
-        double g = pw_profile(w, s);
-        e[0] += g * w.pol[0]; e[1] += g * w.pol[1]; e[2] += g * w.pol[2];
-        h[0] += g * w.kxp[0]; h[1] += g * w.kxp[1]; h[2] += g * w.kxp[2];
+        R s = px * static_cast<R>(w.k[0]) + py * static_cast<R>(w.k[1]) + pz * static_cast<R>(w.k[2]) - t;
+        R g = pw_profile<R>(w, s);
+        e[0] += g * static_cast<R>(w.pol[0]); e[1] += g * static_cast<R>(w.pol[1]); e[2] += g * static_cast<R>(w.pol[2]);
+        h[0] += g * static_cast<R>(w.kxp[0]); h[1] += g * static_cast<R>(w.kxp[1]); h[2] += g * static_cast<R>(w.kxp[2]);
     }
 }
 
-template <int P>
-__device__ __forceinline__ void stage_body(const TablesDev& T, const StageArgs& A, int64_t e0, int b)
+template <int P, typename R = double>
+__device__ __forceinline__ void stage_body(const TablesT<R>& T, const StageArgsT<R>& A, int64_t e0, int b)
 {
     using O = Ord<P>;
     constexpr int Np = O::Np, Nfp = O::Nfp, NF = O::NF, EPB = O::EPB;
-    __shared__ double s_u[6][EPB * Np];
-    __shared__ double s_f[6][EPB * NF];
+    __shared__ R s_u[6][EPB * Np];
+    __shared__ R s_f[6][EPB * NF];
     __shared__ int s_fmask[4 * Nfp];
 
     const int tid = threadIdx.x;
     const int64_t N = T.N;
-    const double* __restrict__ in = A.in + static_cast<int64_t>(b) * 6 * N;
+    const R* __restrict__ in = A.in + static_cast<int64_t>(b) * 6 * N;
     const int nel = (T.K - e0) < EPB ? static_cast<int>(T.K - e0) : EPB;
 
     for (int i = tid; i < 4 * Nfp; i += blockDim.x) s_fmask[i] = T.Fmask[i];
@@ -93,12 +98,12 @@ __device__ __forceinline__ void stage_body(const TablesDev& T, const StageArgs& 
         const int64_t e = e0 + el;
         const int vm = s_fmask[f * Nfp + a];
         const int code = T.fcode[e * 4 + f];
-        const double* fg = T.fgeo + e * 16 + f * 4;
-        const double nx = fg[0], ny = fg[1], nz = fg[2], fs = fg[3];
-        double uM[6], dE[3], dH[3];
+        const R* fg = T.fgeo + e * 16 + f * 4;
+        const R nx = fg[0], ny = fg[1], nz = fg[2], fs = fg[3];
+        R uM[6], dE[3], dH[3];
 #pragma unroll
         for (int c = 0; c < 6; ++c) uM[c] = s_u[c][el * Np + vm];
-        double aE = T.alpha, aH = T.alpha;
+        R aE = T.alpha, aH = T.alpha;
         if (code == 0 || code == 4 || code == 5) {
             const int64_t gp = T.vmapP[(e * 4 + f) * Nfp + a];
 #pragma unroll
@@ -108,29 +113,29 @@ __device__ __forceinline__ void stage_body(const TablesDev& T, const StageArgs& 
             }
             if (code != 0 && !skip_src) {
                 const int64_t gm = e * Np + vm;
-                double pe[3], ph[3];
-                eval_pw(A.pw, A.n_pw, b, T.xyz[gm], T.xyz[N + gm], T.xyz[2 * N + gm], A.t, pe, ph);
-                const double sg = (code == 4) ? 1.0 : -1.0;
+                R pe[3], ph[3];
+                eval_pw<R>(A.pw, A.n_pw, b, T.xyz[gm], T.xyz[N + gm], T.xyz[2 * N + gm], static_cast<R>(A.t), pe, ph);
+                const R sg = (code == 4) ? R(1) : R(-1);
 #pragma unroll
                 for (int c = 0; c < 3; ++c) { dE[c] += sg * pe[c]; dH[c] += sg * ph[c]; }
             }
         } else if (code == 1 || code == 6) {           // PEC
 #pragma unroll
-            for (int c = 0; c < 3; ++c) { dE[c] = -2.0 * uM[c]; dH[c] = 0.0; }
+            for (int c = 0; c < 3; ++c) { dE[c] = R(-2) * uM[c]; dH[c] = R(0); }
         } else if (code == 2 || code == 7) {           // PMC
 #pragma unroll
-            for (int c = 0; c < 3; ++c) { dE[c] = 0.0; dH[c] = -2.0 * uM[c + 3]; }
+            for (int c = 0; c < 3; ++c) { dE[c] = R(0); dH[c] = R(-2) * uM[c + 3]; }
         } else if (code == 3 || code == 8) {           // SMA: penalty 1 regardless of alpha
 #pragma unroll
             for (int c = 0; c < 3; ++c) { dE[c] = -uM[c]; dH[c] = -uM[c + 3]; }
-            aE = 1.0; aH = 1.0;
+            aE = R(1); aH = R(1);
         } else {                                        // open: zero jump
 #pragma unroll
-            for (int c = 0; c < 3; ++c) { dE[c] = 0.0; dH[c] = 0.0; }
+            for (int c = 0; c < 3; ++c) { dE[c] = R(0); dH[c] = R(0); }
         }
-        const double ndE = nx * dE[0] + ny * dE[1] + nz * dE[2];
-        const double ndH = nx * dH[0] + ny * dH[1] + nz * dH[2];
-        const double h = 0.5 * fs;
+        const R ndE = nx * dE[0] + ny * dE[1] + nz * dE[2];
+        const R ndH = nx * dH[0] + ny * dH[1] + nz * dH[2];
+        const R h = R(0.5) * fs;
         const int o = el * NF + fn;
         s_f[0][o] = h * ((ny * dH[2] - nz * dH[1]) + aE * (dE[0] - ndE * nx));
         s_f[1][o] = h * ((nz * dH[0] - nx * dH[2]) + aE * (dE[1] - ndE * ny));
@@ -145,43 +150,43 @@ __device__ __forceinline__ void stage_body(const TablesDev& T, const StageArgs& 
     if (tid >= nel * Np) return;
     const int el = tid / Np, i = tid - el * Np;
     const int64_t e = e0 + el;
-    double ar[6], as[6], at[6];
+    R ar[6], as[6], at[6];
 #pragma unroll
-    for (int c = 0; c < 6; ++c) { ar[c] = 0.0; as[c] = 0.0; at[c] = 0.0; }
-    const double* __restrict__ DrT = T.DrT;
-    const double* __restrict__ DsT = T.DsT;
-    const double* __restrict__ DtT = T.DtT;
+    for (int c = 0; c < 6; ++c) { ar[c] = R(0); as[c] = R(0); at[c] = R(0); }
+    const R* __restrict__ DrT = T.DrT;
+    const R* __restrict__ DsT = T.DsT;
+    const R* __restrict__ DtT = T.DtT;
 #pragma unroll 4
     for (int j = 0; j < Np; ++j) {
-        const double dr = __ldg(DrT + j * Np + i), ds = __ldg(DsT + j * Np + i), dt = __ldg(DtT + j * Np + i);
+        const R dr = __ldg(DrT + j * Np + i), ds = __ldg(DsT + j * Np + i), dt = __ldg(DtT + j * Np + i);
 #pragma unroll
         for (int c = 0; c < 6; ++c) {
-            const double u = s_u[c][el * Np + j];
+            const R u = s_u[c][el * Np + j];
             ar[c] = fma(dr, u, ar[c]);
             as[c] = fma(ds, u, as[c]);
             at[c] = fma(dt, u, at[c]);
         }
     }
-    double lf[6];
+    R lf[6];
 #pragma unroll
-    for (int c = 0; c < 6; ++c) lf[c] = 0.0;
-    const double* __restrict__ LT = T.LIFTT;
+    for (int c = 0; c < 6; ++c) lf[c] = R(0);
+    const R* __restrict__ LT = T.LIFTT;
 #pragma unroll 4
     for (int m = 0; m < NF; ++m) {
-        const double L = __ldg(LT + m * Np + i);
+        const R L = __ldg(LT + m * Np + i);
 #pragma unroll
         for (int c = 0; c < 6; ++c) lf[c] = fma(L, s_f[c][el * NF + m], lf[c]);
     }
-    const double* g = T.geo + e * 9;
-    const double rx = g[0], ry = g[1], rz = g[2], sx = g[3], sy = g[4], sz = g[5], tx = g[6], ty = g[7], tz = g[8];
+    const R* g = T.geo + e * 9;
+    const R rx = g[0], ry = g[1], rz = g[2], sx = g[3], sy = g[4], sz = g[5], tx = g[6], ty = g[7], tz = g[8];
     auto dx = [&](int c) { return rx * ar[c] + sx * as[c] + tx * at[c]; };
     auto dy = [&](int c) { return ry * ar[c] + sy * as[c] + ty * at[c]; };
     auto dz = [&](int c) { return rz * ar[c] + sz * as[c] + tz * at[c]; };
-    const double curlHx = dy(5) - dz(4), curlHy = dz(3) - dx(5), curlHz = dx(4) - dy(3);
-    const double curlEx = dy(2) - dz(1), curlEy = dz(0) - dx(2), curlEz = dx(1) - dy(0);
-    const double* mt = T.mat + e * 3;
-    const double ie = mt[0], im = mt[1], se = mt[2];
-    double k[6];
+    const R curlHx = dy(5) - dz(4), curlHy = dz(3) - dx(5), curlHz = dx(4) - dy(3);
+    const R curlEx = dy(2) - dz(1), curlEy = dz(0) - dx(2), curlEz = dx(1) - dy(0);
+    const R* mt = T.mat + e * 3;
+    const R ie = mt[0], im = mt[1], se = mt[2];
+    R k[6];
     k[0] = ie * (curlHx + lf[0]) - se * s_u[0][tid];
     k[1] = ie * (curlHy + lf[1]) - se * s_u[1][tid];
     k[2] = ie * (curlHz + lf[2]) - se * s_u[2][tid];
@@ -190,7 +195,7 @@ __device__ __forceinline__ void stage_body(const TablesDev& T, const StageArgs& 
     k[5] = im * (-curlEz + lf[5]);
 
     const int64_t base = static_cast<int64_t>(b) * 6 * N + e * Np + i;
-    const double dt = A.dt;
+    const R dt = A.dt;
     switch (A.mode) {
     case MODE_MULT:
 #pragma unroll
@@ -199,35 +204,35 @@ __device__ __forceinline__ void stage_body(const TablesDev& T, const StageArgs& 
     case MODE_RK4_1:
 #pragma unroll
         for (int c = 0; c < 6; ++c) {
-            const double xv = s_u[c][tid];
-            A.yout[base + c * N] = xv + 0.5 * dt * k[c];
-            A.z[base + c * N] = xv + (dt / 6.0) * k[c];
+            const R xv = s_u[c][tid];
+            A.yout[base + c * N] = xv + R(0.5) * dt * k[c];
+            A.z[base + c * N] = xv + (dt / R(6)) * k[c];
         }
         break;
     case MODE_RK4_2:
 #pragma unroll
         for (int c = 0; c < 6; ++c) {
-            const double xv = A.x[base + c * N];
-            A.yout[base + c * N] = xv + 0.5 * dt * k[c];
-            A.z[base + c * N] += (dt / 3.0) * k[c];
+            const R xv = A.x[base + c * N];
+            A.yout[base + c * N] = xv + R(0.5) * dt * k[c];
+            A.z[base + c * N] += (dt / R(3)) * k[c];
         }
         break;
     case MODE_RK4_3:
 #pragma unroll
         for (int c = 0; c < 6; ++c) {
-            const double xv = A.x[base + c * N];
+            const R xv = A.x[base + c * N];
             A.yout[base + c * N] = xv + dt * k[c];
-            A.z[base + c * N] += (dt / 3.0) * k[c];
+            A.z[base + c * N] += (dt / R(3)) * k[c];
         }
         break;
     case MODE_RK4_4:
 #pragma unroll
-        for (int c = 0; c < 6; ++c) A.x[base + c * N] = A.z[base + c * N] + (dt / 6.0) * k[c];
+        for (int c = 0; c < 6; ++c) A.x[base + c * N] = A.z[base + c * N] + (dt / R(6)) * k[c];
         break;
     case MODE_LSRK:
 #pragma unroll
         for (int c = 0; c < 6; ++c) {
-            const double r = A.a * A.res[base + c * N] + dt * k[c];
+            const R r = A.a * A.res[base + c * N] + dt * k[c];
             A.res[base + c * N] = r;
             A.yout[base + c * N] = s_u[c][tid] + A.b * r;
         }
@@ -237,7 +242,8 @@ __device__ __forceinline__ void stage_body(const TablesDev& T, const StageArgs& 
     }
 }
 
-__device__ __forceinline__ void tfsf_skip_body(const TablesDev& T, const PlaneWaveDev* pw, int n_pw, int b, double t,
+template <typename R = double>
+__device__ __forceinline__ void tfsf_skip_body(const TablesT<R>& T, const PlaneWaveDev* pw, int n_pw, int b, double t,
                                               int* skip)
 {
     const int64_t total = T.n_tfsf_elems * T.Np;
@@ -245,10 +251,10 @@ __device__ __forceinline__ void tfsf_skip_body(const TablesDev& T, const PlaneWa
     for (int64_t w = threadIdx.x; w < total; w += blockDim.x) {
         const int64_t e = T.tfsf_elems[w / T.Np];
         const int64_t gm = e * T.Np + (w % T.Np);
-        double pe[3], ph[3];
-        eval_pw(pw, n_pw, b, T.xyz[gm], T.xyz[T.N + gm], T.xyz[2 * T.N + gm], t, pe, ph);
+        R pe[3], ph[3];
+        eval_pw<R>(pw, n_pw, b, T.xyz[gm], T.xyz[T.N + gm], T.xyz[2 * T.N + gm], static_cast<R>(t), pe, ph);
         for (int c = 0; c < 3; ++c) {
-            const double a = 0.5 * pe[c], h = 0.5 * ph[c];
+            const double a = 0.5 * static_cast<double>(pe[c]), h = 0.5 * static_cast<double>(ph[c]);
             acc += a * a + h * h;
         }
     }

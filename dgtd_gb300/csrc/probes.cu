@@ -242,7 +242,7 @@ void ProbeSet::sample(const void* d_state, double t, cudaStream_t s)
         series_t_.push_back(t);
     }
     dim3 grid(static_cast<unsigned>((n_items_ + 127) / 128), static_cast<unsigned>(lay_.B));
-    if (lay_.fp32) probe_sample_kernel<float><<<grid, 128, 0, s>>>(static_cast<const float*>(d_state), a);
+    if (lay_.fp32 || lay_.f32_ref) probe_sample_kernel<float><<<grid, 128, 0, s>>>(static_cast<const float*>(d_state), a);
     else probe_sample_kernel<double><<<grid, 128, 0, s>>>(static_cast<const double*>(d_state), a);
     ckp(cudaGetLastError(), "probe kernel");
     ++launches_;

@@ -35,7 +35,8 @@ struct ProbeSpec {
 // Addressing of one field value (incidence b, component c) of a state vector:
 // state[term_off + c * cstride + b * bstride].
 struct ProbeStateLayout {
-    bool fp32 = false;
+    bool fp32 = false;   // batched FP32 layout [e'][c][i][b]
+    bool f32_ref = false;// FP32 values in the reference layout [b][c][e*Np+i]
     int Np = 0;
     int Bp = 1;          // incidence stride unit of the FP32 layout (padded batch)
     int B = 1;           // incidences

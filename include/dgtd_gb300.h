@@ -44,6 +44,7 @@ extern "C" {
 /* Precision forms. */
 #define DGTD_FP64 0        /* plain form: FP64 state and arithmetic */
 #define DGTD_FP32_3XTF32 1 /* batched form: FP32 state, 3xTF32 tensor-core contractions */
+#define DGTD_FP32 2        /* single-instance form: FP32 state in the reference layout, FP32 arithmetic */
 
 /* Time integrators. */
 #define DGTD_RK4 0    /* classical RK4, mfem::RK4Solver semantics (reference default, Solver.cpp:45-47) */
@@ -77,7 +78,7 @@ typedef struct dgtd_mesh_desc {
 typedef struct dgtd_op_opts {
     int32_t order;      /* polynomial order p, 1..6 (reference solver_options.order) */
     double alpha;       /* upwind coefficient (reference solver_options.upwind_alpha) */
-    int32_t precision;  /* DGTD_FP64 or DGTD_FP32_3XTF32 */
+    int32_t precision;  /* DGTD_FP64, DGTD_FP32_3XTF32 or DGTD_FP32 */
     int32_t batch;      /* B incidences sharing the mesh (>= 1) */
 } dgtd_op_opts;
 
@@ -105,8 +106,9 @@ typedef struct dgtd_op_info {
     int64_t device_bytes;   /* bytes of device tables held by the operator */
     int64_t work_len;       /* entries of the operator's working state (dgtd_op_step / dgtd_op_mult):
                                FP64 form: = state_len (reference layout);
-                               FP32 form: K*6*Np*Bpad floats, element-blocked, incidence fastest */
-    int32_t work_word_bytes;/* 8 (FP64 form) or 4 (FP32 form) */
+                               batched FP32 form: K*6*Np*Bpad floats, element-blocked, incidence fastest;
+                               single-instance FP32 form: = state_len floats (reference layout) */
+    int32_t work_word_bytes;/* 8 (FP64 form) or 4 (FP32 forms) */
     int32_t batch_padded;   /* B rounded up to the incidence chunk (FP32 form), else B */
 } dgtd_op_info;
 
@@ -177,6 +179,13 @@ int64_t dgtd_noalloc_max_state(void);
 /* Contraction path of the FP32 batched form: 0 = tensor cores (tcgen05, 3xTF32) where
  * supported (orders 1..4, B padded to a multiple of 64), else FP32 SIMT; 1 = FP32 SIMT. */
 int dgtd_op_set_contraction(dgtd_op* op, int32_t mode);
+
+/* Batched FP32 form: replay blocks of `steps` classical-RK4 steps of dgtd_op_step from one
+ * captured CUDA graph (stage times read from a device scalar the graph advances); 0 turns
+ * it off (default). Used only on a non-default stream (the legacy stream cannot be
+ * captured) and without probes; the first call with a new state pointer, dt or stream
+ * captures the graph. DGTD_ERR_UNSUPPORTED for the other forms. */
+int dgtd_op_set_graph_steps(dgtd_op* op, int32_t steps);
 
 /* 1 when the FP32 batched form runs its contractions on the tensor cores, else 0. */
 int dgtd_op_uses_tensor_cores(const dgtd_op* op);

@@ -322,6 +322,7 @@ def run_ours(args, world, rank, local):
     op.pack(ref, state)
     del ref
     stream = torch.cuda.current_stream(dev)
+    tune = op.autotune(state, stream=stream) if prec != dg.FP64 else None
     dofs = 6 * op.ndofs * w["batch"]
     flush = torch.empty(int(256 * 2 ** 20) // 4, dtype=torch.float32, device=dev)   # 256 MB > 129 MB L2
 
@@ -387,7 +388,7 @@ def run_ours(args, world, rank, local):
         roofline["fp64_pipe"] = {"achieved_tflops": round(achieved_tflops, 4), "nominal_peak_tflops": 1.25,
                                  "frac_of_nominal": round(achieved_tflops / 1.25, 4),
                                  "note": "plain FP64 form is FP64-issue bound; nominal GB300 FP64 peak, not measured"}
-    res = dict(value=value, ms_per_step=ms_per_step, e2e_value=world * dofs * args.steps / e2e_s,
+    res = dict(value=value, ms_per_step=ms_per_step, e2e_value=world * dofs * args.steps / e2e_s, tune=tune,
                state_bytes=state_bytes, launches=launches, clocks=clk.summary(), roofline=roofline,
                setup_s=setup_s, w=w, dofs=dofs, K=K, Np=Np, dt=dt)
     del state, op
@@ -493,7 +494,7 @@ SERVING_DESC = ("Serving stream (reduced C5): Poisson arrivals; each request a b
                 "n ~ U{4..12}, central PEC cube of round(n/6) hexes (n >= 5), SMA outer boundary, TF/SF box one cell "
                 "in, order p ~ U{2..5}, one Gaussian plane wave (spread 0.1, delay 0.5) with random direction and "
                 "orthogonal polarisation, final time T ~ U[0.5, 1.5], dt from the reference 3D estimator at cfl=1; "
-                "plain FP64 operator, classical RK4; seed 20261206")
+                "classical RK4; seed 20261206")
 
 
 def serving_requests(n_req: int, rate: float, seed: int = 20261206):
@@ -519,7 +520,7 @@ def serving_requests(n_req: int, rate: float, seed: int = 20261206):
     return reqs, arrivals
 
 
-def run_serving(n_req: int, rate: float, serial_sample: int, device: int) -> dict:
+def run_serving(n_req: int, rate: float, serial_sample: int, device: int, precision: str = "fp32") -> dict:
     """Continuous-batching run of a request stream through dgtd_server_*, with time-to-solution
     per request (submit -> result on the host), and a serial sample of the same requests through
     the single-operator path for comparison."""
@@ -532,7 +533,8 @@ def run_serving(n_req: int, rate: float, serial_sample: int, device: int) -> dic
     except Exception:
         pass
     budget = int(min(24 << 30, max(1 << 30, free // 4)))
-    with dg.Server(memory_budget=budget, max_active=64, steps_per_round=4, device=device) as srv:
+    prec = dg.FP32 if precision == "fp32" else dg.FP64
+    with dg.Server(memory_budget=budget, max_active=64, steps_per_round=4, device=device, precision=prec) as srv:
         w = srv.submit(reqs[0]["mesh"], reqs[0]["order"], 0.05, waves=reqs[0]["waves"], cfl=1.0)   # warm-up
         srv.wait(w, timeout=600, want_state=False)
         base = srv.stats()
@@ -568,13 +570,14 @@ def run_serving(n_req: int, rate: float, serial_sample: int, device: int) -> dic
            "dof_updates_per_s": dof / span, "stage_launches": launches,
            "requests_per_stage_launch": packed / max(1, launches), "max_active": end["max_active_seen"],
            "peak_device_bytes": end["peak_bytes_in_use"], "memory_budget": budget, "failed": end["failed"] - base["failed"],
-           "precision": "fp64 (plain form; bit-identical alone and in the mix, tests/test_gpu_serve.py)",
+           "precision": (("fp32 (single-instance FP32 form" if prec == dg.FP32 else "fp64 (plain form") +
+                         "; bit-identical alone and in the mix, tests/test_gpu_serve.py)"),
            "workload": SERVING_DESC}
     if serial_sample > 0:
         # the same first requests one at a time through the single-operator path (one solve per call)
         t1 = time.perf_counter()
         for r in reqs[:serial_sample]:
-            op = dg.Operator(r["mesh"], order=r["order"])
+            op = dg.Operator(r["mesh"], order=r["order"], precision=prec)
             op.set_planewaves(r["waves"])
             op.run_host(np.zeros(op.state_len), 0.0, op.estimate_dt(1.0), r["final_time"])
             op.close()
@@ -601,6 +604,7 @@ def main():
     ap.add_argument("--high-order-steps", type=int, default=10, help="timed steps of the p=6 dielectric (0: skip)")
     ap.add_argument("--serving-rate", type=float, default=4.0, help="Poisson arrival rate of the serving stream (1/s)")
     ap.add_argument("--serving-serial", type=int, default=8, help="requests also run one at a time for comparison")
+    ap.add_argument("--serving-precision", choices=["fp32", "fp64"], default="fp32")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -633,6 +637,9 @@ def main():
     r = run_ours(args, world, rank, local)
     config["elements"] = r["K"]
     config["dofs_per_step"] = r["dofs"]
+    if r.get("tune"):
+        config["stage_kernel"] = r["tune"]["kernel"]
+        config["autotune_ms_per_launch"] = r["tune"]["ms_per_launch"]
     config["dt"] = r["dt"]
     if rank != 0:
         return
@@ -657,7 +664,8 @@ def main():
         import torch
         line["high_order"] = run_high_order(args.high_order_steps, torch.device("cuda", local))
     if args.serving_requests > 0 and world == 1:
-        line["serving"] = run_serving(args.serving_requests, args.serving_rate, args.serving_serial, local)
+        line["serving"] = run_serving(args.serving_requests, args.serving_rate, args.serving_serial, local,
+                                      args.serving_precision)
     print(json.dumps(line), flush=True)
 
 

@@ -93,7 +93,7 @@ class CaseResult(C.Structure):
 
 class ServerOpts(C.Structure):
     _fields_ = [("memory_budget", C.c_int64), ("max_active", C.c_int32), ("steps_per_round", C.c_int32),
-                ("device", C.c_int32)]
+                ("device", C.c_int32), ("precision", C.c_int32)]
 
 
 class Request(C.Structure):
@@ -147,6 +147,7 @@ SIGNATURES = {
     "dgtd_op_set_contraction": (C.c_int, [_P, C.c_int32]),
     "dgtd_op_uses_tensor_cores": (C.c_int, [_P]),
     "dgtd_op_set_graph_steps": (C.c_int, [_P, C.c_int32]),
+    "dgtd_op_autotune": (C.c_int, [_P, _P, _P, _D, _I32]),
     "dgtd_op_check": (C.c_int, [_P, _P]),
     "dgtd_op_estimate_dt": (C.c_int, [_P, C.c_double, _D]),
     "dgtd_box_mesh_size": (C.c_int, [C.POINTER(BoxSpec), _I64, _I64, _I64, _I64]),
@@ -447,6 +448,18 @@ class Operator:
         """FP32 batched form: 0 = tensor cores (tcgen05 3xTF32) where supported, 1 = FP32 SIMT."""
         _check(lib().dgtd_op_set_contraction(self._h, int(mode)), "dgtd_op_set_contraction")
 
+    TUNE_CANDIDATES = ("tensor cores (3xTF32, 64 incidences x 1 element per work item)",
+                       "FP32 SIMT, 4 warps x 32 incidences per block", "FP32 SIMT, 8 warps x 32 incidences per block",
+                       "FP32 SIMT, 16 warps x 32 incidences per block")
+
+    def autotune(self, work, stream=None) -> dict:
+        """Batched FP32 form: time the candidate stage kernels and keep the fastest."""
+        ms = np.zeros(4)
+        ch = C.c_int32()
+        _check(lib().dgtd_op_autotune(self._h, _ptr(work), _stream(stream), _dp(ms), C.byref(ch)), "dgtd_op_autotune")
+        return {"choice": int(ch.value), "kernel": self.TUNE_CANDIDATES[ch.value],
+                "ms_per_launch": {self.TUNE_CANDIDATES[i]: float(ms[i]) for i in range(4) if ms[i] >= 0}}
+
     def set_graph_steps(self, steps: int) -> None:
         """Batched FP32 form: replay blocks of `steps` RK4 steps from one captured CUDA graph (0: off)."""
         _check(lib().dgtd_op_set_graph_steps(self._h, int(steps)), "dgtd_op_set_graph_steps")
@@ -533,9 +546,10 @@ class Server:
     ``wait`` returns the final state (reference layout) and the request's timing.
     """
 
-    def __init__(self, memory_budget: int = 4 << 30, max_active: int = 64, steps_per_round: int = 4, device: int = 0):
+    def __init__(self, memory_budget: int = 4 << 30, max_active: int = 64, steps_per_round: int = 4, device: int = 0,
+                 precision: int = FP64):
         o = ServerOpts(memory_budget=int(memory_budget), max_active=int(max_active),
-                       steps_per_round=int(steps_per_round), device=int(device))
+                       steps_per_round=int(steps_per_round), device=int(device), precision=int(precision))
         h = C.c_void_p()
         _check(lib().dgtd_server_create(C.byref(o), C.byref(h)), "dgtd_server_create")
         self._h = h

@@ -8,7 +8,10 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <numeric>
+#include <tuple>
 #include <stdexcept>
 #include <string>
 
@@ -23,8 +26,7 @@ void ckb(cudaError_t e, const char* what)
     if (e != cudaSuccess) throw std::runtime_error(std::string(what) + ": " + cudaGetErrorString(e));
 }
 
-constexpr int kWarps = 8;
-constexpr int kLanes = 32;
+constexpr int kLanes = 32;   // incidences per block (lane = incidence)
 
 __device__ __forceinline__ void pw_eval_f32(const PlaneWaveF32* pw, const int* pw_off, int b, float px, float py, float pz,
                                             float t, float* e, float* h)
@@ -50,7 +52,9 @@ struct OrdB {
     static constexpr size_t smem = sizeof(float) * 6 * (Np + NF) * kLanes;
 };
 
-template <int P>
+// W warps per block (the tile shape the autotuner picks): warps share the element's face
+// nodes and volume nodes.
+template <int P, int kWarps>
 __global__ void __launch_bounds__(kWarps * kLanes) stage_f32(BatchedTables T, BatchedStageArgs A)
 {
     using O = OrdB<P>;
@@ -314,19 +318,29 @@ uint64_t morton3(uint32_t x, uint32_t y, uint32_t z)
     return spread(x) | (spread(y) << 1) | (spread(z) << 2);
 }
 
-template <int P>
-void launch_stage(const BatchedTables& T, const BatchedStageArgs& A, cudaStream_t s)
+template <int P, int W>
+void launch_stage_w(const BatchedTables& T, const BatchedStageArgs& A, cudaStream_t s)
 {
     using O = OrdB<P>;
     static bool attr = false;
     if (!attr) {
-        ckb(cudaFuncSetAttribute(stage_f32<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(O::smem)),
+        ckb(cudaFuncSetAttribute(stage_f32<P, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(O::smem)),
             "smem attribute");
         attr = true;
     }
     dim3 grid(static_cast<unsigned>(T.K), static_cast<unsigned>(T.Bpad / kLanes));
-    stage_f32<P><<<grid, kWarps * kLanes, O::smem, s>>>(T, A);
+    stage_f32<P, W><<<grid, W * kLanes, O::smem, s>>>(T, A);
     ckb(cudaGetLastError(), "batched stage kernel");
+}
+
+template <int P>
+void launch_stage(const BatchedTables& T, const BatchedStageArgs& A, int warps, cudaStream_t s)
+{
+    switch (warps) {
+    case 4: launch_stage_w<P, 4>(T, A, s); break;
+    case 16: launch_stage_w<P, 16>(T, A, s); break;
+    default: launch_stage_w<P, 8>(T, A, s); break;
+    }
 }
 
 // LSERK4 coefficients (Carpenter & Kennedy 1994)
@@ -499,12 +513,12 @@ void BatchedOp::stage(BatchedStageArgs A, double t, cudaStream_t s)
         return;
     }
     switch (T_.p) {
-    case 1: launch_stage<1>(T_, A, s); break;
-    case 2: launch_stage<2>(T_, A, s); break;
-    case 3: launch_stage<3>(T_, A, s); break;
-    case 4: launch_stage<4>(T_, A, s); break;
-    case 5: launch_stage<5>(T_, A, s); break;
-    case 6: launch_stage<6>(T_, A, s); break;
+    case 1: launch_stage<1>(T_, A, simt_warps_, s); break;
+    case 2: launch_stage<2>(T_, A, simt_warps_, s); break;
+    case 3: launch_stage<3>(T_, A, simt_warps_, s); break;
+    case 4: launch_stage<4>(T_, A, simt_warps_, s); break;
+    case 5: launch_stage<5>(T_, A, simt_warps_, s); break;
+    case 6: launch_stage<6>(T_, A, simt_warps_, s); break;
     default: throw std::runtime_error("unsupported order");
     }
     ++launches_;
@@ -648,6 +662,54 @@ void BatchedOp::step(float* d_x, double t0, double dt, int nsteps, int integrato
         }
         if (cur != d_x) ckb(cudaMemcpyAsync(d_x, cur, L * sizeof(float), cudaMemcpyDeviceToDevice, s), "copy");
     }
+}
+
+int BatchedOp::autotune(const float* d_in, double* ms, cudaStream_t s)
+{
+    static std::mutex mu;
+    static std::map<std::tuple<int, int, int64_t>, int> cache;
+    const auto key = std::make_tuple(T_.p, Bpad_, K_);
+    const int warps[4] = {0, 4, 8, 16};
+    for (int c = 0; c < 4; ++c) ms[c] = -1.0;
+    int best = -1;
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        auto it = cache.find(key);
+        if (it != cache.end()) best = it->second;
+    }
+    if (best < 0) {
+        ensure_ws();
+        cudaEvent_t e0, e1;
+        ckb(cudaEventCreate(&e0), "event");
+        ckb(cudaEventCreate(&e1), "event");
+        const int saved_c = contraction_, saved_w = simt_warps_;
+        double best_ms = 1e300;
+        for (int c = 0; c < 4; ++c) {
+            if (c == 0 && !tc_supported(T_.p, Bpad_)) continue;
+            contraction_ = c == 0 ? 0 : 1;
+            simt_warps_ = c == 0 ? 8 : warps[c];
+            BatchedStageArgs A{};
+            A.mode = MODE_MULT; A.in = d_in; A.out = ws_;
+            stage(A, 0.0, s);                      // warm-up (module load, attributes)
+            ckb(cudaEventRecord(e0, s), "event");
+            for (int r = 0; r < 3; ++r) stage(A, 0.0, s);
+            ckb(cudaEventRecord(e1, s), "event");
+            ckb(cudaEventSynchronize(e1), "event");
+            float t = 0.0f;
+            ckb(cudaEventElapsedTime(&t, e0, e1), "event time");
+            ms[c] = t / 3.0;
+            if (ms[c] < best_ms) { best_ms = ms[c]; best = c; }
+        }
+        contraction_ = saved_c; simt_warps_ = saved_w;
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        std::lock_guard<std::mutex> lk(mu);
+        cache[key] = best;
+    }
+    contraction_ = best == 0 ? 0 : 1;
+    simt_warps_ = best == 0 ? 8 : warps[best];
+    drop_graph();
+    return best;
 }
 
 void BatchedOp::norm2(const float* d_state, double* d_out_dev, cudaStream_t s)

@@ -82,6 +82,11 @@ public:
     void norm2(const float* d_state, double* d_out_dev, cudaStream_t s);
     // contraction path: 0 = tensor cores (tcgen05, 3xTF32) when supported, 1 = FP32 SIMT
     void set_contraction(int mode) { contraction_ = mode; }
+    // Times the candidate stage kernels (tensor cores where supported; FP32 SIMT with 4, 8
+    // and 16 warps per block) on this operator's mesh with MODE_MULT launches on d_in and
+    // keeps the fastest. ms[4] gets the mean launch time of each candidate (-1: not
+    // applicable); returns the chosen index. The choice is cached per (order, Bpad, K).
+    int autotune(const float* d_in, double* ms, cudaStream_t s);
     // RK4 steps per captured CUDA graph (0: launch every stage directly)
     void set_graph_steps(int g);
     bool uses_tensor_cores() const { return contraction_ == 0 && tc_supported(T_.p, Bpad_); }
@@ -112,6 +117,7 @@ private:
     float* ws_ = nullptr;
     bool has_tfsf_ = false;
     int contraction_ = 0;
+    int simt_warps_ = 8;
     // CUDA graph of graph_steps_ RK4 steps (stage times relative to the device scalar t_dev_)
     int graph_steps_ = 0;
     double* t_dev_ = nullptr;

@@ -720,6 +720,22 @@ int dgtd_op_set_graph_steps(dgtd_op* op, int32_t steps)
     return DGTD_OK;
 }
 
+int dgtd_op_autotune(dgtd_op* op, const void* d_work, void* stream, double* h_ms, int32_t* choice)
+{
+    if (!op || !d_work) return fail(DGTD_ERR_INVALID, "NULL argument");
+    if (!op->batched) return fail(DGTD_ERR_UNSUPPORTED, "the autotuner chooses among the batched form's kernels");
+    try {
+        BatchedCount bc(op);
+        double ms[4];
+        const int c = op->batched->autotune(static_cast<const float*>(d_work), ms, static_cast<cudaStream_t>(stream));
+        if (h_ms) std::copy(ms, ms + 4, h_ms);
+        if (choice) *choice = c;
+    } catch (const std::exception& e) {
+        return fail(DGTD_ERR_CUDA, e.what());
+    }
+    return DGTD_OK;
+}
+
 int dgtd_op_uses_tensor_cores(const dgtd_op* op) { return (op && op->batched && op->batched->uses_tensor_cores()) ? 1 : 0; }
 
 int dgtd_op_check(dgtd_op* op, void* stream)

@@ -56,30 +56,31 @@ constexpr int kMaxOrder = 6;
 
 __host__ __device__ inline int64_t al(int64_t v) { return (v + kAlign - 1) / kAlign * kAlign; }
 
-// Byte offsets of one request's tables and state inside its device region.
+// Byte offsets of one request's tables and state inside its device region, for
+// real-number size `ws` (8: FP64 serving, 4: FP32 serving).
 // [0, y0) is uploaded at admission (tables, sources, initial state x);
 // y0, y1, z are the RK4 registers.
 struct Layout {
     int64_t geo, fgeo, mat, vmap, fcode, xyz, tfsf, pw, x, y0, y1, z, total;
 };
 
-__host__ __device__ inline Layout layout(int64_t K, int Np, int Nfp, int64_t n_tfsf)
+__host__ __device__ inline Layout layout(int64_t K, int Np, int Nfp, int64_t n_tfsf, int ws)
 {
     Layout L{};
     const int64_t N = K * Np;
     int64_t o = 0;
-    L.geo = o;   o = al(o + K * 9 * 8);
-    L.fgeo = o;  o = al(o + K * 16 * 8);
-    L.mat = o;   o = al(o + K * 3 * 8);
+    L.geo = o;   o = al(o + K * 9 * ws);
+    L.fgeo = o;  o = al(o + K * 16 * ws);
+    L.mat = o;   o = al(o + K * 3 * ws);
     L.vmap = o;  o = al(o + K * 4 * Nfp * 4);
     L.fcode = o; o = al(o + K * 4 * 4);
-    L.xyz = o;   o = al(o + 3 * N * 8);
+    L.xyz = o;   o = al(o + 3 * N * ws);
     L.tfsf = o;  o = al(o + (n_tfsf > 0 ? n_tfsf : 1) * 4);
     L.pw = o;    o = al(o + kMaxWaves * static_cast<int64_t>(sizeof(PlaneWaveDev)));
-    L.x = o;     o = al(o + 6 * N * 8);
-    L.y0 = o;    o = al(o + 6 * N * 8);
-    L.y1 = o;    o = al(o + 6 * N * 8);
-    L.z = o;     o = al(o + 6 * N * 8);
+    L.x = o;     o = al(o + 6 * N * ws);
+    L.y0 = o;    o = al(o + 6 * N * ws);
+    L.y1 = o;    o = al(o + 6 * N * ws);
+    L.z = o;     o = al(o + 6 * N * ws);
     L.total = o;
     return L;
 }
@@ -96,10 +97,10 @@ struct SlotParam {
 };
 
 struct LaunchParam {
-    const double* DrT;
-    const double* DsT;
-    const double* DtT;
-    const double* LIFTT;
+    const void* DrT;    // reference-element operators in the serving precision
+    const void* DsT;
+    const void* DtT;
+    const void* LIFTT;
     const int* Fmask;
     int* skip;         // [kMaxSlots] TF/SF skip flags
     double c;          // stage time = t + c * dt
@@ -108,29 +109,30 @@ struct LaunchParam {
     SlotParam s[kMaxSlots];
 };
 
-template <int P>
-__device__ __forceinline__ void slot_views(const LaunchParam& L, const SlotParam& S, TablesDev& T, StageArgs& A)
+template <int P, typename R>
+__device__ __forceinline__ void slot_views(const LaunchParam& L, const SlotParam& S, TablesT<R>& T, StageArgsT<R>& A)
 {
     using O = fp64::Ord<P>;
-    const Layout Y = layout(S.K, O::Np, O::Nfp, S.n_tfsf);
+    const Layout Y = layout(S.K, O::Np, O::Nfp, S.n_tfsf, static_cast<int>(sizeof(R)));
     T.p = P; T.Np = O::Np; T.Nfp = O::Nfp; T.K = S.K; T.N = S.K * O::Np;
-    T.DrT = L.DrT; T.DsT = L.DsT; T.DtT = L.DtT; T.LIFTT = L.LIFTT; T.Fmask = L.Fmask;
-    T.geo = reinterpret_cast<const double*>(S.base + Y.geo);
-    T.fgeo = reinterpret_cast<const double*>(S.base + Y.fgeo);
-    T.mat = reinterpret_cast<const double*>(S.base + Y.mat);
+    T.DrT = static_cast<const R*>(L.DrT); T.DsT = static_cast<const R*>(L.DsT);
+    T.DtT = static_cast<const R*>(L.DtT); T.LIFTT = static_cast<const R*>(L.LIFTT); T.Fmask = L.Fmask;
+    T.geo = reinterpret_cast<const R*>(S.base + Y.geo);
+    T.fgeo = reinterpret_cast<const R*>(S.base + Y.fgeo);
+    T.mat = reinterpret_cast<const R*>(S.base + Y.mat);
     T.vmapP = reinterpret_cast<const int32_t*>(S.base + Y.vmap);
     T.fcode = reinterpret_cast<const int32_t*>(S.base + Y.fcode);
-    T.xyz = reinterpret_cast<const double*>(S.base + Y.xyz);
+    T.xyz = reinterpret_cast<const R*>(S.base + Y.xyz);
     T.tfsf_elems = reinterpret_cast<const int32_t*>(S.base + Y.tfsf);
     T.n_tfsf_elems = S.n_tfsf;
-    T.alpha = S.alpha;
-    double* x = reinterpret_cast<double*>(S.base + Y.x);
-    double* y0 = reinterpret_cast<double*>(S.base + Y.y0);
-    double* y1 = reinterpret_cast<double*>(S.base + Y.y1);
-    double* z = reinterpret_cast<double*>(S.base + Y.z);
-    A = StageArgs{};
+    T.alpha = static_cast<R>(S.alpha);
+    R* x = reinterpret_cast<R*>(S.base + Y.x);
+    R* y0 = reinterpret_cast<R*>(S.base + Y.y0);
+    R* y1 = reinterpret_cast<R*>(S.base + Y.y1);
+    R* z = reinterpret_cast<R*>(S.base + Y.z);
+    A = StageArgsT<R>{};
     A.t = S.t + L.c * S.dt;
-    A.dt = S.dt;
+    A.dt = static_cast<R>(S.dt);
     A.mode = L.mode;
     A.batch = 1;
     A.x = x;
@@ -153,7 +155,7 @@ __device__ __forceinline__ void slot_views(const LaunchParam& L, const SlotParam
 }
 
 // One RK4 stage of every request in the launch.
-template <int P>
+template <int P, typename R>
 __global__ void __launch_bounds__(fp64::kBlock) serve_stage(const __grid_constant__ LaunchParam L)
 {
     const int64_t bx = blockIdx.x;
@@ -163,47 +165,53 @@ __global__ void __launch_bounds__(fp64::kBlock) serve_stage(const __grid_constan
         if (L.s[mid].block0 <= bx) lo = mid; else hi = mid - 1;
     }
     const SlotParam& S = L.s[lo];
-    TablesDev T;
-    StageArgs A;
-    slot_views<P>(L, S, T, A);
-    fp64::stage_body<P>(T, A, (bx - S.block0) * fp64::Ord<P>::EPB, 0);
+    TablesT<R> T;
+    StageArgsT<R> A;
+    slot_views<P, R>(L, S, T, A);
+    fp64::stage_body<P, R>(T, A, (bx - S.block0) * fp64::Ord<P>::EPB, 0);
 }
 
 // TF/SF skip flag of every request with sources (one block each).
-template <int P>
+template <int P, typename R>
 __global__ void __launch_bounds__(256) serve_skip(const __grid_constant__ LaunchParam L)
 {
     const SlotParam& S = L.s[blockIdx.x];
     if (S.n_pw <= 0 || S.n_tfsf <= 0) return;
-    TablesDev T;
-    StageArgs A;
-    slot_views<P>(L, S, T, A);
-    fp64::tfsf_skip_body(T, A.pw, A.n_pw, 0, A.t, L.skip + S.pos);
+    TablesT<R> T;
+    StageArgsT<R> A;
+    slot_views<P, R>(L, S, T, A);
+    fp64::tfsf_skip_body<R>(T, A.pw, A.n_pw, 0, A.t, L.skip + S.pos);
 }
 
-template <int P>
+template <int P, typename R>
 cudaError_t launch_round_stage(const LaunchParam& L, int64_t blocks, bool any_src, cudaStream_t s)
 {
     if (any_src) {
-        serve_skip<P><<<L.n, 256, 0, s>>>(L);
+        serve_skip<P, R><<<L.n, 256, 0, s>>>(L);
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }
-    serve_stage<P><<<static_cast<unsigned>(blocks), fp64::kBlock, 0, s>>>(L);
+    serve_stage<P, R><<<static_cast<unsigned>(blocks), fp64::kBlock, 0, s>>>(L);
     return cudaGetLastError();
 }
 
-cudaError_t launch_stage(int p, const LaunchParam& L, int64_t blocks, bool any_src, cudaStream_t s)
+template <typename R>
+cudaError_t launch_stage_r(int p, const LaunchParam& L, int64_t blocks, bool any_src, cudaStream_t s)
 {
     switch (p) {
-    case 1: return launch_round_stage<1>(L, blocks, any_src, s);
-    case 2: return launch_round_stage<2>(L, blocks, any_src, s);
-    case 3: return launch_round_stage<3>(L, blocks, any_src, s);
-    case 4: return launch_round_stage<4>(L, blocks, any_src, s);
-    case 5: return launch_round_stage<5>(L, blocks, any_src, s);
-    case 6: return launch_round_stage<6>(L, blocks, any_src, s);
+    case 1: return launch_round_stage<1, R>(L, blocks, any_src, s);
+    case 2: return launch_round_stage<2, R>(L, blocks, any_src, s);
+    case 3: return launch_round_stage<3, R>(L, blocks, any_src, s);
+    case 4: return launch_round_stage<4, R>(L, blocks, any_src, s);
+    case 5: return launch_round_stage<5, R>(L, blocks, any_src, s);
+    case 6: return launch_round_stage<6, R>(L, blocks, any_src, s);
     default: return cudaErrorInvalidValue;
     }
+}
+
+cudaError_t launch_stage(bool fp32, int p, const LaunchParam& L, int64_t blocks, bool any_src, cudaStream_t s)
+{
+    return fp32 ? launch_stage_r<float>(p, L, blocks, any_src, s) : launch_stage_r<double>(p, L, blocks, any_src, s);
 }
 
 int elements_per_block(int p)
@@ -238,10 +246,10 @@ std::vector<double> transposed(const std::vector<double>& a, int rows, int cols)
 
 struct OrderTables {
     RefTet ref;
-    double* DrT = nullptr;
-    double* DsT = nullptr;
-    double* DtT = nullptr;
-    double* LIFTT = nullptr;
+    void* DrT = nullptr;     // in the serving precision
+    void* DsT = nullptr;
+    void* DtT = nullptr;
+    void* LIFTT = nullptr;
     int* Fmask = nullptr;
 };
 
@@ -282,6 +290,7 @@ using dgtd::serve::ReqP;
 
 struct dgtd_server {
     dgtd_server_opts opts{};
+    bool fp32 = false;              // FP32 serving (single-instance FP32 form of the stage)
     std::chrono::steady_clock::time_point t_start;
     char* arena_base = nullptr;
     dgtd::RangeAllocator arena;
@@ -339,7 +348,8 @@ void fatal_locked(dgtd_server* s, const std::string& msg)
     s->cv_retire.notify_all();
 }
 
-// Host image of [0, lay.y0) of a request's region.
+// Host image of [0, lay.y0) of a request's region; real tables in R.
+template <typename R>
 std::vector<char> region_image(const Req& r, const dgtd::MeshTables& tab)
 {
     const Layout& L = r.lay;
@@ -347,18 +357,22 @@ std::vector<char> region_image(const Req& r, const dgtd::MeshTables& tab)
     auto put = [&](int64_t off, const void* src, size_t bytes) {
         if (bytes) std::memcpy(img.data() + off, src, bytes);
     };
-    put(L.geo, tab.geo.data(), tab.geo.size() * sizeof(double));
-    put(L.fgeo, tab.fgeo.data(), tab.fgeo.size() * sizeof(double));
-    put(L.mat, tab.mat.data(), tab.mat.size() * sizeof(double));
+    auto put_real = [&](int64_t off, const double* src, size_t n) {
+        R* dst = reinterpret_cast<R*>(img.data() + off);
+        for (size_t i = 0; i < n; ++i) dst[i] = static_cast<R>(src[i]);
+    };
+    put_real(L.geo, tab.geo.data(), tab.geo.size());
+    put_real(L.fgeo, tab.fgeo.data(), tab.fgeo.size());
+    put_real(L.mat, tab.mat.data(), tab.mat.size());
     put(L.vmap, tab.vmapP.data(), tab.vmapP.size() * sizeof(int32_t));
     put(L.fcode, tab.fcode.data(), tab.fcode.size() * sizeof(int32_t));
     const size_t N = static_cast<size_t>(r.K) * r.Np;
-    put(L.xyz, tab.x.data(), N * sizeof(double));
-    put(L.xyz + static_cast<int64_t>(N * sizeof(double)), tab.y.data(), N * sizeof(double));
-    put(L.xyz + static_cast<int64_t>(2 * N * sizeof(double)), tab.z.data(), N * sizeof(double));
+    put_real(L.xyz, tab.x.data(), N);
+    put_real(L.xyz + static_cast<int64_t>(N * sizeof(R)), tab.y.data(), N);
+    put_real(L.xyz + static_cast<int64_t>(2 * N * sizeof(R)), tab.z.data(), N);
     put(L.tfsf, tab.tfsf_elems.data(), tab.tfsf_elems.size() * sizeof(int32_t));
     put(L.pw, r.waves.data(), r.waves.size() * sizeof(dgtd::PlaneWaveDev));
-    if (!r.init.empty()) put(L.x, r.init.data(), r.init.size() * sizeof(double));
+    if (!r.init.empty()) put_real(L.x, r.init.data(), r.init.size());
     return img;
 }
 
@@ -382,7 +396,7 @@ void admission_loop(dgtd_server* s)
             r->Np = O.ref.Np;
             r->Nfp = O.ref.Nfp;
             r->n_tfsf = static_cast<int64_t>(tab.tfsf_elems.size());
-            r->lay = layout(r->K, r->Np, r->Nfp, r->n_tfsf);
+            r->lay = layout(r->K, r->Np, r->Nfp, r->n_tfsf, s->fp32 ? 4 : 8);
             if (!r->init.empty() && static_cast<int64_t>(r->init.size()) != 6 * r->K * r->Np)
                 throw ServeError(DGTD_ERR_INVALID, "initial state has the wrong length for this mesh and order");
             if (!(r->dt > 0.0)) {
@@ -391,7 +405,7 @@ void admission_loop(dgtd_server* s)
                 const double rmin = std::fabs(g[1] - g[0]);
                 r->dt = tab.dt_scale_min * rmin * 2.0 / 3.0 * 0.75 * r->cfl / 0.8;
             }
-            std::vector<char> img = region_image(*r, tab);
+            std::vector<char> img = s->fp32 ? region_image<float>(*r, tab) : region_image<double>(*r, tab);
             int64_t off = -1;
             {
                 std::unique_lock<std::mutex> lk(s->mu);
@@ -505,7 +519,7 @@ void engine_loop(dgtd_server* s)
                     for (int q = 0; q < 4; ++q) {
                         L.mode = modes[q];
                         L.c = cs[q];
-                        ck(launch_stage(o, L, blocks, any_src, st), "serving stage kernel");
+                        ck(launch_stage(s->fp32, o, L, blocks, any_src, st), "serving stage kernel");
                     }
                     used[o] = true;
                     const double tnow = s->now();
@@ -561,11 +575,21 @@ void retire_loop(dgtd_server* s)
         }
         try {
             ck(cudaEventSynchronize(r->ev_last), "last kernel of a request");
-            r->result.resize(static_cast<size_t>(6 * r->K * r->Np));
-            ck(cudaMemcpyAsync(r->result.data(), s->arena_base + r->off + r->lay.x, r->result.size() * sizeof(double),
-                               cudaMemcpyDeviceToHost, s->ret_stream),
-               "result download");
-            ck(cudaStreamSynchronize(s->ret_stream), "result download");
+            const size_t n = static_cast<size_t>(6 * r->K * r->Np);
+            r->result.resize(n);
+            if (s->fp32) {
+                std::vector<float> f(n);
+                ck(cudaMemcpyAsync(f.data(), s->arena_base + r->off + r->lay.x, n * sizeof(float),
+                                   cudaMemcpyDeviceToHost, s->ret_stream),
+                   "result download");
+                ck(cudaStreamSynchronize(s->ret_stream), "result download");
+                for (size_t i = 0; i < n; ++i) r->result[i] = f[i];
+            } else {
+                ck(cudaMemcpyAsync(r->result.data(), s->arena_base + r->off + r->lay.x, n * sizeof(double),
+                                   cudaMemcpyDeviceToHost, s->ret_stream),
+                   "result download");
+                ck(cudaStreamSynchronize(s->ret_stream), "result download");
+            }
             cudaEventDestroy(r->ev_last);
             r->ev_last = nullptr;
             std::lock_guard<std::mutex> lk(s->mu);
@@ -668,8 +692,11 @@ int dgtd_server_create(const dgtd_server_opts* opts, dgtd_server** out)
     if (opts->max_active < 1 || opts->max_active > kMaxSlots)
         return sfail(DGTD_ERR_INVALID, "max_active must be in [1, " + std::to_string(kMaxSlots) + "]");
     if (opts->steps_per_round < 1) return sfail(DGTD_ERR_INVALID, "steps_per_round must be >= 1");
+    if (opts->precision != DGTD_FP64 && opts->precision != DGTD_FP32)
+        return sfail(DGTD_ERR_INVALID, "server precision must be DGTD_FP64 or DGTD_FP32");
     dgtd_server* s = new dgtd_server();
     s->opts = *opts;
+    s->fp32 = opts->precision == DGTD_FP32;
     s->t_start = std::chrono::steady_clock::now();
     try {
         ck(cudaSetDevice(opts->device), "cudaSetDevice");
@@ -686,10 +713,14 @@ int dgtd_server_create(const dgtd_server_opts* opts, dgtd_server** out)
             OrderTables& O = s->ord[o];
             O.ref = dgtd::build_ref_tet(o);
             const int Np = O.ref.Np, NF = 4 * O.ref.Nfp;
-            O.DrT = dev_upload(transposed(O.ref.Dr, Np, Np));
-            O.DsT = dev_upload(transposed(O.ref.Ds, Np, Np));
-            O.DtT = dev_upload(transposed(O.ref.Dt, Np, Np));
-            O.LIFTT = dev_upload(transposed(O.ref.LIFT, Np, NF));
+            auto up_real = [&](const std::vector<double>& v) -> void* {
+                if (s->fp32) return dev_upload(std::vector<float>(v.begin(), v.end()));
+                return dev_upload(v);
+            };
+            O.DrT = up_real(transposed(O.ref.Dr, Np, Np));
+            O.DsT = up_real(transposed(O.ref.Ds, Np, Np));
+            O.DtT = up_real(transposed(O.ref.Dt, Np, Np));
+            O.LIFTT = up_real(transposed(O.ref.LIFT, Np, NF));
             O.Fmask = dev_upload(O.ref.Fmask);
             ck(cudaStreamCreateWithFlags(&s->ord_stream[o], cudaStreamNonBlocking), "stream");
             for (int k = 0; k < 2; ++k) ck(cudaEventCreateWithFlags(&s->round_ev[k][o], cudaEventDisableTiming), "event");

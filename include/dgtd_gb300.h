@@ -187,6 +187,15 @@ int dgtd_op_set_contraction(dgtd_op* op, int32_t mode);
  * captures the graph. DGTD_ERR_UNSUPPORTED for the other forms. */
 int dgtd_op_set_graph_steps(dgtd_op* op, int32_t steps);
 
+/* Batched FP32 form: time the candidate stage kernels on this operator's mesh and keep the
+ * fastest (the tile-shape autotuner): 0 = tensor cores (3xTF32, 64 incidences x one element
+ * per work item; orders 1..4, B padded to 64), 1..3 = FP32 SIMT with 4, 8, 16 warps per
+ * block (32 incidences x one element per block). d_work: a working state (device; read
+ * only). h_ms[4] (may be NULL) gets each candidate's mean launch time in ms (-1: not
+ * applicable); *choice gets the index kept. Results are cached per (order, padded batch,
+ * element count) for the process. DGTD_ERR_UNSUPPORTED for the other forms. */
+int dgtd_op_autotune(dgtd_op* op, const void* d_work, void* stream, double* h_ms, int32_t* choice);
+
 /* 1 when the FP32 batched form runs its contractions on the tensor cores, else 0. */
 int dgtd_op_uses_tensor_cores(const dgtd_op* op);
 
@@ -300,9 +309,10 @@ int dgtd_case_run(const dgtd_case* c, const dgtd_case_run_opts* opts, double* h_
  * The reference runs one case per process (driver::buildSolverJson +
  * Solver::run, src/driver/driver.cpp:1545, src/solver/Solver.cpp:483-533). The
  * server runs many such solves at once on one GPU: each request is one
- * Solver::run of its own mesh, order, plane wave and final time, with the
- * plain FP64 operator and classical RK4 (the same arithmetic as dgtd_op_step,
- * so a result is bit-identical alone and in the mix). Requests are admitted as
+ * Solver::run of its own mesh, order, plane wave and final time, with classical
+ * RK4 on the plain FP64 form or the single-instance FP32 form (the same
+ * arithmetic as dgtd_op_step of that form, so a result is bit-identical alone
+ * and in the mix). Requests are admitted as
  * device memory (a fixed budget, allocated once when the server starts) and
  * slots free up; every active request of one order advances in the same
  * kernel launches. Three host threads: admission (mesh tables, memory
@@ -322,6 +332,7 @@ typedef struct dgtd_server_opts {
     int32_t max_active;       /* requests stepping at once, 1..DGTD_SERVER_MAX_ACTIVE */
     int32_t steps_per_round;  /* steps per active request between admission checks (>= 1) */
     int32_t device;           /* CUDA device ordinal */
+    int32_t precision;        /* DGTD_FP64 (plain form) or DGTD_FP32 (single-instance FP32 form) */
 } dgtd_server_opts;
 
 typedef struct dgtd_request {

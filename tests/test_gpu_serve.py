@@ -152,3 +152,24 @@ def test_initial_state_and_no_sources(torch_cuda):
     ref, n = op.run_host(x0, 0.0, 1e-3, 0.05)
     assert st["steps"] == n == 50
     assert np.array_equal(x, ref)
+
+
+def test_fp32_serving_matches_fp32_operator_and_mix(torch_cuda):
+    """FP32 serving runs the single-instance FP32 form's stage: bit-identical to
+    dgtd_op_run_host of that form, alone and in the mix, and within 1e-5 of FP64."""
+    reqs = [scatter_request(n, p, seed=60 + i, T=0.2) for i, (n, p) in enumerate([(4, 3), (5, 2), (4, 4)])]
+    with dg.Server(memory_budget=1 << 30, max_active=8, steps_per_round=3, precision=dg.FP32) as s:
+        ids = [s.submit(r["mesh"], r["order"], r["final_time"], waves=r["waves"], cfl=1.0) for r in reqs]
+        mix = [s.wait(i, timeout=300)[0] for i in ids]
+    for r, xm in zip(reqs, mix):
+        with dg.Server(memory_budget=1 << 30, max_active=2, precision=dg.FP32) as s:
+            alone_x, st = s.wait(s.submit(r["mesh"], r["order"], r["final_time"], waves=r["waves"], cfl=1.0), 300)
+        assert np.array_equal(xm, alone_x)
+        op = dg.Operator(r["mesh"], order=r["order"], precision=dg.FP32)
+        op.set_planewaves(r["waves"])
+        ref32, n = op.run_host(np.zeros(op.state_len), 0.0, op.estimate_dt(1.0), r["final_time"])
+        assert n == st["steps"] and np.array_equal(xm, ref32)
+        op64 = dg.Operator(r["mesh"], order=r["order"])
+        op64.set_planewaves(r["waves"])
+        ref64, _ = op64.run_host(np.zeros(op64.state_len), 0.0, op64.estimate_dt(1.0), r["final_time"])
+        assert rel_l2(xm, ref64) < 1e-5

@@ -6,10 +6,11 @@
 //   RHS^T[(c,b), i] = sum_k W[(c,b), k] * Op[k, i],  Op = [Dr | Ds | Dt | LIFT]^T,
 //
 // with W the per-element operand built on the fly:
-//   k in [0, 3Np)           : (g_r x F, g_s x F, g_t x F) at node k mod Np, where F is the
+//   k in [0, 3Np)           : g_d x F at node j, k = 3 j + d (d = r, s, t), where F is the
 //                             partner field (H for E targets, -E for H targets) and g_r, g_s,
 //                             g_t the element's geometric factors (rows of d(r,s,t)/dx), so the
 //                             product is the curl (reference HesthavenEvolution.cpp:522-534);
+//                             node-major, so a thread's 4 columns touch at most 2 nodes;
 //   k in [3Np, 3Np + 4Nfp)  : Fscale/2 * upwind flux at face node k - 3Np (:509-520).
 // The volume columns come first so that the neighbour traces the flux columns
 // need are loaded while the volume columns are being built.
@@ -87,8 +88,8 @@ struct TcOrd {
 };
 
 // Column metadata: kind in bits 28-29 (0 flux, 1 volume, 2 padding);
-// flux: face node m in bits 16-27, its volume node in bits 0-15;
-// volume: derivative direction (0 r, 1 s, 2 t) in bits 16-23, node in bits 0-15.
+// flux: face node m in bits 16-27, its face in bits 12-15, its volume node in bits 0-11;
+// volume: derivative direction (0 r, 1 s, 2 t) in bits 16-23, node in bits 0-15 (column 3 node + d).
 constexpr int kColFlux = 0, kColVol = 1, kColPad = 2;
 
 __device__ __forceinline__ void pw_eval(const PlaneWaveF32* pw, const int* pw_off, int b, float px, float py, float pz,
@@ -286,8 +287,8 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
     for (int k = tid; k < O::KKp; k += kThreads) {
         int v;
-        if (k < 3 * Np) v = (kColVol << 28) | ((k / Np) << 16) | (k % Np);
-        else if (k < O::KK) v = (kColFlux << 28) | ((k - 3 * Np) << 16) | T.Fmask[k - 3 * Np];
+        if (k < 3 * Np) v = (kColVol << 28) | ((k % 3) << 16) | (k / 3);
+        else if (k < O::KK) v = (kColFlux << 28) | ((k - 3 * Np) << 16) | (((k - 3 * Np) / Nfp) << 12) | T.Fmask[k - 3 * Np];
         else v = kColPad << 28;
         s_col[k] = v;
     }
@@ -352,9 +353,10 @@ __global__ void __launch_bounds__(kThreads, 1)
 #define DGTD_LOAD_NBR(QQ, DST)                                                                          \
     _Pragma("unroll") for (int jj = 0; jj < 4; ++jj)                                                    \
     {                                                                                                   \
-        const int m_ = (QQ) * 8 + kh * 4 + jj - 3 * Np;                                                 \
-        if (m_ >= 0 && m_ < NF) {                                                                       \
-            const int code_ = s_code[m_ / Nfp];                                                         \
+        const int ci_ = s_col[(QQ) * 8 + kh * 4 + jj];                                                   \
+        if ((ci_ >> 28) == kColFlux) {                                                                  \
+            const int m_ = (ci_ >> 16) & 0xfff;                                                         \
+            const int code_ = s_code[(ci_ >> 12) & 0xf];                                                \
             if (code_ == 0 || code_ == 4 || code_ == 5) {                                               \
                 const int32_t gp_ = s_nbr[m_];                                                          \
                 const int32_t en_ = gp_ / Np, node_ = gp_ - en_ * Np;                                   \
@@ -368,13 +370,25 @@ __global__ void __launch_bounds__(kThreads, 1)
             for (int q = grp; q < NKS; q += 2) {
                 if (q + 2 < NKS && (q + 2) * 8 + 7 >= 3 * Np) { DGTD_LOAD_NBR(q + 2, nbn) }
                 float v[6][4];
+                // fields at the (at most two) nodes this thread's volume columns use
+                const int kq0 = q * 8 + kh * 4;
+                const int jA = kq0 / 3;
+                float FA[6], FB[6];
+                if (kq0 < 3 * Np) {
+#pragma unroll
+                    for (int c = 0; c < 6; ++c) FA[c] = s_u[(c * Np + jA) * kChunk + pb];
+                    if (jA + 1 < Np && kq0 + 3 < 3 * Np) {
+#pragma unroll
+                        for (int c = 0; c < 6; ++c) FB[c] = s_u[(c * Np + jA + 1) * kChunk + pb];
+                    }
+                }
 #pragma unroll
                 for (int jj = 0; jj < 4; ++jj) {
                     const int k = q * 8 + kh * 4 + jj;
                     const int ci = s_col[k];
                     const int kind = ci >> 28;
                     if (kind == kColFlux) {
-                        const int m = (ci >> 16) & 0xfff, vm = ci & 0xffff, f = m / Nfp;
+                        const int m = (ci >> 16) & 0xfff, f = (ci >> 12) & 0xf, vm = ci & 0xfff;
                         const int code = s_code[f];
                         const float nx = s_fg[f * 4], ny = s_fg[f * 4 + 1], nz = s_fg[f * 4 + 2];
                         const float hf = 0.5f * s_fg[f * 4 + 3];
@@ -417,9 +431,9 @@ __global__ void __launch_bounds__(kThreads, 1)
                         const float gx = d == 0 ? geo[0] : (d == 1 ? geo[3] : geo[6]);
                         const float gy = d == 0 ? geo[1] : (d == 1 ? geo[4] : geo[7]);
                         const float gz = d == 0 ? geo[2] : (d == 1 ? geo[5] : geo[8]);
-                        const float* uj = s_u + j * kChunk + pb;
-                        const float Ex = uj[0], Ey = uj[Np * kChunk], Ez = uj[2 * Np * kChunk];
-                        const float Hx = uj[3 * Np * kChunk], Hy = uj[4 * Np * kChunk], Hz = uj[5 * Np * kChunk];
+                        const bool a = (j == jA);
+                        const float Ex = a ? FA[0] : FB[0], Ey = a ? FA[1] : FB[1], Ez = a ? FA[2] : FB[2];
+                        const float Hx = a ? FA[3] : FB[3], Hy = a ? FA[4] : FB[4], Hz = a ? FA[5] : FB[5];
                         // E rows: g x H (curl H); H rows: -(g x E) (-curl E)
                         v[0][jj] = gy * Hz - gz * Hy;
                         v[1][jj] = gz * Hx - gx * Hz;
@@ -618,7 +632,7 @@ std::vector<uint32_t> tc_operator_image(const RefTet& ref)
             double v;
             if (k >= 3 * Np) v = ref.LIFT[static_cast<size_t>(i) * NF + (k - 3 * Np)];
             else {
-                const int type = k / Np, j = k - type * Np;
+                const int type = k % 3, j = k / 3;
                 const std::vector<double>& D = type == 0 ? ref.Dr : (type == 1 ? ref.Ds : ref.Dt);
                 v = D[static_cast<size_t>(i) * Np + j];
             }

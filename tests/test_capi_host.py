@@ -81,3 +81,28 @@ def test_reference_tet_tables():
         assert F.shape == (4, (p + 1) * (p + 2) // 2)
         assert np.allclose(R["t"][F[3]], -1) and np.allclose(R["s"][F[2]], -1) and np.allclose(R["r"][F[1]], -1)
         assert np.allclose(R["r"][F[0]] + R["s"][F[0]] + R["t"][F[0]], -1)
+
+
+def test_operator_rejects_bad_options_before_touching_the_device():
+    """Argument checks of dgtd_op_create run before any CUDA call, so they work without a GPU."""
+    m = dg.box_mesh((1, 1, 1))
+    for kw, msg in [(dict(order=0), "order"), (dict(order=7), "order"), (dict(batch=0), "batch"),
+                    (dict(alpha=-1.0), "alpha"), (dict(precision=9), "precision")]:
+        args = dict(order=2, alpha=1.0, precision=dg.FP64, batch=1)
+        args.update(kw)
+        with pytest.raises(dg.DgtdError, match=msg):
+            dg.Operator(m, **args)
+    empty = dg.Mesh(np.zeros((0, 3)), np.zeros((0, 4), np.int32))
+    with pytest.raises(dg.DgtdError):
+        dg.validate_mesh(empty)
+
+
+def test_server_and_case_argument_checks():
+    with pytest.raises(dg.DgtdError, match="memory_budget"):
+        dg.Server(memory_budget=0)
+    with pytest.raises(dg.DgtdError, match="max_active"):
+        dg.Server(max_active=1000)
+    with pytest.raises(dg.DgtdError, match="precision"):
+        dg.Server(precision=dg.FP32_3XTF32)
+    with pytest.raises(dg.DgtdError, match="cannot open case"):
+        dg.Case("/nonexistent/case.json")

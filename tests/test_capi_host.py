@@ -106,3 +106,13 @@ def test_server_and_case_argument_checks():
         dg.Server(precision=dg.FP32_3XTF32)
     with pytest.raises(dg.DgtdError, match="cannot open case"):
         dg.Case("/nonexistent/case.json")
+
+
+def test_missing_library_fails_loudly(monkeypatch, tmp_path):
+    """There is no CPU fallback: without the CUDA library every entry point raises."""
+    monkeypatch.setattr(dg, "LIB_PATH", tmp_path / "libdgtd_gb300.so")
+    monkeypatch.setattr(dg, "_lib_handle", None)
+    with pytest.raises(ImportError, match="missing"):
+        dg.lib()
+    with pytest.raises(ImportError):
+        dg.box_mesh((1, 1, 1))

@@ -6,6 +6,7 @@
 // incidences, so every load and store of the element's fields, its face
 // traces and its neighbours' traces is a coalesced 128-byte row.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -318,16 +319,24 @@ uint64_t morton3(uint32_t x, uint32_t y, uint32_t z)
     return spread(x) | (spread(y) << 1) | (spread(z) << 2);
 }
 
+// True the first time it is called for the current device (per call site): the
+// dynamic shared-memory attribute of a kernel is set once per device, thread-safely.
+inline bool first_use_on_device(std::atomic<uint64_t>& seen)
+{
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const uint64_t bit = uint64_t(1) << (dev & 63);
+    return (seen.fetch_or(bit) & bit) == 0;
+}
+
 template <int P, int W>
 void launch_stage_w(const BatchedTables& T, const BatchedStageArgs& A, cudaStream_t s)
 {
     using O = OrdB<P>;
-    static bool attr = false;
-    if (!attr) {
+    static std::atomic<uint64_t> seen{0};
+    if (first_use_on_device(seen))
         ckb(cudaFuncSetAttribute(stage_f32<P, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(O::smem)),
             "smem attribute");
-        attr = true;
-    }
     dim3 grid(static_cast<unsigned>(T.K), static_cast<unsigned>(T.Bpad / kLanes));
     stage_f32<P, W><<<grid, W * kLanes, O::smem, s>>>(T, A);
     ckb(cudaGetLastError(), "batched stage kernel");
@@ -391,6 +400,7 @@ std::unique_ptr<BatchedOp> BatchedOp::create(const RefTet& ref, const MeshTables
     for (int q = 0; q < Np * Np; ++q) { D[q] = ref.Dr[q]; D[Np * Np + q] = ref.Ds[q]; D[2 * Np * Np + q] = ref.Dt[q]; }
     for (size_t q = 0; q < L.size(); ++q) L[q] = static_cast<float>(ref.LIFT[q]);
     std::vector<int32_t> vmapP(K * 4 * Nfp), fcode(K * 4);
+    std::vector<float> fbc(K * 20, 0.0f);
     std::vector<float> fxyz(K * 4 * Nfp * 3, 0.0f);
     bool has_tfsf = false;
     for (int64_t ei = 0; ei < K; ++ei) {
@@ -401,6 +411,23 @@ std::unique_ptr<BatchedOp> BatchedOp::create(const RefTet& ref, const MeshTables
         for (int f = 0; f < 4; ++f) {
             const int fc = mesh.fcode[er * 4 + f];
             fcode[ei * 4 + f] = fc;
+            // boundary rules as jump coefficients (reference DGOperatorFactory.h:21-45, 486-495):
+            // interior / TF-SF: d = u+ - u-; PEC: dE = -2E-, dH = 0; PMC: dE = 0, dH = -2H-;
+            // SMA: d = -u- with penalty 1; open: d = 0
+            float* cb = &fbc[(ei * 4 + f) * 5];
+            const float alpha = static_cast<float>(dev.alpha);
+            switch (fc) {
+            case FACE_INTERIOR: case FACE_TFSF_TF: case FACE_TFSF_SF:
+                cb[0] = 1.0f; cb[1] = -1.0f; cb[2] = 1.0f; cb[3] = -1.0f; cb[4] = alpha; break;
+            case FACE_PEC: case FACE_INT_PEC:
+                cb[0] = 0.0f; cb[1] = -2.0f; cb[2] = 0.0f; cb[3] = 0.0f; cb[4] = alpha; break;
+            case FACE_PMC: case FACE_INT_PMC:
+                cb[0] = 0.0f; cb[1] = 0.0f; cb[2] = 0.0f; cb[3] = -2.0f; cb[4] = alpha; break;
+            case FACE_SMA: case FACE_INT_SMA:
+                cb[0] = 0.0f; cb[1] = -1.0f; cb[2] = 0.0f; cb[3] = -1.0f; cb[4] = 1.0f; break;
+            default:
+                cb[4] = alpha; break;
+            }
             if (fc == FACE_TFSF_TF || fc == FACE_TFSF_SF) has_tfsf = true;
             for (int a = 0; a < Nfp; ++a) {
                 const int32_t g = mesh.vmapP[(er * 4 + f) * Nfp + a];
@@ -437,7 +464,7 @@ std::unique_ptr<BatchedOp> BatchedOp::create(const RefTet& ref, const MeshTables
     T.alpha = static_cast<float>(dev.alpha);
     T.D = up(D); T.LIFT = up(L); T.Fmask = up(ref.Fmask);
     T.geo = up(geo); T.fgeo = up(fgeo); T.mat = up(mat);
-    T.vmapP = up(vmapP); T.fcode = up(fcode); T.fxyz = up(fxyz);
+    T.vmapP = up(vmapP); T.fcode = up(fcode); T.fxyz = up(fxyz); T.fbc = up(fbc);
     T.nxyz = up(nxyz); T.n_tfsf_nodes = nt;
     op->perm_ = const_cast<int32_t*>(up(perm));
     op->op_img_ = up(tc_operator_image(ref));

@@ -35,6 +35,8 @@ struct BatchedTables {
     const float* mat;      // [K][3]
     const int32_t* vmapP;  // [K][4][Nfp]  neighbour (element' * Np + node), internal numbering
     const int32_t* fcode;  // [K][4]
+    const float* fbc;      // [K][4][5] per face: jump coefficients cE1 cE2 cH1 cH2 (dE = cE1 E+ + cE2 E-,
+                           // dH = cH1 H+ + cH2 H-) and the penalty coefficient of the face
     const float* fxyz;     // [K][4][Nfp][3] face-node coordinates (TF/SF source evaluation)
     const float* nxyz;     // [3][n_tfsf_nodes] coordinates of the TF/SF-submesh nodes (skip test)
     int64_t n_tfsf_nodes;

@@ -40,6 +40,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstdint>
 #include <cstring>
 #include <stdexcept>
@@ -80,8 +81,8 @@ struct TcOrd {
     static constexpr int OpBytes = NKS * OpStep;            // per hi / lo
     static constexpr int UBytes = 6 * Np * kChunk * 4;      // staged element block
     static constexpr int NbrBytes = (4 * NF + 15) / 16 * 16;
-    // U | neighbour table | face geometry (16 floats) | face codes (4 ints)
-    static constexpr int UBufBytes = (UBytes + NbrBytes + 64 + 16 + 127) / 128 * 128;
+    // U | neighbour table | face geometry (16 floats) | face codes (4 ints) | jump coefficients (20 floats)
+    static constexpr int UBufBytes = (UBytes + NbrBytes + 64 + 16 + 80 + 127) / 128 * 128;
     static constexpr size_t smem = 2 * static_cast<size_t>(OpBytes) + 2 * static_cast<size_t>(UBufBytes) +
                                    2 * static_cast<size_t>(kSlot);
     static_assert(3 * N <= static_cast<int>(kAccStride), "accumulator buffer too narrow");
@@ -154,7 +155,7 @@ __device__ __forceinline__ void prefetch_item(const BatchedTables& T, const floa
     const int g = static_cast<int>(w - e * nchunk);
     const int64_t EB = 6 * static_cast<int64_t>(Np) * Bp;
     const float* src = in + e * EB + static_cast<int64_t>(g) * kChunk;
-    mbar_expect_tx(bar, O::UBytes + 4 * NF + 64 + 16);
+    mbar_expect_tx(bar, O::UBytes + 4 * NF + 64 + 16 + 80);
     if (Bp == kChunk) {
         bulk_g2s(buf, src, O::UBytes, bar);
     } else {
@@ -164,6 +165,7 @@ __device__ __forceinline__ void prefetch_item(const BatchedTables& T, const floa
     bulk_g2s(buf + O::UBytes, T.vmapP + e * NF, 4 * NF, bar);
     bulk_g2s(buf + O::UBytes + O::NbrBytes, T.fgeo + e * 16, 64, bar);
     bulk_g2s(buf + O::UBytes + O::NbrBytes + 64, T.fcode + e * 4, 16, bar);
+    bulk_g2s(buf + O::UBytes + O::NbrBytes + 80, T.fbc + e * 20, 80, bar);
 }
 
 // The RK registers the epilogue of work item w reads, brought into L2 ahead of
@@ -337,6 +339,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             const int32_t* s_nbr = reinterpret_cast<const int32_t*>(buf + O::UBytes);
             const float* s_fg = reinterpret_cast<const float*>(buf + O::UBytes + O::NbrBytes);
             const int* s_code = reinterpret_cast<const int*>(buf + O::UBytes + O::NbrBytes + 64);
+            const float* s_bc = reinterpret_cast<const float*>(buf + O::UBytes + O::NbrBytes + 80);
             if (flag_set(&s_err) || !tc::mbar_wait(&u_full[ub], (it >> 1) & 1)) { err = true; break; }
             const int64_t e = w / nchunk;
             const int g = static_cast<int>(w - e * nchunk);
@@ -362,6 +365,8 @@ __global__ void __launch_bounds__(kThreads, 1)
                 const int32_t en_ = gp_ / Np, node_ = gp_ - en_ * Np;                                   \
                 const float* __restrict__ un_ = nin + static_cast<int64_t>(en_) * EB + node_ * Bp;      \
                 _Pragma("unroll") for (int c = 0; c < 6; ++c) DST[jj][c] = __ldg(un_ + c * CB);         \
+            } else {                                                                                    \
+                _Pragma("unroll") for (int c = 0; c < 6; ++c) DST[jj][c] = 0.0f;                        \
             }                                                                                           \
         }                                                                                               \
     }
@@ -389,34 +394,26 @@ __global__ void __launch_bounds__(kThreads, 1)
                     const int kind = ci >> 28;
                     if (kind == kColFlux) {
                         const int m = (ci >> 16) & 0xfff, f = (ci >> 12) & 0xf, vm = ci & 0xfff;
-                        const int code = s_code[f];
-                        const float nx = s_fg[f * 4], ny = s_fg[f * 4 + 1], nz = s_fg[f * 4 + 2];
-                        const float hf = 0.5f * s_fg[f * 4 + 3];
+                        const float4 fg = reinterpret_cast<const float4*>(s_fg)[f];
+                        const float nx = fg.x, ny = fg.y, nz = fg.z;
+                        const float hf = 0.5f * fg.w;
+                        const float* bc = s_bc + f * 5;
+                        const float cE1 = bc[0], cE2 = bc[1], cH1 = bc[2], cH2 = bc[3];
+                        const float aE = bc[4], aH = bc[4];
                         float uM[6];
 #pragma unroll
                         for (int c = 0; c < 6; ++c) uM[c] = s_u[(c * Np + vm) * kChunk + pb];
+                        // jumps with the boundary rule of the face (branch-free: neighbour traces are
+                        // zero where the coefficient is)
                         float dE[3], dH[3];
-                        float aE = T.alpha, aH = T.alpha;
-                        if (code == 0 || code == 4 || code == 5) {
 #pragma unroll
-                            for (int c = 0; c < 3; ++c) {
-                                dE[c] = nb[jj][c] - uM[c];
-                                dH[c] = nb[jj][c + 3] - uM[c + 3];
-                            }
-                            if (code != 0 && !skip_src) tfsf_source(A, T.fxyz + (e * NF + m) * 3, b, code, dE, dH);
-                        } else if (code == 1 || code == 6) {
-#pragma unroll
-                            for (int c = 0; c < 3; ++c) { dE[c] = -2.0f * uM[c]; dH[c] = 0.0f; }
-                        } else if (code == 2 || code == 7) {
-#pragma unroll
-                            for (int c = 0; c < 3; ++c) { dE[c] = 0.0f; dH[c] = -2.0f * uM[c + 3]; }
-                        } else if (code == 3 || code == 8) {
-#pragma unroll
-                            for (int c = 0; c < 3; ++c) { dE[c] = -uM[c]; dH[c] = -uM[c + 3]; }
-                            aE = 1.0f; aH = 1.0f;
-                        } else {
-#pragma unroll
-                            for (int c = 0; c < 3; ++c) { dE[c] = 0.0f; dH[c] = 0.0f; }
+                        for (int c = 0; c < 3; ++c) {
+                            dE[c] = cE1 * nb[jj][c] + cE2 * uM[c];
+                            dH[c] = cH1 * nb[jj][c + 3] + cH2 * uM[c + 3];
+                        }
+                        if (!skip_src) {
+                            const int code = s_code[f];
+                            if (code == 4 || code == 5) tfsf_source(A, T.fxyz + (e * NF + m) * 3, b, code, dE, dH);
                         }
                         const float ndE = nx * dE[0] + ny * dE[1] + nz * dE[2];
                         const float ndH = nx * dH[0] + ny * dH[1] + nz * dH[2];
@@ -649,16 +646,25 @@ std::vector<uint32_t> tc_operator_image(const RefTet& ref)
 
 namespace {
 
+// True the first time it is called for the current device (per call site): the
+// dynamic shared-memory attribute of a kernel is set once per device, thread-safely.
+inline bool first_use_on_device(std::atomic<uint64_t>& seen)
+{
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const uint64_t bit = uint64_t(1) << (dev & 63);
+    return (seen.fetch_or(bit) & bit) == 0;
+}
+
 template <int P, int MODE>
 void launch_tc_instance(const BatchedTables& T, const BatchedStageArgs& A, const uint32_t* op_img, int* status,
                         int64_t grid, int64_t n_work, cudaStream_t s)
 {
-    static bool attr = false;
-    if (!attr) {
+    static std::atomic<uint64_t> seen{0};
+    if (first_use_on_device(seen)) {
         cudaError_t e = cudaFuncSetAttribute(stage_tc<P, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              static_cast<int>(TcOrd<P>::smem));
         if (e != cudaSuccess) throw std::runtime_error(std::string("tc smem attribute: ") + cudaGetErrorString(e));
-        attr = true;
     }
     stage_tc<P, MODE><<<static_cast<unsigned>(grid), kThreads, TcOrd<P>::smem, s>>>(T, A, op_img, n_work, status);
     cudaError_t e = cudaGetLastError();

@@ -11,6 +11,8 @@
 #include <string>
 #include <vector>
 
+#include "skipbound.hpp"
+
 #include "../../include/dgtd_gb300.h"
 #include "batched.hpp"
 #include "kernels.hpp"
@@ -22,6 +24,9 @@ namespace {
 
 thread_local std::string g_err;
 std::atomic<uint64_t> g_launches{0};   // kernels launched by this library (all threads)
+
+// Skip flags a stage reads when the host has decided the TF/SF skip test.
+__device__ const int kDecidedSkip[2] = {0, 1};
 
 int fail(int code, const std::string& msg)
 {
@@ -85,6 +90,9 @@ struct dgtd_op {
     dgtd::PlaneWaveDev* pw_dev = nullptr;
     int pw_cap = 0;
     int* skip_dev = nullptr;
+    dgtd::SkipScratch skip_sc;          // split skip test: per-part sums and tickets
+    dgtd::TfsfSkipBound skip_bound;     // one incidence, one plain wave: host bounds of the skip test
+    const int* skip_const = nullptr;    // device flags {0, 1} a stage reads when the host decided
     double* norm_dev = nullptr;
     // RK scratch (allocated on first dgtd_op_step)
     double* ws = nullptr;
@@ -186,13 +194,16 @@ void run_stage(dgtd_op* op, dgtd::StageArgs A, double t, cudaStream_t s)
     A.t = t;
     A.batch = op->batch;
     if (has_sources(op)) {
-        ck(dgtd::launch_tfsf_skip(op->dev, op->pw_dev, static_cast<int>(op->pw_host.size()), op->batch, t,
-                                  op->skip_dev, s),
-           "tfsf skip kernel");
-        g_launches.fetch_add(1, std::memory_order_relaxed);
+        const int known = op->skip_bound.decide(t);
+        if (known < 0) {
+            ck(dgtd::launch_tfsf_skip(op->dev, op->pw_dev, static_cast<int>(op->pw_host.size()), op->batch, t,
+                                      op->skip_dev, op->skip_sc, s),
+               "tfsf skip kernel");
+            g_launches.fetch_add(1, std::memory_order_relaxed);
+        }
         A.pw = op->pw_dev;
         A.n_pw = static_cast<int>(op->pw_host.size());
-        A.skip = op->skip_dev;
+        A.skip = known < 0 ? op->skip_dev : op->skip_const + known;
     } else {
         A.pw = nullptr;
         A.n_pw = 0;
@@ -254,13 +265,16 @@ void run_stage32(dgtd_op* op, dgtd::StageArgsF32 A, double t, cudaStream_t s)
     A.t = t;
     A.batch = op->batch;
     if (has_sources(op)) {
-        ck(dgtd::launch_tfsf_skip_f32s(op->dev32, op->pw_dev, static_cast<int>(op->pw_host.size()), op->batch, t,
-                                       op->skip_dev, s),
-           "tfsf skip kernel");
-        g_launches.fetch_add(1, std::memory_order_relaxed);
+        const int known = op->skip_bound.decide(t);
+        if (known < 0) {
+            ck(dgtd::launch_tfsf_skip_f32s(op->dev32, op->pw_dev, static_cast<int>(op->pw_host.size()), op->batch, t,
+                                           op->skip_dev, op->skip_sc, s),
+               "tfsf skip kernel");
+            g_launches.fetch_add(1, std::memory_order_relaxed);
+        }
         A.pw = op->pw_dev;
         A.n_pw = static_cast<int>(op->pw_host.size());
-        A.skip = op->skip_dev;
+        A.skip = known < 0 ? op->skip_dev : op->skip_const + known;
     } else {
         A.pw = nullptr;
         A.n_pw = 0;
@@ -366,6 +380,18 @@ int dgtd_op_create(const dgtd_mesh_desc* mesh, const dgtd_op_opts* opts, dgtd_op
         T.tfsf_elems = op->up(op->mesh.tfsf_elems);
         T.n_tfsf_elems = static_cast<int64_t>(op->mesh.tfsf_elems.size());
         ck(cudaMalloc(&op->skip_dev, op->batch * sizeof(int)), "cudaMalloc skip");
+        op->skip_sc.parts = dgtd::tfsf_skip_parts(T.n_tfsf_elems * T.Np);
+        ck(cudaMalloc(&op->skip_sc.partial, static_cast<size_t>(op->batch) * op->skip_sc.parts * sizeof(double)),
+           "cudaMalloc skip partials");
+        op->allocs.push_back(op->skip_sc.partial);
+        ck(cudaMalloc(&op->skip_sc.ticket, op->batch * sizeof(unsigned int)), "cudaMalloc skip tickets");
+        op->allocs.push_back(op->skip_sc.ticket);
+        ck(cudaMemset(op->skip_sc.ticket, 0, op->batch * sizeof(unsigned int)), "memset skip tickets");
+        {
+            void* a = nullptr;
+            ck(cudaGetSymbolAddress(&a, kDecidedSkip), "skip flag symbol");
+            op->skip_const = static_cast<const int*>(a);
+        }
         ck(cudaMalloc(&op->norm_dev, (op->batch + 32) * sizeof(double)), "cudaMalloc norm");
         if (op->precision == DGTD_FP32_3XTF32) op->batched = dgtd::BatchedOp::create(op->ref, op->mesh, op->dev, op->batch);
         if (op->precision == DGTD_FP32) {
@@ -459,6 +485,9 @@ int dgtd_op_set_planewaves(dgtd_op* op, const dgtd_planewave* pw, int32_t n)
     }
     try {
         op->pw_host = v;
+        op->skip_bound = (op->batch == 1 && v.size() == 1)
+                             ? dgtd::TfsfSkipBound(op->mesh.x, op->mesh.y, op->mesh.z, op->mesh.tfsf_elems, op->ref.Np, v[0])
+                             : dgtd::TfsfSkipBound();
         ensure_sources(op);
         if (op->batched) op->batched->set_sources(op->pw_host);
     } catch (const std::exception& e) {

@@ -268,5 +268,52 @@ __device__ __forceinline__ void tfsf_skip_body(const TablesT<R>& T, const PlaneW
     if (threadIdx.x == 0) *skip = (red[0] < 1e-16) ? 1 : 0;
 }
 
+// The same sum split over gridDim.y blocks per incidence: block `part` adds its contiguous
+// share of the TF/SF nodes, and the last block of the incidence to finish (ticket) adds the
+// partial sums in part order, so the decision does not depend on block scheduling.
+template <typename R = double>
+__device__ __forceinline__ void tfsf_skip_part_body(const TablesT<R>& T, const PlaneWaveDev* pw, int n_pw, int b,
+                                                   double t, double* partial, unsigned int* ticket, int* skip)
+{
+    const int part = blockIdx.y, nparts = gridDim.y;
+    const int64_t total = T.n_tfsf_elems * T.Np;
+    // node indices fit in 32 bits (vmapP is int32), so the index arithmetic is 32-bit
+    const int lo = static_cast<int>(total * part / nparts), hi = static_cast<int>(total * (part + 1) / nparts);
+    const int Np = T.Np;
+    double acc = 0.0;
+    for (int w = lo + static_cast<int>(threadIdx.x); w < hi; w += blockDim.x) {
+        const int el = w / Np;
+        const int64_t gm = static_cast<int64_t>(T.tfsf_elems[el]) * Np + (w - el * Np);
+        R pe[3], ph[3];
+        eval_pw<R>(pw, n_pw, b, T.xyz[gm], T.xyz[T.N + gm], T.xyz[2 * T.N + gm], static_cast<R>(t), pe, ph);
+        for (int c = 0; c < 3; ++c) {
+            const double a = 0.5 * static_cast<double>(pe[c]), h = 0.5 * static_cast<double>(ph[c]);
+            acc += a * a + h * h;
+        }
+    }
+    __shared__ double red[256];
+    __shared__ bool last;
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        partial[static_cast<int64_t>(b) * nparts + part] = red[0];
+        __threadfence();
+        last = atomicAdd(&ticket[b], 1u) == static_cast<unsigned int>(nparts - 1);
+    }
+    __syncthreads();
+    if (last && threadIdx.x == 0) {
+        __threadfence();
+        const volatile double* pv = partial + static_cast<int64_t>(b) * nparts;
+        double sum = 0.0;
+        for (int q = 0; q < nparts; ++q) sum += pv[q];
+        skip[b] = (sum < 1e-16) ? 1 : 0;
+        ticket[b] = 0u;
+    }
+}
+
 }  // namespace fp64
 }  // namespace dgtd

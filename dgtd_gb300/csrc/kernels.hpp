@@ -82,8 +82,22 @@ cudaError_t launch_stage_fp64(const TablesDev& T, const StageArgs& A, cudaStream
 
 // Per-incidence TF/SF skip decision (reference GlobalEvolution.cpp:587-598):
 // skip[b] = (sum over TF/SF-submesh nodes and components of (0.5 pw)^2 < 1e-16).
+// The sum is split over `parts` blocks per incidence (partial: batch x parts doubles; ticket:
+// batch counters, zero between launches).
+struct SkipScratch {
+    double* partial = nullptr;
+    unsigned int* ticket = nullptr;
+    int parts = 1;
+};
+
+// Blocks per incidence of the split skip test: about 8192 TF/SF nodes per block, 1..64.
+inline int tfsf_skip_parts(int64_t tfsf_nodes)
+{
+    const int64_t p = (tfsf_nodes + 8191) / 8192;
+    return static_cast<int>(p < 1 ? 1 : (p > 64 ? 64 : p));
+}
 cudaError_t launch_tfsf_skip(const TablesDev& T, const PlaneWaveDev* pw, int n_pw, int batch,
-                             double t, int* skip, cudaStream_t s);
+                             double t, int* skip, const SkipScratch& sc, cudaStream_t s);
 
 // Squared L2 norm of each incidence's state: out[b] = sum_i in[b][i]^2.
 cudaError_t launch_norm2(const double* in, int64_t n_per_batch, int batch, double* out, cudaStream_t s);
@@ -92,7 +106,7 @@ cudaError_t launch_norm2(const double* in, int64_t n_per_batch, int batch, doubl
 // reference layout, one thread per node.
 cudaError_t launch_stage_f32s(const TablesF32& T, const StageArgsF32& A, cudaStream_t s);
 cudaError_t launch_tfsf_skip_f32s(const TablesF32& T, const PlaneWaveDev* pw, int n_pw, int batch, double t, int* skip,
-                                  cudaStream_t s);
+                                  const SkipScratch& sc, cudaStream_t s);
 cudaError_t launch_norm2_f32s(const float* in, int64_t n_per_batch, int batch, double* out, cudaStream_t s);
 cudaError_t launch_convert_f64_to_f32(const double* in, float* out, int64_t n, cudaStream_t s);
 cudaError_t launch_convert_f32_to_f64(const float* in, double* out, int64_t n, cudaStream_t s);

@@ -19,9 +19,10 @@ __global__ void __launch_bounds__(kBlock) stage_fp64(TablesDev T, StageArgs A)
     fp64::stage_body<P>(T, A, static_cast<int64_t>(blockIdx.x) * Ord<P>::EPB, static_cast<int>(blockIdx.y));
 }
 
-__global__ void tfsf_skip_kernel(TablesDev T, const PlaneWaveDev* pw, int n_pw, double t, int* skip)
+__global__ void __launch_bounds__(256) tfsf_skip_kernel(TablesDev T, const PlaneWaveDev* pw, int n_pw, double t,
+                                                        double* partial, unsigned int* ticket, int* skip)
 {
-    fp64::tfsf_skip_body(T, pw, n_pw, static_cast<int>(blockIdx.x), t, skip + blockIdx.x);
+    fp64::tfsf_skip_part_body(T, pw, n_pw, static_cast<int>(blockIdx.x), t, partial, ticket, skip);
 }
 
 __global__ void norm2_kernel(const double* in, int64_t n, double* out)
@@ -65,9 +66,9 @@ cudaError_t launch_stage_fp64(const TablesDev& T, const StageArgs& A, cudaStream
 }
 
 cudaError_t launch_tfsf_skip(const TablesDev& T, const PlaneWaveDev* pw, int n_pw, int batch, double t, int* skip,
-                             cudaStream_t s)
+                             const SkipScratch& sc, cudaStream_t s)
 {
-    tfsf_skip_kernel<<<batch, 256, 0, s>>>(T, pw, n_pw, t, skip);
+    tfsf_skip_kernel<<<dim3(batch, sc.parts), 256, 0, s>>>(T, pw, n_pw, t, sc.partial, sc.ticket, skip);
     return cudaGetLastError();
 }
 

@@ -40,6 +40,7 @@
 
 #include "../../include/dgtd_gb300.h"
 #include "arena.hpp"
+#include "skipbound.hpp"
 #include "fp64_stage.cuh"
 #include "mesh.hpp"
 #include "refelem.hpp"
@@ -271,8 +272,7 @@ struct Req {
     int Np = 0, Nfp = 0;
     int64_t n_tfsf = 0;
     Layout lay{};
-    // one plain Gaussian wave: sorted x.k of the TF/SF-submesh nodes (host bounds of the skip test)
-    std::vector<double> tfsf_s;
+    dgtd::TfsfSkipBound skip_bound;   // one plain Gaussian wave: host bounds of the skip test
     int64_t off = -1;
     int pos = -1;
     // stepping
@@ -404,16 +404,8 @@ void admission_loop(dgtd_server* s)
             r->Nfp = O.ref.Nfp;
             r->n_tfsf = static_cast<int64_t>(tab.tfsf_elems.size());
             r->lay = layout(r->K, r->Np, r->Nfp, r->n_tfsf, s->fp32 ? 4 : 8);
-            if (r->waves.size() == 1 && r->waves[0].freq == 0.0 && r->n_tfsf > 0) {
-                const auto& w = r->waves[0];
-                r->tfsf_s.reserve(static_cast<size_t>(r->n_tfsf) * r->Np);
-                for (int32_t e : tab.tfsf_elems)
-                    for (int i = 0; i < r->Np; ++i) {
-                        const size_t g = static_cast<size_t>(e) * r->Np + i;
-                        r->tfsf_s.push_back(tab.x[g] * w.k[0] + tab.y[g] * w.k[1] + tab.z[g] * w.k[2]);
-                    }
-                std::sort(r->tfsf_s.begin(), r->tfsf_s.end());
-            }
+            if (r->waves.size() == 1)
+                r->skip_bound = dgtd::TfsfSkipBound(tab.x, tab.y, tab.z, tab.tfsf_elems, r->Np, r->waves[0]);
             if (!r->init.empty() && static_cast<int64_t>(r->init.size()) != 6 * r->K * r->Np)
                 throw ServeError(DGTD_ERR_INVALID, "initial state has the wrong length for this mesh and order");
             if (!(r->dt > 0.0)) {
@@ -464,28 +456,6 @@ void admission_loop(dgtd_server* s)
 }
 
 bool running(const Req& r) { return r.t <= r.T - 1e-8 * r.dt; }
-
-// TF/SF skip test of one request at stage time t, decided on the host when it is clear
-// (reference GlobalEvolution.cpp:587-598: skip while ||0.5 pw||^2 < 1e-16 over the TF/SF
-// submesh nodes). For one plain Gaussian wave each node contributes between 0.25 g^2 and
-// 0.5 g^2 (g the Gaussian at the node), so the nearest node to the pulse centre bounds the
-// sum from below and the node count times its term from above. Returns 0 / 1, or -1 when
-// the sum is within a factor 10 of the threshold: the device then computes it exactly.
-int host_skip(const Req& r, double t)
-{
-    if (r.tfsf_s.empty()) return -1;
-    const auto& w = r.waves[0];
-    const double centre = t + w.mean;
-    auto it = std::lower_bound(r.tfsf_s.begin(), r.tfsf_s.end(), centre);
-    double d = std::numeric_limits<double>::infinity();
-    if (it != r.tfsf_s.end()) d = std::min(d, *it - centre);
-    if (it != r.tfsf_s.begin()) d = std::min(d, centre - *(it - 1));
-    const double g2 = std::exp(-d * d / (w.spread * w.spread));
-    const double lower = 0.25 * g2, upper = 0.5 * static_cast<double>(r.tfsf_s.size()) * g2;
-    if (lower > 1e-15) return 0;
-    if (upper < 1e-17) return 1;
-    return -1;
-}
 
 void engine_loop(dgtd_server* s)
 {
@@ -561,7 +531,7 @@ void engine_loop(dgtd_server* s)
                         bool any_device_test = false;
                         for (int i = 0; i < L.n; ++i) {
                             SlotParam& S = L.s[i];
-                            S.skip_known = (S.n_pw > 0 && S.n_tfsf > 0) ? host_skip(*in_launch[i], S.t + cs[q] * S.dt) : 0;
+                            S.skip_known = (S.n_pw > 0 && S.n_tfsf > 0) ? in_launch[i]->skip_bound.decide(S.t + cs[q] * S.dt) : 0;
                             any_device_test = any_device_test || (S.n_pw > 0 && S.n_tfsf > 0 && S.skip_known < 0);
                         }
                         ck(launch_stage(s->fp32, o, L, blocks, any_src && any_device_test, st), "serving stage kernel");

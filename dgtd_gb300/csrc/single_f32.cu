@@ -20,9 +20,10 @@ __global__ void __launch_bounds__(kBlock) stage_f32s(TablesF32 T, StageArgsF32 A
     fp64::stage_body<P, float>(T, A, static_cast<int64_t>(blockIdx.x) * Ord<P>::EPB, static_cast<int>(blockIdx.y));
 }
 
-__global__ void __launch_bounds__(256) tfsf_skip_f32s(TablesF32 T, const PlaneWaveDev* pw, int n_pw, double t, int* skip)
+__global__ void __launch_bounds__(256) tfsf_skip_f32s(TablesF32 T, const PlaneWaveDev* pw, int n_pw, double t,
+                                                      double* partial, unsigned int* ticket, int* skip)
 {
-    fp64::tfsf_skip_body<float>(T, pw, n_pw, static_cast<int>(blockIdx.x), t, skip + blockIdx.x);
+    fp64::tfsf_skip_part_body<float>(T, pw, n_pw, static_cast<int>(blockIdx.x), t, partial, ticket, skip);
 }
 
 __global__ void __launch_bounds__(256) norm2_f32s(const float* in, int64_t n, double* out)
@@ -81,9 +82,9 @@ cudaError_t launch_stage_f32s(const TablesF32& T, const StageArgsF32& A, cudaStr
 }
 
 cudaError_t launch_tfsf_skip_f32s(const TablesF32& T, const PlaneWaveDev* pw, int n_pw, int batch, double t, int* skip,
-                                  cudaStream_t s)
+                                  const SkipScratch& sc, cudaStream_t s)
 {
-    tfsf_skip_f32s<<<batch, 256, 0, s>>>(T, pw, n_pw, t, skip);
+    tfsf_skip_f32s<<<dim3(batch, sc.parts), 256, 0, s>>>(T, pw, n_pw, t, sc.partial, sc.ticket, skip);
     return cudaGetLastError();
 }
 

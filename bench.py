@@ -5,8 +5,10 @@ prints ONE JSON line on rank 0.
 
 A "step" is one full RK4 time step (all stages) of the workload over its mesh.
 ``value`` is the device-timed rate with inputs resident in HBM; ``e2e`` is the
-same metric through the C ABI with host buffers (host->device copy of the
-state, the step, device->host read of the state) inside the timed region.
+same metric through the C ABI with host buffers: every step's host->device copy
+of its whole state, the step and the device->host read of the result are inside
+the timed region, with consecutive steps pipelined (upload of step k+1 and
+download of step k-1 overlap step k's compute).
 
 N > 1: the path is replicas only (independent solves, no collective); every
 rank runs its own copy of the workload on its GPU and ``value`` sums them.
@@ -360,26 +362,45 @@ def run_ours(args, world, rank, local):
     if not bool(torch.isfinite(state).all()):
         raise RuntimeError("non-finite state after the timed steps")
 
-    # --- end to end through the C ABI with host buffers (pinned): every step copies the working
-    # state in, steps it and reads it back
+    # --- end to end through the C ABI with host buffers (pinned): every step uploads its whole
+    # working state from host memory, steps it (dgtd_op_step) and downloads the result. Steps are
+    # independent jobs, pipelined the way a caller streams them: step k+1's upload and step k-1's
+    # download (own copy streams) overlap step k's compute, with three device buffers.
     host = state.detach().cpu().pin_memory()
     out = torch.empty_like(host).pin_memory()
-    dstate = torch.empty_like(state)
-    e2e_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    nbuf = 3
+    dbufs = [torch.empty_like(state) for _ in range(nbuf)]
+    s_up, s_down = torch.cuda.Stream(dev), torch.cuda.Stream(dev)
+    ev = lambda: torch.cuda.Event(enable_timing=False)
+    up_done = [ev() for _ in range(args.steps)]
+    comp_done = [ev() for _ in range(args.steps)]
+    down_done = [ev() for _ in range(args.steps)]
+    e2e_start, e2e_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     t2 = t
     torch.cuda.synchronize(dev)
+    e2e_start.record(s_up)
     for k in range(args.steps):
+        buf = dbufs[k % nbuf]
+        if k >= nbuf:
+            s_up.wait_event(down_done[k - nbuf])          # the buffer's previous result is downloaded
+        with torch.cuda.stream(s_up):
+            buf.copy_(host, non_blocking=True)
+            up_done[k].record(s_up)
+        stream.wait_event(up_done[k])
         flush.zero_()
-        e2e_ev[k][0].record(stream)
-        dstate.copy_(host, non_blocking=True)
-        op.step(dstate, t2, dt, 1, stream=stream)
-        out.copy_(dstate, non_blocking=True)
-        e2e_ev[k][1].record(stream)
+        op.step(buf, t2, dt, 1, stream=stream)
+        comp_done[k].record(stream)
+        s_down.wait_event(comp_done[k])
+        with torch.cuda.stream(s_down):
+            out.copy_(buf, non_blocking=True)
+            down_done[k].record(s_down)
         t2 += dt
+    stream.wait_event(down_done[args.steps - 1])
+    e2e_end.record(stream)
     torch.cuda.synchronize(dev)
-    e2e_s = max_over_ranks(sum(a.elapsed_time(b) for a, b in e2e_ev) / 1e3, world, dev)
+    e2e_s = max_over_ranks(e2e_start.elapsed_time(e2e_end) / 1e3, world, dev)
     state_bytes = int(host.numel() * host.element_size())
-    del dstate, host, out
+    del dbufs, host, out
 
     # --- roofline of the dominant kernel (the fused stage kernel; RK4 = 4 launches per step)
     peaks = measured_peaks()
@@ -636,8 +657,9 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=3)
     ap.add_argument("--serving-requests", type=int, default=64, help="requests of the serving stream (0: skip)")
     ap.add_argument("--high-order-steps", type=int, default=10, help="timed steps of the p=6 dielectric (0: skip)")
-    ap.add_argument("--serving-rates", default="8,64",
-                    help="Poisson arrival rates of the serving stream (1/s): a moderate load and a saturating one")
+    ap.add_argument("--serving-rates", default="8,64,512",
+                    help="Poisson arrival rates of the serving stream (1/s): a light load, one the engine keeps "
+                         "up with, and a saturating one (capacity)")
     ap.add_argument("--serving-serial", type=int, default=8, help="requests also run one at a time for comparison")
     ap.add_argument("--serving-precision", choices=["fp32", "fp64"], default="fp32")
     args = ap.parse_args()

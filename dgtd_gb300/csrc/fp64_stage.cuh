@@ -33,12 +33,13 @@ namespace fp64 {
 
 constexpr int kBlock = 256;
 
-template <int P>
+template <int P, typename R = double>
 struct Ord {
     static constexpr int Np = (P + 1) * (P + 2) * (P + 3) / 6;
     static constexpr int Nfp = (P + 1) * (P + 2) / 2;
     static constexpr int NF = 4 * Nfp;
-    // elements per block: fill 256 threads, capped so static shared memory stays below 48 KB
+    // elements per block: fill 256 threads (one node each), capped so static shared memory
+    // stays below 48 KB
     static constexpr int EPB0 = kBlock / Np > 0 ? kBlock / Np : 1;
     static constexpr int EPB = EPB0 > 32 ? 32 : EPB0;
 };
@@ -71,13 +72,37 @@ __device__ __forceinline__ void eval_pw(const PlaneWaveDev* pw, int n_pw, int b,
     }
 }
 
+// Six components of one node (or face node) stored together in shared memory, so that a
+// thread reads them with vector loads: 8 floats (32 B) or 6 doubles (48 B) per entry.
+template <typename R>
+struct Node6 {
+    static constexpr int S = sizeof(R) == 4 ? 8 : 6;
+};
+
+template <typename R>
+__device__ __forceinline__ void load6(const R* p, R* v)
+{
+    if constexpr (sizeof(R) == 4) {
+        const float4 a = *reinterpret_cast<const float4*>(p);
+        const float2 b = *reinterpret_cast<const float2*>(p + 4);
+        v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y;
+    } else {
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            const double2 a = *reinterpret_cast<const double2*>(p + 2 * q);
+            v[2 * q] = a.x; v[2 * q + 1] = a.y;
+        }
+    }
+}
+
 template <int P, typename R = double>
 __device__ __forceinline__ void stage_body(const TablesT<R>& T, const StageArgsT<R>& A, int64_t e0, int b)
 {
-    using O = Ord<P>;
+    using O = Ord<P, R>;
     constexpr int Np = O::Np, Nfp = O::Nfp, NF = O::NF, EPB = O::EPB;
-    __shared__ R s_u[6][EPB * Np];
-    __shared__ R s_f[6][EPB * NF];
+    constexpr int S = Node6<R>::S;
+    __shared__ __align__(16) R s_u[EPB * Np * S];     // [node][component]
+    __shared__ __align__(16) R s_f[EPB * NF * S];     // [face node][component]
     __shared__ int s_fmask[4 * Nfp];
 
     const int tid = threadIdx.x;
@@ -88,7 +113,7 @@ __device__ __forceinline__ void stage_body(const TablesT<R>& T, const StageArgsT
     for (int i = tid; i < 4 * Nfp; i += blockDim.x) s_fmask[i] = T.Fmask[i];
     // coalesced load of the block's fields
     for (int c = 0; c < 6; ++c)
-        for (int i = tid; i < nel * Np; i += blockDim.x) s_u[c][i] = in[c * N + e0 * Np + i];
+        for (int i = tid; i < nel * Np; i += blockDim.x) s_u[i * S + c] = in[c * N + e0 * Np + i];
     __syncthreads();
 
     // ---- face fluxes -----------------------------------------------------------
@@ -101,8 +126,7 @@ __device__ __forceinline__ void stage_body(const TablesT<R>& T, const StageArgsT
         const R* fg = T.fgeo + e * 16 + f * 4;
         const R nx = fg[0], ny = fg[1], nz = fg[2], fs = fg[3];
         R uM[6], dE[3], dH[3];
-#pragma unroll
-        for (int c = 0; c < 6; ++c) uM[c] = s_u[c][el * Np + vm];
+        load6(s_u + (el * Np + vm) * S, uM);
         R aE = T.alpha, aH = T.alpha;
         if (code == 0 || code == 4 || code == 5) {
             const int64_t gp = T.vmapP[(e * 4 + f) * Nfp + a];
@@ -136,13 +160,13 @@ __device__ __forceinline__ void stage_body(const TablesT<R>& T, const StageArgsT
         const R ndE = nx * dE[0] + ny * dE[1] + nz * dE[2];
         const R ndH = nx * dH[0] + ny * dH[1] + nz * dH[2];
         const R h = R(0.5) * fs;
-        const int o = el * NF + fn;
-        s_f[0][o] = h * ((ny * dH[2] - nz * dH[1]) + aE * (dE[0] - ndE * nx));
-        s_f[1][o] = h * ((nz * dH[0] - nx * dH[2]) + aE * (dE[1] - ndE * ny));
-        s_f[2][o] = h * ((nx * dH[1] - ny * dH[0]) + aE * (dE[2] - ndE * nz));
-        s_f[3][o] = h * (-(ny * dE[2] - nz * dE[1]) + aH * (dH[0] - ndH * nx));
-        s_f[4][o] = h * (-(nz * dE[0] - nx * dE[2]) + aH * (dH[1] - ndH * ny));
-        s_f[5][o] = h * (-(nx * dE[1] - ny * dE[0]) + aH * (dH[2] - ndH * nz));
+        R* so = s_f + (el * NF + fn) * S;
+        so[0] = h * ((ny * dH[2] - nz * dH[1]) + aE * (dE[0] - ndE * nx));
+        so[1] = h * ((nz * dH[0] - nx * dH[2]) + aE * (dE[1] - ndE * ny));
+        so[2] = h * ((nx * dH[1] - ny * dH[0]) + aE * (dE[2] - ndE * nz));
+        so[3] = h * (-(ny * dE[2] - nz * dE[1]) + aH * (dH[0] - ndH * nx));
+        so[4] = h * (-(nz * dE[0] - nx * dE[2]) + aH * (dH[1] - ndH * ny));
+        so[5] = h * (-(nx * dE[1] - ny * dE[0]) + aH * (dH[2] - ndH * nz));
     }
     __syncthreads();
 
@@ -159,12 +183,13 @@ __device__ __forceinline__ void stage_body(const TablesT<R>& T, const StageArgsT
 #pragma unroll 4
     for (int j = 0; j < Np; ++j) {
         const R dr = __ldg(DrT + j * Np + i), ds = __ldg(DsT + j * Np + i), dt = __ldg(DtT + j * Np + i);
+        R uj[6];
+        load6(s_u + (el * Np + j) * S, uj);
 #pragma unroll
         for (int c = 0; c < 6; ++c) {
-            const R u = s_u[c][el * Np + j];
-            ar[c] = fma(dr, u, ar[c]);
-            as[c] = fma(ds, u, as[c]);
-            at[c] = fma(dt, u, at[c]);
+            ar[c] = fma(dr, uj[c], ar[c]);
+            as[c] = fma(ds, uj[c], as[c]);
+            at[c] = fma(dt, uj[c], at[c]);
         }
     }
     R lf[6];
@@ -174,8 +199,10 @@ __device__ __forceinline__ void stage_body(const TablesT<R>& T, const StageArgsT
 #pragma unroll 4
     for (int m = 0; m < NF; ++m) {
         const R L = __ldg(LT + m * Np + i);
+        R fm[6];
+        load6(s_f + (el * NF + m) * S, fm);
 #pragma unroll
-        for (int c = 0; c < 6; ++c) lf[c] = fma(L, s_f[c][el * NF + m], lf[c]);
+        for (int c = 0; c < 6; ++c) lf[c] = fma(L, fm[c], lf[c]);
     }
     const R* g = T.geo + e * 9;
     const R rx = g[0], ry = g[1], rz = g[2], sx = g[3], sy = g[4], sz = g[5], tx = g[6], ty = g[7], tz = g[8];
@@ -186,10 +213,12 @@ __device__ __forceinline__ void stage_body(const TablesT<R>& T, const StageArgsT
     const R curlEx = dy(2) - dz(1), curlEy = dz(0) - dx(2), curlEz = dx(1) - dy(0);
     const R* mt = T.mat + e * 3;
     const R ie = mt[0], im = mt[1], se = mt[2];
+    R uo[6];
+    load6(s_u + tid * S, uo);
     R k[6];
-    k[0] = ie * (curlHx + lf[0]) - se * s_u[0][tid];
-    k[1] = ie * (curlHy + lf[1]) - se * s_u[1][tid];
-    k[2] = ie * (curlHz + lf[2]) - se * s_u[2][tid];
+    k[0] = ie * (curlHx + lf[0]) - se * uo[0];
+    k[1] = ie * (curlHy + lf[1]) - se * uo[1];
+    k[2] = ie * (curlHz + lf[2]) - se * uo[2];
     k[3] = im * (-curlEx + lf[3]);
     k[4] = im * (-curlEy + lf[4]);
     k[5] = im * (-curlEz + lf[5]);
@@ -204,7 +233,7 @@ __device__ __forceinline__ void stage_body(const TablesT<R>& T, const StageArgsT
     case MODE_RK4_1:
 #pragma unroll
         for (int c = 0; c < 6; ++c) {
-            const R xv = s_u[c][tid];
+            const R xv = uo[c];
             A.yout[base + c * N] = xv + R(0.5) * dt * k[c];
             A.z[base + c * N] = xv + (dt / R(6)) * k[c];
         }
@@ -234,7 +263,7 @@ __device__ __forceinline__ void stage_body(const TablesT<R>& T, const StageArgsT
         for (int c = 0; c < 6; ++c) {
             const R r = A.a * A.res[base + c * N] + dt * k[c];
             A.res[base + c * N] = r;
-            A.yout[base + c * N] = s_u[c][tid] + A.b * r;
+            A.yout[base + c * N] = uo[c] + A.b * r;
         }
         break;
     default:

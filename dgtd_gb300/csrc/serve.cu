@@ -174,7 +174,7 @@ __global__ void __launch_bounds__(fp64::kBlock) serve_stage(const __grid_constan
     TablesT<R> T;
     StageArgsT<R> A;
     slot_views<P, R>(L, S, T, A);
-    fp64::stage_body<P, R>(T, A, (bx - S.block0) * fp64::Ord<P>::EPB, 0);
+    fp64::stage_body<P, R>(T, A, (bx - S.block0) * fp64::Ord<P, R>::EPB, 0);
 }
 
 // TF/SF skip flag of every request with sources (one block each).
@@ -220,16 +220,22 @@ cudaError_t launch_stage(bool fp32, int p, const LaunchParam& L, int64_t blocks,
     return fp32 ? launch_stage_r<float>(p, L, blocks, any_src, s) : launch_stage_r<double>(p, L, blocks, any_src, s);
 }
 
-int elements_per_block(int p)
+template <typename R>
+int elements_per_block_r(int p)
 {
     switch (p) {
-    case 1: return fp64::Ord<1>::EPB;
-    case 2: return fp64::Ord<2>::EPB;
-    case 3: return fp64::Ord<3>::EPB;
-    case 4: return fp64::Ord<4>::EPB;
-    case 5: return fp64::Ord<5>::EPB;
-    default: return fp64::Ord<6>::EPB;
+    case 1: return fp64::Ord<1, R>::EPB;
+    case 2: return fp64::Ord<2, R>::EPB;
+    case 3: return fp64::Ord<3, R>::EPB;
+    case 4: return fp64::Ord<4, R>::EPB;
+    case 5: return fp64::Ord<5, R>::EPB;
+    default: return fp64::Ord<6, R>::EPB;
     }
+}
+
+int elements_per_block(int p, bool fp32)
+{
+    return fp32 ? elements_per_block_r<float>(p) : elements_per_block_r<double>(p);
 }
 
 struct ServeError : std::runtime_error {
@@ -497,7 +503,7 @@ void engine_loop(dgtd_server* s)
                 if (grp.empty()) continue;
                 cudaStream_t st = s->ord_stream[o];
                 const OrderTables& O = s->ord[o];
-                const int epb = elements_per_block(o);
+                const int epb = elements_per_block(o, s->fp32);
                 for (int k = 0; k < s->opts.steps_per_round; ++k) {
                     LaunchParam& L = *params;
                     L.DrT = O.DrT; L.DsT = O.DsT; L.DtT = O.DtT; L.LIFTT = O.LIFTT; L.Fmask = O.Fmask;

@@ -17,7 +17,7 @@ using fp64::Ord;
 template <int P>
 __global__ void __launch_bounds__(kBlock) stage_f32s(TablesF32 T, StageArgsF32 A)
 {
-    fp64::stage_body<P, float>(T, A, static_cast<int64_t>(blockIdx.x) * Ord<P>::EPB, static_cast<int>(blockIdx.y));
+    fp64::stage_body<P, float>(T, A, static_cast<int64_t>(blockIdx.x) * Ord<P, float>::EPB, static_cast<int>(blockIdx.y));
 }
 
 __global__ void __launch_bounds__(256) tfsf_skip_f32s(TablesF32 T, const PlaneWaveDev* pw, int n_pw, double t,
@@ -59,7 +59,7 @@ __global__ void f32_to_f64(const float* __restrict__ in, double* __restrict__ ou
 template <int P>
 cudaError_t launch_p(const TablesF32& T, const StageArgsF32& A, cudaStream_t s)
 {
-    dim3 grid(static_cast<unsigned>((T.K + Ord<P>::EPB - 1) / Ord<P>::EPB), static_cast<unsigned>(A.batch));
+    dim3 grid(static_cast<unsigned>((T.K + Ord<P, float>::EPB - 1) / Ord<P, float>::EPB), static_cast<unsigned>(A.batch));
     stage_f32s<P><<<grid, kBlock, 0, s>>>(T, A);
     return cudaGetLastError();
 }

@@ -81,8 +81,10 @@ struct TcOrd {
     static constexpr int OpBytes = NKS * OpStep;            // per hi / lo
     static constexpr int UBytes = 6 * Np * kChunk * 4;      // staged element block
     static constexpr int NbrBytes = (4 * NF + 15) / 16 * 16;
+    static constexpr int XyzBytes = NF * 12;                 // face-node coordinates (TF/SF source)
     // U | neighbour table | face geometry (16 floats) | face codes (4 ints) | jump coefficients (20 floats)
-    static constexpr int UBufBytes = (UBytes + NbrBytes + 64 + 16 + 80 + 127) / 128 * 128;
+    // | face-node coordinates (NF x 3 floats)
+    static constexpr int UBufBytes = (UBytes + NbrBytes + 64 + 16 + 80 + XyzBytes + 127) / 128 * 128;
     static constexpr size_t smem = 2 * static_cast<size_t>(OpBytes) + 2 * static_cast<size_t>(UBufBytes) +
                                    2 * static_cast<size_t>(kSlot);
     static_assert(3 * N <= static_cast<int>(kAccStride), "accumulator buffer too narrow");
@@ -93,12 +95,12 @@ struct TcOrd {
 // volume: derivative direction (0 r, 1 s, 2 t) in bits 16-23, node in bits 0-15 (column 3 node + d).
 constexpr int kColFlux = 0, kColVol = 1, kColPad = 2;
 
-__device__ __forceinline__ void pw_eval(const PlaneWaveF32* pw, const int* pw_off, int b, float px, float py, float pz,
+// Sum of the plane waves pw[q0, q1) (one incidence's) at point p and time t.
+__device__ __forceinline__ void pw_eval(const PlaneWaveF32* pw, int q0, int q1, float px, float py, float pz,
                                         float t, float* e, float* h)
 {
     e[0] = e[1] = e[2] = h[0] = h[1] = h[2] = 0.0f;
-    const int q1 = pw_off[b + 1];
-    for (int q = pw_off[b]; q < q1; ++q) {
+    for (int q = q0; q < q1; ++q) {
         const PlaneWaveF32& w = pw[q];
         const float s = px * w.k[0] + py * w.k[1] + pz * w.k[2] - t;
         const float a = s - w.mean;
@@ -155,7 +157,7 @@ __device__ __forceinline__ void prefetch_item(const BatchedTables& T, const floa
     const int g = static_cast<int>(w - e * nchunk);
     const int64_t EB = 6 * static_cast<int64_t>(Np) * Bp;
     const float* src = in + e * EB + static_cast<int64_t>(g) * kChunk;
-    mbar_expect_tx(bar, O::UBytes + 4 * NF + 64 + 16 + 80);
+    mbar_expect_tx(bar, O::UBytes + 4 * NF + 64 + 16 + 80 + O::XyzBytes);
     if (Bp == kChunk) {
         bulk_g2s(buf, src, O::UBytes, bar);
     } else {
@@ -166,6 +168,7 @@ __device__ __forceinline__ void prefetch_item(const BatchedTables& T, const floa
     bulk_g2s(buf + O::UBytes + O::NbrBytes, T.fgeo + e * 16, 64, bar);
     bulk_g2s(buf + O::UBytes + O::NbrBytes + 64, T.fcode + e * 4, 16, bar);
     bulk_g2s(buf + O::UBytes + O::NbrBytes + 80, T.fbc + e * 20, 80, bar);
+    bulk_g2s(buf + O::UBytes + O::NbrBytes + 160, T.fxyz + e * NF * 3, O::XyzBytes, bar);
 }
 
 // The RK registers the epilogue of work item w reads, brought into L2 ahead of
@@ -247,13 +250,14 @@ __device__ __forceinline__ void epi_store(const BatchedStageArgs& A, int64_t bas
     }
 }
 
-// Jumps (neighbour minus own, with the boundary rules and the TF/SF source) at one
-// face node and the resulting Fscale/2-scaled upwind flux of all six components.
-__device__ __forceinline__ void tfsf_source(const BatchedStageArgs& A, const float* xq, int b, int code, float* dE, float* dH)
+// Adds the incident field of waves pw[q0, q1) at one TF/SF face node (coordinates xq, staged in
+// shared memory) and stage time ts to the jumps: + on the total-field side (code 4), - on the
+// scattered-field side (reference GlobalEvolution.cpp:551-626).
+__device__ __forceinline__ void tfsf_source(const BatchedStageArgs& A, const float* xq, int q0, int q1, float ts, int code,
+                                            float* dE, float* dH)
 {
     float pe[3], ph[3];
-    const float ts = A.t_base ? static_cast<float>(*A.t_base + static_cast<double>(A.t)) : A.t;
-    pw_eval(A.pw, A.pw_off, b, __ldg(xq), __ldg(xq + 1), __ldg(xq + 2), ts, pe, ph);
+    pw_eval(A.pw, q0, q1, xq[0], xq[1], xq[2], ts, pe, ph);
     const float s2 = (code == 4) ? 1.0f : -1.0f;
 #pragma unroll
     for (int c = 0; c < 3; ++c) { dE[c] += s2 * pe[c]; dH[c] += s2 * ph[c]; }
@@ -340,6 +344,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             const float* s_fg = reinterpret_cast<const float*>(buf + O::UBytes + O::NbrBytes);
             const int* s_code = reinterpret_cast<const int*>(buf + O::UBytes + O::NbrBytes + 64);
             const float* s_bc = reinterpret_cast<const float*>(buf + O::UBytes + O::NbrBytes + 80);
+            const float* s_xyz = reinterpret_cast<const float*>(buf + O::UBytes + O::NbrBytes + 160);
             if (flag_set(&s_err) || !tc::mbar_wait(&u_full[ub], (it >> 1) & 1)) { err = true; break; }
             const int64_t e = w / nchunk;
             const int g = static_cast<int>(w - e * nchunk);
@@ -349,6 +354,27 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll
             for (int q = 0; q < 9; ++q) geo[q] = __ldg(gg + q);
             const bool skip_src = (A.skip == nullptr) || A.skip[b];
+            // once per item: this incidence's waves, the stage time, and which faces of the element
+            // take the TF/SF source (bit f of tf_faces; bit f of tf_total: total-field side)
+            int pq0 = 0, pq1 = 0;
+            float ts = A.t;
+            uint32_t tf_faces = 0, tf_total = 0, nb_faces = 0;   // nb_faces: faces with a neighbour trace
+#pragma unroll
+            for (int f = 0; f < 4; ++f) {
+                const int code = s_code[f];
+                nb_faces |= static_cast<uint32_t>(code == 0 || code == 4 || code == 5) << f;
+            }
+            if (!skip_src) {
+                pq0 = A.pw_off[b];
+                pq1 = A.pw_off[b + 1];
+                if (A.t_base) ts = static_cast<float>(*A.t_base + static_cast<double>(A.t));
+#pragma unroll
+                for (int f = 0; f < 4; ++f) {
+                    const int code = s_code[f];
+                    tf_faces |= static_cast<uint32_t>(code == 4 || code == 5) << f;
+                    tf_total |= static_cast<uint32_t>(code == 4) << f;
+                }
+            }
             const float* __restrict__ nin = A.in + static_cast<int64_t>(g) * kChunk + pb;
             // neighbour traces of this thread's 4 columns of a K-step (flux columns of interior faces),
             // loaded one K-step of this group ahead
@@ -359,8 +385,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         const int ci_ = s_col[(QQ) * 8 + kh * 4 + jj];                                                   \
         if ((ci_ >> 28) == kColFlux) {                                                                  \
             const int m_ = (ci_ >> 16) & 0xfff;                                                         \
-            const int code_ = s_code[(ci_ >> 12) & 0xf];                                                \
-            if (code_ == 0 || code_ == 4 || code_ == 5) {                                               \
+            if ((nb_faces >> ((ci_ >> 12) & 0xf)) & 1u) {                                               \
                 const int32_t gp_ = s_nbr[m_];                                                          \
                 const int32_t en_ = gp_ / Np, node_ = gp_ - en_ * Np;                                   \
                 const float* __restrict__ un_ = nin + static_cast<int64_t>(en_) * EB + node_ * Bp;      \
@@ -411,10 +436,8 @@ __global__ void __launch_bounds__(kThreads, 1)
                             dE[c] = cE1 * nb[jj][c] + cE2 * uM[c];
                             dH[c] = cH1 * nb[jj][c + 3] + cH2 * uM[c + 3];
                         }
-                        if (!skip_src) {
-                            const int code = s_code[f];
-                            if (code == 4 || code == 5) tfsf_source(A, T.fxyz + (e * NF + m) * 3, b, code, dE, dH);
-                        }
+                        if ((tf_faces >> f) & 1u)
+                            tfsf_source(A, s_xyz + m * 3, pq0, pq1, ts, ((tf_total >> f) & 1u) ? 4 : 5, dE, dH);
                         const float ndE = nx * dE[0] + ny * dE[1] + nz * dE[2];
                         const float ndH = nx * dH[0] + ny * dH[1] + nz * dH[2];
                         v[0][jj] = hf * ((ny * dH[2] - nz * dH[1]) + aE * (dE[0] - ndE * nx));

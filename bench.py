@@ -296,7 +296,11 @@ def time_steps(op, state, dt, t0, steps, stream, flush, dev):
 
 
 def accuracy_vs_fp64(w: dict, dev) -> dict:
-    """Reduced-size run of the same physics in the FP32 batched form and the FP64 form."""
+    """Reduced-size run of the same physics in the FP32 batched form and the FP64 form.
+
+    The FP32 operator has the workload's batch (64 incidences: the tensor-core kernel, as in
+    the timed run); the FP64 operator runs its first `batch` incidences (same waves) and
+    those are compared."""
     import torch
     import dgtd_gb300 as dg
     acc = w["accuracy"]
@@ -304,21 +308,23 @@ def accuracy_vs_fp64(w: dict, dev) -> dict:
     mesh = build_mesh(wr)
     B = acc["batch"]
     op64 = make_op(wr, mesh, dg.FP64, B)
-    op32 = make_op(wr, mesh, dg.FP32_3XTF32, B)
+    op32 = make_op(wr, mesh, dg.FP32_3XTF32, w["batch"])
     dt = workload_dt(wr, op64)
     x64 = torch.zeros(op64.state_len, dtype=torch.float64, device=dev)
+    x32 = torch.zeros(op32.state_len, dtype=torch.float64, device=dev)
     wk = op32.new_work(dev)
-    op32.pack(x64, wk)
+    op32.pack(x32, wk)
     op64.step(x64, 0.0, dt, acc["steps"])
     op32.step(wk, 0.0, dt, acc["steps"])
-    x32 = torch.zeros_like(x64)
     op32.unpack(wk, x32)
     torch.cuda.synchronize(dev)
     a, r = x32.cpu().numpy(), x64.cpu().numpy()
     L = op64.state_len // B
     errs = [float(np.linalg.norm(a[b * L:(b + 1) * L] - r[b * L:(b + 1) * L]) / np.linalg.norm(r[b * L:(b + 1) * L]))
             for b in range(B)]
-    return {"rel_l2_vs_fp64_max": max(errs), "incidences": B, "steps": acc["steps"], "t_end": acc["steps"] * dt,
+    return {"rel_l2_vs_fp64_max": max(errs), "incidences_compared": B, "fp32_batch": w["batch"],
+            "fp32_kernel": "tensor cores (stage_tc)" if op32.uses_tensor_cores else "FP32 SIMT (stage_f32)",
+            "steps": acc["steps"], "t_end": acc["steps"] * dt,
             "case": f"{acc['cells'][0]}^3 hexes x 6 tets, same order/sources/boundaries"}
 
 

@@ -15,8 +15,8 @@
 // The volume columns come first so that the neighbour traces the flux columns
 // need are loaded while the volume columns are being built.
 // Rows (c, b) are 6 components x 64 incidences = 3 M-tiles of 128; N = Np padded
-// to 16; K padded to 8. W is split into a tf32 high part (mantissa truncated) and
-// the FP32 remainder, the constant Op into round-to-nearest hi/lo parts, giving
+// to 16; K padded to 8. W is split into a tf32 high part (rounded to nearest) and
+// the rounded remainder, the constant Op into round-to-nearest hi/lo parts, giving
 // W_hi Op_hi + W_lo Op_hi + W_hi Op_lo (3xTF32, FP32-level accuracy). The
 // accumulators live in tensor memory; the epilogue applies 1/eps, 1/mu, the
 // conductivity term and the RK stage update.
@@ -64,7 +64,8 @@ constexpr int kChunk = 64;              // incidences per work item
 constexpr int kTile = 4096;             // one W tile: 128 rows x 8 tf32, SBO 256, LBO 128
 constexpr int kWStep = 3 * kTile;       // one K-step of W (3 M-tiles), hi or lo
 constexpr int kSlot = 2 * kWStep;       // hi + lo
-constexpr uint32_t kAccStride = 256;    // TMEM columns between the two accumulator buffers
+constexpr uint32_t kAccStride = 160;    // TMEM columns between the two accumulator buffers
+constexpr uint32_t kCorrCol = 320;      // the correction accumulator (single buffer)
 constexpr uint32_t kTmemCols = 512;
 
 template <int P>
@@ -88,6 +89,7 @@ struct TcOrd {
     static constexpr size_t smem = 2 * static_cast<size_t>(OpBytes) + 2 * static_cast<size_t>(UBufBytes) +
                                    2 * static_cast<size_t>(kSlot);
     static_assert(3 * N <= static_cast<int>(kAccStride), "accumulator buffer too narrow");
+    static_assert(kCorrCol + 3 * N <= kTmemCols, "correction accumulator past the allocation");
 };
 
 // Column metadata: kind in bits 28-29 (0 flux, 1 volume, 2 padding);
@@ -138,10 +140,16 @@ __device__ __forceinline__ void st_shared_v4(uint32_t addr, float a, float b, fl
 }
 
 // tf32 high part by mantissa truncation, and the FP32 remainder
+// v = hi + lo with hi the tf32 value nearest v (ties away from zero) and lo the remainder,
+// itself rounded to the nearest tf32. Both then pass through the tensor core's tf32 operand
+// path unchanged. |lo| <= 2^-11 |v| and its rounding error is <= 2^-11 |lo|; truncating either
+// part instead doubles the error of the 3xTF32 product, which was measurable after a few
+// hundred steps.
 __device__ __forceinline__ void split_tf32(float v, float& hi, float& lo)
 {
-    hi = __uint_as_float(__float_as_uint(v) & 0xFFFFE000u);
-    lo = v - hi;
+    hi = __uint_as_float((__float_as_uint(v) + 0x1000u) & 0xFFFFE000u);
+    const float r = v - hi;
+    lo = __uint_as_float((__float_as_uint(r) + 0x1000u) & 0xFFFFE000u);
 }
 
 __device__ __forceinline__ bool flag_set(const int* f) { return *reinterpret_cast<const volatile int*>(f) != 0; }
@@ -274,7 +282,8 @@ __global__ void __launch_bounds__(kThreads, 1)
     unsigned char* op_lo = sm + O::OpBytes;
     unsigned char* ubuf0 = sm + 2 * O::OpBytes;
     unsigned char* ring = ubuf0 + 2 * O::UBufBytes;
-    __shared__ uint64_t u_full[2], u_empty[2], w_full[2], w_empty[2], acc_full[2], acc_empty[2], drain_bar;
+    __shared__ uint64_t u_full[2], u_empty[2], w_full[2], w_empty[2], acc_full[2], acc_empty[2];
+    __shared__ uint64_t corr_empty, drain_bar;
     __shared__ uint32_t tbase;
     __shared__ int s_col[O::KKp];
     __shared__ int s_err;
@@ -307,6 +316,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             tc::mbar_init(&acc_full[s], 1);
             tc::mbar_init(&acc_empty[s], kEpiThreads);
         }
+        tc::mbar_init(&corr_empty, kEpiThreads);
         tc::mbar_init(&drain_bar, 1);
         s_err = 0;
         tc::mbar_fence_init();
@@ -403,13 +413,20 @@ __global__ void __launch_bounds__(kThreads, 1)
                 // fields at the (at most two) nodes this thread's volume columns use
                 const int kq0 = q * 8 + kh * 4;
                 const int jA = kq0 / 3;
+                // Volume columns take F_j - F_0 (node 0 of the element): Dr, Ds and Dt annihilate
+                // constants, so the product is unchanged in exact arithmetic, while the common part
+                // of F no longer meets the rounding of the tf32 operator (each row of Dr sums to 0
+                // with terms ~100x the result, so that error would otherwise be amplified).
                 float FA[6], FB[6];
                 if (kq0 < 3 * Np) {
+                    float F0[6];
 #pragma unroll
-                    for (int c = 0; c < 6; ++c) FA[c] = s_u[(c * Np + jA) * kChunk + pb];
+                    for (int c = 0; c < 6; ++c) F0[c] = s_u[(c * Np) * kChunk + pb];
+#pragma unroll
+                    for (int c = 0; c < 6; ++c) FA[c] = s_u[(c * Np + jA) * kChunk + pb] - F0[c];
                     if (jA + 1 < Np && kq0 + 3 < 3 * Np) {
 #pragma unroll
-                        for (int c = 0; c < 6; ++c) FB[c] = s_u[(c * Np + jA + 1) * kChunk + pb];
+                        for (int c = 0; c < 6; ++c) FB[c] = s_u[(c * Np + jA + 1) * kChunk + pb] - F0[c];
                     }
                 }
 #pragma unroll
@@ -532,6 +549,25 @@ __global__ void __launch_bounds__(kThreads, 1)
             epi_load<MODE>(A, chunk_base(0), Bp, chunk_nv(0), need_u, o0);
             if (flag_set(&s_err) || !tc::mbar_wait(&acc_full[abuf], (it >> 1) & 1)) { err = true; break; }
             tc::fence_after_sync();
+            // fold the correction accumulator into this item's accumulator (FP32, round to nearest)
+            // and hand it back to the MMA issuer for the next item
+            {
+                const uint32_t tcorr = tmem + kCorrCol + (static_cast<uint32_t>(lq * 32) << 16);
+#pragma unroll 1
+                for (int n = 0; n < NCHT; ++n) {
+                    const int t = n / O::NCH, cb = (n % O::NCH) * kEpiNodes;
+                    float mv[kEpiNodes], cv[kEpiNodes];
+                    tc::tmem_ld8(tacc + t * N + cb, mv);
+                    tc::tmem_ld8(tcorr + t * N + cb, cv);
+                    tc::tmem_ld_wait();
+#pragma unroll
+                    for (int q = 0; q < kEpiNodes; ++q) mv[q] += cv[q];
+                    tc::tmem_st8(tacc + t * N + cb, mv);
+                }
+                tc::tmem_st_wait();
+                tc::fence_before_sync();
+                tc::mbar_arrive(&corr_empty);
+            }
 #pragma unroll 1
             for (int n = 0; n < NCHT; n += 2) {
                 if (n + 1 < NCHT) epi_load<MODE>(A, chunk_base(n + 1), Bp, chunk_nv(n + 1), need_u, o1);
@@ -566,15 +602,26 @@ __global__ void __launch_bounds__(kThreads, 1)
                     const uint32_t ah0 = ring_u32 + slot * kSlot, al0 = ah0 + kWStep;
                     const uint64_t bh = tc::smem_desc(tc::smem_u32(op_hi + q * O::OpStep));
                     const uint64_t blo = tc::smem_desc(tc::smem_u32(op_lo + q * O::OpStep));
+                    // W_hi Op_hi into the item's accumulator; the two small correction products into
+                    // a separate one, so that the truncation in each accumulation is relative to the
+                    // small correction sum, not to the full result
+#pragma unroll
+                    for (int t = 0; t < 3; ++t)
+                        tc::mma_tf32(dacc + t * N, tc::smem_desc(ah0 + t * kTile), bh, idesc, q > 0);
+                    if (q == 0 && it >= 1) {
+                        // the epilogue has folded the previous item's corrections into its accumulator
+                        if (flag_set(&s_err) || !tc::mbar_wait(&corr_empty, (it - 1) & 1)) { err = true; break; }
+                        tc::fence_after_sync();
+                    }
 #pragma unroll
                     for (int t = 0; t < 3; ++t) {
-                        const uint32_t d = dacc + t * N;
+                        const uint32_t dc = tmem + kCorrCol + t * N;
                         const uint64_t ah = tc::smem_desc(ah0 + t * kTile);
                         const uint64_t al = tc::smem_desc(al0 + t * kTile);
-                        tc::mma_tf32(d, ah, bh, idesc, q > 0);
-                        tc::mma_tf32(d, al, bh, idesc, true);
-                        tc::mma_tf32(d, ah, blo, idesc, true);
+                        tc::mma_tf32(dc, al, bh, idesc, q > 0);
+                        tc::mma_tf32(dc, ah, blo, idesc, true);
                     }
+                    if (err) break;
                     tc::mma_commit(&w_empty[slot]);
                 }
                 if (err) break;

@@ -207,3 +207,34 @@ def test_tensor_core_matches_simt_and_fp64(torch_cuda):
     assert np.linalg.norm(r) > 1.0
     assert max(e_tc) <= 1e-5, max(e_tc)
     assert max(e_st) <= 1e-5, max(e_st)
+
+
+def test_tensor_core_p4_long_run_vs_fp64(torch_cuda):
+    """Scattering case at p = 4 with 64 incidences (the tensor-core kernel), 250 RK4 steps:
+    relative L2 vs the FP64 form <= 1e-5 for the compared incidences. This bar failed (1.3e-5)
+    while the correction products shared the main tensor-memory accumulator."""
+    torch = torch_cuda
+    n = 12
+    m = dg.box_mesh((n, n, n), lo=(-1, -1, -1), hi=(1, 1, 1), hole=((5,) * 3, (7,) * 3),
+                    tfsf=((2,) * 3, (10,) * 3), outer_bc=dg.BC_SMA, hole_bc=dg.BC_PEC)
+    B, Bc, order = 64, 4, 4
+    waves = waves_for(B)
+    op64 = dg.Operator(m, order=order, batch=Bc)
+    tc = dg.Operator(m, order=order, precision=dg.FP32_3XTF32, batch=B)
+    assert tc.uses_tensor_cores
+    op64.set_planewaves(waves[:Bc])
+    tc.set_planewaves(waves)
+    dt = op64.estimate_dt(1.0)
+    x64 = torch.zeros(op64.state_len, dtype=torch.float64, device="cuda")
+    x32 = torch.zeros(tc.state_len, dtype=torch.float64, device="cuda")
+    wk = tc.new_work(); tc.pack(x32, wk)
+    op64.step(x64, 0.0, dt, 250)
+    tc.step(wk, 0.0, dt, 250)
+    tc.check()
+    tc.unpack(wk, x32)
+    torch.cuda.synchronize()
+    a, r = x32.cpu().numpy(), x64.cpu().numpy()
+    L = op64.state_len // Bc
+    errs = [rel_l2(a[b * L:(b + 1) * L], r[b * L:(b + 1) * L]) for b in range(Bc)]
+    assert np.linalg.norm(r) > 1.0
+    assert max(errs) <= 1e-5, errs

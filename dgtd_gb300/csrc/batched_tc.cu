@@ -17,9 +17,12 @@
 // Rows (c, b) are 6 components x 64 incidences = 3 M-tiles of 128; N = Np padded
 // to 16; K padded to 8. W is split into a tf32 high part (rounded to nearest) and
 // the rounded remainder, the constant Op into round-to-nearest hi/lo parts, giving
-// W_hi Op_hi + W_lo Op_hi + W_hi Op_lo (3xTF32, FP32-level accuracy). The
-// accumulators live in tensor memory; the epilogue applies 1/eps, 1/mu, the
-// conductivity term and the RK stage update.
+// W_hi Op_hi + W_lo Op_hi + W_hi Op_lo (3xTF32). The accumulators live in tensor
+// memory: W_hi Op_hi in a double-buffered item accumulator (columns 0 and 160), the
+// two small correction products in a separate accumulator (column 320) that the
+// epilogue folds in with FP32 adds. Each MMA's accumulation truncates relative to the
+// accumulator it adds into, so keeping the corrections apart cuts that error 3x.
+// The epilogue applies 1/eps, 1/mu, the conductivity term and the RK stage update.
 //
 // One persistent CTA per SM, warp-specialised, no CTA-wide barrier in the
 // steady state (all hand-offs are mbarriers, every wait bounded):
@@ -28,7 +31,8 @@
 //              owns one incidence and 4 consecutive columns of its K-step and
 //              computes all 6 component rows, stored as 16-byte vectors
 //              (conflict-free in the K-major core-matrix layout);
-//   warps 8-11 epilogue: drain a double-buffered tensor-memory accumulator
+//   warps 8-11 epilogue: fold the correction accumulator into the item's
+//              accumulator and release it, then drain the item's accumulator
 //              (tcgen05.ld) and apply the stage update, with the global
 //              RK-register loads of the next 8 nodes in flight;
 //   warp 12    tensor-memory owner and MMA issuer (one thread);

@@ -188,3 +188,115 @@ def lobatto(p: int) -> np.ndarray:
 
 def threads() -> int:
     return int(lib().orc_threads())
+
+
+# ----------------------------------------------------------------------------- meshes and dt (numpy)
+# Structured box meshes and the reference's 3D time-step estimate, restated in numpy so
+# that the CPU baselines need nothing from the product library. The construction is the
+# product's box generator (dgtd_box_mesh_*): same vertex numbering, element order,
+# orientation and face lists; tests/test_oracle_mesh.py checks that they are identical.
+BC_OPEN, BC_PEC, BC_PMC, BC_SMA = 0, 1, 2, 3
+
+# 6 tetrahedra of a hex (corners 0..7 in the i-fastest order of the cell) sharing the
+# 0-6 diagonal, all positively oriented
+_KUHN = np.array([[0, 1, 2, 6], [0, 5, 1, 6], [0, 4, 5, 6], [0, 2, 3, 6], [0, 3, 7, 6], [0, 7, 4, 6]])
+
+
+class BoxMesh:
+    """Flat mesh tables with the fields Oracle.from_mesh reads."""
+
+    def __init__(self, vertices, elements, bdr_faces, bdr_codes, tfsf_faces):
+        self.vertices = vertices
+        self.elements = elements
+        self.bdr_faces = bdr_faces
+        self.bdr_codes = bdr_codes
+        self.tfsf_faces = tfsf_faces
+        self.int_faces = np.zeros((0, 3), np.int32)
+        self.int_codes = np.zeros((0,), np.int32)
+        self.eps = self.mu = self.sigma = None
+        self.dim = 3
+
+    @property
+    def n_elements(self) -> int:
+        return int(self.elements.shape[0])
+
+
+def box_mesh(n, lo=(0.0, 0.0, 0.0), hi=(1.0, 1.0, 1.0), hole=None, tfsf=None, outer_bc: int = BC_PEC,
+             hole_bc: int = BC_PEC) -> BoxMesh:
+    """n[0] x n[1] x n[2] hexes, each split into 6 tets; hole / tfsf: half-open cell ranges."""
+    nx, ny, nz = (int(v) for v in n)
+    vid = lambda i, j, k: i + (nx + 1) * (j + (ny + 1) * k)
+    kk, jj, ii = np.meshgrid(np.arange(nz + 1), np.arange(ny + 1), np.arange(nx + 1), indexing="ij")
+    V = np.stack([lo[0] + (hi[0] - lo[0]) * ii.ravel() / nx, lo[1] + (hi[1] - lo[1]) * jj.ravel() / ny,
+                  lo[2] + (hi[2] - lo[2]) * kk.ravel() / nz], axis=1)
+    hole_lo, hole_hi = (hole if hole is not None else ((0, 0, 0), (0, 0, 0)))
+    tf_lo, tf_hi = (tfsf if tfsf is not None else ((0, 0, 0), (0, 0, 0)))
+
+    def in_range(i, j, k, a, b):
+        return a[0] <= i < b[0] and a[1] <= j < b[1] and a[2] <= k < b[2]
+
+    def exists(i, j, k):
+        return 0 <= i < nx and 0 <= j < ny and 0 <= k < nz and not in_range(i, j, k, hole_lo, hole_hi)
+
+    cells = [(i, j, k) for k in range(nz) for j in range(ny) for i in range(nx)
+             if not in_range(i, j, k, hole_lo, hole_hi)]
+    c = np.array([[vid(i, j, k), vid(i + 1, j, k), vid(i + 1, j + 1, k), vid(i, j + 1, k), vid(i, j, k + 1),
+                   vid(i + 1, j, k + 1), vid(i + 1, j + 1, k + 1), vid(i, j + 1, k + 1)] for i, j, k in cells],
+                 dtype=np.int64).reshape(-1, 8)
+    E = c[:, _KUHN].reshape(-1, 4).astype(np.int32)
+    have_tf = all(tf_hi[d] > tf_lo[d] for d in range(3))
+    bf, bc, tf = [], [], []
+
+    def quad(dst, a, b, cc, d, flip):            # quad a-b-c-d, diagonal a-c
+        dst.extend([[a, cc, b], [a, d, cc]] if flip else [[a, b, cc], [a, cc, d]])
+
+    lim0 = (nx, ny, nz)
+    for axis in range(3):
+        lim = list(lim0)
+        lim[axis] += 1
+        for k in range(lim[2]):
+            for j in range(lim[1]):
+                for i in range(lim[0]):
+                    im = [i, j, k]
+                    im[axis] -= 1
+                    a_ex, b_ex = exists(*im), exists(i, j, k)
+                    if not a_ex and not b_ex:
+                        continue
+                    if axis == 0:
+                        q = (vid(i, j, k), vid(i, j + 1, k), vid(i, j + 1, k + 1), vid(i, j, k + 1))
+                    elif axis == 1:
+                        q = (vid(i, j, k), vid(i + 1, j, k), vid(i + 1, j, k + 1), vid(i, j, k + 1))
+                    else:
+                        q = (vid(i, j, k), vid(i + 1, j, k), vid(i + 1, j + 1, k), vid(i, j + 1, k))
+                    if a_ex != b_ex:
+                        on_outer = (i in (0, nx)) if axis == 0 else ((j in (0, ny)) if axis == 1 else (k in (0, nz)))
+                        quad(bf, *q, False)
+                        bc.extend([outer_bc if on_outer else hole_bc] * 2)
+                    elif have_tf:
+                        a_tf, b_tf = in_range(*im, tf_lo, tf_hi), in_range(i, j, k, tf_lo, tf_hi)
+                        if a_tf != b_tf:
+                            nrm = np.cross(V[q[1]] - V[q[0]], V[q[2]] - V[q[0]])
+                            quad(tf, *q, bool(nrm[axis] > 0.0) != b_tf)
+    as3 = lambda a: np.asarray(a, dtype=np.int32).reshape(-1, 3)
+    return BoxMesh(V, E, as3(bf), np.asarray(bc, dtype=np.int32), as3(tf))
+
+
+def dt_scale_min(vertices, elements) -> float:
+    """min over elements of volume / (half the sum of its face areas) (reference getTimeStepScale
+    restated for straight-sided tets, src/solver/Solver.cpp:289-300)."""
+    P = np.asarray(vertices, dtype=np.float64)[np.asarray(elements)]          # [K, 4, 3]
+    vol = np.abs(np.einsum("ki,ki->k", P[:, 1] - P[:, 0], np.cross(P[:, 2] - P[:, 0], P[:, 3] - P[:, 0]))) / 6.0
+    area = np.zeros(len(P))
+    for f in ((1, 2, 3), (0, 2, 3), (0, 1, 3), (0, 1, 2)):
+        a, b, cc = P[:, f[0]], P[:, f[1]], P[:, f[2]]
+        area += 0.5 * np.linalg.norm(np.cross(b - a, cc - a), axis=1)
+    return float(np.min(vol / (0.5 * area)))
+
+
+def estimate_dt_3d(mesh, order: int, cfl: float = 1.0) -> float:
+    """The reference's 3D estimate for the Global operator (Solver.cpp:289-300, 349-351):
+    dtscale_min * rmin * 2/3 * 0.75 * cfl / 0.8, rmin the smallest Gauss-Lobatto spacing
+    on [-1, 1] (lobatto() gives the nodes on [0, 1])."""
+    g = lobatto(order)
+    rmin = 2.0 * float(abs(g[1] - g[0]))
+    return dt_scale_min(mesh.vertices, mesh.elements) * rmin * 2.0 / 3.0 * 0.75 * cfl / 0.8

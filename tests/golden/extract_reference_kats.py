@@ -4,7 +4,9 @@ Reads the reference's own GoogleTest sources (Hesthaven & Warburton comparison
 tests) and writes ``reference_kats.json`` beside this script. Run it where the
 reference checkout is available:
 
-    python tests/golden/extract_reference_kats.py /root/reference
+    python tests/golden/extract_reference_kats.py <reference checkout>
+
+(or with the checkout in the DGTD_REFERENCE environment variable).
 
 Only numeric literals are taken (the expected matrices of each test); the
 fixture records the source file and line of every matrix.
@@ -83,7 +85,11 @@ def extract(ref_root: Path) -> dict:
 
 
 def main() -> None:
-    ref = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    import os
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("DGTD_REFERENCE")
+    if not root:
+        sys.exit("usage: extract_reference_kats.py <reference checkout>  (or set DGTD_REFERENCE)")
+    ref = Path(root)
     data = extract(ref)
     (HERE / "reference_kats.json").write_text(json.dumps(data, indent=1))
     print(f"wrote {len(data)} matrices to {HERE / 'reference_kats.json'}")

@@ -1085,12 +1085,20 @@ int dgtd_op_step_noalloc(dgtd_op* op, void* d_state, double t0, double dt, int32
         double* state = static_cast<double*>(d_state);
         double* other = ws;   // LSERK4 second state buffer
         double* cur = state;
+        // installed probes are sampled exactly as dgtd_op_step samples them (same step
+        // counter, so the two calls can be mixed); their buffers were allocated when the
+        // probes were installed, so sampling allocates nothing
+        dgtd::ProbeSet* pr = op->probes.get();
         if (integrator == DGTD_LSERK4)
             ck(cudaMemsetAsync(ws + 2 * op->state_len, 0, op->state_len * sizeof(double), s), "memset");
         double t = t0;
         for (int i = 0; i < nsteps; ++i) {
             rk_step_at(op, ws, state, t, dt, integrator, other, cur, s);
             t += dt;
+            if (pr && ++op->probe_steps % pr->every() == 0) {
+                pr->sample(cur, t, s);
+                g_launches.fetch_add(1, std::memory_order_relaxed);
+            }
         }
         if (integrator == DGTD_LSERK4 && cur != state)
             ck(cudaMemcpyAsync(state, cur, op->state_len * sizeof(double), cudaMemcpyDeviceToDevice, s), "copy");

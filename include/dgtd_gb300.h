@@ -168,7 +168,9 @@ int dgtd_op_run_host(dgtd_op* op, double* h_state, double t0, double dt, double 
  * in the reference; it serves callers that cannot allow a device allocation during
  * stepping. The first call on each device looks up the array's address (set-up: make
  * that call before any stream capture). Errors: DGTD_ERR_INVALID when state_len
- * exceeds dgtd_noalloc_max_state(), DGTD_ERR_UNSUPPORTED for the FP32 batched form.
+ * exceeds dgtd_noalloc_max_state(), DGTD_ERR_UNSUPPORTED for the FP32 forms.
+ * Installed probes (dgtd_op_set_probes) are sampled after every `every`-th step on the
+ * same step counter as dgtd_op_step, so the two calls may be mixed on one operator.
  * The array keeps the last call's contents; calls that overlap on the GPU race. */
 int dgtd_op_step_noalloc(dgtd_op* op, void* d_state, double t0, double dt, int32_t nsteps, int32_t integrator,
                          void* stream);

@@ -70,6 +70,36 @@ def test_noalloc_shared_by_operators(torch_cuda):
         assert rel_l2(got2.cpu().numpy(), ref2.cpu().numpy()) <= TOL
 
 
+def test_noalloc_samples_probes_like_step(torch_cuda):
+    """With probes installed, the no-allocation call samples them on the same cadence as
+    dgtd_op_step: the recorded series and DFT sums agree to the parity bar, also when the
+    two calls are mixed on one operator."""
+    torch = torch_cuda
+    pts = np.array([[0.1, -0.2, 0.3], [-0.5, 0.4, -0.6]])
+    freqs = np.array([0.7, 1.9])
+    ops = [_scatterer_op(), _scatterer_op(), _scatterer_op()]
+    for op in ops:
+        op.set_probes(points=pts, freqs=freqs, every=2, max_records=16)
+    rng = np.random.default_rng(5)
+    x0 = rng.standard_normal(ops[0].state_len) * 1e-3
+    xs = [torch.from_numpy(x0.copy()).cuda() for _ in ops]
+    dt = ops[0].estimate_dt(1.0)
+    for k in range(2):
+        t = 5 * k * dt
+        ops[0].step(xs[0], t, dt, 5)
+        ops[1].step_noalloc(xs[1], t, dt, 5)
+        (ops[2].step if k == 0 else ops[2].step_noalloc)(xs[2], t, dt, 5)
+    torch.cuda.synchronize()
+    want = ops[0].probe_read()
+    assert want["n_samples"] == 5
+    for op in ops[1:]:
+        got = op.probe_read()
+        assert got["n_samples"] == want["n_samples"]
+        assert np.array_equal(got["times"], want["times"])
+        assert rel_l2(got["series"], want["series"]) <= TOL
+        assert np.abs(got["points"] - want["points"]).max() <= TOL * np.abs(want["points"]).max()
+
+
 def test_noalloc_rejects_oversize_state(torch_cuda):
     torch = torch_cuda
     m = dg.box_mesh((8, 8, 8), outer_bc=dg.BC_PEC)

@@ -88,7 +88,7 @@ class CaseRunOpts(C.Structure):
 
 class CaseResult(C.Structure):
     _fields_ = [("steps", C.c_int64), ("dt", C.c_double), ("final_time", C.c_double), ("n_records", C.c_int64),
-                ("seconds", C.c_double)]
+                ("seconds", C.c_double), ("unstable_step", C.c_int64)]
 
 
 class ServerOpts(C.Structure):
@@ -105,7 +105,8 @@ class Request(C.Structure):
 class RequestStats(C.Structure):
     _fields_ = [("status", C.c_int32), ("order", C.c_int32), ("n_elements", C.c_int64), ("state_len", C.c_int64),
                 ("steps", C.c_int64), ("region_bytes", C.c_int64), ("dt", C.c_double), ("t_submit", C.c_double),
-                ("t_admit", C.c_double), ("t_first_launch", C.c_double), ("t_done", C.c_double)]
+                ("t_admit", C.c_double), ("t_first_launch", C.c_double), ("t_done", C.c_double),
+                ("unstable", C.c_int32)]
 
 
 class ServerStats(C.Structure):
@@ -118,6 +119,7 @@ class ServerStats(C.Structure):
 REQ_QUEUED, REQ_ACTIVE, REQ_DONE, REQ_FAILED = 0, 1, 2, 3
 SERVER_MAX_ACTIVE = 128
 DGTD_ERR_TIMEOUT = -5
+DGTD_ERR_UNSTABLE = -6
 
 _lib_handle: Optional[C.CDLL] = None
 
@@ -144,6 +146,10 @@ SIGNATURES = {
     "dgtd_op_step_noalloc": (C.c_int, [_P, _P, C.c_double, C.c_double, C.c_int32, C.c_int32, _P]),
     "dgtd_noalloc_max_state": (C.c_int64, []),
     "dgtd_op_norm2": (C.c_int, [_P, _P, _D, _P]),
+    "dgtd_op_set_stability_check": (C.c_int, [_P, C.c_int32, C.c_int32]),
+    "dgtd_op_stability": (C.c_int, [_P, _I64, _D, _D, _I64]),
+    "dgtd_op_stability_check": (C.c_int, [_P, _P, C.c_int64, C.c_double, _P]),
+    "dgtd_op_stability_reset": (C.c_int, [_P]),
     "dgtd_op_set_contraction": (C.c_int, [_P, C.c_int32]),
     "dgtd_op_uses_tensor_cores": (C.c_int, [_P]),
     "dgtd_op_set_graph_steps": (C.c_int, [_P, C.c_int32]),
@@ -476,6 +482,20 @@ class Operator:
         out = np.zeros(self.batch)
         _check(lib().dgtd_op_norm2(self._h, _ptr(state), _dp(out), _stream(stream)), "dgtd_op_norm2")
         return out
+
+    def set_stability_check(self, every: int = 10, stop: bool = False) -> None:
+        """Instability detector of run_host (reference Solver.cpp:500-516): a device norm check
+        every `every` steps (0: off); stop=True ends the run with DGTD_ERR_UNSTABLE, else a
+        warning is printed on stderr and the run goes on (the reference's behaviour)."""
+        _check(lib().dgtd_op_set_stability_check(self._h, int(every), 1 if stop else 0),
+               "dgtd_op_set_stability_check")
+
+    def stability(self) -> dict:
+        st, t, nrm, ch = C.c_int64(), C.c_double(), C.c_double(), C.c_int64()
+        _check(lib().dgtd_op_stability(self._h, C.byref(st), C.byref(t), C.byref(nrm), C.byref(ch)),
+               "dgtd_op_stability")
+        return {"first_step": st.value, "t": t.value, "norm": nrm.value, "checks": ch.value,
+                "unstable": st.value >= 0}
 
     # -- probes (point probes, near-to-far surface, running FP64 DFT sums)
     def set_probes(self, points=None, surface_faces=None, freqs=(), every: int = 1, max_records: int = 0) -> None:

@@ -4,6 +4,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <memory>
 #include <mutex>
@@ -94,6 +95,11 @@ struct dgtd_op {
     dgtd::TfsfSkipBound skip_bound;     // one incidence, one plain wave: host bounds of the skip test
     const int* skip_const = nullptr;    // device flags {0, 1} a stage reads when the host decided
     double* norm_dev = nullptr;
+    // instability detector of dgtd_op_run_host (reference Solver.cpp:500-516)
+    dgtd::StabilityRecord* stab_dev = nullptr;
+    int stab_every = 10;        // check every `stab_every` steps (0: off)
+    int stab_stop = 0;          // 1: stop the run and return DGTD_ERR_UNSTABLE
+    int n_sm = 152;
     // RK scratch (allocated on first dgtd_op_step)
     double* ws = nullptr;
     int64_t ws_len = 0;
@@ -112,6 +118,7 @@ struct dgtd_op {
         if (pw_dev) cudaFree(pw_dev);
         if (skip_dev) cudaFree(skip_dev);
         if (norm_dev) cudaFree(norm_dev);
+        if (stab_dev) cudaFree(stab_dev);
         if (ws) cudaFree(ws);
         if (ws32) cudaFree(ws32);
     }
@@ -133,6 +140,14 @@ struct BatchedCount {
     explicit BatchedCount(dgtd_op* o) : op(o), before(o->batched->kernel_launches()) {}
     ~BatchedCount() { g_launches.fetch_add(op->batched->kernel_launches() - before, std::memory_order_relaxed); }
 };
+
+// Clears the instability record before a run (no check has tripped).
+void reset_stability(dgtd_op* op)
+{
+    dgtd::StabilityRecord r{};
+    r.first_step = -1;
+    ck(cudaMemcpy(op->stab_dev, &r, sizeof(r), cudaMemcpyHostToDevice), "reset stability record");
+}
 
 dgtd::MeshInput to_input(const dgtd_mesh_desc* m)
 {
@@ -393,6 +408,13 @@ int dgtd_op_create(const dgtd_mesh_desc* mesh, const dgtd_op_opts* opts, dgtd_op
             op->skip_const = static_cast<const int*>(a);
         }
         ck(cudaMalloc(&op->norm_dev, (op->batch + 32) * sizeof(double)), "cudaMalloc norm");
+        ck(cudaMalloc(&op->stab_dev, sizeof(dgtd::StabilityRecord)), "cudaMalloc stability record");
+        reset_stability(op.get());
+        {
+            int dev = 0;
+            ck(cudaGetDevice(&dev), "cudaGetDevice");
+            ck(cudaDeviceGetAttribute(&op->n_sm, cudaDevAttrMultiProcessorCount, dev), "SM count");
+        }
         if (op->precision == DGTD_FP32_3XTF32) op->batched = dgtd::BatchedOp::create(op->ref, op->mesh, op->dev, op->batch);
         if (op->precision == DGTD_FP32) {
             auto f32 = [](const std::vector<double>& v) { return std::vector<float>(v.begin(), v.end()); };
@@ -684,6 +706,26 @@ int dgtd_op_run_host(dgtd_op* op, double* h_state, double t0, double dt, double 
         } else {
             w = d;
         }
+        // instability detector (reference Solver.cpp:500-516): a device check every
+        // stab_every steps, its record read back every kStabReadEvery steps and at the end
+        const bool f32 = op->precision != DGTD_FP64;
+        const int64_t wlen = op->batched ? op->batched->state_len() : op->state_len;
+        constexpr int64_t kStabReadEvery = 256;
+        bool warned = false;
+        auto stability_read = [&]() -> int {
+            dgtd::StabilityRecord r{};
+            ck(cudaMemcpy(&r, op->stab_dev, sizeof(r), cudaMemcpyDeviceToHost), "read stability record");
+            if (r.first_step < 0) return DGTD_OK;
+            const std::string msg = "simulation is potentially unstable: field norm = " + std::to_string(r.norm) +
+                                    " at step " + std::to_string(r.first_step) + ", time " +
+                                    std::to_string(r.t) + " / " + std::to_string(final_time) + ", dt " +
+                                    std::to_string(dt) + "; verify the setup and consider a smaller time step";
+            if (op->stab_stop) return fail(DGTD_ERR_UNSTABLE, msg);
+            if (!warned) std::fprintf(stderr, "dgtd_gb300: WARNING: %s\n", msg.c_str());
+            warned = true;
+            return DGTD_OK;
+        };
+        if (op->stab_every > 0) reset_stability(op);
         double t = t0;
         while (rc == DGTD_OK && t <= final_time - 1e-8 * dt) {
             double truedt = std::min(dt, final_time - t);
@@ -691,6 +733,20 @@ int dgtd_op_run_host(dgtd_op* op, double* h_state, double t0, double dt, double 
             if (rc != DGTD_OK) break;
             t += truedt;
             ++steps;
+            if (op->stab_every > 0 && steps % op->stab_every == 0) {
+                ck(dgtd::launch_stability_check(w, wlen, f32, op->stab_dev, steps, t, op->n_sm, nullptr),
+                   "stability check");
+                g_launches.fetch_add(2, std::memory_order_relaxed);
+                if (steps % kStabReadEvery == 0) rc = stability_read();
+            }
+        }
+        if (rc == DGTD_OK && op->stab_every > 0) {
+            if (steps % op->stab_every != 0) {   // the final state is always checked
+                ck(dgtd::launch_stability_check(w, wlen, f32, op->stab_dev, steps, t, op->n_sm, nullptr),
+                   "stability check");
+                g_launches.fetch_add(2, std::memory_order_relaxed);
+            }
+            rc = stability_read();
         }
         if (rc == DGTD_OK && op->precision != DGTD_FP64) rc = dgtd_op_unpack(op, w, d, nullptr);
         if (rc == DGTD_OK) ck(cudaMemcpy(h_state, d, bytes, cudaMemcpyDeviceToHost), "D2H");
@@ -725,6 +781,59 @@ int dgtd_op_norm2(dgtd_op* op, const void* d_state, double* h_out, void* stream)
     } catch (const std::exception& e) {
         return fail(DGTD_ERR_CUDA, e.what());
     }
+    return DGTD_OK;
+}
+
+int dgtd_op_set_stability_check(dgtd_op* op, int32_t every, int32_t stop)
+{
+    if (!op) return fail(DGTD_ERR_INVALID, "NULL argument");
+    if (every < 0) return fail(DGTD_ERR_INVALID, "every must be >= 0");
+    if (stop != 0 && stop != 1) return fail(DGTD_ERR_INVALID, "stop must be 0 or 1");
+    op->stab_every = every;
+    op->stab_stop = stop;
+    return DGTD_OK;
+}
+
+int dgtd_op_stability_reset(dgtd_op* op)
+{
+    if (!op) return fail(DGTD_ERR_INVALID, "NULL argument");
+    try {
+        reset_stability(op);
+    } catch (const std::exception& e) {
+        return fail(DGTD_ERR_CUDA, e.what());
+    }
+    return DGTD_OK;
+}
+
+int dgtd_op_stability_check(dgtd_op* op, const void* d_state, int64_t step, double t, void* stream)
+{
+    if (!op || !d_state) return fail(DGTD_ERR_INVALID, "NULL argument");
+    try {
+        const bool f32 = op->precision != DGTD_FP64;
+        const int64_t wlen = op->batched ? op->batched->state_len() : op->state_len;
+        ck(dgtd::launch_stability_check(d_state, wlen, f32, op->stab_dev, step, t, op->n_sm,
+                                        static_cast<cudaStream_t>(stream)),
+           "stability check");
+        g_launches.fetch_add(2, std::memory_order_relaxed);
+    } catch (const std::exception& e) {
+        return fail(DGTD_ERR_CUDA, e.what());
+    }
+    return DGTD_OK;
+}
+
+int dgtd_op_stability(const dgtd_op* op, int64_t* first_step, double* t, double* norm, int64_t* checks)
+{
+    if (!op) return fail(DGTD_ERR_INVALID, "NULL argument");
+    dgtd::StabilityRecord r{};
+    try {
+        ck(cudaMemcpy(&r, op->stab_dev, sizeof(r), cudaMemcpyDeviceToHost), "read stability record");
+    } catch (const std::exception& e) {
+        return fail(DGTD_ERR_CUDA, e.what());
+    }
+    if (first_step) *first_step = r.first_step;
+    if (t) *t = r.t;
+    if (norm) *norm = r.norm;
+    if (checks) *checks = r.checks;
     return DGTD_OK;
 }
 

@@ -188,12 +188,18 @@ int dgtd_case_run(const dgtd_case* cs, const dgtd_case_run_opts* ro, double* h_s
         const auto t0 = std::chrono::steady_clock::now();
         double t = 0.0;
         int64_t steps = 0;
+        // instability detector of Solver::run (reference Solver.cpp:500-516): a device check every
+        // kStabEvery steps and of the final state, read back at the end
+        constexpr int64_t kStabEvery = 10;
+        ok(dgtd_op_stability_reset(op), "stability reset");
         while (t <= c.final_time - 1e-8 * dt) {
             const double h = std::min(dt, c.final_time - t);
             ok(dgtd_op_step(op, d, t, h, 1, c.integrator, nullptr), "dgtd_op_step");
             t += h;
             ++steps;
+            if (steps % kStabEvery == 0) ok(dgtd_op_stability_check(op, d, steps, t, nullptr), "stability check");
         }
+        if (steps % kStabEvery != 0) ok(dgtd_op_stability_check(op, d, steps, t, nullptr), "stability check");
         if (probes && npts > 0 && steps % every != 0) ok(dgtd_op_probe_sample(op, d, t, nullptr), "final probe sample");
         if (cudaDeviceSynchronize() != cudaSuccess) throw std::runtime_error("device synchronisation failed");
         const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
@@ -218,12 +224,21 @@ int dgtd_case_run(const dgtd_case* cs, const dgtd_case_run_opts* ro, double* h_s
                 }
             }
         }
+        int64_t unstable_step = -1;
+        double unstable_t = 0.0, unstable_norm = 0.0;
+        ok(dgtd_op_stability(op, &unstable_step, &unstable_t, &unstable_norm, nullptr), "stability record");
+        if (unstable_step >= 0)
+            std::fprintf(stderr,
+                         "dgtd_gb300: WARNING: simulation is potentially unstable (field norm = %g at step %lld, "
+                         "time %g / %g, dt %g); verify the setup and consider a smaller time step\n",
+                         unstable_norm, static_cast<long long>(unstable_step), unstable_t, c.final_time, dt);
         if (res) {
             res->steps = steps;
             res->dt = dt;
             res->final_time = t;
             res->n_records = nrec;
             res->seconds = secs;
+            res->unstable_step = unstable_step;
         }
     } catch (const std::exception& e) {
         rc = cfail(DGTD_ERR_CUDA, e.what());

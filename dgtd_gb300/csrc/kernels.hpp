@@ -111,4 +111,19 @@ cudaError_t launch_norm2_f32s(const float* in, int64_t n_per_batch, int batch, d
 cudaError_t launch_convert_f64_to_f32(const double* in, float* out, int64_t n, cudaStream_t s);
 cudaError_t launch_convert_f32_to_f64(const float* in, double* out, int64_t n, cudaStream_t s);
 
+// Instability detector of the run loop (stability.cu; reference Solver.cpp:500-516): a state
+// whose L2 norm is not finite or above kUnstableNorm. The record lives in device memory;
+// first_step < 0 while no check has tripped.
+constexpr double kUnstableNorm = 1e20;
+struct StabilityRecord {
+    double sumsq;          // running sum of the current check (zero between checks)
+    int64_t first_step;    // step count of the first check that tripped, or -1
+    double t;              // its time
+    double norm;           // its norm (NaN or infinity when the state was not finite)
+    int64_t checks;        // checks run since the record was reset
+};
+// One check of n entries (FP32 or FP64) at step `step`, time t: two launches, no sync.
+cudaError_t launch_stability_check(const void* state, int64_t n, bool f32, StabilityRecord* rec, int64_t step,
+                                   double t, int n_sm, cudaStream_t s);
+
 }  // namespace dgtd

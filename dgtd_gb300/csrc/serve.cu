@@ -27,6 +27,8 @@
 #include <atomic>
 #include <chrono>
 #include <condition_variable>
+#include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <deque>
 #include <limits>
@@ -44,6 +46,10 @@
 #include "fp64_stage.cuh"
 #include "mesh.hpp"
 #include "refelem.hpp"
+
+namespace {
+constexpr double kUnstableNormHost = 1e20;   // reference Solver.cpp:500-516
+}
 
 namespace dgtd {
 
@@ -292,6 +298,7 @@ struct Req {
     std::string err;
     std::vector<double> result;
     double t_submit = 0, t_admit = 0, t_first = 0, t_done = 0;
+    int unstable = 0;   // the final state's norm was not finite or above 1e20
 };
 
 using ReqP = std::shared_ptr<Req>;
@@ -613,6 +620,19 @@ void retire_loop(dgtd_server* s)
             }
             cudaEventDestroy(r->ev_last);
             r->ev_last = nullptr;
+            // instability detector of the run loop (reference Solver::run, Solver.cpp:500-516)
+            // on the downloaded final state: a norm that is not finite or above 1e20
+            {
+                double s2 = 0.0;
+                for (size_t i = 0; i < n; ++i) s2 += r->result[i] * r->result[i];
+                const double nrm = std::sqrt(s2);
+                if (!(nrm <= kUnstableNormHost)) {
+                    r->unstable = 1;
+                    std::fprintf(stderr, "dgtd_gb300: WARNING: request %lld is potentially unstable (field norm = %g "
+                                 "at t = %g, dt %g); verify the setup and consider a smaller time step\n",
+                                 static_cast<long long>(r->id), nrm, r->T, r->dt);
+                }
+            }
             std::lock_guard<std::mutex> lk(s->mu);
             s->arena.release(r->off);
             r->off = -1;
@@ -649,6 +669,7 @@ void fill_stats(const Req& r, dgtd_request_stats* o)
     o->t_admit = r.t_admit;
     o->t_first_launch = r.t_first;
     o->t_done = r.t_done;
+    o->unstable = r.unstable;
 }
 
 void destroy_server(dgtd_server* s)

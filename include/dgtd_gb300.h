@@ -34,6 +34,7 @@ extern "C" {
 #define DGTD_ERR_UNSUPPORTED (-3)
 #define DGTD_ERR_NOMEM (-4)
 #define DGTD_ERR_TIMEOUT (-5)
+#define DGTD_ERR_UNSTABLE (-6) /* the run loop's instability detector tripped (stop mode) */
 
 /* Boundary codes (reference BdrCond, src/components/Types.h:47-55). */
 #define DGTD_BC_OPEN 0
@@ -175,6 +176,27 @@ int dgtd_op_run_host(dgtd_op* op, double* h_state, double t0, double dt, double 
 int dgtd_op_step_noalloc(dgtd_op* op, void* d_state, double t0, double dt, int32_t nsteps, int32_t integrator,
                          void* stream);
 
+/* Instability detector of dgtd_op_run_host (reference Solver::run, Solver.cpp:500-516,
+ * which checks the field norm after every step and prints a warning when it is not finite
+ * or above 1e20). Here a device reduction runs every `every` steps (default 10; 0 turns it
+ * off) and after the last step, without host synchronisation; the host reads the result
+ * every 256 steps and at the end. stop = 0 (default) follows the reference: a warning on
+ * stderr and the run goes on; stop = 1 ends the run at the next read with
+ * DGTD_ERR_UNSTABLE. */
+int dgtd_op_set_stability_check(dgtd_op* op, int32_t every, int32_t stop);
+
+/* The detector's record (of the last dgtd_op_run_host, or of the checks since the last
+ * dgtd_op_stability_reset): the step count and time of the first check that tripped
+ * (first_step = -1: none), its norm, and the number of checks run. Outputs may be NULL. */
+int dgtd_op_stability(const dgtd_op* op, int64_t* first_step, double* t, double* norm, int64_t* checks);
+
+/* For callers that run their own loop (the adapter under Solver::run): one check of the
+ * working state d_state at step count `step` and time t on `stream` (device reduction, no
+ * host synchronisation; the record keeps the first check that tripped), and a reset of the
+ * record. */
+int dgtd_op_stability_check(dgtd_op* op, const void* d_state, int64_t step, double t, void* stream);
+int dgtd_op_stability_reset(dgtd_op* op);
+
 /* Largest state_len (reference-layout entries) dgtd_op_step_noalloc accepts. */
 int64_t dgtd_noalloc_max_state(void);
 
@@ -287,6 +309,9 @@ typedef struct dgtd_case_result {
     double final_time;
     int64_t n_records;           /* point-probe samples recorded */
     double seconds;              /* wall time of the time loop */
+    int64_t unstable_step;       /* first step whose field norm was not finite or above 1e20, checked
+                                    every 10 steps and at the end (reference Solver.cpp:500-516; the
+                                    run goes on after a warning on stderr, as the reference's), or -1 */
 } dgtd_case_result;
 
 /* Read a case file and its mesh. */
@@ -362,6 +387,9 @@ typedef struct dgtd_request_stats {
     double t_admit;        /* region reserved and uploaded */
     double t_first_launch;
     double t_done;         /* result on the host */
+    int32_t unstable;      /* 1: the final state's L2 norm was not finite or above 1e20 (the
+                              instability detector of Solver::run, Solver.cpp:500-516, applied to
+                              the downloaded result; a warning is printed on stderr) */
 } dgtd_request_stats;
 
 typedef struct dgtd_server_stats {

@@ -154,6 +154,24 @@ def test_initial_state_and_no_sources(torch_cuda):
     assert np.array_equal(x, ref)
 
 
+def test_unstable_request_is_flagged(torch_cuda):
+    """The run loop's instability detector (reference Solver.cpp:500-516) on served requests: a
+    NaN planted in one request's initial state flags that request only."""
+    m = dg.box_mesh((3, 3, 3))
+    op = dg.Operator(m, order=2)
+    xyz = op.node_coords()
+    z = np.zeros(op.ndofs)
+    good = np.concatenate([z, z, np.sin(np.pi * xyz[0]) * np.sin(np.pi * xyz[1]), z, z, z])
+    bad = good.copy()
+    bad[7] = np.nan
+    with dg.Server(memory_budget=1 << 28, max_active=4) as s:
+        ids = [s.submit(m, 2, 0.02, init=x, dt=1e-3) for x in (good, bad)]
+        res = [s.wait(i, timeout=120) for i in ids]
+    assert res[0][1]["unstable"] == 0 and np.all(np.isfinite(res[0][0]))
+    assert res[1][1]["unstable"] == 1 and not np.all(np.isfinite(res[1][0]))
+    assert res[1][1]["status"] == dg.REQ_DONE
+
+
 def test_fp32_serving_matches_fp32_operator_and_mix(torch_cuda):
     """FP32 serving runs the single-instance FP32 form's stage: bit-identical to
     dgtd_op_run_host of that form, alone and in the mix, and within 1e-5 of FP64."""

@@ -20,6 +20,7 @@
 #include "mesh.hpp"
 #include "probes.hpp"
 #include "refelem.hpp"
+#include "single_tc.hpp"
 
 namespace {
 
@@ -106,6 +107,11 @@ struct dgtd_op {
     // single-instance FP32 form: FP32 copies of the tables, RK scratch
     dgtd::TablesF32 dev32{};
     float* ws32 = nullptr;
+    // single-instance FP32 form on the tensor cores: A-operand image, device error flag, and
+    // the contraction path (0: tensor cores where supported, 1: FP32 SIMT)
+    uint32_t* tc1_img = nullptr;
+    int* tc1_status = nullptr;
+    int contraction32 = 0;
     // batched FP32 form
     std::unique_ptr<dgtd::BatchedOp> batched;
     // point probes / DFT accumulators, sampled by dgtd_op_step every probes->every() steps
@@ -119,6 +125,8 @@ struct dgtd_op {
         if (skip_dev) cudaFree(skip_dev);
         if (norm_dev) cudaFree(norm_dev);
         if (stab_dev) cudaFree(stab_dev);
+        if (tc1_img) cudaFree(tc1_img);
+        if (tc1_status) cudaFree(tc1_status);
         if (ws) cudaFree(ws);
         if (ws32) cudaFree(ws32);
     }
@@ -275,6 +283,8 @@ void rk_step(dgtd_op* op, double* d_x, double t, double dt, int integrator, doub
 }
 
 // ---- single-instance FP32 form: the same stage sequence on FP32 registers
+bool uses_tc1(const dgtd_op* op) { return op->tc1_img != nullptr && op->contraction32 == 0; }
+
 void run_stage32(dgtd_op* op, dgtd::StageArgsF32 A, double t, cudaStream_t s)
 {
     A.t = t;
@@ -295,7 +305,10 @@ void run_stage32(dgtd_op* op, dgtd::StageArgsF32 A, double t, cudaStream_t s)
         A.n_pw = 0;
         A.skip = nullptr;
     }
-    ck(dgtd::launch_stage_f32s(op->dev32, A, s), "FP32 stage kernel");
+    if (uses_tc1(op))
+        dgtd::launch_stage_tc1(op->dev32, A, op->tc1_img, op->tc1_status, op->n_sm, s);
+    else
+        ck(dgtd::launch_stage_f32s(op->dev32, A, s), "FP32 stage kernel");
     g_launches.fetch_add(1, std::memory_order_relaxed);
 }
 
@@ -434,6 +447,15 @@ int dgtd_op_create(const dgtd_mesh_desc* mesh, const dgtd_op_opts* opts, dgtd_op
             F.xyz = op->up(f32(xyz));
             F.tfsf_elems = T.tfsf_elems;
             F.n_tfsf_elems = T.n_tfsf_elems;
+            if (dgtd::tc1_supported(T.p)) {
+                const std::vector<uint32_t> img = dgtd::tc1_operator_image(op->ref);
+                ck(cudaMalloc(&op->tc1_img, img.size() * sizeof(uint32_t)), "cudaMalloc tensor-core operator");
+                ck(cudaMemcpy(op->tc1_img, img.data(), img.size() * sizeof(uint32_t), cudaMemcpyHostToDevice),
+                   "upload tensor-core operator");
+                op->device_bytes += static_cast<int64_t>(img.size() * sizeof(uint32_t));
+                ck(cudaMalloc(&op->tc1_status, sizeof(int)), "cudaMalloc status");
+                ck(cudaMemset(op->tc1_status, 0, sizeof(int)), "memset status");
+            }
         }
     } catch (const CudaError& e) {
         return fail(DGTD_ERR_CUDA, e.what());
@@ -842,6 +864,7 @@ int dgtd_op_set_contraction(dgtd_op* op, int32_t mode)
     if (!op) return fail(DGTD_ERR_INVALID, "NULL operator");
     if (mode != 0 && mode != 1) return fail(DGTD_ERR_INVALID, "contraction mode must be 0 or 1");
     if (op->batched) op->batched->set_contraction(mode);
+    op->contraction32 = mode;
     return DGTD_OK;
 }
 
@@ -874,7 +897,12 @@ int dgtd_op_autotune(dgtd_op* op, const void* d_work, void* stream, double* h_ms
     return DGTD_OK;
 }
 
-int dgtd_op_uses_tensor_cores(const dgtd_op* op) { return (op && op->batched && op->batched->uses_tensor_cores()) ? 1 : 0; }
+int dgtd_op_uses_tensor_cores(const dgtd_op* op)
+{
+    if (!op) return 0;
+    if (op->batched) return op->batched->uses_tensor_cores() ? 1 : 0;
+    return (op->precision == DGTD_FP32 && uses_tc1(op)) ? 1 : 0;
+}
 
 int dgtd_op_check(dgtd_op* op, void* stream)
 {
@@ -884,6 +912,14 @@ int dgtd_op_check(dgtd_op* op, void* stream)
         ck(cudaStreamSynchronize(s), "sync");
         if (op->batched && op->batched->take_status(s))
             return fail(DGTD_ERR_TIMEOUT, "a tensor-core completion wait inside the stage kernel timed out");
+        if (op->tc1_status) {
+            int st = 0;
+            ck(cudaMemcpy(&st, op->tc1_status, sizeof(int), cudaMemcpyDeviceToHost), "read status");
+            if (st) {
+                ck(cudaMemset(op->tc1_status, 0, sizeof(int)), "clear status");
+                return fail(DGTD_ERR_TIMEOUT, "a tensor-core completion wait inside the stage kernel timed out");
+            }
+        }
     } catch (const std::exception& e) {
         return fail(DGTD_ERR_CUDA, e.what());
     }

@@ -200,8 +200,12 @@ int dgtd_op_stability_reset(dgtd_op* op);
 /* Largest state_len (reference-layout entries) dgtd_op_step_noalloc accepts. */
 int64_t dgtd_noalloc_max_state(void);
 
-/* Contraction path of the FP32 batched form: 0 = tensor cores (tcgen05, 3xTF32) where
- * supported (orders 1..4, B padded to a multiple of 64), else FP32 SIMT; 1 = FP32 SIMT. */
+/* Contraction path of the FP32 forms: 0 (default) = tensor cores (tcgen05, 3xTF32) where
+ * supported, else FP32 SIMT; 1 = FP32 SIMT. Batched form: tensor cores for orders 1..4 with
+ * B padded to a multiple of 64 (work item: one element x 64 incidences). Single-instance
+ * form: tensor cores for orders 1..6 (work item: 8 elements of one incidence; reference-
+ * element matrices as the A operand, fields and fluxes as the B operand, chain rule and curl
+ * in FP32 in the epilogue). */
 int dgtd_op_set_contraction(dgtd_op* op, int32_t mode);
 
 /* Batched FP32 form: replay blocks of `steps` classical-RK4 steps of dgtd_op_step from one

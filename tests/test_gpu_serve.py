@@ -184,6 +184,7 @@ def test_fp32_serving_matches_fp32_operator_and_mix(torch_cuda):
             alone_x, st = s.wait(s.submit(r["mesh"], r["order"], r["final_time"], waves=r["waves"], cfl=1.0), 300)
         assert np.array_equal(xm, alone_x)
         op = dg.Operator(r["mesh"], order=r["order"], precision=dg.FP32)
+        op.set_contraction(1)          # the server steps the FP32 SIMT stage body
         op.set_planewaves(r["waves"])
         ref32, n = op.run_host(np.zeros(op.state_len), 0.0, op.estimate_dt(1.0), r["final_time"])
         assert n == st["steps"] and np.array_equal(xm, ref32)

@@ -195,10 +195,16 @@ __global__ void __launch_bounds__(kWarps * kLanes) stage_f32(BatchedTables T, Ba
                 const float uc = s_u[(c * Np + i) * kLanes + lane];
                 switch (A.mode) {
                 case MODE_MULT: A.out[idx] = k[c]; break;
-                case MODE_RK4_1: A.yout[idx] = uc + 0.5f * dt * k[c]; A.z[idx] = uc + (dt / 6.0f) * k[c]; break;
+                case MODE_RK4_1: A.yout[idx] = uc + 0.5f * dt * k[c]; A.z[idx] = (dt / 6.0f) * k[c]; break;
                 case MODE_RK4_2: A.yout[idx] = A.x[idx] + 0.5f * dt * k[c]; A.z[idx] += (dt / 3.0f) * k[c]; break;
                 case MODE_RK4_3: A.yout[idx] = A.x[idx] + dt * k[c]; A.z[idx] += (dt / 3.0f) * k[c]; break;
-                case MODE_RK4_4: A.x[idx] = A.z[idx] + (dt / 6.0f) * k[c]; break;
+                case MODE_RK4_4: {
+                    float hi = A.x[idx], lo = A.xl[idx];
+                    add_compensated(hi, lo, A.z[idx] + (dt / 6.0f) * k[c]);
+                    A.x[idx] = hi;
+                    A.xl[idx] = lo;
+                    break;
+                }
                 case MODE_LSRK: {
                     const float r = A.a * A.res[idx] + dt * k[c];
                     A.res[idx] = r;
@@ -259,32 +265,73 @@ __global__ void __launch_bounds__(256) tfsf_skip_f32(BatchedTables T, const Plan
     }
 }
 
-// reference [b][c][e*Np+i] (FP64) -> internal [e'][c][i][b] (FP32)
-__global__ void pack_kernel(const double* __restrict__ ref, float* __restrict__ st, const int32_t* __restrict__ perm,
-                            int64_t K, int Np, int B, int Bp)
+// reference [b][c][e*Np+i] (FP64) -> internal [e'][c][i][b] as the FP32 pair (x_hi | x_lo blocks).
+// One block transposes one (element, component, chunk of 64 incidences) tile through shared memory:
+// it reads the reference rows (Np consecutive values per incidence) and writes the internal rows
+// (64 consecutive incidences per node), both as contiguous runs, so the copy also streams well when
+// the reference state is pinned host memory read over the host link.
+constexpr int kPackChunk = 64;
+
+__global__ void __launch_bounds__(256) pack_kernel(const double* __restrict__ ref, float* __restrict__ st,
+                                                   const int32_t* __restrict__ perm, int64_t K, int Np, int B, int Bp)
 {
-    const int64_t total = K * 6 * Np;
-    for (int64_t r = blockIdx.x; r < total; r += gridDim.x) {
-        const int64_t ei = r / (6 * Np);
-        const int rem = static_cast<int>(r - ei * 6 * Np), c = rem / Np, i = rem - c * Np;
-        const int64_t er = perm[ei];
-        const int64_t N = K * Np;
-        for (int b = threadIdx.x; b < Bp; b += blockDim.x)
-            st[r * Bp + b] = (b < B) ? static_cast<float>(ref[(static_cast<int64_t>(b) * 6 + c) * N + er * Np + i]) : 0.0f;
+    extern __shared__ float tile[];                 // [2][Np][kPackChunk]
+    const int64_t r = blockIdx.x;                   // element * 6 + component (internal order)
+    const int64_t ei = r / 6;
+    const int c = static_cast<int>(r - ei * 6);
+    const int b0 = blockIdx.y * kPackChunk;
+    const int64_t N = K * Np;
+    const int64_t er = perm[ei];
+    const int n = Np * kPackChunk;
+    for (int q = threadIdx.x; q < n; q += blockDim.x) {
+        const int bb = q / Np, i = q - bb * Np;
+        const int b = b0 + bb;
+        float hi = 0.0f, lo = 0.0f;
+        if (b < B) {
+            const double v = ref[(static_cast<int64_t>(b) * 6 + c) * N + er * Np + i];
+            hi = static_cast<float>(v);
+            lo = static_cast<float>(v - static_cast<double>(hi));
+        }
+        tile[i * kPackChunk + bb] = hi;
+        tile[n + i * kPackChunk + bb] = lo;
+    }
+    __syncthreads();
+    const int64_t L = K * 6 * static_cast<int64_t>(Np) * Bp;   // x_lo block offset
+    for (int q = threadIdx.x; q < n; q += blockDim.x) {
+        const int i = q / kPackChunk, bb = q - i * kPackChunk;
+        if (b0 + bb >= Bp) continue;                 // Bpad = 32: half a chunk
+        const int64_t o = (r * Np + i) * Bp + b0 + bb;
+        st[o] = tile[q];
+        st[L + o] = tile[n + q];
     }
 }
 
-__global__ void unpack_kernel(const float* __restrict__ st, double* __restrict__ ref, const int32_t* __restrict__ perm,
-                              int64_t K, int Np, int B, int Bp)
+__global__ void __launch_bounds__(256) unpack_kernel(const float* __restrict__ st, double* __restrict__ ref,
+                                                     const int32_t* __restrict__ perm, int64_t K, int Np, int B, int Bp)
 {
-    const int64_t total = K * 6 * Np;
-    for (int64_t r = blockIdx.x; r < total; r += gridDim.x) {
-        const int64_t ei = r / (6 * Np);
-        const int rem = static_cast<int>(r - ei * 6 * Np), c = rem / Np, i = rem - c * Np;
-        const int64_t er = perm[ei];
-        const int64_t N = K * Np;
-        for (int b = threadIdx.x; b < B; b += blockDim.x)
-            ref[(static_cast<int64_t>(b) * 6 + c) * N + er * Np + i] = st[r * Bp + b];
+    extern __shared__ float tile[];                 // [2][Np][kPackChunk]
+    const int64_t r = blockIdx.x;
+    const int64_t ei = r / 6;
+    const int c = static_cast<int>(r - ei * 6);
+    const int b0 = blockIdx.y * kPackChunk;
+    const int64_t N = K * Np;
+    const int64_t er = perm[ei];
+    const int n = Np * kPackChunk;
+    const int64_t L = K * 6 * static_cast<int64_t>(Np) * Bp;
+    for (int q = threadIdx.x; q < n; q += blockDim.x) {
+        const int i = q / kPackChunk, bb = q - i * kPackChunk;
+        if (b0 + bb >= Bp) continue;                 // Bpad = 32: half a chunk (never read back)
+        const int64_t o = (r * Np + i) * Bp + b0 + bb;
+        tile[q] = st[o];
+        tile[n + q] = st[L + o];
+    }
+    __syncthreads();
+    for (int q = threadIdx.x; q < n; q += blockDim.x) {
+        const int bb = q / Np, i = q - bb * Np;
+        const int b = b0 + bb;
+        if (b < B)
+            ref[(static_cast<int64_t>(b) * 6 + c) * N + er * Np + i] =
+                static_cast<double>(tile[i * kPackChunk + bb]) + static_cast<double>(tile[n + i * kPackChunk + bb]);
     }
 }
 
@@ -568,14 +615,20 @@ void BatchedOp::ensure_ws()
 
 void BatchedOp::pack(const double* d_ref, float* d_state, cudaStream_t s)
 {
-    pack_kernel<<<std::min<int64_t>(K_ * 6 * Np_, 1 << 20), 64, 0, s>>>(d_ref, d_state, perm_, K_, Np_, B_, Bpad_);
+    // Bpad is a multiple of 32; a last chunk of 32 padded incidences is handled as b >= B. At most
+    // 2 x 84 x 64 floats (43 KB) of shared memory: within the default limit.
+    const dim3 grid(static_cast<unsigned>(K_ * 6), static_cast<unsigned>((Bpad_ + kPackChunk - 1) / kPackChunk));
+    const size_t smem = 2 * static_cast<size_t>(Np_) * kPackChunk * sizeof(float);
+    pack_kernel<<<grid, 256, smem, s>>>(d_ref, d_state, perm_, K_, Np_, B_, Bpad_);
     ckb(cudaGetLastError(), "pack kernel");
     ++launches_;
 }
 
 void BatchedOp::unpack(const float* d_state, double* d_ref, cudaStream_t s)
 {
-    unpack_kernel<<<std::min<int64_t>(K_ * 6 * Np_, 1 << 20), 64, 0, s>>>(d_state, d_ref, perm_, K_, Np_, B_, Bpad_);
+    const dim3 grid(static_cast<unsigned>(K_ * 6), static_cast<unsigned>((Bpad_ + kPackChunk - 1) / kPackChunk));
+    const size_t smem = 2 * static_cast<size_t>(Np_) * kPackChunk * sizeof(float);
+    unpack_kernel<<<grid, 256, smem, s>>>(d_state, d_ref, perm_, K_, Np_, B_, Bpad_);
     ckb(cudaGetLastError(), "unpack kernel");
     ++launches_;
 }
@@ -585,6 +638,8 @@ void BatchedOp::mult(const float* d_in, float* d_out, double t, cudaStream_t s)
     BatchedStageArgs A{};
     A.mode = MODE_MULT; A.in = d_in; A.out = d_out;
     stage(A, t, s);
+    // d_out is a working state: its x_lo word is zero (the product is an FP32 value)
+    ckb(cudaMemsetAsync(d_out + state_len_, 0, state_len_ * sizeof(float), s), "memset");
 }
 
 void BatchedOp::rk4_steps_direct(float* d_x, double t, double dt, int nsteps, cudaStream_t s)
@@ -595,7 +650,7 @@ void BatchedOp::rk4_steps_direct(float* d_x, double t, double dt, int nsteps, cu
     float* z = ws_ + 2 * L;
     for (int n = 0; n < nsteps; ++n) {
         BatchedStageArgs A{};
-        A.dt = static_cast<float>(dt); A.x = d_x; A.z = z;
+        A.dt = static_cast<float>(dt); A.x = d_x; A.xl = d_x + L; A.z = z;
         A.mode = MODE_RK4_1; A.in = d_x; A.yout = y0; stage(A, t, s);
         A.mode = MODE_RK4_2; A.in = y0; A.yout = y1; stage(A, t + dt / 2, s);
         A.mode = MODE_RK4_3; A.in = y1; A.yout = y0; stage(A, t + dt / 2, s);
@@ -643,7 +698,7 @@ void BatchedOp::step(float* d_x, double t0, double dt, int nsteps, int integrato
                 float* y1 = ws_ + L;
                 for (int n = 0; n < G; ++n) {
                     BatchedStageArgs A{};
-                    A.dt = static_cast<float>(dt); A.x = d_x; A.z = z; A.t_base = t_dev_;
+                    A.dt = static_cast<float>(dt); A.x = d_x; A.xl = d_x + L; A.z = z; A.t_base = t_dev_;
                     const double tn = n * dt;
                     A.mode = MODE_RK4_1; A.in = d_x; A.yout = y0; A.t = static_cast<float>(tn); stage(A, 0.0, s);
                     A.mode = MODE_RK4_2; A.in = y0; A.yout = y1; A.t = static_cast<float>(tn + dt / 2); stage(A, 0.0, s);
@@ -675,6 +730,8 @@ void BatchedOp::step(float* d_x, double t0, double dt, int nsteps, int integrato
         float* res = z;
         float* other = y0;
         ckb(cudaMemsetAsync(res, 0, L * sizeof(float), s), "memset");
+        // the low-storage scheme steps x_hi alone (FP32 state): the x_lo word is cleared
+        ckb(cudaMemsetAsync(d_x + L, 0, L * sizeof(float), s), "memset");
         float* cur = d_x;
         for (int n = 0; n < nsteps; ++n) {
             for (int st = 0; st < 5; ++st) {

@@ -43,10 +43,16 @@ struct BatchedTables {
     float alpha;
 };
 
+// Classical RK4 in the batched form keeps the state register as an unevaluated sum of two FP32
+// words, x = x_hi + x_lo (the working state is [x_hi block | x_lo block]), and the register z as
+// the accumulated increment dt (k1/6 + k2/3 + k3/3) rather than x plus it. Stages read x_hi
+// only; the last stage adds the increment to (x_hi, x_lo) with an error-free two-sum, so the
+// state update itself does not round at FP32 precision every step.
 struct BatchedStageArgs {
     const float* in;
     float* out;
     float* x;
+    float* xl;               // x_lo (RK4 stage 4)
     float* yout;
     float* z;
     float* res;
@@ -57,6 +63,22 @@ struct BatchedStageArgs {
     const int* pw_off;       // [Bpad + 1]: sources of incidence b are pw[pw_off[b] .. pw_off[b+1])
     const int* skip;         // [Bpad]
 };
+
+#ifdef __CUDACC__
+// (hi, lo) += inc with an error-free two-sum (Knuth) and a renormalisation: hi + lo carries
+// the state to about 2^-48 relative, so the RK4 state update does not round each step.
+// Explicitly rounded additions, so that nothing is contracted into a fused multiply-add.
+__device__ __forceinline__ void add_compensated(float& hi, float& lo, float inc)
+{
+    const float s = __fadd_rn(hi, inc);
+    const float bb = __fsub_rn(s, hi);
+    const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(inc, bb));
+    const float l2 = __fadd_rn(lo, err);
+    const float h2 = __fadd_rn(s, l2);
+    lo = __fsub_rn(l2, __fsub_rn(h2, s));
+    hi = h2;
+}
+#endif
 
 // Tensor-core stage kernel (batched_tc.cu).
 bool tc_supported(int p, int Bpad);
@@ -70,13 +92,14 @@ public:
     ~BatchedOp();
     void set_sources(const std::vector<PlaneWaveDev>& pw);
     int64_t device_bytes() const { return device_bytes_; }
-    int64_t state_len() const { return state_len_; }       // floats of one internal state
+    int64_t state_len() const { return state_len_; }       // floats of one internal state (x_hi block)
+    int64_t work_len() const { return 2 * state_len_; }    // floats of the working state: x_hi and x_lo
     int64_t kernel_launches() const { return launches_; }
     int batch_padded() const { return Bpad_; }
     // internal (Morton) index of each reference element, host copy
     const std::vector<int32_t>& inv_perm() const { return inv_perm_host_; }
 
-    // reference layout (FP64, [b][c][e*Np+i]) <-> internal FP32
+    // reference layout (FP64, [b][c][e*Np+i]) <-> internal FP32 pair (x_hi = fl(x), x_lo = fl(x - x_hi))
     void pack(const double* d_ref, float* d_state, cudaStream_t s);
     void unpack(const float* d_state, double* d_ref, cudaStream_t s);
     void mult(const float* d_in, float* d_out, double t, cudaStream_t s);

@@ -22,7 +22,9 @@
 // two small correction products in a separate accumulator (column 320) that the
 // epilogue folds in with FP32 adds. Each MMA's accumulation truncates relative to the
 // accumulator it adds into, so keeping the corrections apart cuts that error 3x.
-// The epilogue applies 1/eps, 1/mu, the conductivity term and the RK stage update.
+// The epilogue applies 1/eps, 1/mu, the conductivity term and the RK stage update (classical
+// RK4 with the state register kept as an FP32 pair and a compensated last-stage update,
+// batched.hpp).
 //
 // One persistent CTA per SM, warp-specialised, no CTA-wide barrier in the
 // steady state (all hand-offs are mbarriers, every wait bounded):
@@ -198,6 +200,8 @@ __device__ __forceinline__ void prefetch_rk_registers(const BatchedStageArgs& A,
         prefetch_l2(A.z + e * EB, eb);
     } else if (MODE == MODE_RK4_4) {
         prefetch_l2(A.z + e * EB, eb);
+        prefetch_l2(A.x + e * EB, eb);
+        prefetch_l2(A.xl + e * EB, eb);
     } else if (MODE == MODE_LSRK) {
         prefetch_l2(A.res + e * EB, eb);
     }
@@ -206,24 +210,28 @@ __device__ __forceinline__ void prefetch_rk_registers(const BatchedStageArgs& A,
 // Epilogue operand loads of one chunk of kEpiNodes nodes (global, stride Bp between nodes).
 constexpr int kEpiNodes = 8;
 struct EpiOps {
-    float a[kEpiNodes];   // x (RK4_2/3) or res (LSRK)
+    float a[kEpiNodes];   // x_hi (RK4_2/3/4) or res (LSRK)
     float z[kEpiNodes];   // z (RK4_2/3/4)
     float u[kEpiNodes];   // stage input (RK4_1, LSRK, conductivity)
+    float l[kEpiNodes];   // x_lo (RK4_4)
 };
 
 template <int MODE>
 __device__ __forceinline__ void epi_load(const BatchedStageArgs& A, int64_t base, int Bp, int nv, bool need_u, EpiOps& o)
 {
-    constexpr bool need_a = (MODE == MODE_RK4_2 || MODE == MODE_RK4_3 || MODE == MODE_LSRK);
+    constexpr bool need_a = (MODE == MODE_RK4_2 || MODE == MODE_RK4_3 || MODE == MODE_RK4_4 || MODE == MODE_LSRK);
     constexpr bool need_z = (MODE == MODE_RK4_2 || MODE == MODE_RK4_3 || MODE == MODE_RK4_4);
+    constexpr bool need_l = (MODE == MODE_RK4_4);
     const float* __restrict__ px = (MODE == MODE_LSRK ? A.res : A.x) + base;
     const float* __restrict__ pz = A.z + base;
     const float* __restrict__ pu = A.in + base;
+    const float* __restrict__ pl = A.xl + base;
 #pragma unroll
     for (int j = 0; j < kEpiNodes; ++j) {
         if (j < nv) {
             if (need_a) o.a[j] = px[j * Bp];
             if (need_z) o.z[j] = pz[j * Bp];
+            if (need_l) o.l[j] = pl[j * Bp];
             if (need_u) o.u[j] = __ldg(pu + j * Bp);
         }
     }
@@ -244,7 +252,7 @@ __device__ __forceinline__ void epi_store(const BatchedStageArgs& A, int64_t bas
                 A.out[ix] = k;
             } else if (MODE == MODE_RK4_1) {
                 A.yout[ix] = uc + 0.5f * dtf * k;
-                A.z[ix] = uc + (dtf / 6.0f) * k;
+                A.z[ix] = (dtf / 6.0f) * k;
             } else if (MODE == MODE_RK4_2) {
                 A.yout[ix] = o.a[j] + 0.5f * dtf * k;
                 A.z[ix] = o.z[j] + (dtf / 3.0f) * k;
@@ -252,7 +260,10 @@ __device__ __forceinline__ void epi_store(const BatchedStageArgs& A, int64_t bas
                 A.yout[ix] = o.a[j] + dtf * k;
                 A.z[ix] = o.z[j] + (dtf / 3.0f) * k;
             } else if (MODE == MODE_RK4_4) {
-                A.x[ix] = o.z[j] + (dtf / 6.0f) * k;
+                float hi = o.a[j], lo = o.l[j];
+                add_compensated(hi, lo, o.z[j] + (dtf / 6.0f) * k);
+                A.x[ix] = hi;
+                A.xl[ix] = lo;
             } else {   // MODE_LSRK
                 const float rr = A.a * o.a[j] + dtf * k;
                 A.res[ix] = rr;

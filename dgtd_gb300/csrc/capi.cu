@@ -149,6 +149,23 @@ struct BatchedCount {
     ~BatchedCount() { g_launches.fetch_add(op->batched->kernel_launches() - before, std::memory_order_relaxed); }
 };
 
+// The reference-layout buffer of pack / unpack: device memory, or pinned host memory the device
+// can address (the conversion kernel then reads or writes it over the host link, so the
+// host-device transfer and the layout conversion are one pass). Anything else (pageable host
+// memory) is rejected before a kernel could touch it.
+const void* device_view(const void* p)
+{
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        throw std::invalid_argument("pack/unpack: cannot query the reference-layout buffer");
+    }
+    if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) return p;
+    if (a.type == cudaMemoryTypeHost && a.devicePointer != nullptr) return a.devicePointer;
+    throw std::invalid_argument("pack/unpack: the reference-layout buffer must be device memory or pinned host "
+                                "memory (pageable host memory is not addressable by the device)");
+}
+
 // Clears the instability record before a run (no check has tripped).
 void reset_stability(dgtd_op* op)
 {
@@ -485,7 +502,7 @@ int dgtd_op_get_info(const dgtd_op* op, dgtd_op_info* info)
     info->min_edge = op->mesh.min_edge;
     info->dt_scale_min = op->mesh.dt_scale_min;
     info->device_bytes = op->device_bytes + (op->batched ? op->batched->device_bytes() : 0);
-    info->work_len = op->batched ? op->batched->state_len() : op->state_len;
+    info->work_len = op->batched ? op->batched->work_len() : op->state_len;
     info->work_word_bytes = op->precision == DGTD_FP64 ? 8 : 4;
     info->batch_padded = op->batched ? static_cast<int32_t>(op->batched->state_len() / (op->mesh.K * 6 * op->ref.Np))
                                      : op->batch;
@@ -574,6 +591,7 @@ int dgtd_op_pack(dgtd_op* op, const double* d_ref, void* d_work, void* stream)
     if (!op || !d_ref || !d_work) return fail(DGTD_ERR_INVALID, "NULL argument");
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     try {
+        d_ref = static_cast<const double*>(device_view(d_ref));
         if (op->batched) {
             BatchedCount bc(op);
             op->batched->pack(d_ref, static_cast<float*>(d_work), s);
@@ -581,8 +599,10 @@ int dgtd_op_pack(dgtd_op* op, const double* d_ref, void* d_work, void* stream)
             ck(dgtd::launch_convert_f64_to_f32(d_ref, static_cast<float*>(d_work), op->state_len, s), "pack kernel");
             g_launches.fetch_add(1, std::memory_order_relaxed);
         } else if (static_cast<const void*>(d_ref) != d_work) {
-            ck(cudaMemcpyAsync(d_work, d_ref, op->state_len * sizeof(double), cudaMemcpyDeviceToDevice, s), "copy");
+            ck(cudaMemcpyAsync(d_work, d_ref, op->state_len * sizeof(double), cudaMemcpyDefault, s), "copy");
         }
+    } catch (const std::invalid_argument& e) {
+        return fail(DGTD_ERR_INVALID, e.what());
     } catch (const std::exception& e) {
         return fail(DGTD_ERR_CUDA, e.what());
     }
@@ -594,6 +614,7 @@ int dgtd_op_unpack(dgtd_op* op, const void* d_work, double* d_ref, void* stream)
     if (!op || !d_ref || !d_work) return fail(DGTD_ERR_INVALID, "NULL argument");
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     try {
+        d_ref = static_cast<double*>(const_cast<void*>(device_view(d_ref)));
         if (op->batched) {
             BatchedCount bc(op);
             op->batched->unpack(static_cast<const float*>(d_work), d_ref, s);
@@ -601,8 +622,10 @@ int dgtd_op_unpack(dgtd_op* op, const void* d_work, double* d_ref, void* stream)
             ck(dgtd::launch_convert_f32_to_f64(static_cast<const float*>(d_work), d_ref, op->state_len, s), "unpack kernel");
             g_launches.fetch_add(1, std::memory_order_relaxed);
         } else if (d_work != static_cast<const void*>(d_ref)) {
-            ck(cudaMemcpyAsync(d_ref, d_work, op->state_len * sizeof(double), cudaMemcpyDeviceToDevice, s), "copy");
+            ck(cudaMemcpyAsync(d_ref, d_work, op->state_len * sizeof(double), cudaMemcpyDefault, s), "copy");
         }
+    } catch (const std::invalid_argument& e) {
+        return fail(DGTD_ERR_INVALID, e.what());
     } catch (const std::exception& e) {
         return fail(DGTD_ERR_CUDA, e.what());
     }
@@ -621,7 +644,7 @@ int dgtd_op_mult_host(dgtd_op* op, const double* h_x, double* h_y, double t)
         ck(cudaMalloc(&dy, bytes), "cudaMalloc");
         ck(cudaMemcpy(dx, h_x, bytes, cudaMemcpyHostToDevice), "H2D");
         if (op->precision != DGTD_FP64) {
-            const size_t wb = (op->batched ? op->batched->state_len() : op->state_len) * sizeof(float);
+            const size_t wb = (op->batched ? op->batched->work_len() : op->state_len) * sizeof(float);
             ck(cudaMalloc(&wx, wb), "cudaMalloc");
             ck(cudaMalloc(&wy, wb), "cudaMalloc");
             rc = dgtd_op_pack(op, dx, wx, nullptr);
@@ -723,7 +746,7 @@ int dgtd_op_run_host(dgtd_op* op, double* h_state, double t0, double dt, double 
         ck(cudaMalloc(&d, bytes), "cudaMalloc");
         ck(cudaMemcpy(d, h_state, bytes, cudaMemcpyHostToDevice), "H2D");
         if (op->precision != DGTD_FP64) {
-            ck(cudaMalloc(&w, (op->batched ? op->batched->state_len() : op->state_len) * sizeof(float)), "cudaMalloc");
+            ck(cudaMalloc(&w, (op->batched ? op->batched->work_len() : op->state_len) * sizeof(float)), "cudaMalloc");
             rc = dgtd_op_pack(op, d, w, nullptr);
         } else {
             w = d;

@@ -107,7 +107,9 @@ typedef struct dgtd_op_info {
     int64_t device_bytes;   /* bytes of device tables held by the operator */
     int64_t work_len;       /* entries of the operator's working state (dgtd_op_step / dgtd_op_mult):
                                FP64 form: = state_len (reference layout);
-                               batched FP32 form: K*6*Np*Bpad floats, element-blocked, incidence fastest;
+                               batched FP32 form: 2*K*6*Np*Bpad floats: the x_hi block then the x_lo
+                               block (each element-blocked, incidence fastest; classical RK4 keeps the
+                               state as that FP32 pair, the other forms and stage inputs read x_hi);
                                single-instance FP32 form: = state_len floats (reference layout) */
     int32_t work_word_bytes;/* 8 (FP64 form) or 4 (FP32 forms) */
     int32_t batch_padded;   /* B rounded up to the incidence chunk (FP32 form), else B */
@@ -141,8 +143,12 @@ int dgtd_op_set_planewaves(dgtd_op* op, const dgtd_planewave* pw, int32_t n);
  * the reference layout for the FP64 form), must not alias. */
 int dgtd_op_mult(dgtd_op* op, const void* d_x, void* d_y, double t, void* stream);
 
-/* Convert between the reference layout (FP64, [b][c][e*Np+i], device) and the
- * operator's working state (device). Identity copy for the FP64 form. */
+/* Convert between the reference layout (FP64, [b][c][e*Np+i]) and the operator's working
+ * state (device). Identity copy for the FP64 form. d_ref may be device memory or pinned
+ * (page-locked) host memory: the conversion kernel then reads or writes the host buffer over
+ * the host link, fusing the transfer with the conversion. Pageable host memory is rejected
+ * with DGTD_ERR_INVALID. The batched form's working state holds each value as an FP32 pair
+ * (x_hi = fl(x), x_lo = fl(x - x_hi)), so pack/unpack keep about 48 bits of the FP64 value. */
 int dgtd_op_pack(dgtd_op* op, const double* d_ref, void* d_work, void* stream);
 int dgtd_op_unpack(dgtd_op* op, const void* d_work, double* d_ref, void* stream);
 

@@ -37,7 +37,8 @@ def test_pack_unpack_roundtrip(torch_cuda):
     m = dg.box_mesh((2, 2, 3))
     B = 5
     op = dg.Operator(m, order=3, precision=dg.FP32_3XTF32, batch=B)
-    assert op.info["batch_padded"] == 32 and op.work_len == 6 * m.n_elements * 20 * 32
+    # working state: the FP32 pair (x_hi, x_lo) of every value, incidences padded to 32
+    assert op.info["batch_padded"] == 32 and op.work_len == 2 * 6 * m.n_elements * 20 * 32
     x = RNG.standard_normal(op.state_len)
     xd = torch.from_numpy(x).cuda()
     w = op.new_work()
@@ -45,7 +46,19 @@ def test_pack_unpack_roundtrip(torch_cuda):
     back = torch.zeros_like(xd)
     op.unpack(w, back)
     torch.cuda.synchronize()
-    assert np.array_equal(back.cpu().numpy(), x.astype(np.float32).astype(np.float64))
+    hi = w[: op.work_len // 2].cpu().numpy()
+    assert np.abs(back.cpu().numpy() - x).max() <= 2.0 ** -46 * np.abs(x).max()
+    assert np.count_nonzero(hi) == x.size            # x_hi = fl(x) of the B real incidences, 0 in the padding
+    # pinned host memory is accepted as the reference-layout buffer (read / written over the host link)
+    hx = torch.from_numpy(x).pin_memory()
+    w2 = op.new_work()
+    op.pack(hx, w2)
+    hb = torch.zeros_like(hx).pin_memory()
+    op.unpack(w2, hb)
+    torch.cuda.synchronize()
+    assert torch.equal(w2, w) and np.array_equal(hb.numpy(), back.cpu().numpy())
+    with pytest.raises(dg.DgtdError, match="pinned host"):
+        op.pack(torch.from_numpy(x), w2)             # pageable host memory is refused
 
 
 @pytest.mark.parametrize("order", [1, 2, 3, 4, 5, 6])

@@ -25,8 +25,10 @@
 // per slot.
 //
 // One persistent CTA per SM, warp-specialised, all hand-offs through mbarriers with bounded waits:
-//   warps 0-7  producers: the item's whole B operand (volume then flux K-steps, hi and lo)
-//              into one of two B buffers, 16-byte stores (conflict-free in the K-major layout);
+//   warps 0-7  producers: stage the item's fields, face geometry and face codes in shared memory
+//              (coalesced loads), then build its whole B operand (volume then flux K-steps, hi
+//              and lo) into one of two B buffers, 16-byte stores (conflict-free in the K-major
+//              layout); only the neighbour traces of the flux come from global memory;
 //   warps 8-11 epilogue (one per TMEM lane quarter: thread = node), with the item's RK-register
 //              rows brought into L2 one item ahead;
 //   warp 12    tensor-memory owner and MMA issuer (one thread);
@@ -62,7 +64,7 @@ constexpr int kCopyWarp = 13;
 constexpr int kBStep = kNcol * 32;       // one K-step of B (48 rows x 8 tf32), one part: 1536 B
 constexpr int kATile = 128 * 32;         // one K-step of A (128 rows x 8 tf32), one part: 4 KB
 constexpr int kASlot = 2 * kATile;       // hi + lo
-constexpr int kNSlot = 6;                // A ring slots
+constexpr int kNSlot = 4;                // A ring slots
 constexpr uint32_t kAccCols = 4 * kNcol; // dr, ds, dt, lift: 192 columns per item
 constexpr uint32_t kAccStride = 256;     // TMEM columns between the two item accumulator sets
 constexpr uint32_t kTmemCols = 512;
@@ -79,7 +81,10 @@ struct Stc {
     static constexpr int NA = 3 * NKV + NKF;                 // A slots per item
     static constexpr int BPart = (NKV + NKF) * kBStep;      // one part (hi or lo) of an item's B
     static constexpr int BBuf = 2 * BPart;
-    static constexpr size_t smem = 2 * static_cast<size_t>(BBuf) + static_cast<size_t>(kNSlot) * kASlot;
+    static constexpr int FBuf = 6 * kG * Np * 4;              // the item's fields [c][e * Np + i]
+    static constexpr int TBuf = kG * (16 + 4) * 4;            // its face geometry and face codes
+    static constexpr size_t smem = 2 * static_cast<size_t>(BBuf) + static_cast<size_t>(kNSlot) * kASlot +
+                                   2 * static_cast<size_t>(FBuf + TBuf);
     static_assert(Np <= 128, "one M tile of nodes");
     static_assert(2 * kAccStride <= kTmemCols && kAccCols <= kAccStride, "tensor memory layout");
 };
@@ -132,21 +137,25 @@ __device__ __forceinline__ void store_b4(uint32_t bbase, int bpart, int ks, int 
 
 // Fscale/2-scaled upwind flux of the six components at face node a of face f of element e
 // (the reference's jumps, boundary rules and TF/SF source; same arithmetic as the SIMT stage).
+// The element's own fields, face geometry and face codes come from the item's staged copy in
+// shared memory (sf: [c][el * Np + i]; sg: [el][16]; sc: [el][4]); the neighbour traces from
+// global memory.
 template <int P>
 __device__ __forceinline__ void face_flux(const TablesF32& T, const StageArgsF32& A, const float* __restrict__ in,
+                                          const float* sf, const float* sg, const int* sc, const int* sfm, int el,
                                           int64_t e, int f, int a, int b, bool skip_src, float* out)
 {
     using O = Stc<P>;
     constexpr int Np = O::Np, Nfp = O::Nfp;
     const int64_t N = T.N;
-    const int vm = __ldg(T.Fmask + f * Nfp + a);
-    const int code = __ldg(T.fcode + e * 4 + f);
-    const float4 fg = __ldg(reinterpret_cast<const float4*>(T.fgeo + e * 16) + f);
+    const int vm = sfm[f * Nfp + a];
+    const int code = sc[el * 4 + f];
+    const float4 fg = reinterpret_cast<const float4*>(sg + el * 16)[f];
     const float nx = fg.x, ny = fg.y, nz = fg.z, fs = fg.w;
     const int64_t gm = e * Np + vm;
     float uM[6], dE[3], dH[3];
 #pragma unroll
-    for (int c = 0; c < 6; ++c) uM[c] = __ldg(in + c * N + gm);
+    for (int c = 0; c < 6; ++c) uM[c] = sf[c * (kG * Np) + el * Np + vm];
     float aE = T.alpha, aH = T.alpha;
     if (code == 0 || code == 4 || code == 5) {
         const int64_t gp = __ldg(T.vmapP + (e * 4 + f) * Nfp + a);
@@ -198,7 +207,10 @@ __global__ void __launch_bounds__(kThreads, 1)
     extern __shared__ __align__(128) unsigned char sm[];
     unsigned char* bbuf0 = sm;
     unsigned char* aring = sm + 2 * O::BBuf;
+    unsigned char* fbuf0 = aring + kNSlot * kASlot;             // [2] x (fields | face geometry | codes)
     __shared__ uint64_t bvol_full[2], bflux_full[2], b_empty[2], acc_full[2], acc_empty[2], geo_full[2];
+    __shared__ uint64_t f_full[2];
+    __shared__ int s_fmask[4 * Nfp];
     __shared__ uint64_t a_full[kNSlot], a_empty[kNSlot];
     __shared__ uint64_t drain_bar;
     __shared__ uint32_t tbase;
@@ -216,6 +228,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             tc::mbar_init(&acc_full[s], 1);
             tc::mbar_init(&acc_empty[s], kEpiThreads);
             tc::mbar_init(&geo_full[s], kEpiThreads);
+            tc::mbar_init(&f_full[s], kProducerThreads);
         }
         for (int s = 0; s < kNSlot; ++s) {
             tc::mbar_init(&a_full[s], 1);
@@ -225,6 +238,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         s_err = 0;
         tc::mbar_fence_init();
     }
+    for (int q = tid; q < 4 * Nfp; q += kThreads) s_fmask[q] = __ldg(T.Fmask + q);
     if (warp == kMmaWarp) {
         tc::tmem_alloc(&tbase, kTmemCols);
         tc::tmem_relinquish();
@@ -248,18 +262,37 @@ __global__ void __launch_bounds__(kThreads, 1)
             const uint32_t bb = tc::smem_u32(bbuf0 + buf * O::BBuf);
             if (use >= 1 && (flag_set(&s_err) || !tc::mbar_wait(&b_empty[buf], (use - 1) & 1))) { err = true; break; }
             const bool skip_src = (A.skip != nullptr) && A.skip[b];
+            // ---- stage the item's fields (6 contiguous runs of nel * Np values, coalesced loads),
+            // face geometry and face codes; the buffer of this parity was last read for item it - 2,
+            // which every producer finished before the MMA released its B buffer (b_empty above)
+            float* sf = reinterpret_cast<float*>(fbuf0 + buf * (O::FBuf + O::TBuf));
+            float* sgeo = sf + 6 * kG * Np;
+            int* scode = reinterpret_cast<int*>(sgeo + kG * 16);
+            for (int q = tid; q < 6 * kG * Np; q += kProducerThreads) {
+                const int c = q / (kG * Np), r = q - c * (kG * Np);
+                sf[q] = (r < nel * Np) ? __ldg(in + c * N + e0 * Np + r) : 0.0f;
+            }
+            for (int q = tid; q < kG * 20; q += kProducerThreads) {
+                if (q < kG * 16) sgeo[q] = (q / 16 < nel) ? __ldg(T.fgeo + e0 * 16 + q) : 0.0f;
+                else {
+                    const int r = q - kG * 16;
+                    scode[r] = (r / 4 < nel) ? __ldg(T.fcode + e0 * 4 + r) : 0;
+                }
+            }
+            tc::mbar_arrive(&f_full[buf]);
+            if (flag_set(&s_err) || !tc::mbar_wait(&f_full[buf], use & 1)) { err = true; break; }
             // ---- volume: B[(c, e), j] = F_c(e, j) - F_c(e, 0); task = (j quad, row n)
             for (int task = tid; task < (O::KV / 4) * kNcol; task += kProducerThreads) {
                 const int jq = task / kNcol, n = task - jq * kNcol;
                 const int c = n / kG, e = n - c * kG;
                 float v[4] = {0.0f, 0.0f, 0.0f, 0.0f};
                 if (e < nel) {
-                    const float* __restrict__ p = in + c * N + (e0 + e) * Np;
-                    const float f0 = __ldg(p);
+                    const float* p = sf + c * (kG * Np) + e * Np;
+                    const float f0 = p[0];
 #pragma unroll
                     for (int q = 0; q < 4; ++q) {
                         const int j = jq * 4 + q;
-                        if (j < Np) v[q] = __ldg(p + j) - f0;
+                        if (j < Np) v[q] = p[j] - f0;
                     }
                 }
                 store_b4(bb, O::BPart, jq >> 1, n, jq & 1, v);
@@ -276,7 +309,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                     float fl[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
                     if (e < nel && m < NF) {
                         const int f = m / Nfp, a = m - f * Nfp;
-                        face_flux<P>(T, A, in, e0 + e, f, a, b, skip_src, fl);
+                        face_flux<P>(T, A, in, sf, sgeo, scode, s_fmask, e, e0 + e, f, a, b, skip_src, fl);
                     }
 #pragma unroll
                     for (int c = 0; c < 6; ++c) v[c][q] = fl[c];

@@ -22,7 +22,7 @@
 // remainder; A_hi B_hi + A_lo B_hi + A_hi B_lo per K-step. The A operand (precomputed on the
 // host) is the same for every work item; it is streamed from global memory (L2-resident, a few
 // hundred KB) through a ring of shared-memory slots, one K-step of one matrix (hi and lo, 8 KB)
-// per slot.
+// per slot, as many slots as the order leaves room for.
 //
 // One persistent CTA per SM, warp-specialised, all hand-offs through mbarriers with bounded waits:
 //   warps 0-7  producers: stage the item's fields, face geometry and face codes in shared memory
@@ -64,7 +64,10 @@ constexpr int kCopyWarp = 13;
 constexpr int kBStep = kNcol * 32;       // one K-step of B (48 rows x 8 tf32), one part: 1536 B
 constexpr int kATile = 128 * 32;         // one K-step of A (128 rows x 8 tf32), one part: 4 KB
 constexpr int kASlot = 2 * kATile;       // hi + lo
-constexpr int kNSlot = 4;                // A ring slots
+constexpr int kMaxSlots = 16;            // A ring slots at most (the ring takes what shared memory is left)
+// Copies of the A image in global memory; CTA i streams copy i % kReplicas. Every CTA reads the
+// same slots at nearly the same time, and one copy makes those lines an L2 hot spot.
+constexpr int kReplicas = 16;
 constexpr uint32_t kAccCols = 4 * kNcol; // dr, ds, dt, lift: 192 columns per item
 constexpr uint32_t kAccStride = 256;     // TMEM columns between the two item accumulator sets
 constexpr uint32_t kTmemCols = 512;
@@ -83,8 +86,12 @@ struct Stc {
     static constexpr int BBuf = 2 * BPart;
     static constexpr int FBuf = 6 * kG * Np * 4;              // the item's fields [c][e * Np + i]
     static constexpr int TBuf = kG * (16 + 4) * 4;            // its face geometry and face codes
-    static constexpr size_t smem = 2 * static_cast<size_t>(BBuf) + static_cast<size_t>(kNSlot) * kASlot +
-                                   2 * static_cast<size_t>(FBuf + TBuf);
+    static constexpr int Fixed = 2 * BBuf + 2 * (FBuf + TBuf);
+    // A ring: as many 8 KB slots as fit in 223 KB of dynamic shared memory (4 at p = 6, 16 at p <= 4)
+    static constexpr int NSlot0 = (223 * 1024 - Fixed) / kASlot;
+    static constexpr int NSlot = NSlot0 > kMaxSlots ? kMaxSlots : NSlot0;
+    static constexpr size_t smem = static_cast<size_t>(Fixed) + static_cast<size_t>(NSlot) * kASlot;
+    static_assert(NSlot >= 2, "A ring");
     static_assert(Np <= 128, "one M tile of nodes");
     static_assert(2 * kAccStride <= kTmemCols && kAccCols <= kAccStride, "tensor memory layout");
 };
@@ -207,11 +214,12 @@ __global__ void __launch_bounds__(kThreads, 1)
     extern __shared__ __align__(128) unsigned char sm[];
     unsigned char* bbuf0 = sm;
     unsigned char* aring = sm + 2 * O::BBuf;
+    constexpr int kNSlot = O::NSlot;
     unsigned char* fbuf0 = aring + kNSlot * kASlot;             // [2] x (fields | face geometry | codes)
     __shared__ uint64_t bvol_full[2], bflux_full[2], b_empty[2], acc_full[2], acc_empty[2], geo_full[2];
     __shared__ uint64_t f_full[2];
     __shared__ int s_fmask[4 * Nfp];
-    __shared__ uint64_t a_full[kNSlot], a_empty[kNSlot];
+    __shared__ uint64_t a_full[kMaxSlots], a_empty[kMaxSlots];
     __shared__ uint64_t drain_bar;
     __shared__ uint32_t tbase;
     __shared__ int s_err;
@@ -346,6 +354,22 @@ __global__ void __launch_bounds__(kThreads, 1)
             }
         };
         if (etid == 0 && blockIdx.x < n_items) prefetch_item(blockIdx.x);
+        // the items' geometric factors and material scales, staged in shared memory for the 128
+        // threads: item it's into s_geo[it & 1] (one value per thread), loaded during item it - 1
+        auto factor = [&](int64_t w) -> float {
+            const int64_t pb = w / items_per_b;
+            const int64_t pe0 = (w - pb * items_per_b) * kG;
+            const int pnel = static_cast<int>(min(static_cast<int64_t>(kG), T.K - pe0));
+            if (etid < kG * 9) return (etid / 9 < pnel) ? __ldg(T.geo + pe0 * 9 + etid) : 0.0f;
+            const int q = etid - kG * 9;
+            if (q < kG * 3) return (q / 3 < pnel) ? __ldg(T.mat + pe0 * 3 + q) : 0.0f;
+            return 0.0f;
+        };
+        auto put_factor = [&](int bufi, float v) {
+            if (etid < kG * 9) s_geo[bufi][etid] = v;
+            else if (etid < kG * 12) s_mat[bufi][etid - kG * 9] = v;
+        };
+        if (blockIdx.x < n_items) put_factor(0, factor(blockIdx.x));
         int it = 0;
         for (int64_t w = blockIdx.x; w < n_items; w += gridDim.x, ++it) {
             const int abuf = it & 1;
@@ -353,39 +377,14 @@ __global__ void __launch_bounds__(kThreads, 1)
             const int64_t e0 = (w - b64 * items_per_b) * kG;
             const int nel = static_cast<int>(min(static_cast<int64_t>(kG), T.K - e0));
             if (etid == 0 && w + gridDim.x < n_items) prefetch_item(w + gridDim.x);
-            // the item's geometric factors and material scales, staged once for the 128 threads
-            float* sg = s_geo[abuf];
-            float* smt = s_mat[abuf];
-            if (etid < kG * 9) {
-                sg[etid] = (etid / 9 < nel) ? __ldg(T.geo + e0 * 9 + etid) : 0.0f;
-            } else if (etid < kG * 9 + kG * 3) {
-                const int q = etid - kG * 9;
-                smt[q] = (q / 3 < nel) ? __ldg(T.mat + e0 * 3 + q) : 0.0f;
-            }
             // hand-off among the 128 epilogue threads through an mbarrier with a bounded wait (a
             // thread that gave up on an earlier wait cannot leave the others blocked)
             tc::mbar_arrive(&geo_full[abuf]);
             if (flag_set(&s_err) || !tc::mbar_wait(&geo_full[abuf], (it >> 1) & 1)) { err = true; break; }
-            if (flag_set(&s_err) || !tc::mbar_wait(&acc_full[abuf], (it >> 1) & 1)) { err = true; break; }
-            tc::fence_after_sync();
-            const uint32_t tacc = tmem + abuf * kAccStride + (static_cast<uint32_t>(lq * 32) << 16);
-            // one target component at a time: its curl from the reference derivatives of the two
-            // source components ([c * kG + e] columns of the dr, ds, dt accumulators) and its lift
-            for (int ct = 0; ct < 6; ++ct) {
-                const int ax = ct % 3;                                 // target axis
-                const int a1 = (ax + 1) % 3, a2 = (ax + 2) % 3;       // curl_ax = d/d(a1) F_a2 - d/d(a2) F_a1
-                const int s1 = (ct < 3 ? 3 : 0) + a2;                  // E targets: curl H; H targets: -curl E
-                const int s2 = (ct < 3 ? 3 : 0) + a1;
-                float r1[kG], q1[kG], t1[kG], r2[kG], q2[kG], t2[kG], lf[kG];
-                tc::tmem_ld8(tacc + 0 * kNcol + s1 * kG, r1);
-                tc::tmem_ld8(tacc + 1 * kNcol + s1 * kG, q1);
-                tc::tmem_ld8(tacc + 2 * kNcol + s1 * kG, t1);
-                tc::tmem_ld8(tacc + 0 * kNcol + s2 * kG, r2);
-                tc::tmem_ld8(tacc + 1 * kNcol + s2 * kG, q2);
-                tc::tmem_ld8(tacc + 2 * kNcol + s2 * kG, t2);
-                tc::tmem_ld8(tacc + 3 * kNcol + ct * kG, lf);
-                // this target's RK-register operands of the 8 elements, all loads in flight together
-                float vx[kG], vz[kG], vu[kG];
+            const float* sg = s_geo[abuf];
+            const float* smt = s_mat[abuf];
+            // the RK-register operands of one target component for the 8 elements (all in flight)
+            auto load_ops = [&](int ct, float* vx, float* vz, float* vu) {
                 const int64_t base = b64 * 6 * N + ct * N + e0 * Np + i;
 #pragma unroll
                 for (int e = 0; e < kG; ++e) {
@@ -398,6 +397,41 @@ __global__ void __launch_bounds__(kThreads, 1)
                         if (kNeedU || (ct < 3 && smt[e * 3 + 2] != 0.0f)) vu[e] = __ldg(A.in + ix);
                     }
                 }
+            };
+            float ox[2][kG], oz[2][kG], ou[2][kG];
+            load_ops(0, ox[0], oz[0], ou[0]);      // in flight while the accumulator completes
+            const bool more = w + gridDim.x < n_items;
+            const float fnext = more ? factor(w + gridDim.x) : 0.0f;
+            if (flag_set(&s_err) || !tc::mbar_wait(&acc_full[abuf], (it >> 1) & 1)) { err = true; break; }
+            tc::fence_after_sync();
+            const uint32_t tacc = tmem + abuf * kAccStride + (static_cast<uint32_t>(lq * 32) << 16);
+            // one target component at a time: its curl from the reference derivatives of the two
+            // source components ([c * kG + e] columns of the dr, ds, dt accumulators) and its lift;
+            // the next target's operands are loaded before this one is computed and stored
+#pragma unroll
+            for (int ct = 0; ct < 6; ++ct) {
+                const int cur = ct & 1;
+                if (ct + 1 < 6) load_ops(ct + 1, ox[cur ^ 1], oz[cur ^ 1], ou[cur ^ 1]);
+                const int ax = ct % 3;                                 // target axis
+                const int a1 = (ax + 1) % 3, a2 = (ax + 2) % 3;       // curl_ax = d/d(a1) F_a2 - d/d(a2) F_a1
+                const int s1 = (ct < 3 ? 3 : 0) + a2;                  // E targets: curl H; H targets: -curl E
+                const int s2 = (ct < 3 ? 3 : 0) + a1;
+                // the curl in two passes over the accumulators, so that at most four 8-column
+                // loads are held at a time: d/d(a1) of s1 with the lift, then d/d(a2) of s2
+                float ra[kG], qa[kG], ta[kG], lf[kG], cu[kG];
+                tc::tmem_ld8(tacc + 0 * kNcol + s1 * kG, ra);
+                tc::tmem_ld8(tacc + 1 * kNcol + s1 * kG, qa);
+                tc::tmem_ld8(tacc + 2 * kNcol + s1 * kG, ta);
+                tc::tmem_ld8(tacc + 3 * kNcol + ct * kG, lf);
+                tc::tmem_ld_wait();
+#pragma unroll
+                for (int e = 0; e < kG; ++e) {
+                    const float* g = sg + e * 9;           // rx ry rz sx sy sz tx ty tz
+                    cu[e] = g[a1] * ra[e] + g[3 + a1] * qa[e] + g[6 + a1] * ta[e];
+                }
+                tc::tmem_ld8(tacc + 0 * kNcol + s2 * kG, ra);
+                tc::tmem_ld8(tacc + 1 * kNcol + s2 * kG, qa);
+                tc::tmem_ld8(tacc + 2 * kNcol + s2 * kG, ta);
                 tc::tmem_ld_wait();
                 if (ct == 5) {
                     tc::fence_before_sync();
@@ -405,13 +439,16 @@ __global__ void __launch_bounds__(kThreads, 1)
                 }
                 if (!active) continue;
                 const float sgn = ct < 3 ? 1.0f : -1.0f;
+                const int64_t base = b64 * 6 * N + ct * N + e0 * Np + i;
+                const float* vx = ox[cur];
+                const float* vz = oz[cur];
+                const float* vu = ou[cur];
 #pragma unroll
                 for (int e = 0; e < kG; ++e) {
                     if (e >= nel) break;
-                    const float* g = sg + e * 9;           // rx ry rz sx sy sz tx ty tz
-                    const float d1 = g[a1] * r1[e] + g[3 + a1] * q1[e] + g[6 + a1] * t1[e];
-                    const float d2 = g[a2] * r2[e] + g[3 + a2] * q2[e] + g[6 + a2] * t2[e];
-                    const float curl = d1 - d2;
+                    const float* g = sg + e * 9;
+                    const float d2 = g[a2] * ra[e] + g[3 + a2] * qa[e] + g[6 + a2] * ta[e];
+                    const float curl = cu[e] - d2;
                     const float uc = vu[e];
                     const float k = ct < 3 ? smt[e * 3] * (sgn * curl + lf[e]) - smt[e * 3 + 2] * uc
                                            : smt[e * 3 + 1] * (sgn * curl + lf[e]);
@@ -436,6 +473,9 @@ __global__ void __launch_bounds__(kThreads, 1)
                     }
                 }
             }
+            // the next item's factors into the other buffer: its last readers (item it - 1) have
+            // all passed this item's hand-off above
+            if (more) put_factor(abuf ^ 1, fnext);
         }
     } else if (warp == kMmaWarp) {
         // ================================================================ MMA issuer
@@ -492,6 +532,8 @@ __global__ void __launch_bounds__(kThreads, 1)
     } else if (warp == kCopyWarp) {
         // ================================================================ copy issuer (A slots)
         if (lane == 0) {
+            const unsigned char* a_mine = reinterpret_cast<const unsigned char*>(a_img) +
+                                          static_cast<size_t>(blockIdx.x % kReplicas) * NA * kASlot;
             int64_t g = 0;
             int64_t n_mine = 0;
             for (int64_t w = blockIdx.x; w < n_items; w += gridDim.x) ++n_mine;
@@ -505,8 +547,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                 }
                 const int t = static_cast<int>(g % NA);
                 mbar_expect_tx(&a_full[slot], kASlot);
-                bulk_g2s(aring + slot * kASlot, reinterpret_cast<const unsigned char*>(a_img) + static_cast<size_t>(t) * kASlot,
-                         kASlot, &a_full[slot]);
+                bulk_g2s(aring + slot * kASlot, a_mine + static_cast<size_t>(t) * kASlot, kASlot, &a_full[slot]);
             }
             if (err && g > 0) {
                 // wait (bounded) for this CTA's last copy in flight
@@ -591,6 +632,7 @@ bool tc1_supported(int p) { return p >= 1 && p <= 6; }
 // Host image of the A operand in the order the kernel consumes it: for every volume K-step q,
 // Dr, Ds, Dt (each one slot: the tf32 hi tile, then the lo tile, 128 rows x 8 columns K-major);
 // then every K-step of LIFT. Row i = node (zero for i >= Np), column k = source node or face node.
+// The image is repeated kReplicas times.
 std::vector<uint32_t> tc1_operator_image(const RefTet& ref)
 {
     const int Np = ref.Np, NF = 4 * ref.Nfp;
@@ -618,7 +660,9 @@ std::vector<uint32_t> tc1_operator_image(const RefTet& ref)
         put(t++, ref.Dt, Np, q);
     }
     for (int q = 0; q < NKF; ++q) put(t++, ref.LIFT, NF, q);
-    return img;
+    std::vector<uint32_t> all(img.size() * kReplicas);
+    for (int r = 0; r < kReplicas; ++r) std::copy(img.begin(), img.end(), all.begin() + r * img.size());
+    return all;
 }
 
 void launch_stage_tc1(const TablesF32& T, const StageArgsF32& A, const uint32_t* a_img, int* status, int n_sm,

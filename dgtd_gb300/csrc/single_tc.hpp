@@ -13,7 +13,8 @@
 namespace dgtd {
 
 bool tc1_supported(int p);
-// A-operand image (uint32 words, tf32 hi/lo tiles) of Dr, Ds, Dt and LIFT in consumption order.
+// A-operand image (uint32 words, tf32 hi/lo tiles) of Dr, Ds, Dt and LIFT in consumption order,
+// repeated so that groups of CTAs stream different copies.
 std::vector<uint32_t> tc1_operator_image(const RefTet& ref);
 // One stage (A.mode) over all incidences; status: device flag set to 1 when a bounded wait gave up.
 void launch_stage_tc1(const TablesF32& T, const StageArgsF32& A, const uint32_t* a_img, int* status, int n_sm,

@@ -84,9 +84,9 @@ WORKLOADS = {
         cells=(32, 32, 32), lo=(0, 0, 0), hi=(1, 1, 1), order=6, batch=1, dt=2e-4, precision="fp32s",
         outer_bc="PEC", init="fourier8", eps_seed=20261204, dtype="f32"),
     "dielectric_p6_fp32_small": dict(
-        desc="Profiling size of the high-order dielectric: 12^3 hexes x 6 tets (10,368), p=6, same fields; "
-             "single-instance FP32 form",
-        cells=(12, 12, 12), lo=(0, 0, 0), hi=(1, 1, 1), order=6, batch=1, dt=2e-4, precision="fp32s",
+        desc="Profiling size of the high-order dielectric: 20^3 hexes x 6 tets (48,000), p=6, same fields "
+             "(97 MB per FP32 state copy: a stage's registers exceed the 129 MB L2); single-instance FP32 form",
+        cells=(20, 20, 20), lo=(0, 0, 0), hi=(1, 1, 1), order=6, batch=1, dt=2e-4, precision="fp32s",
         outer_bc="PEC", init="fourier8", eps_seed=20261204, dtype="f32"),
     "cubic_resonator_fp64": dict(
         desc="3D PEC cubic resonator: unit cube 8^3 hexes x 6 tets (3,072), p=3 (Np=20), eps=mu=1, "
@@ -316,14 +316,15 @@ def time_steps(op, state, dt, t0, steps, stream, flush, dev):
     return [a.elapsed_time(b) for a, b in ev], t
 
 
-def accuracy_vs_fp64(w: dict, dev, contraction: int, dt: float) -> dict:
+def accuracy_vs_fp64(w: dict, dev, contraction: int, dt: float, defect: int = 0) -> dict:
     """Error of the timed FP32 kernel against the FP64 form over the configuration's full length.
 
     A reduced mesh (12^3 hexes instead of 24^3: same order, boundaries, sources and the timed
     run's dt, so the same 4,000 steps reach the same final time T = 9.9) is stepped by the FP32
     batched operator with the workload's 64 incidences and the timed run's contraction path,
     and by the FP64 form for the first `batch` incidences (same waves); the relative L2 of each
-    compared incidence is reported at checkpoints."""
+    compared incidence is reported at checkpoints. defect: the timed run's defect-correction
+    period (0: off)."""
     import torch
     import dgtd_gb300 as dg
     acc = w["accuracy"]
@@ -333,6 +334,8 @@ def accuracy_vs_fp64(w: dict, dev, contraction: int, dt: float) -> dict:
     op64 = make_op(wr, mesh, dg.FP64, B)
     op32 = make_op(wr, mesh, dg.FP32_3XTF32, w["batch"])
     op32.set_contraction(contraction)
+    if defect:
+        op32.set_defect_correction(defect)
     x64 = torch.zeros(op64.state_len, dtype=torch.float64, device=dev)
     x32 = torch.zeros(op32.state_len, dtype=torch.float64, device=dev)
     wk = op32.new_work(dev)
@@ -354,6 +357,7 @@ def accuracy_vs_fp64(w: dict, dev, contraction: int, dt: float) -> dict:
     return {"rel_l2_vs_fp64_max": points[-1]["rel_l2_max"], "steps": n, "t_end": n * dt, "dt": dt,
             "checkpoints": points, "incidences_compared": B, "fp32_batch": w["batch"],
             "fp32_kernel": "tensor cores (stage_tc)" if op32.uses_tensor_cores else "FP32 SIMT (stage_f32)",
+            "defect_correction_every": defect,
             "case": f"{acc['cells'][0]}^3 hexes x 6 tets, same order/sources/boundaries and the timed run's dt"}
 
 
@@ -383,22 +387,54 @@ def run_ours(args, world, rank, local):
             tune = op.autotune(state, stream=stream)
         else:
             op.set_contraction(0 if args.contraction == "tc" else 1)
+    elif prec == dg.FP32 and args.contraction != "auto":
+        op.set_contraction(0 if args.contraction == "tc" else 1)
     dofs = 6 * op.ndofs * w["batch"]
     flush = torch.empty(int(256 * 2 ** 20) // 4, dtype=torch.float32, device=dev)   # 256 MB > 129 MB L2
 
+    # FP64 defect correction (batched form): refreshed every `defect` steps. Timed segments start
+    # right after a refresh, and each adds the refreshes its length calls for beyond those that
+    # fell inside it (K / defect - refreshes inside, times the measured refresh time), so a
+    # segment shorter than the period still pays its share.
+    defect = args.defect_every if prec == dg.FP32_3XTF32 else 0
+    if defect:
+        op.set_defect_correction(defect)
+
     t = 0.0
-    for _ in range(args.warmup):
+    for i in range(args.warmup):
+        if defect and i == args.warmup - 1:
+            op.set_defect_correction(defect)        # refresh in the last warm-up step
         op.step(state, t, dt, 1, stream=stream); t += dt
     torch.cuda.synchronize(dev)
 
     n_launch0 = dg.kernel_launches()
+    r_timed0 = op.defect_refreshes if defect else 0
     barrier(world)
     torch.cuda.synchronize(dev)
     with ClockSampler(local) as clk:
         step_ms, t = time_steps(op, state, dt, t, args.steps, stream, flush, dev)
     barrier(world)
     launches = dg.kernel_launches() - n_launch0
-    total_s = max_over_ranks(sum(step_ms) / 1e3, world, dev)
+    defect_info = None
+    timed_s = sum(step_ms) / 1e3
+    if defect:
+        r_in = op.defect_refreshes - r_timed0
+        # one refresh timed alone: a step that refreshes minus a step that does not (L2 flushed before each)
+        evs = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        flush.zero_()
+        op.set_defect_correction(defect)
+        evs[0].record(stream); op.step(state, t, dt, 1, stream=stream); evs[1].record(stream); t += dt
+        flush.zero_()
+        evs[2].record(stream); op.step(state, t, dt, 1, stream=stream); evs[3].record(stream); t += dt
+        torch.cuda.synchronize(dev)
+        refresh_s = max(0.0, (evs[0].elapsed_time(evs[1]) - evs[2].elapsed_time(evs[3])) / 1e3)
+        extra_s = max(0.0, args.steps / defect - r_in) * refresh_s
+        defect_info = {"every": defect, "refresh_ms": refresh_s * 1e3, "refreshes_in_timed_region": r_in,
+                       "added_ms": extra_s * 1e3, "amortised_ms_per_step": refresh_s * 1e3 / defect,
+                       "note": "FP64 operator correction (dgtd_op_set_defect_correction): value includes "
+                               "max(0, steps/every - refreshes inside) refreshes at the measured refresh time"}
+        timed_s += extra_s
+    total_s = max_over_ranks(timed_s, world, dev)
     value = world * dofs * args.steps / total_s
     ms_per_step = total_s * 1e3 / args.steps
     if not bool(torch.isfinite(state).all()):
@@ -423,6 +459,11 @@ def run_ours(args, world, rank, local):
         layout conversion in one pass over the host link); else cudaMemcpy H2D / D2H into a device
         reference-layout buffer around device-side pack / unpack."""
         t_ = t
+        if defect:                                   # start right after a refresh (untimed step)
+            op.set_defect_correction(defect)
+            op.step(state, t_, dt, 1, stream=stream)
+            t_ += dt
+        r0 = op.defect_refreshes if defect else 0
         e_start, e_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         n0 = dg.kernel_launches()
         torch.cuda.synchronize(dev)
@@ -447,7 +488,10 @@ def run_ours(args, world, rank, local):
                 t_ += dt
         e_end.record(stream)
         torch.cuda.synchronize(dev)
-        return max_over_ranks(e_start.elapsed_time(e_end) / 1e3, world, dev), dg.kernel_launches() - n0
+        sec = e_start.elapsed_time(e_end) / 1e3
+        if defect:
+            sec += max(0.0, e2e_steps / defect - (op.defect_refreshes - r0)) * defect_info["refresh_ms"] / 1e3
+        return max_over_ranks(sec, world, dev), dg.kernel_launches() - n0
 
     variants = {"copy_engine": e2e_chain(False)}
     if prec != dg.FP64:
@@ -470,8 +514,10 @@ def run_ours(args, world, rank, local):
            "d2h_bytes_per_step": ref_bytes, "steps": e2e_steps, "ms_per_step": e2e_s * 1e3 / e2e_steps,
            "gpu_launches": e2e_launches, "path": paths[best] + " (a dependent chain: nothing overlaps across steps)",
            "variants_ms_per_step": {v: variants[v][0] * 1e3 / e2e_steps for v in variants}}
-    t += e2e_steps * dt * len(variants)
+    t += (e2e_steps + (1 if defect else 0)) * dt * len(variants)
     del host, ref_dev
+    if defect:
+        op.set_defect_correction(0)       # the streaming leg steps independent states
 
     # --- streaming variant: independent jobs of the private working layout, pipelined (step k+1's
     # upload and step k-1's download on their own streams under step k's compute, three device
@@ -512,7 +558,8 @@ def run_ours(args, world, rank, local):
     work_bytes = int(host.numel() * host.element_size())
     e2e_streaming = {"value": world * dofs * e2e_steps / st_s, "unit": UNIT, "h2d_bytes_per_step": work_bytes,
                      "d2h_bytes_per_step": work_bytes, "steps": e2e_steps,
-                     "path": "independent states in the working layout, pinned host buffers, uploads/downloads "
+                     "path": "independent states in the working layout (no defect correction: every step is "
+                             "another state), pinned host buffers, uploads/downloads "
                              "pipelined under the previous/next step's compute"}
     del dbufs, host, out
 
@@ -523,8 +570,9 @@ def run_ours(args, world, rank, local):
     word = 8 if prec == dg.FP64 else 4
     K, Np, nfp = op.info["n_elements"], op.info["np"], op.info["nfp"]
     # algorithmic bytes per DOF per RK4 step: 16 words over the 4 stages (x, y, z registers: 3+5+5+3);
-    # the batched form's compensated update adds 3 (stage 4 reads x_hi, x_lo and writes x_lo)
-    words = 19 if prec == dg.FP32_3XTF32 else 16
+    # the batched form's compensated update adds 3 (stage 4 reads x_hi, x_lo and writes x_lo), and
+    # the defect correction 2 (a bf16 read in each of the 4 stages)
+    words = (19 + (2 if defect else 0)) if prec == dg.FP32_3XTF32 else 16
     alg_bytes_launch = words * word * dofs / stage_launches
     achieved_gbs = alg_bytes_launch / avg_launch_s / 1e9
     flops_per_dof_step = 4 * (6 * Np + 8 * nfp)          # contraction terms, FMA = 2
@@ -532,7 +580,7 @@ def run_ours(args, world, rank, local):
     if prec == dg.FP64:
         kname = "stage_fp64"
     elif prec == dg.FP32:
-        kname = "stage_f32s"
+        kname = "stage_tc1" if op.uses_tensor_cores else "stage_f32s"
     else:
         kname = "stage_tc" if op.uses_tensor_cores else "stage_f32"
     traffic = profile_traffic(kname, args.workload)
@@ -550,6 +598,7 @@ def run_ours(args, world, rank, local):
                                  "frac_of_nominal": round(achieved_tflops / 1.25, 4),
                                  "note": "plain FP64 form is FP64-issue bound; nominal GB300 FP64 peak, not measured"}
     res = dict(value=value, ms_per_step=ms_per_step, e2e=e2e, e2e_streaming=e2e_streaming, tune=tune,
+               defect=defect_info,
                launches=launches, uses_tc=bool(getattr(op, "uses_tensor_cores", False)), clocks=clk.summary(), roofline=roofline,
                setup_s=setup_s, w=w, dofs=dofs, K=K, Np=Np, dt=dt)
     del state, op
@@ -567,7 +616,7 @@ def run_ours(args, world, rank, local):
         del s64, op64
         torch.cuda.empty_cache()
         if w.get("accuracy") and not args.no_accuracy:
-            res["accuracy"] = accuracy_vs_fp64(w, dev, 0 if res["uses_tc"] else 1, dt)
+            res["accuracy"] = accuracy_vs_fp64(w, dev, 0 if res["uses_tc"] else 1, dt, defect)
     return res
 
 
@@ -814,8 +863,11 @@ def main():
                          "(capacity)")
     ap.add_argument("--serving-serial", type=int, default=6, help="requests also run one at a time for comparison")
     ap.add_argument("--serving-precision", choices=["fp32", "fp64"], default="fp32")
+    ap.add_argument("--defect-every", type=int, default=250,
+                    help="batched form: refresh period (steps) of the FP64 defect correction (0: off)")
     ap.add_argument("--contraction", choices=["auto", "tc", "simt"], default="auto",
-                    help="batched form: autotuned stage kernel (default), or force tensor cores / FP32 SIMT")
+                    help="batched form: autotuned stage kernel (default), or force tensor cores / FP32 SIMT; "
+                         "single-instance FP32 form: the library default (auto), tensor cores or FP32 SIMT")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -862,6 +914,8 @@ def main():
         line["stage_kernel"] = {"choice": r["tune"]["kernel"], "ms_per_launch": r["tune"]["ms_per_launch"]}
     if r.get("e2e_streaming"):
         line["e2e_streaming"] = r["e2e_streaming"]
+    if r.get("defect"):
+        line["defect_correction"] = r["defect"]
     if "plain_fp64" in r:
         line["plain_fp64"] = r["plain_fp64"]
     if "accuracy" in r:

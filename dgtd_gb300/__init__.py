@@ -153,6 +153,8 @@ SIGNATURES = {
     "dgtd_op_set_contraction": (C.c_int, [_P, C.c_int32]),
     "dgtd_op_uses_tensor_cores": (C.c_int, [_P]),
     "dgtd_op_set_graph_steps": (C.c_int, [_P, C.c_int32]),
+    "dgtd_op_set_defect_correction": (C.c_int, [_P, C.c_int32]),
+    "dgtd_op_defect_refreshes": (C.c_int, [_P, C.POINTER(C.c_int64)]),
     "dgtd_op_autotune": (C.c_int, [_P, _P, _P, _D, _I32]),
     "dgtd_op_check": (C.c_int, [_P, _P]),
     "dgtd_op_estimate_dt": (C.c_int, [_P, C.c_double, _D]),
@@ -469,6 +471,17 @@ class Operator:
     def set_graph_steps(self, steps: int) -> None:
         """Batched FP32 form: replay blocks of `steps` RK4 steps from one captured CUDA graph (0: off)."""
         _check(lib().dgtd_op_set_graph_steps(self._h, int(steps)), "dgtd_op_set_graph_steps")
+
+    def set_defect_correction(self, every: int) -> None:
+        """Batched FP32 form: refresh an FP64 correction of the operator every `every` steps and
+        add it to every RK stage's right-hand side (0: off)."""
+        _check(lib().dgtd_op_set_defect_correction(self._h, int(every)), "dgtd_op_set_defect_correction")
+
+    @property
+    def defect_refreshes(self) -> int:
+        n = C.c_int64()
+        _check(lib().dgtd_op_defect_refreshes(self._h, C.byref(n)), "dgtd_op_defect_refreshes")
+        return int(n.value)
 
     @property
     def uses_tensor_cores(self) -> bool:

@@ -16,6 +16,8 @@
 #include <stdexcept>
 #include <string>
 
+#include <cuda_bf16.h>
+
 #include "batched.hpp"
 
 namespace dgtd {
@@ -189,6 +191,10 @@ __global__ void __launch_bounds__(kWarps * kLanes) stage_f32(BatchedTables T, Ba
             k[4] = im * (-(dz(0) - dx(2)) + lf[4]);
             k[5] = im * (-(dx(1) - dy(0)) + lf[5]);
             const float dt = A.dt;
+            if (A.corr) {
+#pragma unroll
+                for (int c = 0; c < 6; ++c) k[c] += bf16_bits_to_float(A.corr[((e * 6 + c) * Np + i) * Bp + col]);
+            }
 #pragma unroll
             for (int c = 0; c < 6; ++c) {
                 const int64_t idx = ((e * 6 + c) * Np + i) * Bp + col;
@@ -266,72 +272,84 @@ __global__ void __launch_bounds__(256) tfsf_skip_f32(BatchedTables T, const Plan
 }
 
 // reference [b][c][e*Np+i] (FP64) -> internal [e'][c][i][b] as the FP32 pair (x_hi | x_lo blocks).
-// One block transposes one (element, component, chunk of 64 incidences) tile through shared memory:
-// it reads the reference rows (Np consecutive values per incidence) and writes the internal rows
-// (64 consecutive incidences per node), both as contiguous runs, so the copy also streams well when
-// the reference state is pinned host memory read over the host link.
+// One block transposes one tile of E consecutive reference elements x one component x 64
+// incidences through shared memory (rows padded to 65 floats, conflict-free both ways): it reads
+// the reference rows (E * Np contiguous values per incidence) and writes each element's internal
+// rows (64 contiguous incidences per node). Both sides are long contiguous runs, which is also
+// what lets the kernel stream a pinned host vector over the host link.
 constexpr int kPackChunk = 64;
+constexpr int kPackRow = kPackChunk + 1;
+
+// elements per tile: as many as keep the tile (hi and lo) within 48 KB of shared memory, 1..8,
+// so that 4-6 blocks (32-48 warps) share an SM and keep enough loads in flight
+inline int pack_tile_elements(int Np) { return std::max(1, std::min(8, (48 * 1024) / (Np * kPackRow * 8))); }
 
 __global__ void __launch_bounds__(256) pack_kernel(const double* __restrict__ ref, float* __restrict__ st,
-                                                   const int32_t* __restrict__ perm, int64_t K, int Np, int B, int Bp)
+                                                   const int32_t* __restrict__ inv_perm, int64_t K, int Np, int B,
+                                                   int Bp, int E)
 {
-    extern __shared__ float tile[];                 // [2][Np][kPackChunk]
-    const int64_t r = blockIdx.x;                   // element * 6 + component (internal order)
-    const int64_t ei = r / 6;
-    const int c = static_cast<int>(r - ei * 6);
-    const int b0 = blockIdx.y * kPackChunk;
+    extern __shared__ float tile[];                 // [2][E * Np][kPackRow]
+    const int64_t er0 = static_cast<int64_t>(blockIdx.x) * E;
+    const int c = blockIdx.y;
+    const int b0 = blockIdx.z * kPackChunk;
+    const int ne = static_cast<int>(min(static_cast<int64_t>(E), K - er0));
     const int64_t N = K * Np;
-    const int64_t er = perm[ei];
-    const int n = Np * kPackChunk;
-    for (int q = threadIdx.x; q < n; q += blockDim.x) {
-        const int bb = q / Np, i = q - bb * Np;
+    const int rows = ne * Np;                       // tile rows of this block: (element, node)
+    const int half = E * Np * kPackRow;
+    for (int q = threadIdx.x; q < kPackChunk * rows; q += blockDim.x) {
+        const int bb = q / rows, r = q - bb * rows;
         const int b = b0 + bb;
         float hi = 0.0f, lo = 0.0f;
         if (b < B) {
-            const double v = ref[(static_cast<int64_t>(b) * 6 + c) * N + er * Np + i];
+            const double v = ref[(static_cast<int64_t>(b) * 6 + c) * N + er0 * Np + r];
             hi = static_cast<float>(v);
             lo = static_cast<float>(v - static_cast<double>(hi));
         }
-        tile[i * kPackChunk + bb] = hi;
-        tile[n + i * kPackChunk + bb] = lo;
+        tile[r * kPackRow + bb] = hi;
+        tile[half + r * kPackRow + bb] = lo;
     }
     __syncthreads();
     const int64_t L = K * 6 * static_cast<int64_t>(Np) * Bp;   // x_lo block offset
-    for (int q = threadIdx.x; q < n; q += blockDim.x) {
-        const int i = q / kPackChunk, bb = q - i * kPackChunk;
+    for (int q = threadIdx.x; q < kPackChunk * rows; q += blockDim.x) {
+        const int r = q / kPackChunk, bb = q - r * kPackChunk;
         if (b0 + bb >= Bp) continue;                 // Bpad = 32: half a chunk
-        const int64_t o = (r * Np + i) * Bp + b0 + bb;
-        st[o] = tile[q];
-        st[L + o] = tile[n + q];
+        const int el = r / Np, i = r - el * Np;
+        const int64_t ei = inv_perm[er0 + el];
+        const int64_t o = ((ei * 6 + c) * Np + i) * Bp + b0 + bb;
+        st[o] = tile[r * kPackRow + bb];
+        st[L + o] = tile[half + r * kPackRow + bb];
     }
 }
 
 __global__ void __launch_bounds__(256) unpack_kernel(const float* __restrict__ st, double* __restrict__ ref,
-                                                     const int32_t* __restrict__ perm, int64_t K, int Np, int B, int Bp)
+                                                     const int32_t* __restrict__ inv_perm, int64_t K, int Np, int B,
+                                                     int Bp, int E)
 {
-    extern __shared__ float tile[];                 // [2][Np][kPackChunk]
-    const int64_t r = blockIdx.x;
-    const int64_t ei = r / 6;
-    const int c = static_cast<int>(r - ei * 6);
-    const int b0 = blockIdx.y * kPackChunk;
+    extern __shared__ float tile[];                 // [2][E * Np][kPackRow]
+    const int64_t er0 = static_cast<int64_t>(blockIdx.x) * E;
+    const int c = blockIdx.y;
+    const int b0 = blockIdx.z * kPackChunk;
+    const int ne = static_cast<int>(min(static_cast<int64_t>(E), K - er0));
     const int64_t N = K * Np;
-    const int64_t er = perm[ei];
-    const int n = Np * kPackChunk;
+    const int rows = ne * Np;
+    const int half = E * Np * kPackRow;
     const int64_t L = K * 6 * static_cast<int64_t>(Np) * Bp;
-    for (int q = threadIdx.x; q < n; q += blockDim.x) {
-        const int i = q / kPackChunk, bb = q - i * kPackChunk;
-        if (b0 + bb >= Bp) continue;                 // Bpad = 32: half a chunk (never read back)
-        const int64_t o = (r * Np + i) * Bp + b0 + bb;
-        tile[q] = st[o];
-        tile[n + q] = st[L + o];
+    for (int q = threadIdx.x; q < kPackChunk * rows; q += blockDim.x) {
+        const int r = q / kPackChunk, bb = q - r * kPackChunk;
+        if (b0 + bb >= Bp) continue;                 // Bpad = 32: half a chunk (never written back)
+        const int el = r / Np, i = r - el * Np;
+        const int64_t ei = inv_perm[er0 + el];
+        const int64_t o = ((ei * 6 + c) * Np + i) * Bp + b0 + bb;
+        tile[r * kPackRow + bb] = st[o];
+        tile[half + r * kPackRow + bb] = st[L + o];
     }
     __syncthreads();
-    for (int q = threadIdx.x; q < n; q += blockDim.x) {
-        const int bb = q / Np, i = q - bb * Np;
+    for (int q = threadIdx.x; q < kPackChunk * rows; q += blockDim.x) {
+        const int bb = q / rows, r = q - bb * rows;
         const int b = b0 + bb;
         if (b < B)
-            ref[(static_cast<int64_t>(b) * 6 + c) * N + er * Np + i] =
-                static_cast<double>(tile[i * kPackChunk + bb]) + static_cast<double>(tile[n + i * kPackChunk + bb]);
+            ref[(static_cast<int64_t>(b) * 6 + c) * N + er0 * Np + r] =
+                static_cast<double>(tile[r * kPackRow + bb]) + static_cast<double>(tile[half + r * kPackRow + bb]);
     }
 }
 
@@ -513,7 +531,7 @@ std::unique_ptr<BatchedOp> BatchedOp::create(const RefTet& ref, const MeshTables
     T.geo = up(geo); T.fgeo = up(fgeo); T.mat = up(mat);
     T.vmapP = up(vmapP); T.fcode = up(fcode); T.fxyz = up(fxyz); T.fbc = up(fbc);
     T.nxyz = up(nxyz); T.n_tfsf_nodes = nt;
-    op->perm_ = const_cast<int32_t*>(up(perm));
+    op->inv_perm_ = const_cast<int32_t*>(up(inv));
     op->op_img_ = up(tc_operator_image(ref));
     ckb(cudaMalloc(&op->status_, sizeof(int)), "cudaMalloc status");
     op->allocs_.push_back(op->status_);
@@ -572,6 +590,7 @@ void BatchedOp::set_sources(const std::vector<PlaneWaveDev>& pw)
 void BatchedOp::stage(BatchedStageArgs A, double t, cudaStream_t s)
 {
     if (A.t_base == nullptr) A.t = static_cast<float>(t);   // else t is the offset set by the caller
+    A.corr = (A.mode == MODE_MULT) ? nullptr : corr_;
     if (has_tfsf_ && n_pw_ > 0) {
         tfsf_skip_f32<<<dim3(Bpad_, kSkipParts), 256, 0, s>>>(T_, pw_dev_, pw_off_, A.t, A.t_base, skip_partial_,
                                                              skip_ticket_, skip_);
@@ -615,20 +634,38 @@ void BatchedOp::ensure_ws()
 
 void BatchedOp::pack(const double* d_ref, float* d_state, cudaStream_t s)
 {
-    // Bpad is a multiple of 32; a last chunk of 32 padded incidences is handled as b >= B. At most
-    // 2 x 84 x 64 floats (43 KB) of shared memory: within the default limit.
-    const dim3 grid(static_cast<unsigned>(K_ * 6), static_cast<unsigned>((Bpad_ + kPackChunk - 1) / kPackChunk));
-    const size_t smem = 2 * static_cast<size_t>(Np_) * kPackChunk * sizeof(float);
-    pack_kernel<<<grid, 256, smem, s>>>(d_ref, d_state, perm_, K_, Np_, B_, Bpad_);
+    // grid: tiles of E reference elements x 6 components x chunks of 64 incidences (Bpad is a
+    // multiple of 32; a last chunk of 32 padded incidences is handled as b >= B)
+    const int E = pack_tile_elements(Np_);
+    const dim3 grid(static_cast<unsigned>((K_ + E - 1) / E), 6u,
+                    static_cast<unsigned>((Bpad_ + kPackChunk - 1) / kPackChunk));
+    const size_t smem = 2 * static_cast<size_t>(E) * Np_ * kPackRow * sizeof(float);
+    static std::atomic<uint64_t> seen{0};
+    if (first_use_on_device(seen)) {
+        ckb(cudaFuncSetAttribute(pack_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024),
+            "pack smem attribute");
+        ckb(cudaFuncSetAttribute(unpack_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024),
+            "unpack smem attribute");
+    }
+    pack_kernel<<<grid, 256, smem, s>>>(d_ref, d_state, inv_perm_, K_, Np_, B_, Bpad_, E);
     ckb(cudaGetLastError(), "pack kernel");
     ++launches_;
 }
 
 void BatchedOp::unpack(const float* d_state, double* d_ref, cudaStream_t s)
 {
-    const dim3 grid(static_cast<unsigned>(K_ * 6), static_cast<unsigned>((Bpad_ + kPackChunk - 1) / kPackChunk));
-    const size_t smem = 2 * static_cast<size_t>(Np_) * kPackChunk * sizeof(float);
-    unpack_kernel<<<grid, 256, smem, s>>>(d_state, d_ref, perm_, K_, Np_, B_, Bpad_);
+    const int E = pack_tile_elements(Np_);
+    const dim3 grid(static_cast<unsigned>((K_ + E - 1) / E), 6u,
+                    static_cast<unsigned>((Bpad_ + kPackChunk - 1) / kPackChunk));
+    const size_t smem = 2 * static_cast<size_t>(E) * Np_ * kPackRow * sizeof(float);
+    static std::atomic<uint64_t> seen{0};
+    if (first_use_on_device(seen)) {
+        ckb(cudaFuncSetAttribute(pack_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024),
+            "pack smem attribute");
+        ckb(cudaFuncSetAttribute(unpack_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024),
+            "unpack smem attribute");
+    }
+    unpack_kernel<<<grid, 256, smem, s>>>(d_state, d_ref, inv_perm_, K_, Np_, B_, Bpad_, E);
     ckb(cudaGetLastError(), "unpack kernel");
     ++launches_;
 }
@@ -640,6 +677,33 @@ void BatchedOp::mult(const float* d_in, float* d_out, double t, cudaStream_t s)
     stage(A, t, s);
     // d_out is a working state: its x_lo word is zero (the product is an FP32 value)
     ckb(cudaMemsetAsync(d_out + state_len_, 0, state_len_ * sizeof(float), s), "memset");
+}
+
+// corr[i] = bf16((ref[i] - l32[i]) + ref[L + i]) over one state block: the FP64 operator's
+// product (held as a pair) minus this form's product of the same state. The two products agree
+// to about FP32 precision, so the difference is exact and its bf16 rounding (2^-9 relative)
+// only scales the correction, which is itself at the FP32 rounding level of the product.
+__global__ void __launch_bounds__(256) correction_kernel(const float* __restrict__ ref, const float* __restrict__ l32,
+                                                       uint16_t* __restrict__ corr, int64_t L)
+{
+    for (int64_t i = blockIdx.x * 256ll + threadIdx.x; i < L; i += static_cast<int64_t>(gridDim.x) * 256) {
+        const float d = (ref[i] - l32[i]) + ref[L + i];
+        corr[i] = __bfloat16_as_ushort(__float2bfloat16_rn(d));
+    }
+}
+
+void BatchedOp::set_correction(const uint16_t* corr)
+{
+    corr_ = corr;
+}
+
+void BatchedOp::build_correction(const float* ref_pair, const float* l32, uint16_t* corr, cudaStream_t s)
+{
+    const int64_t want = (state_len_ + 2047) / 2048;
+    const unsigned grid = static_cast<unsigned>(std::max<int64_t>(1, std::min<int64_t>(want, 8ll * n_sm_)));
+    correction_kernel<<<grid, 256, 0, s>>>(ref_pair, l32, corr, state_len_);
+    ckb(cudaGetLastError(), "correction kernel");
+    ++launches_;
 }
 
 void BatchedOp::rk4_steps_direct(float* d_x, double t, double dt, int nsteps, cudaStream_t s)
@@ -685,7 +749,9 @@ void BatchedOp::step(float* d_x, double t0, double dt, int nsteps, int integrato
         // blocks of G steps replayed from one captured graph (not on the legacy default stream,
         // which cannot be captured); the stage times are offsets from the device scalar t_dev_
         if (G > 0 && s != nullptr && nsteps >= G) {
-            if (gexec_ && (g_x_ != d_x || g_dt_ != dt || g_stream_ != s || g_contraction_ != contraction_)) drop_graph();
+            if (gexec_ && (g_x_ != d_x || g_dt_ != dt || g_stream_ != s || g_contraction_ != contraction_ ||
+                           g_corr_ != corr_))
+                drop_graph();
             if (!gexec_) {
                 if (!t_dev_) ckb(cudaMalloc(&t_dev_, sizeof(double)), "cudaMalloc graph time");
                 // one direct step first so that every kernel attribute is set outside the capture
@@ -713,7 +779,7 @@ void BatchedOp::step(float* d_x, double t0, double dt, int nsteps, int integrato
                 if (ce != cudaSuccess) { gexec_ = nullptr; throw std::runtime_error(std::string("graph instantiate: ") + cudaGetErrorString(ce)); }
                 g_graph_launches_ = launches_ - before + 1;
                 launches_ = before;
-                g_x_ = d_x; g_dt_ = dt; g_stream_ = s; g_contraction_ = contraction_;
+                g_x_ = d_x; g_dt_ = dt; g_stream_ = s; g_contraction_ = contraction_; g_corr_ = corr_;
             }
             set_time<<<1, 1, 0, s>>>(t_dev_, t);
             ckb(cudaGetLastError(), "set time");

@@ -62,6 +62,8 @@ struct BatchedStageArgs {
     const PlaneWaveF32* pw;  // sources sorted by incidence
     const int* pw_off;       // [Bpad + 1]: sources of incidence b are pw[pw_off[b] .. pw_off[b+1])
     const int* skip;         // [Bpad]
+    const uint16_t* corr;    // operator correction added to every right-hand side (bf16 bits, internal
+                             // layout of one state block), or nullptr; never set for MODE_MULT
 };
 
 #ifdef __CUDACC__
@@ -78,6 +80,9 @@ __device__ __forceinline__ void add_compensated(float& hi, float& lo, float inc)
     lo = __fsub_rn(l2, __fsub_rn(h2, s));
     hi = h2;
 }
+
+// bf16 bits -> FP32 (exact)
+__device__ __forceinline__ float bf16_bits_to_float(uint16_t h) { return __uint_as_float(static_cast<uint32_t>(h) << 16); }
 #endif
 
 // Tensor-core stage kernel (batched_tc.cu).
@@ -117,6 +122,12 @@ public:
     bool uses_tensor_cores() const { return contraction_ == 0 && tc_supported(T_.p, Bpad_); }
     // reads and clears the device error flag (synchronises the stream)
     int take_status(cudaStream_t s);
+    // Operator correction: corr (bf16, state_len() entries, internal layout) is added to the
+    // right-hand side of every RK stage from now on (nullptr: none). Mult never adds it.
+    void set_correction(const uint16_t* corr);
+    // corr = bf16((ref_hi - l32) + ref_lo): ref is a working state (pair) holding the FP64
+    // operator's product, l32 the hi block of this form's product of the same state
+    void build_correction(const float* ref_pair, const float* l32, uint16_t* corr, cudaStream_t s);
 
 private:
     void stage(BatchedStageArgs A, double t, cudaStream_t s);
@@ -131,7 +142,7 @@ private:
     int64_t device_bytes_ = 0;
     int64_t launches_ = 0;
     std::vector<void*> allocs_;
-    int32_t* perm_ = nullptr;   // internal element -> reference element
+    int32_t* inv_perm_ = nullptr;   // reference element -> internal element
     std::vector<int32_t> inv_perm_host_;
     PlaneWaveF32* pw_dev_ = nullptr;
     int* pw_off_ = nullptr;
@@ -151,7 +162,9 @@ private:
     double g_dt_ = 0.0;
     cudaStream_t g_stream_ = nullptr;
     int g_contraction_ = -1;
+    const uint16_t* g_corr_ = nullptr;
     int64_t g_graph_launches_ = 0;   // kernels in one replay
+    const uint16_t* corr_ = nullptr; // operator correction of the RK stages (set_correction)
     const uint32_t* op_img_ = nullptr;
     int* status_ = nullptr;
     int n_sm_ = 152;

@@ -114,6 +114,16 @@ struct dgtd_op {
     int contraction32 = 0;
     // batched FP32 form
     std::unique_ptr<dgtd::BatchedOp> batched;
+    // FP64 defect correction of the batched form: refresh period (steps, 0: off), steps since
+    // the last refresh, the state buffer it was made from (nullptr: none valid), two scratch
+    // buffers (each max(FP64 reference state, FP32 working state) bytes) and the bf16 term
+    int defect_every = 0;
+    int64_t defect_age = 0;
+    const void* defect_state = nullptr;
+    int64_t defect_refreshes = 0;
+    void* defect_a = nullptr;
+    void* defect_b = nullptr;
+    uint16_t* defect_corr = nullptr;
     // point probes / DFT accumulators, sampled by dgtd_op_step every probes->every() steps
     std::unique_ptr<dgtd::ProbeSet> probes;
     int64_t probe_steps = 0;
@@ -127,8 +137,18 @@ struct dgtd_op {
         if (stab_dev) cudaFree(stab_dev);
         if (tc1_img) cudaFree(tc1_img);
         if (tc1_status) cudaFree(tc1_status);
+        free_defect_buffers();
         if (ws) cudaFree(ws);
         if (ws32) cudaFree(ws32);
+    }
+    void free_defect_buffers()
+    {
+        if (defect_a) cudaFree(defect_a);
+        if (defect_b) cudaFree(defect_b);
+        if (defect_corr) cudaFree(defect_corr);
+        defect_a = defect_b = nullptr;
+        defect_corr = nullptr;
+        defect_state = nullptr;
     }
     template <typename T>
     T* up(const std::vector<T>& v)
@@ -251,6 +271,58 @@ void run_stage(dgtd_op* op, dgtd::StageArgs A, double t, cudaStream_t s)
     }
     ck(dgtd::launch_stage_fp64(op->dev, A, s), "stage kernel");
     g_launches.fetch_add(1, std::memory_order_relaxed);
+}
+
+// FP64 defect correction of the batched form (dgtd_op_set_defect_correction): from the state in
+// d_work at time t, c = L64(x) - L32(x_hi), kept in bf16 and added by every later RK stage.
+// Scratch a: x (reference layout, FP64), then L64(x) as a working state; scratch b: L64(x)
+// (reference layout), then L32(x_hi). All on stream s, no host synchronisation.
+void defect_refresh(dgtd_op* op, float* d_work, double t, cudaStream_t s)
+{
+    dgtd::BatchedOp& B = *op->batched;
+    if (!op->defect_a) {
+        const size_t bytes = std::max(static_cast<size_t>(op->state_len) * sizeof(double),
+                                      static_cast<size_t>(B.work_len()) * sizeof(float));
+        ck(cudaMalloc(&op->defect_a, bytes), "cudaMalloc defect-correction scratch");
+        ck(cudaMalloc(&op->defect_b, bytes), "cudaMalloc defect-correction scratch");
+        ck(cudaMalloc(&op->defect_corr, static_cast<size_t>(B.state_len()) * sizeof(uint16_t)),
+           "cudaMalloc defect correction");
+    }
+    double* x64 = static_cast<double*>(op->defect_a);
+    double* l64 = static_cast<double*>(op->defect_b);
+    B.unpack(d_work, x64, s);
+    dgtd::StageArgs A{};
+    A.mode = dgtd::MODE_MULT;
+    A.in = x64;
+    A.out = l64;
+    run_stage(op, A, t, s);
+    float* l64w = static_cast<float*>(op->defect_a);
+    float* l32 = static_cast<float*>(op->defect_b);
+    B.pack(l64, l64w, s);
+    B.mult(d_work, l32, t, s);
+    B.build_correction(l64w, l32, op->defect_corr, s);
+    B.set_correction(op->defect_corr);
+    op->defect_state = d_work;
+    op->defect_age = 0;
+    ++op->defect_refreshes;
+}
+
+// nsteps steps of the batched form, with the defect correction refreshed on its schedule
+void batched_steps(dgtd_op* op, float* d_work, double t, double dt, int nsteps, int integrator, cudaStream_t s)
+{
+    dgtd::BatchedOp& B = *op->batched;
+    if (op->defect_every <= 0) {
+        B.step(d_work, t, dt, nsteps, integrator, s);
+        return;
+    }
+    while (nsteps > 0) {
+        if (op->defect_state != d_work || op->defect_age >= op->defect_every) defect_refresh(op, d_work, t, s);
+        const int n = static_cast<int>(std::min<int64_t>(nsteps, op->defect_every - op->defect_age));
+        B.step(d_work, t, dt, n, integrator, s);
+        t += n * dt;
+        nsteps -= n;
+        op->defect_age += n;
+    }
 }
 
 void ensure_ws(dgtd_op* op)
@@ -551,6 +623,7 @@ int dgtd_op_set_planewaves(dgtd_op* op, const dgtd_planewave* pw, int32_t n)
                              : dgtd::TfsfSkipBound();
         ensure_sources(op);
         if (op->batched) op->batched->set_sources(op->pw_host);
+        op->defect_state = nullptr;
     } catch (const std::exception& e) {
         return fail(DGTD_ERR_CUDA, e.what());
     }
@@ -675,12 +748,12 @@ int dgtd_op_step(dgtd_op* op, void* d_work, double t0, double dt, int32_t nsteps
         if (op->batched) {
             BatchedCount bc(op);
             if (!pr) {
-                op->batched->step(static_cast<float*>(d_work), t0, dt, nsteps, integrator, s);
+                batched_steps(op, static_cast<float*>(d_work), t0, dt, nsteps, integrator, s);
                 return DGTD_OK;
             }
             double t = t0;
             for (int i = 0; i < nsteps; ++i) {
-                op->batched->step(static_cast<float*>(d_work), t, dt, 1, integrator, s);
+                batched_steps(op, static_cast<float*>(d_work), t, dt, 1, integrator, s);
                 t += dt;
                 if (++op->probe_steps % pr->every() == 0) {
                     pr->sample(d_work, t, s);
@@ -747,6 +820,7 @@ int dgtd_op_run_host(dgtd_op* op, double* h_state, double t0, double dt, double 
         ck(cudaMemcpy(d, h_state, bytes, cudaMemcpyHostToDevice), "H2D");
         if (op->precision != DGTD_FP64) {
             ck(cudaMalloc(&w, (op->batched ? op->batched->work_len() : op->state_len) * sizeof(float)), "cudaMalloc");
+            op->defect_state = nullptr;   // a new trajectory: the defect correction refreshes at its first step
             rc = dgtd_op_pack(op, d, w, nullptr);
         } else {
             w = d;
@@ -888,6 +962,28 @@ int dgtd_op_set_contraction(dgtd_op* op, int32_t mode)
     if (mode != 0 && mode != 1) return fail(DGTD_ERR_INVALID, "contraction mode must be 0 or 1");
     if (op->batched) op->batched->set_contraction(mode);
     op->contraction32 = mode;
+    return DGTD_OK;
+}
+
+int dgtd_op_set_defect_correction(dgtd_op* op, int32_t every)
+{
+    if (!op) return fail(DGTD_ERR_INVALID, "NULL operator");
+    if (every < 0) return fail(DGTD_ERR_INVALID, "defect-correction period must be >= 0");
+    if (!op->batched) return fail(DGTD_ERR_UNSUPPORTED, "the defect correction is implemented for the batched FP32 form");
+    op->defect_every = every;
+    op->defect_state = nullptr;
+    op->defect_age = 0;
+    if (every == 0) {
+        op->batched->set_correction(nullptr);
+        op->free_defect_buffers();
+    }
+    return DGTD_OK;
+}
+
+int dgtd_op_defect_refreshes(const dgtd_op* op, int64_t* refreshes)
+{
+    if (!op) return fail(DGTD_ERR_INVALID, "NULL operator");
+    if (refreshes) *refreshes = op->defect_refreshes;
     return DGTD_OK;
 }
 

@@ -221,6 +221,28 @@ int dgtd_op_set_contraction(dgtd_op* op, int32_t mode);
  * captures the graph. DGTD_ERR_UNSUPPORTED for the other forms. */
 int dgtd_op_set_graph_steps(dgtd_op* op, int32_t steps);
 
+/* Batched FP32 form: FP64 defect correction of the operator (no counterpart in the reference,
+ * whose operator is FP64 throughout). Every `every` steps of dgtd_op_step (0: off, the default)
+ * the state is unpacked, the plain FP64 form applies the operator to it, and the difference
+ * c = L64(x) - L32(x_hi) from this form's product of the same state is kept (bf16, one state
+ * block). Every RK stage then adds c to its right-hand side, so a field that changes little
+ * between refreshes (a static remainder, a slowly varying mode) is advanced with the FP64
+ * operator's right-hand side instead of accumulating the FP32 rounding of it step after step.
+ * The correction belongs to the trajectory being stepped: it is also refreshed at the first step
+ * after this call, when dgtd_op_step is given another state buffer, after
+ * dgtd_op_set_planewaves and at the start of dgtd_op_run_host, but not by dgtd_op_pack (a caller
+ * that moves the state through the reference layout every step keeps it). A caller that loads an
+ * unrelated state into the same buffer calls this function again; until then a stale correction
+ * adds a forcing at the FP32 rounding level of the old state's right-hand side. Costs per
+ * refresh: unpack, one FP64 product, pack and one FP32 product; in device memory two scratch
+ * buffers of max(FP64 reference state, FP32 working state) bytes and the bf16 correction (half
+ * an FP32 state block); in each stage one more 2-byte read per value. Mult does not add the
+ * correction. DGTD_ERR_UNSUPPORTED for the other forms. */
+int dgtd_op_set_defect_correction(dgtd_op* op, int32_t every);
+
+/* Refreshes made by the defect correction since the operator was created (may be NULL). */
+int dgtd_op_defect_refreshes(const dgtd_op* op, int64_t* refreshes);
+
 /* Batched FP32 form: time the candidate stage kernels on this operator's mesh and keep the
  * fastest (the tile-shape autotuner): 0 = tensor cores (3xTF32, 64 incidences x one element
  * per work item; orders 1..4, B padded to 64), 1..3 = FP32 SIMT with 4, 8, 16 warps per

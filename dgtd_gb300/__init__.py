@@ -473,8 +473,9 @@ class Operator:
         _check(lib().dgtd_op_set_graph_steps(self._h, int(steps)), "dgtd_op_set_graph_steps")
 
     def set_defect_correction(self, every: int) -> None:
-        """Batched FP32 form: refresh an FP64 correction of the operator every `every` steps and
-        add it to every RK stage's right-hand side (0: off)."""
+        """Batched FP32 form, classical RK4: every `every` steps (0: off) form c = L64(x) - L32(x)
+        with the FP64 operator, keep it where the state has not moved since the previous refresh,
+        and add its RK4 step increment to the state after every step."""
         _check(lib().dgtd_op_set_defect_correction(self._h, int(every)), "dgtd_op_set_defect_correction")
 
     @property

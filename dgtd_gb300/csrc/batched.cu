@@ -191,10 +191,7 @@ __global__ void __launch_bounds__(kWarps * kLanes) stage_f32(BatchedTables T, Ba
             k[4] = im * (-(dz(0) - dx(2)) + lf[4]);
             k[5] = im * (-(dx(1) - dy(0)) + lf[5]);
             const float dt = A.dt;
-            if (A.corr) {
-#pragma unroll
-                for (int c = 0; c < 6; ++c) k[c] += bf16_bits_to_float(A.corr[((e * 6 + c) * Np + i) * Bp + col]);
-            }
+
 #pragma unroll
             for (int c = 0; c < 6; ++c) {
                 const int64_t idx = ((e * 6 + c) * Np + i) * Bp + col;
@@ -590,8 +587,7 @@ void BatchedOp::set_sources(const std::vector<PlaneWaveDev>& pw)
 void BatchedOp::stage(BatchedStageArgs A, double t, cudaStream_t s)
 {
     if (A.t_base == nullptr) A.t = static_cast<float>(t);   // else t is the offset set by the caller
-    A.corr = (A.mode == MODE_MULT) ? nullptr : corr_;
-    if (has_tfsf_ && n_pw_ > 0) {
+    if (has_tfsf_ && n_pw_ > 0 && !no_sources_) {
         tfsf_skip_f32<<<dim3(Bpad_, kSkipParts), 256, 0, s>>>(T_, pw_dev_, pw_off_, A.t, A.t_base, skip_partial_,
                                                              skip_ticket_, skip_);
         ckb(cudaGetLastError(), "tfsf skip kernel");
@@ -679,30 +675,105 @@ void BatchedOp::mult(const float* d_in, float* d_out, double t, cudaStream_t s)
     ckb(cudaMemsetAsync(d_out + state_len_, 0, state_len_ * sizeof(float), s), "memset");
 }
 
-// corr[i] = bf16((ref[i] - l32[i]) + ref[L + i]) over one state block: the FP64 operator's
-// product (held as a pair) minus this form's product of the same state. The two products agree
-// to about FP32 precision, so the difference is exact and its bf16 rounding (2^-9 relative)
-// only scales the correction, which is itself at the FP32 rounding level of the product.
+// c[i] = (ref[i] - l32[i]) + ref[L + i] over one state block: the FP64 operator's product (held
+// as a pair) minus this form's product of the same state. The two products agree to about FP32
+// precision, so the difference is exact and its bf16 rounding (2^-9 relative) only scales the
+// correction, which is itself at the FP32 rounding level of the product. It is kept where the
+// state has stayed put since the previous refresh (|x - x_prev| <= 1e-3 |x|): there the field's
+// FP32 rounding repeats step after step and would otherwise accumulate into a drift, while a
+// moving field's rounding error is random from step to step and a stale constant correction
+// applied for a whole refresh period would make it systematic. x_prev is then set to x.
 __global__ void __launch_bounds__(256) correction_kernel(const float* __restrict__ ref, const float* __restrict__ l32,
-                                                       uint16_t* __restrict__ corr, int64_t L)
+                                                       const float* __restrict__ x, float* __restrict__ x_prev,
+                                                       uint16_t* __restrict__ c, int64_t L)
 {
     for (int64_t i = blockIdx.x * 256ll + threadIdx.x; i < L; i += static_cast<int64_t>(gridDim.x) * 256) {
+        const float xv = x[i];
+        const bool still = fabsf(xv - x_prev[i]) <= 1e-3f * fabsf(xv);   // false for a NaN x_prev
         const float d = (ref[i] - l32[i]) + ref[L + i];
-        corr[i] = __bfloat16_as_ushort(__float2bfloat16_rn(d));
+        c[i] = still ? __bfloat16_as_ushort(__float2bfloat16_rn(d)) : uint16_t(0);
+        x_prev[i] = xv;
     }
 }
 
-void BatchedOp::set_correction(const uint16_t* corr)
+// One stage of the forced RK4 step from zero: k = A y + c (kprod = A y, or none for k1 = c);
+// d += wd k; y = wy k. d and y: FP32 state blocks.
+__global__ void __launch_bounds__(256) forcing_stage_kernel(const float* __restrict__ kprod,
+                                                          const uint16_t* __restrict__ c, float* __restrict__ d,
+                                                          float* __restrict__ y, float wd, float wy, bool first,
+                                                          int64_t L)
 {
-    corr_ = corr;
+    for (int64_t i = blockIdx.x * 256ll + threadIdx.x; i < L; i += static_cast<int64_t>(gridDim.x) * 256) {
+        const float k = (kprod ? kprod[i] : 0.0f) + bf16_bits_to_float(c[i]);
+        d[i] = first ? wd * k : d[i] + wd * k;
+        if (y) y[i] = wy * k;
+    }
 }
 
-void BatchedOp::build_correction(const float* ref_pair, const float* l32, uint16_t* corr, cudaStream_t s)
+// inc[i] = bf16(d[i])
+__global__ void __launch_bounds__(256) to_bf16_kernel(const float* __restrict__ d, uint16_t* __restrict__ inc,
+                                                    int64_t L)
+{
+    for (int64_t i = blockIdx.x * 256ll + threadIdx.x; i < L; i += static_cast<int64_t>(gridDim.x) * 256)
+        inc[i] = __bfloat16_as_ushort(__float2bfloat16_rn(d[i]));
+}
+
+// x_lo[i] += inc[i] (the pair (x_hi, x_lo) need not be normalised: the next compensated update
+// and unpack take x_hi + x_lo as the value)
+__global__ void __launch_bounds__(256) add_increment_kernel(float* __restrict__ xl, const uint16_t* __restrict__ inc,
+                                                          int64_t L)
+{
+    for (int64_t i = blockIdx.x * 256ll + threadIdx.x; i < L; i += static_cast<int64_t>(gridDim.x) * 256)
+        xl[i] += bf16_bits_to_float(inc[i]);
+}
+
+unsigned BatchedOp::stream_grid() const
 {
     const int64_t want = (state_len_ + 2047) / 2048;
-    const unsigned grid = static_cast<unsigned>(std::max<int64_t>(1, std::min<int64_t>(want, 8ll * n_sm_)));
-    correction_kernel<<<grid, 256, 0, s>>>(ref_pair, l32, corr, state_len_);
+    return static_cast<unsigned>(std::max<int64_t>(1, std::min<int64_t>(want, 8ll * n_sm_)));
+}
+
+void BatchedOp::build_correction(const float* ref_pair, const float* l32, const float* x, float* x_prev, uint16_t* c,
+                                 cudaStream_t s)
+{
+    correction_kernel<<<stream_grid(), 256, 0, s>>>(ref_pair, l32, x, x_prev, c, state_len_);
     ckb(cudaGetLastError(), "correction kernel");
+    ++launches_;
+}
+
+void BatchedOp::build_increment(const uint16_t* c, float* scratch_a, float* scratch_b, uint16_t* inc, double dt,
+                                cudaStream_t s)
+{
+    const int64_t L = state_len_;
+    float* d = scratch_a;          // accumulated increment
+    float* y = scratch_a + L;      // stage input of the next product
+    float* kp = scratch_b;         // product A y (working state: hi block, lo block cleared)
+    const float h = static_cast<float>(dt);
+    const float wd[4] = {h / 6.0f, h / 3.0f, h / 3.0f, h / 6.0f};
+    const float wy[3] = {0.5f * h, 0.5f * h, h};
+    no_sources_ = true;
+    try {
+        for (int st = 0; st < 4; ++st) {
+            if (st > 0) mult(y, kp, 0.0, s);
+            forcing_stage_kernel<<<stream_grid(), 256, 0, s>>>(st > 0 ? kp : nullptr, c, d, st < 3 ? y : nullptr,
+                                                               wd[st], st < 3 ? wy[st] : 0.0f, st == 0, L);
+            ckb(cudaGetLastError(), "forcing stage kernel");
+            ++launches_;
+        }
+    } catch (...) {
+        no_sources_ = false;
+        throw;
+    }
+    no_sources_ = false;
+    to_bf16_kernel<<<stream_grid(), 256, 0, s>>>(d, inc, L);
+    ckb(cudaGetLastError(), "increment kernel");
+    ++launches_;
+}
+
+void BatchedOp::add_increment(float* x, const uint16_t* inc, cudaStream_t s)
+{
+    add_increment_kernel<<<stream_grid(), 256, 0, s>>>(x + state_len_, inc, state_len_);
+    ckb(cudaGetLastError(), "add increment kernel");
     ++launches_;
 }
 
@@ -749,9 +820,7 @@ void BatchedOp::step(float* d_x, double t0, double dt, int nsteps, int integrato
         // blocks of G steps replayed from one captured graph (not on the legacy default stream,
         // which cannot be captured); the stage times are offsets from the device scalar t_dev_
         if (G > 0 && s != nullptr && nsteps >= G) {
-            if (gexec_ && (g_x_ != d_x || g_dt_ != dt || g_stream_ != s || g_contraction_ != contraction_ ||
-                           g_corr_ != corr_))
-                drop_graph();
+            if (gexec_ && (g_x_ != d_x || g_dt_ != dt || g_stream_ != s || g_contraction_ != contraction_)) drop_graph();
             if (!gexec_) {
                 if (!t_dev_) ckb(cudaMalloc(&t_dev_, sizeof(double)), "cudaMalloc graph time");
                 // one direct step first so that every kernel attribute is set outside the capture
@@ -779,7 +848,7 @@ void BatchedOp::step(float* d_x, double t0, double dt, int nsteps, int integrato
                 if (ce != cudaSuccess) { gexec_ = nullptr; throw std::runtime_error(std::string("graph instantiate: ") + cudaGetErrorString(ce)); }
                 g_graph_launches_ = launches_ - before + 1;
                 launches_ = before;
-                g_x_ = d_x; g_dt_ = dt; g_stream_ = s; g_contraction_ = contraction_; g_corr_ = corr_;
+                g_x_ = d_x; g_dt_ = dt; g_stream_ = s; g_contraction_ = contraction_;
             }
             set_time<<<1, 1, 0, s>>>(t_dev_, t);
             ckb(cudaGetLastError(), "set time");

@@ -62,8 +62,6 @@ struct BatchedStageArgs {
     const PlaneWaveF32* pw;  // sources sorted by incidence
     const int* pw_off;       // [Bpad + 1]: sources of incidence b are pw[pw_off[b] .. pw_off[b+1])
     const int* skip;         // [Bpad]
-    const uint16_t* corr;    // operator correction added to every right-hand side (bf16 bits, internal
-                             // layout of one state block), or nullptr; never set for MODE_MULT
 };
 
 #ifdef __CUDACC__
@@ -122,15 +120,27 @@ public:
     bool uses_tensor_cores() const { return contraction_ == 0 && tc_supported(T_.p, Bpad_); }
     // reads and clears the device error flag (synchronises the stream)
     int take_status(cudaStream_t s);
-    // Operator correction: corr (bf16, state_len() entries, internal layout) is added to the
-    // right-hand side of every RK stage from now on (nullptr: none). Mult never adds it.
-    void set_correction(const uint16_t* corr);
-    // corr = bf16((ref_hi - l32) + ref_lo): ref is a working state (pair) holding the FP64
-    // operator's product, l32 the hi block of this form's product of the same state
-    void build_correction(const float* ref_pair, const float* l32, uint16_t* corr, cudaStream_t s);
+    // FP64 defect correction (bf16 c and its step increment inc: state_len() entries each,
+    // internal layout of one state block).
+    // c = (ref_hi - l32) + ref_lo, where ref is a working state (pair) holding the FP64 operator's
+    // product and l32 the hi block of this form's product of the state x (a working state), kept
+    // only where x_hi has stayed within 1e-3 (relative) of x_prev, its value at the previous
+    // refresh (x_prev is then overwritten with x_hi; NaN entries never match).
+    void build_correction(const float* ref_pair, const float* l32, const float* x, float* x_prev, uint16_t* c,
+                          cudaStream_t s);
+    // inc = one classical RK4 step of size dt from the zero state under the constant forcing c,
+    // with the source-free operator A: dt/6 (k1 + 2 k2 + 2 k3 + k4), k1 = c, k2 = A (dt/2 k1) + c,
+    // k3 = A (dt/2 k2) + c, k4 = A (dt k3) + c. The operator is linear, so a step of
+    // u' = Au + s(t) + c equals the step of u' = Au + s(t) plus inc. scratch_a, scratch_b: working
+    // states (2 state_len() floats each).
+    void build_increment(const uint16_t* c, float* scratch_a, float* scratch_b, uint16_t* inc, double dt,
+                         cudaStream_t s);
+    // x_lo += inc over the working state x
+    void add_increment(float* x, const uint16_t* inc, cudaStream_t s);
 
 private:
     void stage(BatchedStageArgs A, double t, cudaStream_t s);
+    unsigned stream_grid() const;   // grid of the elementwise kernels over one state block
     void ensure_ws();
     void rk4_steps_direct(float* d_x, double t, double dt, int nsteps, cudaStream_t s);
     void drop_graph();
@@ -162,9 +172,8 @@ private:
     double g_dt_ = 0.0;
     cudaStream_t g_stream_ = nullptr;
     int g_contraction_ = -1;
-    const uint16_t* g_corr_ = nullptr;
     int64_t g_graph_launches_ = 0;   // kernels in one replay
-    const uint16_t* corr_ = nullptr; // operator correction of the RK stages (set_correction)
+    bool no_sources_ = false;        // stages without the TF/SF sources (build_increment)
     const uint32_t* op_img_ = nullptr;
     int* status_ = nullptr;
     int n_sm_ = 152;

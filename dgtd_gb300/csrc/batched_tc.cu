@@ -205,7 +205,6 @@ __device__ __forceinline__ void prefetch_rk_registers(const BatchedStageArgs& A,
     } else if (MODE == MODE_LSRK) {
         prefetch_l2(A.res + e * EB, eb);
     }
-    if (A.corr) prefetch_l2(A.corr + e * EB, eb / 2);
 }
 
 // Epilogue operand loads of one chunk of kEpiNodes nodes (global, stride Bp between nodes).
@@ -215,7 +214,6 @@ struct EpiOps {
     float z[kEpiNodes];   // z (RK4_2/3/4)
     float u[kEpiNodes];   // stage input (RK4_1, LSRK, conductivity)
     float l[kEpiNodes];   // x_lo (RK4_4)
-    float c[kEpiNodes];   // operator correction (zero without one)
 };
 
 template <int MODE>
@@ -228,16 +226,13 @@ __device__ __forceinline__ void epi_load(const BatchedStageArgs& A, int64_t base
     const float* __restrict__ pz = A.z + base;
     const float* __restrict__ pu = A.in + base;
     const float* __restrict__ pl = A.xl + base;
-    const uint16_t* __restrict__ pc = A.corr;
 #pragma unroll
     for (int j = 0; j < kEpiNodes; ++j) {
-        o.c[j] = 0.0f;
         if (j < nv) {
             if (need_a) o.a[j] = px[j * Bp];
             if (need_z) o.z[j] = pz[j * Bp];
             if (need_l) o.l[j] = pl[j * Bp];
             if (need_u) o.u[j] = __ldg(pu + j * Bp);
-            if (MODE != MODE_MULT && pc) o.c[j] = bf16_bits_to_float(__ldg(pc + base + j * Bp));
         }
     }
 }
@@ -251,7 +246,7 @@ __device__ __forceinline__ void epi_store(const BatchedStageArgs& A, int64_t bas
     for (int j = 0; j < kEpiNodes; ++j) {
         if (j < nv) {
             const float uc = need_u ? o.u[j] : 0.0f;
-            const float k = fe * kv[j] - fs * uc + o.c[j];
+            const float k = fe * kv[j] - fs * uc;
             const int64_t ix = base + static_cast<int64_t>(j) * Bp;
             if (MODE == MODE_MULT) {
                 A.out[ix] = k;

@@ -123,7 +123,11 @@ struct dgtd_op {
     int64_t defect_refreshes = 0;
     void* defect_a = nullptr;
     void* defect_b = nullptr;
-    uint16_t* defect_corr = nullptr;
+    uint16_t* defect_corr = nullptr;   // the applied correction c (bf16)
+    float* defect_prev = nullptr;      // x_hi at the previous refresh (NaN: none)
+    uint16_t* defect_inc = nullptr;    // c's classical-RK4 step increment for dt = defect_inc_dt (bf16)
+    double defect_inc_dt = 0.0;
+    bool defect_inc_stale = true;
     // point probes / DFT accumulators, sampled by dgtd_op_step every probes->every() steps
     std::unique_ptr<dgtd::ProbeSet> probes;
     int64_t probe_steps = 0;
@@ -146,9 +150,13 @@ struct dgtd_op {
         if (defect_a) cudaFree(defect_a);
         if (defect_b) cudaFree(defect_b);
         if (defect_corr) cudaFree(defect_corr);
+        if (defect_prev) cudaFree(defect_prev);
+        if (defect_inc) cudaFree(defect_inc);
         defect_a = defect_b = nullptr;
-        defect_corr = nullptr;
+        defect_corr = defect_inc = nullptr;
+        defect_prev = nullptr;
         defect_state = nullptr;
+        defect_inc_stale = true;
     }
     template <typename T>
     T* up(const std::vector<T>& v)
@@ -274,19 +282,22 @@ void run_stage(dgtd_op* op, dgtd::StageArgs A, double t, cudaStream_t s)
 }
 
 // FP64 defect correction of the batched form (dgtd_op_set_defect_correction): from the state in
-// d_work at time t, c = L64(x) - L32(x_hi), kept in bf16 and added by every later RK stage.
-// Scratch a: x (reference layout, FP64), then L64(x) as a working state; scratch b: L64(x)
-// (reference layout), then L32(x_hi). All on stream s, no host synchronisation.
+// d_work at time t, c = L64(x) - L32(x_hi) in bf16, kept where the state has not moved since the
+// previous refresh. Scratch a: x (reference layout, FP64), then L64(x) as a working state;
+// scratch b: L64(x) (reference layout), then L32(x_hi). All on stream s, no host synchronisation.
 void defect_refresh(dgtd_op* op, float* d_work, double t, cudaStream_t s)
 {
     dgtd::BatchedOp& B = *op->batched;
+    const int64_t L = B.state_len();
     if (!op->defect_a) {
         const size_t bytes = std::max(static_cast<size_t>(op->state_len) * sizeof(double),
                                       static_cast<size_t>(B.work_len()) * sizeof(float));
         ck(cudaMalloc(&op->defect_a, bytes), "cudaMalloc defect-correction scratch");
         ck(cudaMalloc(&op->defect_b, bytes), "cudaMalloc defect-correction scratch");
-        ck(cudaMalloc(&op->defect_corr, static_cast<size_t>(B.state_len()) * sizeof(uint16_t)),
-           "cudaMalloc defect correction");
+        ck(cudaMalloc(&op->defect_corr, static_cast<size_t>(L) * sizeof(uint16_t)), "cudaMalloc defect correction");
+        ck(cudaMalloc(&op->defect_inc, static_cast<size_t>(L) * sizeof(uint16_t)), "cudaMalloc defect correction");
+        ck(cudaMalloc(&op->defect_prev, static_cast<size_t>(L) * sizeof(float)), "cudaMalloc defect correction");
+        ck(cudaMemsetAsync(op->defect_prev, 0xff, static_cast<size_t>(L) * sizeof(float), s), "memset");
     }
     double* x64 = static_cast<double*>(op->defect_a);
     double* l64 = static_cast<double*>(op->defect_b);
@@ -300,14 +311,25 @@ void defect_refresh(dgtd_op* op, float* d_work, double t, cudaStream_t s)
     float* l32 = static_cast<float*>(op->defect_b);
     B.pack(l64, l64w, s);
     B.mult(d_work, l32, t, s);
-    B.build_correction(l64w, l32, op->defect_corr, s);
-    B.set_correction(op->defect_corr);
+    B.build_correction(l64w, l32, d_work, op->defect_prev, op->defect_corr, s);
     op->defect_state = d_work;
     op->defect_age = 0;
+    op->defect_inc_stale = true;
     ++op->defect_refreshes;
 }
 
-// nsteps steps of the batched form, with the defect correction refreshed on its schedule
+// A new trajectory: refresh at the next step, with no earlier state to compare with.
+void defect_restart(dgtd_op* op)
+{
+    op->defect_state = nullptr;
+    op->defect_age = 0;
+    if (op->defect_prev && op->batched)
+        ck(cudaMemset(op->defect_prev, 0xff, static_cast<size_t>(op->batched->state_len()) * sizeof(float)),
+           "memset");
+}
+
+// nsteps steps of the batched form; with the defect correction on, one step at a time, each
+// followed by the correction's increment, and the correction refreshed on its schedule
 void batched_steps(dgtd_op* op, float* d_work, double t, double dt, int nsteps, int integrator, cudaStream_t s)
 {
     dgtd::BatchedOp& B = *op->batched;
@@ -315,13 +337,20 @@ void batched_steps(dgtd_op* op, float* d_work, double t, double dt, int nsteps, 
         B.step(d_work, t, dt, nsteps, integrator, s);
         return;
     }
-    while (nsteps > 0) {
+    if (integrator != DGTD_RK4)
+        throw std::invalid_argument("the defect correction is implemented for classical RK4 (DGTD_RK4)");
+    for (int i = 0; i < nsteps; ++i) {
         if (op->defect_state != d_work || op->defect_age >= op->defect_every) defect_refresh(op, d_work, t, s);
-        const int n = static_cast<int>(std::min<int64_t>(nsteps, op->defect_every - op->defect_age));
-        B.step(d_work, t, dt, n, integrator, s);
-        t += n * dt;
-        nsteps -= n;
-        op->defect_age += n;
+        if (op->defect_inc_stale || op->defect_inc_dt != dt) {
+            B.build_increment(op->defect_corr, static_cast<float*>(op->defect_a), static_cast<float*>(op->defect_b),
+                              op->defect_inc, dt, s);
+            op->defect_inc_dt = dt;
+            op->defect_inc_stale = false;
+        }
+        B.step(d_work, t, dt, 1, integrator, s);
+        B.add_increment(d_work, op->defect_inc, s);
+        t += dt;
+        ++op->defect_age;
     }
 }
 
@@ -623,7 +652,7 @@ int dgtd_op_set_planewaves(dgtd_op* op, const dgtd_planewave* pw, int32_t n)
                              : dgtd::TfsfSkipBound();
         ensure_sources(op);
         if (op->batched) op->batched->set_sources(op->pw_host);
-        op->defect_state = nullptr;
+        defect_restart(op);
     } catch (const std::exception& e) {
         return fail(DGTD_ERR_CUDA, e.what());
     }
@@ -799,6 +828,8 @@ int dgtd_op_step(dgtd_op* op, void* d_work, double t0, double dt, int32_t nsteps
         }
         if (integrator == DGTD_LSERK4 && cur != d_state)
             ck(cudaMemcpyAsync(d_state, cur, op->state_len * sizeof(double), cudaMemcpyDeviceToDevice, s), "copy");
+    } catch (const std::invalid_argument& e) {
+        return fail(DGTD_ERR_UNSUPPORTED, e.what());
     } catch (const std::exception& e) {
         return fail(DGTD_ERR_CUDA, e.what());
     }
@@ -820,7 +851,7 @@ int dgtd_op_run_host(dgtd_op* op, double* h_state, double t0, double dt, double 
         ck(cudaMemcpy(d, h_state, bytes, cudaMemcpyHostToDevice), "H2D");
         if (op->precision != DGTD_FP64) {
             ck(cudaMalloc(&w, (op->batched ? op->batched->work_len() : op->state_len) * sizeof(float)), "cudaMalloc");
-            op->defect_state = nullptr;   // a new trajectory: the defect correction refreshes at its first step
+            defect_restart(op);   // a new trajectory: the defect correction refreshes at its first step
             rc = dgtd_op_pack(op, d, w, nullptr);
         } else {
             w = d;
@@ -970,12 +1001,12 @@ int dgtd_op_set_defect_correction(dgtd_op* op, int32_t every)
     if (!op) return fail(DGTD_ERR_INVALID, "NULL operator");
     if (every < 0) return fail(DGTD_ERR_INVALID, "defect-correction period must be >= 0");
     if (!op->batched) return fail(DGTD_ERR_UNSUPPORTED, "the defect correction is implemented for the batched FP32 form");
-    op->defect_every = every;
-    op->defect_state = nullptr;
-    op->defect_age = 0;
-    if (every == 0) {
-        op->batched->set_correction(nullptr);
-        op->free_defect_buffers();
+    try {
+        op->defect_every = every;
+        defect_restart(op);
+        if (every == 0) op->free_defect_buffers();
+    } catch (const std::exception& e) {
+        return fail(DGTD_ERR_CUDA, e.what());
     }
     return DGTD_OK;
 }

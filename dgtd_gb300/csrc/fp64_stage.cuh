@@ -42,6 +42,10 @@ struct Ord {
     // stays below 48 KB
     static constexpr int EPB0 = kBlock / Np > 0 ? kBlock / Np : 1;
     static constexpr int EPB = EPB0 > 32 ? 32 : EPB0;
+    // small-block variant for meshes too small to fill the SMs with kBlock-thread blocks:
+    // about 64 threads (one or two warps) per block
+    static constexpr int EPB_SMALL = 64 / Np > 0 ? (64 / Np > 16 ? 16 : 64 / Np) : 1;
+    static constexpr int BLOCK_SMALL = (EPB_SMALL * Np + 31) / 32 * 32;
 };
 
 // The body is written for an arithmetic type R: double (the FP64 form) or float
@@ -95,11 +99,12 @@ __device__ __forceinline__ void load6(const R* p, R* v)
     }
 }
 
-template <int P, typename R = double>
+// EPB_: elements per block (0: Ord's default); the block has at least EPB_ * Np threads
+template <int P, typename R = double, int EPB_ = 0>
 __device__ __forceinline__ void stage_body(const TablesT<R>& T, const StageArgsT<R>& A, int64_t e0, int b)
 {
     using O = Ord<P, R>;
-    constexpr int Np = O::Np, Nfp = O::Nfp, NF = O::NF, EPB = O::EPB;
+    constexpr int Np = O::Np, Nfp = O::Nfp, NF = O::NF, EPB = EPB_ > 0 ? EPB_ : O::EPB;
     constexpr int S = Node6<R>::S;
     __shared__ __align__(16) R s_u[EPB * Np * S];     // [node][component]
     __shared__ __align__(16) R s_f[EPB * NF * S];     // [face node][component]

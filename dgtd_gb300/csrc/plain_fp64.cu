@@ -19,6 +19,18 @@ __global__ void __launch_bounds__(kBlock) stage_fp64(TablesDev T, StageArgs A)
     fp64::stage_body<P>(T, A, static_cast<int64_t>(blockIdx.x) * Ord<P>::EPB, static_cast<int>(blockIdx.y));
 }
 
+// Small meshes: blocks of about 64 threads, so that the grid spreads over every SM evenly
+// (3,072 tets at p = 3 give 256 blocks of 240 threads, 0.56 waves, but 1,024 of 60).
+template <int P>
+__global__ void __launch_bounds__(Ord<P>::BLOCK_SMALL) stage_fp64_small(TablesDev T, StageArgs A)
+{
+    fp64::stage_body<P, double, Ord<P>::EPB_SMALL>(T, A, static_cast<int64_t>(blockIdx.x) * Ord<P>::EPB_SMALL,
+                                                   static_cast<int>(blockIdx.y));
+}
+
+// below this many default blocks (4 per SM of a 152-SM GB300) the small-block variant is used
+constexpr int64_t kSmallGridBlocks = 4 * 152;
+
 __global__ void __launch_bounds__(256) tfsf_skip_kernel(TablesDev T, const PlaneWaveDev* pw, int n_pw, double t,
                                                         double* partial, unsigned int* ticket, int* skip)
 {
@@ -45,7 +57,13 @@ template <int P>
 cudaError_t launch_p(const TablesDev& T, const StageArgs& A, cudaStream_t s)
 {
     using O = Ord<P>;
-    dim3 grid(static_cast<unsigned>((T.K + O::EPB - 1) / O::EPB), static_cast<unsigned>(A.batch));
+    const int64_t blocks = (T.K + O::EPB - 1) / O::EPB;
+    if (blocks * A.batch < kSmallGridBlocks) {
+        dim3 grid(static_cast<unsigned>((T.K + O::EPB_SMALL - 1) / O::EPB_SMALL), static_cast<unsigned>(A.batch));
+        stage_fp64_small<P><<<grid, O::BLOCK_SMALL, 0, s>>>(T, A);
+        return cudaGetLastError();
+    }
+    dim3 grid(static_cast<unsigned>(blocks), static_cast<unsigned>(A.batch));
     stage_fp64<P><<<grid, kBlock, 0, s>>>(T, A);
     return cudaGetLastError();
 }

@@ -221,23 +221,31 @@ int dgtd_op_set_contraction(dgtd_op* op, int32_t mode);
  * captures the graph. DGTD_ERR_UNSUPPORTED for the other forms. */
 int dgtd_op_set_graph_steps(dgtd_op* op, int32_t steps);
 
-/* Batched FP32 form: FP64 defect correction of the operator (no counterpart in the reference,
- * whose operator is FP64 throughout). Every `every` steps of dgtd_op_step (0: off, the default)
- * the state is unpacked, the plain FP64 form applies the operator to it, and the difference
- * c = L64(x) - L32(x_hi) from this form's product of the same state is kept (bf16, one state
- * block). Every RK stage then adds c to its right-hand side, so a field that changes little
- * between refreshes (a static remainder, a slowly varying mode) is advanced with the FP64
- * operator's right-hand side instead of accumulating the FP32 rounding of it step after step.
+/* Batched FP32 form, classical RK4: FP64 defect correction of the operator (no counterpart in
+ * the reference, whose operator is FP64 throughout). Every `every` steps of dgtd_op_step (0: off,
+ * the default) the state is unpacked, the plain FP64 form applies the operator to it, and the
+ * difference c = L64(x) - L32(x_hi) from this form's product of the same state is formed (bf16,
+ * one state block). c is kept where the state has stayed within 1e-3 (relative) of its value at
+ * the previous refresh: there the field stays put (a static remainder, a slowly varying mode) and
+ * its FP32 rounding would otherwise repeat step after step and accumulate into a drift; where the
+ * field moves, its rounding error is random from step to step and a stale c held for a whole
+ * refresh period would make it systematic, so c is left out. The first refresh of a trajectory
+ * therefore applies nothing. The operator is linear, so adding c to every stage's right-hand side
+ * adds, per step, the increment dt (1 + dtL/2 + (dtL)^2/6 + (dtL)^3/24) c: it is formed once per
+ * refresh and dt (three source-free FP32 products) and added to the state's low word after every
+ * step by an elementwise kernel; the stage kernels are unchanged.
  * The correction belongs to the trajectory being stepped: it is also refreshed at the first step
  * after this call, when dgtd_op_step is given another state buffer, after
- * dgtd_op_set_planewaves and at the start of dgtd_op_run_host, but not by dgtd_op_pack (a caller
- * that moves the state through the reference layout every step keeps it). A caller that loads an
- * unrelated state into the same buffer calls this function again; until then a stale correction
- * adds a forcing at the FP32 rounding level of the old state's right-hand side. Costs per
- * refresh: unpack, one FP64 product, pack and one FP32 product; in device memory two scratch
- * buffers of max(FP64 reference state, FP32 working state) bytes and the bf16 correction (half
- * an FP32 state block); in each stage one more 2-byte read per value. Mult does not add the
- * correction. DGTD_ERR_UNSUPPORTED for the other forms. */
+ * dgtd_op_set_planewaves and at the start of dgtd_op_run_host (these also forget the previous
+ * state), but not by dgtd_op_pack (a caller that moves the state through the reference layout
+ * every step keeps it). A caller that loads an unrelated state into the same buffer calls this
+ * function again; until then a stale correction adds a forcing at the FP32 rounding level of the
+ * old state's right-hand side. Costs per refresh: unpack, one FP64 product, pack and four FP32
+ * products; per step one elementwise pass (read x_lo and the bf16 increment, write x_lo); in
+ * device memory two scratch buffers of max(FP64 reference state, FP32 working state) bytes, one
+ * FP32 state block and two bf16 blocks. Steps run one at a time (no CUDA-graph replay). Mult does
+ * not add the correction. DGTD_ERR_UNSUPPORTED for the other forms, and from dgtd_op_step with
+ * DGTD_LSERK4 while the correction is on. */
 int dgtd_op_set_defect_correction(dgtd_op* op, int32_t every);
 
 /* Refreshes made by the defect correction since the operator was created (may be NULL). */

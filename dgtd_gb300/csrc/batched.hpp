@@ -124,10 +124,11 @@ public:
     // internal layout of one state block).
     // c = (ref_hi - l32) + ref_lo, where ref is a working state (pair) holding the FP64 operator's
     // product and l32 the hi block of this form's product of the state x (a working state), kept
-    // only where x_hi has stayed within 1e-3 (relative) of x_prev, its value at the previous
-    // refresh (x_prev is then overwritten with x_hi; NaN entries never match).
-    void build_correction(const float* ref_pair, const float* l32, const float* x, float* x_prev, uint16_t* c,
-                          cudaStream_t s);
+    // only where x_hi has stayed within 0.1 of the incidence's RMS value of x_prev, its value at
+    // the previous refresh (x_prev is then overwritten with x_hi; NaN entries never match).
+    // sumsq: Bpad doubles of device scratch.
+    void build_correction(const float* ref_pair, const float* l32, const float* x, float* x_prev, double* sumsq,
+                          uint16_t* c, cudaStream_t s);
     // inc = one classical RK4 step of size dt from the zero state under the constant forcing c,
     // with the source-free operator A: dt/6 (k1 + 2 k2 + 2 k3 + k4), k1 = c, k2 = A (dt/2 k1) + c,
     // k3 = A (dt/2 k2) + c, k4 = A (dt k3) + c. The operator is linear, so a step of

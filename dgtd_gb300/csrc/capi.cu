@@ -125,6 +125,7 @@ struct dgtd_op {
     void* defect_b = nullptr;
     uint16_t* defect_corr = nullptr;   // the applied correction c (bf16)
     float* defect_prev = nullptr;      // x_hi at the previous refresh (NaN: none)
+    double* defect_sumsq = nullptr;    // per-incidence sum of squares of the state (refresh scratch)
     uint16_t* defect_inc = nullptr;    // c's classical-RK4 step increment for dt = defect_inc_dt (bf16)
     double defect_inc_dt = 0.0;
     bool defect_inc_stale = true;
@@ -152,6 +153,8 @@ struct dgtd_op {
         if (defect_corr) cudaFree(defect_corr);
         if (defect_prev) cudaFree(defect_prev);
         if (defect_inc) cudaFree(defect_inc);
+        if (defect_sumsq) cudaFree(defect_sumsq);
+        defect_sumsq = nullptr;
         defect_a = defect_b = nullptr;
         defect_corr = defect_inc = nullptr;
         defect_prev = nullptr;
@@ -297,6 +300,8 @@ void defect_refresh(dgtd_op* op, float* d_work, double t, cudaStream_t s)
         ck(cudaMalloc(&op->defect_corr, static_cast<size_t>(L) * sizeof(uint16_t)), "cudaMalloc defect correction");
         ck(cudaMalloc(&op->defect_inc, static_cast<size_t>(L) * sizeof(uint16_t)), "cudaMalloc defect correction");
         ck(cudaMalloc(&op->defect_prev, static_cast<size_t>(L) * sizeof(float)), "cudaMalloc defect correction");
+        ck(cudaMalloc(&op->defect_sumsq, static_cast<size_t>(B.batch_padded()) * sizeof(double)),
+           "cudaMalloc defect correction");
         ck(cudaMemsetAsync(op->defect_prev, 0xff, static_cast<size_t>(L) * sizeof(float), s), "memset");
     }
     double* x64 = static_cast<double*>(op->defect_a);
@@ -311,7 +316,7 @@ void defect_refresh(dgtd_op* op, float* d_work, double t, cudaStream_t s)
     float* l32 = static_cast<float*>(op->defect_b);
     B.pack(l64, l64w, s);
     B.mult(d_work, l32, t, s);
-    B.build_correction(l64w, l32, d_work, op->defect_prev, op->defect_corr, s);
+    B.build_correction(l64w, l32, d_work, op->defect_prev, op->defect_sumsq, op->defect_corr, s);
     op->defect_state = d_work;
     op->defect_age = 0;
     op->defect_inc_stale = true;

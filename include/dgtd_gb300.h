@@ -225,8 +225,10 @@ int dgtd_op_set_graph_steps(dgtd_op* op, int32_t steps);
  * the reference, whose operator is FP64 throughout). Every `every` steps of dgtd_op_step (0: off,
  * the default) the state is unpacked, the plain FP64 form applies the operator to it, and the
  * difference c = L64(x) - L32(x_hi) from this form's product of the same state is formed (bf16,
- * one state block). c is kept where the state has stayed within 1e-3 (relative) of its value at
- * the previous refresh: there the field stays put (a static remainder, a slowly varying mode) and
+ * one state block). c is kept where the state has stayed within 0.1 of the incidence's RMS value
+ * of its value at the previous refresh: there the field stays put (a static remainder, a slowly
+ * varying mode; the scale is per incidence because a static field's drift builds up in components
+ * near zero, such as H beside a static E) and
  * its FP32 rounding would otherwise repeat step after step and accumulate into a drift; where the
  * field moves, its rounding error is random from step to step and a stale c held for a whole
  * refresh period would make it systematic, so c is left out. The first refresh of a trajectory

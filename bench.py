@@ -863,7 +863,7 @@ def main():
                          "(capacity)")
     ap.add_argument("--serving-serial", type=int, default=6, help="requests also run one at a time for comparison")
     ap.add_argument("--serving-precision", choices=["fp32", "fp64"], default="fp32")
-    ap.add_argument("--defect-every", type=int, default=250,
+    ap.add_argument("--defect-every", type=int, default=100,
                     help="batched form: refresh period (steps) of the FP64 defect correction (0: off)")
     ap.add_argument("--contraction", choices=["auto", "tc", "simt"], default="auto",
                     help="batched form: autotuned stage kernel (default), or force tensor cores / FP32 SIMT; "

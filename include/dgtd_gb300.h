@@ -206,10 +206,11 @@ int dgtd_op_stability_reset(dgtd_op* op);
 /* Largest state_len (reference-layout entries) dgtd_op_step_noalloc accepts. */
 int64_t dgtd_noalloc_max_state(void);
 
-/* Contraction path of the FP32 forms: 0 (default) = tensor cores (tcgen05, 3xTF32) where
- * supported, else FP32 SIMT; 1 = FP32 SIMT. Batched form: tensor cores for orders 1..4 with
+/* Contraction path of the FP32 forms: 0 = tensor cores (tcgen05, 3xTF32) where supported,
+ * else FP32 SIMT; 1 = FP32 SIMT. Batched form (default 0): tensor cores for orders 1..4 with
  * B padded to a multiple of 64 (work item: one element x 64 incidences). Single-instance
- * form: tensor cores for orders 1..6 (work item: 8 elements of one incidence; reference-
+ * form (default 1: its SIMT stage takes 0.91 x the tensor-core stage's time at p = 6 on
+ * GB300): tensor cores for orders 1..6 (work item: 8 elements of one incidence; reference-
  * element matrices as the A operand, fields and fluxes as the B operand, chain rule and curl
  * in FP32 in the epilogue). */
 int dgtd_op_set_contraction(dgtd_op* op, int32_t mode);

@@ -58,6 +58,8 @@ def test_f32_tc_mult_many_items_batch_ragged(torch_cuda, order):
     assert m.n_elements % 8 != 0 and 2 * (m.n_elements // 8) > 2 * 152   # work items over both incidences
     waves = [dict(WAVE, batch=0), dict(WAVE, propagation=[-0.2, 1.0, 0.4], polarization=[1.0, 0.2, 0.0], batch=1)]
     op = dg.Operator(m, order=order, precision=dg.FP32, batch=2)
+    assert not op.uses_tensor_cores          # the single-instance default is FP32 SIMT
+    op.set_contraction(0)
     assert op.uses_tensor_cores
     op.set_planewaves(waves)
     orc = po.Oracle.from_mesh(m, order)

@@ -277,11 +277,18 @@ __global__ void __launch_bounds__(256) tfsf_skip_f32(BatchedTables T, const Plan
 constexpr int kPackChunk = 64;
 constexpr int kPackRow = kPackChunk + 1;
 
-// elements per tile: as many as keep the tile (hi and lo) within 48 KB of shared memory, 1..8,
-// so that 4-6 blocks (32-48 warps) share an SM and keep enough loads in flight
-inline int pack_tile_elements(int Np) { return std::max(1, std::min(8, (48 * 1024) / (Np * kPackRow * 8))); }
+// Elements per tile, 1..8. Device memory on the reference side: tiles within 48 KB of shared
+// memory, so that 4-6 blocks (32-48 warps) share an SM and keep enough loads in flight. Pinned
+// host memory: tiles within 160 KB, for long contiguous runs per incidence row over the host
+// link (measured at p = 4, 64 incidences, 82,560 tets: host-side pack + unpack 90 ms per step
+// with 8-element tiles against 105 ms with 2-element tiles; device-side, the other way round).
+inline int pack_tile_elements(int Np, bool host)
+{
+    return std::max(1, std::min(8, ((host ? 160 : 48) * 1024) / (Np * kPackRow * 8)));
+}
+constexpr int kPackUnroll = 4;   // reference-side loads in flight per thread
 
-__global__ void __launch_bounds__(256) pack_kernel(const double* __restrict__ ref, float* __restrict__ st,
+__global__ void __launch_bounds__(1024) pack_kernel(const double* __restrict__ ref, float* __restrict__ st,
                                                    const int32_t* __restrict__ inv_perm, int64_t K, int Np, int B,
                                                    int Bp, int E)
 {
@@ -293,17 +300,29 @@ __global__ void __launch_bounds__(256) pack_kernel(const double* __restrict__ re
     const int64_t N = K * Np;
     const int rows = ne * Np;                       // tile rows of this block: (element, node)
     const int half = E * Np * kPackRow;
-    for (int q = threadIdx.x; q < kPackChunk * rows; q += blockDim.x) {
-        const int bb = q / rows, r = q - bb * rows;
-        const int b = b0 + bb;
-        float hi = 0.0f, lo = 0.0f;
-        if (b < B) {
-            const double v = ref[(static_cast<int64_t>(b) * 6 + c) * N + er0 * Np + r];
-            hi = static_cast<float>(v);
-            lo = static_cast<float>(v - static_cast<double>(hi));
+    const int total = kPackChunk * rows;
+    const int stride = blockDim.x;
+    for (int q0 = threadIdx.x; q0 < total; q0 += kPackUnroll * stride) {
+        double v[kPackUnroll];
+#pragma unroll
+        for (int u = 0; u < kPackUnroll; ++u) {   // all loads first: kPackUnroll in flight
+            const int q = q0 + u * stride;
+            v[u] = 0.0;
+            if (q < total) {
+                const int bb = q / rows, r = q - bb * rows;
+                if (b0 + bb < B) v[u] = ref[(static_cast<int64_t>(b0 + bb) * 6 + c) * N + er0 * Np + r];
+            }
         }
-        tile[r * kPackRow + bb] = hi;
-        tile[half + r * kPackRow + bb] = lo;
+#pragma unroll
+        for (int u = 0; u < kPackUnroll; ++u) {
+            const int q = q0 + u * stride;
+            if (q < total) {
+                const int bb = q / rows, r = q - bb * rows;
+                const float hi = static_cast<float>(v[u]);
+                tile[r * kPackRow + bb] = hi;
+                tile[half + r * kPackRow + bb] = static_cast<float>(v[u] - static_cast<double>(hi));
+            }
+        }
     }
     __syncthreads();
     const int64_t L = K * 6 * static_cast<int64_t>(Np) * Bp;   // x_lo block offset
@@ -318,7 +337,7 @@ __global__ void __launch_bounds__(256) pack_kernel(const double* __restrict__ re
     }
 }
 
-__global__ void __launch_bounds__(256) unpack_kernel(const float* __restrict__ st, double* __restrict__ ref,
+__global__ void __launch_bounds__(1024) unpack_kernel(const float* __restrict__ st, double* __restrict__ ref,
                                                      const int32_t* __restrict__ inv_perm, int64_t K, int Np, int B,
                                                      int Bp, int E)
 {
@@ -628,40 +647,41 @@ void BatchedOp::ensure_ws()
     ckb(cudaMalloc(&ws_, 3 * state_len_ * sizeof(float)), "cudaMalloc RK scratch");
 }
 
-void BatchedOp::pack(const double* d_ref, float* d_state, cudaStream_t s)
+void BatchedOp::pack(const double* d_ref, float* d_state, cudaStream_t s, bool ref_on_host)
 {
     // grid: tiles of E reference elements x 6 components x chunks of 64 incidences (Bpad is a
     // multiple of 32; a last chunk of 32 padded incidences is handled as b >= B)
-    const int E = pack_tile_elements(Np_);
+    const int E = pack_tile_elements(Np_, ref_on_host);
     const dim3 grid(static_cast<unsigned>((K_ + E - 1) / E), 6u,
                     static_cast<unsigned>((Bpad_ + kPackChunk - 1) / kPackChunk));
     const size_t smem = 2 * static_cast<size_t>(E) * Np_ * kPackRow * sizeof(float);
     static std::atomic<uint64_t> seen{0};
     if (first_use_on_device(seen)) {
-        ckb(cudaFuncSetAttribute(pack_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024),
+        ckb(cudaFuncSetAttribute(pack_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 164 * 1024),
             "pack smem attribute");
-        ckb(cudaFuncSetAttribute(unpack_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024),
+        ckb(cudaFuncSetAttribute(unpack_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 164 * 1024),
             "unpack smem attribute");
     }
-    pack_kernel<<<grid, 256, smem, s>>>(d_ref, d_state, inv_perm_, K_, Np_, B_, Bpad_, E);
+    // host side: one 146 KB tile per SM at p = 4, so 1024 threads keep more loads in flight
+    pack_kernel<<<grid, ref_on_host ? 1024 : 256, smem, s>>>(d_ref, d_state, inv_perm_, K_, Np_, B_, Bpad_, E);
     ckb(cudaGetLastError(), "pack kernel");
     ++launches_;
 }
 
-void BatchedOp::unpack(const float* d_state, double* d_ref, cudaStream_t s)
+void BatchedOp::unpack(const float* d_state, double* d_ref, cudaStream_t s, bool ref_on_host)
 {
-    const int E = pack_tile_elements(Np_);
+    const int E = pack_tile_elements(Np_, ref_on_host);
     const dim3 grid(static_cast<unsigned>((K_ + E - 1) / E), 6u,
                     static_cast<unsigned>((Bpad_ + kPackChunk - 1) / kPackChunk));
     const size_t smem = 2 * static_cast<size_t>(E) * Np_ * kPackRow * sizeof(float);
     static std::atomic<uint64_t> seen{0};
     if (first_use_on_device(seen)) {
-        ckb(cudaFuncSetAttribute(pack_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024),
+        ckb(cudaFuncSetAttribute(pack_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 164 * 1024),
             "pack smem attribute");
-        ckb(cudaFuncSetAttribute(unpack_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024),
+        ckb(cudaFuncSetAttribute(unpack_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 164 * 1024),
             "unpack smem attribute");
     }
-    unpack_kernel<<<grid, 256, smem, s>>>(d_state, d_ref, inv_perm_, K_, Np_, B_, Bpad_, E);
+    unpack_kernel<<<grid, ref_on_host ? 1024 : 256, smem, s>>>(d_state, d_ref, inv_perm_, K_, Np_, B_, Bpad_, E);
     ckb(cudaGetLastError(), "unpack kernel");
     ++launches_;
 }
@@ -691,14 +711,20 @@ void BatchedOp::mult(const float* d_in, float* d_out, double t, cudaStream_t s)
 // steps against 4.8e-6 without the correction)
 constexpr double kStillTol = 1e-1;
 
+// Grid (row blocks, Bp / 32), block (32, 8): a thread owns one incidence b (its tolerance is
+// computed once) and strides over the rows (element, component, node) of one state block.
 __global__ void __launch_bounds__(256) correction_kernel(const float* __restrict__ ref, const float* __restrict__ l32,
                                                        const float* __restrict__ x, float* __restrict__ x_prev,
                                                        const double* __restrict__ sumsq, double inv_rows, int Bp,
-                                                       uint16_t* __restrict__ c, int64_t L)
+                                                       uint16_t* __restrict__ c, int64_t rows)
 {
-    for (int64_t i = blockIdx.x * 256ll + threadIdx.x; i < L; i += static_cast<int64_t>(gridDim.x) * 256) {
+    const int b = blockIdx.y * 32 + threadIdx.x;
+    const float tol = static_cast<float>(kStillTol * sqrt(sumsq[b] * inv_rows));
+    const int64_t L = rows * Bp;
+    for (int64_t r = blockIdx.x * static_cast<int64_t>(blockDim.y) + threadIdx.y; r < rows;
+         r += static_cast<int64_t>(gridDim.x) * blockDim.y) {
+        const int64_t i = r * Bp + b;
         const float xv = x[i];
-        const float tol = static_cast<float>(kStillTol * sqrt(sumsq[i % Bp] * inv_rows));
         const bool still = fabsf(xv - x_prev[i]) <= tol;   // false for a NaN x_prev
         const float d = (ref[i] - l32[i]) + ref[L + i];
         c[i] = still ? __bfloat16_as_ushort(__float2bfloat16_rn(d)) : uint16_t(0);
@@ -747,8 +773,11 @@ void BatchedOp::build_correction(const float* ref_pair, const float* l32, const 
                                  double* sumsq, uint16_t* c, cudaStream_t s)
 {
     norm2(x, sumsq, s);
-    correction_kernel<<<stream_grid(), 256, 0, s>>>(ref_pair, l32, x, x_prev, sumsq,
-                                                    1.0 / static_cast<double>(K_ * 6 * Np_), Bpad_, c, state_len_);
+    const int64_t rows = K_ * 6 * Np_;
+    const dim3 grid(static_cast<unsigned>(std::max<int64_t>(1, std::min<int64_t>((rows + 7) / 8, 4ll * n_sm_))),
+                    static_cast<unsigned>(Bpad_ / 32));
+    correction_kernel<<<grid, dim3(32, 8), 0, s>>>(ref_pair, l32, x, x_prev, sumsq, 1.0 / static_cast<double>(rows),
+                                                   Bpad_, c, rows);
     ckb(cudaGetLastError(), "correction kernel");
     ++launches_;
 }

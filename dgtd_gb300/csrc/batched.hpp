@@ -103,8 +103,10 @@ public:
     const std::vector<int32_t>& inv_perm() const { return inv_perm_host_; }
 
     // reference layout (FP64, [b][c][e*Np+i]) <-> internal FP32 pair (x_hi = fl(x), x_lo = fl(x - x_hi))
-    void pack(const double* d_ref, float* d_state, cudaStream_t s);
-    void unpack(const float* d_state, double* d_ref, cudaStream_t s);
+    // ref_on_host: the reference-layout buffer is pinned host memory read or written over the
+    // host link (larger tiles: longer contiguous runs per incidence row)
+    void pack(const double* d_ref, float* d_state, cudaStream_t s, bool ref_on_host = false);
+    void unpack(const float* d_state, double* d_ref, cudaStream_t s, bool ref_on_host = false);
     void mult(const float* d_in, float* d_out, double t, cudaStream_t s);
     void step(float* d_state, double t0, double dt, int nsteps, int integrator, cudaStream_t s);
     void norm2(const float* d_state, double* d_out_dev, cudaStream_t s);

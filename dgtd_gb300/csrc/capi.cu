@@ -184,13 +184,14 @@ struct BatchedCount {
 // can address (the conversion kernel then reads or writes it over the host link, so the
 // host-device transfer and the layout conversion are one pass). Anything else (pageable host
 // memory) is rejected before a kernel could touch it.
-const void* device_view(const void* p)
+const void* device_view(const void* p, bool* on_host = nullptr)
 {
     cudaPointerAttributes a{};
     if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
         cudaGetLastError();
         throw std::invalid_argument("pack/unpack: cannot query the reference-layout buffer");
     }
+    if (on_host) *on_host = a.type == cudaMemoryTypeHost;
     if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) return p;
     if (a.type == cudaMemoryTypeHost && a.devicePointer != nullptr) return a.devicePointer;
     throw std::invalid_argument("pack/unpack: the reference-layout buffer must be device memory or pinned host "
@@ -698,10 +699,11 @@ int dgtd_op_pack(dgtd_op* op, const double* d_ref, void* d_work, void* stream)
     if (!op || !d_ref || !d_work) return fail(DGTD_ERR_INVALID, "NULL argument");
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     try {
-        d_ref = static_cast<const double*>(device_view(d_ref));
+        bool host = false;
+        d_ref = static_cast<const double*>(device_view(d_ref, &host));
         if (op->batched) {
             BatchedCount bc(op);
-            op->batched->pack(d_ref, static_cast<float*>(d_work), s);
+            op->batched->pack(d_ref, static_cast<float*>(d_work), s, host);
         } else if (op->precision == DGTD_FP32) {
             ck(dgtd::launch_convert_f64_to_f32(d_ref, static_cast<float*>(d_work), op->state_len, s), "pack kernel");
             g_launches.fetch_add(1, std::memory_order_relaxed);
@@ -721,10 +723,11 @@ int dgtd_op_unpack(dgtd_op* op, const void* d_work, double* d_ref, void* stream)
     if (!op || !d_ref || !d_work) return fail(DGTD_ERR_INVALID, "NULL argument");
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     try {
-        d_ref = static_cast<double*>(const_cast<void*>(device_view(d_ref)));
+        bool host = false;
+        d_ref = static_cast<double*>(const_cast<void*>(device_view(d_ref, &host)));
         if (op->batched) {
             BatchedCount bc(op);
-            op->batched->unpack(static_cast<const float*>(d_work), d_ref, s);
+            op->batched->unpack(static_cast<const float*>(d_work), d_ref, s, host);
         } else if (op->precision == DGTD_FP32) {
             ck(dgtd::launch_convert_f32_to_f64(static_cast<const float*>(d_work), d_ref, op->state_len, s), "unpack kernel");
             g_launches.fetch_add(1, std::memory_order_relaxed);

@@ -27,6 +27,7 @@
 #include <cmath>
 
 #include "kernels.hpp"
+#include "tc_common.cuh"
 
 namespace dgtd {
 namespace fp64 {
@@ -99,27 +100,86 @@ __device__ __forceinline__ void load6(const R* p, R* v)
     }
 }
 
-// EPB_: elements per block (0: Ord's default); the block has at least EPB_ * Np threads
-template <int P, typename R = double, int EPB_ = 0>
+// Bulk (TMA-engine) copy of `bytes` (multiple of 16, both addresses 16-byte aligned) from global
+// to shared memory, completing on the mbarrier's transaction count.
+__device__ __forceinline__ void bulk_to_shared(void* dst, const void* src, uint32_t bytes, uint64_t* bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     tc::smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(tc::smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void expect_bytes(uint64_t* bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(tc::smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+// Shared-memory copies of the operator matrices and of a block's face tables (the staged
+// variant of the FP64 stage): Dr, Ds, Dt and LIFT (transposed), and per element its face-partner
+// indices, face codes and face geometry. Every piece is a multiple of 16 bytes for P <= 3.
+template <int P, int EPB>
+struct StagedOps {
+    static constexpr int Np = (P + 1) * (P + 2) * (P + 3) / 6;
+    static constexpr int NF = 4 * (P + 1) * (P + 2) / 2;
+    double D[3 * Np * Np];
+    double L[NF * Np];
+    double fgeo[EPB * 16];
+    int32_t vmapP[EPB * NF];
+    int32_t fcode[EPB * 4];
+    uint64_t bar;
+};
+
+// EPB_: elements per block (0: Ord's default); the block has at least EPB_ * Np threads.
+// STAGE (FP64, P <= 3): the operator matrices and the block's face tables are brought into
+// shared memory by bulk copies issued by one thread on one mbarrier (bounded wait; on expiry the
+// block reads them from global memory instead), and a face node whose partner lies in the same
+// block reads the partner's values from the block's staged fields instead of global memory.
+// The arithmetic and its order are unchanged, so results are bit-identical to STAGE = false.
+template <int P, typename R = double, int EPB_ = 0, bool STAGE = false>
 __device__ __forceinline__ void stage_body(const TablesT<R>& T, const StageArgsT<R>& A, int64_t e0, int b)
 {
     using O = Ord<P, R>;
     constexpr int Np = O::Np, Nfp = O::Nfp, NF = O::NF, EPB = EPB_ > 0 ? EPB_ : O::EPB;
     constexpr int S = Node6<R>::S;
+    static_assert(!STAGE || (P <= 3 && sizeof(R) == 8), "staged operators: FP64, orders 1-3");
     __shared__ __align__(16) R s_u[EPB * Np * S];     // [node][component]
     __shared__ __align__(16) R s_f[EPB * NF * S];     // [face node][component]
     __shared__ int s_fmask[4 * Nfp];
+    __shared__ __align__(16) StagedOps<STAGE ? P : 1, STAGE ? EPB : 1> s_ops;
 
     const int tid = threadIdx.x;
     const int64_t N = T.N;
     const R* __restrict__ in = A.in + static_cast<int64_t>(b) * 6 * N;
     const int nel = (T.K - e0) < EPB ? static_cast<int>(T.K - e0) : EPB;
 
+    if (STAGE && tid == 0) {
+        tc::mbar_init(&s_ops.bar, 1);
+        tc::mbar_fence_init();
+        const uint32_t dbytes = Np * Np * 8, lbytes = NF * Np * 8;
+        const uint32_t vbytes = nel * NF * 4, cbytes = nel * 16, gbytes = nel * 128;
+        expect_bytes(&s_ops.bar, 3 * dbytes + lbytes + vbytes + cbytes + gbytes);
+        bulk_to_shared(s_ops.D, T.DrT, dbytes, &s_ops.bar);
+        bulk_to_shared(s_ops.D + Np * Np, T.DsT, dbytes, &s_ops.bar);
+        bulk_to_shared(s_ops.D + 2 * Np * Np, T.DtT, dbytes, &s_ops.bar);
+        bulk_to_shared(s_ops.L, T.LIFTT, lbytes, &s_ops.bar);
+        bulk_to_shared(s_ops.vmapP, T.vmapP + e0 * NF, vbytes, &s_ops.bar);
+        bulk_to_shared(s_ops.fcode, T.fcode + e0 * 4, cbytes, &s_ops.bar);
+        bulk_to_shared(s_ops.fgeo, T.fgeo + e0 * 16, gbytes, &s_ops.bar);
+    }
     for (int i = tid; i < 4 * Nfp; i += blockDim.x) s_fmask[i] = T.Fmask[i];
     // coalesced load of the block's fields
     for (int c = 0; c < 6; ++c)
         for (int i = tid; i < nel * Np; i += blockDim.x) s_u[i * S + c] = in[c * N + e0 * Np + i];
     __syncthreads();
+    const bool staged = STAGE && tc::mbar_wait(&s_ops.bar, 0);
+    if (STAGE && !staged) tc::mbar_wait(&s_ops.bar, 0);   // copies still in flight: a second bounded
+                                                          // wait before the tables are read from global
+    // the block's face tables, indexed by the element's position el in the block
+    const int32_t* __restrict__ vmapP = staged ? s_ops.vmapP : T.vmapP + e0 * NF;
+    const int32_t* __restrict__ fcode = staged ? s_ops.fcode : T.fcode + e0 * 4;
+    const R* __restrict__ fgeo = staged ? reinterpret_cast<const R*>(s_ops.fgeo) : T.fgeo + e0 * 16;
 
     // ---- face fluxes -----------------------------------------------------------
     const bool skip_src = (A.skip != nullptr) && A.skip[b];
@@ -127,18 +187,26 @@ __device__ __forceinline__ void stage_body(const TablesT<R>& T, const StageArgsT
         const int el = w / NF, fn = w - el * NF, f = fn / Nfp, a = fn - f * Nfp;
         const int64_t e = e0 + el;
         const int vm = s_fmask[f * Nfp + a];
-        const int code = T.fcode[e * 4 + f];
-        const R* fg = T.fgeo + e * 16 + f * 4;
+        const int code = fcode[el * 4 + f];
+        const R* fg = fgeo + el * 16 + f * 4;
         const R nx = fg[0], ny = fg[1], nz = fg[2], fs = fg[3];
         R uM[6], dE[3], dH[3];
         load6(s_u + (el * Np + vm) * S, uM);
         R aE = T.alpha, aH = T.alpha;
         if (code == 0 || code == 4 || code == 5) {
-            const int64_t gp = T.vmapP[(e * 4 + f) * Nfp + a];
+            const int64_t gp = vmapP[(el * 4 + f) * Nfp + a];
+            const int64_t lp = gp - e0 * Np;           // partner node within the block's elements
+            if (STAGE && lp >= 0 && lp < nel * Np) {
+                R uP[6];
+                load6(s_u + lp * S, uP);
 #pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                dE[c] = __ldg(in + c * N + gp) - uM[c];
-                dH[c] = __ldg(in + (c + 3) * N + gp) - uM[c + 3];
+                for (int c = 0; c < 3; ++c) { dE[c] = uP[c] - uM[c]; dH[c] = uP[c + 3] - uM[c + 3]; }
+            } else {
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    dE[c] = __ldg(in + c * N + gp) - uM[c];
+                    dH[c] = __ldg(in + (c + 3) * N + gp) - uM[c + 3];
+                }
             }
             if (code != 0 && !skip_src) {
                 const int64_t gm = e * Np + vm;
@@ -182,12 +250,17 @@ __device__ __forceinline__ void stage_body(const TablesT<R>& T, const StageArgsT
     R ar[6], as[6], at[6];
 #pragma unroll
     for (int c = 0; c < 6; ++c) { ar[c] = R(0); as[c] = R(0); at[c] = R(0); }
-    const R* __restrict__ DrT = T.DrT;
-    const R* __restrict__ DsT = T.DsT;
-    const R* __restrict__ DtT = T.DtT;
+    // operator entries: staged copies in shared memory, else the read-only cache
+    auto op_ld = [&](const R* p) -> R {
+        if (STAGE) return *p;
+        return __ldg(p);
+    };
+    const R* __restrict__ DrT = staged ? reinterpret_cast<const R*>(s_ops.D) : T.DrT;
+    const R* __restrict__ DsT = staged ? reinterpret_cast<const R*>(s_ops.D) + Np * Np : T.DsT;
+    const R* __restrict__ DtT = staged ? reinterpret_cast<const R*>(s_ops.D) + 2 * Np * Np : T.DtT;
 #pragma unroll 4
     for (int j = 0; j < Np; ++j) {
-        const R dr = __ldg(DrT + j * Np + i), ds = __ldg(DsT + j * Np + i), dt = __ldg(DtT + j * Np + i);
+        const R dr = op_ld(DrT + j * Np + i), ds = op_ld(DsT + j * Np + i), dt = op_ld(DtT + j * Np + i);
         R uj[6];
         load6(s_u + (el * Np + j) * S, uj);
 #pragma unroll
@@ -200,10 +273,10 @@ __device__ __forceinline__ void stage_body(const TablesT<R>& T, const StageArgsT
     R lf[6];
 #pragma unroll
     for (int c = 0; c < 6; ++c) lf[c] = R(0);
-    const R* __restrict__ LT = T.LIFTT;
+    const R* __restrict__ LT = staged ? reinterpret_cast<const R*>(s_ops.L) : T.LIFTT;
 #pragma unroll 4
     for (int m = 0; m < NF; ++m) {
-        const R L = __ldg(LT + m * Np + i);
+        const R L = op_ld(LT + m * Np + i);
         R fm[6];
         load6(s_f + (el * NF + m) * S, fm);
 #pragma unroll

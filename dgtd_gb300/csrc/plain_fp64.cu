@@ -21,11 +21,14 @@ __global__ void __launch_bounds__(kBlock) stage_fp64(TablesDev T, StageArgs A)
 
 // Small meshes: blocks of about 64 threads, so that the grid spreads over every SM evenly
 // (3,072 tets at p = 3 give 256 blocks of 240 threads, 0.56 waves, but 1,024 of 60).
+// Orders 1-3 run the staged body (operators and face tables brought into shared memory by bulk
+// copies, in-block face partners read from shared memory); it fits the static shared-memory limit
+// with these small blocks.
 template <int P>
 __global__ void __launch_bounds__(Ord<P>::BLOCK_SMALL) stage_fp64_small(TablesDev T, StageArgs A)
 {
-    fp64::stage_body<P, double, Ord<P>::EPB_SMALL>(T, A, static_cast<int64_t>(blockIdx.x) * Ord<P>::EPB_SMALL,
-                                                   static_cast<int>(blockIdx.y));
+    fp64::stage_body<P, double, Ord<P>::EPB_SMALL, (P <= 3)>(T, A, static_cast<int64_t>(blockIdx.x) * Ord<P>::EPB_SMALL,
+                                                             static_cast<int>(blockIdx.y));
 }
 
 // below this many default blocks (4 per SM of a 152-SM GB300) the small-block variant is used

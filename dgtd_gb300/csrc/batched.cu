@@ -281,14 +281,15 @@ constexpr int kPackRow = kPackChunk + 1;
 // memory, so that 4-6 blocks (32-48 warps) share an SM and keep enough loads in flight. Pinned
 // host memory: tiles within 160 KB, for long contiguous runs per incidence row over the host
 // link (measured at p = 4, 64 incidences, 82,560 tets: host-side pack + unpack 90 ms per step
-// with 8-element tiles against 105 ms with 2-element tiles; device-side, the other way round).
+// with 8-element tiles against 105 ms with 2-element tiles; device-side, the other way round;
+// 1024 instead of 256 threads per block changed nothing on the host side).
 inline int pack_tile_elements(int Np, bool host)
 {
     return std::max(1, std::min(8, ((host ? 160 : 48) * 1024) / (Np * kPackRow * 8)));
 }
 constexpr int kPackUnroll = 4;   // reference-side loads in flight per thread
 
-__global__ void __launch_bounds__(1024) pack_kernel(const double* __restrict__ ref, float* __restrict__ st,
+__global__ void __launch_bounds__(256) pack_kernel(const double* __restrict__ ref, float* __restrict__ st,
                                                    const int32_t* __restrict__ inv_perm, int64_t K, int Np, int B,
                                                    int Bp, int E)
 {
@@ -337,7 +338,7 @@ __global__ void __launch_bounds__(1024) pack_kernel(const double* __restrict__ r
     }
 }
 
-__global__ void __launch_bounds__(1024) unpack_kernel(const float* __restrict__ st, double* __restrict__ ref,
+__global__ void __launch_bounds__(256) unpack_kernel(const float* __restrict__ st, double* __restrict__ ref,
                                                      const int32_t* __restrict__ inv_perm, int64_t K, int Np, int B,
                                                      int Bp, int E)
 {
@@ -662,8 +663,7 @@ void BatchedOp::pack(const double* d_ref, float* d_state, cudaStream_t s, bool r
         ckb(cudaFuncSetAttribute(unpack_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 164 * 1024),
             "unpack smem attribute");
     }
-    // host side: one 146 KB tile per SM at p = 4, so 1024 threads keep more loads in flight
-    pack_kernel<<<grid, ref_on_host ? 1024 : 256, smem, s>>>(d_ref, d_state, inv_perm_, K_, Np_, B_, Bpad_, E);
+    pack_kernel<<<grid, 256, smem, s>>>(d_ref, d_state, inv_perm_, K_, Np_, B_, Bpad_, E);
     ckb(cudaGetLastError(), "pack kernel");
     ++launches_;
 }
@@ -681,7 +681,7 @@ void BatchedOp::unpack(const float* d_state, double* d_ref, cudaStream_t s, bool
         ckb(cudaFuncSetAttribute(unpack_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 164 * 1024),
             "unpack smem attribute");
     }
-    unpack_kernel<<<grid, ref_on_host ? 1024 : 256, smem, s>>>(d_state, d_ref, inv_perm_, K_, Np_, B_, Bpad_, E);
+    unpack_kernel<<<grid, 256, smem, s>>>(d_state, d_ref, inv_perm_, K_, Np_, B_, Bpad_, E);
     ckb(cudaGetLastError(), "unpack kernel");
     ++launches_;
 }
@@ -755,12 +755,20 @@ __global__ void __launch_bounds__(256) to_bf16_kernel(const float* __restrict__ 
 }
 
 // x_lo[i] += inc[i] (the pair (x_hi, x_lo) need not be normalised: the next compensated update
-// and unpack take x_hi + x_lo as the value)
-__global__ void __launch_bounds__(256) add_increment_kernel(float* __restrict__ xl, const uint16_t* __restrict__ inc,
-                                                          int64_t L)
+// and unpack take x_hi + x_lo as the value). Four values per thread and access (L is a multiple
+// of 32, both blocks 16-byte aligned).
+__global__ void __launch_bounds__(256) add_increment_kernel(float4* __restrict__ xl, const uint2* __restrict__ inc,
+                                                          int64_t L4)
 {
-    for (int64_t i = blockIdx.x * 256ll + threadIdx.x; i < L; i += static_cast<int64_t>(gridDim.x) * 256)
-        xl[i] += bf16_bits_to_float(inc[i]);
+    for (int64_t i = blockIdx.x * 256ll + threadIdx.x; i < L4; i += static_cast<int64_t>(gridDim.x) * 256) {
+        float4 v = xl[i];
+        const uint2 h = inc[i];
+        v.x += __uint_as_float(h.x << 16);
+        v.y += __uint_as_float(h.x & 0xffff0000u);
+        v.z += __uint_as_float(h.y << 16);
+        v.w += __uint_as_float(h.y & 0xffff0000u);
+        xl[i] = v;
+    }
 }
 
 unsigned BatchedOp::stream_grid() const
@@ -813,7 +821,8 @@ void BatchedOp::build_increment(const uint16_t* c, float* scratch_a, float* scra
 
 void BatchedOp::add_increment(float* x, const uint16_t* inc, cudaStream_t s)
 {
-    add_increment_kernel<<<stream_grid(), 256, 0, s>>>(x + state_len_, inc, state_len_);
+    add_increment_kernel<<<stream_grid(), 256, 0, s>>>(reinterpret_cast<float4*>(x + state_len_),
+                                                       reinterpret_cast<const uint2*>(inc), state_len_ / 4);
     ckb(cudaGetLastError(), "add increment kernel");
     ++launches_;
 }

@@ -176,10 +176,6 @@ __device__ __forceinline__ void stage_body(const TablesT<R>& T, const StageArgsT
     const bool staged = STAGE && tc::mbar_wait(&s_ops.bar, 0);
     if (STAGE && !staged) tc::mbar_wait(&s_ops.bar, 0);   // copies still in flight: a second bounded
                                                           // wait before the tables are read from global
-    // the block's face tables, indexed by the element's position el in the block
-    const int32_t* __restrict__ vmapP = staged ? s_ops.vmapP : T.vmapP + e0 * NF;
-    const int32_t* __restrict__ fcode = staged ? s_ops.fcode : T.fcode + e0 * 4;
-    const R* __restrict__ fgeo = staged ? reinterpret_cast<const R*>(s_ops.fgeo) : T.fgeo + e0 * 16;
 
     // ---- face fluxes -----------------------------------------------------------
     const bool skip_src = (A.skip != nullptr) && A.skip[b];
@@ -187,14 +183,16 @@ __device__ __forceinline__ void stage_body(const TablesT<R>& T, const StageArgsT
         const int el = w / NF, fn = w - el * NF, f = fn / Nfp, a = fn - f * Nfp;
         const int64_t e = e0 + el;
         const int vm = s_fmask[f * Nfp + a];
-        const int code = fcode[el * 4 + f];
-        const R* fg = fgeo + el * 16 + f * 4;
+        // face tables: the block's staged copies (indexed by the element's position in the block)
+        // or global memory
+        const int code = staged ? s_ops.fcode[el * 4 + f] : T.fcode[e * 4 + f];
+        const R* fg = staged ? reinterpret_cast<const R*>(s_ops.fgeo) + el * 16 + f * 4 : T.fgeo + e * 16 + f * 4;
         const R nx = fg[0], ny = fg[1], nz = fg[2], fs = fg[3];
         R uM[6], dE[3], dH[3];
         load6(s_u + (el * Np + vm) * S, uM);
         R aE = T.alpha, aH = T.alpha;
         if (code == 0 || code == 4 || code == 5) {
-            const int64_t gp = vmapP[(el * 4 + f) * Nfp + a];
+            const int64_t gp = staged ? s_ops.vmapP[(el * 4 + f) * Nfp + a] : T.vmapP[(e * 4 + f) * Nfp + a];
             const int64_t lp = gp - e0 * Np;           // partner node within the block's elements
             if (STAGE && lp >= 0 && lp < nel * Np) {
                 R uP[6];

@@ -263,7 +263,8 @@ int dgtd_op_defect_refreshes(const dgtd_op* op, int64_t* refreshes);
  * element count) for the process. DGTD_ERR_UNSUPPORTED for the other forms. */
 int dgtd_op_autotune(dgtd_op* op, const void* d_work, void* stream, double* h_ms, int32_t* choice);
 
-/* 1 when the FP32 batched form runs its contractions on the tensor cores, else 0. */
+/* 1 when an FP32 form (batched or single-instance) runs its contractions on the tensor cores
+ * with the current contraction setting, else 0. */
 int dgtd_op_uses_tensor_cores(const dgtd_op* op);
 
 /* Synchronise the stream and report device-side failures of earlier calls

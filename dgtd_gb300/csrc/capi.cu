@@ -129,6 +129,7 @@ struct dgtd_op {
     uint16_t* defect_inc = nullptr;    // c's classical-RK4 step increment for dt = defect_inc_dt (bf16)
     double defect_inc_dt = 0.0;
     bool defect_inc_stale = true;
+    bool defect_prev_reset = true;     // clear defect_prev before the next refresh
     // point probes / DFT accumulators, sampled by dgtd_op_step every probes->every() steps
     std::unique_ptr<dgtd::ProbeSet> probes;
     int64_t probe_steps = 0;
@@ -294,16 +295,26 @@ void defect_refresh(dgtd_op* op, float* d_work, double t, cudaStream_t s)
     dgtd::BatchedOp& B = *op->batched;
     const int64_t L = B.state_len();
     if (!op->defect_a) {
+        // all buffers or none: a failed allocation leaves the operator without any
         const size_t bytes = std::max(static_cast<size_t>(op->state_len) * sizeof(double),
                                       static_cast<size_t>(B.work_len()) * sizeof(float));
-        ck(cudaMalloc(&op->defect_a, bytes), "cudaMalloc defect-correction scratch");
-        ck(cudaMalloc(&op->defect_b, bytes), "cudaMalloc defect-correction scratch");
-        ck(cudaMalloc(&op->defect_corr, static_cast<size_t>(L) * sizeof(uint16_t)), "cudaMalloc defect correction");
-        ck(cudaMalloc(&op->defect_inc, static_cast<size_t>(L) * sizeof(uint16_t)), "cudaMalloc defect correction");
-        ck(cudaMalloc(&op->defect_prev, static_cast<size_t>(L) * sizeof(float)), "cudaMalloc defect correction");
-        ck(cudaMalloc(&op->defect_sumsq, static_cast<size_t>(B.batch_padded()) * sizeof(double)),
-           "cudaMalloc defect correction");
+        try {
+            ck(cudaMalloc(&op->defect_a, bytes), "cudaMalloc defect-correction scratch");
+            ck(cudaMalloc(&op->defect_b, bytes), "cudaMalloc defect-correction scratch");
+            ck(cudaMalloc(&op->defect_corr, static_cast<size_t>(L) * sizeof(uint16_t)), "cudaMalloc defect correction");
+            ck(cudaMalloc(&op->defect_inc, static_cast<size_t>(L) * sizeof(uint16_t)), "cudaMalloc defect correction");
+            ck(cudaMalloc(&op->defect_prev, static_cast<size_t>(L) * sizeof(float)), "cudaMalloc defect correction");
+            ck(cudaMalloc(&op->defect_sumsq, static_cast<size_t>(B.batch_padded()) * sizeof(double)),
+               "cudaMalloc defect correction");
+        } catch (...) {
+            op->free_defect_buffers();
+            throw;
+        }
+        op->defect_prev_reset = true;
+    }
+    if (op->defect_prev_reset) {   // no earlier state to compare with: NaN never matches
         ck(cudaMemsetAsync(op->defect_prev, 0xff, static_cast<size_t>(L) * sizeof(float), s), "memset");
+        op->defect_prev_reset = false;
     }
     double* x64 = static_cast<double*>(op->defect_a);
     double* l64 = static_cast<double*>(op->defect_b);
@@ -324,14 +335,13 @@ void defect_refresh(dgtd_op* op, float* d_work, double t, cudaStream_t s)
     ++op->defect_refreshes;
 }
 
-// A new trajectory: refresh at the next step, with no earlier state to compare with.
+// A new trajectory: refresh at the next step, with no earlier state to compare with (the
+// previous-state buffer is reset on the refresh's own stream).
 void defect_restart(dgtd_op* op)
 {
     op->defect_state = nullptr;
     op->defect_age = 0;
-    if (op->defect_prev && op->batched)
-        ck(cudaMemset(op->defect_prev, 0xff, static_cast<size_t>(op->batched->state_len()) * sizeof(float)),
-           "memset");
+    op->defect_prev_reset = true;
 }
 
 // nsteps steps of the batched form; with the defect correction on, one step at a time, each

@@ -1,6 +1,6 @@
 """Batched FP32 form (B incidences on one mesh) against the FP64 oracle / FP64 GPU form.
 
-Bar (the benchmark spec): relative L2 <= 1e-5 against FP64 per incidence, stated for
+Bar: relative L2 <= 1e-5 against FP64 per incidence, stated for
 every result; a single RHS evaluation is checked tighter (FP32 rounding only).
 """
 import numpy as np

@@ -5,6 +5,7 @@
 #include <array>
 #include <cctype>
 #include <cmath>
+#include <cstdio>
 #include <cstdlib>
 #include <fstream>
 #include <set>
@@ -168,6 +169,39 @@ Json parse_json(const std::string& text)
 }
 
 // ============================================================================ gmsh 2.2
+namespace {
+
+// Second-order elements whose edge nodes sit within this distance of their straight edges' midpoints
+// are straight (the reference's tolerance for its curved-element test).
+constexpr double kCurvedTol = 1e-5;
+
+// Largest distance from an edge node to the nearest midpoint of the element's straight edges
+// (v: nc corner nodes, then nm edge nodes, indices into xyz). A second-order element with all its
+// edge nodes on midpoints has an affine geometry map.
+double edge_node_deviation(const std::vector<double>& xyz, const int32_t* v, int nc, int nm)
+{
+    double worst = 0.0;
+    for (int k = 0; k < nm; ++k) {
+        const double* xm = &xyz[3 * static_cast<size_t>(v[nc + k])];
+        double best = INFINITY;
+        for (int a = 0; a < nc; ++a)
+            for (int b = a + 1; b < nc; ++b) {
+                const double* xa = &xyz[3 * static_cast<size_t>(v[a])];
+                const double* xb = &xyz[3 * static_cast<size_t>(v[b])];
+                double d2 = 0.0;
+                for (int r = 0; r < 3; ++r) {
+                    const double d = xm[r] - 0.5 * (xa[r] + xb[r]);
+                    d2 += d * d;
+                }
+                best = std::min(best, std::sqrt(d2));
+            }
+        worst = std::max(worst, best);
+    }
+    return worst;
+}
+
+}  // namespace
+
 GmshMesh read_gmsh22(const std::string& path)
 {
     std::ifstream f(path);
@@ -176,6 +210,9 @@ GmshMesh read_gmsh22(const std::string& path)
     std::map<long, int32_t> node_index;
     std::string line;
     bool have_format = false, have_nodes = false;
+    long curved = 0;          // second-order elements whose edge nodes are off the straight edges
+    double max_dev = 0.0;
+    bool second_order = false;
     while (std::getline(f, line)) {
         if (line.rfind("$MeshFormat", 0) == 0) {
             std::getline(f, line);
@@ -229,8 +266,28 @@ GmshMesh read_gmsh22(const std::string& path)
                     auto v = nodes(3);
                     m.tris.insert(m.tris.end(), v.begin(), v.end());
                     m.tri_tag.push_back(phys);
-                } else if (type == 11 || type == 29 || type == 9 || type == 20 || type == 21) {
-                    throw std::runtime_error(path + ": curved (high-order) elements are not supported");
+                } else if (type == 11 || type == 9) {
+                    // second-order tetrahedron (10 nodes) / triangle (6 nodes): corners first, then one
+                    // node per edge. Straight when every edge node lies on the midpoint of one of the
+                    // element's edges (the reference's curved-element test, HesthavenEvolution.cpp:207-241,
+                    // with its absolute tolerance 1e-5); straight elements load as linear ones.
+                    const int nc = (type == 11) ? 4 : 3;
+                    auto v = nodes(type == 11 ? 10 : 6);
+                    second_order = true;
+                    const double dev = edge_node_deviation(m.xyz, v.data(), nc, static_cast<int>(v.size()) - nc);
+                    if (dev > kCurvedTol) {
+                        ++curved;
+                        max_dev = std::max(max_dev, dev);
+                    }
+                    if (type == 11) {
+                        m.tets.insert(m.tets.end(), v.begin(), v.begin() + 4);
+                        m.tet_tag.push_back(phys);
+                    } else {
+                        m.tris.insert(m.tris.end(), v.begin(), v.begin() + 3);
+                        m.tri_tag.push_back(phys);
+                    }
+                } else if (type == 29 || type == 20 || type == 21) {
+                    throw std::runtime_error(path + ": third-order (curved) elements are not supported");
                 } else if (type == 15 || type == 1 || type == 8 || type == 26 || type == 27 || type == 28) {
                     // points and lines: not part of a tetrahedral model
                 } else {
@@ -241,6 +298,28 @@ GmshMesh read_gmsh22(const std::string& path)
     }
     if (!have_format) throw std::runtime_error(path + ": no $MeshFormat section");
     if (m.tets.empty()) throw std::runtime_error(path + ": no tetrahedra (only 3D meshes are supported)");
+    if (second_order) {
+        // keep only the corner nodes the (linear) elements use, in their original order
+        std::vector<int32_t> remap(m.xyz.size() / 3, -1);
+        for (int32_t v : m.tets) remap[v] = 0;
+        for (int32_t v : m.tris) remap[v] = 0;
+        std::vector<double> xyz;
+        for (size_t k = 0; k < remap.size(); ++k)
+            if (remap[k] == 0) {
+                remap[k] = static_cast<int32_t>(xyz.size() / 3);
+                xyz.insert(xyz.end(), m.xyz.begin() + 3 * k, m.xyz.begin() + 3 * k + 3);
+            }
+        for (auto& v : m.tets) v = remap[v];
+        for (auto& v : m.tris) v = remap[v];
+        m.xyz.swap(xyz);
+    }
+    if (curved > 0) {
+        char buf[160];
+        std::snprintf(buf, sizeof(buf), ": %ld second-order elements are curved (edge nodes up to %.3g off the straight "
+                                        "edges): curved geometry is not supported",
+                      curved, max_dev);
+        throw std::runtime_error(path + buf);
+    }
     return m;
 }
 

@@ -108,3 +108,79 @@ def test_reference_cases_load(name):
     m = c.mesh()
     assert m.n_elements > 0 and c.info["order"] >= 1
     dg.validate_mesh(m, order=1)
+
+
+def _second_order_copy(src: Path, dst: Path, bump: float = 0.0) -> None:
+    """Rewrite a linear gmsh 2.2 mesh with second-order elements: a node at every edge midpoint
+    (shared by the elements of the edge), tetrahedra as type 11, triangles as type 9. bump > 0
+    moves the first edge node off its edge by that distance."""
+    lines = src.read_text().splitlines()
+    i = lines.index("$Nodes")
+    n = int(lines[i + 1])
+    nodes = {}
+    for ln in lines[i + 2:i + 2 + n]:
+        k, x, y, z = ln.split()
+        nodes[int(k)] = np.array([float(x), float(y), float(z)])
+    j = lines.index("$Elements")
+    ne = int(lines[j + 1])
+    mids, elems = {}, []
+    next_id = max(nodes) + 1
+
+    def mid(a, b):
+        nonlocal next_id
+        key = (min(a, b), max(a, b))
+        if key not in mids:
+            mids[key] = next_id
+            nodes[next_id] = 0.5 * (nodes[a] + nodes[b])
+            next_id += 1
+        return mids[key]
+
+    for ln in lines[j + 2:j + 2 + ne]:
+        f = [int(v) for v in ln.split()]
+        eid, typ, ntag = f[0], f[1], f[2]
+        tags, vs = f[3:3 + ntag], f[3 + ntag:]
+        if typ == 4:
+            a, b, c, d = vs
+            extra = [mid(a, b), mid(b, c), mid(a, c), mid(a, d), mid(c, d), mid(b, d)]
+            elems.append((eid, 11, tags, vs + extra))
+        elif typ == 2:
+            a, b, c = vs
+            elems.append((eid, 9, tags, vs + [mid(a, b), mid(b, c), mid(a, c)]))
+        else:
+            elems.append((eid, typ, tags, vs))
+    if bump:
+        first = next(iter(mids.values()))
+        nodes[first] = nodes[first] + np.array([bump, 0.0, 0.0])
+    out = ["$MeshFormat", "2.2 0 8", "$EndMeshFormat", "$Nodes", str(len(nodes))]
+    out += [f"{k} {float(v[0])!r} {float(v[1])!r} {float(v[2])!r}" for k, v in sorted(nodes.items())]
+    out += ["$EndNodes", "$Elements", str(len(elems))]
+    out += [" ".join(map(str, [e, t, len(g)] + g + v)) for e, t, g, v in elems]
+    out += ["$EndElements"]
+    dst.write_text("\n".join(out) + "\n")
+
+
+def test_straight_second_order_mesh_loads_as_linear(tmp_path):
+    """A second-order mesh whose edge nodes sit on the straight edges (the reference's
+    curved-element test: high-order nodes within 1e-5 of the linear positions) loads as its
+    linear elements: same tables as the linear mesh."""
+    _second_order_copy(CASES / "box_resonant.msh", tmp_path / "box_p2.msh")
+    (tmp_path / "box_p2.json").write_text(
+        (CASES / "box_resonant.json").read_text().replace("box_resonant.msh", "box_p2.msh"))
+    lin = dg.Case(CASES / "box_resonant.json")
+    quad = dg.Case(tmp_path / "box_p2.json")
+    ml, mq = lin.mesh(), quad.mesh()
+    assert quad.info["n_elements"] == lin.info["n_elements"]
+    assert np.array_equal(ml.vertices[ml.elements], mq.vertices[mq.elements])
+    assert {k: v for k, v in quad.info.items() if k != "mesh_path"} == \
+        {k: v for k, v in lin.info.items() if k != "mesh_path"}
+
+
+def test_curved_second_order_mesh_rejected(tmp_path):
+    _second_order_copy(CASES / "box_resonant.msh", tmp_path / "box_p2c.msh", bump=1e-3)
+    (tmp_path / "box_p2c.json").write_text(
+        (CASES / "box_resonant.json").read_text().replace("box_resonant.msh", "box_p2c.msh"))
+    with pytest.raises(dg.DgtdError, match=r"second-order elements are curved .*curved geometry is not supported"):
+        dg.Case(tmp_path / "box_p2c.json")
+    # the reference's own curved case: its curved elements are counted and refused
+    with pytest.raises(dg.DgtdError, match=r"\d+ second-order elements are curved"):
+        dg.Case(REFERENCE_INPUTS / "3D_Curved_Element_Test" / "3D_Curved_Element_Test.json")

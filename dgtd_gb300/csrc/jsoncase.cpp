@@ -506,6 +506,11 @@ Case load_case(const std::string& json_path)
                 const double kh[3] = {w.propagation[0] / kn, w.propagation[1] / kn, w.propagation[2] / kn};
                 std::vector<int> tags = s.has("tags") ? int_list(s.at("tags")) : std::vector<int>();
                 if (const Json* m = mag.find("mean")) {
+                    // a position (the reference reads it with assemble3DVector, driver.cpp:346-353,
+                    // 574-575, which fails on a plain number as well)
+                    if (m->type != Json::Array)
+                        throw std::runtime_error("plane wave magnitude.mean must be a 3-vector (a position on "
+                                                 "the propagation axis), not a number");
                     double mv[3];
                     vec3(*m, mv);
                     w.mean = mv[0] * kh[0] + mv[1] * kh[1] + mv[2] * kh[2];

@@ -99,6 +99,14 @@ def test_rejects_unsupported_and_malformed(tmp_path):
     nomesh.write_text(src.replace("box_resonant.msh", "missing.msh"))
     with pytest.raises(dg.DgtdError, match="cannot open mesh"):
         dg.Case(nomesh)
+    # a plane wave's Gaussian mean is a position (the reference fails on a plain number too)
+    import json
+    tf = json.loads((CASES / "box_tfsf.json").read_text())
+    tf["sources"][0]["magnitude"]["mean"] = 5.0
+    (tmp_path / "box_tfsf.msh").write_text((CASES / "box_tfsf.msh").read_text())
+    (tmp_path / "scalar_mean.json").write_text(json.dumps(tf))
+    with pytest.raises(dg.DgtdError, match="magnitude.mean must be a 3-vector"):
+        dg.Case(tmp_path / "scalar_mean.json")
 
 
 @pytest.mark.parametrize("name", ["3D_PEC", "3D_TFSF", "3D_TFSF_InteriorPEC"])

@@ -1269,6 +1269,14 @@ int orc_ref_emat(int order, double* emat)
     return 0;
 }
 
+// Incident field of the operator's plane waves at point x and time t (E and H, 3 each), for
+// tests of the source definition (reference Planewave / Gaussian / ModulatedGaussian,
+// src/math/Function.h:45-143, 329-416).
+void orc_pw_eval(void* h, const double* x, double t, double* e, double* hf)
+{
+    orc::pw_at(*static_cast<orc::Oracle*>(h), x, t, e, hf);
+}
+
 // Gauss-Lobatto points on [0,1] (the 1D node set), for tests.
 int orc_lobatto(int p, double* out)
 {

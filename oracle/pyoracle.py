@@ -57,6 +57,7 @@ def lib() -> C.CDLL:
         h.orc_element_matrices.argtypes = [C.c_int, C.c_int, _D, _D, _D, _D, _D, _D]
         h.orc_ref_emat.restype = C.c_int; h.orc_ref_emat.argtypes = [C.c_int, _D]
         h.orc_lobatto.restype = C.c_int; h.orc_lobatto.argtypes = [C.c_int, _D]
+        h.orc_pw_eval.restype = None; h.orc_pw_eval.argtypes = [C.c_void_p, _D, C.c_double, _D, _D]
         h.orc_threads.restype = C.c_int
         h.orc_subop.restype = C.c_int
         h.orc_subop.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, _D]
@@ -128,6 +129,13 @@ class Oracle:
             prm[i, 0:3] = w["propagation"]; prm[i, 3:6] = w["polarization"]
             prm[i, 6] = w["spread"]; prm[i, 7] = w["mean"]; prm[i, 8] = w.get("frequency", 0.0)
         lib().orc_set_planewaves(self.h, len(waves), _d(prm))
+
+    def pw_eval(self, x, t: float):
+        """Incident (E, H) of the installed plane waves at point x (3) and time t."""
+        xx = np.ascontiguousarray(np.asarray(x, dtype=np.float64).reshape(3))
+        e, h = np.zeros(3), np.zeros(3)
+        lib().orc_pw_eval(self.h, _d(xx), float(t), _d(e), _d(h))
+        return e, h
 
     def _chk(self, rc):
         if rc != 0:

@@ -121,3 +121,38 @@ def test_node_set_gauss_lobatto(order):
     on_edge = np.isclose(R["s"], -1) & np.isclose(R["t"], -1)
     r = np.sort(R["r"][on_edge])
     assert np.allclose((r + 1) / 2, g, atol=1e-15)
+
+
+def _pw_oracle(waves):
+    """An oracle on one reference tetrahedron with the given plane waves installed (the source
+    evaluation does not depend on the mesh)."""
+    V = [[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1]]
+    o = po.Oracle(V, [[0, 1, 2, 3]], 1)
+    o.set_planewaves(waves)
+    return o
+
+
+def test_planewave_source_kats():
+    """The reference's SourcesTest.planewave (test/maxwell/solver/SourcesTest.cpp:18-36): a
+    Gaussian plane wave (spread 0.2, mean -1.5) polarised along y and travelling along x peaks
+    at (x = -1.5, t = 0) and at (x = 0, t = 1.5), and its H_z equals its E_y."""
+    o = _pw_oracle([dict(propagation=[1, 0, 0], polarization=[0, 1, 0], spread=0.2, mean=-1.5)])
+    e, _ = o.pw_eval([-1.5, 0, 0], 0.0)
+    assert abs(e[1] - 1.0) <= 1e-6
+    e, _ = o.pw_eval([0.0, 0, 0], 1.5)
+    assert abs(e[1] - 1.0) <= 1e-6
+    for x in np.arange(0.0, 3.0, 0.1):
+        e, h = o.pw_eval([x, 0, 0], 0.0)
+        assert abs(e[1] - h[2]) <= 1e-6
+
+
+def test_modulated_gaussian_kats():
+    """The reference's FunctionTest.ModulatedGaussian_atMean / _zeroCrossing
+    (test/maxwell/math/FunctionTest.cpp:81-102), as the plane wave's time profile: 1 at the
+    mean; 0 a quarter period from it under a wide envelope."""
+    o = _pw_oracle([dict(propagation=[1, 0, 0], polarization=[0, 0, 1], spread=0.2, mean=0.5, frequency=3.0)])
+    e, _ = o.pw_eval([0.5, 0, 0], 0.0)
+    assert e[2] == 1.0
+    o = _pw_oracle([dict(propagation=[1, 0, 0], polarization=[0, 0, 1], spread=10.0, mean=0.0, frequency=1.0)])
+    e, _ = o.pw_eval([0.25, 0, 0], 0.0)
+    assert abs(e[2]) <= 1e-10

@@ -410,6 +410,29 @@ double orient(const double* a, const double* b, const double* c, const double* d
     return u[0] * (v[1] * w[2] - v[2] * w[1]) - u[1] * (v[0] * w[2] - v[2] * w[0]) + u[2] * (v[0] * w[1] - v[1] * w[0]);
 }
 
+// The reference's case layout (validateCaseNamingStyle, driver.cpp:1487-1543): a folder named as
+// the case holding <case>.json and <case>.msh, and model.filename = "<case>.msh" with no path.
+void check_case_naming(const std::string& json_path, const Json& J, const std::string& dir, const std::string& name)
+{
+    const size_t dot = json_path.find_last_of('.');
+    if (dot == std::string::npos || json_path.substr(dot) != ".json")
+        throw std::runtime_error("input case file must be a .json file: " + json_path);
+    const Json* model = J.find("model");
+    const Json* fn = model ? model->find("filename") : nullptr;
+    if (!fn || fn->type != Json::String)
+        throw std::runtime_error("invalid JSON style in " + json_path + ": model.filename is required and must be a string");
+    const std::string folder = dir.substr(dir.find_last_of('/') == std::string::npos ? 0 : dir.find_last_of('/') + 1);
+    const std::string& filename = fn->string();
+    const std::string expected = name + ".msh";
+    const bool ok = folder == name && filename == expected && filename.find('/') == std::string::npos &&
+                    std::ifstream(dir + "/" + expected).good();
+    if (!ok)
+        throw std::runtime_error("invalid case naming style for " + json_path +
+                                 ": folder name, .json name, .msh name and model.filename must match (expected folder '" +
+                                 name + "', model.filename '" + expected + "'; found folder '" + folder +
+                                 "', model.filename '" + filename + "')");
+}
+
 }  // namespace
 
 Case load_case(const std::string& json_path)
@@ -422,6 +445,7 @@ Case load_case(const std::string& json_path)
     Case c;
     c.dir = dirname(json_path);
     c.name = stem(json_path);
+    check_case_naming(json_path, J, c.dir, c.name);
 
     // ---- solver options (driver.cpp:644-705)
     if (const Json* so = J.find("solver_options")) {

@@ -358,7 +358,10 @@ typedef struct dgtd_case_result {
                                     run goes on after a warning on stderr, as the reference's), or -1 */
 } dgtd_case_result;
 
-/* Read a case file and its mesh. */
+/* Read a case file and its mesh (reference driver::buildSolverJson, driver.cpp:1545, with its
+ * case layout, driver.cpp:1487-1543: <case>/<case>.json beside <case>/<case>.msh, and
+ * model.filename = "<case>.msh"; other layouts fail with DGTD_ERR_INVALID and a message naming
+ * what differs). */
 int dgtd_case_load(const char* json_path, dgtd_case** out);
 void dgtd_case_destroy(dgtd_case* c);
 int dgtd_case_get_info(const dgtd_case* c, dgtd_case_info* info);

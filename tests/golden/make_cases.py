@@ -1,4 +1,4 @@
-"""Writes the small JSON cases and gmsh 2.2 meshes under tests/golden/cases/.
+"""Writes the small JSON cases and gmsh 2.2 meshes under tests/golden/cases/<case>/.
 
 The cases follow the reference's case-file schema (solver_options / model /
 sources / probes, as read by driver::buildSolverJson) and are built from this
@@ -22,6 +22,14 @@ import numpy as np
 ROOT = Path(__file__).resolve().parents[2]
 sys.path.insert(0, str(ROOT))
 OUT = Path(__file__).resolve().parent / "cases"
+
+
+def case_dir(name: str) -> Path:
+    """<cases>/<name>/: the reference's case layout (a folder named as the case holding
+    <name>.json and <name>.msh)."""
+    d = OUT / name
+    d.mkdir(parents=True, exist_ok=True)
+    return d
 
 
 def write_msh(path, V, E, etag, F, ftag):
@@ -60,7 +68,7 @@ def main():
     # ---- box_resonant
     m = dg.box_mesh((3, 3, 3))
     tags = side_tags(m.vertices, m.bdr_faces, (0, 0, 0), (1, 1, 1))
-    write_msh(OUT / "box_resonant.msh", m.vertices, m.elements, [1] * m.n_elements, m.bdr_faces, tags)
+    write_msh(case_dir("box_resonant") / "box_resonant.msh", m.vertices, m.elements, [1] * m.n_elements, m.bdr_faces, tags)
     case = {
         "solver_options": {"upwind_alpha": 1.0, "time_step": 1e-2, "final_time": 0.3, "order": 2,
                            "evolution_operator": "global"},
@@ -72,7 +80,7 @@ def main():
         "sources": [{"type": "initial", "field_type": "electric", "polarization": [0.0, 0.0, 1.0],
                      "magnitude": {"type": "resonant", "modes": [1, 1]}}],
     }
-    (OUT / "box_resonant.json").write_text(json.dumps(case, indent=2) + "\n")
+    (case_dir("box_resonant") / "box_resonant.json").write_text(json.dumps(case, indent=2) + "\n")
 
     # ---- box_tfsf
     m = dg.box_mesh((4, 4, 4), lo=(-1, -1, -1), hi=(1, 1, 1), tfsf=((1, 1, 1), (3, 3, 3)), outer_bc=dg.BC_SMA)
@@ -80,7 +88,7 @@ def main():
     cen = m.vertices[m.elements].mean(axis=1)
     etag = [2 if np.all(np.abs(c) < 0.5) else 1 for c in cen]
     F = np.concatenate([m.bdr_faces, m.tfsf_faces[:, ::-1]])      # reversed: the file's winding carries no meaning
-    write_msh(OUT / "box_tfsf.msh", m.vertices, m.elements, etag, F, tags + [7] * len(m.tfsf_faces))
+    write_msh(case_dir("box_tfsf") / "box_tfsf.msh", m.vertices, m.elements, etag, F, tags + [7] * len(m.tfsf_faces))
     case = {
         "solver_options": {"upwind_alpha": 1.0, "time_step": 2e-2, "final_time": 0.4, "order": 2},
         "model": {"filename": "box_tfsf.msh",
@@ -91,14 +99,14 @@ def main():
         "sources": [{"type": "planewave", "polarization": [0.0, 0.0, 1.0], "propagation": [1.0, 0.0, 0.0],
                      "tags": [7], "magnitude": {"type": "gaussian", "spread": 0.2}}],
     }
-    (OUT / "box_tfsf.json").write_text(json.dumps(case, indent=2) + "\n")
+    (case_dir("box_tfsf") / "box_tfsf.json").write_text(json.dumps(case, indent=2) + "\n")
 
     # ---- box_dielectric
     m = dg.box_mesh((2, 2, 2))
     tags = side_tags(m.vertices, m.bdr_faces, (0, 0, 0), (1, 1, 1))
     cen = m.vertices[m.elements].mean(axis=1)
     etag = [3 if c[2] < 0.5 else 4 for c in cen]
-    write_msh(OUT / "box_dielectric.msh", m.vertices, m.elements, etag, m.bdr_faces, tags)
+    write_msh(case_dir("box_dielectric") / "box_dielectric.msh", m.vertices, m.elements, etag, m.bdr_faces, tags)
     case = {
         "solver_options": {"upwind_alpha": 0.5, "final_time": 0.1, "cfl": 0.5, "order": 3, "ode_type": "LSERK4"},
         "model": {"filename": "box_dielectric.msh", "refinement": 1,
@@ -110,7 +118,7 @@ def main():
                      "polarization": [1.0, 0.0, 0.0], "dimension": 3,
                      "magnitude": {"type": "gaussian", "spread": 0.2}}],
     }
-    (OUT / "box_dielectric.json").write_text(json.dumps(case, indent=2) + "\n")
+    (case_dir("box_dielectric") / "box_dielectric.json").write_text(json.dumps(case, indent=2) + "\n")
     print("wrote", sorted(p.name for p in OUT.iterdir()))
 
 

@@ -32,7 +32,7 @@ def operator_run(case):
 
 @pytest.mark.parametrize("name", ["box_resonant", "box_tfsf", "box_dielectric"])
 def test_case_run_matches_operator_and_oracle(torch_cuda, tmp_path, name):
-    case = dg.Case(CASES / f"{name}.json")
+    case = dg.Case(CASES / name / f"{name}.json")
     state, res = case.run(freqs=[0.5, 1.0], out_dir=tmp_path)
     m, op, x0, dt, ref, n = operator_run(case)
     assert res["steps"] == n and res["dt"] == dt
@@ -55,7 +55,7 @@ def test_case_run_matches_operator_and_oracle(torch_cuda, tmp_path, name):
 
 def test_resonant_case_probe_values(torch_cuda, tmp_path):
     """The probe at the cavity centre follows the TE110 mode: Ez(t) ~ cos(w t) with w = pi sqrt(2)."""
-    case = dg.Case(CASES / "box_resonant.json")
+    case = dg.Case(CASES / "box_resonant" / "box_resonant.json")
     _, res = case.run(out_dir=tmp_path, want_state=False)
     rows = np.loadtxt(tmp_path / "PointProbe0.dat")
     t, ez = rows[:, 0], rows[:, 3]

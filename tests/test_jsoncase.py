@@ -1,7 +1,7 @@
 """JSON-case front end on the host: the reference's case schema and gmsh 2.2 meshes
 read into the library's tables (no GPU needed).
 
-Fixtures: tests/golden/cases/ (written by tests/golden/make_cases.py from the
+Fixtures: tests/golden/cases/<case>/ (written by tests/golden/make_cases.py from the
 library's box mesher, so every expected count is known exactly).
 """
 from pathlib import Path
@@ -21,7 +21,7 @@ def orient(V, t):
 
 
 def test_resonant_case_tables():
-    c = dg.Case(CASES / "box_resonant.json")
+    c = dg.Case(CASES / "box_resonant" / "box_resonant.json")
     inf = c.info
     assert inf["order"] == 2 and inf["time_step"] == 1e-2 and inf["final_time"] == 0.3 and inf["alpha"] == 1.0
     assert inf["n_elements"] == 162 and inf["n_point_probes"] == 2 and inf["n_waves"] == 0
@@ -40,7 +40,7 @@ def test_resonant_case_tables():
 
 
 def test_tfsf_case_orientation_and_auto_delay():
-    c = dg.Case(CASES / "box_tfsf.json")
+    c = dg.Case(CASES / "box_tfsf" / "box_tfsf.json")
     m = c.mesh()
     assert (m.bdr_codes == dg.BC_SMA).sum() == 6 * 32
     nt = m.tfsf_faces.shape[0]
@@ -64,7 +64,7 @@ def test_tfsf_case_orientation_and_auto_delay():
 
 
 def test_refined_dielectric_case():
-    c = dg.Case(CASES / "box_dielectric.json")
+    c = dg.Case(CASES / "box_dielectric" / "box_dielectric.json")
     inf = c.info
     assert inf["n_elements"] == 48 * 8 and inf["integrator"] == dg.LSERK4 and inf["alpha"] == 0.5
     assert inf["time_step"] == 0.0 and inf["cfl"] == 0.5
@@ -84,29 +84,72 @@ def test_refined_dielectric_case():
     assert np.allclose(u[3], g) and np.abs(u[[0, 1, 2, 4, 5]]).max() == 0.0
 
 
+def _case_copy(tmp_path, src: str, name: str, edit=None, mesh=None) -> Path:
+    """A copy of fixture case `src` as case `name` in the reference's layout
+    (<tmp>/<name>/<name>.json and <name>.msh); edit(dict) may change the JSON."""
+    import json
+    d = tmp_path / name
+    d.mkdir()
+    case = json.loads((CASES / src / f"{src}.json").read_text())
+    case["model"]["filename"] = f"{name}.msh"
+    if edit:
+        edit(case)
+    (d / f"{name}.json").write_text(json.dumps(case))
+    if mesh is None:
+        (d / f"{name}.msh").write_text((CASES / src / f"{src}.msh").read_text())
+    else:
+        mesh(CASES / src / f"{src}.msh", d / f"{name}.msh")
+    return d / f"{name}.json"
+
+
 def test_rejects_unsupported_and_malformed(tmp_path):
     bad = tmp_path / "bad.json"
     bad.write_text('{"solver_options": {"order": 2}, "model": {"filename": "box.msh", "materials": []')
     with pytest.raises(dg.DgtdError, match="JSON parse error"):
         dg.Case(bad)
-    src = (CASES / "box_resonant.json").read_text().replace('"PMC"', '"SGBC"')
-    (tmp_path / "box_resonant.msh").write_text((CASES / "box_resonant.msh").read_text())
-    sg = tmp_path / "sgbc.json"
-    sg.write_text(src)
+
+    def sgbc(c):
+        for b in c["model"]["boundaries"]:
+            if b["type"] == "PMC":
+                b["type"] = "SGBC"
     with pytest.raises(dg.DgtdError, match="not supported"):
-        dg.Case(sg)
-    nomesh = tmp_path / "nomesh.json"
-    nomesh.write_text(src.replace("box_resonant.msh", "missing.msh"))
-    with pytest.raises(dg.DgtdError, match="cannot open mesh"):
-        dg.Case(nomesh)
+        dg.Case(_case_copy(tmp_path, "box_resonant", "sgbc", sgbc))
+
     # a plane wave's Gaussian mean is a position (the reference fails on a plain number too)
-    import json
-    tf = json.loads((CASES / "box_tfsf.json").read_text())
-    tf["sources"][0]["magnitude"]["mean"] = 5.0
-    (tmp_path / "box_tfsf.msh").write_text((CASES / "box_tfsf.msh").read_text())
-    (tmp_path / "scalar_mean.json").write_text(json.dumps(tf))
+    def scalar_mean(c):
+        c["sources"][0]["magnitude"]["mean"] = 5.0
     with pytest.raises(dg.DgtdError, match="magnitude.mean must be a 3-vector"):
-        dg.Case(tmp_path / "scalar_mean.json")
+        dg.Case(_case_copy(tmp_path, "box_tfsf", "scalar_mean", scalar_mean))
+
+
+def test_case_naming_style(tmp_path):
+    """The reference's case layout (driver.cpp:1487-1543, and its DriverTest
+    throwsWhenCaseNamingStyleIsInconsistent): a folder named as the case holding <case>.json
+    and <case>.msh, with model.filename = "<case>.msh"."""
+    import json
+    ok = _case_copy(tmp_path, "box_resonant", "named_ok")
+    assert dg.Case(ok).info["n_elements"] == 162
+    # model.filename naming another mesh (the reference test's case)
+    d = tmp_path / "DriverStyleCheckMismatch"
+    d.mkdir()
+    (d / "DriverStyleCheckMismatch.json").write_text(json.dumps({"model": {"filename": "WrongMeshName.msh"}}))
+    with pytest.raises(dg.DgtdError, match="naming style"):
+        dg.Case(d / "DriverStyleCheckMismatch.json")
+    # folder not named as the case
+    other = tmp_path / "elsewhere"
+    other.mkdir()
+    (other / "named_ok.json").write_text(ok.read_text())
+    (other / "named_ok.msh").write_text((ok.parent / "named_ok.msh").read_text())
+    with pytest.raises(dg.DgtdError, match="naming style"):
+        dg.Case(other / "named_ok.json")
+    # mesh file missing
+    (ok.parent / "named_ok.msh").unlink()
+    with pytest.raises(dg.DgtdError, match="naming style"):
+        dg.Case(ok)
+    # model.filename absent
+    (d / "DriverStyleCheckMismatch.json").write_text(json.dumps({"model": {}}))
+    with pytest.raises(dg.DgtdError, match="model.filename is required"):
+        dg.Case(d / "DriverStyleCheckMismatch.json")
 
 
 @pytest.mark.parametrize("name", ["3D_PEC", "3D_TFSF", "3D_TFSF_InteriorPEC"])
@@ -171,24 +214,20 @@ def test_straight_second_order_mesh_loads_as_linear(tmp_path):
     """A second-order mesh whose edge nodes sit on the straight edges (the reference's
     curved-element test: high-order nodes within 1e-5 of the linear positions) loads as its
     linear elements: same tables as the linear mesh."""
-    _second_order_copy(CASES / "box_resonant.msh", tmp_path / "box_p2.msh")
-    (tmp_path / "box_p2.json").write_text(
-        (CASES / "box_resonant.json").read_text().replace("box_resonant.msh", "box_p2.msh"))
-    lin = dg.Case(CASES / "box_resonant.json")
-    quad = dg.Case(tmp_path / "box_p2.json")
+    lin = dg.Case(CASES / "box_resonant" / "box_resonant.json")
+    quad = dg.Case(_case_copy(tmp_path, "box_resonant", "box_p2", mesh=_second_order_copy))
     ml, mq = lin.mesh(), quad.mesh()
     assert quad.info["n_elements"] == lin.info["n_elements"]
     assert np.array_equal(ml.vertices[ml.elements], mq.vertices[mq.elements])
-    assert {k: v for k, v in quad.info.items() if k != "mesh_path"} == \
-        {k: v for k, v in lin.info.items() if k != "mesh_path"}
+    assert {k: v for k, v in quad.info.items() if k not in ("mesh_path", "name")} == \
+        {k: v for k, v in lin.info.items() if k not in ("mesh_path", "name")}
 
 
 def test_curved_second_order_mesh_rejected(tmp_path):
-    _second_order_copy(CASES / "box_resonant.msh", tmp_path / "box_p2c.msh", bump=1e-3)
-    (tmp_path / "box_p2c.json").write_text(
-        (CASES / "box_resonant.json").read_text().replace("box_resonant.msh", "box_p2c.msh"))
+    bumped = _case_copy(tmp_path, "box_resonant", "box_p2c",
+                        mesh=lambda src, dst: _second_order_copy(src, dst, bump=1e-3))
     with pytest.raises(dg.DgtdError, match=r"second-order elements are curved .*curved geometry is not supported"):
-        dg.Case(tmp_path / "box_p2c.json")
+        dg.Case(bumped)
     # the reference's own curved case: its curved elements are counted and refused
     with pytest.raises(dg.DgtdError, match=r"\d+ second-order elements are curved"):
         dg.Case(REFERENCE_INPUTS / "3D_Curved_Element_Test" / "3D_Curved_Element_Test.json")

@@ -369,8 +369,11 @@ void refine_uniform(GmshMesh& m)
 // ============================================================================ case
 namespace {
 
-constexpr double kFreeSpaceImpedance = 376.730313668;   // ohm; bulk conductivity S/m -> normalised units
 constexpr double kSpeedOfLight = 299792458.0;           // m/s; modulation frequency Hz -> normalised units
+// ohm; bulk conductivity S/m -> normalised units. The reference's value and expression,
+// mu0_SI * c_SI with mu0_SI = 4 pi 1e-7 (src/math/PhysicalConstants.h, driver.cpp:963), so that
+// a lossy case gets the same sigma to the last bit (the CODATA 376.730313668 differs by 5e-10).
+constexpr double kFreeSpaceImpedance = 4.0 * M_PI * 1e-7 * kSpeedOfLight;
 constexpr double kAutoDelaySigmas = 5.0;                 // automatic plane-wave delay (pulse this many sigmas upstream)
 
 std::string dirname(const std::string& p)

@@ -76,7 +76,9 @@ def test_refined_dielectric_case():
     cen = m.vertices[m.elements].mean(axis=1)
     low = cen[:, 2] < 0.5
     assert np.all(m.eps[low] == 2.0) and np.all(m.eps[~low] == 1.0)
-    assert np.allclose(m.sigma[low], 0.001 * 376.730313668) and np.all(m.sigma[~low] == 0.0)
+    # the reference's conversion: sigma * mu0_SI * c_SI, mu0_SI = 4 pi 1e-7 (PhysicalConstants.h)
+    z0 = 4.0 * np.pi * 1e-7 * 299792458.0
+    assert np.all(m.sigma[low] == 0.001 * z0) and np.all(m.sigma[~low] == 0.0)
     assert dg.validate_mesh(m, order=3)["n_elements"] == 384
     xyz = np.random.default_rng(2).uniform(0, 1, (3, 20))
     u = c.initial_state(xyz).reshape(6, -1)

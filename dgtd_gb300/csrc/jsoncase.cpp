@@ -481,15 +481,24 @@ Case load_case(const std::string& json_path)
         if (orient(X + 3 * v[0], X + 3 * v[1], X + 3 * v[2], X + 3 * v[3]) < 0.0) std::swap(v[2], v[3]);
     }
 
-    // ---- materials by volume tag (driver.cpp:946-982)
+    // ---- materials by volume tag (driver.cpp:946-982): the first entry of a tag wins, a tag the
+    // mesh does not have is an error, and no materials at all means vacuum on attribute 1
+    // (Model.cpp:61-66)
     std::map<int, std::array<double, 3>> mat;
+    const std::set<int> mesh_tags(g.tet_tag.begin(), g.tet_tag.end());
     for (const Json& mj : model.at("materials").arr) {
         std::array<double, 3> em = {1.0, 1.0, 0.0};
         if (const Json* v = mj.find("relative_permittivity")) em[0] = v->number();
         if (const Json* v = mj.find("relative_permeability")) em[1] = v->number();
         if (const Json* v = mj.find("bulk_conductivity")) em[2] = v->number() * kFreeSpaceImpedance;
-        for (int t : int_list(mj.at("tags"))) mat[t] = em;
+        for (int t : int_list(mj.at("tags"))) {
+            if (!mesh_tags.count(t))
+                throw std::runtime_error("there is no attribute " + std::to_string(t) +
+                                         " defined in the mesh, but it is defined in the JSON");
+            mat.emplace(t, em);
+        }
     }
+    if (mat.empty()) mat.emplace(1, std::array<double, 3>{1.0, 1.0, 0.0});
     c.eps.resize(K); c.mu.resize(K); c.sigma.resize(K);
     for (int64_t e = 0; e < K; ++e) {
         auto it = mat.find(g.tet_tag[e]);

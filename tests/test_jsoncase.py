@@ -233,3 +233,24 @@ def test_curved_second_order_mesh_rejected(tmp_path):
     # the reference's own curved case: its curved elements are counted and refused
     with pytest.raises(dg.DgtdError, match=r"\d+ second-order elements are curved"):
         dg.Case(REFERENCE_INPUTS / "3D_Curved_Element_Test" / "3D_Curved_Element_Test.json")
+
+
+def test_material_rules_follow_the_reference(tmp_path):
+    """driver.cpp:946-982 and Model.cpp:61-66: the first material entry of a tag wins; a
+    material tag the mesh does not have is an error; no materials at all means vacuum on
+    attribute 1."""
+    def dup(c):
+        c["model"]["materials"] = [{"tags": [1], "relative_permittivity": 2.0},
+                                   {"tags": [1], "relative_permittivity": 3.0}]
+    m = dg.Case(_case_copy(tmp_path, "box_resonant", "dup_tag", dup)).mesh()
+    assert np.all(m.eps == 2.0)
+
+    def absent(c):
+        c["model"]["materials"] = [{"tags": [1]}, {"tags": [99], "relative_permittivity": 4.0}]
+    with pytest.raises(dg.DgtdError, match="no attribute 99 defined in the mesh"):
+        dg.Case(_case_copy(tmp_path, "box_resonant", "absent_tag", absent))
+
+    def none(c):
+        c["model"]["materials"] = []
+    m = dg.Case(_case_copy(tmp_path, "box_resonant", "no_materials", none)).mesh()
+    assert np.all(m.eps == 1.0) and np.all(m.mu == 1.0) and np.all(m.sigma == 0.0)

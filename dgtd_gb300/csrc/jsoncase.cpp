@@ -627,33 +627,53 @@ Case load_case(const std::string& json_path)
         }
     }
 
-    // ---- boundaries by surface tag (driver.cpp:1005-1049)
+    // ---- boundaries by surface tag (driver.cpp:985-1049). As in the reference: every entry needs
+    // non-empty tags and a type; the first entry of a tag wins; a tag is an interior boundary as a
+    // whole when any of its faces lies between two elements, and then only its interior faces get
+    // the condition (the reference applies interior-boundary tags through interior face
+    // integrators only, so that tag's faces on the domain boundary keep no condition: open).
     std::map<int, int> bc_of_tag;
     if (const Json* bs = model.find("boundaries")) {
-        for (const Json& bj : bs->arr) {
-            const std::string& type = bj.at("type").string();
+        for (size_t b = 0; b < bs->arr.size(); ++b) {
+            const Json& bj = bs->arr[b];
+            const Json* tj = bj.find("tags");
+            if (!tj) throw std::runtime_error("boundary " + std::to_string(b) + " does not have defined 'tags'");
+            const std::vector<int> tags = int_list(*tj);
+            if (tags.empty()) throw std::runtime_error("boundary " + std::to_string(b) + " 'tags' are empty");
+            const Json* ty = bj.find("type");
+            if (!ty) throw std::runtime_error("boundary " + std::to_string(b) + " does not have a defined 'type'");
+            const std::string& type = ty->string();
             int code;
             if (type == "PEC") code = DGTD_BC_PEC;
             else if (type == "PMC") code = DGTD_BC_PMC;
             else if (type == "SMA") code = DGTD_BC_SMA;
             else throw std::runtime_error("boundary type '" + type + "' is not supported (PEC, PMC, SMA)");
-            for (int t : int_list(bj.at("tags"))) bc_of_tag[t] = code;
+            for (int t : tags) bc_of_tag.emplace(t, code);
         }
+    }
+    std::vector<int> tri_nelem(g.tri_tag.size());
+    std::set<int> interior_tags;
+    for (size_t t = 0; t < g.tri_tag.size(); ++t) {
+        if (!bc_of_tag.count(g.tri_tag[t])) continue;
+        const auto& el = face_elems[key_of(g.tris[3 * t], g.tris[3 * t + 1], g.tris[3 * t + 2])];
+        if (el.size() != 1 && el.size() != 2)
+            throw std::runtime_error("tagged surface triangle is not a face of the tetrahedral mesh");
+        tri_nelem[t] = static_cast<int>(el.size());
+        if (el.size() == 2) interior_tags.insert(g.tri_tag[t]);
     }
     for (size_t t = 0; t < g.tri_tag.size(); ++t) {
         const int tag = g.tri_tag[t];
         auto it = bc_of_tag.find(tag);
         if (it == bc_of_tag.end()) continue;
         const int32_t a = g.tris[3 * t], b = g.tris[3 * t + 1], d = g.tris[3 * t + 2];
-        const auto& el = face_elems[key_of(a, b, d)];
-        if (el.size() == 1) {
+        if (interior_tags.count(tag)) {
+            if (tri_nelem[t] == 2) {
+                c.int_faces.insert(c.int_faces.end(), {a, b, d});
+                c.int_codes.push_back(it->second);
+            }
+        } else {
             c.bdr_faces.insert(c.bdr_faces.end(), {a, b, d});
             c.bdr_codes.push_back(it->second);
-        } else if (el.size() == 2) {
-            c.int_faces.insert(c.int_faces.end(), {a, b, d});
-            c.int_codes.push_back(it->second);
-        } else {
-            throw std::runtime_error("tagged surface triangle is not a face of the tetrahedral mesh");
         }
     }
 

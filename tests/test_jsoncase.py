@@ -254,3 +254,57 @@ def test_material_rules_follow_the_reference(tmp_path):
         c["model"]["materials"] = []
     m = dg.Case(_case_copy(tmp_path, "box_resonant", "no_materials", none)).mesh()
     assert np.all(m.eps == 1.0) and np.all(m.mu == 1.0) and np.all(m.sigma == 0.0)
+
+
+def test_boundary_rules_follow_the_reference(tmp_path):
+    """driver.cpp:985-1049: every boundary entry needs non-empty tags and a type, and the first
+    entry of a tag wins (the resonant box: tags 1-4 PEC, 5-6 PMC, 18 triangles per wall)."""
+    def dup(c):
+        c["model"]["boundaries"] = [{"tags": [1, 2, 3, 4], "type": "PEC"}, {"tags": [5, 6], "type": "PMC"},
+                                    {"tags": [5], "type": "SMA"}]
+    m = dg.Case(_case_copy(tmp_path, "box_resonant", "dup_bdr", dup)).mesh()
+    codes, counts = np.unique(m.bdr_codes, return_counts=True)
+    assert dict(zip(codes.tolist(), counts.tolist())) == {dg.BC_PEC: 72, dg.BC_PMC: 36}
+
+    def no_tags(c):
+        c["model"]["boundaries"][1]["tags"] = []
+    with pytest.raises(dg.DgtdError, match="boundary 1 'tags' are empty"):
+        dg.Case(_case_copy(tmp_path, "box_resonant", "no_tags", no_tags))
+
+    def no_type(c):
+        del c["model"]["boundaries"][0]["type"]
+    with pytest.raises(dg.DgtdError, match="boundary 0 does not have a defined 'type'"):
+        dg.Case(_case_copy(tmp_path, "box_resonant", "no_type", no_type))
+
+
+def _with_interior_triangle(src: Path, dst: Path, tag: int) -> None:
+    """Copy a gmsh 2.2 mesh and add one triangle with physical tag `tag` on a face shared by
+    two tetrahedra."""
+    lines = src.read_text().splitlines()
+    j = lines.index("$Elements")
+    ne = int(lines[j + 1])
+    faces = {}
+    for ln in lines[j + 2:j + 2 + ne]:
+        f = [int(v) for v in ln.split()]
+        if f[1] != 4:
+            continue
+        vs = f[3 + f[2]:]
+        for q in range(4):
+            key = tuple(sorted(vs[:q] + vs[q + 1:]))
+            faces[key] = faces.get(key, 0) + 1
+    shared = next(k for k, n in faces.items() if n == 2)
+    eid = max(int(ln.split()[0]) for ln in lines[j + 2:j + 2 + ne]) + 1
+    new = f"{eid} 2 2 {tag} {tag} {shared[0]} {shared[1]} {shared[2]}"
+    lines = lines[:j + 1] + [str(ne + 1)] + lines[j + 2:j + 2 + ne] + [new] + lines[j + 2 + ne:]
+    dst.write_text("\n".join(lines) + "\n")
+
+
+def test_mixed_interior_exterior_tag_is_an_interior_boundary(tmp_path):
+    """A tag with any face between two elements is an interior boundary as a whole: its interior
+    faces get the condition and its faces on the domain boundary keep none (the reference's
+    per-tag classification, driver.cpp:1024-1048)."""
+    m = dg.Case(_case_copy(tmp_path, "box_resonant", "mixed_tag",
+                           mesh=lambda s, d: _with_interior_triangle(s, d, 1))).mesh()
+    codes, counts = np.unique(m.bdr_codes, return_counts=True)
+    assert dict(zip(codes.tolist(), counts.tolist())) == {dg.BC_PEC: 54, dg.BC_PMC: 36}
+    assert m.int_codes.tolist() == [dg.BC_PEC]

@@ -457,12 +457,32 @@ Case load_case(const std::string& json_path)
         if (const Json* v = so->find("final_time")) c.final_time = v->number();
         if (const Json* v = so->find("cfl")) c.cfl = v->number();
         if (const Json* v = so->find("order")) c.order = v->integer();
-        if (const Json* v = so->find("evolution_operator")) c.evolution_operator = v->string();
+        if (const Json* v = so->find("evolution_operator")) {
+            // the reference's three names (driver.cpp:679-691); all run on this library's operator
+            c.evolution_operator = v->string();
+            if (c.evolution_operator != "maxwell" && c.evolution_operator != "global" &&
+                c.evolution_operator != "hesthaven")
+                throw std::runtime_error("wrong type of evolution operator '" + c.evolution_operator +
+                                         "': choose 'maxwell', 'global' or 'hesthaven'");
+        }
         if (const Json* v = so->find("ode_type")) {
-            const std::string& o = v->string();
-            if (o == "RK4" || o == "rk4") c.integrator = DGTD_RK4;
-            else if (o == "LSERK4" || o == "lserk4") c.integrator = DGTD_LSERK4;
-            else throw std::runtime_error("ode_type '" + o + "' is not supported (RK4, LSERK4)");
+            if (v->type == Json::String) {   // this library's names (LSERK4 has no number in the reference)
+                const std::string& o = v->string();
+                if (o == "RK4" || o == "rk4") c.integrator = DGTD_RK4;
+                else if (o == "LSERK4" || o == "lserk4") c.integrator = DGTD_LSERK4;
+                else throw std::runtime_error("ode_type '" + o + "' is not supported (RK4, LSERK4)");
+            } else {
+                // the reference's numbering (SolverOptions.h:8-16, Solver.cpp:41-77): 0 = RK4,
+                // 1-6 the implicit solvers (BackwardEuler, Trapezoidal, ImplicitMidpoint, SDIRK33,
+                // SDIRK23, SDIRK34)
+                const int o = v->integer();
+                if (o == 0) c.integrator = DGTD_RK4;
+                else if (o >= 1 && o <= 6)
+                    throw std::runtime_error("implicit ode_type " + std::to_string(o) +
+                                             " is not supported (the explicit RK4, ode_type 0, is)");
+                else
+                    throw std::runtime_error("wrong ode type defined in json (ode_type " + std::to_string(o) + ")");
+            }
         }
     }
     if (c.order < 1 || c.order > 6) throw std::runtime_error("order must be in [1, 6]");

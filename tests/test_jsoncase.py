@@ -308,3 +308,25 @@ def test_mixed_interior_exterior_tag_is_an_interior_boundary(tmp_path):
     codes, counts = np.unique(m.bdr_codes, return_counts=True)
     assert dict(zip(codes.tolist(), counts.tolist())) == {dg.BC_PEC: 54, dg.BC_PMC: 36}
     assert m.int_codes.tolist() == [dg.BC_PEC]
+
+
+def test_solver_option_names_follow_the_reference(tmp_path):
+    """SolverOptions.h:8-16 / Solver.cpp:41-77: ode_type is a number, 0 = RK4 and 1-6 the
+    implicit solvers; driver.cpp:679-691: evolution_operator is maxwell, global or hesthaven."""
+    def ode(n):
+        return lambda c: c.setdefault("solver_options", {}).__setitem__("ode_type", n)
+    c = dg.Case(_case_copy(tmp_path, "box_resonant", "ode0", ode(0)))
+    assert c.info["integrator"] == dg.RK4
+    with pytest.raises(dg.DgtdError, match="implicit ode_type 2 is not supported"):
+        dg.Case(_case_copy(tmp_path, "box_resonant", "ode2", ode(2)))
+    with pytest.raises(dg.DgtdError, match="wrong ode type"):
+        dg.Case(_case_copy(tmp_path, "box_resonant", "ode9", ode(9)))
+    c = dg.Case(_case_copy(tmp_path, "box_resonant", "odes", ode("LSERK4")))
+    assert c.info["integrator"] == dg.LSERK4
+
+    def evo(name):
+        return lambda c: c.setdefault("solver_options", {}).__setitem__("evolution_operator", name)
+    for name in ("maxwell", "global", "hesthaven"):
+        dg.Case(_case_copy(tmp_path, "box_resonant", f"evo_{name}", evo(name)))
+    with pytest.raises(dg.DgtdError, match="wrong type of evolution operator"):
+        dg.Case(_case_copy(tmp_path, "box_resonant", "evo_bad", evo("spectral")))

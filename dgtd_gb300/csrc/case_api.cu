@@ -2,6 +2,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <limits>
 #include <chrono>
 #include <cstdio>
 #include <memory>
@@ -167,7 +168,12 @@ int dgtd_case_run(const dgtd_case* cs, const dgtd_case_run_opts* ro, double* h_s
         std::vector<int32_t> faces;
         for (const auto& s : c.surfaces) faces.insert(faces.end(), s.faces.begin(), s.faces.end());
         int every = 1;
-        if (npts > 0) every = *std::min_element(c.point_interval.begin(), c.point_interval.end());
+        if (npts > 0) {
+            every = std::numeric_limits<int>::max();
+            for (int32_t k = 0; k < npts; ++k)
+                every = std::min(every, dgtd::probe_interval(c.point_saves[k], c.point_interval[k], c.final_time, dt));
+            every = std::max(1, every);
+        }
         const int64_t est_steps = dt > 0.0 ? static_cast<int64_t>(c.final_time / dt) + 2 : 2;
         const bool probes = npts > 0 || !faces.empty();
         if (probes) {

@@ -697,15 +697,12 @@ Case load_case(const std::string& json_path)
         }
     }
 
-    // ---- probes (driver.cpp:707-868)
+    // ---- probes (driver.cpp:707-868): "steps" is the interval; "saves" asks for that many samples
+    // over the run, turned into an interval with the run's dt (placeholder 1 while dt is automatic)
+    auto saves_of = [](const Json& pj) { return pj.has("saves") ? pj.at("saves").integer() : 0; };
     auto interval_of = [&](const Json& pj) {
         if (const Json* st = pj.find("steps")) return std::max(1, st->integer());
-        if (const Json* sv = pj.find("saves")) {
-            // a number of saves over the run: interval = steps / saves (driver.cpp:718-733)
-            const double dt = c.dt > 0.0 ? c.dt : 1.0;
-            const long steps = std::lround(c.final_time / dt);
-            return std::max<int>(1, static_cast<int>(steps / std::max(1, sv->integer())));
-        }
+        if (pj.has("saves")) return c.dt > 0.0 ? probe_interval(saves_of(pj), 1, c.final_time, c.dt) : 1;
         return 1;
     };
     if (const Json* pr = J.find("probes")) {
@@ -715,6 +712,7 @@ Case load_case(const std::string& json_path)
                 vec3(pj.at("position"), x);
                 c.point_pos.insert(c.point_pos.end(), {x[0], x[1], x[2]});
                 c.point_interval.push_back(interval_of(pj));
+                c.point_saves.push_back(saves_of(pj));
             }
         for (const char* kind : {"rcssurface", "farfield"})
             if (const Json* surf = pr->find(kind))
@@ -741,6 +739,13 @@ Case load_case(const std::string& json_path)
                 }
     }
     return c;
+}
+
+int probe_interval(int saves, int steps_interval, double final_time, double dt)
+{
+    if (saves <= 0 || !(dt > 0.0)) return steps_interval;
+    const int total = static_cast<int>(std::ceil(final_time / dt));
+    return std::max(1, total / saves);
 }
 
 std::vector<double> case_initial_state(const Case& c, const double* xyz, int64_t n)

@@ -91,11 +91,19 @@ struct Case {
     std::vector<CaseInitialField> initial;
     // probes
     std::vector<double> point_pos;  // [n][3]
-    std::vector<int> point_interval;
+    std::vector<int> point_interval;   // sampling interval in steps ("steps", or from "saves")
+    std::vector<int> point_saves;      // requested number of saves (0: none); the runner turns it
+                                       // into an interval once dt is known (probe_interval)
     std::vector<CaseSurface> surfaces;
 };
 
 Case load_case(const std::string& json_path);
+
+// Sampling interval of a probe that asked for `saves` samples over a run of final_time with step
+// dt (reference ProbesManager::recalculateExportSteps, src/solver/ProbesManager.cpp:578-607, run
+// with the solver's dt, Solver.cpp:122): max(1, ceil(final_time / dt) / saves); saves <= 0
+// keeps `steps_interval`.
+int probe_interval(int saves, int steps_interval, double final_time, double dt);
 
 // Initial field at the nodes (reference SourcesManager::setInitialFields,
 // src/solver/SourcesManager.cpp:16-36: nodal projection of InitialField::eval,

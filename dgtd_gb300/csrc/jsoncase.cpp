@@ -465,6 +465,14 @@ Case load_case(const std::string& json_path)
                 throw std::runtime_error("wrong type of evolution operator '" + c.evolution_operator +
                                          "': choose 'maxwell', 'global' or 'hesthaven'");
         }
+        if (const Json* v = so->find("basis_type")) {
+            // MFEM's BasisType numbering (SolverOptions.h:74-77; 0 Gauss-Legendre, 1 Gauss-Lobatto,
+            // 2 positive/Bernstein, ...): the operator is built on the Gauss-Lobatto node set only
+            const int bt = v->integer();
+            if (bt != 1)
+                throw std::runtime_error("basis_type " + std::to_string(bt) +
+                                         " is not supported (the Gauss-Lobatto nodal basis, basis_type 1, is)");
+        }
         if (const Json* v = so->find("ode_type")) {
             if (v->type == Json::String) {   // this library's names (LSERK4 has no number in the reference)
                 const std::string& o = v->string();

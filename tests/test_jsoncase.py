@@ -330,3 +330,13 @@ def test_solver_option_names_follow_the_reference(tmp_path):
         dg.Case(_case_copy(tmp_path, "box_resonant", f"evo_{name}", evo(name)))
     with pytest.raises(dg.DgtdError, match="wrong type of evolution operator"):
         dg.Case(_case_copy(tmp_path, "box_resonant", "evo_bad", evo("spectral")))
+
+
+def test_basis_type_other_than_gauss_lobatto_refused(tmp_path):
+    """The reference's basis_type is MFEM's BasisType number; the operator here is built on the
+    Gauss-Lobatto node set (1) only, so e.g. Gauss-Legendre (0) is refused, not ignored."""
+    def bt(n):
+        return lambda c: c.setdefault("solver_options", {}).__setitem__("basis_type", n)
+    dg.Case(_case_copy(tmp_path, "box_resonant", "bt1", bt(1)))
+    with pytest.raises(dg.DgtdError, match="basis_type 0 is not supported"):
+        dg.Case(_case_copy(tmp_path, "box_resonant", "bt0", bt(0)))

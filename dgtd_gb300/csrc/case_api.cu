@@ -217,14 +217,22 @@ int dgtd_case_run(const dgtd_case* cs, const dgtd_case_run_opts* ro, double* h_s
             if (ro && ro->out_dir && npts > 0) {
                 std::vector<double> series(static_cast<size_t>(nrec) * npts * 6), times(nrec);
                 ok(dgtd_op_probe_read(op, nullptr, nullptr, series.data(), times.data(), nullptr), "probe_read");
+                // the reference's point-probe file (ProbesManager.cpp:203-215, 400-407): four header
+                // lines (ID, "Spatial Position (X, Y, Z)", the position, the column names), then per
+                // sample the time in seconds (normalised time / c) and the six field values
+                constexpr double kSpeedOfLightSI = 299792458.0;
                 for (int32_t k = 0; k < npts; ++k) {
                     const std::string path = std::string(ro->out_dir) + "/PointProbe" + std::to_string(k) + ".dat";
                     FILE* f = std::fopen(path.c_str(), "w");
                     if (!f) throw std::runtime_error("cannot write " + path);
+                    const double* x = &c.point_pos[3 * static_cast<size_t>(k)];
+                    std::fprintf(f, "PointProbe ID %d\nSpatial Position (X, Y, Z) \n%s %s %s\n", k,
+                                 std::to_string(x[0]).c_str(), std::to_string(x[1]).c_str(), std::to_string(x[2]).c_str());
+                    std::fprintf(f, "Time (s) // Ex // Ey // Ez // Hx // Hy // Hz \n");
                     for (int64_t r = 0; r < nrec; ++r) {
                         const double* v = &series[(static_cast<size_t>(r) * npts + k) * 6];
-                        std::fprintf(f, "%.10e %.10e %.10e %.10e %.10e %.10e %.10e\n", times[r], v[0], v[1], v[2], v[3],
-                                     v[4], v[5]);
+                        std::fprintf(f, "%.10e %.10e %.10e %.10e %.10e %.10e %.10e\n", times[r] / kSpeedOfLightSI, v[0],
+                                     v[1], v[2], v[3], v[4], v[5]);
                     }
                     std::fclose(f);
                 }

@@ -344,7 +344,9 @@ typedef struct dgtd_case_run_opts {
     int32_t precision;           /* DGTD_FP64 (the plain form) */
     const double* freqs;         /* DFT frequencies of the point probes and surfaces (may be NULL) */
     int32_t n_freqs;
-    const char* out_dir;         /* if not NULL: PointProbe<k>.dat files (t Ex Ey Ez Hx Hy Hz) */
+    const char* out_dir;         /* if not NULL: PointProbe<k>.dat files in the reference's layout
+                                    (ProbesManager.cpp:203-215, 400-407): four header lines, then
+                                    t Ex Ey Ez Hx Hy Hz per sample with t in seconds (t / c) */
 } dgtd_case_run_opts;
 
 typedef struct dgtd_case_result {

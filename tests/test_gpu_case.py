@@ -11,7 +11,7 @@ import pytest
 
 import dgtd_gb300 as dg
 from oracle import pyoracle as po
-from conftest import rel_l2
+from conftest import read_point_probe, rel_l2
 
 pytestmark = pytest.mark.gpu
 CASES = Path(__file__).resolve().parent / "golden" / "cases"
@@ -48,7 +48,7 @@ def test_case_run_matches_operator_and_oracle(torch_cuda, tmp_path, name):
     files = sorted(tmp_path.glob("PointProbe*.dat"))
     assert len(files) == npts
     for f in files:
-        rows = np.loadtxt(f, ndmin=2)
+        rows = read_point_probe(f)
         assert rows.shape == (res["n_records"], 7)
         assert rows[-1, 0] == pytest.approx(res["final_time"])
 
@@ -57,7 +57,7 @@ def test_resonant_case_probe_values(torch_cuda, tmp_path):
     """The probe at the cavity centre follows the TE110 mode: Ez(t) ~ cos(w t) with w = pi sqrt(2)."""
     case = dg.Case(CASES / "box_resonant" / "box_resonant.json")
     _, res = case.run(out_dir=tmp_path, want_state=False)
-    rows = np.loadtxt(tmp_path / "PointProbe0.dat")
+    rows = read_point_probe(tmp_path / "PointProbe0.dat")
     t, ez = rows[:, 0], rows[:, 3]
     w = np.pi * np.sqrt(2.0)
     # order 2 on 3^3 hexes: a few percent of discretisation error
@@ -90,7 +90,7 @@ def test_reference_case_end_to_end(torch_cuda, tmp_path, name):
     files = sorted(tmp_path.glob("PointProbe*.dat"))
     assert len(files) == inf["n_point_probes"]
     for f in files:
-        rows = np.loadtxt(f, ndmin=2)
+        rows = read_point_probe(f)
         assert rows.shape == (res["n_records"], 7) and np.all(np.isfinite(rows))
 
 

@@ -340,3 +340,20 @@ def test_basis_type_other_than_gauss_lobatto_refused(tmp_path):
     dg.Case(_case_copy(tmp_path, "box_resonant", "bt1", bt(1)))
     with pytest.raises(dg.DgtdError, match="basis_type 0 is not supported"):
         dg.Case(_case_copy(tmp_path, "box_resonant", "bt0", bt(0)))
+
+
+def test_point_probe_file_format(tmp_path):
+    """The case runner's point-probe files follow the reference's layout; this writes one with the
+    runner's format strings (case_api.cu) and reads it back with the tests' parser."""
+    from conftest import read_point_probe
+    c = 299792458.0
+    x = (0.5, 0.25, 0.75)
+    lines = ["PointProbe ID 0", "Spatial Position (X, Y, Z) ", "%f %f %f" % x,
+             "Time (s) // Ex // Ey // Ez // Hx // Hy // Hz "]
+    t = np.array([0.0, 0.01, 0.02])
+    v = np.arange(18, dtype=float).reshape(3, 6) * 0.1
+    lines += ["%.10e %.10e %.10e %.10e %.10e %.10e %.10e" % ((t[r] / c,) + tuple(v[r])) for r in range(3)]
+    (tmp_path / "PointProbe0.dat").write_text("\n".join(lines) + "\n")
+    rows = read_point_probe(tmp_path / "PointProbe0.dat")
+    assert rows.shape == (3, 7)
+    assert np.allclose(rows[:, 0], t, rtol=1e-9, atol=1e-14) and np.allclose(rows[:, 1:], v)

@@ -185,7 +185,7 @@ int dgtd_case_run(const dgtd_case* cs, const dgtd_case_run_opts* ro, double* h_s
             ps.n_freqs = ro ? ro->n_freqs : 0;
             ps.freqs = ro ? ro->freqs : nullptr;
             ps.every = every;
-            ps.max_records = npts > 0 ? static_cast<int32_t>(std::min<int64_t>(est_steps / every + 2, 1 << 24)) : 0;
+            ps.max_records = npts > 0 ? static_cast<int32_t>(std::min<int64_t>(est_steps / every + 3, 1 << 24)) : 0;
             ok(dgtd_op_set_probes(op, &ps), "set_probes");
         }
         const size_t bytes = u.size() * sizeof(double);
@@ -198,6 +198,9 @@ int dgtd_case_run(const dgtd_case* cs, const dgtd_case_run_opts* ro, double* h_s
         // kStabEvery steps and of the final state, read back at the end
         constexpr int64_t kStabEvery = 10;
         ok(dgtd_op_stability_reset(op), "stability reset");
+        // probes: the initial state (the reference's Solver constructor samples at cycle 0,
+        // Solver.cpp:129), then every `every` steps inside dgtd_op_step, and the final state
+        if (probes) ok(dgtd_op_probe_sample(op, d, 0.0, nullptr), "initial probe sample");
         while (t <= c.final_time - 1e-8 * dt) {
             const double h = std::min(dt, c.final_time - t);
             ok(dgtd_op_step(op, d, t, h, 1, c.integrator, nullptr), "dgtd_op_step");

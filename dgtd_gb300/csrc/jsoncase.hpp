@@ -74,10 +74,12 @@ struct CaseSurface {
 
 struct Case {
     std::string dir, name;
-    int order = 3;
+    // defaults of the reference's SolverOptions / EvolutionOptions (SolverOptions.h:19-24,
+    // EvolutionOptions.h:13-16)
+    int order = 2;
     double alpha = 1.0;
     double dt = 0.0;                // 0: estimate from cfl
-    double final_time = 0.0;
+    double final_time = 2.0;
     double cfl = 1.0;
     int integrator = DGTD_RK4;
     std::string evolution_operator = "global";

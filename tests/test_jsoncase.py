@@ -357,3 +357,13 @@ def test_point_probe_file_format(tmp_path):
     rows = read_point_probe(tmp_path / "PointProbe0.dat")
     assert rows.shape == (3, 7)
     assert np.allclose(rows[:, 0], t, rtol=1e-9, atol=1e-14) and np.allclose(rows[:, 1:], v)
+
+
+def test_solver_option_defaults_follow_the_reference(tmp_path):
+    """Without solver_options the reference runs order 2, upwind alpha 1, final time 2, an
+    automatic time step at cfl 1 (SolverOptions.h, EvolutionOptions.h)."""
+    def bare(c):
+        c.pop("solver_options", None)
+    inf = dg.Case(_case_copy(tmp_path, "box_resonant", "bare", bare)).info
+    assert inf["order"] == 2 and inf["alpha"] == 1.0 and inf["final_time"] == 2.0
+    assert inf["time_step"] == 0.0 and inf["cfl"] == 1.0

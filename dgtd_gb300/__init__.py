@@ -173,6 +173,7 @@ SIGNATURES = {
     "dgtd_case_load": (C.c_int, [C.c_char_p, C.POINTER(_P)]),
     "dgtd_case_destroy": (None, [_P]),
     "dgtd_case_get_info": (C.c_int, [_P, C.POINTER(CaseInfo)]),
+    "dgtd_case_auto_dt": (C.c_int, [_P, C.POINTER(C.c_double)]),
     "dgtd_case_mesh": (C.c_int, [_P, C.POINTER(MeshDesc)]),
     "dgtd_case_planewaves": (C.c_int, [_P, C.POINTER(PlaneWave), C.c_int32]),
     "dgtd_case_point_probes": (C.c_int, [_P, _D]),
@@ -693,6 +694,13 @@ class Case:
                 self._h = C.c_void_p()
         except Exception:
             pass
+
+    def auto_dt(self) -> float:
+        """The time step of a run with time_step 0: the reference's estimate for the case's
+        evolution operator (computed on the host)."""
+        v = C.c_double()
+        _check(lib().dgtd_case_auto_dt(self._h, C.byref(v)), "dgtd_case_auto_dt")
+        return float(v.value)
 
     def mesh(self) -> Mesh:
         d = MeshDesc()

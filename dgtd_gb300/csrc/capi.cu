@@ -1098,10 +1098,7 @@ int dgtd_op_estimate_dt(const dgtd_op* op, double cfl, double* dt_out)
 {
     if (!op || !dt_out) return fail(DGTD_ERR_INVALID, "NULL argument");
     if (!(cfl > 0.0)) return fail(DGTD_ERR_INVALID, "cfl must be positive");
-    auto g = dgtd::gauss_lobatto(op->ref.p);
-    const double rmin = std::fabs(g[1] - g[0]);   // GLL spacing on a segment of length 2
-    double dt = op->mesh.dt_scale_min * rmin * 2.0 / 3.0 * 0.75 * cfl;
-    *dt_out = dt / 0.8;
+    *dt_out = dgtd::estimate_dt(op->mesh, op->ref.p, cfl, 1);   // the reference's default, global
     return DGTD_OK;
 }
 

@@ -12,6 +12,7 @@
 
 #include "../../include/dgtd_gb300.h"
 #include "jsoncase.hpp"
+#include "mesh.hpp"
 
 namespace dgtd {
 int set_last_error(int code, const std::string& msg);   // capi.cu
@@ -99,6 +100,32 @@ int dgtd_case_mesh(const dgtd_case* cs, dgtd_mesh_desc* m)
     return DGTD_OK;
 }
 
+int dgtd_case_auto_dt(const dgtd_case* cs, double* dt)
+{
+    if (!cs || !dt) return cfail(DGTD_ERR_INVALID, "NULL argument");
+    const dgtd::Case& c = cs->c;
+    try {
+        dgtd::MeshInput in;
+        in.dim = 3;
+        in.vertices = c.vertices;
+        in.elements = c.elements;
+        in.eps = c.eps;
+        in.mu = c.mu;
+        in.sigma = c.sigma;
+        in.bdr_faces = c.bdr_faces;
+        in.bdr_codes = c.bdr_codes;
+        in.tfsf_faces = c.tfsf_faces;
+        in.int_faces = c.int_faces;
+        in.int_codes = c.int_codes;
+        const dgtd::MeshTables T = dgtd::build_tables(in, dgtd::build_ref_tet(c.order));
+        const int evolution = c.evolution_operator == "maxwell" ? 0 : (c.evolution_operator == "hesthaven" ? 2 : 1);
+        *dt = dgtd::estimate_dt(T, c.order, c.cfl, evolution);
+    } catch (const std::exception& e) {
+        return cfail(DGTD_ERR_INVALID, e.what());
+    }
+    return DGTD_OK;
+}
+
 int dgtd_case_planewaves(const dgtd_case* cs, dgtd_planewave* out, int32_t capacity)
 {
     if (!cs || (!out && capacity > 0)) return cfail(DGTD_ERR_INVALID, "NULL argument");
@@ -155,7 +182,7 @@ int dgtd_case_run(const dgtd_case* cs, const dgtd_case_run_opts* ro, double* h_s
         if (!c.waves.empty())
             ok(dgtd_op_set_planewaves(op, c.waves.data(), static_cast<int32_t>(c.waves.size())), "set_planewaves");
         double dt = c.dt;
-        if (!(dt > 0.0)) ok(dgtd_op_estimate_dt(op, c.cfl, &dt), "estimate_dt");
+        if (!(dt > 0.0)) ok(dgtd_case_auto_dt(cs, &dt), "automatic time step");
         dgtd_op_info info;
         ok(dgtd_op_get_info(op, &info), "get_info");
         const int64_t N = info.ndofs;

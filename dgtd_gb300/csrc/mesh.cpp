@@ -49,6 +49,19 @@ inline double dot3(const double* a, const double* b) { return a[0] * b[0] + a[1]
 
 }  // namespace
 
+double estimate_dt(const MeshTables& T, int p, double cfl, int evolution)
+{
+    if (evolution == 2) {
+        double maxf = 0.0;
+        for (size_t q = 3; q < T.fgeo.size(); q += 4) maxf = std::max(maxf, T.fgeo[q]);
+        return 1.0 * cfl / (maxf * p * p);
+    }
+    const auto g = gauss_lobatto(p);
+    const double rmin = std::fabs(g[1] - g[0]);   // GLL spacing on a segment of length 2
+    const double base = T.dt_scale_min * rmin * 2.0 / 3.0 * 0.75 * cfl;
+    return evolution == 1 ? base / 0.8 : base;
+}
+
 MeshTables build_tables(const MeshInput& in, const RefTet& ref)
 {
     if (in.dim != 3) throw std::runtime_error("build_tables: only 3D tetrahedral meshes");

@@ -62,6 +62,13 @@ struct MeshTables {
 
 MeshTables build_tables(const MeshInput& in, const RefTet& ref);
 
+// The reference's automatic time step (Solver::estimateTimeStep, src/solver/Solver.cpp:289-345)
+// for the 3D evolution operators: base = dtscale_min * rmin * 2/3 * 0.75 * cfl (rmin the smallest
+// Gauss-Lobatto spacing on [-1, 1]); global: base / 0.8; maxwell: base; hesthaven:
+// cfl / (max Fscale * p^2), Fscale = 2 sJ / J per face. evolution: 0 maxwell, 1 global,
+// 2 hesthaven (the reference's EvolutionOperatorType).
+double estimate_dt(const MeshTables& T, int p, double cfl, int evolution);
+
 // Structured box [x0,x1]x[y0,y1]x[z0,z1] of n cells per axis, each hex split
 // into 6 tetrahedra around its (0,0,0)-(1,1,1) diagonal. Optional hole (cells
 // [hole_lo, hole_hi) removed) and TF/SF box (cells [tf_lo, tf_hi) are the

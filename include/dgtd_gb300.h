@@ -367,6 +367,12 @@ typedef struct dgtd_case_result {
 int dgtd_case_load(const char* json_path, dgtd_case** out);
 void dgtd_case_destroy(dgtd_case* c);
 int dgtd_case_get_info(const dgtd_case* c, dgtd_case_info* info);
+
+/* The automatic time step a run of the case takes when solver_options.time_step is 0: the
+ * reference's estimate for the case's evolution operator (Solver::estimateTimeStep,
+ * Solver.cpp:289-345; global: base / 0.8, maxwell: base, hesthaven: cfl / (max Fscale p^2)),
+ * from the case's mesh on the host (no device needed). */
+int dgtd_case_auto_dt(const dgtd_case* c, double* dt);
 /* Views into the case's tables (valid while the case lives). */
 int dgtd_case_mesh(const dgtd_case* c, dgtd_mesh_desc* mesh);
 int dgtd_case_planewaves(const dgtd_case* c, dgtd_planewave* out, int32_t capacity);

@@ -367,3 +367,34 @@ def test_solver_option_defaults_follow_the_reference(tmp_path):
     inf = dg.Case(_case_copy(tmp_path, "box_resonant", "bare", bare)).info
     assert inf["order"] == 2 and inf["alpha"] == 1.0 and inf["final_time"] == 2.0
     assert inf["time_step"] == 0.0 and inf["cfl"] == 1.0
+
+
+def test_automatic_time_step_follows_the_reference(tmp_path):
+    """Solver::estimateTimeStep (Solver.cpp:289-345) for the three 3D evolution operators, on
+    the host: global = the oracle's restatement (base / 0.8); maxwell = base; hesthaven =
+    cfl / (max Fscale p^2) with Fscale = 2 sJ / J = (2/3) area / volume per face."""
+    from oracle import pyoracle as po
+
+    def opts(op, cfl=0.7):
+        def edit(c):
+            so = c.setdefault("solver_options", {})
+            so["time_step"] = 0.0
+            so["cfl"] = cfl
+            if op:
+                so["evolution_operator"] = op
+        return edit
+    glob_ = dg.Case(_case_copy(tmp_path, "box_tfsf", "dt_global", opts(None)))
+    mesh = glob_.mesh()
+    p = glob_.info["order"]
+    want = po.estimate_dt_3d(mesh, p, 0.7)
+    assert abs(glob_.auto_dt() - want) <= 1e-15 * want
+    mx = dg.Case(_case_copy(tmp_path, "box_tfsf", "dt_maxwell", opts("maxwell"))).auto_dt()
+    assert abs(mx - 0.8 * want) <= 1e-14 * want
+    P = mesh.vertices[mesh.elements]
+    vol = np.abs(np.einsum("ki,ki->k", P[:, 1] - P[:, 0], np.cross(P[:, 2] - P[:, 0], P[:, 3] - P[:, 0]))) / 6.0
+    fmax = 0.0
+    for f in ((1, 2, 3), (0, 2, 3), (0, 1, 3), (0, 1, 2)):
+        area = 0.5 * np.linalg.norm(np.cross(P[:, f[1]] - P[:, f[0]], P[:, f[2]] - P[:, f[0]]), axis=1)
+        fmax = max(fmax, float(np.max(2.0 / 3.0 * area / vol)))
+    he = dg.Case(_case_copy(tmp_path, "box_tfsf", "dt_hesthaven", opts("hesthaven"))).auto_dt()
+    assert abs(he - 0.7 / (fmax * p * p)) <= 1e-12 * he

@@ -19,7 +19,7 @@ _PKG = Path(__file__).resolve().parent
 LIB_PATH = _PKG / "libdgtd_gb300.so"
 
 DGTD_OK = 0
-BC_OPEN, BC_PEC, BC_PMC, BC_SMA = 0, 1, 2, 3
+BC_OPEN, BC_PEC, BC_PMC, BC_SMA, BC_SGBC = 0, 1, 2, 3, 4
 FP64, FP32_3XTF32, FP32 = 0, 1, 2
 RK4, LSERK4 = 0, 1
 
@@ -74,11 +74,22 @@ class ProbeSpec(C.Structure):
                 ("every", C.c_int32), ("max_records", C.c_int32)]
 
 
+class SgbcLayer(C.Structure):
+    _fields_ = [("eps_r", C.c_double), ("mu_r", C.c_double), ("sigma", C.c_double), ("width", C.c_double),
+                ("segments", C.c_int32), ("order", C.c_int32)]
+
+
+class SgbcStack(C.Structure):
+    _fields_ = [("n_layers", C.c_int32), ("layers", C.POINTER(SgbcLayer)), ("left_bc", C.c_int32),
+                ("right_bc", C.c_int32), ("sub_dt", C.c_double)]
+
+
 class CaseInfo(C.Structure):
     _fields_ = [("order", C.c_int32), ("integrator", C.c_int32), ("alpha", C.c_double), ("time_step", C.c_double),
                 ("final_time", C.c_double), ("cfl", C.c_double), ("n_waves", C.c_int32),
                 ("n_initial_fields", C.c_int32), ("n_point_probes", C.c_int32), ("n_surfaces", C.c_int32),
-                ("n_elements", C.c_int64), ("n_vertices", C.c_int64)]
+                ("n_elements", C.c_int64), ("n_vertices", C.c_int64), ("n_sgbc_stacks", C.c_int32),
+                ("n_sgbc_layers", C.c_int32), ("n_sgbc_faces", C.c_int64)]
 
 
 class CaseRunOpts(C.Structure):
@@ -164,6 +175,10 @@ SIGNATURES = {
     "dgtd_mesh_validate": (C.c_int, [C.POINTER(MeshDesc), C.POINTER(OpOpts), C.POINTER(OpInfo)]),
     "dgtd_tc_selftest": (C.c_int, [_D_F, _D_F, _D_F, C.c_int32, _I32]),
     "dgtd_op_set_probes": (C.c_int, [_P, C.POINTER(ProbeSpec)]),
+    "dgtd_op_set_sgbc": (C.c_int, [_P, C.POINTER(SgbcStack), C.c_int32, _I32]),
+    "dgtd_op_sgbc_states": (C.c_int, [_P, _I64, _I64, _D, C.c_int64]),
+    "dgtd_sgbc_stack_operator": (C.c_int, [C.POINTER(SgbcStack), _I64, _I64, _I64, _D, C.c_int64]),
+    "dgtd_sgbc_stack_maps": (C.c_int, [C.POINTER(SgbcStack), C.c_double, C.c_int32, _D, _D, _D, _D, _D]),
     "dgtd_op_clear_probes": (C.c_int, [_P]),
     "dgtd_op_probe_reset": (C.c_int, [_P, _P]),
     "dgtd_op_probe_info": (C.c_int, [_P, _I64, _I64, _I64]),
@@ -174,6 +189,7 @@ SIGNATURES = {
     "dgtd_case_destroy": (None, [_P]),
     "dgtd_case_get_info": (C.c_int, [_P, C.POINTER(CaseInfo)]),
     "dgtd_case_auto_dt": (C.c_int, [_P, C.POINTER(C.c_double)]),
+    "dgtd_case_sgbc": (C.c_int, [_P, C.POINTER(SgbcStack), C.POINTER(SgbcLayer), _I32]),
     "dgtd_case_mesh": (C.c_int, [_P, C.POINTER(MeshDesc)]),
     "dgtd_case_planewaves": (C.c_int, [_P, C.POINTER(PlaneWave), C.c_int32]),
     "dgtd_case_point_probes": (C.c_int, [_P, _D]),
@@ -338,6 +354,45 @@ def _stream(s) -> Optional[int]:
     return int(s.cuda_stream) if hasattr(s, "cuda_stream") else int(s)
 
 
+def _sgbc_structs(stacks: Sequence[dict]):
+    """ctypes stacks (and the layer arrays they point to) from dicts {"layers": [{"eps", "mu",
+    "sigma", "width", "segments", "order"}], "left": bc, "right": bc, "sub_dt": s}."""
+    keep = []
+    arr = (SgbcStack * max(1, len(stacks)))()
+    for i, st in enumerate(stacks):
+        L = (SgbcLayer * len(st["layers"]))()
+        for j, l in enumerate(st["layers"]):
+            L[j] = SgbcLayer(float(l.get("eps", 1.0)), float(l.get("mu", 1.0)), float(l.get("sigma", 0.0)),
+                             float(l["width"]), int(l["segments"]), int(l["order"]))
+        keep.append(L)
+        arr[i] = SgbcStack(len(st["layers"]), C.cast(L, C.POINTER(SgbcLayer)), int(st.get("left", 0)),
+                           int(st.get("right", 0)), float(st.get("sub_dt", 0.0)))
+    return arr, keep
+
+
+def sgbc_stack_operator(stack: dict) -> dict:
+    """The thin-layer sub-solver of one stack, built on the host: its operator A [n, n] and its
+    interface rows (no GPU)."""
+    arr, keep = _sgbc_structs([stack])
+    n, il, ir = C.c_int64(), C.c_int64(), C.c_int64()
+    _check(lib().dgtd_sgbc_stack_operator(arr, C.byref(n), C.byref(il), C.byref(ir), None, 0), "sgbc_stack_operator")
+    A = np.zeros((n.value, n.value))
+    _check(lib().dgtd_sgbc_stack_operator(arr, None, None, None, _dp(A), A.size), "sgbc_stack_operator")
+    return {"A": A, "n": n.value, "idx_left": il.value, "idx_right": ir.value}
+
+
+def sgbc_stack_maps(stack: dict, span: float, nsteps: int) -> dict:
+    """Composed sub-step maps of one stack (no GPU): interface values R x + G g with ghosts held,
+    state F x + Vo g_old + Vn g_new with ghosts interpolated."""
+    n = sgbc_stack_operator(stack)["n"]
+    arr, keep = _sgbc_structs([stack])
+    out = {"R": np.zeros((12, n)), "G": np.zeros((12, 12)), "F": np.zeros((n, n)), "Vo": np.zeros((n, 12)),
+           "Vn": np.zeros((n, 12))}
+    _check(lib().dgtd_sgbc_stack_maps(arr, float(span), int(nsteps), *(_dp(out[k]) for k in ("R", "G", "F", "Vo", "Vn"))),
+           "sgbc_stack_maps")
+    return out
+
+
 def _mesh_desc(m: Mesh) -> MeshDesc:
     d = MeshDesc()
     d.dim = 3
@@ -438,6 +493,22 @@ class Operator:
         v = C.c_double()
         _check(lib().dgtd_op_estimate_dt(self._h, cfl, C.byref(v)), "estimate_dt")
         return v.value
+
+    def set_sgbc(self, stacks: Sequence[dict], face_stack) -> None:
+        """Thin-layer stacks of the mesh's SGBC interior faces (code BC_SGBC), face_stack[i] the
+        stack of the i-th such face in mesh order (see sgbc_stack_operator for the stack dicts)."""
+        arr, keep = _sgbc_structs(stacks)
+        fs = np.ascontiguousarray(face_stack, dtype=np.int32)
+        _check(lib().dgtd_op_set_sgbc(self._h, arr, len(stacks), _ip(fs)), "dgtd_op_set_sgbc")
+
+    def sgbc_states(self) -> np.ndarray:
+        """The sub-solver states, pair after pair (empty without SGBC)."""
+        npair, sl = C.c_int64(), C.c_int64()
+        _check(lib().dgtd_op_sgbc_states(self._h, C.byref(npair), C.byref(sl), None, 0), "sgbc_states")
+        out = np.zeros(sl.value)
+        if sl.value:
+            _check(lib().dgtd_op_sgbc_states(self._h, None, None, _dp(out), out.size), "sgbc_states")
+        return out
 
     # -- device API (torch tensors or raw device addresses)
     def mult(self, x, y, t: float = 0.0, stream=None) -> None:
@@ -719,6 +790,22 @@ class Case:
         _check(lib().dgtd_case_planewaves(self._h, a, n), "dgtd_case_planewaves")
         return [dict(propagation=list(a[i].propagation), polarization=list(a[i].polarization), spread=a[i].spread,
                      mean=a[i].mean, frequency=a[i].frequency, batch=a[i].batch) for i in range(n)]
+
+    def sgbc(self):
+        """The case's thin-layer stacks (dicts as Operator.set_sgbc takes them) and the stack of each
+        SGBC interior face in mesh order."""
+        ns, nl, nf = self.info["n_sgbc_stacks"], self.info["n_sgbc_layers"], self.info["n_sgbc_faces"]
+        st = (SgbcStack * max(1, ns))()
+        ly = (SgbcLayer * max(1, nl))()
+        fs = np.zeros(nf, np.int32)
+        _check(lib().dgtd_case_sgbc(self._h, st, ly, _ip(fs) if nf else None), "dgtd_case_sgbc")
+        stacks = []
+        for i in range(ns):
+            layers = [dict(eps=st[i].layers[j].eps_r, mu=st[i].layers[j].mu_r, sigma=st[i].layers[j].sigma,
+                           width=st[i].layers[j].width, segments=st[i].layers[j].segments, order=st[i].layers[j].order)
+                      for j in range(st[i].n_layers)]
+            stacks.append(dict(layers=layers, left=st[i].left_bc, right=st[i].right_bc, sub_dt=st[i].sub_dt))
+        return stacks, fs
 
     def point_probes(self) -> np.ndarray:
         p = np.zeros((self.info["n_point_probes"], 3))

@@ -20,6 +20,7 @@
 #include "mesh.hpp"
 #include "probes.hpp"
 #include "refelem.hpp"
+#include "sgbc_dev.hpp"
 #include "single_tc.hpp"
 
 namespace {
@@ -133,6 +134,8 @@ struct dgtd_op {
     // point probes / DFT accumulators, sampled by dgtd_op_step every probes->every() steps
     std::unique_ptr<dgtd::ProbeSet> probes;
     int64_t probe_steps = 0;
+    // thin-layer (SGBC) sub-solvers of the mesh's DGTD_BC_SGBC faces (dgtd_op_set_sgbc)
+    std::unique_ptr<dgtd::SgbcOp> sgbc;
 
     ~dgtd_op()
     {
@@ -261,11 +264,19 @@ void ensure_sources(dgtd_op* op)
 
 bool has_sources(const dgtd_op* op) { return op->mesh.tfsf_elems.size() > 0 && !op->pw_host.empty(); }
 
-// One fused stage on the plain FP64 form.
+// One fused stage on the plain FP64 form (with the thin-layer coupling around it when the mesh
+// has SGBC faces).
 void run_stage(dgtd_op* op, dgtd::StageArgs A, double t, cudaStream_t s)
 {
     A.t = t;
     A.batch = op->batch;
+    if (!op->mesh.sgbc_faces.empty()) {
+        if (!op->sgbc)
+            throw std::invalid_argument("the mesh has thin-layer (SGBC) faces: give their stacks with dgtd_op_set_sgbc");
+        const int64_t before = op->sgbc->launches();
+        op->sgbc->before_stage(op->dev, A, t, s);
+        g_launches.fetch_add(op->sgbc->launches() - before, std::memory_order_relaxed);
+    }
     if (has_sources(op)) {
         const int known = op->skip_bound.decide(t);
         if (known < 0) {
@@ -284,6 +295,11 @@ void run_stage(dgtd_op* op, dgtd::StageArgs A, double t, cudaStream_t s)
     }
     ck(dgtd::launch_stage_fp64(op->dev, A, s), "stage kernel");
     g_launches.fetch_add(1, std::memory_order_relaxed);
+    if (op->sgbc) {
+        const int64_t before = op->sgbc->launches();
+        op->sgbc->after_stage(op->dev, A, s);
+        g_launches.fetch_add(op->sgbc->launches() - before, std::memory_order_relaxed);
+    }
 }
 
 // FP64 defect correction of the batched form (dgtd_op_set_defect_correction): from the state in
@@ -517,6 +533,8 @@ int dgtd_op_create(const dgtd_mesh_desc* mesh, const dgtd_op_opts* opts, dgtd_op
         op->alpha = opts->alpha;
         const int Np = op->ref.Np, Nfp = op->ref.Nfp;
         op->state_len = 6 * op->mesh.K * Np * static_cast<int64_t>(op->batch);
+        if (!op->mesh.sgbc_faces.empty() && (op->precision != DGTD_FP64 || op->batch != 1))
+            return fail(DGTD_ERR_UNSUPPORTED, "thin-layer (SGBC) faces need the FP64 form with one incidence");
         for (auto c : op->mesh.fcode)
             if (c == dgtd::FACE_TFSF_TF || c == dgtd::FACE_TFSF_SF) ++op->n_tfsf_faces;
 
@@ -698,6 +716,8 @@ int dgtd_op_mult(dgtd_op* op, const void* d_x, void* d_y, double t, void* stream
         A.in = static_cast<const double*>(d_x);
         A.out = static_cast<double*>(d_y);
         run_stage(op, A, t, static_cast<cudaStream_t>(stream));
+    } catch (const std::invalid_argument& e) {
+        return fail(DGTD_ERR_UNSUPPORTED, e.what());
     } catch (const std::exception& e) {
         return fail(DGTD_ERR_CUDA, e.what());
     }
@@ -1207,6 +1227,109 @@ int dgtd_op_probe_read(dgtd_op* op, double* h_point_dft, double* h_surface_dft, 
     return DGTD_OK;
 }
 
+namespace {
+
+std::vector<dgtd::SgbcStackSpec> sgbc_specs(const dgtd_sgbc_stack* stacks, int32_t n)
+{
+    std::vector<dgtd::SgbcStackSpec> out;
+    for (int32_t i = 0; i < n; ++i) {
+        const dgtd_sgbc_stack& S = stacks[i];
+        if (S.n_layers < 1 || !S.layers) throw std::invalid_argument("SGBC stack without layers");
+        dgtd::SgbcStackSpec sp;
+        for (int32_t l = 0; l < S.n_layers; ++l) {
+            const dgtd_sgbc_layer& L = S.layers[l];
+            sp.layers.push_back({L.eps_r, L.mu_r, L.sigma, L.width, L.segments, L.order});
+        }
+        sp.left_bc = S.left_bc;
+        sp.right_bc = S.right_bc;
+        sp.sub_dt = S.sub_dt;
+        out.push_back(sp);
+    }
+    return out;
+}
+
+}  // namespace
+
+int dgtd_op_set_sgbc(dgtd_op* op, const dgtd_sgbc_stack* stacks, int32_t n_stacks, const int32_t* face_stack)
+{
+    if (!op || !stacks || n_stacks < 1) return fail(DGTD_ERR_INVALID, "NULL argument or no stacks");
+    const int64_t nf = static_cast<int64_t>(op->mesh.sgbc_faces.size() / 4);
+    if (nf == 0) return fail(DGTD_ERR_INVALID, "the mesh has no thin-layer (SGBC) faces");
+    if (!face_stack) return fail(DGTD_ERR_INVALID, "face_stack is NULL");
+    try {
+        std::vector<int32_t> fs(face_stack, face_stack + nf);
+        auto S = std::make_unique<dgtd::SgbcOp>(op->mesh, op->ref, sgbc_specs(stacks, n_stacks), fs);
+        op->sgbc = std::move(S);
+    } catch (const std::invalid_argument& e) {
+        return fail(DGTD_ERR_UNSUPPORTED, e.what());
+    } catch (const std::exception& e) {
+        return fail(DGTD_ERR_CUDA, e.what());
+    }
+    return DGTD_OK;
+}
+
+int dgtd_op_sgbc_states(const dgtd_op* op, int64_t* n_pairs, int64_t* state_len, double* h_states, int64_t cap)
+{
+    if (!op) return fail(DGTD_ERR_INVALID, "NULL argument");
+    const int64_t np = op->sgbc ? op->sgbc->n_pairs() : 0, sl = op->sgbc ? op->sgbc->state_len() : 0;
+    if (n_pairs) *n_pairs = np;
+    if (state_len) *state_len = sl;
+    if (h_states && op->sgbc) {
+        if (cap < sl) return fail(DGTD_ERR_INVALID, "state buffer too small");
+        try { op->sgbc->read_states(h_states); }
+        catch (const std::exception& e) { return fail(DGTD_ERR_CUDA, e.what()); }
+    }
+    return DGTD_OK;
+}
+
+int dgtd_sgbc_stack_operator(const dgtd_sgbc_stack* stack, int64_t* n, int64_t* idx_left, int64_t* idx_right,
+                             double* A, int64_t cap)
+{
+    if (!stack) return fail(DGTD_ERR_INVALID, "NULL argument");
+    try {
+        const dgtd::SgbcStack1D S = dgtd::build_sgbc_stack(sgbc_specs(stack, 1)[0]);
+        if (n) *n = S.n;
+        if (idx_left) *idx_left = S.idx_left;
+        if (idx_right) *idx_right = S.idx_right;
+        if (A) {
+            if (cap < S.n * S.n) return fail(DGTD_ERR_INVALID, "operator buffer too small");
+            std::memcpy(A, S.A.data(), S.A.size() * sizeof(double));
+        }
+    } catch (const std::invalid_argument& e) {
+        return fail(DGTD_ERR_UNSUPPORTED, e.what());
+    } catch (const std::exception& e) {
+        return fail(DGTD_ERR_INVALID, e.what());
+    }
+    return DGTD_OK;
+}
+
+int dgtd_sgbc_stack_maps(const dgtd_sgbc_stack* stack, double span, int32_t nsteps, double* R, double* G, double* F,
+                         double* Vo, double* Vn)
+{
+    if (!stack || nsteps < 1 || !(span > 0.0)) return fail(DGTD_ERR_INVALID, "NULL stack, nsteps < 1 or span <= 0");
+    try {
+        const dgtd::SgbcStack1D S = dgtd::build_sgbc_stack(sgbc_specs(stack, 1)[0]);
+        if (R || G) {
+            const dgtd::SgbcStageMap M = dgtd::sgbc_stage_map(S, span, nsteps);
+            if (R) std::memcpy(R, M.R.data(), M.R.size() * sizeof(double));
+            if (G) std::memcpy(G, M.G.data(), M.G.size() * sizeof(double));
+        }
+        if (F || Vo || Vn) {
+            const dgtd::SgbcFinalMap M = dgtd::sgbc_final_map(S, span, nsteps);
+            if (F)
+                for (int64_t i = 0; i < S.n; ++i)
+                    for (int64_t j = 0; j < S.n; ++j) F[i * S.n + j] = M.FT[j * S.n + i];
+            if (Vo) std::memcpy(Vo, M.Vo.data(), M.Vo.size() * sizeof(double));
+            if (Vn) std::memcpy(Vn, M.Vn.data(), M.Vn.size() * sizeof(double));
+        }
+    } catch (const std::invalid_argument& e) {
+        return fail(DGTD_ERR_UNSUPPORTED, e.what());
+    } catch (const std::exception& e) {
+        return fail(DGTD_ERR_INVALID, e.what());
+    }
+    return DGTD_OK;
+}
+
 int dgtd_mesh_validate(const dgtd_mesh_desc* mesh, const dgtd_op_opts* opts, dgtd_op_info* info)
 {
     if (!opts || !info) return fail(DGTD_ERR_INVALID, "NULL argument");
@@ -1385,6 +1508,9 @@ int dgtd_op_step_noalloc(dgtd_op* op, void* d_state, double t0, double dt, int32
     if (integrator != DGTD_RK4 && integrator != DGTD_LSERK4) return fail(DGTD_ERR_INVALID, "unknown integrator");
     if (op->precision != DGTD_FP64)
         return fail(DGTD_ERR_UNSUPPORTED, "dgtd_op_step_noalloc supports the FP64 form only");
+    if (!op->mesh.sgbc_faces.empty())
+        return fail(DGTD_ERR_UNSUPPORTED, "dgtd_op_step_noalloc does not step thin-layer (SGBC) faces "
+                                          "(their sub-step maps are built on first use)");
     if (op->state_len > kNoAllocMaxState)
         return fail(DGTD_ERR_INVALID, "dgtd_op_step_noalloc: state of " + std::to_string(op->state_len) +
                                           " entries exceeds the fixed scratch limit of " +

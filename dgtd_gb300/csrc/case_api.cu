@@ -73,6 +73,31 @@ int dgtd_case_get_info(const dgtd_case* cs, dgtd_case_info* info)
     info->n_surfaces = static_cast<int32_t>(c.surfaces.size());
     info->n_elements = static_cast<int64_t>(c.elements.size() / 4);
     info->n_vertices = static_cast<int64_t>(c.vertices.size() / 3);
+    info->n_sgbc_stacks = static_cast<int32_t>(c.sgbc_stacks.size());
+    int32_t nl = 0;
+    for (const auto& st : c.sgbc_stacks) nl += static_cast<int32_t>(st.layers.size());
+    info->n_sgbc_layers = nl;
+    info->n_sgbc_faces = static_cast<int64_t>(c.sgbc_face_stack.size());
+    return DGTD_OK;
+}
+
+int dgtd_case_sgbc(const dgtd_case* cs, dgtd_sgbc_stack* stacks, dgtd_sgbc_layer* layers, int32_t* face_stack)
+{
+    if (!cs) return cfail(DGTD_ERR_INVALID, "NULL argument");
+    const dgtd::Case& c = cs->c;
+    if (!c.sgbc_stacks.empty() && (!stacks || !layers)) return cfail(DGTD_ERR_INVALID, "NULL stack or layer array");
+    if (!c.sgbc_face_stack.empty() && !face_stack) return cfail(DGTD_ERR_INVALID, "NULL face_stack");
+    int32_t li = 0;
+    for (size_t i = 0; i < c.sgbc_stacks.size(); ++i) {
+        const dgtd::SgbcStackSpec& sp = c.sgbc_stacks[i];
+        stacks[i].n_layers = static_cast<int32_t>(sp.layers.size());
+        stacks[i].layers = layers + li;
+        stacks[i].left_bc = sp.left_bc;
+        stacks[i].right_bc = sp.right_bc;
+        stacks[i].sub_dt = sp.sub_dt;
+        for (const auto& L : sp.layers) layers[li++] = dgtd_sgbc_layer{L.eps, L.mu, L.sigma, L.width, L.segments, L.order};
+    }
+    std::copy(c.sgbc_face_stack.begin(), c.sgbc_face_stack.end(), face_stack);
     return DGTD_OK;
 }
 
@@ -181,6 +206,15 @@ int dgtd_case_run(const dgtd_case* cs, const dgtd_case_run_opts* ro, double* h_s
         ok(dgtd_op_create(&m, &o, &op), "dgtd_op_create");
         if (!c.waves.empty())
             ok(dgtd_op_set_planewaves(op, c.waves.data(), static_cast<int32_t>(c.waves.size())), "set_planewaves");
+        if (!c.sgbc_face_stack.empty()) {
+            dgtd_case_info ci;
+            ok(dgtd_case_get_info(cs, &ci), "case info");
+            std::vector<dgtd_sgbc_stack> st(ci.n_sgbc_stacks);
+            std::vector<dgtd_sgbc_layer> ly(ci.n_sgbc_layers);
+            std::vector<int32_t> fs(ci.n_sgbc_faces);
+            ok(dgtd_case_sgbc(cs, st.data(), ly.data(), fs.data()), "case SGBC stacks");
+            ok(dgtd_op_set_sgbc(op, st.data(), ci.n_sgbc_stacks, fs.data()), "set_sgbc");
+        }
         double dt = c.dt;
         if (!(dt > 0.0)) ok(dgtd_case_auto_dt(cs, &dt), "automatic time step");
         dgtd_op_info info;

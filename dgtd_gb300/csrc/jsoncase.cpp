@@ -8,6 +8,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <fstream>
+#include <limits>
 #include <set>
 #include <sstream>
 #include <stdexcept>
@@ -438,6 +439,114 @@ void check_case_naming(const std::string& json_path, const Json& J, const std::s
 
 }  // namespace
 
+namespace {
+
+// The largest frequency of the case's pulses (calculateMaximumSourceFrequency, driver.cpp:20-61):
+// modulated Gaussians give carrier + c / (2 spread), else plain Gaussians c / (2 min spread),
+// else 1 GHz.
+double max_source_frequency(const Json& J)
+{
+    double min_spread = 1e300, max_freq = 0.0;
+    bool gaussian = false, modulated = false;
+    if (const Json* srcs = J.find("sources"))
+        for (const Json& s : srcs->arr) {
+            const Json* mag = s.find("magnitude");
+            if (!mag) continue;
+            if (mag->has("frequency") && mag->has("spread")) {
+                const double f_edge = mag->at("frequency").number() + kSpeedOfLight / (2.0 * mag->at("spread").number());
+                if (f_edge > max_freq) { max_freq = f_edge; modulated = true; }
+            } else if (mag->has("type") && mag->at("type").type == Json::String && mag->at("type").string() == "gaussian" &&
+                       mag->has("spread")) {
+                const double sp = mag->at("spread").number();
+                if (sp > 0.0 && sp < min_spread) { min_spread = sp; gaussian = true; }
+            }
+        }
+    if (modulated) return max_freq;
+    if (gaussian) return kSpeedOfLight / (2.0 * min_spread);
+    return 1e9;
+}
+
+int sgbc_side(const Json& v)
+{
+    // assignBoundaryType (driver.cpp:1225-1239)
+    const std::string& t = v.string();
+    if (t == "PEC") return DGTD_BC_PEC;
+    if (t == "PMC") return DGTD_BC_PMC;
+    if (t == "SMA") return DGTD_BC_SMA;
+    throw std::runtime_error("Incorrect sgbc_bdr_type defined in .json.");
+}
+
+// One "SGBC" boundary entry (driver.cpp:1298-1462): its layers with the automatic order and
+// segment count, the optional sheets, and the sub-solver's recommended step
+// (SGBCWrapper ctor, SolverExtension.cpp:509-541).
+SgbcStackSpec parse_sgbc(const Json& bj, double max_freq)
+{
+    constexpr double mu0 = 4.0 * M_PI * 1e-7, eps0 = 8.8541878188e-12;
+    SgbcStackSpec sp;
+    std::vector<double> skin_depths;
+    auto layer_of = [&](const Json& mj) {
+        SgbcLayer L;
+        L.eps = mj.has("relative_permittivity") ? mj.at("relative_permittivity").number() : 1.0;
+        L.mu = mj.has("relative_permeability") ? mj.at("relative_permeability").number() : 1.0;
+        if (!mj.has("bulk_conductivity"))
+            throw std::runtime_error("SGBC layer defined without 'bulk_conductivity' parameter. Verify .json parameters.");
+        const double sigma_si = mj.at("bulk_conductivity").number();
+        L.sigma = sigma_si * kFreeSpaceImpedance;
+        if (!mj.has("material_width")) throw std::runtime_error("SGBC layer must define 'material_width'.");
+        L.width = mj.at("material_width").number();
+        const double mu_si = L.mu * mu0, eps_si = L.eps * eps0;
+        const double peclet = sigma_si > 0.0 ? sigma_si / (max_freq * eps_si) : 0.0;
+        if (peclet > 100.0) L.order = 2;
+        else if (peclet < 0.1 && sigma_si < 1e-3) L.order = 4;
+        else L.order = 3;
+        const double wavelength = 1.0 / (max_freq * std::sqrt(mu_si * eps_si));
+        const int segs_per_wavelength = static_cast<int>(std::ceil(20.0 / L.order));
+        const double dx_wave = wavelength / segs_per_wavelength;
+        double dx_skin = std::numeric_limits<double>::max(), skin = 0.0;
+        if (sigma_si > 0.0) {
+            skin = 1.0 / std::sqrt(M_PI * max_freq * mu_si * sigma_si);
+            dx_skin = skin / 2.0;
+        }
+        const int autoseg = static_cast<int>(std::ceil(L.width / std::min(dx_wave, dx_skin)));
+        L.segments = std::clamp(autoseg, 4, 1000);
+        if (mj.has("num_of_segments")) L.segments = mj.at("num_of_segments").integer();
+        if (mj.has("order")) L.order = mj.at("order").integer();
+        sp.layers.push_back(L);
+        skin_depths.push_back((sigma_si > 0.0 && skin > 0.0) ? L.width / skin : 0.0);
+    };
+    if (const Json* ls = bj.find("layers")) {
+        for (const Json& lj : ls->arr) layer_of(lj);
+    } else if (const Json* mj = bj.find("material")) {
+        layer_of(*mj);
+    } else {
+        throw std::runtime_error("SGBC boundary must define either 'material' or 'layers'. Verify .json parameters.");
+    }
+    bool left = false, right = false;
+    auto sides = [&](const Json& src) {
+        if (const Json* sb = src.find("sgbc_boundaries")) {
+            if (const Json* l = sb->find("left")) { left = true; sp.left_bc = sgbc_side(*l); }
+            if (const Json* r = sb->find("right")) { right = true; sp.right_bc = sgbc_side(*r); }
+        }
+    };
+    sides(bj);
+    if (!left && !right)
+        if (const Json* mj = bj.find("material")) sides(*mj);
+    // recommended sub-step: half the wave crossing time of a segment, relaxed by min(N^2, 50) for
+    // layers N > 3 skin depths thick, minimum over layers (computed in seconds, as the reference)
+    double rec = std::numeric_limits<double>::max();
+    for (size_t i = 0; i < sp.layers.size(); ++i) {
+        const SgbcLayer& L = sp.layers[i];
+        const double dx = L.width / L.segments;
+        double layer_dt = (dx * std::sqrt(L.eps * L.mu)) / kSpeedOfLight * 0.5;
+        if (skin_depths[i] > 3.0) layer_dt *= std::min(skin_depths[i] * skin_depths[i], 50.0);
+        rec = std::min(rec, layer_dt);
+    }
+    sp.sub_dt = rec * kSpeedOfLight;
+    return sp;
+}
+
+}  // namespace
+
 Case load_case(const std::string& json_path)
 {
     std::ifstream jf(json_path);
@@ -661,6 +770,8 @@ Case load_case(const std::string& json_path)
     // the condition (the reference applies interior-boundary tags through interior face
     // integrators only, so that tag's faces on the domain boundary keep no condition: open).
     std::map<int, int> bc_of_tag;
+    std::map<int, int> sgbc_of_tag;   // tag -> stack
+    const double max_freq = max_source_frequency(J);
     if (const Json* bs = model.find("boundaries")) {
         for (size_t b = 0; b < bs->arr.size(); ++b) {
             const Json& bj = bs->arr[b];
@@ -675,7 +786,13 @@ Case load_case(const std::string& json_path)
             if (type == "PEC") code = DGTD_BC_PEC;
             else if (type == "PMC") code = DGTD_BC_PMC;
             else if (type == "SMA") code = DGTD_BC_SMA;
-            else throw std::runtime_error("boundary type '" + type + "' is not supported (PEC, PMC, SMA)");
+            else if (type == "SGBC") code = DGTD_BC_SGBC;
+            else throw std::runtime_error("boundary type '" + type + "' is not supported (PEC, PMC, SMA, SGBC)");
+            if (code == DGTD_BC_SGBC) {
+                const int idx = static_cast<int>(c.sgbc_stacks.size());
+                c.sgbc_stacks.push_back(parse_sgbc(bj, max_freq));
+                for (int t : tags) sgbc_of_tag.emplace(t, idx);
+            }
             for (int t : tags) bc_of_tag.emplace(t, code);
         }
     }
@@ -698,7 +815,17 @@ Case load_case(const std::string& json_path)
             if (tri_nelem[t] == 2) {
                 c.int_faces.insert(c.int_faces.end(), {a, b, d});
                 c.int_codes.push_back(it->second);
+                if (it->second == DGTD_BC_SGBC) c.sgbc_face_stack.push_back(sgbc_of_tag.at(tag));
             }
+        } else if (it->second == DGTD_BC_SGBC) {
+            // an SGBC tag on the domain boundary: the reference's operator gives these faces the
+            // boundary coefficients {1, 1} (SMA's) scaled by alpha (DGOperatorFactory.h:21-35,
+            // 483-497), and its source-face operator, assembled on interior faces, injects nothing
+            if (c.alpha != 1.0)
+                throw std::runtime_error("SGBC on the domain boundary (tag " + std::to_string(tag) +
+                                         ") is supported with upwind_alpha 1 only (SMA coefficients scaled by alpha)");
+            c.bdr_faces.insert(c.bdr_faces.end(), {a, b, d});
+            c.bdr_codes.push_back(DGTD_BC_SMA);
         } else {
             c.bdr_faces.insert(c.bdr_faces.end(), {a, b, d});
             c.bdr_codes.push_back(it->second);
@@ -746,6 +873,9 @@ Case load_case(const std::string& json_path)
                     c.surfaces.push_back(s);
                 }
     }
+    if (!c.sgbc_face_stack.empty() && c.evolution_operator != "global")
+        throw std::runtime_error("thin-layer (SGBC) boundaries run with evolution_operator 'global' only "
+                                 "(the reference couples them in GlobalEvolution)");
     return c;
 }
 

@@ -19,6 +19,7 @@
 #include <vector>
 
 #include "../../include/dgtd_gb300.h"
+#include "sgbc.hpp"
 
 namespace dgtd {
 
@@ -88,6 +89,10 @@ struct Case {
     std::vector<int32_t> elements;
     std::vector<double> eps, mu, sigma;
     std::vector<int32_t> bdr_faces, bdr_codes, tfsf_faces, int_faces, int_codes;
+    // thin-layer (SGBC) boundaries: one stack per "SGBC" boundary entry, and the stack of each
+    // interior face given with code DGTD_BC_SGBC (in int_faces order)
+    std::vector<SgbcStackSpec> sgbc_stacks;
+    std::vector<int32_t> sgbc_face_stack;
     // sources
     std::vector<dgtd_planewave> waves;
     std::vector<CaseInitialField> initial;

@@ -200,7 +200,13 @@ MeshTables build_tables(const MeshInput& in, const RefTet& ref)
         if (!find_face(in.int_faces[3 * b], in.int_faces[3 * b + 1], in.int_faces[3 * b + 2], e1, f1, e2, f2) || e2 < 0)
             throw std::runtime_error("interior boundary face is not shared by two elements");
         int code = in.int_codes[b];
-        if (code < 1 || code > 3) throw std::runtime_error("unknown interior boundary code");
+        if (code < 1 || code > 4) throw std::runtime_error("unknown interior boundary code");
+        if (code == 4) {   // thin layer: the first element is the lower index (the face's owner)
+            T.fcode[e1 * 4 + f1] = FACE_SGBC;
+            T.fcode[e2 * 4 + f2] = FACE_SGBC;
+            T.sgbc_faces.insert(T.sgbc_faces.end(), {static_cast<int32_t>(e1), f1, static_cast<int32_t>(e2), f2});
+            continue;
+        }
         T.fcode[e1 * 4 + f1] = FACE_INT_PEC + (code - 1);
         T.fcode[e2 * 4 + f2] = FACE_INT_PEC + (code - 1);
     }

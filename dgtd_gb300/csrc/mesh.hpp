@@ -28,6 +28,8 @@ enum FaceCode : int32_t {
     FACE_INT_PMC = 7,
     FACE_INT_SMA = 8,
     FACE_OPEN = 9,        // boundary face with no condition: zero jump
+    FACE_SGBC = 10,       // interior thin-layer (SGBC) face: no flux in the stage kernels; the SGBC
+                          // kernels add the flux with the sub-solver's interface values
 };
 
 struct MeshInput {
@@ -38,8 +40,8 @@ struct MeshInput {
     std::vector<int32_t> bdr_faces;    // [nb][3] (dim 3) or [nb][1] (dim 1) vertex ids
     std::vector<int32_t> bdr_codes;    // [nb] 1 PEC, 2 PMC, 3 SMA, 0 open
     std::vector<int32_t> tfsf_faces;   // [nt][3]: oriented so the winding normal points into the TF side
-    std::vector<int32_t> int_faces;    // [ni][3]: interior PEC/PMC/SMA sheets
-    std::vector<int32_t> int_codes;    // [ni] 1 PEC, 2 PMC, 3 SMA
+    std::vector<int32_t> int_faces;    // [ni][3]: interior PEC/PMC/SMA sheets and thin layers
+    std::vector<int32_t> int_codes;    // [ni] 1 PEC, 2 PMC, 3 SMA, 4 SGBC
 };
 
 // Device-ready tables (host copies).
@@ -54,6 +56,8 @@ struct MeshTables {
     std::vector<int32_t> fcode;         // [K][Nfaces]
     std::vector<int32_t> nbr;           // [K][Nfaces] neighbour element or -1
     std::vector<int32_t> tfsf_elems;    // elements adjacent to a TF/SF face (unique, ascending)
+    std::vector<int32_t> sgbc_faces;    // [n][4] e1 f1 e2 f2 of the SGBC faces, in input order
+                                        // (e1 < e2: the face's first element)
     std::vector<int32_t> elem_vertices; // [K][4] vertex ids (input order)
     std::vector<double> vertices;       // [nv][3]
     double min_edge = 0.0;              // smallest edge length

@@ -824,6 +824,9 @@ int dgtd_server_submit(dgtd_server* s, const dgtd_request* q, int64_t* id_out)
             if (!m->int_faces || !m->int_codes) return sfail(DGTD_ERR_INVALID, "interior faces without arrays");
             in.int_faces.assign(m->int_faces, m->int_faces + 3 * m->n_int_faces);
             in.int_codes.assign(m->int_codes, m->int_codes + m->n_int_faces);
+            for (int32_t c : in.int_codes)
+                if (c == DGTD_BC_SGBC)
+                    return sfail(DGTD_ERR_UNSUPPORTED, "served requests do not take thin-layer (SGBC) faces");
         }
         for (int i = 0; i < q->n_waves; ++i) {
             const dgtd_planewave& w = q->waves[i];

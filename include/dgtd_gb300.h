@@ -41,6 +41,7 @@ extern "C" {
 #define DGTD_BC_PEC 1
 #define DGTD_BC_PMC 2
 #define DGTD_BC_SMA 3
+#define DGTD_BC_SGBC 4   /* interior faces only: a thin-layer stack (dgtd_op_set_sgbc) */
 
 /* Precision forms. */
 #define DGTD_FP64 0        /* plain form: FP64 state and arithmetic */
@@ -73,7 +74,7 @@ typedef struct dgtd_mesh_desc {
     const int32_t* tfsf_faces;  /* [n][3], winding normal points into the total-field side */
     int64_t n_int_faces;
     const int32_t* int_faces;   /* [n][3] interior PEC/PMC/SMA sheets */
-    const int32_t* int_codes;   /* [n] DGTD_BC_PEC/PMC/SMA */
+    const int32_t* int_codes;   /* [n] DGTD_BC_PEC/PMC/SMA/SGBC */
 } dgtd_mesh_desc;
 
 typedef struct dgtd_op_opts {
@@ -175,7 +176,8 @@ int dgtd_op_run_host(dgtd_op* op, double* h_state, double t0, double dt, double 
  * in the reference; it serves callers that cannot allow a device allocation during
  * stepping. The first call on each device looks up the array's address (set-up: make
  * that call before any stream capture). Errors: DGTD_ERR_INVALID when state_len
- * exceeds dgtd_noalloc_max_state(), DGTD_ERR_UNSUPPORTED for the FP32 forms.
+ * exceeds dgtd_noalloc_max_state(), DGTD_ERR_UNSUPPORTED for the FP32 forms and for
+ * meshes with thin-layer (SGBC) faces (their sub-step maps are built on first use).
  * Installed probes (dgtd_op_set_probes) are sampled after every `every`-th step on the
  * same step counter as dgtd_op_step, so the two calls may be mixed on one operator.
  * The array keeps the last call's contents; calls that overlap on the GPU race. */
@@ -301,6 +303,63 @@ typedef struct dgtd_probe_spec {
 
 /* Install probes (replaces earlier ones; sums start at zero; the step counter restarts). */
 int dgtd_op_set_probes(dgtd_op* op, const dgtd_probe_spec* spec);
+
+/* ---- thin-layer boundaries (SGBC) ----------------------------------------------------------
+ * A stack of thin layers on interior faces, each face node pair coupled to its own 1D DG
+ * sub-solver (reference SGBCWrapper, src/solver/SolverExtension.cpp:49-559, and its coupling in
+ * GlobalEvolution, src/evolution/GlobalEvolution.cpp:48-300, 395-545, 639-1001):
+ *  - the sub-solver mesh is the layers with max(3, p+1) vacuum ghost segments on each side
+ *    (width = total width / total segments), SMA at its two ends, and the stack's optional
+ *    sheets at the ghost/layer interfaces; order p = max over layers; upwind alpha 1; SDIRK33
+ *    steps with a dense implicit solve (at most 600 sub-solver unknowns: larger stacks fail with
+ *    DGTD_ERR_UNSUPPORTED, the reference iterates with GMRES there);
+ *  - the pair of a face node is (node of the face's first element = the lower element index,
+ *    partner node of the second); the sub-solver's x axis is the first element's outward normal,
+ *    its left ghosts hold the first node's fields and its right ghosts the second's;
+ *  - every RK stage restarts the sub-solvers from the step's start and advances them to the stage
+ *    time (ceil(span / sub_dt) sub-steps) with the stage input as ghost data; the face flux of
+ *    the first element then takes the slab's left interface value as neighbour trace (or the left
+ *    sheet's mirror of its own value), the second element the right one; after the step the
+ *    sub-solvers advance over the whole step with ghosts interpolated between its two ends;
+ *  - pairs, and the whole coupling, are skipped while their fields stay below 1e-8.
+ * The FP64 form with one incidence and classical RK4 (and dgtd_op_mult) only:
+ * DGTD_ERR_UNSUPPORTED for the other forms, batches, LSERK4 and dgtd_op_step_noalloc. Before
+ * dgtd_op_set_sgbc, stepping an operator whose mesh has DGTD_BC_SGBC faces fails with
+ * DGTD_ERR_UNSUPPORTED. dgtd_op_mult at time t advances from the last step's start (0 before the
+ * first step). */
+typedef struct dgtd_sgbc_layer {
+    double eps_r, mu_r;
+    double sigma;        /* conductivity in solver units (S/m times the free-space impedance) */
+    double width;        /* mesh units */
+    int32_t segments;    /* sub-solver segments across the layer (>= 1) */
+    int32_t order;       /* polynomial order (1..16; the stack uses the largest) */
+} dgtd_sgbc_layer;
+
+typedef struct dgtd_sgbc_stack {
+    int32_t n_layers;
+    const dgtd_sgbc_layer* layers;   /* first layer next to the faces' first elements */
+    int32_t left_bc, right_bc;       /* 0: none, or DGTD_BC_PEC/PMC/SMA sheet on that side */
+    double sub_dt;                   /* the sub-solver's step (normalised time), the reference's
+                                        SGBCWrapper::getRecommendedDt; <= 0: one sub-step per span */
+} dgtd_sgbc_stack;
+
+/* face_stack[i]: stack of the i-th interior face given with DGTD_BC_SGBC (mesh order). The
+ * sub-solver states start at zero. */
+int dgtd_op_set_sgbc(dgtd_op* op, const dgtd_sgbc_stack* stacks, int32_t n_stacks, const int32_t* face_stack);
+/* Pairs and total sub-solver unknowns (0, 0 without SGBC); h_states (if not NULL, capacity
+ * `cap` entries) receives the pairs' states, pair after pair. */
+int dgtd_op_sgbc_states(const dgtd_op* op, int64_t* n_pairs, int64_t* state_len, double* h_states, int64_t cap);
+
+/* Host-side tables of one stack (no GPU): the sub-solver's size n and operator A [n][n]
+ * (A may be NULL to query n; cap = entries available in A), and its interface rows. */
+int dgtd_sgbc_stack_operator(const dgtd_sgbc_stack* stack, int64_t* n, int64_t* idx_left, int64_t* idx_right,
+                             double* A, int64_t cap);
+/* The composed maps of nsteps sub-steps over span (no GPU): with ghosts held at g, the 12
+ * interface values (left E,H then right E,H, face frame) are R x + G g, R [12][n], G [12][12];
+ * with ghosts interpolated from g_old to g_new, the state is F x + Vo g_old + Vn g_new, F [n][n],
+ * Vo and Vn [n][12]. Any output may be NULL. */
+int dgtd_sgbc_stack_maps(const dgtd_sgbc_stack* stack, double span, int32_t nsteps, double* R, double* G, double* F,
+                         double* Vo, double* Vn);
 int dgtd_op_clear_probes(dgtd_op* op);
 /* Zero the sums and the time series. */
 int dgtd_op_probe_reset(dgtd_op* op, void* stream);
@@ -338,6 +397,9 @@ typedef struct dgtd_case_info {
     int32_t n_surfaces;
     int64_t n_elements;
     int64_t n_vertices;
+    int32_t n_sgbc_stacks;       /* "SGBC" boundary entries (dgtd_case_sgbc) */
+    int32_t n_sgbc_layers;       /* layers over all stacks */
+    int64_t n_sgbc_faces;        /* interior faces given with DGTD_BC_SGBC in the case mesh */
 } dgtd_case_info;
 
 typedef struct dgtd_case_run_opts {
@@ -367,6 +429,18 @@ typedef struct dgtd_case_result {
 int dgtd_case_load(const char* json_path, dgtd_case** out);
 void dgtd_case_destroy(dgtd_case* c);
 int dgtd_case_get_info(const dgtd_case* c, dgtd_case_info* info);
+/* The case's thin-layer stacks (n_sgbc_stacks entries; their `layers` point into `layers`,
+ * n_sgbc_layers entries) and the stack of each DGTD_BC_SGBC face (n_sgbc_faces), ready for
+ * dgtd_op_set_sgbc. A "SGBC" boundary entry (driver.cpp:1298-1462) takes "material" (one layer) or
+ * "layers"; a layer needs "bulk_conductivity" (S/m) and "material_width", takes
+ * "relative_permittivity" / "relative_permeability" (1), and an automatic order (2, 3 or 4 by
+ * its loss tangent at the pulses' top frequency) and segment count (20 nodes per wavelength and
+ * two segments per skin depth, 4..1000) unless "order" / "num_of_segments" are given;
+ * "sgbc_boundaries": {"left", "right"} (PEC/PMC/SMA) at the entry or, when absent there, in its
+ * material. The sub-step is half a segment's wave crossing time, relaxed by min(N^2, 50) for
+ * layers N > 3 skin depths thick (SolverExtension.cpp:509-541). SGBC tags on the domain boundary
+ * become SMA faces (upwind_alpha 1 only); SGBC runs with evolution_operator "global" only. */
+int dgtd_case_sgbc(const dgtd_case* c, dgtd_sgbc_stack* stacks, dgtd_sgbc_layer* layers, int32_t* face_stack);
 
 /* The automatic time step a run of the case takes when solver_options.time_step is 0: the
  * reference's estimate for the case's evolution operator (Solver::estimateTimeStep,

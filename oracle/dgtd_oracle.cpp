@@ -316,12 +316,13 @@ struct CSR {
 // Row-wise triplet accumulation (rows are owned by one element block, so each
 // element's rows are built independently and merged).
 
-enum { BC_OPEN = 0, BC_PEC = 1, BC_PMC = 2, BC_SMA = 3 };
+enum { BC_OPEN = 0, BC_PEC = 1, BC_PMC = 2, BC_SMA = 3, BC_SGBC = 4 };
 
 struct Face {
     int64_t e1, e2;      // e2 = -1 on the boundary
     int f1, f2;
-    int kind;            // 0 interior, 1 boundary, 2 TF/SF (interior), 3 interior PEC/PMC/SMA sheet
+    int kind;            // 0 interior, 1 boundary, 2 TF/SF (interior), 3 interior PEC/PMC/SMA sheet,
+                         // 4 thin-layer (SGBC) sheet (interior)
     int bc;              // BC code for kinds 1 and 3
     double n[3];         // unit normal, outward from e1
     double jac;          // face Jacobian |J_f| w.r.t. the reference face (MFEM measure: tri 1/2, point 1)
@@ -347,13 +348,16 @@ struct Oracle {
     vector<int32_t> tfsf_elems;
     vector<PW> pws;
     // (A) global
-    bool have_csr = false; CSR Aglob, Ttfsf;
+    bool have_csr = false; CSR Aglob, Ttfsf, Tsgbc;
+    vector<int64_t> sgbc_faces;   // kind-4 faces in the order their interior-face records were given
     // (B) nodal
     bool have_nodal = false;
     vector<double> Dx;            // per shape class: [3][Np][Np] physical derivative M^-1 S_d
     vector<double> Lf;            // per shape class: [nfaces][Np][Nfp] M^-1 * face mass (face nodes)
     vector<int> shape_of;         // element -> shape class
     vector<int64_t> vmapP;        // [K][nfaces][Nfp]
+    // thin-layer (SGBC) sub-solvers, set by orc_set_sgbc
+    std::shared_ptr<struct Sgbc> sgbc;
 
     // ---- geometry
     void ref_to_phys(int64_t e, const double* xi, double* x) const
@@ -514,7 +518,8 @@ static void build_faces(Oracle& O, int64_t nb, const int32_t* bf, const int32_t*
     for (int64_t b = 0; b < ni; ++b) {
         int64_t fi = lookup(&ifc[b * fv]);
         if (O.faces[fi].kind != 0) throw std::runtime_error("oracle: interior sheet on boundary face");
-        O.faces[fi].kind = 3; O.faces[fi].bc = icodes[b];
+        if (icodes[b] == BC_SGBC) { O.faces[fi].kind = 4; O.faces[fi].bc = 0; O.sgbc_faces.push_back(fi); }
+        else { O.faces[fi].kind = 3; O.faces[fi].bc = icodes[b]; }
     }
     vector<char> mark(O.K, 0);
     for (int64_t b = 0; b < nt; ++b) {
@@ -690,17 +695,19 @@ static void build_global(Oracle& O)
     for (int64_t c = 0; c < static_cast<int64_t>(rep.size()); ++c) cls_mats[c] = elem_mats(O, rep[c], vq);
 
     // per element: dense local rows [R][S slots][6][Np] -> compressed rows
-    vector<vector<int32_t>> colsA(O.K), colsT(O.K);
-    vector<vector<double>> valsA(O.K), valsT(O.K);
-    vector<vector<int32_t>> cntA(O.K), cntT(O.K);
+    vector<vector<int32_t>> colsA(O.K), colsT(O.K), colsS(O.K);
+    vector<vector<double>> valsA(O.K), valsT(O.K), valsS(O.K);
+    vector<vector<int32_t>> cntA(O.K), cntT(O.K), cntS(O.K);
 #pragma omp parallel
     {
-        vector<double> LA(static_cast<size_t>(R) * S * R), LT(static_cast<size_t>(R) * S * R);
+        vector<double> LA(static_cast<size_t>(R) * S * R), LT(static_cast<size_t>(R) * S * R),
+            LS(static_cast<size_t>(R) * S * R);
         vector<double> own(Np * Np), coup(Np * Np), tmp(Np * Np);
 #pragma omp for schedule(dynamic, 8)
         for (int64_t e = 0; e < O.K; ++e) {
             std::fill(LA.begin(), LA.end(), 0.0);
             std::fill(LT.begin(), LT.end(), 0.0);
+            std::fill(LS.begin(), LS.end(), 0.0);
             const ElemMats& m = cls_mats[O.shape_of[e]];
             int64_t slot_elem[5] = {e, -1, -1, -1, -1};
             // add sign * scale * (Minv * blk | blk) at rows (field, rc), slot s cols (gfield, cc)
@@ -738,7 +745,10 @@ static void build_global(Oracle& O)
                 const int s = 1 + lf;
                 slot_elem[s] = (side == 1) ? F.e2 : F.e1;
                 if (F.kind == 1 && F.bc == BC_OPEN) continue;
-                const bool interior = (F.kind == 0 || F.kind == 2);
+                // thin-layer (SGBC) faces are left out of the interior flux (the interior ignore marker,
+                // DGOperatorFactory.h:373-389, 473-481) and get the interior-face integrators in their own
+                // source-face operator instead (buildSGBCGlobalOperator, DGOperatorFactory.h:1364-1425)
+                const bool interior = (F.kind == 0 || F.kind == 2 || F.kind == 4);
                 const bool sheet = (F.kind == 3);
                 for (int f = 0; f < 2; ++f) {
                     const int g = 1 - f;
@@ -748,7 +758,11 @@ static void build_global(Oracle& O)
                     if (interior) { beta0 = O.alpha; beta1 = 1.0; }
                     else if (F.bc == BC_SMA) { beta0 = 1.0; beta1 = 1.0; }
                     else { beta0 = bc_coeff(F.bc, f) * O.alpha; beta1 = bc_coeff(F.bc, g); }
-                    auto both = [&](auto&& fn) { fn(LA); if (F.kind == 2) fn(LT); };
+                    auto both = [&](auto&& fn) {
+                        if (F.kind == 4) { fn(LS); return; }
+                        fn(LA);
+                        if (F.kind == 2) fn(LT);
+                    };
                     if (beta0 != 0.0) {
                         face_rows(O, F, side, 0, 0, 0, beta0, sheet, own.data(), coup.data());
                         both([&](vector<double>& L) {
@@ -799,6 +813,7 @@ static void build_global(Oracle& O)
             };
             compress(LA, colsA[e], valsA[e], cntA[e]);
             compress(LT, colsT[e], valsT[e], cntT[e]);
+            compress(LS, colsS[e], valsS[e], cntS[e]);
         }
     }
     auto finalize = [&](vector<vector<int32_t>>& cols, vector<vector<double>>& vals, vector<vector<int32_t>>& cnt, CSR& M) {
@@ -821,6 +836,7 @@ static void build_global(Oracle& O)
     };
     finalize(colsA, valsA, cntA, O.Aglob);
     finalize(colsT, valsT, cntT, O.Ttfsf);
+    finalize(colsS, valsS, cntS, O.Tsgbc);
     O.have_csr = true;
 }
 
@@ -857,10 +873,23 @@ static bool tfsf_skip(const Oracle& O, double t)
     return acc < 1e-16;
 }
 
+static void sgbc_stage(Oracle& O, const double* x, double t, bool& quiescent);
+static void sgbc_inject(Oracle& O, const double* x, double* y);
+static void tfsf_apply(Oracle& O, double* y, double t);
+
 static void mult_global(Oracle& O, const double* x, double* y, double t)
 {
     if (!O.have_csr) build_global(O);
+    // GlobalEvolution::Mult order (GlobalEvolution.cpp:639-1001): sub-solves, A x, TF/SF, injection
+    bool quiescent = true;
+    if (O.sgbc) sgbc_stage(O, x, t, quiescent);
     O.Aglob.spmv(x, y, 1.0, false);
+    tfsf_apply(O, y, t);
+    if (O.sgbc && !quiescent) sgbc_inject(O, x, y);
+}
+
+static void tfsf_apply(Oracle& O, double* y, double t)
+{
     if (O.tfsf_elems.empty() || tfsf_skip(O, t)) return;
     // w = +-0.5 pw on every DOF of the TF/SF-adjacent elements; out -= T w
     vector<double> w(6 * O.N, 0.0);
@@ -883,6 +912,8 @@ static void mult_global(Oracle& O, const double* x, double* y, double t)
 static void build_nodal(Oracle& O)
 {
     const int Np = O.Np, Nfp = O.Nfp, dim = O.dim, nf = O.nfaces;
+    if (!O.sgbc_faces.empty())
+        throw std::runtime_error("oracle: thin-layer (SGBC) faces exist in the global form only (GlobalEvolution)");
     Quad vq;
     if (dim == 3) vq = tet_quad(O.p + 3);
     else { vector<double> g, gw; gauss_legendre01(O.p + 2, g, gw); vq.x = g; vq.w = gw; }
@@ -1053,6 +1084,429 @@ static void lserk_step(Oracle& O, int form, double* x, double t, double dt, vect
     }
 }
 
+
+// ---------------------------------------------------------------- thin layers (SGBC)
+// Restates the reference's SGBC coupling:
+//  - one 1D DG sub-solver per face node pair (SGBCWrapper, src/solver/SolverExtension.cpp:49-173,
+//    509-559): n_ghost = max(3, p+1) vacuum ghost segments of width (total width / total segments)
+//    on each side of the layers, SMA at both ends, the stack's optional PEC/PMC/SMA sheets at the
+//    ghost/layer interfaces, order max over layers, upwind alpha 1;
+//  - SDIRK33 steps (Solver options of the sub-solver, SolverExtension.cpp:163-170) whose implicit
+//    solves use the dense (I - h A) factorisation (GlobalEvolution::ImplicitSolve,
+//    GlobalEvolution.cpp:1118-1168), Alexander's three-stage L-stable tableau;
+//  - pairs: per face node, (node of the face's first element, matching node of the second),
+//    rotation from the first element's outward normal (GlobalEvolution.cpp:48-127,
+//    SolverExtension.h:68-107);
+//  - per step: checkpoint, per stage a sub-solve from the checkpoint to the stage time with the
+//    stage vector as ghost data and the 1e-8 quiescence skips, two-pass injection through the
+//    source-face operator, and a final advance over the whole step with ghosts interpolated
+//    linearly between the step's end points (GlobalEvolution.cpp:395-545, 639-1001;
+//    Solver::step, Solver.cpp:535-551).
+struct SgbcLayerP { double eps, mu, sigma, width; int segments, order; };
+
+struct SgbcStack {
+    vector<SgbcLayerP> layers;
+    int left_bc = 0, right_bc = 0;   // 0: transparent, else BC_PEC / BC_PMC / BC_SMA
+    double sub_dt = 0.0;
+    int p = 1, nghost = 3, Np1 = 2;
+    int64_t K1 = 0, local = 0, n = 0;   // local = K1 * Np1 nodes per component; n = 6 * local
+    vector<double> A;                    // dense n x n sub-solver operator
+    double lu_h = -1.0; vector<double> LU; vector<int> piv;
+    int64_t idx_left() const { return static_cast<int64_t>(nghost) * Np1; }
+    int64_t idx_right() const { return local - 1 - static_cast<int64_t>(nghost) * Np1; }
+};
+
+struct SgbcPair {
+    int64_t gl, gr;
+    double rot[9];
+    int stack;
+    vector<double> state, cp;
+    double ghost_old[12], ghost_new[12];
+};
+
+struct Sgbc {
+    vector<SgbcStack> stacks;
+    vector<SgbcPair> pairs;
+    vector<int64_t> elem1, elem2;   // elements of the pairs' first / second nodes (unique, ascending)
+    double base = 0.0, dt = 0.0;
+};
+
+static void sgbc_rotation(const double* nrm, double* R)
+{
+    // buildFaceRotationMatrix, 3D branch (SolverExtension.h:68-107)
+    double nx = nrm[0], ny = nrm[1], nz = nrm[2];
+    const double len = std::sqrt(nx * nx + ny * ny + nz * nz);
+    nx /= len; ny /= len; nz /= len;
+    R[0] = nx; R[1] = ny; R[2] = nz;
+    double rx = 0, ry = 0, rz = 0;
+    if (std::fabs(nx) < 0.9) rx = 1.0; else ry = 1.0;
+    double t1x = ny * rz - nz * ry, t1y = nz * rx - nx * rz, t1z = nx * ry - ny * rx;
+    const double tl = std::sqrt(t1x * t1x + t1y * t1y + t1z * t1z);
+    t1x /= tl; t1y /= tl; t1z /= tl;
+    R[3] = t1x; R[4] = t1y; R[5] = t1z;
+    R[6] = ny * t1z - nz * t1y; R[7] = nz * t1x - nx * t1z; R[8] = nx * t1y - ny * t1x;
+}
+
+// The sub-solver mesh (buildSGBCMesh, SolverExtension.cpp:49-118) and its assembled operator.
+static void sgbc_build_stack(SgbcStack& S)
+{
+    if (S.layers.empty()) throw std::runtime_error("oracle: SGBC stack without layers");
+    int64_t nseg = 0; double width = 0.0; int p = 1;
+    for (auto& L : S.layers) {
+        if (L.segments < 1 || !(L.width > 0)) throw std::runtime_error("oracle: SGBC layer needs segments >= 1, width > 0");
+        nseg += L.segments; width += L.width; p = std::max(p, L.order);
+    }
+    S.p = p; S.Np1 = p + 1; S.nghost = std::max(3, p + 1);
+    const double gdx = width / static_cast<double>(nseg);
+    vector<double> xs;
+    for (int i = 0; i <= S.nghost; ++i) xs.push_back(i * gdx);
+    double x = S.nghost * gdx;
+    for (auto& L : S.layers) {
+        const double dx = L.width / L.segments;
+        for (int i = 0; i < L.segments; ++i) { x += dx; xs.push_back(x); }
+    }
+    for (int i = 1; i <= S.nghost; ++i) xs.push_back(x + i * gdx);
+    const int64_t nv = static_cast<int64_t>(xs.size()), ne = nv - 1;
+    vector<double> verts(3 * nv, 0.0);
+    for (int64_t i = 0; i < nv; ++i) verts[3 * i] = xs[i];
+    vector<int32_t> el(2 * ne);
+    vector<double> eps(ne, 1.0), mu(ne, 1.0), sig(ne, 0.0);
+    for (int64_t i = 0; i < ne; ++i) { el[2 * i] = static_cast<int32_t>(i); el[2 * i + 1] = static_cast<int32_t>(i + 1); }
+    int64_t e = S.nghost;
+    for (auto& L : S.layers)
+        for (int i = 0; i < L.segments; ++i, ++e) { eps[e] = L.eps; mu[e] = L.mu; sig[e] = L.sigma; }
+    Oracle O;
+    O.dim = 1; O.p = p; O.alpha = 1.0; O.K = ne;
+    O.B.init(1, p);
+    O.Np = O.B.Np;
+    O.verts = verts; O.elems = el; O.eps = eps; O.mu = mu; O.sig = sig;
+    build_geometry(O);
+    local_face_nodes(O);
+    int32_t bf[2] = {0, static_cast<int32_t>(nv - 1)}, bc[2] = {BC_SMA, BC_SMA};
+    vector<int32_t> ifc, ic;
+    if (S.left_bc) { ifc.push_back(S.nghost); ic.push_back(S.left_bc); }
+    if (S.right_bc) { ifc.push_back(static_cast<int32_t>(S.nghost + nseg)); ic.push_back(S.right_bc); }
+    build_faces(O, 2, bf, bc, 0, nullptr, static_cast<int64_t>(ic.size()), ifc.data(), ic.data());
+    build_global(O);
+    S.K1 = ne; S.local = O.N; S.n = 6 * O.N;
+    if (O.Np != S.Np1) throw std::runtime_error("oracle: 1D node count");
+    S.A.assign(S.n * S.n, 0.0);
+    for (int64_t r = 0; r < S.n; ++r)
+        for (int64_t k = O.Aglob.rp[r]; k < O.Aglob.rp[r + 1]; ++k) S.A[r * S.n + O.Aglob.ci[k]] += O.Aglob.v[k];
+}
+
+// LU factorisation (partial pivoting) of I - h A, kept until h changes
+static void sgbc_factor(SgbcStack& S, double h)
+{
+    const int64_t n = S.n;
+    if (h != S.lu_h) {
+        S.LU.assign(n * n, 0.0); S.piv.resize(n);
+        for (int64_t i = 0; i < n * n; ++i) S.LU[i] = -h * S.A[i];
+        for (int64_t i = 0; i < n; ++i) S.LU[i * n + i] += 1.0;
+        for (int64_t c = 0; c < n; ++c) {
+            int64_t pr = c; double best = std::fabs(S.LU[c * n + c]);
+            for (int64_t r = c + 1; r < n; ++r) if (std::fabs(S.LU[r * n + c]) > best) { best = std::fabs(S.LU[r * n + c]); pr = r; }
+            S.piv[c] = static_cast<int>(pr);
+            if (pr != c) for (int64_t q = 0; q < n; ++q) std::swap(S.LU[c * n + q], S.LU[pr * n + q]);
+            const double d = S.LU[c * n + c];
+            for (int64_t r = c + 1; r < n; ++r) {
+                const double f = S.LU[r * n + c] / d;
+                S.LU[r * n + c] = f;
+                if (f != 0.0) for (int64_t q = c + 1; q < n; ++q) S.LU[r * n + q] -= f * S.LU[c * n + q];
+            }
+        }
+        S.lu_h = h;
+    }
+}
+
+// k = (I - h A)^-1 A x with the factorisation of sgbc_factor (read only: safe across threads)
+static void sgbc_implicit(const SgbcStack& S, const double* x, double* k)
+{
+    const int64_t n = S.n;
+    for (int64_t r = 0; r < n; ++r) {
+        double a = 0; for (int64_t q = 0; q < n; ++q) a += S.A[r * n + q] * x[q];
+        k[r] = a;
+    }
+    for (int64_t c = 0; c < n; ++c) if (S.piv[c] != c) std::swap(k[c], k[S.piv[c]]);
+    for (int64_t r = 0; r < n; ++r) { double a = k[r]; for (int64_t q = 0; q < r; ++q) a -= S.LU[r * n + q] * k[q]; k[r] = a; }
+    for (int64_t r = n - 1; r >= 0; --r) {
+        double a = k[r]; for (int64_t q = r + 1; q < n; ++q) a -= S.LU[r * n + q] * k[q];
+        k[r] = a / S.LU[r * n + r];
+    }
+}
+
+static const double kSdirkGamma = 0.43586652150845899941601945;   // root of 6x^3 - 18x^2 + 9x - 1 in (1/6, 1/2)
+
+// The step SGBCWrapper::solve takes (SolverExtension.cpp:412-445): the sub-solver's Solver::step
+// of dt from t is one SDIRK33 step of min(dt, (t + dt) - t); none below 1e-9 (returns 0).
+static double sgbc_step_size(double t, double dt)
+{
+    if (std::fabs(dt) < 1e-9) return 0.0;
+    return std::min(dt, (t + dt) - t);
+}
+
+// One SDIRK33 step of size h (> 0) with the factorisation of I - gamma h A in place.
+static void sgbc_sdirk(const SgbcStack& S, double* x, double h)
+{
+    const double g = kSdirkGamma;
+    const double a21 = 0.5 * (1.0 - g);
+    const double b1 = -(6.0 * g * g - 16.0 * g + 1.0) / 4.0;
+    const double b2 = (6.0 * g * g - 20.0 * g + 5.0) / 4.0;
+    const int64_t n = S.n;
+    vector<double> k(n), y(n);
+    sgbc_implicit(S, x, k.data());
+    for (int64_t i = 0; i < n; ++i) { y[i] = x[i] + a21 * h * k[i]; x[i] += b1 * h * k[i]; }
+    sgbc_implicit(S, y.data(), k.data());
+    for (int64_t i = 0; i < n; ++i) x[i] += b2 * h * k[i];
+    sgbc_implicit(S, x, k.data());
+    for (int64_t i = 0; i < n; ++i) x[i] += g * h * k[i];
+}
+
+static void sgbc_set_ghosts(const SgbcStack& S, double* x, const double* g);
+
+// Sub-step q of every listed pair of stack S: ghosts (per pair, from ghost(P, g)), then the
+// SDIRK33 step from t; the factorisation is made once, the pairs run in parallel.
+template <typename GhostFn>
+static void sgbc_substep(SgbcStack& S, vector<SgbcPair*>& pairs, double t, double dt, GhostFn&& ghost)
+{
+    const double h = sgbc_step_size(t, dt);
+    if (h > 0.0) sgbc_factor(S, kSdirkGamma * h);
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int64_t i = 0; i < static_cast<int64_t>(pairs.size()); ++i) {
+        SgbcPair& P = *pairs[i];
+        double g[12];
+        ghost(P, g);
+        sgbc_set_ghosts(S, P.state.data(), g);
+        if (h > 0.0) sgbc_sdirk(S, P.state.data(), h);
+    }
+}
+
+// Ghost elements take the face-local values (updateFieldsWithGlobalVector /
+// updateFieldsWithInterpolatedGhost, SolverExtension.cpp:250-371): g[0..5] left, g[6..11] right.
+static void sgbc_set_ghosts(const SgbcStack& S, double* x, const double* g)
+{
+    const int64_t tg = static_cast<int64_t>(S.nghost) * S.Np1, L = S.local;
+    for (int c = 0; c < 6; ++c)
+        for (int64_t q = 0; q < tg; ++q) { x[c * L + q] = g[c]; x[c * L + (L - 1 - q)] = g[6 + c]; }
+}
+
+static void sgbc_local(const SgbcPair& P, const double* x, int64_t N, int64_t node, double* out6)
+{
+    double eg[3], hg[3];
+    for (int d = 0; d < 3; ++d) { eg[d] = x[d * N + node]; hg[d] = x[(3 + d) * N + node]; }
+    for (int i = 0; i < 3; ++i) {
+        out6[i] = P.rot[3 * i] * eg[0] + P.rot[3 * i + 1] * eg[1] + P.rot[3 * i + 2] * eg[2];
+        out6[3 + i] = P.rot[3 * i] * hg[0] + P.rot[3 * i + 1] * hg[1] + P.rot[3 * i + 2] * hg[2];
+    }
+}
+
+static double sgbc_norm(const vector<double>& v)
+{
+    double a = 0; for (double q : v) a += q * q;
+    return std::sqrt(a);
+}
+
+static double sgbc_iface2(const SgbcPair& P, const double* x, int64_t N)
+{
+    double a = 0;
+    for (int c = 0; c < 6; ++c) { const double u = x[c * N + P.gl], w = x[c * N + P.gr]; a += u * u + w * w; }
+    return a;
+}
+
+static int sgbc_nsteps(double sub_dt, double span)
+{
+    return (sub_dt > 0.0 && sub_dt < span) ? static_cast<int>(std::ceil(span / sub_dt)) : 1;
+}
+
+static const double kSgbcThr = 1e-8;
+
+static void sgbc_stage(Oracle& O, const double* x, double t, bool& quiescent)
+{
+    Sgbc& G = *O.sgbc;
+    const double thr2 = kSgbcThr * kSgbcThr;
+    for (auto& P : G.pairs) P.state = P.cp;
+    quiescent = true;
+    for (auto& P : G.pairs)
+        if (sgbc_norm(P.state) >= kSgbcThr || sgbc_iface2(P, x, O.N) >= thr2) { quiescent = false; break; }
+    const double span = t - G.base;
+    if (quiescent || !(span > 1e-12)) return;
+    for (size_t s = 0; s < G.stacks.size(); ++s) {
+        SgbcStack& S = G.stacks[s];
+        const int ns = sgbc_nsteps(S.sub_dt, span);
+        const double h = span / ns;
+        vector<SgbcPair*> list;
+        for (auto& P : G.pairs) {
+            if (P.stack != static_cast<int>(s)) continue;
+            if (sgbc_norm(P.state) < kSgbcThr && sgbc_iface2(P, x, O.N) < thr2) continue;
+            list.push_back(&P);
+        }
+        const int64_t N = O.N;
+        for (int q = 0; q < ns; ++q)
+            sgbc_substep(S, list, G.base + q * h, h, [&](const SgbcPair& P, double* g) {
+                sgbc_local(P, x, N, P.gl, g);
+                sgbc_local(P, x, N, P.gr, g + 6);
+            });
+    }
+}
+
+// Slot values of the injection (fillBCSlot, GlobalEvolution.cpp:839-871)
+static void sgbc_slot(const SgbcPair& P, const SgbcStack& S, int bc, const double* x, int64_t N, int64_t src,
+                      int64_t idx, double* out6)
+{
+    if (bc == BC_PEC || bc == BC_PMC || bc == BC_SMA) {
+        const double se = (bc == BC_PEC) ? -1.0 : 1.0, sh = (bc == BC_PMC) ? -1.0 : 1.0;
+        for (int d = 0; d < 3; ++d) { out6[d] = se * x[d * N + src]; out6[3 + d] = sh * x[(3 + d) * N + src]; }
+        return;
+    }
+    double el[3], hl[3];
+    for (int d = 0; d < 3; ++d) { el[d] = P.state[d * S.local + idx]; hl[d] = P.state[(3 + d) * S.local + idx]; }
+    for (int d = 0; d < 3; ++d) {
+        out6[d] = P.rot[d] * el[0] + P.rot[3 + d] * el[1] + P.rot[6 + d] * el[2];
+        out6[3 + d] = P.rot[d] * hl[0] + P.rot[3 + d] * hl[1] + P.rot[6 + d] * hl[2];
+    }
+}
+
+static void sgbc_rows(const Oracle& O, const vector<int64_t>& elems, const vector<double>& sv, double* y)
+{
+    for (int c = 0; c < 6; ++c)
+        for (int64_t e : elems)
+            for (int i = 0; i < O.Np; ++i) {
+                const int64_t r = c * O.N + e * O.Np + i;
+                double a = 0;
+                for (int64_t k = O.Tsgbc.rp[r]; k < O.Tsgbc.rp[r + 1]; ++k) a += O.Tsgbc.v[k] * sv[O.Tsgbc.ci[k]];
+                y[r] += a;
+            }
+}
+
+// Two-pass injection (GlobalEvolution.cpp:822-986): rows of the first elements with
+// (u at the first node, slab left value) and rows of the second elements with
+// (slab right value, u at the second node).
+static void sgbc_inject(Oracle& O, const double* x, double* y)
+{
+    Sgbc& G = *O.sgbc;
+    const int64_t N = O.N;
+    vector<double> sv(6 * N, 0.0);
+    double v[6];
+    for (auto& P : G.pairs) {
+        const SgbcStack& S = G.stacks[P.stack];
+        for (int c = 0; c < 6; ++c) sv[c * N + P.gl] = x[c * N + P.gl];
+        sgbc_slot(P, S, S.left_bc, x, N, P.gl, S.idx_left(), v);
+        for (int c = 0; c < 6; ++c) sv[c * N + P.gr] = v[c];
+    }
+    sgbc_rows(O, G.elem1, sv, y);
+    std::fill(sv.begin(), sv.end(), 0.0);
+    for (auto& P : G.pairs) {
+        const SgbcStack& S = G.stacks[P.stack];
+        sgbc_slot(P, S, S.right_bc, x, N, P.gr, S.idx_right(), v);
+        for (int c = 0; c < 6; ++c) sv[c * N + P.gl] = v[c];
+        for (int c = 0; c < 6; ++c) sv[c * N + P.gr] = x[c * N + P.gr];
+    }
+    sgbc_rows(O, G.elem2, sv, y);
+}
+
+static void sgbc_commit(Oracle& O, double t, double dt, const double* x)
+{
+    Sgbc& G = *O.sgbc;
+    G.base = t; G.dt = dt;
+    for (auto& P : G.pairs) {
+        P.cp = P.state;
+        sgbc_local(P, x, O.N, P.gl, P.ghost_old);
+        sgbc_local(P, x, O.N, P.gr, P.ghost_old + 6);
+    }
+}
+
+static void sgbc_finalize(Oracle& O, const double* x)
+{
+    Sgbc& G = *O.sgbc;
+    const double thr2 = kSgbcThr * kSgbcThr;
+    bool quiescent = true;
+    for (auto& P : G.pairs) {
+        P.state = P.cp;
+        sgbc_local(P, x, O.N, P.gl, P.ghost_new);
+        sgbc_local(P, x, O.N, P.gr, P.ghost_new + 6);
+    }
+    for (auto& P : G.pairs)
+        if (sgbc_norm(P.state) >= kSgbcThr || sgbc_iface2(P, x, O.N) >= thr2) { quiescent = false; break; }
+    if (quiescent) return;
+    for (size_t s = 0; s < G.stacks.size(); ++s) {
+        SgbcStack& S = G.stacks[s];
+        const int ns = sgbc_nsteps(S.sub_dt, G.dt);
+        const double h = G.dt / ns;
+        vector<SgbcPair*> list;
+        for (auto& P : G.pairs)
+            if (P.stack == static_cast<int>(s)) list.push_back(&P);
+        for (int q = 0; q < ns; ++q) {
+            const double a = static_cast<double>(q + 1) / ns, b = 1.0 - a;
+            sgbc_substep(S, list, G.base + q * h, h, [&](const SgbcPair& P, double* g) {
+                for (int c = 0; c < 12; ++c) g[c] = b * P.ghost_old[c] + a * P.ghost_new[c];
+            });
+        }
+    }
+}
+
+// Pairs of the kind-4 faces: (node of e1, node of e2 at the same position), stack per face.
+static void sgbc_setup(Oracle& O, vector<SgbcStack> stacks, const int32_t* face_stack)
+{
+    if (O.dim != 3) throw std::runtime_error("oracle: SGBC coupling is 3D");
+    auto G = std::make_shared<Sgbc>();
+    G->stacks = std::move(stacks);
+    for (auto& S : G->stacks) sgbc_build_stack(S);
+    vector<char> m1(O.K, 0), m2(O.K, 0);
+    for (size_t q = 0; q < O.sgbc_faces.size(); ++q) {
+        const Face& F = O.faces[O.sgbc_faces[q]];
+        const int st = face_stack[q];
+        if (st < 0 || st >= static_cast<int>(G->stacks.size())) throw std::runtime_error("oracle: SGBC stack index");
+        double R[9]; sgbc_rotation(F.n, R);
+        for (int a = 0; a < O.Nfp; ++a) {
+            const int n1 = O.fnodes[F.f1 * O.Nfp + a];
+            const int64_t g1 = F.e1 * O.Np + n1;
+            int64_t g2 = -1; double best = 1e300;
+            for (int b = 0; b < O.Nfp; ++b) {
+                const int64_t c2 = F.e2 * O.Np + O.fnodes[F.f2 * O.Nfp + b];
+                double d = 0; for (int r = 0; r < 3; ++r) { const double u = O.X[r * O.N + g1] - O.X[r * O.N + c2]; d += u * u; }
+                if (d < best) { best = d; g2 = c2; }
+            }
+            SgbcPair P;
+            P.gl = g1; P.gr = g2; std::memcpy(P.rot, R, sizeof R); P.stack = st;
+            P.state.assign(G->stacks[st].n, 0.0); P.cp = P.state;
+            std::fill(P.ghost_old, P.ghost_old + 12, 0.0); std::fill(P.ghost_new, P.ghost_new + 12, 0.0);
+            G->pairs.push_back(std::move(P));
+        }
+        m1[F.e1] = 1; m2[F.e2] = 1;
+    }
+    for (int64_t e = 0; e < O.K; ++e) { if (m1[e]) G->elem1.push_back(e); if (m2[e]) G->elem2.push_back(e); }
+    O.sgbc = G;
+}
+
+static vector<SgbcStack> sgbc_stacks_from(int n_stacks, const int32_t* layer_counts, const double* layer_prm,
+                                          const int32_t* bcs, const double* sub_dts)
+{
+    vector<SgbcStack> out(n_stacks);
+    int64_t li = 0;
+    for (int s = 0; s < n_stacks; ++s) {
+        for (int q = 0; q < layer_counts[s]; ++q, ++li) {
+            const double* L = layer_prm + 6 * li;
+            out[s].layers.push_back({L[0], L[1], L[2], L[3], static_cast<int>(L[4]), static_cast<int>(L[5])});
+        }
+        out[s].left_bc = bcs[2 * s]; out[s].right_bc = bcs[2 * s + 1];
+        out[s].sub_dt = sub_dts[s];
+    }
+    return out;
+}
+
+// One RK step with the SGBC checkpoint and finalisation around it (Solver::step)
+static void step_any(Oracle& O, int form, double* x, double t, double dt, int integrator, vector<double>& k,
+                     vector<double>& y, vector<double>& z)
+{
+    if (O.sgbc) {
+        if (form != 0) throw std::runtime_error("oracle: thin-layer (SGBC) faces exist in the global form only");
+        sgbc_commit(O, t, dt, x);
+    }
+    if (integrator == 0) rk4_step(O, form, x, t, dt, k, y, z);
+    else lserk_step(O, form, x, t, dt, k, z);
+    if (O.sgbc) sgbc_finalize(O, x);
+}
+
 }  // namespace orc
 
 // ================================================================ C API
@@ -1129,8 +1583,7 @@ int orc_step(void* h, int form, double* x, double t0, double dt, int nsteps, int
         std::vector<double> k(L), y(L), z(L, 0.0);
         double t = t0;
         for (int s = 0; s < nsteps; ++s) {
-            if (integrator == 0) orc::rk4_step(O, form, x, t, dt, k, y, z);
-            else orc::lserk_step(O, form, x, t, dt, k, z);
+            orc::step_any(O, form, x, t, dt, integrator, k, y, z);
             t += dt;
         }
     } catch (const std::exception& e) { g_orc_err = e.what(); return -1; }
@@ -1147,8 +1600,7 @@ int orc_run(void* h, int form, double* x, double t0, double dt, double T, int in
         double t = t0; int64_t n = 0;
         while (t <= T - 1e-8 * dt) {
             double h2 = std::min(dt, T - t);
-            if (integrator == 0) orc::rk4_step(O, form, x, t, h2, k, y, z);
-            else orc::lserk_step(O, form, x, t, h2, k, z);
+            orc::step_any(O, form, x, t, h2, integrator, k, y, z);
             t += h2; ++n;
         }
         if (steps) *steps = n;
@@ -1292,6 +1744,73 @@ int orc_threads(void)
 #else
     return 1;
 #endif
+}
+
+// Thin-layer (SGBC) stacks: layer_prm [total layers][6] = eps_r, mu_r, sigma (solver units), width,
+// segments, order; layer_counts [n_stacks]; bcs [n_stacks][2] left/right (0 none, 1 PEC, 2 PMC,
+// 3 SMA); sub_dts [n_stacks]; face_stack [SGBC interior faces, in the order given] stack index.
+int orc_set_sgbc(void* h, int n_stacks, const int32_t* layer_counts, const double* layer_prm, const int32_t* bcs,
+                 const double* sub_dts, const int32_t* face_stack)
+{
+    try {
+        auto& O = *static_cast<orc::Oracle*>(h);
+        orc::sgbc_setup(O, orc::sgbc_stacks_from(n_stacks, layer_counts, layer_prm, bcs, sub_dts), face_stack);
+    } catch (const std::exception& e) { g_orc_err = e.what(); return -1; }
+    return 0;
+}
+
+int64_t orc_sgbc_pairs(void* h)
+{
+    auto& O = *static_cast<orc::Oracle*>(h);
+    return O.sgbc ? static_cast<int64_t>(O.sgbc->pairs.size()) : 0;
+}
+
+// One stack on its own, for tests of the sub-solver: its size n, its dense operator, and the
+// advance of a state x by span from t0 (ghosts g_old[12] held, or interpolated to g_new[12]).
+void* orc_sgbc_stack_create(int n_layers, const double* layer_prm, int left_bc, int right_bc, double sub_dt)
+{
+    try {
+        int32_t cnt = n_layers, bc[2] = {left_bc, right_bc};
+        auto v = orc::sgbc_stacks_from(1, &cnt, layer_prm, bc, &sub_dt);
+        auto S = std::make_unique<orc::SgbcStack>(std::move(v[0]));
+        orc::sgbc_build_stack(*S);
+        return S.release();
+    } catch (const std::exception& e) { g_orc_err = e.what(); return nullptr; }
+}
+void orc_sgbc_stack_destroy(void* s) { delete static_cast<orc::SgbcStack*>(s); }
+int64_t orc_sgbc_stack_size(void* s) { return static_cast<orc::SgbcStack*>(s)->n; }
+void orc_sgbc_stack_matrix(void* s, double* A)
+{
+    auto& S = *static_cast<orc::SgbcStack*>(s);
+    std::memcpy(A, S.A.data(), S.A.size() * sizeof(double));
+}
+void orc_sgbc_stack_advance(void* s, double* x, const double* g_old, const double* g_new, double t0, double span,
+                            int interpolate)
+{
+    auto& S = *static_cast<orc::SgbcStack*>(s);
+    if (!(span > 1e-12)) return;
+    const int ns = orc::sgbc_nsteps(S.sub_dt, span);
+    const double hh = span / ns;
+    for (int q = 0; q < ns; ++q) {
+        double g[12];
+        if (interpolate) {
+            const double a = static_cast<double>(q + 1) / ns, b = 1.0 - a;
+            for (int c = 0; c < 12; ++c) g[c] = b * g_old[c] + a * g_new[c];
+        } else {
+            for (int c = 0; c < 12; ++c) g[c] = g_old[c];
+        }
+        orc::sgbc_set_ghosts(S, x, g);
+        const double h = orc::sgbc_step_size(t0 + q * hh, hh);
+        if (h > 0.0) {
+            orc::sgbc_factor(S, orc::kSdirkGamma * h);
+            orc::sgbc_sdirk(S, x, h);
+        }
+    }
+}
+int64_t orc_sgbc_stack_iface(void* s, int right)
+{
+    auto& S = *static_cast<orc::SgbcStack*>(s);
+    return right ? S.idx_right() : S.idx_left();
 }
 
 }  // extern "C"

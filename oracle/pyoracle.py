@@ -61,6 +61,16 @@ def lib() -> C.CDLL:
         h.orc_threads.restype = C.c_int
         h.orc_subop.restype = C.c_int
         h.orc_subop.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, _D]
+        h.orc_set_sgbc.restype = C.c_int
+        h.orc_set_sgbc.argtypes = [C.c_void_p, C.c_int, _I32, _D, _I32, _D, _I32]
+        h.orc_sgbc_pairs.restype = C.c_int64; h.orc_sgbc_pairs.argtypes = [C.c_void_p]
+        h.orc_sgbc_stack_create.restype = C.c_void_p
+        h.orc_sgbc_stack_create.argtypes = [C.c_int, _D, C.c_int, C.c_int, C.c_double]
+        h.orc_sgbc_stack_destroy.argtypes = [C.c_void_p]
+        h.orc_sgbc_stack_size.restype = C.c_int64; h.orc_sgbc_stack_size.argtypes = [C.c_void_p]
+        h.orc_sgbc_stack_matrix.argtypes = [C.c_void_p, _D]
+        h.orc_sgbc_stack_advance.argtypes = [C.c_void_p, _D, _D, _D, C.c_double, C.c_double, C.c_int]
+        h.orc_sgbc_stack_iface.restype = C.c_int64; h.orc_sgbc_stack_iface.argtypes = [C.c_void_p, C.c_int]
         _lib = h
     return _lib
 
@@ -162,12 +172,71 @@ class Oracle:
     def nnz(self) -> int:
         return int(lib().orc_nnz(self.h))
 
+    def set_sgbc(self, stacks: Sequence[dict], face_stack) -> None:
+        """Thin-layer (SGBC) sub-solvers for the interior faces given with code 4, in their order:
+        face_stack[i] is the stack of the i-th such face (stack dicts: see sgbc_stack_arrays)."""
+        counts, prm, bcs, subs = sgbc_stack_arrays(stacks)
+        fs = np.ascontiguousarray(face_stack, dtype=np.int32)
+        self._keep += [counts, prm, bcs, subs, fs]
+        self._chk(lib().orc_set_sgbc(self.h, len(stacks), _i(counts), _d(prm), _i(bcs), _d(subs), _i(fs)))
+
+    def sgbc_pairs(self) -> int:
+        return int(lib().orc_sgbc_pairs(self.h))
+
     def subop(self, kind: int, d: int = 0, d2: int = 0, beta_int: float = 1.0, beta_bdr: float = 1.0,
               minv_coef: float = 1.0) -> np.ndarray:
         """Dense (M^-1/minv_coef) F for one integrator (see orc_subop)."""
         out = np.zeros((self.ndofs, self.ndofs))
         self._chk(lib().orc_subop(self.h, kind, d, d2, beta_int, beta_bdr, minv_coef, _d(out)))
         return out
+
+
+def sgbc_stack_arrays(stacks: Sequence[dict]):
+    """Flat arrays of SGBC stacks. A stack is {"layers": [{"eps", "mu", "sigma", "width", "segments",
+    "order"}], "left": bc, "right": bc, "sub_dt": s}; sigma in solver units, bc 0 (none), 1 PEC,
+    2 PMC, 3 SMA."""
+    counts = np.array([len(s["layers"]) for s in stacks], dtype=np.int32)
+    prm = np.array([[L.get("eps", 1.0), L.get("mu", 1.0), L.get("sigma", 0.0), L["width"], L["segments"], L["order"]]
+                    for s in stacks for L in s["layers"]], dtype=np.float64).reshape(-1, 6)
+    bcs = np.array([[s.get("left", 0), s.get("right", 0)] for s in stacks], dtype=np.int32).reshape(-1, 2)
+    subs = np.array([s.get("sub_dt", 0.0) for s in stacks], dtype=np.float64)
+    return counts, prm, bcs, subs
+
+
+class SgbcStack:
+    """One SGBC sub-solver on its own (tests of the 1D operator and of the sub-stepping)."""
+
+    def __init__(self, stack: dict):
+        counts, prm, bcs, subs = sgbc_stack_arrays([stack])
+        self._keep = (prm,)
+        self.h = lib().orc_sgbc_stack_create(int(counts[0]), _d(prm), int(bcs[0, 0]), int(bcs[0, 1]), float(subs[0]))
+        if not self.h:
+            raise RuntimeError("oracle: " + lib().orc_last_error().decode())
+        self.n = int(lib().orc_sgbc_stack_size(self.h))
+        self.idx_left = int(lib().orc_sgbc_stack_iface(self.h, 0))
+        self.idx_right = int(lib().orc_sgbc_stack_iface(self.h, 1))
+
+    def __del__(self):
+        try:
+            if self.h:
+                lib().orc_sgbc_stack_destroy(self.h)
+                self.h = None
+        except Exception:
+            pass
+
+    def matrix(self) -> np.ndarray:
+        A = np.zeros((self.n, self.n))
+        lib().orc_sgbc_stack_matrix(self.h, _d(A))
+        return A
+
+    def advance(self, x, g_old, g_new=None, t0: float = 0.0, span: float = 0.0) -> np.ndarray:
+        """x advanced by span from t0: ghosts g_old (12 face-local values) held, or interpolated
+        towards g_new when it is given."""
+        x = np.array(x, dtype=np.float64, copy=True)
+        go = np.ascontiguousarray(g_old, dtype=np.float64)
+        gn = np.ascontiguousarray(go if g_new is None else g_new, dtype=np.float64)
+        lib().orc_sgbc_stack_advance(self.h, _d(x), _d(go), _d(gn), float(t0), float(span), int(g_new is not None))
+        return x
 
 
 def element_matrices(dim: int, order: int, verts) -> dict:

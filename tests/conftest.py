@@ -54,3 +54,29 @@ def read_point_probe(path):
     rows = np.loadtxt(path, skiprows=4, ndmin=2)
     rows[:, 0] *= SPEED_OF_LIGHT_SI
     return rows
+
+
+def plane_faces(vertices, elements, x0, tol=1e-12):
+    """Interior faces (vertex triples) of a tetrahedral mesh lying on the plane x = x0."""
+    import numpy as np
+    from collections import Counter
+    V = np.asarray(vertices)
+    cnt = Counter()
+    for t in np.asarray(elements):
+        for f in range(4):
+            fv = tuple(sorted(int(v) for v in np.delete(t, f)))
+            if all(abs(V[v, 0] - x0) < tol for v in fv):
+                cnt[fv] += 1
+    return np.array([list(k) for k, c in sorted(cnt.items()) if c == 2], dtype=np.int32).reshape(-1, 3)
+
+
+def sgbc_box(n=(4, 3, 3), hi=(2.0, 1.0, 1.0), planes=(1.0,), tfsf=True):
+    """A box with SMA walls, a TF/SF box from the second cell on, and thin-layer (SGBC) sheets on
+    the planes x = planes[i] (interior faces with code 4). Returns (mesh tables as the oracle's
+    BoxMesh fields, the sheet faces per plane)."""
+    import numpy as np
+    from oracle import pyoracle as po
+    m = po.box_mesh(n, hi=hi, outer_bc=po.BC_SMA, tfsf=((1, 0, 0), tuple(n)) if tfsf else None)
+    sheets = [plane_faces(m.vertices, m.elements, x) for x in planes]
+    faces = np.concatenate(sheets) if sheets else np.zeros((0, 3), np.int32)
+    return m, sheets, faces

@@ -14,7 +14,7 @@ import sys
 from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
-CASES = ("3D_PEC", "3D_TFSF", "3D_TFSF_InteriorPEC", "3D_Curved_Element_Test")
+CASES = ("3D_PEC", "3D_TFSF", "3D_TFSF_InteriorPEC", "3D_Curved_Element_Test", "3D_SGBC")
 
 
 def main() -> None:

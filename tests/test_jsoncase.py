@@ -114,8 +114,13 @@ def test_rejects_unsupported_and_malformed(tmp_path):
         for b in c["model"]["boundaries"]:
             if b["type"] == "PMC":
                 b["type"] = "SGBC"
-    with pytest.raises(dg.DgtdError, match="not supported"):
+    with pytest.raises(dg.DgtdError, match="must define either 'material' or 'layers'"):
         dg.Case(_case_copy(tmp_path, "box_resonant", "sgbc", sgbc))
+
+    def unknown(c):
+        c["model"]["boundaries"][0]["type"] = "SIBC"
+    with pytest.raises(dg.DgtdError, match="not supported"):
+        dg.Case(_case_copy(tmp_path, "box_resonant", "unknown_bc", unknown))
 
     # a plane wave's Gaussian mean is a position (the reference fails on a plain number too)
     def scalar_mean(c):

@@ -177,6 +177,8 @@ SIGNATURES = {
     "dgtd_op_set_probes": (C.c_int, [_P, C.POINTER(ProbeSpec)]),
     "dgtd_op_set_sgbc": (C.c_int, [_P, C.POINTER(SgbcStack), C.c_int32, _I32]),
     "dgtd_op_sgbc_states": (C.c_int, [_P, _I64, _I64, _D, C.c_int64]),
+    "dgtd_op_sgbc_commit": (C.c_int, [_P, _P, C.c_double, C.c_double, _P]),
+    "dgtd_op_sgbc_finalize": (C.c_int, [_P, _P, _P]),
     "dgtd_sgbc_stack_operator": (C.c_int, [C.POINTER(SgbcStack), _I64, _I64, _I64, _D, C.c_int64]),
     "dgtd_sgbc_stack_maps": (C.c_int, [C.POINTER(SgbcStack), C.c_double, C.c_int32, _D, _D, _D, _D, _D]),
     "dgtd_op_clear_probes": (C.c_int, [_P]),
@@ -500,6 +502,14 @@ class Operator:
         arr, keep = _sgbc_structs(stacks)
         fs = np.ascontiguousarray(face_stack, dtype=np.int32)
         _check(lib().dgtd_op_set_sgbc(self._h, arr, len(stacks), _ip(fs)), "dgtd_op_set_sgbc")
+
+    def sgbc_commit(self, x, t: float, dt: float, stream=None) -> None:
+        """Start of a step driven through mult (the reference's commitSGBCCheckpoint)."""
+        _check(lib().dgtd_op_sgbc_commit(self._h, _ptr(x), float(t), float(dt), _stream(stream)), "dgtd_op_sgbc_commit")
+
+    def sgbc_finalize(self, x, stream=None) -> None:
+        """End of a step driven through mult, x the step's end state (finalizeSGBCStep)."""
+        _check(lib().dgtd_op_sgbc_finalize(self._h, _ptr(x), _stream(stream)), "dgtd_op_sgbc_finalize")
 
     def sgbc_states(self) -> np.ndarray:
         """The sub-solver states, pair after pair (empty without SGBC)."""

@@ -1268,6 +1268,36 @@ int dgtd_op_set_sgbc(dgtd_op* op, const dgtd_sgbc_stack* stacks, int32_t n_stack
     return DGTD_OK;
 }
 
+int dgtd_op_sgbc_commit(dgtd_op* op, const void* d_x, double t, double dt, void* stream)
+{
+    if (!op || !d_x) return fail(DGTD_ERR_INVALID, "NULL argument");
+    if (!op->sgbc) return fail(DGTD_ERR_INVALID, "no thin-layer (SGBC) stacks are set");
+    try {
+        const int64_t before = op->sgbc->launches();
+        op->sgbc->commit(op->dev, static_cast<const double*>(d_x), t, dt, static_cast<cudaStream_t>(stream));
+        g_launches.fetch_add(op->sgbc->launches() - before, std::memory_order_relaxed);
+    } catch (const std::exception& e) {
+        return fail(DGTD_ERR_CUDA, e.what());
+    }
+    return DGTD_OK;
+}
+
+int dgtd_op_sgbc_finalize(dgtd_op* op, const void* d_x, void* stream)
+{
+    if (!op || !d_x) return fail(DGTD_ERR_INVALID, "NULL argument");
+    if (!op->sgbc) return fail(DGTD_ERR_INVALID, "no thin-layer (SGBC) stacks are set");
+    try {
+        const int64_t before = op->sgbc->launches();
+        op->sgbc->finalize(op->dev, static_cast<const double*>(d_x), static_cast<cudaStream_t>(stream));
+        g_launches.fetch_add(op->sgbc->launches() - before, std::memory_order_relaxed);
+    } catch (const std::invalid_argument& e) {
+        return fail(DGTD_ERR_UNSUPPORTED, e.what());
+    } catch (const std::exception& e) {
+        return fail(DGTD_ERR_CUDA, e.what());
+    }
+    return DGTD_OK;
+}
+
 int dgtd_op_sgbc_states(const dgtd_op* op, int64_t* n_pairs, int64_t* state_len, double* h_states, int64_t cap)
 {
     if (!op) return fail(DGTD_ERR_INVALID, "NULL argument");

@@ -384,6 +384,8 @@ SgbcLayout build_sgbc_layout(const MeshTables& T, const RefTet& ref, const std::
         }
     }
     Lo.el_start.push_back(static_cast<int32_t>(ents.size()));
+    for (size_t i = 0; i + 1 < Lo.el_start.size(); ++i)
+        if (Lo.el_start[i + 1] - Lo.el_start[i] > 4) throw std::runtime_error("SGBC: more than four SGBC faces on an element");
     return Lo;
 }
 

@@ -19,6 +19,8 @@
 #include "sgbc_dev.hpp"
 
 #include <algorithm>
+#include <cmath>
+#include <limits>
 #include <stdexcept>
 #include <string>
 
@@ -46,8 +48,10 @@ struct PairArgs {
     const int32_t* pstack;
     const double* rot;
     const int64_t* xoff;
-    double* X;
-    double* snorm;
+    const double* X;       // checkpoint states
+    const double* snorm;   // their norms
+    double* Xout;          // finalisation: the new states
+    double* snorm_out;     // and their norms
     double* gold;
     double* gnew;
     double* trace;
@@ -247,17 +251,24 @@ __global__ void __launch_bounds__(256) sgbc_quiesce_kernel(PairArgs A, const dou
     if (A.snorm[p] >= kQuiet || if2 >= kQuiet * kQuiet) atomicOr(A.flag, 1);
 }
 
-// one block per pair: x = F x_cp + Vo g_old + Vn g_new, and |x|
+// one block per pair: x = F x_cp + Vo g_old + Vn g_new, and |x|; every pair quiescent: the
+// states stay at the checkpoint (copied)
 __global__ void __launch_bounds__(256) sgbc_final_kernel(PairArgs A, int64_t n_max)
 {
-    if (*A.flag == 0) return;   // every pair quiescent: the states stay at the checkpoint
+    const bool advance = *A.flag != 0;
     extern __shared__ double sx[];   // [n_max] state, then [24] ghosts
     __shared__ double red[256];
     double* gg = sx + n_max;
     for (int64_t p = blockIdx.x; p < A.n_pairs; p += gridDim.x) {
         const StackInfo& S = A.st[A.pstack[p]];
         const int64_t n = S.n;
-        double* x = A.X + A.xoff[p];
+        const double* x = A.X + A.xoff[p];
+        double* xo = A.Xout + A.xoff[p];
+        if (!advance) {
+            for (int64_t j = threadIdx.x; j < n; j += blockDim.x) xo[j] = x[j];
+            if (threadIdx.x == 0) A.snorm_out[p] = A.snorm[p];
+            continue;
+        }
         for (int64_t j = threadIdx.x; j < n; j += blockDim.x) sx[j] = x[j];
         if (threadIdx.x < 24)
             gg[threadIdx.x] = (threadIdx.x < 12) ? A.gold[p * 12 + threadIdx.x] : A.gnew[p * 12 + threadIdx.x - 12];
@@ -271,7 +282,7 @@ __global__ void __launch_bounds__(256) sgbc_final_kernel(PairArgs A, int64_t n_m
                 acc = fma(S.Vo[i * 12 + c], gg[c], acc);
                 acc = fma(S.Vn[i * 12 + c], gg[12 + c], acc);
             }
-            x[i] = acc;
+            xo[i] = acc;
             ss += acc * acc;
         }
         red[threadIdx.x] = ss;
@@ -280,7 +291,7 @@ __global__ void __launch_bounds__(256) sgbc_final_kernel(PairArgs A, int64_t n_m
             if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
             __syncthreads();
         }
-        if (threadIdx.x == 0) A.snorm[p] = sqrt(red[0]);
+        if (threadIdx.x == 0) A.snorm_out[p] = sqrt(red[0]);
         __syncthreads();
     }
 }
@@ -336,8 +347,11 @@ SgbcOp::SgbcOp(const MeshTables& T, const RefTet& ref, const std::vector<SgbcSta
     try {
         gl_ = upload(layout_.gl); gr_ = upload(layout_.gr); pstack_ = upload(layout_.stack);
         rot_ = upload(layout_.rot); xoff_ = upload(xoff);
-        X_ = zeros<double>(static_cast<size_t>(state_len_));
-        snorm_ = zeros<double>(np); gold_ = zeros<double>(12 * np); gnew_ = zeros<double>(12 * np);
+        for (int b = 0; b < 2; ++b) {
+            X_[b] = zeros<double>(static_cast<size_t>(state_len_));
+            snorm_[b] = zeros<double>(np);
+        }
+        gold_ = zeros<double>(12 * np); gnew_ = zeros<double>(12 * np);
         trace_ = zeros<double>(12 * np); flags_ = zeros<int>(8);
         el_elem_ = upload(layout_.el_elem); el_start_ = upload(layout_.el_start);
         ent_face_ = upload(layout_.ent_face); ent_role_ = upload(layout_.ent_role); ent_pairs_ = upload(layout_.ent_pairs);
@@ -353,11 +367,24 @@ void SgbcOp::release()
 {
     for (auto& kv : maps_) cudaFree(kv.second.a);
     maps_.clear();
-    void* bufs[] = {gl_, gr_, pstack_, rot_, xoff_, X_, snorm_, gold_, gnew_, trace_, flags_,
+    void* bufs[] = {gl_, gr_, pstack_, rot_, xoff_, X_[0], X_[1], snorm_[0], snorm_[1], gold_, gnew_, trace_, flags_,
                     el_elem_, el_start_, ent_face_, ent_role_, ent_pairs_};
     for (void* b : bufs) if (b) cudaFree(b);
-    gl_ = gr_ = pstack_ = nullptr; rot_ = nullptr; xoff_ = nullptr; X_ = snorm_ = gold_ = gnew_ = trace_ = nullptr;
+    gl_ = gr_ = pstack_ = nullptr; rot_ = nullptr; xoff_ = nullptr;
+    X_[0] = X_[1] = snorm_[0] = snorm_[1] = gold_ = gnew_ = trace_ = nullptr;
     flags_ = nullptr; el_elem_ = el_start_ = ent_face_ = ent_role_ = ent_pairs_ = nullptr;
+}
+
+// Called before the maps of one launch are looked up (never between two look-ups of a launch, whose
+// pointers go into the same kernel arguments): a Mult at many different times would grow the
+// cache without bound, so it starts again once it holds 64 maps (after the device has finished
+// with them).
+void SgbcOp::trim_maps()
+{
+    if (maps_.size() + 2 * stacks_.size() <= 64) return;
+    ckd(cudaDeviceSynchronize(), "SGBC map cache");
+    for (auto& kv : maps_) cudaFree(kv.second.a);
+    maps_.clear();
 }
 
 const SgbcOp::DevMap& SgbcOp::stage_map(int st, double span, int nsteps)
@@ -365,11 +392,6 @@ const SgbcOp::DevMap& SgbcOp::stage_map(int st, double span, int nsteps)
     auto key = std::make_tuple(0, st, span, nsteps);
     auto it = maps_.find(key);
     if (it != maps_.end()) return it->second;
-    if (maps_.size() >= 64) {   // a Mult at many different times: start the cache again
-        ckd(cudaDeviceSynchronize(), "SGBC map cache");
-        for (auto& kv : maps_) cudaFree(kv.second.a);
-        maps_.clear();
-    }
     const SgbcStack1D& S = stacks_[st];
     SgbcStageMap M = sgbc_stage_map(S, span, nsteps);
     std::vector<double> buf(M.R);
@@ -385,11 +407,6 @@ const SgbcOp::DevMap& SgbcOp::final_map(int st, double span, int nsteps)
     auto key = std::make_tuple(1, st, span, nsteps);
     auto it = maps_.find(key);
     if (it != maps_.end()) return it->second;
-    if (maps_.size() >= 64) {
-        ckd(cudaDeviceSynchronize(), "SGBC map cache");
-        for (auto& kv : maps_) cudaFree(kv.second.a);
-        maps_.clear();
-    }
     const SgbcStack1D& S = stacks_[st];
     SgbcFinalMap M = sgbc_final_map(S, span, nsteps);
     std::vector<double> buf(M.FT);
@@ -403,13 +420,14 @@ const SgbcOp::DevMap& SgbcOp::final_map(int st, double span, int nsteps)
 
 namespace {
 
-PairArgs pair_args(int64_t np, int64_t N, int32_t* gl, int32_t* gr, int32_t* ps, double* rot, int64_t* xoff, double* X,
-                   double* snorm, double* gold, double* gnew, double* trace, int* flag,
-                   const std::vector<SgbcStack1D>& stacks)
+PairArgs pair_args(int64_t np, int64_t N, int32_t* gl, int32_t* gr, int32_t* ps, double* rot, int64_t* xoff,
+                   const double* X, const double* snorm, double* Xout, double* snorm_out, double* gold, double* gnew,
+                   double* trace, int* flag, const std::vector<SgbcStack1D>& stacks)
 {
     PairArgs A{};
     A.n_pairs = np; A.N = N; A.gl = gl; A.gr = gr; A.pstack = ps; A.rot = rot; A.xoff = xoff; A.X = X;
-    A.snorm = snorm; A.gold = gold; A.gnew = gnew; A.trace = trace; A.flag = flag;
+    A.snorm = snorm; A.Xout = Xout; A.snorm_out = snorm_out;
+    A.gold = gold; A.gnew = gnew; A.trace = trace; A.flag = flag;
     A.n_stacks = static_cast<int>(stacks.size());
     for (size_t s = 0; s < stacks.size(); ++s) {
         StackInfo& I = A.st[s];
@@ -421,24 +439,53 @@ PairArgs pair_args(int64_t np, int64_t N, int32_t* gl, int32_t* gr, int32_t* ps,
 
 }  // namespace
 
+void SgbcOp::commit(const TablesDev& T, const double* x, double t, double dt, cudaStream_t s)
+{
+    cp_ = cur_;
+    base_ = t;
+    step_dt_ = dt;
+    // the ghost values of the step's start state (the trace kernel without an advance)
+    PairArgs P = pair_args(n_pairs(), T.N, gl_, gr_, pstack_, rot_, xoff_, X_[cp_], snorm_[cp_], nullptr, nullptr,
+                           gold_, gnew_, trace_, flags_ + 6, stacks_);
+    ckd(cudaMemsetAsync(flags_ + 6, 0, sizeof(int), s), "SGBC flag reset");
+    const int grid = static_cast<int>(std::min<int64_t>(kGridCap, (n_pairs() + 7) / 8));
+    sgbc_trace_kernel<<<std::max(1, grid), 256, 0, s>>>(P, x, 0, 1);
+    ckd(cudaGetLastError(), "SGBC trace kernel");
+    ++launches_;
+}
+
 void SgbcOp::before_stage(const TablesDev& T, const StageArgs& A, double t, cudaStream_t s)
 {
+    if (A.batch != 1) throw std::invalid_argument("thin-layer (SGBC) sub-solvers need a single incidence");
     double span = 0.0, nominal = 0.0;
     int store_old = 0;
     switch (A.mode) {
-    case MODE_MULT: span = t - base_; nominal = span; break;
-    case MODE_RK4_1: base_ = t; step_dt_ = A.dt; span = 0.0; store_old = 1; break;
+    case MODE_MULT: {
+        // a Mult at stage time t: (t + c dt) - t differs from c dt by rounding only, so a cached
+        // map of a span within a few ulps of t is reused rather than rebuilt every step
+        span = t - base_;
+        nominal = span;
+        const double tol = 8.0 * std::numeric_limits<double>::epsilon() * std::max(1.0, std::fabs(t));
+        for (const auto& kv : maps_) {
+            const auto& k = kv.first;
+            if (std::get<0>(k) == 0 && std::fabs(std::get<2>(k) - span) <= tol) { nominal = std::get<2>(k); break; }
+        }
+        break;
+    }
+    case MODE_RK4_1:   // the step's checkpoint (Solver::step, Solver.cpp:535-542)
+        cp_ = cur_; base_ = t; step_dt_ = A.dt; span = 0.0; store_old = 1;
+        break;
     case MODE_RK4_2:
     case MODE_RK4_3: span = t - base_; nominal = 0.5 * A.dt; break;
     case MODE_RK4_4: span = t - base_; nominal = A.dt; break;
     default:
         throw std::invalid_argument("thin-layer (SGBC) sub-solvers are coupled to classical RK4 (DGTD_RK4) and Mult");
     }
-    if (A.batch != 1) throw std::invalid_argument("thin-layer (SGBC) sub-solvers need a single incidence");
     const int advance = span > 1e-12 ? 1 : 0;
     cur_flag_ = (A.mode == MODE_MULT) ? 0 : A.mode;
-    PairArgs P = pair_args(n_pairs(), T.N, gl_, gr_, pstack_, rot_, xoff_, X_, snorm_, gold_, gnew_, trace_,
-                           flags_ + cur_flag_, stacks_);
+    if (advance) trim_maps();
+    PairArgs P = pair_args(n_pairs(), T.N, gl_, gr_, pstack_, rot_, xoff_, X_[cp_], snorm_[cp_], nullptr, nullptr,
+                           gold_, gnew_, trace_, flags_ + cur_flag_, stacks_);
     if (advance)
         for (int st = 0; st < n_stacks(); ++st) {
             const DevMap& M = stage_map(st, nominal, sgbc_nsteps(stacks_[st].spec.sub_dt, span));
@@ -446,8 +493,7 @@ void SgbcOp::before_stage(const TablesDev& T, const StageArgs& A, double t, cuda
             P.st[st].G = M.a + 12 * M.n;
         }
     ckd(cudaMemsetAsync(flags_ + cur_flag_, 0, sizeof(int), s), "SGBC flag reset");
-    const int64_t warps_per_block = 8;
-    const int grid = static_cast<int>(std::min<int64_t>(kGridCap, (n_pairs() + warps_per_block - 1) / warps_per_block));
+    const int grid = static_cast<int>(std::min<int64_t>(kGridCap, (n_pairs() + 7) / 8));
     sgbc_trace_kernel<<<std::max(1, grid), 256, 0, s>>>(P, A.in, advance, store_old);
     ckd(cudaGetLastError(), "SGBC trace kernel");
     ++launches_;
@@ -465,11 +511,15 @@ void SgbcOp::after_stage(const TablesDev& T, const StageArgs& A, cudaStream_t s)
     sgbc_flux_kernel<<<grid, 128, shmem, s>>>(T, F);
     ckd(cudaGetLastError(), "SGBC flux kernel");
     ++launches_;
-    if (A.mode != MODE_RK4_4) return;
+    if (A.mode == MODE_RK4_4) finalize(T, A.x, s);
+}
 
-    // finalisation over the step
-    PairArgs P = pair_args(n_pairs(), T.N, gl_, gr_, pstack_, rot_, xoff_, X_, snorm_, gold_, gnew_, trace_,
-                           flags_ + 7, stacks_);
+void SgbcOp::finalize(const TablesDev& T, const double* x, cudaStream_t s)
+{
+    const int out = 1 - cp_;
+    trim_maps();
+    PairArgs P = pair_args(n_pairs(), T.N, gl_, gr_, pstack_, rot_, xoff_, X_[cp_], snorm_[cp_], X_[out], snorm_[out],
+                           gold_, gnew_, trace_, flags_ + 7, stacks_);
     int64_t n_max = 0;
     for (int st = 0; st < n_stacks(); ++st) {
         const DevMap& M = final_map(st, step_dt_, sgbc_nsteps(stacks_[st].spec.sub_dt, step_dt_));
@@ -480,18 +530,19 @@ void SgbcOp::after_stage(const TablesDev& T, const StageArgs& A, cudaStream_t s)
     }
     ckd(cudaMemsetAsync(flags_ + 7, 0, sizeof(int), s), "SGBC flag reset");
     const int qgrid = static_cast<int>(std::max<int64_t>(1, (n_pairs() + 255) / 256));
-    sgbc_quiesce_kernel<<<qgrid, 256, 0, s>>>(P, A.x);
+    sgbc_quiesce_kernel<<<qgrid, 256, 0, s>>>(P, x);
     ckd(cudaGetLastError(), "SGBC quiescence kernel");
     const size_t fsh = static_cast<size_t>(n_max + 24) * sizeof(double);
     const int fgrid = static_cast<int>(std::min<int64_t>(kGridCap, std::max<int64_t>(1, n_pairs())));
     sgbc_final_kernel<<<fgrid, 256, fsh, s>>>(P, n_max);
     ckd(cudaGetLastError(), "SGBC final kernel");
     launches_ += 2;
+    cur_ = out;
 }
 
 void SgbcOp::read_states(double* host) const
 {
-    ckd(cudaMemcpy(host, X_, static_cast<size_t>(state_len_) * sizeof(double), cudaMemcpyDeviceToHost),
+    ckd(cudaMemcpy(host, X_[cur_], static_cast<size_t>(state_len_) * sizeof(double), cudaMemcpyDeviceToHost),
         "cudaMemcpy SGBC states");
 }
 

@@ -29,14 +29,22 @@ public:
     int n_stacks() const { return static_cast<int>(stacks_.size()); }
     const SgbcStack1D& stack(int i) const { return stacks_[i]; }
 
+    // The step's checkpoint (GlobalEvolution::commitSGBCCheckpoint): the current states become
+    // the checkpoint every stage restarts from, t the start time, dt the step, and the face-frame
+    // ghost values of x (the step's start state) are kept for the finalisation.
+    void commit(const TablesDev& T, const double* x, double t, double dt, cudaStream_t s);
+    // The step's end (GlobalEvolution::finalizeSGBCStep): the states advance from the checkpoint
+    // over dt with ghosts interpolated between the checkpoint's and x's (the step's end state).
+    void finalize(const TablesDev& T, const double* x, cudaStream_t s);
+
     // Before a stage on input `in` at stage time t (MODE_MULT: span t - base; RK4 stage k: the
-    // nominal span c_k dt, sub-step count from t - base). RK4 stage 1 sets the checkpoint time.
+    // nominal span c_k dt, sub-step count from t - base). RK4 stage 1 commits the checkpoint.
     void before_stage(const TablesDev& T, const StageArgs& A, double t, cudaStream_t s);
     // After the stage kernel: adds the SGBC face flux into the stage's outputs; after RK4 stage 4
-    // advances the sub-solvers over the step (finalisation).
+    // finalises the step.
     void after_stage(const TablesDev& T, const StageArgs& A, cudaStream_t s);
 
-    // Copies of the per-pair states (tests): [pairs][n of the pair's stack] concatenated.
+    // Copies of the current per-pair states (tests): [pairs][n of the pair's stack] concatenated.
     void read_states(double* host) const;
     int64_t state_len() const { return state_len_; }
     double base_time() const { return base_; }
@@ -49,6 +57,7 @@ private:
     };
     const DevMap& stage_map(int st, double span, int nsteps);
     void release();
+    void trim_maps();
     const DevMap& final_map(int st, double span, int nsteps);
 
     std::vector<SgbcStack1D> stacks_;
@@ -56,15 +65,17 @@ private:
     int64_t state_len_ = 0;
     double base_ = 0.0;
     double step_dt_ = 0.0;
-    int flag_slot_ = 0;
     int64_t launches_ = 0;
     std::map<std::tuple<int, int, double, int>, DevMap> maps_;   // (kind, stack, span, nsteps)
     // device buffers
     int32_t *gl_ = nullptr, *gr_ = nullptr, *pstack_ = nullptr;
     double* rot_ = nullptr;
     int64_t* xoff_ = nullptr;
-    double* X_ = nullptr;
-    double* snorm_ = nullptr;
+    // states and their norms, double-buffered: [cp_] is the checkpoint every stage restarts from,
+    // [cur_] the current states (the finalisation writes the buffer that is not the checkpoint)
+    double* X_[2] = {nullptr, nullptr};
+    double* snorm_[2] = {nullptr, nullptr};
+    int cp_ = 0, cur_ = 0;
     double* gold_ = nullptr;
     double* gnew_ = nullptr;
     double* trace_ = nullptr;

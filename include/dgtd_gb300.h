@@ -325,8 +325,8 @@ int dgtd_op_set_probes(dgtd_op* op, const dgtd_probe_spec* spec);
  * The FP64 form with one incidence and classical RK4 (and dgtd_op_mult) only:
  * DGTD_ERR_UNSUPPORTED for the other forms, batches, LSERK4 and dgtd_op_step_noalloc. Before
  * dgtd_op_set_sgbc, stepping an operator whose mesh has DGTD_BC_SGBC faces fails with
- * DGTD_ERR_UNSUPPORTED. dgtd_op_mult at time t advances from the last step's start (0 before the
- * first step). */
+ * DGTD_ERR_UNSUPPORTED. dgtd_op_mult at time t advances the checkpoint (the states at the last
+ * step's start; zero, at time 0, before the first) over t minus that start. */
 typedef struct dgtd_sgbc_layer {
     double eps_r, mu_r;
     double sigma;        /* conductivity in solver units (S/m times the free-space impedance) */
@@ -346,6 +346,14 @@ typedef struct dgtd_sgbc_stack {
 /* face_stack[i]: stack of the i-th interior face given with DGTD_BC_SGBC (mesh order). The
  * sub-solver states start at zero. */
 int dgtd_op_set_sgbc(dgtd_op* op, const dgtd_sgbc_stack* stacks, int32_t n_stacks, const int32_t* face_stack);
+/* The step hooks of the reference's Solver::step (Solver.cpp:535-551) for callers that drive
+ * their own integrator with dgtd_op_mult: commit before the step's first stage (the states become
+ * the checkpoint every Mult restarts from; t the step's start, dt its length, d_x its start
+ * state; GlobalEvolution::commitSGBCCheckpoint) and finalize after its last (the states advance
+ * from the checkpoint over dt with ghosts interpolated towards d_x, the step's end state;
+ * GlobalEvolution::finalizeSGBCStep). dgtd_op_step does both itself. */
+int dgtd_op_sgbc_commit(dgtd_op* op, const void* d_x, double t, double dt, void* stream);
+int dgtd_op_sgbc_finalize(dgtd_op* op, const void* d_x, void* stream);
 /* Pairs and total sub-solver unknowns (0, 0 without SGBC); h_states (if not NULL, capacity
  * `cap` entries) receives the pairs' states, pair after pair. */
 int dgtd_op_sgbc_states(const dgtd_op* op, int64_t* n_pairs, int64_t* state_len, double* h_states, int64_t cap);

@@ -80,3 +80,52 @@ def sgbc_box(n=(4, 3, 3), hi=(2.0, 1.0, 1.0), planes=(1.0,), tfsf=True):
     sheets = [plane_faces(m.vertices, m.elements, x) for x in planes]
     faces = np.concatenate(sheets) if sheets else np.zeros((0, 3), np.int32)
     return m, sheets, faces
+
+
+FREE_SPACE_IMPEDANCE = 4e-7 * 3.141592653589793 * SPEED_OF_LIGHT_SI
+
+
+def tem_waveguide(n=(16, 2, 2), hi=(4.0, 0.5, 0.5), tf_cell=4, sheet_x=2.5):
+    """A TEM waveguide along x: PEC walls at y = 0, hi[1], PMC walls at z = 0, hi[2], SMA ends;
+    the TF/SF plane at cell tf_cell (total field beyond), and the interior faces on x = sheet_x.
+    An Ey/Hz plane wave along x travels in it as in free space. Returns (box mesh, boundary codes,
+    sheet faces)."""
+    import numpy as np
+    from oracle import pyoracle as po
+    m = po.box_mesh(n, hi=hi, outer_bc=po.BC_SMA, tfsf=((tf_cell, 0, 0), tuple(n)))
+    V = np.asarray(m.vertices)
+    codes = []
+    for f in np.asarray(m.bdr_faces):
+        P = V[f]
+        on = lambda a, v: bool(np.all(np.abs(P[:, a] - v) < 1e-12))
+        if on(1, 0.0) or on(1, hi[1]):
+            codes.append(1)
+        elif on(2, 0.0) or on(2, hi[2]):
+            codes.append(2)
+        else:
+            codes.append(3)
+    return m, np.array(codes, np.int32), plane_faces(V, m.elements, sheet_x)
+
+
+def slab_pulse(times, x_sheet, x_probe, spread, mean, eps, mu, sigma, width, kind):
+    """Analytic response of a homogeneous slab (relative eps, mu, conductivity sigma in solver
+    units, thickness width) of zero extent in the mesh at x_sheet to the Gaussian plane wave
+    exp(-(x - t - mean)^2 / (2 spread^2)) at normal incidence: the transmitted ('t', probe beyond
+    the sheet) or reflected ('r', probe before it) field at x_probe, from the slab's S21 / S11
+    (transmission-line matrix of the slab, fields referred to its faces)."""
+    import numpy as np
+    dt = times[1] - times[0]
+    N = 1 << 16
+    t = np.arange(N) * dt - 20.0
+    F = np.fft.fft(np.exp(-((x_sheet - t - mean) ** 2) / (2 * spread ** 2)))
+    w = 2 * np.pi * np.fft.fftfreq(N, dt)
+    wa = np.where(w == 0, 1e-30, np.abs(w))
+    ec = eps - 1j * sigma / wa                       # e^{+i w t}: eps_c = eps - i sigma / w
+    k = wa * np.sqrt(mu * ec)
+    Z = np.sqrt(mu / ec)
+    den = np.cos(k * width) + 0.5j * (Z + 1 / Z) * np.sin(k * width)
+    S = (1 / den) if kind == "t" else (0.5j * (Z - 1 / Z) * np.sin(k * width) / den)
+    S = np.where(w >= 0, S, np.conj(S))
+    lag = (x_probe - x_sheet) if kind == "t" else (x_sheet - x_probe)
+    out = np.real(np.fft.ifft(F * S * np.exp(-1j * w * lag)))
+    return np.interp(times, t, out)

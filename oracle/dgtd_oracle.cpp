@@ -358,6 +358,11 @@ struct Oracle {
     vector<int64_t> vmapP;        // [K][nfaces][Nfp]
     // thin-layer (SGBC) sub-solvers, set by orc_set_sgbc
     std::shared_ptr<struct Sgbc> sgbc;
+    // second-order (curved) elements, set by orc_set_curved: per element its index into cnodes
+    // (-1: affine), cnodes [n][10][3] = corners, then edge nodes of (0,1) (0,2) (0,3) (1,2) (1,3) (2,3)
+    vector<int64_t> cidx;
+    vector<double> cnodes;
+    bool is_curved(int64_t e) const { return !cidx.empty() && cidx[e] >= 0; }
 
     // ---- geometry
     void ref_to_phys(int64_t e, const double* xi, double* x) const
@@ -550,10 +555,53 @@ static void build_faces(Oracle& O, int64_t nb, const int32_t* bf, const int32_t*
 // precision (the mass matrix of the p = 6 node set has condition number ~2e3).
 struct ElemMats { vector<double> M, Minv, S[3], D[3]; };
 
+// Geometry map of element e at reference point xi: position x and Jacobian J[r][d] = dx_r/dxi_d
+// (affine, or the second-order isoparametric map x = sum_k l_k (2 l_k - 1) X_k + sum 4 l_a l_b X_ab).
+static const int kEdgeA[6] = {0, 0, 0, 1, 1, 2}, kEdgeB[6] = {1, 2, 3, 2, 3, 3};
+static void geom(const Oracle& O, int64_t e, const double* xi, double* x, double* J)
+{
+    if (!O.is_curved(e)) {
+        O.ref_to_phys(e, xi, x);
+        for (int r = 0; r < 3; ++r) for (int d = 0; d < 3; ++d) J[r * 3 + d] = (d < O.dim) ? O.A[e * 3 * O.dim + r * O.dim + d] : 0.0;
+        return;
+    }
+    const double* G = &O.cnodes[O.cidx[e] * 30];
+    const double l[4] = {1.0 - xi[0] - xi[1] - xi[2], xi[0], xi[1], xi[2]};
+    static const double dl[4][3] = {{-1, -1, -1}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+    for (int r = 0; r < 3; ++r) { x[r] = 0.0; for (int d = 0; d < 3; ++d) J[r * 3 + d] = 0.0; }
+    for (int k = 0; k < 4; ++k) {
+        const double N = l[k] * (2.0 * l[k] - 1.0);
+        for (int r = 0; r < 3; ++r) {
+            x[r] += N * G[3 * k + r];
+            for (int d = 0; d < 3; ++d) J[r * 3 + d] += (4.0 * l[k] - 1.0) * dl[k][d] * G[3 * k + r];
+        }
+    }
+    for (int m = 0; m < 6; ++m) {
+        const int a = kEdgeA[m], b = kEdgeB[m];
+        const double N = 4.0 * l[a] * l[b];
+        for (int r = 0; r < 3; ++r) {
+            x[r] += N * G[3 * (4 + m) + r];
+            for (int d = 0; d < 3; ++d) J[r * 3 + d] += 4.0 * (l[b] * dl[a][d] + l[a] * dl[b][d]) * G[3 * (4 + m) + r];
+        }
+    }
+}
+
+static double det3(const double* J, double* Jinv)
+{
+    const double c0 = J[4] * J[8] - J[5] * J[7], c1 = J[5] * J[6] - J[3] * J[8], c2 = J[3] * J[7] - J[4] * J[6];
+    const double det = J[0] * c0 + J[1] * c1 + J[2] * c2;
+    // Jinv[d][r] = d xi_d / d x_r
+    Jinv[0] = c0 / det; Jinv[3] = c1 / det; Jinv[6] = c2 / det;
+    Jinv[1] = (J[2] * J[7] - J[1] * J[8]) / det; Jinv[4] = (J[0] * J[8] - J[2] * J[6]) / det; Jinv[7] = (J[1] * J[6] - J[0] * J[7]) / det;
+    Jinv[2] = (J[1] * J[5] - J[2] * J[4]) / det; Jinv[5] = (J[2] * J[3] - J[0] * J[5]) / det; Jinv[8] = (J[0] * J[4] - J[1] * J[3]) / det;
+    return det;
+}
+
 static ElemMats elem_mats(const Oracle& O, int64_t e, const Quad& q)
 {
     typedef long double R;
     const int Np = O.Np, dim = O.dim;
+    const bool curved = O.is_curved(e);
     vector<R> M(Np * Np, 0), S[3];
     for (int d = 0; d < 3; ++d) S[d].assign(Np * Np, 0);
     vector<R> phi(Np), dphi(Np * dim), g(Np);
@@ -561,12 +609,20 @@ static ElemMats elem_mats(const Oracle& O, int64_t e, const Quad& q)
     for (size_t k = 0; k < nq; ++k) {
         const double* xi = &q.x[k * dim];
         O.B.shapeR(xi, phi.data()); O.B.dshapeR(xi, dphi.data());
-        R w = static_cast<R>(q.w[k]) * O.detJ[e];
+        double Jinv[9], detJ = O.detJ[e];
+        if (curved) {
+            double x[3], J[9];
+            geom(O, e, xi, x, J);
+            detJ = det3(J, Jinv);
+            if (!(detJ > 0)) throw std::runtime_error("oracle: curved element with a non-positive Jacobian");
+        }
+        R w = static_cast<R>(q.w[k]) * detJ;
         for (int i = 0; i < Np; ++i) for (int j = 0; j < Np; ++j) M[i * Np + j] += w * phi[i] * phi[j];
         for (int d = 0; d < dim; ++d) {
             // d phi_j / d x_d = sum_r dphi_j/dxi_r * Ainv[r][d]
             for (int j = 0; j < Np; ++j) {
-                R gg = 0; for (int r = 0; r < dim; ++r) gg += dphi[j * dim + r] * O.Ainv[e * 3 * dim + r * 3 + d];
+                R gg = 0;
+                for (int r = 0; r < dim; ++r) gg += dphi[j * dim + r] * (curved ? Jinv[r * 3 + d] : O.Ainv[e * 3 * dim + r * 3 + d]);
                 g[j] = gg;
             }
             for (int i = 0; i < Np; ++i) for (int j = 0; j < Np; ++j) S[d][i * Np + j] += w * phi[i] * g[j];
@@ -611,6 +667,7 @@ static void shape_classes(Oracle& O, vector<int64_t>& rep)
     O.shape_of.resize(O.K);
     rep.clear();
     for (int64_t e = 0; e < O.K; ++e) {
+        if (O.is_curved(e)) { O.shape_of[e] = static_cast<int>(rep.size()); rep.push_back(e); continue; }
         vector<double> key(O.A.begin() + e * 3 * dim, O.A.begin() + (e + 1) * 3 * dim);
         for (auto& v : key) v = std::round(v * 1e12) / 1e12;
         auto it = cls.find(key);
@@ -644,9 +701,16 @@ static void face_points(const Oracle& O, const Face& F, vector<double>& xq, vect
 // the other element). mode 0: zero-normal (w = beta/2 wq |J|), 1: one-normal
 // dir d (w = beta/2 wq n_d |J|, un-normalised normal), 2: two-normal (d, d2)
 // (w = beta/2 wq n_d n_d2 / |J| with the un-normalised normal).
+static void face_rows_curved(const Oracle& O, const Face& F, int side, int mode, int d, int d2, double beta,
+                             bool decoupled, double* own, double* coup);
+
 static void face_rows(const Oracle& O, const Face& F, int side, int mode, int d, int d2, double beta, bool decoupled,
                       double* own, double* coup)
 {
+    if (O.is_curved(F.e1) || (F.e2 >= 0 && O.is_curved(F.e2))) {
+        face_rows_curved(O, F, side, mode, d, d2, beta, decoupled, own, coup);
+        return;
+    }
     const int Np = O.Np;
     vector<double> xq, wq; face_points(O, F, xq, wq);
     double nn = 1.0;
@@ -680,6 +744,68 @@ static void face_rows(const Oracle& O, const Face& F, int side, int mode, int d,
     }
 }
 
+// The same rows on a face with a curved side: points from the reference face of e1, mapped to
+// each element's reference coordinates through the shared vertices (the face's barycentric
+// coordinates), and the face's un-normalised normal t_u x t_v from e1's geometry map at each
+// point (oriented out of e1): mode 0 weighs by |t_u x t_v|, mode 1 by its component d, mode 2 by
+// c_d c_d2 / |c|.
+static void face_rows_curved(const Oracle& O, const Face& F, int side, int mode, int d, int d2, double beta,
+                             bool decoupled, double* own, double* coup)
+{
+    const int Np = O.Np;
+    static const double rv[4][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+    int l1[3], l2[3] = {0, 0, 0}, c = 0;
+    for (int q = 0; q < 4; ++q) if (q != F.f1) l1[c++] = q;
+    const bool has2 = F.e2 >= 0;
+    if (has2)
+        for (int k = 0; k < 3; ++k) {
+            const int32_t g = O.elems[F.e1 * 4 + l1[k]];
+            int found = -1;
+            for (int q = 0; q < 4; ++q) if (O.elems[F.e2 * 4 + q] == g) found = q;
+            if (found < 0) throw std::runtime_error("oracle: face vertices do not match");
+            l2[k] = found;
+        }
+    std::fill(own, own + Np * Np, 0.0);
+    std::fill(coup, coup + Np * Np, 0.0);
+    const Quad tq = tri_quad(O.p + 4);
+    vector<double> p1(Np), p2(Np);
+    for (size_t k = 0; k < tq.w.size(); ++k) {
+        const double u = tq.x[2 * k], v = tq.x[2 * k + 1];
+        const double b[3] = {1.0 - u - v, u, v};
+        double xi1[3] = {0, 0, 0}, xi2[3] = {0, 0, 0}, du[3], dv[3];
+        for (int r = 0; r < 3; ++r) {
+            for (int q = 0; q < 3; ++q) { xi1[r] += b[q] * rv[l1[q]][r]; xi2[r] += b[q] * rv[l2[q]][r]; }
+            du[r] = rv[l1[1]][r] - rv[l1[0]][r];
+            dv[r] = rv[l1[2]][r] - rv[l1[0]][r];
+        }
+        double x[3], J[9], tu[3], tv[3], cr[3];
+        geom(O, F.e1, xi1, x, J);
+        for (int r = 0; r < 3; ++r) {
+            tu[r] = J[r * 3] * du[0] + J[r * 3 + 1] * du[1] + J[r * 3 + 2] * du[2];
+            tv[r] = J[r * 3] * dv[0] + J[r * 3 + 1] * dv[1] + J[r * 3 + 2] * dv[2];
+        }
+        cross(tu, tv, cr);
+        if (cr[0] * F.n[0] + cr[1] * F.n[1] + cr[2] * F.n[2] < 0) for (int r = 0; r < 3; ++r) cr[r] = -cr[r];
+        const double len = std::sqrt(cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2]);
+        const double nn = (mode == 0) ? len : (mode == 1 ? cr[d] : cr[d] * cr[d2] / len);
+        O.B.shape(xi1, p1.data());
+        if (has2) O.B.shape(xi2, p2.data());
+        const double w = 0.5 * beta * tq.w[k] * nn;
+        if (side == 1) {
+            for (int i = 0; i < Np; ++i) for (int j = 0; j < Np; ++j) {
+                own[i * Np + j] += w * p1[i] * p1[j];
+                if (has2 && !decoupled) coup[i * Np + j] -= w * p1[i] * p2[j];
+            }
+        } else {
+            const double s2 = (mode == 1) ? -1.0 : 1.0;
+            for (int i = 0; i < Np; ++i) for (int j = 0; j < Np; ++j) {
+                own[i * Np + j] += s2 * w * p2[i] * p2[j];
+                if (!decoupled) coup[i * Np + j] -= s2 * w * p2[i] * p1[j];
+            }
+        }
+    }
+}
+
 static void build_global(Oracle& O)
 {
     const int Np = O.Np, dim = O.dim, nf = O.nfaces, R = 6 * Np, S = (1 + nf);
@@ -691,8 +817,10 @@ static void build_global(Oracle& O)
     vector<int64_t> rep;
     shape_classes(O, rep);
     vector<ElemMats> cls_mats(rep.size());
+    const Quad vqc = (dim == 3) ? tet_quad(O.p + 4) : vq;   // curved elements: one point more per direction
 #pragma omp parallel for schedule(dynamic, 1)
-    for (int64_t c = 0; c < static_cast<int64_t>(rep.size()); ++c) cls_mats[c] = elem_mats(O, rep[c], vq);
+    for (int64_t c = 0; c < static_cast<int64_t>(rep.size()); ++c)
+        cls_mats[c] = elem_mats(O, rep[c], O.is_curved(rep[c]) ? vqc : vq);
 
     // per element: dense local rows [R][S slots][6][Np] -> compressed rows
     vector<vector<int32_t>> colsA(O.K), colsT(O.K), colsS(O.K);
@@ -914,6 +1042,8 @@ static void build_nodal(Oracle& O)
     const int Np = O.Np, Nfp = O.Nfp, dim = O.dim, nf = O.nfaces;
     if (!O.sgbc_faces.empty())
         throw std::runtime_error("oracle: thin-layer (SGBC) faces exist in the global form only (GlobalEvolution)");
+    if (!O.cidx.empty())
+        throw std::runtime_error("oracle: curved elements are assembled in the global form only");
     Quad vq;
     if (dim == 3) vq = tet_quad(O.p + 3);
     else { vector<double> g, gw; gauss_legendre01(O.p + 2, g, gw); vq.x = g; vq.w = gw; }
@@ -1744,6 +1874,37 @@ int orc_threads(void)
 #else
     return 1;
 #endif
+}
+
+// Second-order (curved) geometry of n elements: elems[n] element ids, nodes [n][10][3] = the
+// element's four corners (its vertex order) then its edge nodes of (0,1) (0,2) (0,3) (1,2) (1,3)
+// (2,3). Their DOF node positions move onto the curved map; the global form assembles them with
+// per-point Jacobians. Affine meshes need no call.
+int orc_set_curved(void* h, int64_t n, const int32_t* elems, const double* nodes)
+{
+    try {
+        auto& O = *static_cast<orc::Oracle*>(h);
+        if (O.dim != 3) throw std::runtime_error("oracle: curved elements are 3D");
+        O.cidx.assign(O.K, -1);
+        O.cnodes.assign(nodes, nodes + 30 * n);
+        for (int64_t i = 0; i < n; ++i) {
+            if (elems[i] < 0 || elems[i] >= O.K) throw std::runtime_error("oracle: curved element id out of range");
+            O.cidx[elems[i]] = i;
+        }
+        for (int32_t e : O.tfsf_elems)
+            if (O.cidx[e] >= 0) throw std::runtime_error("oracle: TF/SF faces on curved elements are not supported");
+        for (int64_t i = 0; i < n; ++i) {
+            const int64_t e = elems[i];
+            for (int k = 0; k < O.Np; ++k) {
+                double x[3], J[9], Ji[9];
+                orc::geom(O, e, &O.B.nodes[k * 3], x, J);
+                if (!(orc::det3(J, Ji) > 0)) throw std::runtime_error("oracle: curved element with a non-positive Jacobian");
+                for (int r = 0; r < 3; ++r) O.X[r * O.N + e * O.Np + k] = x[r];
+            }
+        }
+        O.have_csr = false;
+    } catch (const std::exception& e) { g_orc_err = e.what(); return -1; }
+    return 0;
 }
 
 // Thin-layer (SGBC) stacks: layer_prm [total layers][6] = eps_r, mu_r, sigma (solver units), width,

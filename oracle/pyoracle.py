@@ -61,6 +61,8 @@ def lib() -> C.CDLL:
         h.orc_threads.restype = C.c_int
         h.orc_subop.restype = C.c_int
         h.orc_subop.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, _D]
+        h.orc_set_curved.restype = C.c_int
+        h.orc_set_curved.argtypes = [C.c_void_p, C.c_int64, _I32, _D]
         h.orc_set_sgbc.restype = C.c_int
         h.orc_set_sgbc.argtypes = [C.c_void_p, C.c_int, _I32, _D, _I32, _D, _I32]
         h.orc_sgbc_pairs.restype = C.c_int64; h.orc_sgbc_pairs.argtypes = [C.c_void_p]
@@ -171,6 +173,14 @@ class Oracle:
 
     def nnz(self) -> int:
         return int(lib().orc_nnz(self.h))
+
+    def set_curved(self, elems, nodes) -> None:
+        """Second-order geometry of the listed elements: nodes [n, 10, 3] = corners (the element's
+        vertex order) then edge nodes of (0,1) (0,2) (0,3) (1,2) (1,3) (2,3)."""
+        el = np.ascontiguousarray(elems, dtype=np.int32).reshape(-1)
+        nd = np.ascontiguousarray(nodes, dtype=np.float64).reshape(-1)
+        self._keep += [el, nd]
+        self._chk(lib().orc_set_curved(self.h, el.size, _i(el), _d(nd)))
 
     def set_sgbc(self, stacks: Sequence[dict], face_stack) -> None:
         """Thin-layer (SGBC) sub-solvers for the interior faces given with code 4, in their order:

@@ -41,6 +41,7 @@ class MeshDesc(C.Structure):
         ("n_bdr_faces", C.c_int64), ("bdr_faces", C.POINTER(C.c_int32)), ("bdr_codes", C.POINTER(C.c_int32)),
         ("n_tfsf_faces", C.c_int64), ("tfsf_faces", C.POINTER(C.c_int32)),
         ("n_int_faces", C.c_int64), ("int_faces", C.POINTER(C.c_int32)), ("int_codes", C.POINTER(C.c_int32)),
+        ("n_curved", C.c_int64), ("curved_elems", C.POINTER(C.c_int32)), ("curved_nodes", C.POINTER(C.c_double)),
     ]
 
 
@@ -181,6 +182,7 @@ SIGNATURES = {
     "dgtd_op_sgbc_finalize": (C.c_int, [_P, _P, _P]),
     "dgtd_sgbc_stack_operator": (C.c_int, [C.POINTER(SgbcStack), _I64, _I64, _I64, _D, C.c_int64]),
     "dgtd_sgbc_stack_maps": (C.c_int, [C.POINTER(SgbcStack), C.c_double, C.c_int32, _D, _D, _D, _D, _D]),
+    "dgtd_curved_block_rows": (C.c_int, [C.POINTER(MeshDesc), C.c_int32, C.c_double, _I32, _I32, _D, C.c_int64]),
     "dgtd_op_clear_probes": (C.c_int, [_P]),
     "dgtd_op_probe_reset": (C.c_int, [_P, _P]),
     "dgtd_op_probe_info": (C.c_int, [_P, _I64, _I64, _I64]),
@@ -275,6 +277,10 @@ class Mesh:
     mu: Optional[np.ndarray] = None
     sigma: Optional[np.ndarray] = None
     dim: int = 3
+    # second-order (curved) elements: ids and [n, 10, 3] geometry nodes (corners, then the edge
+    # nodes of (0,1) (0,2) (0,3) (1,2) (1,3) (2,3))
+    curved_elems: np.ndarray = field(default_factory=lambda: np.zeros((0,), np.int32))
+    curved_nodes: np.ndarray = field(default_factory=lambda: np.zeros((0, 10, 3), np.float64))
 
     @property
     def n_elements(self) -> int:
@@ -286,7 +292,8 @@ class Mesh:
         return Mesh(f64(self.vertices), i32(self.elements), i32(self.bdr_faces).reshape(-1, 3),
                     i32(self.bdr_codes).reshape(-1), i32(self.tfsf_faces).reshape(-1, 3),
                     i32(self.int_faces).reshape(-1, 3), i32(self.int_codes).reshape(-1),
-                    f64(self.eps), f64(self.mu), f64(self.sigma), self.dim)
+                    f64(self.eps), f64(self.mu), f64(self.sigma), self.dim,
+                    i32(self.curved_elems).reshape(-1), f64(self.curved_nodes).reshape(-1, 10, 3))
 
 
 def box_mesh(n: Sequence[int], lo=(0.0, 0.0, 0.0), hi=(1.0, 1.0, 1.0), hole=None, tfsf=None,
@@ -407,7 +414,23 @@ def _mesh_desc(m: Mesh) -> MeshDesc:
     d.n_bdr_faces = m.bdr_codes.shape[0]; d.bdr_faces = _ip(m.bdr_faces); d.bdr_codes = _ip(m.bdr_codes)
     d.n_tfsf_faces = m.tfsf_faces.shape[0]; d.tfsf_faces = _ip(m.tfsf_faces)
     d.n_int_faces = m.int_codes.shape[0]; d.int_faces = _ip(m.int_faces); d.int_codes = _ip(m.int_codes)
+    d.n_curved = m.curved_elems.shape[0]
+    d.curved_elems = _ip(m.curved_elems) if d.n_curved else C.POINTER(C.c_int32)()
+    d.curved_nodes = _dp(m.curved_nodes) if d.n_curved else null_d
     return d
+
+
+def curved_block_rows(mesh: Mesh, order: int, alpha: float = 1.0) -> dict:
+    """The curved elements' rows of the operator, built on the host (no GPU): blocks
+    [n, 5, 6 Np, 6 Np] over the element's own state (block 0) and its face neighbours'."""
+    m = mesh.normalized()
+    d = _mesh_desc(m)
+    n = m.curved_elems.shape[0]
+    Np = (order + 1) * (order + 2) * (order + 3) // 6
+    el, nb = np.zeros(n, np.int32), np.zeros((n, 4), np.int32)
+    B = np.zeros((n, 5, 6 * Np, 6 * Np))
+    _check(lib().dgtd_curved_block_rows(C.byref(d), order, alpha, _ip(el), _ip(nb), _dp(B), B.size), "curved_block_rows")
+    return {"elems": el, "nbr": nb, "blocks": B}
 
 
 def validate_mesh(mesh: Mesh, order: int = 3, batch: int = 1) -> dict:
@@ -788,11 +811,13 @@ class Case:
         _check(lib().dgtd_case_mesh(self._h, C.byref(d)), "dgtd_case_mesh")
         nv, ne, nb, nt, ni = d.n_vertices, d.n_elements, d.n_bdr_faces, d.n_tfsf_faces, d.n_int_faces
         arr = lambda p, n, dt: np.ctypeslib.as_array(p, shape=(n,)).astype(dt).copy() if n > 0 else np.zeros(0, dt)
+        nc = d.n_curved
         return Mesh(arr(d.vertices, 3 * nv, np.float64).reshape(-1, 3), arr(d.elements, 4 * ne, np.int32).reshape(-1, 4),
                     arr(d.bdr_faces, 3 * nb, np.int32).reshape(-1, 3), arr(d.bdr_codes, nb, np.int32),
                     arr(d.tfsf_faces, 3 * nt, np.int32).reshape(-1, 3), arr(d.int_faces, 3 * ni, np.int32).reshape(-1, 3),
                     arr(d.int_codes, ni, np.int32), arr(d.eps_r, ne, np.float64), arr(d.mu_r, ne, np.float64),
-                    arr(d.sigma, ne, np.float64))
+                    arr(d.sigma, ne, np.float64), 3, arr(d.curved_elems, nc, np.int32),
+                    arr(d.curved_nodes, 30 * nc, np.float64).reshape(-1, 10, 3))
 
     def planewaves(self) -> list:
         n = self.info["n_waves"]

@@ -24,7 +24,7 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompil
 
 SOURCES = ["refelem.cpp", "mesh.cpp", "plain_fp64.cu", "batched.cu", "batched_tc.cu", "tc_selftest.cu", "capi.cu",
            "serve.cu", "probes.cu", "jsoncase.cpp", "case_api.cu",
-           "single_f32.cu", "stability.cu", "single_tc.cu", "sgbc.cpp", "sgbc_dev.cu"]
+           "single_f32.cu", "stability.cu", "single_tc.cu", "sgbc.cpp", "sgbc_dev.cu", "curved.cpp", "curved_dev.cu"]
 
 
 def nvcc() -> str:

@@ -20,6 +20,8 @@
 #include "mesh.hpp"
 #include "probes.hpp"
 #include "refelem.hpp"
+#include "curved.hpp"
+#include "curved_dev.hpp"
 #include "sgbc_dev.hpp"
 #include "single_tc.hpp"
 
@@ -136,6 +138,8 @@ struct dgtd_op {
     int64_t probe_steps = 0;
     // thin-layer (SGBC) sub-solvers of the mesh's DGTD_BC_SGBC faces (dgtd_op_set_sgbc)
     std::unique_ptr<dgtd::SgbcOp> sgbc;
+    // block rows of the mesh's curved (second-order) elements
+    std::unique_ptr<dgtd::CurvedOp> curved;
 
     ~dgtd_op()
     {
@@ -237,6 +241,12 @@ dgtd::MeshInput to_input(const dgtd_mesh_desc* m)
         in.int_faces.assign(m->int_faces, m->int_faces + 3 * m->n_int_faces);
         in.int_codes.assign(m->int_codes, m->int_codes + m->n_int_faces);
     }
+    if (m->n_curved < 0) throw std::invalid_argument("n_curved must be >= 0");
+    if (m->n_curved > 0) {
+        if (!m->curved_elems || !m->curved_nodes) throw std::invalid_argument("curved elements without arrays");
+        in.curved_elems.assign(m->curved_elems, m->curved_elems + m->n_curved);
+        in.curved_nodes.assign(m->curved_nodes, m->curved_nodes + 30 * m->n_curved);
+    }
     return in;
 }
 
@@ -295,6 +305,10 @@ void run_stage(dgtd_op* op, dgtd::StageArgs A, double t, cudaStream_t s)
     }
     ck(dgtd::launch_stage_fp64(op->dev, A, s), "stage kernel");
     g_launches.fetch_add(1, std::memory_order_relaxed);
+    if (op->curved) {
+        op->curved->apply(op->dev, A, s);
+        g_launches.fetch_add(1, std::memory_order_relaxed);
+    }
     if (op->sgbc) {
         const int64_t before = op->sgbc->launches();
         op->sgbc->after_stage(op->dev, A, s);
@@ -535,6 +549,8 @@ int dgtd_op_create(const dgtd_mesh_desc* mesh, const dgtd_op_opts* opts, dgtd_op
         op->state_len = 6 * op->mesh.K * Np * static_cast<int64_t>(op->batch);
         if (!op->mesh.sgbc_faces.empty() && (op->precision != DGTD_FP64 || op->batch != 1))
             return fail(DGTD_ERR_UNSUPPORTED, "thin-layer (SGBC) faces need the FP64 form with one incidence");
+        if (!op->mesh.curved_elems.empty() && op->precision != DGTD_FP64)
+            return fail(DGTD_ERR_UNSUPPORTED, "curved (second-order) elements need the FP64 form");
         for (auto c : op->mesh.fcode)
             if (c == dgtd::FACE_TFSF_TF || c == dgtd::FACE_TFSF_SF) ++op->n_tfsf_faces;
 
@@ -559,6 +575,11 @@ int dgtd_op_create(const dgtd_mesh_desc* mesh, const dgtd_op_opts* opts, dgtd_op
         T.xyz = op->up(xyz);
         T.tfsf_elems = op->up(op->mesh.tfsf_elems);
         T.n_tfsf_elems = static_cast<int64_t>(op->mesh.tfsf_elems.size());
+        if (!op->mesh.curved_elems.empty()) {
+            op->curved = std::make_unique<dgtd::CurvedOp>(op->mesh, op->ref, opts->alpha);
+            T.curved = op->curved->flags();
+            op->device_bytes += op->curved->device_bytes();
+        }
         ck(cudaMalloc(&op->skip_dev, op->batch * sizeof(int)), "cudaMalloc skip");
         op->skip_sc.parts = dgtd::tfsf_skip_parts(T.n_tfsf_elems * T.Np);
         ck(cudaMalloc(&op->skip_sc.partial, static_cast<size_t>(op->batch) * op->skip_sc.parts * sizeof(double)),
@@ -1354,6 +1375,25 @@ int dgtd_sgbc_stack_maps(const dgtd_sgbc_stack* stack, double span, int32_t nste
         }
     } catch (const std::invalid_argument& e) {
         return fail(DGTD_ERR_UNSUPPORTED, e.what());
+    } catch (const std::exception& e) {
+        return fail(DGTD_ERR_INVALID, e.what());
+    }
+    return DGTD_OK;
+}
+
+int dgtd_curved_block_rows(const dgtd_mesh_desc* mesh, int32_t order, double alpha, int32_t* elems, int32_t* nbr,
+                           double* blocks, int64_t cap)
+{
+    if (!mesh) return fail(DGTD_ERR_INVALID, "NULL mesh");
+    if (order < 1 || order > 6) return fail(DGTD_ERR_UNSUPPORTED, "order must be in [1, 6]");
+    try {
+        const dgtd::RefTet ref = dgtd::build_ref_tet(order);
+        const dgtd::MeshTables T = dgtd::build_tables(to_input(mesh), ref);
+        const dgtd::CurvedRows C = dgtd::build_curved_rows(T, ref, alpha);
+        if (static_cast<int64_t>(C.blocks.size()) > cap) return fail(DGTD_ERR_INVALID, "block buffer too small");
+        if (elems) std::copy(C.elems.begin(), C.elems.end(), elems);
+        if (nbr) std::copy(C.nbr.begin(), C.nbr.end(), nbr);
+        if (blocks) std::copy(C.blocks.begin(), C.blocks.end(), blocks);
     } catch (const std::exception& e) {
         return fail(DGTD_ERR_INVALID, e.what());
     }

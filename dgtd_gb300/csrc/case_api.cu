@@ -122,6 +122,9 @@ int dgtd_case_mesh(const dgtd_case* cs, dgtd_mesh_desc* m)
     m->n_int_faces = static_cast<int64_t>(c.int_codes.size());
     m->int_faces = c.int_faces.data();
     m->int_codes = c.int_codes.data();
+    m->n_curved = static_cast<int64_t>(c.curved_elems.size());
+    m->curved_elems = c.curved_elems.data();
+    m->curved_nodes = c.curved_nodes.data();
     return DGTD_OK;
 }
 
@@ -142,6 +145,8 @@ int dgtd_case_auto_dt(const dgtd_case* cs, double* dt)
         in.tfsf_faces = c.tfsf_faces;
         in.int_faces = c.int_faces;
         in.int_codes = c.int_codes;
+        in.curved_elems = c.curved_elems;
+        in.curved_nodes = c.curved_nodes;
         const dgtd::MeshTables T = dgtd::build_tables(in, dgtd::build_ref_tet(c.order));
         const int evolution = c.evolution_operator == "maxwell" ? 0 : (c.evolution_operator == "hesthaven" ? 2 : 1);
         *dt = dgtd::estimate_dt(T, c.order, c.cfl, evolution);

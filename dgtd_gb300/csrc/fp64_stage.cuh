@@ -245,6 +245,7 @@ __device__ __forceinline__ void stage_body(const TablesT<R>& T, const StageArgsT
     if (tid >= nel * Np) return;
     const int el = tid / Np, i = tid - el * Np;
     const int64_t e = e0 + el;
+    if (T.curved != nullptr && T.curved[e]) return;   // rows from the curved-element kernel
     R ar[6], as[6], at[6];
 #pragma unroll
     for (int c = 0; c < 6; ++c) { ar[c] = R(0); as[c] = R(0); at[c] = R(0); }

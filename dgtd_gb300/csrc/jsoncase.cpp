@@ -276,9 +276,35 @@ GmshMesh read_gmsh22(const std::string& path)
                     auto v = nodes(type == 11 ? 10 : 6);
                     second_order = true;
                     const double dev = edge_node_deviation(m.xyz, v.data(), nc, static_cast<int>(v.size()) - nc);
-                    if (dev > kCurvedTol) {
+                    if (dev > kCurvedTol && type == 11) {
+                        // a curved tetrahedron keeps its edge nodes: each on the edge whose midpoint is
+                        // nearest, in the order (0,1) (0,2) (0,3) (1,2) (1,3) (2,3)
+                        static const int ea[6] = {0, 0, 0, 1, 1, 2}, eb[6] = {1, 2, 3, 2, 3, 3};
+                        double pos[6][3];
+                        bool used[6] = {false, false, false, false, false, false};
+                        for (int k = 0; k < 6; ++k) {
+                            const double* xm = &m.xyz[3 * static_cast<size_t>(v[4 + k])];
+                            int best = -1;
+                            double bd = INFINITY;
+                            for (int q = 0; q < 6; ++q) {
+                                double d2 = 0.0;
+                                for (int r = 0; r < 3; ++r) {
+                                    const double d = xm[r] - 0.5 * (m.xyz[3 * static_cast<size_t>(v[ea[q]]) + r] +
+                                                                    m.xyz[3 * static_cast<size_t>(v[eb[q]]) + r]);
+                                    d2 += d * d;
+                                }
+                                if (d2 < bd) { bd = d2; best = q; }
+                            }
+                            if (used[best]) throw std::runtime_error(path + ": curved tetrahedron with two nodes on one edge");
+                            used[best] = true;
+                            for (int r = 0; r < 3; ++r) pos[best][r] = xm[r];
+                        }
+                        m.curved_tets.push_back(static_cast<int32_t>(m.tet_tag.size()));
+                        for (int q = 0; q < 6; ++q) m.curved_edges.insert(m.curved_edges.end(), pos[q], pos[q] + 3);
                         ++curved;
                         max_dev = std::max(max_dev, dev);
+                    } else if (dev > kCurvedTol) {
+                        ++curved;   // a curved triangle: its geometry comes from the tetrahedra
                     }
                     if (type == 11) {
                         m.tets.insert(m.tets.end(), v.begin(), v.begin() + 4);
@@ -314,13 +340,7 @@ GmshMesh read_gmsh22(const std::string& path)
         for (auto& v : m.tris) v = remap[v];
         m.xyz.swap(xyz);
     }
-    if (curved > 0) {
-        char buf[160];
-        std::snprintf(buf, sizeof(buf), ": %ld second-order elements are curved (edge nodes up to %.3g off the straight "
-                                        "edges): curved geometry is not supported",
-                      curved, max_dev);
-        throw std::runtime_error(path + buf);
-    }
+    (void)max_dev;
     return m;
 }
 
@@ -608,14 +628,32 @@ Case load_case(const std::string& json_path)
     const Json& model = J.at("model");
     GmshMesh g = read_gmsh22(c.dir + "/" + model.at("filename").string());
     if (const Json* r = model.find("refinement"))
+        if (r->integer() > 0 && !g.curved_tets.empty())
+            throw std::runtime_error("refinement of meshes with curved elements is not supported");
+    if (const Json* r = model.find("refinement"))
         for (int k = 0; k < r->integer(); ++k) refine_uniform(g);
     const int64_t K = static_cast<int64_t>(g.tet_tag.size());
     c.vertices = g.xyz;
     c.elements = g.tets;
+    std::vector<int64_t> curved_of(K, -1);
+    for (size_t q = 0; q < g.curved_tets.size(); ++q) curved_of[g.curved_tets[q]] = static_cast<int64_t>(q);
     for (int64_t e = 0; e < K; ++e) {
         int32_t* v = &c.elements[4 * e];
         const double* X = c.vertices.data();
-        if (orient(X + 3 * v[0], X + 3 * v[1], X + 3 * v[2], X + 3 * v[3]) < 0.0) std::swap(v[2], v[3]);
+        const bool flip = orient(X + 3 * v[0], X + 3 * v[1], X + 3 * v[2], X + 3 * v[3]) < 0.0;
+        if (flip) std::swap(v[2], v[3]);
+        if (curved_of[e] >= 0) {
+            // corners in the (possibly swapped) vertex order, then the edges; swapping corners 2 and
+            // 3 exchanges the edges (0,2) <-> (0,3) and (1,2) <-> (1,3)
+            static const int keep[6] = {0, 1, 2, 3, 4, 5}, swapped[6] = {0, 2, 1, 4, 3, 5};
+            const double* ed = &g.curved_edges[18 * curved_of[e]];
+            c.curved_elems.push_back(static_cast<int32_t>(e));
+            for (int k = 0; k < 4; ++k) c.curved_nodes.insert(c.curved_nodes.end(), X + 3 * v[k], X + 3 * v[k] + 3);
+            for (int q = 0; q < 6; ++q) {
+                const int src = flip ? swapped[q] : keep[q];
+                c.curved_nodes.insert(c.curved_nodes.end(), ed + 3 * src, ed + 3 * src + 3);
+            }
+        }
     }
 
     // ---- materials by volume tag (driver.cpp:946-982): the first entry of a tag wins, a tag the

@@ -49,6 +49,10 @@ struct GmshMesh {
     std::vector<int32_t> tet_tag;      // physical tag per tet
     std::vector<int32_t> tris;         // [nt][3]
     std::vector<int32_t> tri_tag;
+    // curved second-order tetrahedra: tet index and [6][3] edge-node positions on the edges
+    // (0,1) (0,2) (0,3) (1,2) (1,3) (2,3) of the tet's corner order
+    std::vector<int32_t> curved_tets;
+    std::vector<double> curved_edges;
 };
 
 GmshMesh read_gmsh22(const std::string& path);
@@ -93,6 +97,9 @@ struct Case {
     // interior face given with code DGTD_BC_SGBC (in int_faces order)
     std::vector<SgbcStackSpec> sgbc_stacks;
     std::vector<int32_t> sgbc_face_stack;
+    // curved (second-order) elements: ids and [n][10][3] geometry nodes (dgtd_mesh_desc layout)
+    std::vector<int32_t> curved_elems;
+    std::vector<double> curved_nodes;
     // sources
     std::vector<dgtd_planewave> waves;
     std::vector<CaseInitialField> initial;

@@ -52,6 +52,8 @@ struct TablesT {
     const int32_t* tfsf_elems; // [n_tfsf_elems]
     int64_t n_tfsf_elems;
     R alpha;
+    const uint8_t* curved;     // [K] 1: the element's rows come from the curved-element kernel (the
+                               // stage leaves its outputs alone); nullptr: no curved elements
 };
 
 template <typename R>

@@ -237,6 +237,41 @@ MeshTables build_tables(const MeshInput& in, const RefTet& ref)
     }
     for (int64_t e = 0; e < K; ++e) if (tfsf_elem[e]) T.tfsf_elems.push_back(static_cast<int32_t>(e));
 
+    // ---- curved (second-order) elements: DOF nodes on the isoparametric map
+    //   x = sum_k l_k (2 l_k - 1) X_k + sum_(a<b) 4 l_a l_b X_ab
+    const int64_t ncv = static_cast<int64_t>(in.curved_elems.size());
+    if (static_cast<int64_t>(in.curved_nodes.size()) != 30 * ncv) throw std::runtime_error("curved element geometry size mismatch");
+    {
+        static const int ea[6] = {0, 0, 0, 1, 1, 2}, eb[6] = {1, 2, 3, 2, 3, 3};
+        std::vector<char> seen(K, 0);
+        for (int64_t c = 0; c < ncv; ++c) {
+            const int64_t e = in.curved_elems[c];
+            if (e < 0 || e >= K || seen[e]) throw std::runtime_error("curved element ids must be distinct elements");
+            seen[e] = 1;
+            const double* G = &in.curved_nodes[30 * c];
+            for (int q = 0; q < 4; ++q)
+                for (int d = 0; d < 3; ++d)
+                    if (G[3 * q + d] != X[3 * in.elements[4 * e + q] + d])
+                        throw std::runtime_error("curved element geometry: corners must be the element's vertices");
+            for (int n = 0; n < Np; ++n) {
+                const double* l = &ref.bary[4 * n];
+                double P[3] = {0.0, 0.0, 0.0};
+                for (int k = 0; k < 4; ++k)
+                    for (int d = 0; d < 3; ++d) P[d] += l[k] * (2.0 * l[k] - 1.0) * G[3 * k + d];
+                for (int m = 0; m < 6; ++m)
+                    for (int d = 0; d < 3; ++d) P[d] += 4.0 * l[ea[m]] * l[eb[m]] * G[3 * (4 + m) + d];
+                T.x[e * Np + n] = P[0]; T.y[e * Np + n] = P[1]; T.z[e * Np + n] = P[2];
+            }
+        }
+        for (int32_t e : T.tfsf_elems)
+            if (seen[e]) throw std::runtime_error("TF/SF faces on curved elements are not supported");
+        for (size_t q = 0; q < T.sgbc_faces.size(); q += 4)
+            if (seen[T.sgbc_faces[q]] || seen[T.sgbc_faces[q + 2]])
+                throw std::runtime_error("thin-layer (SGBC) faces on curved elements are not supported");
+        T.curved_elems = in.curved_elems;
+        T.curved_nodes = in.curved_nodes;
+    }
+
     // ---- node maps ----------------------------------------------------------------
     T.vmapP.resize(K * 4 * Nfp);
     const double tol = 1e-7 * min_edge;

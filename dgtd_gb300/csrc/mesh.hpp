@@ -42,6 +42,10 @@ struct MeshInput {
     std::vector<int32_t> tfsf_faces;   // [nt][3]: oriented so the winding normal points into the TF side
     std::vector<int32_t> int_faces;    // [ni][3]: interior PEC/PMC/SMA sheets and thin layers
     std::vector<int32_t> int_codes;    // [ni] 1 PEC, 2 PMC, 3 SMA, 4 SGBC
+    // second-order (curved) elements: ids and [n][10][3] geometry nodes = the element's corners (its
+    // vertex order) then the edge nodes of (0,1) (0,2) (0,3) (1,2) (1,3) (2,3)
+    std::vector<int32_t> curved_elems;
+    std::vector<double> curved_nodes;
 };
 
 // Device-ready tables (host copies).
@@ -56,6 +60,8 @@ struct MeshTables {
     std::vector<int32_t> fcode;         // [K][Nfaces]
     std::vector<int32_t> nbr;           // [K][Nfaces] neighbour element or -1
     std::vector<int32_t> tfsf_elems;    // elements adjacent to a TF/SF face (unique, ascending)
+    std::vector<int32_t> curved_elems;  // curved elements (input order) and their geometry nodes
+    std::vector<double> curved_nodes;   // [n][10][3] (MeshInput layout); their DOF nodes lie on the curved map
     std::vector<int32_t> sgbc_faces;    // [n][4] e1 f1 e2 f2 of the SGBC faces, in input order
                                         // (e1 < e2: the face's first element)
     std::vector<int32_t> elem_vertices; // [K][4] vertex ids (input order)

@@ -302,6 +302,47 @@ void nodal_basis_at(const RefTet& T, double r, double s, double t, double* phi)
     }
 }
 
+void nodal_basis_grad_at(const RefTet& T, double r, double s, double t, double* dphi)
+{
+    const int p = T.p, Np = T.Np;
+    std::vector<double> gr(Np), gs(Np), gt(Np);
+    int m = 0;
+    for (int i = 0; i <= p; ++i)
+        for (int j = 0; i + j <= p; ++j)
+            for (int k = 0; i + j + k <= p; ++k, ++m) grad_simplex3d(r, s, t, i, j, k, gr[m], gs[m], gt[m]);
+    for (int n = 0; n < Np; ++n) {
+        double a = 0.0, b = 0.0, c = 0.0;
+        for (int q = 0; q < Np; ++q) {
+            const double v = T.Vinv[static_cast<size_t>(q) * Np + n];
+            a += v * gr[q]; b += v * gs[q]; c += v * gt[q];
+        }
+        dphi[3 * n] = a; dphi[3 * n + 1] = b; dphi[3 * n + 2] = c;
+    }
+}
+
+void gauss_legendre01(int n, std::vector<double>& x, std::vector<double>& w)
+{
+    // Newton on P_n from the Chebyshev-like first guesses; P_n and P_n' by the three-term recurrence
+    x.resize(n); w.resize(n);
+    for (int i = 0; i < n; ++i) {
+        double z = std::cos(M_PI * (i + 0.75) / (n + 0.5)), dp = 1.0;
+        for (int it = 0; it < 100; ++it) {
+            double p0 = 1.0, p1 = z;
+            for (int k = 2; k <= n; ++k) {
+                const double pk = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p0) / k;
+                p0 = p1; p1 = pk;
+            }
+            const double pn = (n == 1) ? z : p1, pm = (n == 1) ? 1.0 : p0;
+            dp = n * (z * pn - pm) / (z * z - 1.0);
+            const double dz = pn / dp;
+            z -= dz;
+            if (std::fabs(dz) < 1e-16) break;
+        }
+        x[i] = 0.5 * (1.0 - z);
+        w[i] = 1.0 / ((1.0 - z * z) * dp * dp);
+    }
+}
+
 RefSeg build_ref_seg(int p)
 {
     if (p < 1 || p > 16) throw std::runtime_error("segment order must be in [1, 16]");

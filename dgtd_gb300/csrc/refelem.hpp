@@ -54,6 +54,10 @@ RefTet build_ref_tet(int p);
 // Values of the Np nodal basis functions at reference point (r, s, t) (Hesthaven
 // coordinates): phi_n = sum_m Vinv[m][n] psi_m(r, s, t).
 void nodal_basis_at(const RefTet& T, double r, double s, double t, double* phi);
+// Their derivatives: dphi[n][0..2] = d phi_n / d (r, s, t).
+void nodal_basis_grad_at(const RefTet& T, double r, double s, double t, double* dphi);
+// Gauss-Legendre points and weights on [0, 1] (n points, exact to degree 2n - 1).
+void gauss_legendre01(int n, std::vector<double>& x, std::vector<double>& w);
 RefSeg build_ref_seg(int p);
 
 inline int tet_np(int p) { return (p + 1) * (p + 2) * (p + 3) / 6; }

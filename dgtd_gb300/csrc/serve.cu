@@ -138,6 +138,7 @@ __device__ __forceinline__ void slot_views(const LaunchParam& L, const SlotParam
     T.tfsf_elems = reinterpret_cast<const int32_t*>(S.base + Y.tfsf);
     T.n_tfsf_elems = S.n_tfsf;
     T.alpha = static_cast<R>(S.alpha);
+    T.curved = nullptr;
     R* x = reinterpret_cast<R*>(S.base + Y.x);
     R* y0 = reinterpret_cast<R*>(S.base + Y.y0);
     R* y1 = reinterpret_cast<R*>(S.base + Y.y1);
@@ -177,8 +178,8 @@ __global__ void __launch_bounds__(fp64::kBlock) serve_stage(const __grid_constan
         if (L.s[mid].block0 <= bx) lo = mid; else hi = mid - 1;
     }
     const SlotParam& S = L.s[lo];
-    TablesT<R> T;
-    StageArgsT<R> A;
+    TablesT<R> T{};
+    StageArgsT<R> A{};
     slot_views<P, R>(L, S, T, A);
     fp64::stage_body<P, R>(T, A, (bx - S.block0) * fp64::Ord<P, R>::EPB, 0);
 }
@@ -189,8 +190,8 @@ __global__ void __launch_bounds__(256) serve_skip(const __grid_constant__ Launch
 {
     const SlotParam& S = L.s[blockIdx.x];
     if (S.n_pw <= 0 || S.n_tfsf <= 0 || S.skip_known >= 0) return;
-    TablesT<R> T;
-    StageArgsT<R> A;
+    TablesT<R> T{};
+    StageArgsT<R> A{};
     slot_views<P, R>(L, S, T, A);
     fp64::tfsf_skip_body<R>(T, A.pw, A.n_pw, 0, A.t, L.skip + S.pos);
 }
@@ -828,6 +829,7 @@ int dgtd_server_submit(dgtd_server* s, const dgtd_request* q, int64_t* id_out)
                 if (c == DGTD_BC_SGBC)
                     return sfail(DGTD_ERR_UNSUPPORTED, "served requests do not take thin-layer (SGBC) faces");
         }
+        if (m->n_curved != 0) return sfail(DGTD_ERR_UNSUPPORTED, "served requests do not take curved elements");
         for (int i = 0; i < q->n_waves; ++i) {
             const dgtd_planewave& w = q->waves[i];
             if (w.batch != 0) return sfail(DGTD_ERR_INVALID, "a served request is one incidence: wave batch must be 0");

@@ -75,6 +75,13 @@ typedef struct dgtd_mesh_desc {
     int64_t n_int_faces;
     const int32_t* int_faces;   /* [n][3] interior PEC/PMC/SMA sheets */
     const int32_t* int_codes;   /* [n] DGTD_BC_PEC/PMC/SMA/SGBC */
+    /* second-order (curved) elements: their ids and geometry nodes [n_curved][10][3] = the
+     * element's four corners (its vertex order) then the nodes on its edges (0,1) (0,2) (0,3)
+     * (1,2) (1,3) (2,3). They are assembled on their isoparametric map (FP64 form only; no TF/SF
+     * or SGBC faces on them). n_curved = 0 for affine meshes. */
+    int64_t n_curved;
+    const int32_t* curved_elems;
+    const double* curved_nodes;
 } dgtd_mesh_desc;
 
 typedef struct dgtd_op_opts {
@@ -357,6 +364,13 @@ int dgtd_op_sgbc_finalize(dgtd_op* op, const void* d_x, void* stream);
 /* Pairs and total sub-solver unknowns (0, 0 without SGBC); h_states (if not NULL, capacity
  * `cap` entries) receives the pairs' states, pair after pair. */
 int dgtd_op_sgbc_states(const dgtd_op* op, int64_t* n_pairs, int64_t* state_len, double* h_states, int64_t cap);
+
+/* Host-side rows of the curved elements of a mesh (no GPU): elems [n_curved], nbr [n_curved][4]
+ * (face neighbour or -1) and blocks [n_curved][5][6 Np][6 Np] (row-major; rows (component, node)
+ * of dU/dt, columns (component, node) of the element's own state, block 0, or of its neighbour
+ * across face f, block 1 + f). cap = entries available in blocks. */
+int dgtd_curved_block_rows(const dgtd_mesh_desc* mesh, int32_t order, double alpha, int32_t* elems, int32_t* nbr,
+                           double* blocks, int64_t cap);
 
 /* Host-side tables of one stack (no GPU): the sub-solver's size n and operator A [n][n]
  * (A may be NULL to query n; cap = entries available in A), and its interface rows. */

@@ -129,3 +129,43 @@ def slab_pulse(times, x_sheet, x_probe, spread, mean, eps, mu, sigma, width, kin
     lag = (x_probe - x_sheet) if kind == "t" else (x_sheet - x_probe)
     out = np.real(np.fft.ifft(F * S * np.exp(-1j * w * lag)))
     return np.interp(times, t, out)
+
+
+EDGE_PAIRS = [(0, 1), (0, 2), (0, 3), (1, 2), (1, 3), (2, 3)]
+
+
+def curved_box(n=(2, 2, 2), bump=0.03, bc=1, mode="all"):
+    """Box meshes with second-order (curved) tetrahedra for the curved-element tests.
+    mode "all": every vertex and edge node through x -> x + bump sin(pi x) sin(pi y) sin(pi z)
+    (1, 0.6, 0.3), every element curved (the map vanishes on the box's faces);
+    mode "edge": one interior edge's node moved by `bump` across it, the tetrahedra on that edge
+    curved, the rest straight. Returns (box mesh, vertices, elements, curved ids, [n, 10, 3] nodes)."""
+    import numpy as np
+    from oracle import pyoracle as po
+    m = po.box_mesh(n, outer_bc=bc)
+    V = np.asarray(m.vertices, dtype=np.float64)
+    E = np.asarray(m.elements)
+    if mode == "all":
+        f = lambda P: P + bump * np.sin(np.pi * P[..., [0]]) * np.sin(np.pi * P[..., [1]]) * \
+            np.sin(np.pi * P[..., [2]]) * np.array([1.0, 0.6, 0.3])
+        Vc = f(V)
+        els = np.arange(E.shape[0])
+        nodes = np.array([np.vstack([Vc[E[e]]] + [f(0.5 * (V[E[e][a]] + V[E[e][b]])) for a, b in EDGE_PAIRS])
+                          for e in els])
+        return m, Vc, E, els, nodes
+    # the edge from the box's centre vertex along +x
+    c = np.argmin(np.linalg.norm(V - 0.5 * (V.min(0) + V.max(0)), axis=1))
+    nb = [v for v in range(len(V)) if np.allclose(V[v] - V[c], [np.ptp(V[:, 0]) / n[0], 0, 0])]
+    a, b = c, nb[0]
+    els = np.array([e for e in range(E.shape[0]) if a in E[e] and b in E[e]], dtype=np.int32)
+    nodes = []
+    for e in els:
+        t = E[e]
+        mids = []
+        for p, q in EDGE_PAIRS:
+            mid = 0.5 * (V[t[p]] + V[t[q]])
+            if {t[p], t[q]} == {a, b}:
+                mid = mid + np.array([0.0, bump, 0.4 * bump])
+            mids.append(mid)
+        nodes.append(np.vstack([V[t]] + mids))
+    return m, V, E, els, np.array(nodes)

@@ -230,14 +230,34 @@ def test_straight_second_order_mesh_loads_as_linear(tmp_path):
         {k: v for k, v in lin.info.items() if k not in ("mesh_path", "name")}
 
 
-def test_curved_second_order_mesh_rejected(tmp_path):
-    bumped = _case_copy(tmp_path, "box_resonant", "box_p2c",
-                        mesh=lambda src, dst: _second_order_copy(src, dst, bump=1e-3))
-    with pytest.raises(dg.DgtdError, match=r"second-order elements are curved .*curved geometry is not supported"):
-        dg.Case(bumped)
-    # the reference's own curved case: its curved elements are counted and refused
-    with pytest.raises(dg.DgtdError, match=r"\d+ second-order elements are curved"):
-        dg.Case(REFERENCE_INPUTS / "3D_Curved_Element_Test" / "3D_Curved_Element_Test.json")
+def test_curved_second_order_mesh_keeps_its_geometry(tmp_path):
+    """A second-order mesh with an edge node moved off its edge: the tetrahedra on that edge are
+    curved (the reference's test, HesthavenEvolution.cpp:207-241) and keep their ten geometry nodes
+    (corners in the element's vertex order, then the edges (0,1) (0,2) (0,3) (1,2) (1,3) (2,3))."""
+    bumped = dg.Case(_case_copy(tmp_path, "box_resonant", "box_p2c",
+                                mesh=lambda src, dst: _second_order_copy(src, dst, bump=1e-3)))
+    m = bumped.mesh()
+    assert 1 <= len(m.curved_elems) <= 8 and m.curved_nodes.shape == (len(m.curved_elems), 10, 3)
+    pairs = [(0, 1), (0, 2), (0, 3), (1, 2), (1, 3), (2, 3)]
+    devs = []
+    for i, e in enumerate(m.curved_elems):
+        G = m.curved_nodes[i]
+        assert np.array_equal(G[:4], m.vertices[m.elements[e]])
+        devs += [np.linalg.norm(G[4 + q] - 0.5 * (G[a] + G[b])) for q, (a, b) in enumerate(pairs)]
+    assert max(devs) == pytest.approx(1e-3, rel=1e-9) and sorted(devs)[-len(m.curved_elems) - 1] < 1e-12
+    # the reference's own curved case: 122 curved tetrahedra, edge nodes up to 8.8e-3 off
+    c = dg.Case(REFERENCE_INPUTS / "3D_Curved_Element_Test" / "3D_Curved_Element_Test.json")
+    mc = c.mesh()
+    assert len(mc.curved_elems) == 122
+    dev = max(np.linalg.norm(G[4 + q] - 0.5 * (G[a] + G[b])) for G in mc.curved_nodes for q, (a, b) in enumerate(pairs))
+    assert 8.8e-3 < dev < 8.9e-3
+    assert dg.validate_mesh(mc, order=2)["n_elements"] == 1151
+
+    def refine(cj):
+        cj["model"]["refinement"] = 1
+    with pytest.raises(dg.DgtdError, match="refinement of meshes with curved elements"):
+        dg.Case(_case_copy(tmp_path, "box_resonant", "box_p2r", refine,
+                           mesh=lambda src, dst: _second_order_copy(src, dst, bump=1e-3)))
 
 
 def test_material_rules_follow_the_reference(tmp_path):

@@ -277,28 +277,13 @@ GmshMesh read_gmsh22(const std::string& path)
                     second_order = true;
                     const double dev = edge_node_deviation(m.xyz, v.data(), nc, static_cast<int>(v.size()) - nc);
                     if (dev > kCurvedTol && type == 11) {
-                        // a curved tetrahedron keeps its edge nodes: each on the edge whose midpoint is
-                        // nearest, in the order (0,1) (0,2) (0,3) (1,2) (1,3) (2,3)
-                        static const int ea[6] = {0, 0, 0, 1, 1, 2}, eb[6] = {1, 2, 3, 2, 3, 3};
+                        // a curved tetrahedron keeps its edge nodes. gmsh orders them on the edges
+                        // (0,1) (1,2) (0,2) (0,3) (2,3) (1,3); they are stored in the order
+                        // (0,1) (0,2) (0,3) (1,2) (1,3) (2,3)
+                        static const int slot_of[6] = {0, 3, 1, 2, 5, 4};
                         double pos[6][3];
-                        bool used[6] = {false, false, false, false, false, false};
-                        for (int k = 0; k < 6; ++k) {
-                            const double* xm = &m.xyz[3 * static_cast<size_t>(v[4 + k])];
-                            int best = -1;
-                            double bd = INFINITY;
-                            for (int q = 0; q < 6; ++q) {
-                                double d2 = 0.0;
-                                for (int r = 0; r < 3; ++r) {
-                                    const double d = xm[r] - 0.5 * (m.xyz[3 * static_cast<size_t>(v[ea[q]]) + r] +
-                                                                    m.xyz[3 * static_cast<size_t>(v[eb[q]]) + r]);
-                                    d2 += d * d;
-                                }
-                                if (d2 < bd) { bd = d2; best = q; }
-                            }
-                            if (used[best]) throw std::runtime_error(path + ": curved tetrahedron with two nodes on one edge");
-                            used[best] = true;
-                            for (int r = 0; r < 3; ++r) pos[best][r] = xm[r];
-                        }
+                        for (int k = 0; k < 6; ++k)
+                            for (int r = 0; r < 3; ++r) pos[slot_of[k]][r] = m.xyz[3 * static_cast<size_t>(v[4 + k]) + r];
                         m.curved_tets.push_back(static_cast<int32_t>(m.tet_tag.size()));
                         for (int q = 0; q < 6; ++q) m.curved_edges.insert(m.curved_edges.end(), pos[q], pos[q] + 3);
                         ++curved;

@@ -1,9 +1,15 @@
 // Second-order (curved) tetrahedra: block rows of the assembled operator (host).
 #include "curved.hpp"
 
+#include <algorithm>
+#include <atomic>
 #include <cmath>
+#include <exception>
+#include <map>
+#include <mutex>
 #include <stdexcept>
 #include <string>
+#include <thread>
 
 namespace dgtd {
 
@@ -101,44 +107,86 @@ CurvedRows build_curved_rows(const MeshTables& T, const RefTet& ref, double alph
     for (int64_t c = 0; c < nc; ++c) cidx[T.curved_elems[c]] = c;
     auto geo_of = [&](int64_t e) -> const double* { return cidx[e] >= 0 ? &T.curved_nodes[30 * cidx[e]] : nullptr; };
 
-    // collapsed Gauss-Legendre rules on the unit tetrahedron and triangle, p + 4 points per direction
+    // collapsed Gauss-Legendre rules on the unit tetrahedron and triangle, p + 4 points per direction,
+    // with the basis tabulated once at the volume points and, per ordered triple of local vertices,
+    // at the face points
     std::vector<double> g, gw;
     gauss_legendre01(ref.p + 4, g, gw);
     const int ng = static_cast<int>(g.size());
+    std::vector<double> vx, vw, vphi, vdphi;
+    for (int a = 0; a < ng; ++a)
+        for (int b = 0; b < ng; ++b)
+            for (int q = 0; q < ng; ++q) {
+                const double u = g[a], v = g[b], w = g[q];
+                const double xi[3] = {u * (1 - v) * (1 - w), v * (1 - w), w};
+                vx.insert(vx.end(), xi, xi + 3);
+                vw.push_back(gw[a] * gw[b] * gw[q] * (1 - v) * (1 - w) * (1 - w));
+                std::vector<double> ph(Np), dp(3 * Np);
+                basis(ref, xi, ph.data());
+                nodal_basis_grad_at(ref, 2 * xi[0] - 1, 2 * xi[1] - 1, 2 * xi[2] - 1, dp.data());
+                vphi.insert(vphi.end(), ph.begin(), ph.end());
+                vdphi.insert(vdphi.end(), dp.begin(), dp.end());
+            }
+    const int nvq = static_cast<int>(vw.size());
+    std::vector<double> fu, fv, fwt;
+    for (int a = 0; a < ng; ++a)
+        for (int b = 0; b < ng; ++b) {
+            fu.push_back(g[a] * (1 - g[b])); fv.push_back(g[b]); fwt.push_back(gw[a] * gw[b] * (1 - g[b]));
+        }
+    const int nfq = static_cast<int>(fwt.size());
+    std::map<int, std::vector<double>> ftab;   // key l0*16 + l1*4 + l2 -> [nfq][Np]
+    std::mutex ftab_mu;
+    auto face_table = [&](const int* l) -> const std::vector<double>& {
+        const int key = l[0] * 16 + l[1] * 4 + l[2];
+        std::lock_guard<std::mutex> lk(ftab_mu);
+        auto it = ftab.find(key);
+        if (it != ftab.end()) return it->second;
+        std::vector<double> t(static_cast<size_t>(nfq) * Np);
+        for (int k = 0; k < nfq; ++k) {
+            const double bc[3] = {1.0 - fu[k] - fv[k], fu[k], fv[k]};
+            double xi[3] = {0, 0, 0};
+            for (int r = 0; r < 3; ++r)
+                for (int m = 0; m < 3; ++m) xi[r] += bc[m] * kRefV[l[m]][r];
+            basis(ref, xi, &t[static_cast<size_t>(k) * Np]);
+        }
+        return ftab.emplace(key, std::move(t)).first->second;
+    };
 
     C.elems = T.curved_elems;
     C.nbr.assign(4 * nc, -1);
     C.blocks.assign(static_cast<size_t>(nc) * 5 * R * R, 0.0);
-    std::vector<double> phi(Np), dphi(3 * Np), M(Np * Np), S[3], D[3], Minv, W(36 * Np * Np), Wn(36 * Np * Np), pn(Np);
-    for (int64_t c = 0; c < nc; ++c) {
+
+    auto assemble = [&](int64_t c) {
         const int64_t e = T.curved_elems[c];
         const double* G = geo_of(e);
-        // ---- element matrices on the curved map
-        std::fill(M.begin(), M.end(), 0.0);
+        std::vector<double> M(Np * Np, 0.0), S[3], D[3], Minv;
         for (int d = 0; d < 3; ++d) S[d].assign(Np * Np, 0.0);
-        for (int a = 0; a < ng; ++a)
-            for (int b = 0; b < ng; ++b)
-                for (int q = 0; q < ng; ++q) {
-                    const double u = g[a], v = g[b], w = g[q];
-                    const double xi[3] = {u * (1 - v) * (1 - w), v * (1 - w), w};
-                    const double wt = gw[a] * gw[b] * gw[q] * (1 - v) * (1 - w) * (1 - w);
-                    double x[3], J[9], Ji[9];
-                    geom(T, e, G, xi, x, J);
-                    const double det = inv3(J, Ji);
-                    if (!(det > 0.0)) throw std::runtime_error("curved element " + std::to_string(e) + " with a non-positive Jacobian");
-                    basis(ref, xi, phi.data());
-                    nodal_basis_grad_at(ref, 2 * xi[0] - 1, 2 * xi[1] - 1, 2 * xi[2] - 1, dphi.data());
-                    const double ww = wt * det;
-                    for (int i = 0; i < Np; ++i)
-                        for (int j = 0; j < Np; ++j) M[i * Np + j] += ww * phi[i] * phi[j];
-                    for (int d = 0; d < 3; ++d)
-                        for (int j = 0; j < Np; ++j) {
-                            // d phi_j / dx_d = sum_r (2 d phi_j / d rst_r) dxi_r / dx_d
-                            double gj = 0.0;
-                            for (int r = 0; r < 3; ++r) gj += 2.0 * dphi[3 * j + r] * Ji[r * 3 + d];
-                            for (int i = 0; i < Np; ++i) S[d][i * Np + j] += ww * phi[i] * gj;
-                        }
+        std::vector<double> gx(3 * Np);
+        for (int k = 0; k < nvq; ++k) {
+            double x[3], J[9], Ji[9];
+            geom(T, e, G, &vx[3 * k], x, J);
+            const double det = inv3(J, Ji);
+            if (!(det > 0.0)) throw std::runtime_error("curved element " + std::to_string(e) + " with a non-positive Jacobian");
+            const double* phi = &vphi[static_cast<size_t>(k) * Np];
+            const double* dphi = &vdphi[static_cast<size_t>(k) * 3 * Np];
+            const double ww = vw[k] * det;
+            for (int j = 0; j < Np; ++j)
+                for (int d = 0; d < 3; ++d) {
+                    // d phi_j / dx_d = sum_r (2 d phi_j / d rst_r) dxi_r / dx_d
+                    double a = 0.0;
+                    for (int r = 0; r < 3; ++r) a += 2.0 * dphi[3 * j + r] * Ji[r * 3 + d];
+                    gx[3 * j + d] = a;
                 }
+            for (int i = 0; i < Np; ++i) {
+                const double wi = ww * phi[i];
+                for (int j = 0; j < Np; ++j) {
+                    M[i * Np + j] += wi * phi[j];
+                    S[0][i * Np + j] += wi * gx[3 * j];
+                    S[1][i * Np + j] += wi * gx[3 * j + 1];
+                    S[2][i * Np + j] += wi * gx[3 * j + 2];
+                }
+            }
+        }
         Minv = M;
         if (!invert_matrix(Minv, Np)) throw std::runtime_error("singular curved-element mass matrix");
         for (int d = 0; d < 3; ++d) {
@@ -148,9 +196,9 @@ CurvedRows build_curved_rows(const MeshTables& T, const RefTet& ref, double alph
         double* B0 = &C.blocks[(static_cast<size_t>(c) * 5) * R * R];
         const double ie = T.mat[3 * e], im = T.mat[3 * e + 1], se = T.mat[3 * e + 2];
         // curl H into E rows, -curl E into H rows (component blocks of D), conductivity on E
-        auto vol = [&](int row, int col, int d, double s) {
+        auto vol = [&](int row, int col, int d, double sg) {
             for (int i = 0; i < Np; ++i)
-                for (int j = 0; j < Np; ++j) B0[(row * Np + i) * R + col * Np + j] += s * D[d][i * Np + j];
+                for (int j = 0; j < Np; ++j) B0[(row * Np + i) * R + col * Np + j] += sg * D[d][i * Np + j];
         };
         vol(0, 5, 1, ie); vol(0, 4, 2, -ie);    // Ex: dy Hz - dz Hy
         vol(1, 3, 2, ie); vol(1, 5, 0, -ie);    // Ey: dz Hx - dx Hz
@@ -162,6 +210,7 @@ CurvedRows build_curved_rows(const MeshTables& T, const RefTet& ref, double alph
             for (int i = 0; i < Np; ++i) B0[(cmp * Np + i) * R + cmp * Np + i] -= se;
 
         // ---- faces: Minv int phi F dS, F from the traces at each face point
+        std::vector<double> W(36 * Np * Np), Wn(36 * Np * Np), tmp(Np * Np);
         for (int f = 0; f < 4; ++f) {
             const int64_t nb = T.nbr[4 * e + f];
             const int code = T.fcode[4 * e + f];
@@ -175,17 +224,11 @@ CurvedRows build_curved_rows(const MeshTables& T, const RefTet& ref, double alph
             if (nb >= 0 && nb < e) {
                 fe = nb;
                 ff = -1;
-                for (int q = 0; q < 4; ++q) if (T.nbr[4 * nb + q] == e) {
-                    // the neighbour's face opposite its vertex not on this face
-                    bool shared = true;
-                    for (int k = 0; k < 4; ++k) {
-                        if (k == q) continue;
-                        const int32_t gv = T.elem_vertices[4 * nb + k];
-                        bool in_e = false;
-                        for (int m = 0; m < 4; ++m) if (m != f && T.elem_vertices[4 * e + m] == gv) in_e = true;
-                        shared = shared && in_e;
-                    }
-                    if (shared) ff = q;
+                for (int q = 0; q < 4; ++q) {
+                    bool on_face = false;
+                    for (int m = 0; m < 4; ++m)
+                        if (m != f && T.elem_vertices[4 * e + m] == T.elem_vertices[4 * nb + q]) on_face = true;
+                    if (!on_face) ff = q;   // the neighbour's vertex off the shared face
                 }
                 if (ff < 0) throw std::runtime_error("curved element: face not found on its neighbour");
             }
@@ -201,59 +244,65 @@ CurvedRows build_curved_rows(const MeshTables& T, const RefTet& ref, double alph
                 if (le[k] < 0 || (nb >= 0 && ln[k] < 0)) throw std::runtime_error("curved element: face vertices do not match");
             }
             const bool coupled = (code == FACE_INTERIOR);
+            const std::vector<double>& te = face_table(le);
+            const std::vector<double>* tn = coupled ? &face_table(ln) : nullptr;
             const double* nA = &T.fgeo[(4 * e + f) * 4];   // e's outward (affine) normal: orientation only
+            const double* Gf = geo_of(fe);
             std::fill(W.begin(), W.end(), 0.0);
             std::fill(Wn.begin(), Wn.end(), 0.0);
-            for (int a = 0; a < ng; ++a)
-                for (int b = 0; b < ng; ++b) {
-                    const double u = g[a] * (1 - g[b]), v = g[b];
-                    const double wt = gw[a] * gw[b] * (1 - g[b]);
-                    const double bc[3] = {1.0 - u - v, u, v};
-                    double xf[3] = {0, 0, 0}, xe[3] = {0, 0, 0}, xn[3] = {0, 0, 0}, du[3], dv[3];
-                    for (int r = 0; r < 3; ++r) {
-                        for (int k = 0; k < 3; ++k) {
-                            xf[r] += bc[k] * kRefV[l1[k]][r];
-                            xe[r] += bc[k] * kRefV[le[k]][r];
-                            xn[r] += bc[k] * kRefV[ln[k]][r];
-                        }
-                        du[r] = kRefV[l1[1]][r] - kRefV[l1[0]][r];
-                        dv[r] = kRefV[l1[2]][r] - kRefV[l1[0]][r];
-                    }
-                    double x[3], J[9], tu[3], tv[3];
-                    geom(T, fe, geo_of(fe), xf, x, J);
-                    for (int r = 0; r < 3; ++r) {
-                        tu[r] = J[r * 3] * du[0] + J[r * 3 + 1] * du[1] + J[r * 3 + 2] * du[2];
-                        tv[r] = J[r * 3] * dv[0] + J[r * 3 + 1] * dv[1] + J[r * 3 + 2] * dv[2];
-                    }
-                    double cr[3] = {tu[1] * tv[2] - tu[2] * tv[1], tu[2] * tv[0] - tu[0] * tv[2], tu[0] * tv[1] - tu[1] * tv[0]};
-                    if (cr[0] * nA[0] + cr[1] * nA[1] + cr[2] * nA[2] < 0.0) for (int r = 0; r < 3; ++r) cr[r] = -cr[r];
-                    const double len = std::sqrt(cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2]);
-                    const double n[3] = {cr[0] / len, cr[1] / len, cr[2] / len};
-                    double Cm[36], Cp[36];
-                    flux_coeffs(code, n, alpha, Cm, Cp);
-                    basis(ref, xe, phi.data());
-                    if (coupled) basis(ref, xn, pn.data());
-                    const double ds = wt * len;
-                    for (int rc = 0; rc < 36; ++rc) {
-                        const double cm = ds * Cm[rc], cp = ds * Cp[rc];
+            double du[3], dv[3];
+            for (int r = 0; r < 3; ++r) {
+                du[r] = kRefV[l1[1]][r] - kRefV[l1[0]][r];
+                dv[r] = kRefV[l1[2]][r] - kRefV[l1[0]][r];
+            }
+            for (int k = 0; k < nfq; ++k) {
+                const double bc[3] = {1.0 - fu[k] - fv[k], fu[k], fv[k]};
+                double xf[3] = {0, 0, 0};
+                for (int r = 0; r < 3; ++r)
+                    for (int m = 0; m < 3; ++m) xf[r] += bc[m] * kRefV[l1[m]][r];
+                double x[3], J[9], tu[3], tv[3];
+                geom(T, fe, Gf, xf, x, J);
+                for (int r = 0; r < 3; ++r) {
+                    tu[r] = J[r * 3] * du[0] + J[r * 3 + 1] * du[1] + J[r * 3 + 2] * du[2];
+                    tv[r] = J[r * 3] * dv[0] + J[r * 3 + 1] * dv[1] + J[r * 3 + 2] * dv[2];
+                }
+                double cr[3] = {tu[1] * tv[2] - tu[2] * tv[1], tu[2] * tv[0] - tu[0] * tv[2], tu[0] * tv[1] - tu[1] * tv[0]};
+                if (cr[0] * nA[0] + cr[1] * nA[1] + cr[2] * nA[2] < 0.0) for (int r = 0; r < 3; ++r) cr[r] = -cr[r];
+                const double len = std::sqrt(cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2]);
+                const double n[3] = {cr[0] / len, cr[1] / len, cr[2] / len};
+                double Cm[36], Cp[36];
+                flux_coeffs(code, n, alpha, Cm, Cp);
+                const double* phi = &te[static_cast<size_t>(k) * Np];
+                const double* pn = coupled ? &(*tn)[static_cast<size_t>(k) * Np] : nullptr;
+                const double ds = fwt[k] * len;
+                for (int rc = 0; rc < 36; ++rc) {
+                    const double cm = ds * Cm[rc], cp = ds * Cp[rc];
+                    if (cm != 0.0) {
                         double* w0 = &W[static_cast<size_t>(rc) * Np * Np];
+                        for (int i = 0; i < Np; ++i) {
+                            const double a = cm * phi[i];
+                            for (int j = 0; j < Np; ++j) w0[i * Np + j] += a * phi[j];
+                        }
+                    }
+                    if (coupled && cp != 0.0) {
                         double* w1 = &Wn[static_cast<size_t>(rc) * Np * Np];
-                        if (cm != 0.0)
-                            for (int i = 0; i < Np; ++i)
-                                for (int j = 0; j < Np; ++j) w0[i * Np + j] += cm * phi[i] * phi[j];
-                        if (coupled && cp != 0.0)
-                            for (int i = 0; i < Np; ++i)
-                                for (int j = 0; j < Np; ++j) w1[i * Np + j] += cp * phi[i] * pn[j];
+                        for (int i = 0; i < Np; ++i) {
+                            const double a = cp * phi[i];
+                            for (int j = 0; j < Np; ++j) w1[i * Np + j] += a * pn[j];
+                        }
                     }
                 }
+            }
             // B += scale(row) Minv W  (per component pair)
             double* Bf = &C.blocks[(static_cast<size_t>(c) * 5 + 1 + f) * R * R];
-            std::vector<double> tmp(Np * Np);
             for (int rc = 0; rc < 36; ++rc) {
                 const int row = rc / 6, col = rc % 6;
                 const double sc = row < 3 ? ie : im;
                 for (int pass = 0; pass < (coupled ? 2 : 1); ++pass) {
                     const double* w = &(pass == 0 ? W : Wn)[static_cast<size_t>(rc) * Np * Np];
+                    bool any = false;
+                    for (int q = 0; q < Np * Np && !any; ++q) any = (w[q] != 0.0);
+                    if (!any) continue;
                     matmul(Minv.data(), w, tmp.data(), Np, Np, Np);
                     double* B = pass == 0 ? B0 : Bf;
                     for (int i = 0; i < Np; ++i)
@@ -261,7 +310,32 @@ CurvedRows build_curved_rows(const MeshTables& T, const RefTet& ref, double alph
                 }
             }
         }
-    }
+    };
+
+    // elements in parallel (each writes its own blocks)
+    const int nth = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(nc, std::max(1u, std::thread::hardware_concurrency()))));
+    std::atomic<int64_t> next(0);
+    std::exception_ptr err;
+    std::mutex err_mu;
+    auto worker = [&]() {
+        for (;;) {
+            const int64_t c = next.fetch_add(1);
+            if (c >= nc) return;
+            try {
+                assemble(c);
+            } catch (...) {
+                std::lock_guard<std::mutex> lk(err_mu);
+                if (!err) err = std::current_exception();
+                next.store(nc);
+                return;
+            }
+        }
+    };
+    std::vector<std::thread> pool;
+    for (int t = 1; t < nth; ++t) pool.emplace_back(worker);
+    worker();
+    for (auto& th : pool) th.join();
+    if (err) std::rethrow_exception(err);
     return C;
 }
 

@@ -331,17 +331,34 @@ GmshMesh read_gmsh22(const std::string& path)
 
 void refine_uniform(GmshMesh& m)
 {
+    // curved parents: the position of each curved edge's node, and per tet its geometry
+    static const int ea[6] = {0, 0, 0, 1, 1, 2}, eb[6] = {1, 2, 3, 2, 3, 3};
+    std::map<std::pair<int32_t, int32_t>, std::array<double, 3>> curved_edge;
+    std::vector<int64_t> curved_of(m.tet_tag.size(), -1);
+    for (size_t q = 0; q < m.curved_tets.size(); ++q) {
+        const int32_t e = m.curved_tets[q];
+        curved_of[e] = static_cast<int64_t>(q);
+        for (int k = 0; k < 6; ++k) {
+            const int32_t a = m.tets[4 * e + ea[k]], b = m.tets[4 * e + eb[k]];
+            const double* p = &m.curved_edges[18 * q + 3 * k];
+            curved_edge[{std::min(a, b), std::max(a, b)}] = {p[0], p[1], p[2]};
+        }
+    }
     std::map<std::pair<int32_t, int32_t>, int32_t> mid;
     auto midpoint = [&](int32_t a, int32_t b) {
         auto key = std::make_pair(std::min(a, b), std::max(a, b));
         auto it = mid.find(key);
         if (it != mid.end()) return it->second;
         const int32_t id = static_cast<int32_t>(m.xyz.size() / 3);
-        for (int d = 0; d < 3; ++d) m.xyz.push_back(0.5 * (m.xyz[3 * a + d] + m.xyz[3 * b + d]));
+        auto ce = curved_edge.find(key);
+        // a curved edge's midpoint is its edge node (the quadratic edge at parameter 1/2)
+        for (int d = 0; d < 3; ++d)
+            m.xyz.push_back(ce != curved_edge.end() ? ce->second[d] : 0.5 * (m.xyz[3 * a + d] + m.xyz[3 * b + d]));
         mid[key] = id;
         return id;
     };
-    std::vector<int32_t> tets, ttag, tris, rtag;
+    std::vector<int32_t> tets, ttag, tris, rtag, ctets;
+    std::vector<double> cedges;
     const size_t ne = m.tet_tag.size();
     for (size_t e = 0; e < ne; ++e) {
         const int32_t v0 = m.tets[4 * e], v1 = m.tets[4 * e + 1], v2 = m.tets[4 * e + 2], v3 = m.tets[4 * e + 3];
@@ -351,9 +368,55 @@ void refine_uniform(GmshMesh& m)
                                     // the inner octahedron split along the m02-m13 diagonal
                                     {m01, m02, m03, m13}, {m01, m02, m12, m13}, {m02, m03, m13, m23},
                                     {m02, m12, m13, m23}};
-        for (const auto& k : kids) {
+        // the kids' vertices in the parent's barycentric coordinates (vertex k = e_k, midpoint of
+        // (a, b) = (e_a + e_b) / 2), for curved parents
+        static const int kid_pairs[8][4][2] = {
+            {{0, 0}, {0, 1}, {0, 2}, {0, 3}}, {{0, 1}, {1, 1}, {1, 2}, {1, 3}},
+            {{0, 2}, {1, 2}, {2, 2}, {2, 3}}, {{0, 3}, {1, 3}, {2, 3}, {3, 3}},
+            {{0, 1}, {0, 2}, {0, 3}, {1, 3}}, {{0, 1}, {0, 2}, {1, 2}, {1, 3}},
+            {{0, 2}, {0, 3}, {1, 3}, {2, 3}}, {{0, 2}, {1, 2}, {1, 3}, {2, 3}}};
+        for (int kk = 0; kk < 8; ++kk) {
+            const auto& k = kids[kk];
             tets.insert(tets.end(), k, k + 4);
             ttag.push_back(m.tet_tag[e]);
+            if (curved_of[e] < 0) continue;
+            // the kid's edge nodes: the parent's second-order map at the kid's edge midpoints
+            const double* ed = &m.curved_edges[18 * curved_of[e]];
+            double G[10][3];
+            for (int q = 0; q < 4; ++q)
+                for (int d = 0; d < 3; ++d) G[q][d] = m.xyz[3 * static_cast<size_t>(m.tets[4 * e + q]) + d];
+            for (int q = 0; q < 6; ++q)
+                for (int d = 0; d < 3; ++d) G[4 + q][d] = ed[3 * q + d];
+            auto parent_map = [&](const double* l, double* x) {
+                for (int d = 0; d < 3; ++d) {
+                    double a = 0.0;
+                    for (int q = 0; q < 4; ++q) a += l[q] * (2.0 * l[q] - 1.0) * G[q][d];
+                    for (int q = 0; q < 6; ++q) a += 4.0 * l[ea[q]] * l[eb[q]] * G[4 + q][d];
+                    x[d] = a;
+                }
+            };
+            double lv[4][4];
+            for (int q = 0; q < 4; ++q) {
+                for (int r = 0; r < 4; ++r) lv[q][r] = 0.0;
+                lv[q][kid_pairs[kk][q][0]] += 0.5;
+                lv[q][kid_pairs[kk][q][1]] += 0.5;
+            }
+            double nodes[6][3], dev = 0.0;
+            for (int q = 0; q < 6; ++q) {
+                double l[4];
+                for (int r = 0; r < 4; ++r) l[r] = 0.5 * (lv[ea[q]][r] + lv[eb[q]][r]);
+                parent_map(l, nodes[q]);
+                double d2 = 0.0;
+                for (int d = 0; d < 3; ++d) {
+                    const double mm = 0.5 * (m.xyz[3 * static_cast<size_t>(k[ea[q]]) + d] + m.xyz[3 * static_cast<size_t>(k[eb[q]]) + d]);
+                    d2 += (nodes[q][d] - mm) * (nodes[q][d] - mm);
+                }
+                dev = std::max(dev, std::sqrt(d2));
+            }
+            if (dev > kCurvedTol) {
+                ctets.push_back(static_cast<int32_t>(ttag.size() - 1));
+                for (int q = 0; q < 6; ++q) cedges.insert(cedges.end(), nodes[q], nodes[q] + 3);
+            }
         }
     }
     const size_t nt = m.tri_tag.size();
@@ -370,6 +433,8 @@ void refine_uniform(GmshMesh& m)
     m.tet_tag.swap(ttag);
     m.tris.swap(tris);
     m.tri_tag.swap(rtag);
+    m.curved_tets.swap(ctets);
+    m.curved_edges.swap(cedges);
 }
 
 // ============================================================================ case
@@ -613,9 +678,6 @@ Case load_case(const std::string& json_path)
     const Json& model = J.at("model");
     GmshMesh g = read_gmsh22(c.dir + "/" + model.at("filename").string());
     if (const Json* r = model.find("refinement"))
-        if (r->integer() > 0 && !g.curved_tets.empty())
-            throw std::runtime_error("refinement of meshes with curved elements is not supported");
-    if (const Json* r = model.find("refinement"))
         for (int k = 0; k < r->integer(); ++k) refine_uniform(g);
     const int64_t K = static_cast<int64_t>(g.tet_tag.size());
     c.vertices = g.xyz;
@@ -749,8 +811,13 @@ Case load_case(const std::string& json_path)
                 } else if (mt == "resonant") {
                     f.kind = 1;
                     f.modes = int_list(mag.at("modes"));
+                } else if (mt == "besselj6_2D") {   // driver.cpp:552-557, Function.h:170-193
+                    f.kind = 2;
+                } else if (mt == "besselj6_3D") {   // driver.cpp:558-563, Function.h:195-226
+                    f.kind = 3;
                 } else {
-                    throw std::runtime_error("initial field magnitude '" + mt + "' is not supported (gaussian, resonant)");
+                    throw std::runtime_error("initial field magnitude '" + mt +
+                                             "' is not supported (gaussian, resonant, besselj6_2D, besselj6_3D)");
                 }
                 c.initial.push_back(f);
             } else {
@@ -909,6 +976,57 @@ int probe_interval(int saves, int steps_interval, double final_time, double dt)
     return std::max(1, total / saves);
 }
 
+namespace {
+
+// Spherical Bessel function j_l(x): below x = l + 2 the power series
+// x^l sum_k (-x^2 / 2)^k / (k! (2l + 2k + 1)!!), above it the upward recurrence
+// j_(k+1) = (2k + 1) / x j_k - j_(k-1) from j_0 = sin x / x and j_1 = sin x / x^2 - cos x / x.
+double sph_bessel_j(int l, double x)
+{
+    if (x == 0.0) return l == 0 ? 1.0 : 0.0;
+    if (x < l + 2.0) {
+        double dfact = 1.0;
+        for (int k = 1; k <= 2 * l + 1; k += 2) dfact *= k;
+        double term = std::pow(x, l) / dfact, sum = term;
+        for (int k = 1; k < 80; ++k) {
+            term *= -x * x / (2.0 * k * (2.0 * l + 2.0 * k + 1.0));
+            sum += term;
+            if (std::fabs(term) < 1e-18 * std::fabs(sum)) break;
+        }
+        return sum;
+    }
+    double j0 = std::sin(x) / x, j1 = std::sin(x) / (x * x) - std::cos(x) / x;
+    if (l == 0) return j0;
+    for (int k = 1; k < l; ++k) {
+        const double j2 = (2.0 * k + 1.0) / x * j1 - j0;
+        j0 = j1;
+        j1 = j2;
+    }
+    return j1;
+}
+
+// The reference's Bessel cavity fields at t = 0 (alpha6 = 13.589290170541217, the second zero of
+// J_6): 2D: J_6(alpha6 rho) cos(6 phi); 3D: j_6(alpha6 r) Y_66(theta, phi) with the normalised
+// associated Legendre function sqrt(13 / (4 pi) / 12!) 11!! sin^6(theta) (Condon-Shortley sign
+// (-1)^6 = 1).
+constexpr double kAlpha6 = 13.589290170541217;
+
+double besselj6_2d(const double* p)
+{
+    return ::jn(6, kAlpha6 * std::sqrt(p[0] * p[0] + p[1] * p[1])) * std::cos(6.0 * std::atan2(p[1], p[0]));
+}
+
+double besselj6_3d(const double* p)
+{
+    const double r = std::sqrt(p[0] * p[0] + p[1] * p[1] + p[2] * p[2]);
+    if (r == 0.0) return 0.0;
+    const double c = p[2] / r, s2 = 1.0 - c * c;
+    const double P66 = std::sqrt(13.0 / (4.0 * M_PI) / 479001600.0) * 10395.0 * s2 * s2 * s2;
+    return sph_bessel_j(6, kAlpha6 * r) * P66 * std::cos(6.0 * std::atan2(p[1], p[0]));
+}
+
+}  // namespace
+
 std::vector<double> case_initial_state(const Case& c, const double* xyz, int64_t n)
 {
     std::vector<double> u(6 * static_cast<size_t>(n), 0.0);
@@ -920,9 +1038,13 @@ std::vector<double> case_initial_state(const Case& c, const double* xyz, int64_t
                 double r2 = 0.0;
                 for (int d = 0; d < f.dimension; ++d) r2 += (p[d] - f.center[d]) * (p[d] - f.center[d]);
                 v = std::exp(-r2 / (2.0 * f.spread * f.spread));
-            } else {
+            } else if (f.kind == 1) {
                 v = 1.0;
                 for (size_t d = 0; d < f.modes.size() && d < 3; ++d) v *= std::sin(f.modes[d] * M_PI * p[d]);
+            } else if (f.kind == 2) {
+                v = besselj6_2d(p);
+            } else {
+                v = besselj6_3d(p);
             }
             for (int k = 0; k < 3; ++k) u[(3 * f.field + k) * static_cast<size_t>(n) + i] += v * f.pol[k];
         }

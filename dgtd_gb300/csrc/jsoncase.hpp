@@ -62,7 +62,7 @@ void refine_uniform(GmshMesh& m);
 
 struct CaseInitialField {
     int field = 0;                  // 0 electric, 1 magnetic
-    int kind = 0;                   // 0 gaussian, 1 resonant mode
+    int kind = 0;                   // 0 gaussian, 1 resonant mode, 2 besselj6_2D, 3 besselj6_3D
     double spread = 0.1;
     double center[3] = {0, 0, 0};
     double pol[3] = {0, 0, 1};

@@ -273,8 +273,14 @@ MeshTables build_tables(const MeshInput& in, const RefTet& ref)
     }
 
     // ---- node maps ----------------------------------------------------------------
+    // A face node's partner is the neighbour's face node with the same barycentric coordinates on
+    // the same three (global) vertices; positions only confirm it. A curved element and a straight
+    // neighbour (edge nodes within 1e-5 of the midpoints, taken as affine) may place a shared
+    // face's nodes up to a few 1e-5 apart, so faces touching a curved element get that slack.
     T.vmapP.resize(K * 4 * Nfp);
     const double tol = 1e-7 * min_edge;
+    std::vector<char> curved_el(K, 0);
+    for (int32_t e : in.curved_elems) curved_el[e] = 1;
     for (int64_t e = 0; e < K; ++e)
         for (int f = 0; f < 4; ++f) {
             int32_t* out = &T.vmapP[(e * 4 + f) * Nfp];
@@ -284,17 +290,32 @@ MeshTables build_tables(const MeshInput& in, const RefTet& ref)
                 continue;
             }
             int fn = nbr_face[e * 4 + f];
+            // local vertex of the neighbour for each local vertex of e on this face
+            int loc[4] = {-1, -1, -1, -1};
+            for (int q = 0; q < 4; ++q) {
+                if (q == f) continue;
+                for (int r = 0; r < 4; ++r)
+                    if (in.elements[4 * en + r] == in.elements[4 * e + q]) loc[q] = r;
+                if (loc[q] < 0) throw std::runtime_error("neighbouring elements do not share a face's vertices");
+            }
+            const double slack = (curved_el[e] || curved_el[en]) ? 5e-5 : 0.0;
             for (int a = 0; a < Nfp; ++a) {
-                int64_t gm = e * Np + ref.Fmask[f * Nfp + a];
-                int best = -1; double bd = 1e300;
+                const int vm = ref.Fmask[f * Nfp + a];
+                const int64_t gm = e * Np + vm;
+                int best = -1;
+                double bw = 1e300;
                 for (int b = 0; b < Nfp; ++b) {
-                    int64_t gp = en * Np + ref.Fmask[fn * Nfp + b];
-                    double dx = T.x[gm] - T.x[gp], dy = T.y[gm] - T.y[gp], dz = T.z[gm] - T.z[gp];
-                    double d = dx * dx + dy * dy + dz * dz;
-                    if (d < bd) { bd = d; best = b; }
+                    const int vp = ref.Fmask[fn * Nfp + b];
+                    double w = 0.0;
+                    for (int q = 0; q < 4; ++q)
+                        if (q != f) w += std::fabs(ref.bary[4 * vm + q] - ref.bary[4 * vp + loc[q]]);
+                    if (w < bw) { bw = w; best = b; }
                 }
-                if (std::sqrt(bd) > tol) throw std::runtime_error("face nodes of neighbouring elements do not coincide");
-                out[a] = static_cast<int32_t>(en * Np + ref.Fmask[fn * Nfp + best]);
+                const int64_t gp = en * Np + ref.Fmask[fn * Nfp + best];
+                const double dx = T.x[gm] - T.x[gp], dy = T.y[gm] - T.y[gp], dz = T.z[gm] - T.z[gp];
+                if (bw > 1e-9 || std::sqrt(dx * dx + dy * dy + dz * dz) > tol + slack)
+                    throw std::runtime_error("face nodes of neighbouring elements do not coincide");
+                out[a] = static_cast<int32_t>(gp);
             }
         }
     T.elem_vertices = in.elements;

@@ -14,7 +14,8 @@ import sys
 from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
-CASES = ("3D_PEC", "3D_TFSF", "3D_TFSF_InteriorPEC", "3D_Curved_Element_Test", "3D_SGBC")
+CASES = ("3D_PEC", "3D_TFSF", "3D_TFSF_InteriorPEC", "3D_Curved_Element_Test", "3D_SGBC", "3D_Resonant_Cylinder",
+         "3D_Resonant_Sphere")
 
 
 def main() -> None:

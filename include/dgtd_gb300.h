@@ -403,8 +403,9 @@ int dgtd_op_probe_read(dgtd_op* op, double* h_point_dft, double* h_surface_dft, 
  * solver_options, model {filename (gmsh 2.2 ASCII), refinement, materials,
  * boundaries}, sources {initial, planewave}, probes {point, rcssurface, farfield})
  * loaded into this library's tables, with SGBC layers (dgtd_case_sgbc) and curved second-order
- * tetrahedra (their geometry in dgtd_case_mesh). Unsupported features (dipoles, 1D/2D meshes,
- * SGBC faces on curved elements, refinement of curved meshes) are rejected with an error. */
+ * tetrahedra (their geometry in dgtd_case_mesh; refinement keeps children on the parent's map).
+ * Unsupported features (dipoles, 1D/2D meshes, SGBC faces on curved elements) are rejected with
+ * an error. */
 typedef struct dgtd_case dgtd_case;
 
 typedef struct dgtd_case_info {

@@ -253,11 +253,17 @@ def test_curved_second_order_mesh_keeps_its_geometry(tmp_path):
     assert 8.8e-3 < dev < 8.9e-3
     assert dg.validate_mesh(mc, order=2)["n_elements"] == 1151
 
+    # refinement: children on the parent's second-order map; the bumped edge's node becomes a
+    # vertex, and the children along that edge stay curved
     def refine(cj):
         cj["model"]["refinement"] = 1
-    with pytest.raises(dg.DgtdError, match="refinement of meshes with curved elements"):
-        dg.Case(_case_copy(tmp_path, "box_resonant", "box_p2r", refine,
-                           mesh=lambda src, dst: _second_order_copy(src, dst, bump=1e-3)))
+    r = dg.Case(_case_copy(tmp_path, "box_resonant", "box_p2r", refine,
+                           mesh=lambda src, dst: _second_order_copy(src, dst, bump=1e-3))).mesh()
+    assert r.n_elements == 8 * m.n_elements and len(r.curved_elems) > len(m.curved_elems)
+    bumped = [G[4 + q] for G in m.curved_nodes for q, (a, b) in enumerate(pairs)
+              if np.linalg.norm(G[4 + q] - 0.5 * (G[a] + G[b])) > 1e-6]
+    assert np.min(np.linalg.norm(r.vertices - bumped[0], axis=1)) < 1e-14
+    assert dg.validate_mesh(r, order=3)["n_elements"] == r.n_elements
 
 
 def test_material_rules_follow_the_reference(tmp_path):

@@ -1279,7 +1279,7 @@ int dgtd_op_set_sgbc(dgtd_op* op, const dgtd_sgbc_stack* stacks, int32_t n_stack
     if (!face_stack) return fail(DGTD_ERR_INVALID, "face_stack is NULL");
     try {
         std::vector<int32_t> fs(face_stack, face_stack + nf);
-        auto S = std::make_unique<dgtd::SgbcOp>(op->mesh, op->ref, sgbc_specs(stacks, n_stacks), fs);
+        auto S = std::make_unique<dgtd::SgbcOp>(op->mesh, op->ref, sgbc_specs(stacks, n_stacks), fs, op->alpha);
         op->sgbc = std::move(S);
     } catch (const std::invalid_argument& e) {
         return fail(DGTD_ERR_UNSUPPORTED, e.what());

@@ -214,9 +214,9 @@ CurvedRows build_curved_rows(const MeshTables& T, const RefTet& ref, double alph
         for (int f = 0; f < 4; ++f) {
             const int64_t nb = T.nbr[4 * e + f];
             const int code = T.fcode[4 * e + f];
-            if (code == FACE_TFSF_TF || code == FACE_TFSF_SF || code == FACE_SGBC)
-                throw std::runtime_error("TF/SF and thin-layer faces on curved elements are not supported");
-            if (code == FACE_OPEN) continue;
+            if (code == FACE_TFSF_TF || code == FACE_TFSF_SF)
+                throw std::runtime_error("TF/SF faces on curved elements are not supported");
+            if (code == FACE_OPEN || code == FACE_SGBC) continue;   // SGBC: the injection's terms
             C.nbr[4 * c + f] = (code == FACE_INTERIOR) ? static_cast<int32_t>(nb) : -1;
             // the face's first element (lower index) parametrises it
             int64_t fe = e;
@@ -337,6 +337,142 @@ CurvedRows build_curved_rows(const MeshTables& T, const RefTet& ref, double alph
     for (auto& th : pool) th.join();
     if (err) std::rethrow_exception(err);
     return C;
+}
+
+namespace {
+
+// the geometry of element e (second-order nodes when it is curved)
+const double* curved_geometry(const MeshTables& T, int64_t e)
+{
+    for (size_t c = 0; c < T.curved_elems.size(); ++c)
+        if (T.curved_elems[c] == e) return &T.curved_nodes[30 * c];
+    return nullptr;
+}
+
+}  // namespace
+
+void element_face_normal(const MeshTables& T, int64_t e, int f, const double* l, double* n)
+{
+    int l1[3], k1 = 0;
+    for (int q = 0; q < 4; ++q) if (q != f) l1[k1++] = q;
+    const double xi[3] = {l[1], l[2], l[3]};
+    double x[3], J[9], tu[3], tv[3];
+    geom(T, e, curved_geometry(T, e), xi, x, J);
+    for (int r = 0; r < 3; ++r) {
+        tu[r] = tv[r] = 0.0;
+        for (int d = 0; d < 3; ++d) {
+            tu[r] += J[r * 3 + d] * (kRefV[l1[1]][d] - kRefV[l1[0]][d]);
+            tv[r] += J[r * 3 + d] * (kRefV[l1[2]][d] - kRefV[l1[0]][d]);
+        }
+    }
+    double cr[3] = {tu[1] * tv[2] - tu[2] * tv[1], tu[2] * tv[0] - tu[0] * tv[2], tu[0] * tv[1] - tu[1] * tv[0]};
+    const double* nA = &T.fgeo[(4 * e + f) * 4];
+    if (cr[0] * nA[0] + cr[1] * nA[1] + cr[2] * nA[2] < 0.0) for (int r = 0; r < 3; ++r) cr[r] = -cr[r];
+    const double len = std::sqrt(cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2]);
+    for (int r = 0; r < 3; ++r) n[r] = cr[r] / len;
+}
+
+void build_curved_sgbc_face(const MeshTables& T, const RefTet& ref, double alpha, int64_t e, int f,
+                            std::vector<double>& Bm, std::vector<double>& Bp)
+{
+    const int Np = ref.Np, Nfp = ref.Nfp, R = 6 * Np;
+    const double* G = curved_geometry(T, e);
+    std::vector<double> g, gw;
+    gauss_legendre01(ref.p + 4, g, gw);
+    const int ng = static_cast<int>(g.size());
+    // mass matrix on e's map
+    std::vector<double> M(Np * Np, 0.0), phi(Np), pf(Nfp);
+    for (int a = 0; a < ng; ++a)
+        for (int b = 0; b < ng; ++b)
+            for (int q = 0; q < ng; ++q) {
+                const double u = g[a], v = g[b], w = g[q];
+                const double xi[3] = {u * (1 - v) * (1 - w), v * (1 - w), w};
+                double x[3], J[9], Ji[9];
+                geom(T, e, G, xi, x, J);
+                const double ww = gw[a] * gw[b] * gw[q] * (1 - v) * (1 - w) * (1 - w) * inv3(J, Ji);
+                basis(ref, xi, phi.data());
+                for (int i = 0; i < Np; ++i)
+                    for (int j = 0; j < Np; ++j) M[i * Np + j] += ww * phi[i] * phi[j];
+            }
+    std::vector<double> Minv = M;
+    if (!invert_matrix(Minv, Np)) throw std::runtime_error("singular curved-element mass matrix");
+    // the face parametrised from its first element (lower index), as the rows
+    const int64_t nb = T.nbr[4 * e + f];
+    int64_t fe = e;
+    int ff = f;
+    if (nb >= 0 && nb < e) {
+        fe = nb;
+        ff = -1;
+        for (int q = 0; q < 4; ++q) {
+            bool on_face = false;
+            for (int m = 0; m < 4; ++m)
+                if (m != f && T.elem_vertices[4 * e + m] == T.elem_vertices[4 * nb + q]) on_face = true;
+            if (!on_face) ff = q;
+        }
+    }
+    int l1[3], le[3], k1 = 0;
+    for (int q = 0; q < 4; ++q) if (q != ff) l1[k1++] = q;
+    for (int k = 0; k < 3; ++k) {
+        const int32_t gv = T.elem_vertices[4 * fe + l1[k]];
+        le[k] = -1;
+        for (int q = 0; q < 4; ++q) if (T.elem_vertices[4 * e + q] == gv) le[k] = q;
+        if (le[k] < 0) throw std::runtime_error("curved SGBC face: vertices do not match");
+    }
+    const double* Gf = (fe == e) ? G : curved_geometry(T, fe);
+    const double* nA = &T.fgeo[(4 * e + f) * 4];
+    std::vector<double> Wm(36 * Np * Np, 0.0), Wp(36 * Np * Nfp, 0.0);
+    double du[3], dv[3];
+    for (int r = 0; r < 3; ++r) {
+        du[r] = kRefV[l1[1]][r] - kRefV[l1[0]][r];
+        dv[r] = kRefV[l1[2]][r] - kRefV[l1[0]][r];
+    }
+    for (int a = 0; a < ng; ++a)
+        for (int b = 0; b < ng; ++b) {
+            const double u = g[a] * (1 - g[b]), v = g[b], wt = gw[a] * gw[b] * (1 - g[b]);
+            const double bc[3] = {1.0 - u - v, u, v};
+            double xf[3] = {0, 0, 0}, xe[3] = {0, 0, 0};
+            for (int r = 0; r < 3; ++r)
+                for (int m = 0; m < 3; ++m) { xf[r] += bc[m] * kRefV[l1[m]][r]; xe[r] += bc[m] * kRefV[le[m]][r]; }
+            double x[3], J[9], tu[3], tv[3];
+            geom(T, fe, Gf, xf, x, J);
+            for (int r = 0; r < 3; ++r) {
+                tu[r] = J[r * 3] * du[0] + J[r * 3 + 1] * du[1] + J[r * 3 + 2] * du[2];
+                tv[r] = J[r * 3] * dv[0] + J[r * 3 + 1] * dv[1] + J[r * 3 + 2] * dv[2];
+            }
+            double cr[3] = {tu[1] * tv[2] - tu[2] * tv[1], tu[2] * tv[0] - tu[0] * tv[2], tu[0] * tv[1] - tu[1] * tv[0]};
+            if (cr[0] * nA[0] + cr[1] * nA[1] + cr[2] * nA[2] < 0.0) for (int r = 0; r < 3; ++r) cr[r] = -cr[r];
+            const double len = std::sqrt(cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2]);
+            const double n[3] = {cr[0] / len, cr[1] / len, cr[2] / len};
+            double Cm[36], Cp[36];
+            flux_coeffs(FACE_INTERIOR, n, alpha, Cm, Cp);
+            basis(ref, xe, phi.data());
+            for (int q = 0; q < Nfp; ++q) pf[q] = phi[ref.Fmask[f * Nfp + q]];   // e's face-node basis
+            const double ds = wt * len;
+            for (int rc = 0; rc < 36; ++rc) {
+                const double cm = ds * Cm[rc], cp = ds * Cp[rc];
+                if (cm != 0.0)
+                    for (int i = 0; i < Np; ++i)
+                        for (int j = 0; j < Np; ++j) Wm[(static_cast<size_t>(rc) * Np + i) * Np + j] += cm * phi[i] * phi[j];
+                if (cp != 0.0)
+                    for (int i = 0; i < Np; ++i)
+                        for (int q = 0; q < Nfp; ++q) Wp[(static_cast<size_t>(rc) * Np + i) * Nfp + q] += cp * phi[i] * pf[q];
+            }
+        }
+    const double ie = T.mat[3 * e], im = T.mat[3 * e + 1];
+    Bm.assign(static_cast<size_t>(R) * R, 0.0);
+    Bp.assign(static_cast<size_t>(R) * 6 * Nfp, 0.0);
+    std::vector<double> tmp(static_cast<size_t>(Np) * std::max(Np, Nfp));
+    for (int rc = 0; rc < 36; ++rc) {
+        const int row = rc / 6, col = rc % 6;
+        const double sc = row < 3 ? ie : im;
+        matmul(Minv.data(), &Wm[static_cast<size_t>(rc) * Np * Np], tmp.data(), Np, Np, Np);
+        for (int i = 0; i < Np; ++i)
+            for (int j = 0; j < Np; ++j) Bm[(row * Np + i) * static_cast<size_t>(R) + col * Np + j] += sc * tmp[i * Np + j];
+        matmul(Minv.data(), &Wp[static_cast<size_t>(rc) * Np * Nfp], tmp.data(), Np, Np, Nfp);
+        for (int i = 0; i < Np; ++i)
+            for (int q = 0; q < Nfp; ++q)
+                Bp[(row * Np + i) * static_cast<size_t>(6 * Nfp) + col * Nfp + q] += sc * tmp[i * Nfp + q];
+    }
 }
 
 }  // namespace dgtd

@@ -29,7 +29,18 @@ struct CurvedRows {
 
 // Quadrature: collapsed Gauss-Legendre rules with p + 4 points per direction on the element and on
 // its faces (faces parametrised from their first element, the lower index).
-// Materials come from T.mat, faces from T.nbr / T.fcode (TF/SF and SGBC faces are refused).
+// Materials come from T.mat, faces from T.nbr / T.fcode (TF/SF faces are refused; SGBC faces get
+// no terms here: their flux is the SGBC injection, build_curved_sgbc_face).
 CurvedRows build_curved_rows(const MeshTables& T, const RefTet& ref, double alpha);
+
+// Unit normal, out of element e, of its face f at the point with barycentric coordinates l (e's
+// vertex order; l[f] = 0), from e's geometry map (second-order or affine).
+void element_face_normal(const MeshTables& T, int64_t e, int f, const double* l, double* n);
+
+// The SGBC injection on face f of curved element e: dU_e/dt += Bm U_e + Bp t, t the slab traces
+// at e's face nodes (component-major: [6][Nfp], face nodes in e's face order), for the interior
+// upwind flux with upwind coefficient alpha. Bm [6 Np][6 Np] and Bp [6 Np][6 Nfp], row-major.
+void build_curved_sgbc_face(const MeshTables& T, const RefTet& ref, double alpha, int64_t e, int f,
+                            std::vector<double>& Bm, std::vector<double>& Bp);
 
 }  // namespace dgtd

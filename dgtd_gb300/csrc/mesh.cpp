@@ -265,9 +265,6 @@ MeshTables build_tables(const MeshInput& in, const RefTet& ref)
         }
         for (int32_t e : T.tfsf_elems)
             if (seen[e]) throw std::runtime_error("TF/SF faces on curved elements are not supported");
-        for (size_t q = 0; q < T.sgbc_faces.size(); q += 4)
-            if (seen[T.sgbc_faces[q]] || seen[T.sgbc_faces[q + 2]])
-                throw std::runtime_error("thin-layer (SGBC) faces on curved elements are not supported");
         T.curved_elems = in.curved_elems;
         T.curved_nodes = in.curved_nodes;
     }

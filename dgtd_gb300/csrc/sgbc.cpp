@@ -1,6 +1,8 @@
 // Thin-layer boundaries (SGBC): sub-solver operators, sub-step maps and face node pairs.
 #include "sgbc.hpp"
 
+#include "curved.hpp"
+
 #include <algorithm>
 #include <cmath>
 #include <stdexcept>
@@ -342,6 +344,8 @@ SgbcLayout build_sgbc_layout(const MeshTables& T, const RefTet& ref, const std::
     struct Ent { int32_t e, f, role, q; };
     std::vector<Ent> ents;
     std::unordered_map<int64_t, int32_t> pair_of_gr;
+    std::vector<char> curved(T.K, 0);
+    for (int32_t e : T.curved_elems) curved[e] = 1;
     for (int64_t q = 0; q < nf; ++q) {
         const int32_t e1 = T.sgbc_faces[4 * q], f1 = T.sgbc_faces[4 * q + 1];
         const int32_t e2 = T.sgbc_faces[4 * q + 2], f2 = T.sgbc_faces[4 * q + 3];
@@ -349,8 +353,14 @@ SgbcLayout build_sgbc_layout(const MeshTables& T, const RefTet& ref, const std::
         if (st < 0 || st >= n_stacks) throw std::invalid_argument("SGBC: face stack index out of range");
         double R[9];
         sgbc_rotation(&T.fgeo[(static_cast<int64_t>(e1) * 4 + f1) * 4], R);
+        const bool curved_face = curved[e1] || curved[e2];
         for (int a = 0; a < Nfp; ++a) {
             const int64_t gl = static_cast<int64_t>(e1) * Np + ref.Fmask[f1 * Nfp + a];
+            if (curved_face) {   // per-node normal on a curved face (the reference's per-DOF normals)
+                double n[3];
+                element_face_normal(T, e1, f1, &ref.bary[4 * ref.Fmask[f1 * Nfp + a]], n);
+                sgbc_rotation(n, R);
+            }
             const int64_t gr = T.vmapP[(static_cast<int64_t>(e1) * 4 + f1) * Nfp + a];
             if (gr / Np != e2) throw std::runtime_error("SGBC: face node partner outside the face's second element");
             const int32_t pid = static_cast<int32_t>(Lo.gl.size());

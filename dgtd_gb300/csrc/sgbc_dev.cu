@@ -18,6 +18,8 @@
 // Every kernel indexes only the pairs, entries and stacks the host built and checked.
 #include "sgbc_dev.hpp"
 
+#include "curved.hpp"
+
 #include <algorithm>
 #include <cmath>
 #include <limits>
@@ -156,6 +158,8 @@ struct FluxArgs {
     const int32_t* ent_face;
     const int32_t* ent_role;
     const int32_t* ent_pairs;
+    const int64_t* ent_cblk;
+    const double* cblk;
     int mode;
     double dt;
     double* out;
@@ -164,16 +168,57 @@ struct FluxArgs {
     double* x;
 };
 
+__device__ __forceinline__ void sgbc_add(const FluxArgs& A, int64_t o, double ks)
+{
+    const double dt = A.dt;
+    switch (A.mode) {
+    case MODE_MULT: A.out[o] += ks; break;
+    case MODE_RK4_1: A.yout[o] += 0.5 * dt * ks; A.z[o] += (dt / 6.0) * ks; break;
+    case MODE_RK4_2: A.yout[o] += 0.5 * dt * ks; A.z[o] += (dt / 3.0) * ks; break;
+    case MODE_RK4_3: A.yout[o] += dt * ks; A.z[o] += (dt / 3.0) * ks; break;
+    case MODE_RK4_4: A.x[o] += (dt / 6.0) * ks; break;
+    default: break;
+    }
+}
+
 // one block per element with SGBC faces (at most 4 entries: one per face)
 __global__ void __launch_bounds__(128) sgbc_flux_kernel(TablesDev T, FluxArgs A)
 {
     if (*A.flag == 0) return;   // every pair quiescent: no injection
-    extern __shared__ double sfl[];   // [4][Nfp][6]
+    extern __shared__ double sfl[];   // straight: [4][Nfp][6]; curved: [6 Np] state, [4][6][Nfp] traces
     const int Np = T.Np, Nfp = T.Nfp;
     const int64_t N = T.N;
     for (int64_t ie = blockIdx.x; ie < A.n_elems; ie += gridDim.x) {
         const int64_t e = A.el_elem[ie];
         const int k0 = A.el_start[ie], nent = A.el_start[ie + 1] - k0;
+        if (A.ent_cblk[k0] >= 0) {   // a curved element: its dense injection blocks
+            const int R = 6 * Np, F6 = 6 * Nfp;
+            double* su = sfl;
+            double* st = sfl + R;
+            for (int w = threadIdx.x; w < R; w += blockDim.x) {
+                const int c = w / Np, i = w - c * Np;
+                su[w] = A.in[c * N + e * Np + i];
+            }
+            for (int w = threadIdx.x; w < nent * F6; w += blockDim.x) {
+                const int k = w / F6, rr = w - k * F6, c = rr / Nfp, a = rr - c * Nfp;
+                const int64_t pr = A.ent_pairs[static_cast<int64_t>(k0 + k) * Nfp + a];
+                st[w] = A.trace[pr * 12 + A.ent_role[k0 + k] * 6 + c];
+            }
+            __syncthreads();
+            for (int r = threadIdx.x; r < R; r += blockDim.x) {
+                double acc = 0.0;
+                for (int k = 0; k < nent; ++k) {
+                    const double* BmT = A.cblk + A.ent_cblk[k0 + k];
+                    const double* BpT = BmT + static_cast<size_t>(R) * R;
+                    for (int col = 0; col < R; ++col) acc = fma(BmT[static_cast<size_t>(col) * R + r], su[col], acc);
+                    for (int col = 0; col < F6; ++col) acc = fma(BpT[static_cast<size_t>(col) * R + r], st[k * F6 + col], acc);
+                }
+                const int c = r / Np, i = r - c * Np;
+                sgbc_add(A, c * N + e * Np + i, acc);
+            }
+            __syncthreads();
+            continue;
+        }
         for (int w = threadIdx.x; w < nent * Nfp; w += blockDim.x) {
             const int k = w / Nfp, a = w - k * Nfp;
             const int ent = k0 + k;
@@ -215,20 +260,8 @@ __global__ void __launch_bounds__(128) sgbc_flux_kernel(TablesDev T, FluxArgs A)
                 }
             }
             const int64_t base = e * Np + i;
-            const double dt = A.dt;
 #pragma unroll
-            for (int c = 0; c < 6; ++c) {
-                const double ks = (c < 3 ? ie_ : im_) * lf[c];
-                const int64_t o = base + c * N;
-                switch (A.mode) {
-                case MODE_MULT: A.out[o] += ks; break;
-                case MODE_RK4_1: A.yout[o] += 0.5 * dt * ks; A.z[o] += (dt / 6.0) * ks; break;
-                case MODE_RK4_2: A.yout[o] += 0.5 * dt * ks; A.z[o] += (dt / 3.0) * ks; break;
-                case MODE_RK4_3: A.yout[o] += dt * ks; A.z[o] += (dt / 3.0) * ks; break;
-                case MODE_RK4_4: A.x[o] += (dt / 6.0) * ks; break;
-                default: break;
-                }
-            }
+            for (int c = 0; c < 6; ++c) sgbc_add(A, base + c * N, (c < 3 ? ie_ : im_) * lf[c]);
         }
         __syncthreads();
     }
@@ -329,7 +362,7 @@ constexpr int kGridCap = 4 * 152;
 }  // namespace
 
 SgbcOp::SgbcOp(const MeshTables& T, const RefTet& ref, const std::vector<SgbcStackSpec>& stacks,
-               const std::vector<int32_t>& face_stack)
+               const std::vector<int32_t>& face_stack, double alpha)
 {
     if (stacks.empty()) throw std::invalid_argument("SGBC: at least one stack is needed");
     if (static_cast<int>(stacks.size()) > kSgbcMaxStacks)
@@ -355,6 +388,30 @@ SgbcOp::SgbcOp(const MeshTables& T, const RefTet& ref, const std::vector<SgbcSta
         trace_ = zeros<double>(12 * np); flags_ = zeros<int>(8);
         el_elem_ = upload(layout_.el_elem); el_start_ = upload(layout_.el_start);
         ent_face_ = upload(layout_.ent_face); ent_role_ = upload(layout_.ent_role); ent_pairs_ = upload(layout_.ent_pairs);
+        // curved elements' SGBC faces: dense injection blocks, transposed for coalesced reads
+        std::vector<char> curved(T.K, 0);
+        for (int32_t e : T.curved_elems) curved[e] = 1;
+        const int Np = ref.Np, Nfp = ref.Nfp, R = 6 * Np;
+        std::vector<int64_t> ent_cblk(layout_.ent_face.size(), -1);
+        std::vector<double> cblk, Bm, Bp;
+        for (size_t i = 0; i < layout_.el_elem.size(); ++i) {
+            const int64_t e = layout_.el_elem[i];
+            if (!curved[e]) continue;
+            for (int32_t k = layout_.el_start[i]; k < layout_.el_start[i + 1]; ++k) {
+                build_curved_sgbc_face(T, ref, alpha, e, layout_.ent_face[k], Bm, Bp);
+                ent_cblk[k] = static_cast<int64_t>(cblk.size());
+                const size_t o = cblk.size();
+                cblk.resize(o + static_cast<size_t>(R) * R + static_cast<size_t>(6 * Nfp) * R);
+                for (int r = 0; r < R; ++r)
+                    for (int c = 0; c < R; ++c) cblk[o + static_cast<size_t>(c) * R + r] = Bm[static_cast<size_t>(r) * R + c];
+                const size_t op = o + static_cast<size_t>(R) * R;
+                for (int r = 0; r < R; ++r)
+                    for (int c = 0; c < 6 * Nfp; ++c) cblk[op + static_cast<size_t>(c) * R + r] = Bp[static_cast<size_t>(r) * 6 * Nfp + c];
+            }
+        }
+        ent_cblk_ = upload(ent_cblk);
+        cblk_ = upload(cblk);
+        flux_shmem_ = static_cast<size_t>(std::max(4 * Nfp * 6, 6 * Np + 4 * 6 * Nfp)) * sizeof(double);
     } catch (...) {
         release();
         throw;
@@ -368,11 +425,12 @@ void SgbcOp::release()
     for (auto& kv : maps_) cudaFree(kv.second.a);
     maps_.clear();
     void* bufs[] = {gl_, gr_, pstack_, rot_, xoff_, X_[0], X_[1], snorm_[0], snorm_[1], gold_, gnew_, trace_, flags_,
-                    el_elem_, el_start_, ent_face_, ent_role_, ent_pairs_};
+                    el_elem_, el_start_, ent_face_, ent_role_, ent_pairs_, ent_cblk_, cblk_};
     for (void* b : bufs) if (b) cudaFree(b);
     gl_ = gr_ = pstack_ = nullptr; rot_ = nullptr; xoff_ = nullptr;
     X_[0] = X_[1] = snorm_[0] = snorm_[1] = gold_ = gnew_ = trace_ = nullptr;
     flags_ = nullptr; el_elem_ = el_start_ = ent_face_ = ent_role_ = ent_pairs_ = nullptr;
+    ent_cblk_ = nullptr; cblk_ = nullptr;
 }
 
 // Called before the maps of one launch are looked up (never between two look-ups of a launch, whose
@@ -505,8 +563,9 @@ void SgbcOp::after_stage(const TablesDev& T, const StageArgs& A, cudaStream_t s)
     F.in = A.in; F.trace = trace_; F.flag = flags_ + cur_flag_;
     F.n_elems = static_cast<int64_t>(layout_.el_elem.size());
     F.el_elem = el_elem_; F.el_start = el_start_; F.ent_face = ent_face_; F.ent_role = ent_role_; F.ent_pairs = ent_pairs_;
+    F.ent_cblk = ent_cblk_; F.cblk = cblk_;
     F.mode = A.mode; F.dt = A.dt; F.out = A.out; F.yout = A.yout; F.z = A.z; F.x = A.x;
-    const size_t shmem = static_cast<size_t>(4) * T.Nfp * 6 * sizeof(double);
+    const size_t shmem = flux_shmem_;
     const int grid = static_cast<int>(std::min<int64_t>(kGridCap, std::max<int64_t>(1, F.n_elems)));
     sgbc_flux_kernel<<<grid, 128, shmem, s>>>(T, F);
     ckd(cudaGetLastError(), "SGBC flux kernel");

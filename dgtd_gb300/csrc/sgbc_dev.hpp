@@ -19,8 +19,9 @@ constexpr int kSgbcMaxStacks = 16;
 class SgbcOp {
 public:
     // Builds the sub-solvers and the pair layout and allocates the device state (zero fields).
+    // alpha: the operator's upwind coefficient (the injection flux of curved elements' SGBC faces)
     SgbcOp(const MeshTables& T, const RefTet& ref, const std::vector<SgbcStackSpec>& stacks,
-           const std::vector<int32_t>& face_stack);
+           const std::vector<int32_t>& face_stack, double alpha);
     ~SgbcOp();
     SgbcOp(const SgbcOp&) = delete;
     SgbcOp& operator=(const SgbcOp&) = delete;
@@ -81,6 +82,11 @@ private:
     double* trace_ = nullptr;
     int* flags_ = nullptr;   // [8]: per-stage quiescence flags (0 all quiescent), slot 7 finalisation
     int32_t *el_elem_ = nullptr, *el_start_ = nullptr, *ent_face_ = nullptr, *ent_role_ = nullptr, *ent_pairs_ = nullptr;
+    // SGBC faces of curved elements: per entry the offset of its dense injection blocks (Bm then
+    // Bp, transposed) in cblk_, or -1 for a straight element's face
+    int64_t* ent_cblk_ = nullptr;
+    double* cblk_ = nullptr;
+    size_t flux_shmem_ = 0;
     int cur_flag_ = 0;
 };
 

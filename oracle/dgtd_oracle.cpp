@@ -1587,9 +1587,29 @@ static void sgbc_setup(Oracle& O, vector<SgbcStack> stacks, const int32_t* face_
         const int st = face_stack[q];
         if (st < 0 || st >= static_cast<int>(G->stacks.size())) throw std::runtime_error("oracle: SGBC stack index");
         double R[9]; sgbc_rotation(F.n, R);
+        const bool curved_face = O.is_curved(F.e1) || O.is_curved(F.e2);
         for (int a = 0; a < O.Nfp; ++a) {
             const int n1 = O.fnodes[F.f1 * O.Nfp + a];
             const int64_t g1 = F.e1 * O.Np + n1;
+            if (curved_face) {
+                // per-node normal on a curved face (computePerDofFaceNormals, SubMesher.cpp:138-194;
+                // here exactly at the node): the face tangents of e1's map there, out of e1
+                static const double rv[4][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+                int l1[3], c = 0;
+                for (int q = 0; q < 4; ++q) if (q != F.f1) l1[c++] = q;
+                double x[3], J[9], tu[3], tv[3], cr[3];
+                geom(O, F.e1, &O.B.nodes[n1 * 3], x, J);
+                for (int r = 0; r < 3; ++r) {
+                    tu[r] = tv[r] = 0.0;
+                    for (int d = 0; d < 3; ++d) {
+                        tu[r] += J[r * 3 + d] * (rv[l1[1]][d] - rv[l1[0]][d]);
+                        tv[r] += J[r * 3 + d] * (rv[l1[2]][d] - rv[l1[0]][d]);
+                    }
+                }
+                cross(tu, tv, cr);
+                if (cr[0] * F.n[0] + cr[1] * F.n[1] + cr[2] * F.n[2] < 0) for (int r = 0; r < 3; ++r) cr[r] = -cr[r];
+                sgbc_rotation(cr, R);
+            }
             int64_t g2 = -1; double best = 1e300;
             for (int b = 0; b < O.Nfp; ++b) {
                 const int64_t c2 = F.e2 * O.Np + O.fnodes[F.f2 * O.Nfp + b];

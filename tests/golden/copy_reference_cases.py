@@ -15,7 +15,7 @@ from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
 CASES = ("3D_PEC", "3D_TFSF", "3D_TFSF_InteriorPEC", "3D_Curved_Element_Test", "3D_SGBC", "3D_Resonant_Cylinder",
-         "3D_Resonant_Sphere")
+         "3D_Resonant_Sphere", "3D_RCS_Sphere_Box_05m_G2")
 
 
 def main() -> None:

@@ -237,3 +237,67 @@ def test_sgbc_refusals(torch_cuda):
     op.step(u, 0.0, 0.01, 2)
     torch.cuda.synchronize()
     assert torch.count_nonzero(u).item() == 0   # zero fields stay zero
+
+
+def _curved_sheet_mesh(code):
+    from conftest import curved_box, plane_faces
+    m, Vc, E, els, nodes = curved_box(mode="all", bump=0.03)
+    F = plane_faces(np.asarray(m.vertices), E, 0.5)
+    mesh = dg.Mesh(Vc, E, np.asarray(m.bdr_faces), np.asarray(m.bdr_codes), np.zeros((0, 3), np.int32), F,
+                   np.full(len(F), code, np.int32), curved_elems=els, curved_nodes=nodes)
+    return mesh, F
+
+
+def test_sgbc_on_a_curved_sheet_matches_oracle(torch_cuda):
+    """Every element curved, the layer on the bent sheet x = 1/2: the curved elements' injection
+    blocks (per-point normals) and the pairs' per-node rotations, 40 steps."""
+    mesh, F = _curved_sheet_mesh(dg.BC_SGBC)
+    op = dg.Operator(mesh, order=2)
+    op.set_sgbc([LOSSY], np.zeros(len(F), np.int32))
+    orc = po.Oracle(mesh.vertices, mesh.elements, 2, 1.0, 3, mesh.bdr_faces, mesh.bdr_codes, None, F,
+                    np.full(len(F), 4, np.int32))
+    orc.set_curved(mesh.curved_elems, mesh.curved_nodes)
+    orc.set_sgbc([LOSSY], np.zeros(len(F), np.int32))
+    x0 = _bump(orc.nodes(), 0.5)
+    x, n = op.run_host(x0, 0.0, 0.005, 0.2)
+    xo, no = orc.run(x0, 0.0, 0.005, 0.2)
+    assert n == no == 40 and rel_l2(x, xo) <= 1e-10
+
+
+def test_pec_closed_stack_on_a_curved_sheet_is_a_pec_sheet(torch_cuda):
+    closed = {"layers": [{"eps": 3.0, "sigma": 2.0, "width": 0.05, "segments": 2, "order": 2}],
+              "left": 1, "right": 1, "sub_dt": 0.004}
+    mesh, F = _curved_sheet_mesh(dg.BC_SGBC)
+    layer = dg.Operator(mesh, order=2)
+    layer.set_sgbc([closed], np.zeros(len(F), np.int32))
+    sheet = dg.Operator(_curved_sheet_mesh(dg.BC_PEC)[0], order=2)
+    x0 = _bump(layer.node_coords(), 0.5)
+    a, _ = sheet.run_host(x0, 0.0, 0.005, 0.2)
+    b, _ = layer.run_host(x0, 0.0, 0.005, 0.2)
+    assert np.linalg.norm(a) > 1.0 and rel_l2(b, a) <= 1e-12
+
+
+def test_reference_curved_sgbc_sphere_matches_oracle(torch_cuda):
+    """The reference's 3D_RCS_Sphere_Box_05m_G2: an SGBC layer on a curved sphere of radius 0.5
+    (9,103 tetrahedra, 724 curved, 62 SGBC faces), a pulse started on the sphere; 20 steps of the
+    case's estimated dt."""
+    d = Path(__file__).resolve().parent / "golden" / "cases" / "reference" / "3D_RCS_Sphere_Box_05m_G2"
+    c = dg.Case(d / "3D_RCS_Sphere_Box_05m_G2.json")
+    mesh = c.mesh()
+    stacks, fs = c.sgbc()
+    assert len(mesh.curved_elems) == 724 and len(fs) == 62
+    op = dg.Operator(mesh, order=c.info["order"], alpha=c.info["alpha"])
+    op.set_sgbc(stacks, fs)
+    orc = po.Oracle.from_mesh(mesh, c.info["order"], alpha=c.info["alpha"])
+    orc.set_curved(mesh.curved_elems, mesh.curved_nodes)
+    orc.set_sgbc(stacks, fs)
+    X = orc.nodes()
+    N = X.shape[1]
+    x0 = np.zeros(6 * N)
+    g = np.exp(-np.sum((X - np.array([[0.5], [0.0], [0.0]])) ** 2, axis=0) / (2 * 0.1 ** 2))
+    x0[N:2 * N] = g
+    x0[5 * N:6 * N] = g
+    dt = c.auto_dt()
+    x, n = op.run_host(x0, 0.0, dt, 20 * dt)
+    xo, no = orc.run(x0, 0.0, dt, 20 * dt)
+    assert n == no and np.linalg.norm(xo) > 0.1 and rel_l2(x, xo) <= 1e-10

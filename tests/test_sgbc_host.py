@@ -255,3 +255,21 @@ def test_sgbc_on_the_domain_boundary_and_operator_rules(tmp_path):
         c["solver_options"]["evolution_operator"] = "hesthaven"
     with pytest.raises(dg.DgtdError, match="evolution_operator 'global' only"):
         dg.Case(_ref_sgbc_copy(tmp_path, "hest", hesthaven))
+
+
+def test_oracle_pec_closed_stack_on_a_curved_sheet_is_a_pec_sheet():
+    """The same identity on a curved sheet (every element curved, the sheet x = 1/2 bent by the
+    map): per-point normals in the injection's face integrals and per-node normals in the pairs'
+    rotations."""
+    from conftest import curved_box, plane_faces
+    m, Vc, E, els, nodes = curved_box(mode="all", bump=0.03)
+    F = plane_faces(np.asarray(m.vertices), E, 0.5)
+    mk = lambda code: po.Oracle(Vc, E, 2, 1.0, 3, m.bdr_faces, m.bdr_codes, None, F, np.full(len(F), code, np.int32))
+    sheet, layer = mk(1), mk(4)
+    for o in (sheet, layer):
+        o.set_curved(els, nodes)
+    layer.set_sgbc([{"layers": [{"eps": 3.0, "sigma": 2.0, "width": 0.05, "segments": 2, "order": 2}],
+                     "left": 1, "right": 1, "sub_dt": 0.004}], np.zeros(len(F), np.int32))
+    u0 = _bump(sheet, 0.5)
+    a, b = sheet.step(u0, 0.0, 0.005, 40), layer.step(u0, 0.0, 0.005, 40)
+    assert np.linalg.norm(a) > 1.0 and rel_l2(b, a) <= 1e-12

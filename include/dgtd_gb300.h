@@ -78,7 +78,7 @@ typedef struct dgtd_mesh_desc {
     /* second-order (curved) elements: their ids and geometry nodes [n_curved][10][3] = the
      * element's four corners (its vertex order) then the nodes on its edges (0,1) (0,2) (0,3)
      * (1,2) (1,3) (2,3). They are assembled on their isoparametric map (FP64 form only; no TF/SF
-     * or SGBC faces on them). n_curved = 0 for affine meshes. */
+     * faces on them). n_curved = 0 for affine meshes. */
     int64_t n_curved;
     const int32_t* curved_elems;
     const double* curved_nodes;
@@ -404,8 +404,8 @@ int dgtd_op_probe_read(dgtd_op* op, double* h_point_dft, double* h_surface_dft, 
  * boundaries}, sources {initial, planewave}, probes {point, rcssurface, farfield})
  * loaded into this library's tables, with SGBC layers (dgtd_case_sgbc) and curved second-order
  * tetrahedra (their geometry in dgtd_case_mesh; refinement keeps children on the parent's map).
- * Unsupported features (dipoles, 1D/2D meshes, SGBC faces on curved elements) are rejected with
- * an error. */
+ * Unsupported features (dipoles, 1D/2D meshes, TF/SF faces on curved elements) are rejected
+ * with an error. */
 typedef struct dgtd_case dgtd_case;
 
 typedef struct dgtd_case_info {

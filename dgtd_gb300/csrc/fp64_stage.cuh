@@ -24,6 +24,7 @@
 // the FP64 pipe fed (shared-memory broadcast of the element's fields,
 // coalesced transposed operator rows from L1/L2) rather than to save bytes.
 #pragma once
+#include <type_traits>
 #include <cmath>
 
 #include "kernels.hpp"
@@ -245,7 +246,8 @@ __device__ __forceinline__ void stage_body(const TablesT<R>& T, const StageArgsT
     if (tid >= nel * Np) return;
     const int el = tid / Np, i = tid - el * Np;
     const int64_t e = e0 + el;
-    if (T.curved != nullptr && T.curved[e]) return;   // rows from the curved-element kernel
+    if constexpr (std::is_same<R, double>::value)      // curved elements exist on the FP64 form only
+        if (T.curved != nullptr && T.curved[e]) return;   // rows from the curved-element kernel
     R ar[6], as[6], at[6];
 #pragma unroll
     for (int c = 0; c < 6; ++c) { ar[c] = R(0); as[c] = R(0); at[c] = R(0); }

@@ -14,6 +14,15 @@ def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
 
 
+# Modules whose GPU paths are the newest (thin layers, curved elements) run after the others, so
+# that with -x a failure there does not keep the rest of the suite from running.
+RUN_LAST = ("test_gpu_sgbc.py", "test_gpu_curved.py")
+
+
+def pytest_collection_modifyitems(session, config, items):
+    items.sort(key=lambda it: 1 if Path(str(it.fspath)).name in RUN_LAST else 0)
+
+
 def _ensure_built():
     from dgtd_gb300 import build as pkg_build
     from oracle import pyoracle

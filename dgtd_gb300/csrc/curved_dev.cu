@@ -91,6 +91,14 @@ CurvedOp::CurvedOp(const MeshTables& T, const RefTet& ref, double alpha)
     const CurvedRows C = build_curved_rows(T, ref, alpha);
     Np_ = C.Np;
     n_ = static_cast<int64_t>(C.elems.size());
+    // every index the kernel follows, checked once here
+    if (static_cast<int64_t>(C.nbr.size()) != 4 * n_ ||
+        static_cast<int64_t>(C.blocks.size()) != n_ * 5 * 36 * static_cast<int64_t>(Np_) * Np_ || Np_ != T.Np)
+        throw std::runtime_error("curved rows: inconsistent tables");
+    for (int32_t e : C.elems)
+        if (e < 0 || e >= T.K) throw std::runtime_error("curved rows: element out of range");
+    for (int32_t e : C.nbr)
+        if (e < -1 || e >= T.K) throw std::runtime_error("curved rows: neighbour out of range");
     const int64_t R = 6 * static_cast<int64_t>(Np_);
     std::vector<double> bt(C.blocks.size());
     for (int64_t b = 0; b < 5 * n_; ++b)

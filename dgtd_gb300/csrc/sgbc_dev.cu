@@ -377,6 +377,24 @@ SgbcOp::SgbcOp(const MeshTables& T, const RefTet& ref, const std::vector<SgbcSta
     }
     state_len_ = off;
     const size_t np = layout_.gl.size();
+    // every index the kernels follow, checked once here
+    const int64_t Ntot = T.K * static_cast<int64_t>(T.Np);
+    for (size_t p = 0; p < np; ++p)
+        if (layout_.gl[p] < 0 || layout_.gl[p] >= Ntot || layout_.gr[p] < 0 || layout_.gr[p] >= Ntot ||
+            layout_.stack[p] < 0 || layout_.stack[p] >= static_cast<int32_t>(stacks_.size()))
+            throw std::runtime_error("SGBC layout: pair index out of range");
+    if (layout_.el_start.size() != layout_.el_elem.size() + 1 || layout_.el_start.back() != static_cast<int32_t>(layout_.ent_face.size()) ||
+        layout_.ent_pairs.size() != layout_.ent_face.size() * static_cast<size_t>(T.Nfp))
+        throw std::runtime_error("SGBC layout: inconsistent entry tables");
+    for (size_t i = 0; i < layout_.el_elem.size(); ++i)
+        if (layout_.el_elem[i] < 0 || layout_.el_elem[i] >= T.K || layout_.el_start[i + 1] - layout_.el_start[i] < 1 ||
+            layout_.el_start[i + 1] - layout_.el_start[i] > 4)
+            throw std::runtime_error("SGBC layout: element entry out of range");
+    for (size_t k = 0; k < layout_.ent_face.size(); ++k)
+        if (layout_.ent_face[k] < 0 || layout_.ent_face[k] > 3 || layout_.ent_role[k] < 0 || layout_.ent_role[k] > 1)
+            throw std::runtime_error("SGBC layout: face entry out of range");
+    for (int32_t q : layout_.ent_pairs)
+        if (q < 0 || q >= static_cast<int32_t>(np)) throw std::runtime_error("SGBC layout: entry pair out of range");
     try {
         gl_ = upload(layout_.gl); gr_ = upload(layout_.gr); pstack_ = upload(layout_.stack);
         rot_ = upload(layout_.rot); xoff_ = upload(xoff);

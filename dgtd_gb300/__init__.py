@@ -90,7 +90,7 @@ class CaseInfo(C.Structure):
                 ("final_time", C.c_double), ("cfl", C.c_double), ("n_waves", C.c_int32),
                 ("n_initial_fields", C.c_int32), ("n_point_probes", C.c_int32), ("n_surfaces", C.c_int32),
                 ("n_elements", C.c_int64), ("n_vertices", C.c_int64), ("n_sgbc_stacks", C.c_int32),
-                ("n_sgbc_layers", C.c_int32), ("n_sgbc_faces", C.c_int64)]
+                ("n_sgbc_layers", C.c_int32), ("n_sgbc_faces", C.c_int64), ("basis_type", C.c_int32)]
 
 
 class CaseRunOpts(C.Structure):
@@ -183,6 +183,8 @@ SIGNATURES = {
     "dgtd_sgbc_stack_operator": (C.c_int, [C.POINTER(SgbcStack), _I64, _I64, _I64, _D, C.c_int64]),
     "dgtd_sgbc_stack_maps": (C.c_int, [C.POINTER(SgbcStack), C.c_double, C.c_int32, _D, _D, _D, _D, _D]),
     "dgtd_curved_block_rows": (C.c_int, [C.POINTER(MeshDesc), C.c_int32, C.c_double, _I32, _I32, _D, C.c_int64]),
+    "dgtd_tet_nodes": (C.c_int, [C.c_int32, C.c_int32, _D]),
+    "dgtd_tet_basis_change": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, _D]),
     "dgtd_op_clear_probes": (C.c_int, [_P]),
     "dgtd_op_probe_reset": (C.c_int, [_P, _P]),
     "dgtd_op_probe_info": (C.c_int, [_P, _I64, _I64, _I64]),
@@ -431,6 +433,26 @@ def curved_block_rows(mesh: Mesh, order: int, alpha: float = 1.0) -> dict:
     B = np.zeros((n, 5, 6 * Np, 6 * Np))
     _check(lib().dgtd_curved_block_rows(C.byref(d), order, alpha, _ip(el), _ip(nb), _dp(B), B.size), "curved_block_rows")
     return {"elems": el, "nbr": nb, "blocks": B}
+
+
+BASIS_GAUSS_LEGENDRE, BASIS_GAUSS_LOBATTO = 0, 1
+
+
+def tet_nodes(order: int, basis_type: int = BASIS_GAUSS_LOBATTO) -> np.ndarray:
+    """Barycentric coordinates [Np, 4] of the order-p tetrahedron's nodes of an MFEM basis type
+    (1 Gauss-Lobatto: the operator's node set; 0 Gauss-Legendre), in DOF order."""
+    Np = (order + 1) * (order + 2) * (order + 3) // 6
+    out = np.zeros((Np, 4))
+    _check(lib().dgtd_tet_nodes(order, basis_type, _dp(out)), "dgtd_tet_nodes")
+    return out
+
+
+def tet_basis_change(order: int, from_basis: int, to_basis: int) -> np.ndarray:
+    """[Np, Np] matrix M with v_to = M v_from for the nodal values of a degree-p polynomial."""
+    Np = (order + 1) * (order + 2) * (order + 3) // 6
+    out = np.zeros((Np, Np))
+    _check(lib().dgtd_tet_basis_change(order, from_basis, to_basis, _dp(out)), "dgtd_tet_basis_change")
+    return out
 
 
 def validate_mesh(mesh: Mesh, order: int = 3, batch: int = 1) -> dict:

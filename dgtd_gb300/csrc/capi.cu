@@ -1400,6 +1400,32 @@ int dgtd_curved_block_rows(const dgtd_mesh_desc* mesh, int32_t order, double alp
     return DGTD_OK;
 }
 
+int dgtd_tet_nodes(int32_t order, int32_t basis_type, double* bary)
+{
+    if (!bary) return fail(DGTD_ERR_INVALID, "NULL argument");
+    if (order < 1 || order > 6) return fail(DGTD_ERR_UNSUPPORTED, "order must be in [1, 6]");
+    try {
+        const std::vector<double> b = dgtd::tet_node_bary(order, basis_type);
+        std::copy(b.begin(), b.end(), bary);
+    } catch (const std::exception& e) {
+        return fail(DGTD_ERR_INVALID, e.what());
+    }
+    return DGTD_OK;
+}
+
+int dgtd_tet_basis_change(int32_t order, int32_t from_basis, int32_t to_basis, double* m)
+{
+    if (!m) return fail(DGTD_ERR_INVALID, "NULL argument");
+    if (order < 1 || order > 6) return fail(DGTD_ERR_UNSUPPORTED, "order must be in [1, 6]");
+    try {
+        const std::vector<double> M = dgtd::tet_basis_change(order, from_basis, to_basis);
+        std::copy(M.begin(), M.end(), m);
+    } catch (const std::exception& e) {
+        return fail(DGTD_ERR_INVALID, e.what());
+    }
+    return DGTD_OK;
+}
+
 int dgtd_mesh_validate(const dgtd_mesh_desc* mesh, const dgtd_op_opts* opts, dgtd_op_info* info)
 {
     if (!opts || !info) return fail(DGTD_ERR_INVALID, "NULL argument");

@@ -13,6 +13,7 @@
 #include "../../include/dgtd_gb300.h"
 #include "jsoncase.hpp"
 #include "mesh.hpp"
+#include "refelem.hpp"
 
 namespace dgtd {
 int set_last_error(int code, const std::string& msg);   // capi.cu
@@ -78,6 +79,7 @@ int dgtd_case_get_info(const dgtd_case* cs, dgtd_case_info* info)
     for (const auto& st : c.sgbc_stacks) nl += static_cast<int32_t>(st.layers.size());
     info->n_sgbc_layers = nl;
     info->n_sgbc_faces = static_cast<int64_t>(c.sgbc_face_stack.size());
+    info->basis_type = c.basis_type;
     return DGTD_OK;
 }
 
@@ -227,7 +229,40 @@ int dgtd_case_run(const dgtd_case* cs, const dgtd_case_run_opts* ro, double* h_s
         const int64_t N = info.ndofs;
         std::vector<double> xyz(3 * N);
         ok(dgtd_op_node_coords(op, xyz.data()), "node_coords");
+        // a Gauss-Legendre case: its initial fields are interpolated at its own nodes (straight
+        // elements: the affine image of the node set), then moved to the operator's node set
+        const bool legendre = c.basis_type == dgtd::kBasisGaussLegendre;
+        const int64_t K = info.n_elements;
+        const int Np = info.np;
+        std::vector<double> to_lobatto, to_legendre;
+        if (legendre) {
+            const std::vector<double> b = dgtd::tet_node_bary(c.order, dgtd::kBasisGaussLegendre);
+            for (int64_t e = 0; e < K; ++e)
+                for (int n = 0; n < Np; ++n)
+                    for (int r = 0; r < 3; ++r) {
+                        double x = 0.0;
+                        for (int v = 0; v < 4; ++v)
+                            x += b[4 * n + v] * c.vertices[3 * static_cast<size_t>(c.elements[4 * e + v]) + r];
+                        xyz[r * N + e * Np + n] = x;
+                    }
+            to_lobatto = dgtd::tet_basis_change(c.order, dgtd::kBasisGaussLegendre, dgtd::kBasisGaussLobatto);
+            to_legendre = dgtd::tet_basis_change(c.order, dgtd::kBasisGaussLobatto, dgtd::kBasisGaussLegendre);
+        }
+        // element-block change of nodal basis of all six components, in place
+        auto change_basis = [&](std::vector<double>& v, const std::vector<double>& M) {
+            std::vector<double> tmp(Np);
+            for (int64_t blk = 0; blk < 6 * K; ++blk) {
+                double* x = &v[static_cast<size_t>(blk) * Np];
+                for (int i = 0; i < Np; ++i) {
+                    double a = 0.0;
+                    for (int j = 0; j < Np; ++j) a += M[static_cast<size_t>(i) * Np + j] * x[j];
+                    tmp[i] = a;
+                }
+                std::copy(tmp.begin(), tmp.end(), x);
+            }
+        };
         std::vector<double> u = dgtd::case_initial_state(c, xyz.data(), N);
+        if (legendre) change_basis(u, to_lobatto);
 
         // probes: points at the smallest requested interval, all surfaces in one set
         const int32_t npts = static_cast<int32_t>(c.point_pos.size() / 3);
@@ -280,6 +315,11 @@ int dgtd_case_run(const dgtd_case* cs, const dgtd_case_run_opts* ro, double* h_s
         const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         if (h_state && cudaMemcpy(h_state, d, bytes, cudaMemcpyDeviceToHost) != cudaSuccess)
             throw std::runtime_error("D2H failed");
+        if (h_state && legendre) {
+            std::vector<double> v(h_state, h_state + u.size());
+            change_basis(v, to_legendre);
+            std::copy(v.begin(), v.end(), h_state);
+        }
         int64_t nrec = 0;
         if (probes) {
             ok(dgtd_op_probe_info(op, nullptr, nullptr, &nrec), "probe_info");

@@ -646,11 +646,15 @@ Case load_case(const std::string& json_path)
         }
         if (const Json* v = so->find("basis_type")) {
             // MFEM's BasisType numbering (SolverOptions.h:74-77; 0 Gauss-Legendre, 1 Gauss-Lobatto,
-            // 2 positive/Bernstein, ...): the operator is built on the Gauss-Lobatto node set only
+            // 2 positive/Bernstein, ...). The operator runs on the Gauss-Lobatto node set; a
+            // Gauss-Legendre case is the same polynomial space, whose state the runner maps to and
+            // from that node set (the reference's integration rules are exact on straight elements,
+            // so both bases give the same semi-discrete system)
             const int bt = v->integer();
-            if (bt != 1)
+            if (bt != 0 && bt != 1)
                 throw std::runtime_error("basis_type " + std::to_string(bt) +
-                                         " is not supported (the Gauss-Lobatto nodal basis, basis_type 1, is)");
+                                         " is not supported (Gauss-Legendre, 0, and Gauss-Lobatto, 1, are)");
+            c.basis_type = bt;
         }
         if (const Json* v = so->find("ode_type")) {
             if (v->type == Json::String) {   // this library's names (LSERK4 has no number in the reference)
@@ -966,6 +970,20 @@ Case load_case(const std::string& json_path)
     if (!c.sgbc_face_stack.empty() && c.evolution_operator != "global")
         throw std::runtime_error("thin-layer (SGBC) boundaries run with evolution_operator 'global' only "
                                  "(the reference couples them in GlobalEvolution)");
+    if (c.basis_type == 0) {
+        // The change of basis is exact where the operator is basis-free: straight elements
+        // (curved ones integrate non-polynomial terms), no source sampled at the nodes (a plane
+        // wave is interpolated on the case's node set), no face-node sub-solvers (SGBC), and not
+        // the Hesthaven evolution (built on face nodes)
+        if (!c.curved_elems.empty())
+            throw std::runtime_error("basis_type 0 (Gauss-Legendre) with curved elements is not supported");
+        if (!c.waves.empty())
+            throw std::runtime_error("basis_type 0 (Gauss-Legendre) with plane-wave sources is not supported");
+        if (!c.sgbc_face_stack.empty())
+            throw std::runtime_error("basis_type 0 (Gauss-Legendre) with SGBC boundaries is not supported");
+        if (c.evolution_operator == "hesthaven")
+            throw std::runtime_error("basis_type 0 (Gauss-Legendre) with the hesthaven evolution is not supported");
+    }
     return c;
 }
 

@@ -88,6 +88,9 @@ struct Case {
     double cfl = 1.0;
     int integrator = DGTD_RK4;
     std::string evolution_operator = "global";
+    // MFEM BasisType of the case's nodal basis: 1 Gauss-Lobatto (the operator's own node set),
+    // 0 Gauss-Legendre (the same polynomial space; the runner changes basis at the run's ends)
+    int basis_type = 1;
     // mesh
     std::vector<double> vertices;
     std::vector<int32_t> elements;

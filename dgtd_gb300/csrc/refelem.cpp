@@ -343,6 +343,56 @@ void gauss_legendre01(int n, std::vector<double>& x, std::vector<double>& w)
     }
 }
 
+std::vector<double> tet_node_bary(int p, int basis_type)
+{
+    if (p < 1 || p > 10) throw std::runtime_error("tetrahedron order must be in [1, 10]");
+    std::vector<double> g;
+    if (basis_type == kBasisGaussLobatto) {
+        g = gauss_lobatto(p);
+        for (auto& v : g) v = 0.5 * (v + 1.0);
+    } else if (basis_type == kBasisGaussLegendre) {
+        std::vector<double> w;
+        gauss_legendre01(p + 1, g, w);
+        std::sort(g.begin(), g.end());
+    } else {
+        throw std::runtime_error("basis_type must be 0 (Gauss-Legendre) or 1 (Gauss-Lobatto)");
+    }
+    std::vector<double> b;
+    b.reserve(4 * tet_np(p));
+    for (int k = 0; k <= p; ++k)
+        for (int j = 0; j + k <= p; ++j)
+            for (int i = 0; i + j + k <= p; ++i) {
+                const int l = p - i - j - k;
+                const double w = g[i] + g[j] + g[k] + g[l];
+                b.insert(b.end(), {g[l] / w, g[i] / w, g[j] / w, g[k] / w});
+            }
+    return b;
+}
+
+std::vector<double> tet_basis_change(int p, int from_basis, int to_basis)
+{
+    // M = V_to V_from^-1 with V[n][m] the orthonormal modes at the nodes
+    const int Np = tet_np(p);
+    auto vander = [&](int basis) {
+        const std::vector<double> b = tet_node_bary(p, basis);
+        std::vector<double> V(static_cast<size_t>(Np) * Np);
+        int m = 0;
+        for (int i = 0; i <= p; ++i)
+            for (int j = 0; i + j <= p; ++j)
+                for (int k = 0; i + j + k <= p; ++k) {
+                    for (int n = 0; n < Np; ++n)
+                        V[n * Np + m] = simplex3d(2.0 * b[4 * n + 1] - 1.0, 2.0 * b[4 * n + 2] - 1.0,
+                                                  2.0 * b[4 * n + 3] - 1.0, i, j, k);
+                    ++m;
+                }
+        return V;
+    };
+    std::vector<double> Vf = vander(from_basis), Vt = vander(to_basis), M(static_cast<size_t>(Np) * Np);
+    if (!invert_matrix(Vf, Np)) throw std::runtime_error("singular tet Vandermonde");
+    matmul(Vt.data(), Vf.data(), M.data(), Np, Np, Np);
+    return M;
+}
+
 RefSeg build_ref_seg(int p)
 {
     if (p < 1 || p > 16) throw std::runtime_error("segment order must be in [1, 16]");

@@ -60,6 +60,18 @@ void nodal_basis_grad_at(const RefTet& T, double r, double s, double t, double* 
 void gauss_legendre01(int n, std::vector<double>& x, std::vector<double>& w);
 RefSeg build_ref_seg(int p);
 
+// MFEM basis types of the tetrahedron's L2 node sets (the reference's solver_options.basis_type):
+// the operator runs on the Gauss-Lobatto set; the Gauss-Legendre set (L2_FECollection(p, 3,
+// BasisType::GaussLegendre)) is the same barycentric blend of the p + 1 Gauss-Legendre points of
+// (0, 1), enumerated in the same order, with no node on a face.
+constexpr int kBasisGaussLegendre = 0;
+constexpr int kBasisGaussLobatto = 1;
+// Barycentric coordinates [Np][4] (l0, l1, l2, l3) of the order-p nodes of that set.
+std::vector<double> tet_node_bary(int p, int basis_type);
+// Change of nodal basis on the order-p tetrahedron, [Np][Np] row-major: v_to = M v_from for the
+// nodal values of any polynomial of degree p (M[i][j] = phi^from_j at node i of `to`).
+std::vector<double> tet_basis_change(int p, int from_basis, int to_basis);
+
 inline int tet_np(int p) { return (p + 1) * (p + 2) * (p + 3) / 6; }
 inline int tri_np(int p) { return (p + 1) * (p + 2) / 2; }
 

@@ -365,6 +365,21 @@ int dgtd_op_sgbc_finalize(dgtd_op* op, const void* d_x, void* stream);
  * `cap` entries) receives the pairs' states, pair after pair. */
 int dgtd_op_sgbc_states(const dgtd_op* op, int64_t* n_pairs, int64_t* state_len, double* h_states, int64_t cap);
 
+/* Node sets of the order-p tetrahedron (no GPU). The operator's state holds nodal values on MFEM's
+ * Gauss-Lobatto L2 node set; the reference's solver_options.basis_type 0 selects MFEM's
+ * Gauss-Legendre set of the same polynomial space (L2_FECollection(p, 3, BasisType::GaussLegendre),
+ * Solver.cpp:86). The reference's integration rules are exact on straight elements (faces: order
+ * 2p + 1, IntegratorFunctions.cpp:7-35; volume: 2p - 1 and 2p), so its operator in either basis is
+ * the same semi-discrete system: A_legendre = M(lobatto -> legendre) A M(legendre -> lobatto),
+ * element by element. */
+#define DGTD_BASIS_GAUSS_LEGENDRE 0
+#define DGTD_BASIS_GAUSS_LOBATTO 1
+/* Barycentric coordinates [Np][4] (l0..l3, on the element's vertices 0..3) of the nodes of a
+ * basis type, in DOF order. */
+int dgtd_tet_nodes(int32_t order, int32_t basis_type, double* bary);
+/* [Np][Np] row-major M with v_to = M v_from for the nodal values of any degree-p polynomial. */
+int dgtd_tet_basis_change(int32_t order, int32_t from_basis, int32_t to_basis, double* m);
+
 /* Host-side rows of the curved elements of a mesh (no GPU): elems [n_curved], nbr [n_curved][4]
  * (face neighbour or -1) and blocks [n_curved][5][6 Np][6 Np] (row-major; rows (component, node)
  * of dU/dt, columns (component, node) of the element's own state, block 0, or of its neighbour
@@ -424,6 +439,10 @@ typedef struct dgtd_case_info {
     int32_t n_sgbc_stacks;       /* "SGBC" boundary entries (dgtd_case_sgbc) */
     int32_t n_sgbc_layers;       /* layers over all stacks */
     int64_t n_sgbc_faces;        /* interior faces given with DGTD_BC_SGBC in the case mesh */
+    int32_t basis_type;          /* solver_options.basis_type: DGTD_BASIS_GAUSS_LOBATTO (default) or
+                                    DGTD_BASIS_GAUSS_LEGENDRE; dgtd_case_run then takes the initial
+                                    fields at the Gauss-Legendre nodes and returns the final state
+                                    on them (the operator runs on the Gauss-Lobatto set between) */
 } dgtd_case_info;
 
 typedef struct dgtd_case_run_opts {

@@ -140,6 +140,9 @@ struct LU {
 // ---------------------------------------------------------------- element basis
 // Lagrange basis on the GaussLobatto node set of the reference simplex
 // (dim 1: [0,1]; dim 3: tet (0,0,0),(1,0,0),(0,1,0),(0,0,1)), through Bernstein polynomials.
+// With `legendre` the node set is MFEM's GaussLegendre one instead (L2_FECollection(p, 3,
+// BasisType::GaussLegendre), the reference's basis_type 0): the same barycentric blend of the
+// p + 1 Gauss-Legendre points, which puts no node on a face.
 struct Basis {
     // Evaluated in extended precision: the Bernstein-to-Lagrange change of
     // basis is moderately ill-conditioned at p = 6.
@@ -171,11 +174,13 @@ struct Basis {
         for (int d = 0; d < dim; ++d) { lam[d + 1] = xi[d]; s += xi[d]; }
         lam[0] = 1 - s;
     }
-    void init(int dim_, int p_)
+    void init(int dim_, int p_, bool legendre = false)
     {
         dim = dim_; p = p_;
         fact.resize(p + 2); fact[0] = 1; for (int i = 1; i < p + 2; ++i) fact[i] = fact[i - 1] * i;
-        auto g = lobatto01(p);
+        vector<double> g, gw;
+        if (legendre) { gauss_legendre01(p + 1, g, gw); std::sort(g.begin(), g.end()); }
+        else g = lobatto01(p);
         nodes.clear(); bidx.clear();
         if (dim == 1) {
             Np = p + 1;
@@ -336,6 +341,7 @@ struct Oracle {
     double alpha = 1.0;
     int64_t K = 0, N = 0;
     Basis B;
+    bool legendre = false;   // Gauss-Legendre node set (orc_set_basis): no face nodes
     vector<double> verts; vector<int32_t> elems;
     vector<double> eps, mu, sig;
     vector<double> A;      // per element affine map: x = v0 + A xi, A [3][dim]
@@ -1039,6 +1045,7 @@ static void tfsf_apply(Oracle& O, double* y, double t)
 // ---------------------------------------------------------------- (B) nodal
 static void build_nodal(Oracle& O)
 {
+    if (O.legendre) throw std::runtime_error("oracle: the nodal form needs face nodes (Gauss-Lobatto basis)");
     const int Np = O.Np, Nfp = O.Nfp, dim = O.dim, nf = O.nfaces;
     if (!O.sgbc_faces.empty())
         throw std::runtime_error("oracle: thin-layer (SGBC) faces exist in the global form only (GlobalEvolution)");
@@ -1692,6 +1699,30 @@ void* orc_create(int dim, int order, double alpha, int64_t nv, const double* ver
     }
 }
 
+// Switch a fresh 3D oracle to the Gauss-Legendre node set (basis_type 0; 1 keeps Gauss-Lobatto):
+// the global form is assembled by quadrature and holds for either; the nodal form, SGBC and
+// curved elements need the Gauss-Lobatto set's face nodes and are refused afterwards.
+int orc_set_basis(void* h, int basis_type)
+{
+    try {
+        auto* O = static_cast<orc::Oracle*>(h);
+        if (basis_type == 1 && !O->legendre) return 0;
+        if (basis_type != 0) throw std::runtime_error("oracle: basis_type must be 0 or 1 (and set once)");
+        if (O->dim != 3) throw std::runtime_error("oracle: Gauss-Legendre basis in 3D only");
+        if (O->have_csr || O->have_nodal || O->sgbc || !O->cidx.empty())
+            throw std::runtime_error("oracle: set the basis before assembling, SGBC or curved elements");
+        O->B.init(3, O->p, true);
+        O->legendre = true;
+        orc::build_geometry(*O);
+        O->Nfp = 0;
+        O->fnodes.clear();
+        return 0;
+    } catch (const std::exception& e) {
+        g_orc_err = e.what();
+        return -1;
+    }
+}
+
 void orc_destroy(void* h) { delete static_cast<orc::Oracle*>(h); }
 int64_t orc_ndofs(void* h) { return static_cast<orc::Oracle*>(h)->N; }
 int orc_np(void* h) { return static_cast<orc::Oracle*>(h)->Np; }
@@ -1905,6 +1936,7 @@ int orc_set_curved(void* h, int64_t n, const int32_t* elems, const double* nodes
     try {
         auto& O = *static_cast<orc::Oracle*>(h);
         if (O.dim != 3) throw std::runtime_error("oracle: curved elements are 3D");
+        if (O.legendre) throw std::runtime_error("oracle: curved elements with the Gauss-Legendre basis");
         O.cidx.assign(O.K, -1);
         O.cnodes.assign(nodes, nodes + 30 * n);
         for (int64_t i = 0; i < n; ++i) {
@@ -1935,6 +1967,7 @@ int orc_set_sgbc(void* h, int n_stacks, const int32_t* layer_counts, const doubl
 {
     try {
         auto& O = *static_cast<orc::Oracle*>(h);
+        if (O.legendre) throw std::runtime_error("oracle: SGBC needs face nodes (Gauss-Lobatto basis)");
         orc::sgbc_setup(O, orc::sgbc_stacks_from(n_stacks, layer_counts, layer_prm, bcs, sub_dts), face_stack);
     } catch (const std::exception& e) { g_orc_err = e.what(); return -1; }
     return 0;

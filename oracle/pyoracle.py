@@ -63,6 +63,8 @@ def lib() -> C.CDLL:
         h.orc_subop.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, _D]
         h.orc_set_curved.restype = C.c_int
         h.orc_set_curved.argtypes = [C.c_void_p, C.c_int64, _I32, _D]
+        h.orc_set_basis.restype = C.c_int
+        h.orc_set_basis.argtypes = [C.c_void_p, C.c_int]
         h.orc_set_sgbc.restype = C.c_int
         h.orc_set_sgbc.argtypes = [C.c_void_p, C.c_int, _I32, _D, _I32, _D, _I32]
         h.orc_sgbc_pairs.restype = C.c_int64; h.orc_sgbc_pairs.argtypes = [C.c_void_p]
@@ -181,6 +183,11 @@ class Oracle:
         nd = np.ascontiguousarray(nodes, dtype=np.float64).reshape(-1)
         self._keep += [el, nd]
         self._chk(lib().orc_set_curved(self.h, el.size, _i(el), _d(nd)))
+
+    def set_basis(self, basis_type: int) -> None:
+        """MFEM basis type of the node set: 0 Gauss-Legendre, 1 Gauss-Lobatto (the default). Set
+        before the first product; the Gauss-Legendre set runs the global form only."""
+        self._chk(lib().orc_set_basis(self.h, int(basis_type)))
 
     def set_sgbc(self, stacks: Sequence[dict], face_stack) -> None:
         """Thin-layer (SGBC) sub-solvers for the interior faces given with code 4, in their order:

@@ -3,8 +3,9 @@
     python tests/golden/copy_reference_cases.py <reference checkout>
 
 (or with the checkout in the DGTD_REFERENCE environment variable). The files are copied
-byte for byte from testData/maxwellInputs/<case>/ into tests/golden/cases/reference/<case>/,
-so that the tests run the reference's inputs where the reference checkout is absent.
+byte for byte from testData/maxwellInputs/[<group>/]<case>/ into
+tests/golden/cases/reference/<case>/, so that the tests run the reference's inputs where the
+reference checkout is absent.
 """
 from __future__ import annotations
 
@@ -15,7 +16,10 @@ from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
 CASES = ("3D_PEC", "3D_TFSF", "3D_TFSF_InteriorPEC", "3D_Curved_Element_Test", "3D_SGBC", "3D_Resonant_Cylinder",
-         "3D_Resonant_Sphere", "3D_RCS_Sphere_Box_05m_G2")
+         "3D_Resonant_Sphere", "3D_RCS_Sphere_Box_05m_G2",
+         "3D_Resonant_Box_TM55/3D_Resonant_Box_TM55_H1_P3",
+         "Performance/3D_Resonant_Box_TM55_PERF/3D_Resonant_Box_TM55_H0_P2_PERF",
+         "Performance/3D_Resonant_Box_BLEG_TM55_PERF/3D_Resonant_Box_BLEG_TM55_H0_P2_PERF")
 
 
 def main() -> None:
@@ -23,12 +27,13 @@ def main() -> None:
     if not root:
         sys.exit("usage: copy_reference_cases.py <reference checkout>  (or set DGTD_REFERENCE)")
     src = Path(root) / "testData" / "maxwellInputs"
-    for name in CASES:
+    for entry in CASES:
+        name = Path(entry).name
         dst = HERE / "cases" / "reference" / name
         dst.mkdir(parents=True, exist_ok=True)
         for ext in (".json", ".msh"):
-            shutil.copyfile(src / name / f"{name}{ext}", dst / f"{name}{ext}")
-            print(f"{src / name / (name + ext)} -> {dst / (name + ext)}")
+            shutil.copyfile(src / entry / f"{name}{ext}", dst / f"{name}{ext}")
+            print(f"{src / entry / (name + ext)} -> {dst / (name + ext)}")
 
 
 if __name__ == "__main__":

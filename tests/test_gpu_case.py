@@ -4,6 +4,8 @@ Bar: the case runner's final state is bit-identical to the same solve through
 dgtd_op_run_host (same operator, same loop), and within 1e-12 relative L2 of the
 oracle's RK4 loop; point-probe files hold one record per sampled step.
 """
+import json
+import shutil
 from pathlib import Path
 
 import numpy as np
@@ -117,3 +119,79 @@ def test_reference_case_3d_pec_is_unstable_as_given(torch_cuda, tmp_path):
     op.step(xd, 0.0, inf["time_step"], 5)
     torch.cuda.synchronize()
     assert rel_l2(xd.cpu().numpy(), orc.step(x0, 0.0, inf["time_step"], 5, form=po.NODAL)) <= 1e-12
+
+
+TM55 = REFERENCE_CASES / "3D_Resonant_Box_TM55_H1_P3" / "3D_Resonant_Box_TM55_H1_P3.json"
+TM55_W = 5 * np.pi * np.sqrt(2.0)
+
+
+def _tm55_case(tmp_path, refinement):
+    """The H1_P3 input with its refinement level changed (the reference's H<k> inputs differ in
+    nothing else but the order), in a folder named as the case."""
+    if refinement == 1:
+        return dg.Case(TM55)
+    name = f"3D_Resonant_Box_TM55_H{refinement}"
+    d = tmp_path / name
+    d.mkdir()
+    js = json.loads(TM55.read_text())
+    js["model"]["refinement"] = refinement
+    js["model"]["filename"] = f"{name}.msh"
+    (d / f"{name}.json").write_text(json.dumps(js))
+    shutil.copyfile(TM55.with_suffix(".msh"), d / f"{name}.msh")
+    return dg.Case(d / f"{name}.json")
+
+
+@pytest.mark.parametrize("refinement,order,bar", [(1, 2, 0.22), (1, 3, 0.09), (2, 2, 0.045)])
+def test_reference_tm55_mode_converges(torch_cuda, tmp_path, refinement, order, bar):
+    """The reference's TM55 resonant box (the unit PEC cube of 350 tetrahedra, refined once, H1,
+    or twice, H2) started on the TM(5,5) mode Ez = sin(5 pi x) sin(5 pi y) follows Ez cos(w t),
+    Hx = -(5 pi / w) sin(5 pi x) cos(5 pi y) sin(w t), Hy = (5 pi / w) cos(5 pi x) sin(5 pi y)
+    sin(w t), w = 5 pi sqrt(2) (test/cases/L2ErrorAnalysis.cpp:32-54) over one period of 200
+    steps. The bars are the oracle's own errors at the node set (H1: 0.214 at order 2, 0.083 at
+    order 3; H2 order 2: 0.043, five times below H1), so they pin the discretisation, and the first
+    20 steps match the oracle to 1e-12."""
+    case = _tm55_case(tmp_path, refinement)
+    m = case.mesh()
+    assert m.n_elements == 350 * 8 ** refinement
+    op = dg.Operator(m, order=order, alpha=case.info["alpha"])
+    X = op.node_coords()
+    N = X.shape[1]
+    x0 = case.initial_state(X)
+    period = 2 * np.pi / TM55_W
+    dt = period / 200
+    orc = po.Oracle.from_mesh(m, order, alpha=case.info["alpha"])
+    x20, n20 = op.run_host(x0, 0.0, dt, 20 * dt)
+    assert n20 == 20 and rel_l2(x20, orc.run(x0, 0.0, dt, 20 * dt)[0]) <= 1e-12
+    x, n = op.run_host(x0, 0.0, dt, period)
+    assert n == 200
+    sx, cx = np.sin(5 * np.pi * X[0]), np.cos(5 * np.pi * X[0])
+    sy, cy = np.sin(5 * np.pi * X[1]), np.cos(5 * np.pi * X[1])
+    ez = sx * sy
+    assert np.linalg.norm(x[2 * N:3 * N] - ez * np.cos(TM55_W * period)) / np.linalg.norm(ez) <= bar
+    amp = 5 * np.pi / TM55_W
+    hx = -amp * sx * cy * np.sin(TM55_W * period)
+    hy = amp * cx * sy * np.sin(TM55_W * period)
+    # sin(w T) = 0 after one period: the magnetic field is back to zero up to the same error
+    assert np.linalg.norm(x[3 * N:4 * N] - hx) / np.linalg.norm(ez) <= bar
+    assert np.linalg.norm(x[4 * N:5 * N] - hy) / np.linalg.norm(ez) <= bar
+
+
+def test_reference_tm55_performance_case_runs(torch_cuda, tmp_path):
+    """The reference's Performance input 3D_Resonant_Box_TM55_H0_P2_PERF (350 tetrahedra, order 2,
+    dt 1e-4 to t = 2: 20,000 steps) runs end to end through dgtd_case_run: the step count, no
+    instability, one record per sampled step in both probe files, their Ez varying,
+    and the field decaying as the upwind flux damps the under-resolved mode."""
+    name = "3D_Resonant_Box_TM55_H0_P2_PERF"
+    case = dg.Case(REFERENCE_CASES / name / f"{name}.json")
+    state, res = case.run(out_dir=tmp_path)
+    assert res["steps"] == 20000 and res["unstable_step"] == -1 and np.all(np.isfinite(state))
+    files = sorted(tmp_path.glob("PointProbe*.dat"))
+    assert len(files) == 2
+    for f in files:
+        rows = read_point_probe(f)
+        assert rows.shape == (res["n_records"], 7) and np.all(np.isfinite(rows))
+        assert np.ptp(rows[:, 3]) > 0.1
+    # Five half-wavelengths on seven elements per side at order 2 are under-resolved, and the
+    # upwind flux takes about two thirds of the nodal norm by t = 2 (the oracle: 0.35 of it).
+    x0 = case.initial_state(dg.Operator(case.mesh(), order=2).node_coords())
+    assert 0.2 < np.linalg.norm(state) / np.linalg.norm(x0) < 0.5

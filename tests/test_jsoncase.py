@@ -159,13 +159,38 @@ def test_case_naming_style(tmp_path):
         dg.Case(d / "DriverStyleCheckMismatch.json")
 
 
-@pytest.mark.parametrize("name", ["3D_PEC", "3D_TFSF", "3D_TFSF_InteriorPEC"])
+@pytest.mark.parametrize("name", ["3D_PEC", "3D_TFSF", "3D_TFSF_InteriorPEC", "3D_Resonant_Box_TM55_H1_P3",
+                                  "3D_Resonant_Box_TM55_H0_P2_PERF"])
 def test_reference_cases_load(name):
     """The reference's own 3D case files load."""
     c = dg.Case(REFERENCE_INPUTS / name / f"{name}.json")
     m = c.mesh()
     assert m.n_elements > 0 and c.info["order"] >= 1
     dg.validate_mesh(m, order=1)
+
+
+@pytest.mark.parametrize("name,tets,order,final", [("3D_Resonant_Box_TM55_H1_P3", 2800, 3, 10.0),
+                                                   ("3D_Resonant_Box_TM55_H0_P2_PERF", 350, 2, 2.0)])
+def test_reference_tm55_cases(name, tets, order, final):
+    """The resonant-box inputs (the TM55 convergence study and the Performance set): the unit cube of
+    350 tetrahedra, one uniform refinement in H1, PEC walls, and the initial field Ez = sin(5 pi x)
+    sin(5 pi y) of the TM(5,5) cavity mode (the exact solution the reference's L2 error analysis
+    uses, test/cases/L2ErrorAnalysis.cpp:32-54) at every node, the other components zero."""
+    c = dg.Case(REFERENCE_INPUTS / name / f"{name}.json")
+    m = c.mesh()
+    assert m.n_elements == tets and c.info["order"] == order
+    assert c.info["time_step"] == 1e-4 and c.info["final_time"] == final and c.info["alpha"] == 1.0
+    V = np.asarray(m.vertices)
+    assert np.allclose(V.min(0), 0.0) and np.allclose(V.max(0), 1.0)
+    assert set(np.unique(m.bdr_codes).tolist()) == {dg.BC_PEC}
+    from oracle import pyoracle as po
+    orc = po.Oracle.from_mesh(m, order)
+    X = orc.nodes()
+    N = X.shape[1]
+    x0 = c.initial_state(X)
+    ez = np.sin(5 * np.pi * X[0]) * np.sin(5 * np.pi * X[1])
+    assert np.abs(x0[2 * N:3 * N] - ez).max() <= 1e-14
+    assert np.count_nonzero(x0[:2 * N]) == 0 and np.count_nonzero(x0[3 * N:]) == 0
 
 
 def _second_order_copy(src: Path, dst: Path, bump: float = 0.0) -> None:
@@ -363,14 +388,15 @@ def test_solver_option_names_follow_the_reference(tmp_path):
         dg.Case(_case_copy(tmp_path, "box_resonant", "evo_bad", evo("spectral")))
 
 
-def test_basis_type_other_than_gauss_lobatto_refused(tmp_path):
-    """The reference's basis_type is MFEM's BasisType number; the operator here is built on the
-    Gauss-Lobatto node set (1) only, so e.g. Gauss-Legendre (0) is refused, not ignored."""
+def test_basis_types(tmp_path):
+    """The reference's basis_type is MFEM's BasisType number: Gauss-Lobatto (1) and Gauss-Legendre
+    (0) load (the case info keeps which), others (e.g. 2, positive) are refused, not ignored."""
     def bt(n):
         return lambda c: c.setdefault("solver_options", {}).__setitem__("basis_type", n)
-    dg.Case(_case_copy(tmp_path, "box_resonant", "bt1", bt(1)))
-    with pytest.raises(dg.DgtdError, match="basis_type 0 is not supported"):
-        dg.Case(_case_copy(tmp_path, "box_resonant", "bt0", bt(0)))
+    assert dg.Case(_case_copy(tmp_path, "box_resonant", "bt1", bt(1))).info["basis_type"] == 1
+    assert dg.Case(_case_copy(tmp_path, "box_resonant", "bt0", bt(0))).info["basis_type"] == 0
+    with pytest.raises(dg.DgtdError, match="basis_type 2 is not supported"):
+        dg.Case(_case_copy(tmp_path, "box_resonant", "bt2", bt(2)))
 
 
 def test_point_probe_file_format(tmp_path):

@@ -236,15 +236,25 @@ int dgtd_case_run(const dgtd_case* cs, const dgtd_case_run_opts* ro, double* h_s
         const int Np = info.np;
         std::vector<double> to_lobatto, to_legendre;
         if (legendre) {
+            // the element's corners as the operator holds them: its Gauss-Lobatto nodes at the
+            // vertices (barycentric unit vectors), so both node sets share its vertex order
+            const std::vector<double> bl = dgtd::tet_node_bary(c.order, dgtd::kBasisGaussLobatto);
+            int corner[4] = {-1, -1, -1, -1};
+            for (int n = 0; n < Np; ++n)
+                for (int v = 0; v < 4; ++v)
+                    if (bl[4 * n + v] == 1.0) corner[v] = n;
+            for (int v = 0; v < 4; ++v)
+                if (corner[v] < 0) throw std::runtime_error("Gauss-Lobatto node set without a vertex node");
             const std::vector<double> b = dgtd::tet_node_bary(c.order, dgtd::kBasisGaussLegendre);
+            std::vector<double> gl(3 * static_cast<size_t>(N));
             for (int64_t e = 0; e < K; ++e)
                 for (int n = 0; n < Np; ++n)
                     for (int r = 0; r < 3; ++r) {
                         double x = 0.0;
-                        for (int v = 0; v < 4; ++v)
-                            x += b[4 * n + v] * c.vertices[3 * static_cast<size_t>(c.elements[4 * e + v]) + r];
-                        xyz[r * N + e * Np + n] = x;
+                        for (int v = 0; v < 4; ++v) x += b[4 * n + v] * xyz[r * N + e * Np + corner[v]];
+                        gl[r * N + e * Np + n] = x;
                     }
+            xyz.swap(gl);
             to_lobatto = dgtd::tet_basis_change(c.order, dgtd::kBasisGaussLegendre, dgtd::kBasisGaussLobatto);
             to_legendre = dgtd::tet_basis_change(c.order, dgtd::kBasisGaussLobatto, dgtd::kBasisGaussLegendre);
         }

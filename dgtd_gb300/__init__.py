@@ -150,6 +150,7 @@ SIGNATURES = {
     "dgtd_op_node_coords": (C.c_int, [_P, _D]),
     "dgtd_op_set_planewaves": (C.c_int, [_P, C.POINTER(PlaneWave), C.c_int32]),
     "dgtd_op_mult": (C.c_int, [_P, _P, _P, C.c_double, _P]),
+    "dgtd_op_change_basis": (C.c_int, [_P, _P, _P, C.c_int32, C.c_int32, _P]),
     "dgtd_op_mult_host": (C.c_int, [_P, _D, _D, C.c_double]),
     "dgtd_op_pack": (C.c_int, [_P, _P, _P, _P]),
     "dgtd_op_unpack": (C.c_int, [_P, _P, _P, _P]),
@@ -568,6 +569,12 @@ class Operator:
     # -- device API (torch tensors or raw device addresses)
     def mult(self, x, y, t: float = 0.0, stream=None) -> None:
         _check(lib().dgtd_op_mult(self._h, _ptr(x), _ptr(y), float(t), _stream(stream)), "dgtd_op_mult")
+
+    def change_basis(self, x, y, from_basis: int, to_basis: int, stream=None) -> None:
+        """FP64 form: y = the state x moved between nodal bases (BASIS_GAUSS_LEGENDRE,
+        BASIS_GAUSS_LOBATTO) element by element on the device; x and y distinct."""
+        _check(lib().dgtd_op_change_basis(self._h, _ptr(x), _ptr(y), int(from_basis), int(to_basis),
+                                          _stream(stream)), "dgtd_op_change_basis")
 
     def step(self, state, t0: float, dt: float, nsteps: int, integrator: int = RK4, stream=None) -> None:
         _check(lib().dgtd_op_step(self._h, _ptr(state), float(t0), float(dt), int(nsteps), int(integrator),

@@ -107,6 +107,9 @@ struct dgtd_op {
     // RK scratch (allocated on first dgtd_op_step)
     double* ws = nullptr;
     int64_t ws_len = 0;
+    // change of nodal basis (dgtd_op_change_basis): [2][Np][Np], Gauss-Legendre -> Gauss-Lobatto
+    // then back; allocated on first use, freed with `allocs`
+    double* basis_dev = nullptr;
     // single-instance FP32 form: FP32 copies of the tables, RK scratch
     dgtd::TablesF32 dev32{};
     float* ws32 = nullptr;
@@ -708,6 +711,71 @@ int dgtd_op_set_planewaves(dgtd_op* op, const dgtd_planewave* pw, int32_t n)
         ensure_sources(op);
         if (op->batched) op->batched->set_sources(op->pw_host);
         defect_restart(op);
+    } catch (const std::exception& e) {
+        return fail(DGTD_ERR_CUDA, e.what());
+    }
+    return DGTD_OK;
+}
+
+namespace {
+
+// out = M in on every block of Np nodal values of the reference-layout state (incidence,
+// component, element): a thread per output value, M and the block read through the read-only
+// cache; a grid-stride loop over the n = state_len values
+__global__ void basis_change_kernel(const double* __restrict__ M, int Np, int64_t n,
+                                    const double* __restrict__ in, double* __restrict__ out)
+{
+    for (int64_t g = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; g < n;
+         g += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const int64_t blk = g / Np;
+        const int i = static_cast<int>(g - blk * Np);
+        const double* x = in + blk * Np;
+        const double* m = M + static_cast<int64_t>(i) * Np;
+        double a = 0.0;
+        for (int j = 0; j < Np; ++j) a = fma(__ldg(m + j), __ldg(x + j), a);
+        out[g] = a;
+    }
+}
+
+}  // namespace
+
+int dgtd_op_change_basis(dgtd_op* op, const void* d_in, void* d_out, int32_t from_basis, int32_t to_basis,
+                         void* stream)
+{
+    if (!op || !d_in || !d_out) return fail(DGTD_ERR_INVALID, "NULL argument");
+    if (d_in == d_out) return fail(DGTD_ERR_INVALID, "in and out must not alias");
+    if ((from_basis != DGTD_BASIS_GAUSS_LEGENDRE && from_basis != DGTD_BASIS_GAUSS_LOBATTO) ||
+        (to_basis != DGTD_BASIS_GAUSS_LEGENDRE && to_basis != DGTD_BASIS_GAUSS_LOBATTO))
+        return fail(DGTD_ERR_INVALID, "basis types are 0 (Gauss-Legendre) and 1 (Gauss-Lobatto)");
+    if (op->batched || op->precision != DGTD_FP64)
+        return fail(DGTD_ERR_UNSUPPORTED, "the change of basis works on the FP64 form's reference-layout state");
+    try {
+        const cudaStream_t st = static_cast<cudaStream_t>(stream);
+        const int Np = op->ref.Np;
+        const int64_t n = op->state_len;
+        if (from_basis == to_basis) {
+            ck(cudaMemcpyAsync(d_out, d_in, static_cast<size_t>(n) * sizeof(double), cudaMemcpyDeviceToDevice, st),
+               "basis copy");
+            return DGTD_OK;
+        }
+        if (!op->basis_dev) {
+            std::vector<double> h = dgtd::tet_basis_change(op->ref.p, dgtd::kBasisGaussLegendre, dgtd::kBasisGaussLobatto);
+            const std::vector<double> back =
+                dgtd::tet_basis_change(op->ref.p, dgtd::kBasisGaussLobatto, dgtd::kBasisGaussLegendre);
+            h.insert(h.end(), back.begin(), back.end());
+            double* d = nullptr;
+            ck(cudaMalloc(&d, h.size() * sizeof(double)), "cudaMalloc basis matrices");
+            op->allocs.push_back(d);
+            ck(cudaMemcpy(d, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice), "upload basis matrices");
+            op->basis_dev = d;
+        }
+        const double* M = op->basis_dev + (from_basis == DGTD_BASIS_GAUSS_LEGENDRE ? 0 : static_cast<int64_t>(Np) * Np);
+        const int threads = 256;
+        const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>((n + threads - 1) / threads, 8 * op->n_sm));
+        basis_change_kernel<<<static_cast<unsigned>(blocks), threads, 0, st>>>(
+            M, Np, n, static_cast<const double*>(d_in), static_cast<double*>(d_out));
+        ck(cudaGetLastError(), "basis change kernel");
+        g_launches.fetch_add(1, std::memory_order_relaxed);
     } catch (const std::exception& e) {
         return fail(DGTD_ERR_CUDA, e.what());
     }

@@ -379,6 +379,11 @@ int dgtd_op_sgbc_states(const dgtd_op* op, int64_t* n_pairs, int64_t* state_len,
 int dgtd_tet_nodes(int32_t order, int32_t basis_type, double* bary);
 /* [Np][Np] row-major M with v_to = M v_from for the nodal values of any degree-p polynomial. */
 int dgtd_tet_basis_change(int32_t order, int32_t from_basis, int32_t to_basis, double* m);
+/* The same change applied on the device to a whole FP64 reference-layout state (state_len
+ * values; d_in and d_out distinct): a Gauss-Legendre caller runs
+ * change(GL -> GLL), dgtd_op_mult / dgtd_op_step, change(GLL -> GL). One kernel launch. */
+int dgtd_op_change_basis(dgtd_op* op, const void* d_in, void* d_out, int32_t from_basis, int32_t to_basis,
+                         void* stream);
 
 /* Host-side rows of the curved elements of a mesh (no GPU): elems [n_curved], nbr [n_curved][4]
  * (face neighbour or -1) and blocks [n_curved][5][6 Np][6 Np] (row-major; rows (component, node)

@@ -56,3 +56,30 @@ def test_bleg_performance_case_runs(torch_cuda, tmp_path):
     """The whole BLEG input (20,000 steps to t = 2) runs stable to its end."""
     state, res = dg.Case(REF / BLEG / f"{BLEG}.json").run(out_dir=tmp_path)
     assert res["steps"] == 20000 and res["unstable_step"] == -1 and np.all(np.isfinite(state))
+
+
+@pytest.mark.parametrize("p", [2, 3])
+def test_op_change_basis_and_legendre_mult(torch_cuda, p):
+    """dgtd_op_change_basis on the device equals the host matrix applied per element block, and
+    change(GL -> GLL), Mult, change(GLL -> GL) equals the oracle's operator assembled on the
+    Gauss-Legendre nodes (1e-12)."""
+    torch = torch_cuda
+    m = po.box_mesh((2, 2, 2), outer_bc=po.BC_SMA)
+    mesh = dg.Mesh(m.vertices, m.elements, m.bdr_faces, m.bdr_codes)
+    op = dg.Operator(mesh, order=p, alpha=1.0)
+    x = np.random.default_rng(p).standard_normal(op.state_len)
+    xd = torch.from_numpy(x).cuda()
+    yd, zd, wd = torch.empty_like(xd), torch.empty_like(xd), torch.empty_like(xd)
+    op.change_basis(xd, yd, dg.BASIS_GAUSS_LEGENDRE, dg.BASIS_GAUSS_LOBATTO)
+    torch.cuda.synchronize()
+    M = dg.tet_basis_change(p, 0, 1)
+    host = (x.reshape(-1, M.shape[0]) @ M.T).reshape(-1)
+    assert np.abs(yd.cpu().numpy() - host).max() <= 1e-13 * np.abs(host).max()
+    op.mult(yd, zd, 0.0)
+    op.change_basis(zd, wd, dg.BASIS_GAUSS_LOBATTO, dg.BASIS_GAUSS_LEGENDRE)
+    torch.cuda.synchronize()
+    gl = po.Oracle(m.vertices, m.elements, p, 1.0, 3, m.bdr_faces, m.bdr_codes)
+    gl.set_basis(0)
+    assert rel_l2(wd.cpu().numpy(), gl.mult(x)) <= 1e-12
+    with pytest.raises(dg.DgtdError, match="alias"):
+        op.change_basis(xd, xd, 0, 1)

@@ -14,9 +14,9 @@ def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
 
 
-# Modules whose GPU paths are the newest (thin layers, curved elements) run after the others, so
-# that with -x a failure there does not keep the rest of the suite from running.
-RUN_LAST = ("test_gpu_sgbc.py", "test_gpu_curved.py")
+# Modules whose GPU paths are the newest (change of basis, thin layers, curved elements) run after
+# the others, so that with -x a failure there does not keep the rest of the suite from running.
+RUN_LAST = ("test_gpu_basis.py", "test_gpu_sgbc.py", "test_gpu_curved.py")
 
 
 def pytest_collection_modifyitems(session, config, items):

@@ -455,3 +455,21 @@ def test_automatic_time_step_follows_the_reference(tmp_path):
         fmax = max(fmax, float(np.max(2.0 / 3.0 * area / vol)))
     he = dg.Case(_case_copy(tmp_path, "box_tfsf", "dt_hesthaven", opts("hesthaven"))).auto_dt()
     assert abs(he - 0.7 / (fmax * p * p)) <= 1e-12 * he
+
+
+def test_oracle_tm55_mode_one_period():
+    """The oracle on the reference's TM55 box (H1: 2,800 tetrahedra) at order 2 follows the exact
+    TM(5,5) mode (test/cases/L2ErrorAnalysis.cpp:32-54) over one period of 200 steps to 0.214
+    relative L2 in Ez: the figure the GPU test holds the product to."""
+    from oracle import pyoracle as po
+    name = "3D_Resonant_Box_TM55_H1_P3"
+    c = dg.Case(REFERENCE_INPUTS / name / f"{name}.json")
+    orc = po.Oracle.from_mesh(c.mesh(), 2, alpha=c.info["alpha"])
+    X = orc.nodes()
+    N = X.shape[1]
+    w = 5 * np.pi * np.sqrt(2.0)
+    period = 2 * np.pi / w
+    x, n = orc.run(c.initial_state(X), 0.0, period / 200, period)
+    ez = np.sin(5 * np.pi * X[0]) * np.sin(5 * np.pi * X[1])
+    err = np.linalg.norm(x[2 * N:3 * N] - ez * np.cos(w * period)) / np.linalg.norm(ez)
+    assert n == 200 and 0.20 <= err <= 0.22

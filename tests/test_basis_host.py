@@ -115,3 +115,19 @@ def test_legendre_case_refusals(tmp_path, case, extra, match):
     shutil.copyfile(src / f"{case}.msh", d / f"{case}.msh")
     with pytest.raises(dg.DgtdError, match=match):
         dg.Case(d / f"{case}.json")
+
+
+def test_bleg_run_through_change_of_basis_is_the_legendre_run():
+    """What the case runner does for the reference's BLEG input, restated on the oracle: the
+    Gauss-Lobatto system started from M(GL -> GLL) x0 and mapped back after 500 RK4 steps (dt 1e-4)
+    equals the Gauss-Legendre system run directly, to rounding (1e-13 relative L2)."""
+    c = dg.Case(REF / BLEG / f"{BLEG}.json")
+    m = c.mesh()
+    gl = po.Oracle.from_mesh(m, 2, alpha=c.info["alpha"])
+    gl.set_basis(0)
+    x0 = c.initial_state(gl.nodes())
+    xo, no = gl.run(x0, 0.0, c.info["time_step"], 0.05)
+    gll = po.Oracle.from_mesh(m, 2, alpha=c.info["alpha"])
+    x1, n1 = gll.run(_blocks(x0, dg.tet_basis_change(2, 0, 1)), 0.0, c.info["time_step"], 0.05)
+    assert no == n1 == 500 and np.linalg.norm(xo) > 1.0
+    assert rel_l2(_blocks(x1, dg.tet_basis_change(2, 1, 0)), xo) <= 1e-13
